@@ -1,0 +1,994 @@
+// engine.cu -- the C ABI (include/ermod_gpu.h): context life cycle, uploads, the
+// per-frame preparation and the batched placement loop that replaces engconst's
+// `do cntdst` (engproc.F90:388-392).
+//
+// Per batch of B placements the stream carries:
+//   place_prep -> [mixed] spectrum -> cuFFT C2R (batched)      -> mol_energy -> accumulate
+//              -> [fp64]  spread64 -> D2Z -> influence64 -> Z2D -> mol_energy -> accumulate
+// and every `ring_cap` placements (reference-solvent mode) the ecorr flush.
+// Status is reported once per call (host API) or per ermod_sync (device API).
+#include <cufft.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "engine.cuh"
+
+namespace ermod {
+
+const char* const kPhaseNames[PH_COUNT] = {"frame", "place_prep", "spectrum", "fft_c2r", "mol_energy",
+                                           "accumulate", "ecorr", "copy"};
+
+namespace {
+thread_local std::string g_err;
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  return cudaMalloc((void**)p, sizeof(T) * n);
+}
+template <typename T>
+void dfree(T*& p) {
+  if (p) cudaFree((void*)p);
+  p = nullptr;
+}
+}  // namespace
+
+void set_error_string(const std::string& s) { g_err = s; }
+
+int fail_cuda(cudaError_t e, const char* where) {
+  g_err = std::string(where) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? ERMOD_E_NOMEM : ERMOD_E_CUDA;
+}
+
+static int fail_fft(cufftResult r, const char* where) {
+  g_err = std::string(where) + ": cuFFT error " + std::to_string((int)r);
+  return ERMOD_E_CUFFT;
+}
+
+static int fail_param(const char* what) {
+  g_err = what;
+  return ERMOD_E_PARAM;
+}
+
+void Engine::phase_begin(int ph) {
+  if (!timing) return;
+  cudaEvent_t ev;
+  if (!ev_pool.empty()) {
+    ev = ev_pool.back();
+    ev_pool.pop_back();
+  } else {
+    cudaEventCreate(&ev);
+  }
+  cudaEventRecord(ev, stream);
+  cur_phase = ph;
+  cur_ev = ev;
+}
+
+void Engine::phase_end() {
+  if (!timing || cur_phase < 0) return;
+  cudaEvent_t ev;
+  if (!ev_pool.empty()) {
+    ev = ev_pool.back();
+    ev_pool.pop_back();
+  } else {
+    cudaEventCreate(&ev);
+  }
+  cudaEventRecord(ev, stream);
+  pending.push_back(Pending{cur_ev, ev, cur_phase});
+  cur_phase = -1;
+  if (pending.size() > 8192) {  // harvest to bound the pool
+    cudaEventSynchronize(ev);
+    for (auto& p : pending) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, p.a, p.b);
+      phase_ms[p.phase] += ms;
+      ev_pool.push_back(p.a);
+      ev_pool.push_back(p.b);
+    }
+    pending.clear();
+  }
+}
+
+static void harvest(Engine& e) {
+  if (e.pending.empty()) return;
+  cudaEventSynchronize(e.pending.back().b);
+  for (auto& p : e.pending) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p.a, p.b);
+    e.phase_ms[p.phase] += ms;
+    e.ev_pool.push_back(p.a);
+    e.ev_pool.push_back(p.b);
+  }
+  e.pending.clear();
+}
+
+}  // namespace ermod
+
+using namespace ermod;
+
+struct ermod_ctx {
+  Engine e;
+};
+
+// ---------------------------------------------------------------------------------
+static int free_batch(Engine& e) {
+  BatchArgs& b = e.buf;
+  dfree(b.u_nsite);
+  dfree(b.u_x);
+  dfree(b.u_pos);
+  dfree(b.u_q);
+  dfree(b.u_grid);
+  dfree(b.u_w);
+  dfree(b.u_bvec);
+  dfree(b.u_qmol);
+  dfree(b.u_usreal);
+  dfree(b.u_radius);
+  dfree(b.spec);
+  dfree(b.phi);
+  dfree(b.spec64);
+  dfree(b.phi64);
+  dfree(b.self_part);
+  dfree(b.part);
+  dfree(b.engnmfc);
+  dfree(e.d_ring_hist);
+  dfree(e.d_ring_w);
+  dfree(e.d_ring_nz);
+  dfree(e.d_ring_nnz);
+  dfree(e.d_ring_valid);
+  e.buf = BatchArgs{};
+  return ERMOD_OK;
+}
+
+static int free_frame(Engine& e) {
+  dfree(e.d_sitepos);
+  dfree(e.d_wrapped);
+  dfree(e.d_sort_key);
+  dfree(e.d_sort_key_alt);
+  dfree(e.d_sort_val);
+  dfree(e.d_sort_val_alt);
+  dfree(e.d_cub_tmp);
+  dfree(e.d_slot_mol);
+  dfree(e.d_slot_site);
+  dfree(e.d_slot_species);
+  dfree(e.d_slot_qmol);
+  dfree(e.d_site_pos);
+  dfree(e.d_site_rec);
+  dfree(e.d_site_grid);
+  dfree(e.d_site_x);
+  dfree(e.d_site_w);
+  dfree(e.d_site_q);
+  dfree(e.d_frame_scal);
+  return ERMOD_OK;
+}
+
+static int free_topology(Engine& e) {
+  dfree(e.d_charge);
+  dfree(e.d_ljtype);
+  dfree(e.d_ljene);
+  dfree(e.d_ljlensq);
+  dfree(e.d_mol_atom0);
+  dfree(e.d_mol_nsite);
+  dfree(e.d_mol_species);
+  dfree(e.d_mol_qmol);
+  dfree(e.d_mbi0);
+  dfree(e.d_qmol_all);
+  dfree(e.d_mol_to_k);
+  return ERMOD_OK;
+}
+
+static int free_bins(Engine& e) {
+  dfree(e.d_uvkey);
+  dfree(e.d_eskey);
+  dfree(e.d_spec);
+  dfree(e.d_edens);
+  dfree(e.d_ecorr);
+  dfree(e.d_ecorr_n);
+  dfree(e.d_eself);
+  dfree(e.d_slnuv);
+  dfree(e.d_minuv);
+  dfree(e.d_maxuv);
+  dfree(e.d_scal);
+  return ERMOD_OK;
+}
+
+// batch buffers: need topology (slvmax), bins (ermax, numslv) and the PME grid
+static int ensure_batch(Engine& e) {
+  if (e.buf.u_nsite) return ERMOD_OK;
+  const int S = kMaxSoluteSites;
+  const int B = e.Bmax;
+  BatchArgs& b = e.buf;
+  const size_t nr = e.grid_real(), nc = e.grid_cplx();
+  e.ntile = (e.slvmax + e.tile - 1) / e.tile;
+  ERMOD_CUDA(dalloc(&b.u_nsite, B));
+  ERMOD_CUDA(dalloc(&b.u_x, (size_t)B * S * 3));
+  ERMOD_CUDA(dalloc(&b.u_pos, (size_t)B * S));
+  ERMOD_CUDA(dalloc(&b.u_q, (size_t)B * S));
+  ERMOD_CUDA(dalloc(&b.u_grid, (size_t)B * S));
+  ERMOD_CUDA(dalloc(&b.u_w, (size_t)B * S * 3 * kMaxSplineOrder));
+  ERMOD_CUDA(dalloc(&b.u_qmol, B));
+  ERMOD_CUDA(dalloc(&b.u_usreal, B));
+  ERMOD_CUDA(dalloc(&b.u_radius, B));
+  ERMOD_CUDA(dalloc(&b.engnmfc, B));
+  if (e.mixed) {
+    ERMOD_CUDA(dalloc(&b.u_bvec, (size_t)B * S * 3 * e.Kmax()));
+    ERMOD_CUDA(dalloc(&b.spec, nc * B));
+    ERMOD_CUDA(dalloc(&b.phi, nr * B));
+    const int kc = spectrum_chunk(e.H());
+    ERMOD_CUDA(dalloc(&b.self_part, (size_t)B * e.geom.K[2] * ((e.geom.K[1] + kc - 1) / kc)));
+  } else {
+    ERMOD_CUDA(dalloc(&b.spec64, nc * B));
+    ERMOD_CUDA(dalloc(&b.phi64, nr * B));
+    ERMOD_CUDA(dalloc(&b.self_part, (size_t)B * influence64_blocks()));
+  }
+  ERMOD_CUDA(dalloc(&b.part, (size_t)B * e.ntile * e.numslv * 3));
+  e.ring_cap = e.P.corrcal ? std::max(B, (512 / B) * B) : B;
+  e.ring_fill = 0;
+  ERMOD_CUDA(dalloc(&e.d_ring_hist, (size_t)e.ring_cap * e.ermax));
+  ERMOD_CUDA(dalloc(&e.d_ring_w, e.ring_cap));
+  ERMOD_CUDA(dalloc(&e.d_ring_nnz, e.ring_cap));
+  ERMOD_CUDA(dalloc(&e.d_ring_valid, e.ring_cap));
+  if (e.P.corrcal) ERMOD_CUDA(dalloc(&e.d_ring_nz, (size_t)2 * e.ring_cap * e.ermax));
+  // FFT plans
+  if (!e.plans_ready) {
+    int n[3] = {e.geom.K[2], e.geom.K[1], e.geom.K[0]};
+    cufftResult r;
+    if (e.mixed) {
+      r = cufftPlanMany(&e.plan_c2r, 3, n, nullptr, 1, (int)nc, nullptr, 1, (int)nr, CUFFT_C2R, B);
+      if (r != CUFFT_SUCCESS) return fail_fft(r, "cufftPlanMany(C2R)");
+      cufftSetStream(e.plan_c2r, e.stream);
+    } else {
+      r = cufftPlanMany(&e.plan_d2z, 3, n, nullptr, 1, (int)nr, nullptr, 1, (int)nc, CUFFT_D2Z, B);
+      if (r != CUFFT_SUCCESS) return fail_fft(r, "cufftPlanMany(D2Z)");
+      r = cufftPlanMany(&e.plan_z2d, 3, n, nullptr, 1, (int)nc, nullptr, 1, (int)nr, CUFFT_Z2D, B);
+      if (r != CUFFT_SUCCESS) return fail_fft(r, "cufftPlanMany(Z2D)");
+      cufftSetStream(e.plan_d2z, e.stream);
+      cufftSetStream(e.plan_z2d, e.stream);
+    }
+    e.plans_ready = true;
+  }
+  return ERMOD_OK;
+}
+
+// ---------------------------------------------------------------------------------
+extern "C" {
+
+const char* ermod_last_error_string(void) { return g_err.c_str(); }
+
+const char* ermod_status_string(int s) {
+  switch (s) {
+    case ERMOD_OK: return "ok";
+    case ERMOD_E_ENG_MIN: return "eng_min: the minimum of the energy coordinate is too large";
+    case ERMOD_E_ENG_SFT: return "eng_sft: energy beyond the soft region in the solution system";
+    case ERMOD_E_ENG_BUG: return "eng_bug";
+    case ERMOD_E_ENG_CNS: return "eng_cns: inconsistency in the species assignment";
+    case ERMOD_E_RCP_CNS: return "rcp_cns: inconsistency in the reciprocal-space set-up";
+    case ERMOD_E_RCP_FST: return "rcp_fst: the solute must not be a solvent";
+    case ERMOD_W_MBIN: return "mbin: the maximum binning energy is too low for this species";
+    case ERMOD_E_PARAM: return "invalid argument";
+    case ERMOD_E_NONCUBOID: return "a non-cuboidal cell is not supported";
+    case ERMOD_E_UNSUPPORTED: return "unsupported mode";
+    case ERMOD_E_CUDA: return "CUDA error";
+    case ERMOD_E_CUFFT: return "cuFFT error";
+    case ERMOD_E_NOMEM: return "device allocation failed";
+    case ERMOD_E_DEVICE: return "device-side check failed";
+    default: return "unknown status";
+  }
+}
+
+void ermod_default_params(ermod_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->abi_version = ERMOD_ABI_VERSION;
+  p->slttype = 1;
+  p->estype = 2;
+  p->cltype = 2;
+  p->ljswitch = 0;
+  p->splodr = 4;
+  p->ms1max = p->ms2max = p->ms3max = 64;
+  p->wgtslf = 0;
+  p->corrcal = 0;
+  p->selfcal = 0;
+  p->force_calculation = 0;
+  p->precision = ERMOD_PRECISION_MIXED;
+  p->batch = 0;
+  p->count_mirror = 0;
+  p->elecut = 12.0;
+  p->upljcut = 12.0;
+  p->lwljcut = 10.0;
+  p->screen = 0.0;
+  p->temp = 300.0 * 8.314510e-3 / 4.184;
+  p->block_threshold = 4.0;
+}
+
+int ermod_create(const ermod_params* p, int device, ermod_ctx** out) {
+  if (!p || !out) return fail_param("null argument");
+  *out = nullptr;
+  if (p->abi_version != ERMOD_ABI_VERSION) return fail_param("abi_version mismatch");
+  if (p->cltype != 2) {
+    g_err = "only cltype = 2 (PME) is implemented on the GPU";
+    return ERMOD_E_UNSUPPORTED;
+  }
+  if (p->slttype < 1 || p->slttype > 3) return fail_param("slttype must be 1, 2 or 3");
+  if (p->ljswitch < 0 || p->ljswitch > 3) return fail_param("ljswitch must be 0..3");
+  if (p->splodr != 4 && p->splodr != 6 && p->splodr != 8) {
+    g_err = "splodr must be 4, 6 or 8 on the GPU";
+    return ERMOD_E_UNSUPPORTED;
+  }
+  const int K[3] = {p->ms1max, p->ms2max, p->ms3max};
+  for (int i = 0; i < 3; ++i)
+    if (K[i] < p->splodr || K[i] > 1000) return fail_param("PME grid sizes must lie in [splodr, 1000]");
+  if (p->precision == ERMOD_PRECISION_MIXED && K[0] / 2 + 1 > 128)
+    return fail_param("mixed precision needs ms1max <= 254");
+  if (!(p->screen > 0) || !(p->temp > 0) || !(p->elecut > 0) || !(p->upljcut > 0) || !(p->lwljcut >= 0) ||
+      p->lwljcut >= p->upljcut)
+    return fail_param("screen, temp and cutoffs must be positive with lwljcut < upljcut");
+  if (p->precision != ERMOD_PRECISION_FP64 && p->precision != ERMOD_PRECISION_MIXED)
+    return fail_param("precision must be ERMOD_PRECISION_FP64 or ERMOD_PRECISION_MIXED");
+  if (p->batch < 0 || p->batch > accumulate_max_batch()) return fail_param("batch out of range");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    g_err = "no CUDA device";
+    return ERMOD_E_CUDA;
+  }
+  if (device < 0 || device >= ndev) return fail_param("device out of range");
+  ERMOD_CUDA(cudaSetDevice(device));
+  auto* c = new ermod_ctx();
+  Engine& e = c->e;
+  e.P = *p;
+  e.device = device;
+  e.mixed = p->precision == ERMOD_PRECISION_MIXED;
+  e.P_order = p->splodr;
+  e.geom.K[0] = K[0];
+  e.geom.K[1] = K[1];
+  e.geom.K[2] = K[2];
+  e.Bmax = e.mixed ? (p->batch > 0 ? p->batch : 32) : 1;
+  e.G = e.mixed ? std::min(8, e.Bmax) : 1;
+  cudaError_t err = cudaStreamCreateWithFlags(&e.stream, cudaStreamNonBlocking);
+  if (err != cudaSuccess) {
+    delete c;
+    return fail_cuda(err, "cudaStreamCreate");
+  }
+  e.own_stream = true;
+  if ((err = dalloc(&e.d_status, 1)) != cudaSuccess || (err = cudaMallocHost(&e.h_status, sizeof(DevStatus))) != cudaSuccess) {
+    ermod_destroy(c);
+    return fail_cuda(err, "status allocation");
+  }
+  DevStatus s0{kNoError, 0, 0};
+  cudaMemcpy(e.d_status, &s0, sizeof(s0), cudaMemcpyHostToDevice);
+  *e.h_status = s0;
+  // splfc tables (init_spline_axis, recpcal.F90:87-109) and FFT twiddles
+  std::vector<double> splfc;
+  std::vector<float2> tw;
+  for (int ax = 0; ax < 3; ++ax) {
+    for (int rci = 0; rci < K[ax]; ++rci) {
+      double re = 0.0, im = 0.0;
+      for (int spi = 0; spi <= p->splodr - 2; ++spi) {
+        const double chr = host_spline_value(p->splodr, (double)(spi + 1));
+        const double rtp2 = 2.0 * kPi * (double)(spi * rci) / (double)K[ax];
+        re += chr * std::cos(rtp2);
+        im += chr * std::sin(rtp2);
+      }
+      splfc.push_back(re * re + im * im);
+      const double ang = 2.0 * kPi * (double)rci / (double)K[ax];
+      tw.push_back(make_float2((float)std::cos(ang), (float)(-std::sin(ang))));
+    }
+  }
+  if ((err = dalloc(&e.d_splfc, splfc.size())) != cudaSuccess || (err = dalloc(&e.d_twiddle, tw.size())) != cudaSuccess ||
+      (err = dalloc(&e.d_engfac, e.grid_cplx())) != cudaSuccess ||
+      (err = dalloc(&e.d_engfac_f, e.grid_cplx())) != cudaSuccess) {
+    ermod_destroy(c);
+    return fail_cuda(err, "PME tables");
+  }
+  cudaMemcpy(e.d_splfc, splfc.data(), sizeof(double) * splfc.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(e.d_twiddle, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice);
+  *out = c;
+  return ERMOD_OK;
+}
+
+int ermod_destroy(ermod_ctx* c) {
+  if (!c) return ERMOD_OK;
+  Engine& e = c->e;
+  cudaSetDevice(e.device);
+  if (e.stream) cudaStreamSynchronize(e.stream);
+  free_batch(e);
+  free_frame(e);
+  free_topology(e);
+  free_bins(e);
+  dfree(e.d_engfac);
+  dfree(e.d_engfac_f);
+  dfree(e.d_splfc);
+  dfree(e.d_twiddle);
+  dfree(e.d_status);
+  if (e.h_status) cudaFreeHost(e.h_status);
+  if (e.plan_c2r) cufftDestroy(e.plan_c2r);
+  if (e.plan_d2z) cufftDestroy(e.plan_d2z);
+  if (e.plan_z2d) cufftDestroy(e.plan_z2d);
+  harvest(e);
+  for (auto ev : e.ev_pool) cudaEventDestroy(ev);
+  if (e.own_stream && e.stream) cudaStreamDestroy(e.stream);
+  delete c;
+  return ERMOD_OK;
+}
+
+int ermod_set_stream(ermod_ctx* c, void* stream) {
+  if (!c) return fail_param("null context");
+  Engine& e = c->e;
+  cudaSetDevice(e.device);
+  if (e.stream) cudaStreamSynchronize(e.stream);
+  if (e.own_stream && e.stream) cudaStreamDestroy(e.stream);
+  e.stream = (cudaStream_t)stream;
+  e.own_stream = false;
+  if (e.plan_c2r) cufftSetStream(e.plan_c2r, e.stream);
+  if (e.plan_d2z) cufftSetStream(e.plan_d2z, e.stream);
+  if (e.plan_z2d) cufftSetStream(e.plan_z2d, e.stream);
+  return ERMOD_OK;
+}
+
+int ermod_set_topology(ermod_ctx* c, int nummol, int numatm, const int* mbi, const int* sluvid, const int* uvspec,
+                       const double* charge, const int* ljtype, int ljtype_max, const double* ljene,
+                       const double* ljlensq) {
+  if (!c || !mbi || !sluvid || !uvspec || !charge || !ljtype || !ljene || !ljlensq) return fail_param("null argument");
+  if (nummol <= 0 || numatm <= 0 || ljtype_max <= 0) return fail_param("sizes must be positive");
+  Engine& e = c->e;
+  cudaSetDevice(e.device);
+  cudaStreamSynchronize(e.stream);
+  if (mbi[0] != 1 || mbi[nummol] - 1 != numatm) return fail_param("mol_begin_index must run from 1 to numatm+1");
+  for (int i = 0; i < nummol; ++i) {
+    if (mbi[i + 1] <= mbi[i]) return fail_param("every molecule needs at least one site");
+    if (sluvid[i] < 0 || sluvid[i] > 3) return ERMOD_E_ENG_BUG;  // sanity_check_sluvid, engproc.F90:1023-1043
+  }
+  for (int a = 0; a < numatm; ++a)
+    if (ljtype[a] < 1 || ljtype[a] > ljtype_max) return fail_param("ljtype out of range");
+  // sanity_check_sluvid per slttype
+  bool any_solute = false, any_solvent = false;
+  for (int i = 0; i < nummol; ++i) {
+    any_solute |= sluvid[i] != 0;
+    any_solvent |= sluvid[i] == 0;
+    if (e.P.slttype == 1 && sluvid[i] >= 2) {
+      g_err = "eng_par: solution mode needs sluvid 0 or 1";
+      return ERMOD_E_PARAM;
+    }
+    if (e.P.slttype != 1 && sluvid[i] == 1) {
+      g_err = "eng_par: reference mode needs sluvid 0, 2 or 3";
+      return ERMOD_E_PARAM;
+    }
+  }
+  if (!any_solute || (e.P.slttype != 1 && !any_solvent)) {
+    g_err = "eng_par: solute and solvent must both exist";
+    return ERMOD_E_PARAM;
+  }
+  free_batch(e);
+  free_frame(e);
+  free_topology(e);
+  e.frame_ready = false;
+  e.topo_ready = false;
+  e.nummol = nummol;
+  e.numatm = numatm;
+  e.ljtype_max = ljtype_max;
+  e.mbi0.assign(nummol + 1, 0);
+  for (int i = 0; i <= nummol; ++i) e.mbi0[i] = mbi[i] - 1;
+  e.sluvid.assign(sluvid, sluvid + nummol);
+  e.uvspec.assign(uvspec, uvspec + nummol);
+  e.charge.assign(charge, charge + numatm);
+  e.ljtype0.resize(numatm);
+  for (int a = 0; a < numatm; ++a) e.ljtype0[a] = ljtype[a] - 1;
+  e.numsite.resize(nummol);
+  e.mol_charge.assign(nummol, 0.0);
+  e.tagpt.clear();
+  std::vector<int> mol_to_k(nummol, -1);
+  e.total_charge_phys = 0.0;
+  e.max_mol_sites = 0;
+  for (int i = 0; i < nummol; ++i) {
+    e.numsite[i] = e.mbi0[i + 1] - e.mbi0[i];
+    double s = 0.0;  // mol_charge (setconf.F90:832-834)
+    for (int a = e.mbi0[i]; a < e.mbi0[i + 1]; ++a) s += charge[a];
+    e.mol_charge[i] = s;
+    if (sluvid[i] == 0 || sluvid[i] == 1) {  // tagpt (engproc.F90:336-348)
+      mol_to_k[i] = (int)e.tagpt.size();
+      e.tagpt.push_back(i);
+      e.max_mol_sites = std::max(e.max_mol_sites, e.numsite[i]);
+    }
+  }
+  // volcorrect's charge sum in the reference's order (engproc.F90:880-881)
+  for (int i = 0; i < nummol; ++i)
+    if (sluvid[i] == 0 || sluvid[i] == 1) e.total_charge_phys += e.mol_charge[i];
+  e.slvmax = (int)e.tagpt.size();
+  if (e.slvmax == 0) return fail_param("no physical molecules");
+  std::vector<int> atom0(e.slvmax), nsite(e.slvmax), species(e.slvmax);
+  std::vector<double> qmol(e.slvmax);
+  e.nsite_phys = 0;
+  for (int k = 0; k < e.slvmax; ++k) {
+    const int i = e.tagpt[k];
+    atom0[k] = e.mbi0[i];
+    nsite[k] = e.numsite[i];
+    species[k] = uvspec[i];
+    qmol[k] = e.mol_charge[i];
+    e.nsite_phys += nsite[k];
+  }
+  std::vector<double> lje(ljene, ljene + (size_t)ljtype_max * ljtype_max);
+  std::vector<double> ljl(ljlensq, ljlensq + (size_t)ljtype_max * ljtype_max);
+  ERMOD_CUDA(dalloc(&e.d_charge, numatm));
+  ERMOD_CUDA(dalloc(&e.d_ljtype, numatm));
+  ERMOD_CUDA(dalloc(&e.d_ljene, lje.size()));
+  ERMOD_CUDA(dalloc(&e.d_ljlensq, ljl.size()));
+  ERMOD_CUDA(dalloc(&e.d_mol_atom0, e.slvmax));
+  ERMOD_CUDA(dalloc(&e.d_mol_nsite, e.slvmax));
+  ERMOD_CUDA(dalloc(&e.d_mol_species, e.slvmax));
+  ERMOD_CUDA(dalloc(&e.d_mol_qmol, e.slvmax));
+  ERMOD_CUDA(dalloc(&e.d_mbi0, nummol + 1));
+  ERMOD_CUDA(dalloc(&e.d_qmol_all, nummol));
+  ERMOD_CUDA(dalloc(&e.d_mol_to_k, nummol));
+  ERMOD_CUDA(cudaMemcpy(e.d_charge, charge, sizeof(double) * numatm, cudaMemcpyHostToDevice));
+  ERMOD_CUDA(cudaMemcpy(e.d_ljtype, e.ljtype0.data(), sizeof(int) * numatm, cudaMemcpyHostToDevice));
+  ERMOD_CUDA(cudaMemcpy(e.d_ljene, lje.data(), sizeof(double) * lje.size(), cudaMemcpyHostToDevice));
+  ERMOD_CUDA(cudaMemcpy(e.d_ljlensq, ljl.data(), sizeof(double) * ljl.size(), cudaMemcpyHostToDevice));
+  ERMOD_CUDA(cudaMemcpy(e.d_mol_atom0, atom0.data(), sizeof(int) * e.slvmax, cudaMemcpyHostToDevice));
+  ERMOD_CUDA(cudaMemcpy(e.d_mol_nsite, nsite.data(), sizeof(int) * e.slvmax, cudaMemcpyHostToDevice));
+  ERMOD_CUDA(cudaMemcpy(e.d_mol_species, species.data(), sizeof(int) * e.slvmax, cudaMemcpyHostToDevice));
+  ERMOD_CUDA(cudaMemcpy(e.d_mol_qmol, qmol.data(), sizeof(double) * e.slvmax, cudaMemcpyHostToDevice));
+  ERMOD_CUDA(cudaMemcpy(e.d_mbi0, e.mbi0.data(), sizeof(int) * (nummol + 1), cudaMemcpyHostToDevice));
+  ERMOD_CUDA(cudaMemcpy(e.d_qmol_all, e.mol_charge.data(), sizeof(double) * nummol, cudaMemcpyHostToDevice));
+  ERMOD_CUDA(cudaMemcpy(e.d_mol_to_k, mol_to_k.data(), sizeof(int) * nummol, cudaMemcpyHostToDevice));
+  // frame buffers
+  ERMOD_CUDA(dalloc(&e.d_sitepos, 3 * (size_t)numatm));
+  ERMOD_CUDA(dalloc(&e.d_wrapped, 3 * (size_t)numatm));
+  ERMOD_CUDA(dalloc(&e.d_sort_key, e.slvmax));
+  ERMOD_CUDA(dalloc(&e.d_sort_key_alt, e.slvmax));
+  ERMOD_CUDA(dalloc(&e.d_sort_val, e.slvmax));
+  ERMOD_CUDA(dalloc(&e.d_sort_val_alt, e.slvmax + 1));
+  ERMOD_CUDA(cudaMemset(e.d_sort_val_alt, 0, sizeof(int) * (e.slvmax + 1)));
+  e.cub_tmp_bytes = frame_cub_bytes(e.slvmax);
+  ERMOD_CUDA(dalloc((char**)&e.d_cub_tmp, e.cub_tmp_bytes));
+  ERMOD_CUDA(dalloc(&e.d_slot_mol, e.slvmax));
+  ERMOD_CUDA(dalloc(&e.d_slot_site, e.slvmax + 1));
+  ERMOD_CUDA(dalloc(&e.d_slot_species, e.slvmax));
+  ERMOD_CUDA(dalloc(&e.d_slot_qmol, e.slvmax));
+  ERMOD_CUDA(dalloc(&e.d_site_pos, e.nsite_phys));
+  ERMOD_CUDA(dalloc(&e.d_site_grid, e.nsite_phys));
+  if (e.mixed) {
+    ERMOD_CUDA(dalloc(&e.d_site_rec, e.nsite_phys));
+  } else {
+    ERMOD_CUDA(dalloc(&e.d_site_x, 3 * (size_t)e.nsite_phys));
+    ERMOD_CUDA(dalloc(&e.d_site_w, (size_t)e.nsite_phys * 3 * e.P_order));
+    ERMOD_CUDA(dalloc(&e.d_site_q, e.nsite_phys));
+  }
+  ERMOD_CUDA(dalloc(&e.d_frame_scal, 4));
+  e.green_valid = false;
+  e.topo_ready = true;
+  return ERMOD_OK;
+}
+
+int ermod_set_bins(ermod_ctx* c, int numslv, const int* uvmax, const int* uvsoft, const double* uvcrd, int esmax,
+                   const double* escrd) {
+  if (!c || !uvmax || !uvsoft || !uvcrd) return fail_param("null argument");
+  if (numslv <= 0 || numslv > kMaxSpecies) return fail_param("numslv out of range");
+  if (esmax < 0 || (esmax > 0 && !escrd)) return fail_param("escrd missing");
+  Engine& e = c->e;
+  cudaSetDevice(e.device);
+  cudaStreamSynchronize(e.stream);
+  int ermax = 0;
+  for (int s = 0; s < numslv; ++s) {
+    if (uvmax[s] <= 0 || uvsoft[s] < 0 || uvsoft[s] > uvmax[s]) return fail_param("uvmax/uvsoft inconsistent");
+    ermax += uvmax[s];
+  }
+  for (int i = 1; i < ermax; ++i) (void)uvcrd;
+  free_batch(e);
+  free_bins(e);
+  e.bins_ready = false;
+  e.numslv = numslv;
+  e.ermax = ermax;
+  e.esmax = esmax;
+  e.uvmax.assign(uvmax, uvmax + numslv);
+  e.uvsoft.assign(uvsoft, uvsoft + numslv);
+  e.uvoff.assign(numslv, 0);
+  std::vector<int> spec(3 * numslv);
+  int off = 0;
+  for (int s = 0; s < numslv; ++s) {
+    e.uvoff[s] = off;
+    spec[3 * s] = off;
+    spec[3 * s + 1] = uvmax[s];
+    spec[3 * s + 2] = uvsoft[s];
+    off += uvmax[s];
+  }
+  e.uvcrd.assign(uvcrd, uvcrd + ermax);
+  e.escrd.assign(escrd ? escrd : uvcrd, (escrd ? escrd : uvcrd) + esmax);
+  std::vector<long long> uk(ermax), ek(std::max(esmax, 1));
+  for (int i = 0; i < ermax; ++i) uk[i] = ordered_key(uvcrd[i]);
+  for (int i = 0; i < esmax; ++i) ek[i] = ordered_key(escrd[i]);
+  ERMOD_CUDA(dalloc(&e.d_uvkey, ermax));
+  ERMOD_CUDA(dalloc(&e.d_eskey, ek.size()));
+  ERMOD_CUDA(dalloc(&e.d_spec, spec.size()));
+  ERMOD_CUDA(cudaMemcpy(e.d_uvkey, uk.data(), sizeof(long long) * ermax, cudaMemcpyHostToDevice));
+  ERMOD_CUDA(cudaMemcpy(e.d_eskey, ek.data(), sizeof(long long) * ek.size(), cudaMemcpyHostToDevice));
+  ERMOD_CUDA(cudaMemcpy(e.d_spec, spec.data(), sizeof(int) * spec.size(), cudaMemcpyHostToDevice));
+  ERMOD_CUDA(dalloc(&e.d_edens, ermax));
+  if (e.P.corrcal) {
+    ERMOD_CUDA(dalloc(&e.d_ecorr, (size_t)ermax * ermax));
+    if (e.P.count_mirror) ERMOD_CUDA(dalloc(&e.d_ecorr_n, (size_t)ermax * ermax));
+  }
+  ERMOD_CUDA(dalloc(&e.d_eself, std::max(esmax, 1)));
+  ERMOD_CUDA(dalloc(&e.d_slnuv, numslv));
+  ERMOD_CUDA(dalloc(&e.d_minuv, numslv + 1));
+  ERMOD_CUDA(dalloc(&e.d_maxuv, numslv + 1));
+  ERMOD_CUDA(dalloc(&e.d_scal, 8));
+  // enginit's initial values (engproc.F90:255-260): minuv = infty, maxuv = -infty, voffset = -infty
+  std::vector<double> mn(numslv + 1, 1.0e50), mx(numslv + 1, -1.0e50);
+  ERMOD_CUDA(cudaMemcpy(e.d_minuv, mn.data(), sizeof(double) * (numslv + 1), cudaMemcpyHostToDevice));
+  ERMOD_CUDA(cudaMemcpy(e.d_maxuv, mx.data(), sizeof(double) * (numslv + 1), cudaMemcpyHostToDevice));
+  const double scal[8] = {0.0, 0.0, 0.0, -1.0e50, 0.0, 0.0, 0.0, 0.0};
+  ERMOD_CUDA(cudaMemcpy(e.d_scal, scal, sizeof(scal), cudaMemcpyHostToDevice));
+  if (e.P.corrcal) {
+    ERMOD_CUDA(cudaMemset(e.d_ecorr, 0, sizeof(double) * (size_t)ermax * ermax));
+    if (e.d_ecorr_n) ERMOD_CUDA(cudaMemset(e.d_ecorr_n, 0, sizeof(long long) * (size_t)ermax * ermax));
+  }
+  ERMOD_CUDA(cudaMemset(e.d_edens, 0, sizeof(double) * ermax));
+  ERMOD_CUDA(cudaMemset(e.d_eself, 0, sizeof(double) * std::max(esmax, 1)));
+  ERMOD_CUDA(cudaMemset(e.d_slnuv, 0, sizeof(double) * numslv));
+  e.warn_bin_firsttime = true;
+  e.bins_ready = true;
+  return ERMOD_OK;
+}
+
+static int frame_common(Engine& e, const double* cell, double sws) {
+  // cuboid cells only (realcal.F90:859-866); lower off-diagonals too, since the QR
+  // rotation of normalize_periodic is not applied
+  if (std::fabs(cell[3]) > 1e-8 || std::fabs(cell[6]) > 1e-8 || std::fabs(cell[7]) > 1e-8 ||
+      std::fabs(cell[1]) > 1e-8 || std::fabs(cell[2]) > 1e-8 || std::fabs(cell[5]) > 1e-8 || !(cell[0] > 0) ||
+      !(cell[4] > 0) || !(cell[8] > 0)) {
+    g_err = "A non-cuboidal cell is not supported";
+    return ERMOD_E_NONCUBOID;
+  }
+  std::memcpy(e.cell, cell, sizeof(double) * 9);
+  e.stat_weight_system = sws;
+  FrameGeom& g = e.geom;
+  // get_inverted_cell (engproc.F90:898-919)
+  auto C = [&](int i, int j) { return cell[(i - 1) + 3 * (j - 1)]; };
+  const double v = C(1, 1) * C(2, 2) * C(3, 3) + C(1, 2) * C(2, 3) * C(3, 1) + C(1, 3) * C(2, 1) * C(3, 2) -
+                   C(1, 3) * C(2, 2) * C(3, 1) - C(1, 2) * C(2, 1) * C(3, 3) - C(1, 1) * C(2, 3) * C(3, 2);
+  double ic[9];
+  ic[0] = C(2, 2) * C(3, 3) - C(2, 3) * C(3, 2);
+  ic[3] = C(1, 3) * C(3, 2) - C(1, 2) * C(3, 3);
+  ic[6] = C(1, 2) * C(2, 3) - C(1, 3) * C(2, 2);
+  ic[1] = C(2, 3) * C(3, 1) - C(2, 1) * C(3, 3);
+  ic[4] = C(1, 1) * C(3, 3) - C(1, 3) * C(3, 1);
+  ic[7] = C(1, 3) * C(2, 1) - C(1, 1) * C(2, 3);
+  ic[2] = C(2, 1) * C(3, 2) - C(2, 2) * C(3, 1);
+  ic[5] = C(1, 2) * C(3, 1) - C(1, 1) * C(3, 2);
+  ic[8] = C(1, 1) * C(2, 2) - C(1, 2) * C(2, 1);
+  for (int i = 0; i < 9; ++i) g.invcl[i] = ic[i] / v;
+  g.volume = v;
+  for (int i = 0; i < 3; ++i) {
+    g.L[i] = std::fabs(cell[4 * i]);
+    g.invL[i] = 1.0 / g.L[i];
+    g.fx_scale[i] = g.L[i] / 4294967296.0;
+  }
+  return ERMOD_OK;
+}
+
+static int frame_launch(Engine& e) {
+  e.phase_begin(PH_FRAME);
+  bool changed = !e.green_valid;
+  for (int i = 0; i < 9; ++i) changed = changed || (e.prevcl[i] != e.cell[i]);
+  if (changed) ERMOD_CUDA(launch_greenfunc(e));
+  std::memcpy(e.prevcl, e.cell, sizeof(e.cell));
+  e.green_valid = true;
+  ERMOD_CUDA(launch_frame_wrap(e));
+  ERMOD_CUDA(launch_frame_sort(e));
+  ERMOD_CUDA(launch_frame_sites(e));
+  e.phase_end();
+  e.frame_ready = true;
+  return ERMOD_OK;
+}
+
+int ermod_frame(ermod_ctx* c, const double* sitepos, const double* cell, double sws) {
+  if (!c || !sitepos || !cell) return fail_param("null argument");
+  Engine& e = c->e;
+  if (!e.topo_ready) return fail_param("ermod_set_topology must come first");
+  cudaSetDevice(e.device);
+  int st = frame_common(e, cell, sws);
+  if (st) return st;
+  ERMOD_CUDA(cudaMemcpyAsync(e.d_sitepos, sitepos, sizeof(double) * 3 * e.numatm, cudaMemcpyHostToDevice, e.stream));
+  st = frame_launch(e);
+  if (st) return st;
+  ERMOD_CUDA(cudaStreamSynchronize(e.stream));
+  return ERMOD_OK;
+}
+
+int ermod_frame_device(ermod_ctx* c, const double* sitepos_d, const double* cell, double sws) {
+  if (!c || !sitepos_d || !cell) return fail_param("null argument");
+  Engine& e = c->e;
+  if (!e.topo_ready) return fail_param("ermod_set_topology must come first");
+  cudaSetDevice(e.device);
+  int st = frame_common(e, cell, sws);
+  if (st) return st;
+  ERMOD_CUDA(cudaMemcpyAsync(e.d_sitepos, sitepos_d, sizeof(double) * 3 * e.numatm, cudaMemcpyDeviceToDevice,
+                             e.stream));
+  return frame_launch(e);
+}
+
+// the placement loop on device-resident inputs
+static int run_placements(Engine& e, int nplace, const int* d_tag, const double* d_sol, const double* d_sws,
+                          double* d_uv, double* d_fl, int ns_solute) {
+  int st = ensure_batch(e);
+  if (st) return st;
+  const int B = e.Bmax;
+  for (int b0 = 0; b0 < nplace; b0 += B) {
+    const int nb = std::min(B, nplace - b0);
+    BatchArgs a = e.buf;
+    a.nb = nb;
+    a.b0 = b0;
+    a.G = e.G;
+    a.tagslt = d_tag + b0;
+    a.stat_weight_solute = d_sws ? d_sws + b0 : nullptr;
+    a.uvengy_out = d_uv;
+    a.flceng_out = d_fl;
+    a.hist = e.d_ring_hist + (size_t)e.ring_fill * e.ermax;
+    const double* sol = d_sol ? d_sol + (size_t)b0 * ns_solute * 3 : nullptr;
+    e.phase_begin(PH_PREP);
+    ERMOD_CUDA(cudaMemsetAsync(a.hist, 0, sizeof(int) * (size_t)nb * e.ermax, e.stream));
+    ERMOD_CUDA(launch_place_prep(e, a, sol, e.P.slttype == 2 ? 2 : 1));
+    e.phase_end();
+    if (e.mixed) {
+      e.phase_begin(PH_SPECTRUM);
+      ERMOD_CUDA(launch_spectrum(e, a));
+      e.phase_end();
+      e.phase_begin(PH_FFT);
+      cufftResult r = cufftExecC2R(e.plan_c2r, (cufftComplex*)a.spec, a.phi);
+      if (r != CUFFT_SUCCESS) return fail_fft(r, "cufftExecC2R");
+      e.phase_end();
+    } else {
+      e.phase_begin(PH_SPECTRUM);
+      ERMOD_CUDA(launch_spread64(e, a));
+      cufftResult r = cufftExecD2Z(e.plan_d2z, a.phi64, (cufftDoubleComplex*)a.spec64);
+      if (r != CUFFT_SUCCESS) return fail_fft(r, "cufftExecD2Z");
+      ERMOD_CUDA(launch_influence64(e, a));
+      e.phase_end();
+      e.phase_begin(PH_FFT);
+      r = cufftExecZ2D(e.plan_z2d, (cufftDoubleComplex*)a.spec64, a.phi64);
+      if (r != CUFFT_SUCCESS) return fail_fft(r, "cufftExecZ2D");
+      e.phase_end();
+    }
+    e.phase_begin(PH_MOL);
+    ERMOD_CUDA(launch_mol_energy(e, a));
+    e.phase_end();
+    e.phase_begin(PH_ACCUM);
+    ERMOD_CUDA(launch_accumulate(e, a));
+    e.phase_end();
+    if (e.P.corrcal) {
+      e.ring_fill += nb;
+      if (e.ring_fill + B > e.ring_cap) {
+        e.phase_begin(PH_ECORR);
+        ERMOD_CUDA(launch_ecorr_flush(e));
+        e.phase_end();
+        e.ring_fill = 0;
+      }
+    }
+  }
+  if (e.P.corrcal && e.ring_fill > 0) {
+    e.phase_begin(PH_ECORR);
+    ERMOD_CUDA(launch_ecorr_flush(e));
+    e.phase_end();
+    e.ring_fill = 0;
+  }
+  // status snapshot (read by ermod_sync)
+  ERMOD_CUDA(cudaMemcpyAsync(e.h_status, e.d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, e.stream));
+  return ERMOD_OK;
+}
+
+static int check_ready(Engine& e, int nplace) {
+  if (!e.topo_ready) return fail_param("ermod_set_topology must come first");
+  if (!e.bins_ready) return fail_param("ermod_set_bins must come first");
+  if (!e.frame_ready) return fail_param("ermod_frame must come first");
+  if (nplace < 0) return fail_param("nplace < 0");
+  return ERMOD_OK;
+}
+
+static int reset_status(Engine& e) {
+  DevStatus s0{kNoError, 0, 0};
+  ERMOD_CUDA(cudaMemcpyAsync(e.d_status, &s0, sizeof(s0), cudaMemcpyHostToDevice, e.stream));
+  *e.h_status = s0;
+  return ERMOD_OK;
+}
+
+int ermod_sync(ermod_ctx* c) {
+  if (!c) return fail_param("null context");
+  Engine& e = c->e;
+  cudaSetDevice(e.device);
+  ERMOD_CUDA(cudaStreamSynchronize(e.stream));
+  const DevStatus s = *e.h_status;
+  if (s.mbin_hit || (s.err_key != kNoError && (int)(s.err_key & 0xff) == ERMOD_W_MBIN)) e.warn_bin_firsttime = false;
+  if (s.err_key != kNoError) {
+    e.err_placement = (int)(s.err_key >> 36);
+    e.err_molecule = (int)((s.err_key >> 8) & 0x0fffffff);
+    e.err_energy = std::nan("");
+    return (int)(s.err_key & 0xff);
+  }
+  if (s.range_fault) return ERMOD_E_DEVICE;
+  return ERMOD_OK;
+}
+
+int ermod_placements_device(ermod_ctx* c, int nplace, const int* tag_d, const double* sol_d, const double* sws_d,
+                            double* uv_d, double* fl_d) {
+  if (!c) return fail_param("null context");
+  Engine& e = c->e;
+  cudaSetDevice(e.device);
+  int st = check_ready(e, nplace);
+  if (st) return st;
+  if (nplace == 0) return ERMOD_OK;
+  if (!tag_d) return fail_param("tagslt missing");
+  // the solute of every placement is the same molecule type in a batch; take its size
+  // from the host copy of the topology (tagslt of placement 0 read back)
+  int tag0 = 0;
+  ERMOD_CUDA(cudaMemcpy(&tag0, tag_d, sizeof(int), cudaMemcpyDeviceToHost));
+  if (tag0 < 1 || tag0 > e.nummol) return fail_param("tagslt out of range");
+  const int ns = e.numsite[tag0 - 1];
+  if (ns > kMaxSoluteSites) {
+    g_err = "solute larger than 256 sites";
+    return ERMOD_E_UNSUPPORTED;
+  }
+  st = reset_status(e);
+  if (st) return st;
+  return run_placements(e, nplace, tag_d, sol_d, sws_d, uv_d, fl_d, ns);
+}
+
+int ermod_placements(ermod_ctx* c, int nplace, const int* tagslt, const double* sol, const double* sws,
+                     double* uv_out, double* fl_out) {
+  if (!c) return fail_param("null context");
+  Engine& e = c->e;
+  cudaSetDevice(e.device);
+  int st = check_ready(e, nplace);
+  if (st) return st;
+  if (nplace == 0) return ERMOD_OK;
+  if (!tagslt) return fail_param("tagslt missing");
+  const int ns = e.numsite[std::max(0, std::min(e.nummol - 1, tagslt[0] - 1))];
+  for (int p = 0; p < nplace; ++p) {
+    if (tagslt[p] < 1 || tagslt[p] > e.nummol) return fail_param("tagslt out of range");
+    const int m = tagslt[p] - 1;
+    if (e.sluvid[m] == 0) return ERMOD_E_RCP_FST;  // recpcal.F90:468-469
+    if (e.numsite[m] > kMaxSoluteSites) {
+      g_err = "solute larger than 256 sites";
+      return ERMOD_E_UNSUPPORTED;
+    }
+    if (sol && e.numsite[m] != ns) return fail_param("all placements of a call need the same solute size");
+    if (e.P.slttype != 1 && m != e.nummol - 1) {
+      g_err = "eng_ins: the inserted solute must be the last molecule";
+      return ERMOD_E_PARAM;
+    }
+  }
+  if (e.P.slttype != 1 && !sol) return fail_param("reference mode needs solute_sitepos");
+  // uploads
+  if (nplace > e.cap_place) {
+    dfree(e.d_tagslt);
+    dfree(e.d_solxyz);
+    dfree(e.d_sws);
+    e.cap_place = std::max(nplace, 1024);
+    ERMOD_CUDA(dalloc(&e.d_tagslt, e.cap_place));
+    ERMOD_CUDA(dalloc(&e.d_solxyz, (size_t)e.cap_place * kMaxSoluteSites * 3));
+    ERMOD_CUDA(dalloc(&e.d_sws, e.cap_place));
+  }
+  e.phase_begin(PH_COPY);
+  ERMOD_CUDA(cudaMemcpyAsync(e.d_tagslt, tagslt, sizeof(int) * nplace, cudaMemcpyHostToDevice, e.stream));
+  if (sol)
+    ERMOD_CUDA(cudaMemcpyAsync(e.d_solxyz, sol, sizeof(double) * 3 * (size_t)ns * nplace, cudaMemcpyHostToDevice,
+                               e.stream));
+  if (sws) ERMOD_CUDA(cudaMemcpyAsync(e.d_sws, sws, sizeof(double) * nplace, cudaMemcpyHostToDevice, e.stream));
+  e.phase_end();
+  double* d_uv = nullptr;
+  double* d_fl = nullptr;
+  if (uv_out) ERMOD_CUDA(dalloc(&d_uv, (size_t)nplace * (e.slvmax + 1)));
+  if (fl_out) ERMOD_CUDA(dalloc(&d_fl, (size_t)nplace * e.numslv));
+  st = reset_status(e);
+  if (!st) st = run_placements(e, nplace, e.d_tagslt, sol ? e.d_solxyz : nullptr, sws ? e.d_sws : nullptr, d_uv, d_fl, ns);
+  if (!st) {
+    if (uv_out)
+      st = cudaMemcpyAsync(uv_out, d_uv, sizeof(double) * (size_t)nplace * (e.slvmax + 1), cudaMemcpyDeviceToHost,
+                           e.stream) == cudaSuccess ? ERMOD_OK : ERMOD_E_CUDA;
+    if (fl_out && !st)
+      st = cudaMemcpyAsync(fl_out, d_fl, sizeof(double) * (size_t)nplace * e.numslv, cudaMemcpyDeviceToHost,
+                           e.stream) == cudaSuccess ? ERMOD_OK : ERMOD_E_CUDA;
+  }
+  const int st2 = ermod_sync(c);
+  if (d_uv) cudaFree(d_uv);
+  if (d_fl) cudaFree(d_fl);
+  return st ? st : st2;
+}
+
+int ermod_clear(ermod_ctx* c) {  // engclear (engproc.F90:276-288)
+  if (!c) return fail_param("null context");
+  Engine& e = c->e;
+  if (!e.bins_ready) return fail_param("ermod_set_bins must come first");
+  cudaSetDevice(e.device);
+  ERMOD_CUDA(cudaMemsetAsync(e.d_edens, 0, sizeof(double) * e.ermax, e.stream));
+  if (e.d_ecorr) ERMOD_CUDA(cudaMemsetAsync(e.d_ecorr, 0, sizeof(double) * (size_t)e.ermax * e.ermax, e.stream));
+  if (e.d_ecorr_n)
+    ERMOD_CUDA(cudaMemsetAsync(e.d_ecorr_n, 0, sizeof(long long) * (size_t)e.ermax * e.ermax, e.stream));
+  ERMOD_CUDA(cudaMemsetAsync(e.d_eself, 0, sizeof(double) * std::max(e.esmax, 1), e.stream));
+  ERMOD_CUDA(cudaMemsetAsync(e.d_slnuv, 0, sizeof(double) * e.numslv, e.stream));
+  ERMOD_CUDA(cudaMemsetAsync(e.d_scal, 0, sizeof(double) * 3, e.stream));  // engnorm, engsmpl, avslf
+  ERMOD_CUDA(cudaStreamSynchronize(e.stream));
+  return ERMOD_OK;
+}
+
+int ermod_get_accum(ermod_ctx* c, double* edens, double* ecorr, double* eself, double* slnuv, double* minuv,
+                    double* maxuv, double* scalars, int64_t* ecorr_count) {
+  if (!c) return fail_param("null context");
+  Engine& e = c->e;
+  if (!e.bins_ready) return fail_param("ermod_set_bins must come first");
+  cudaSetDevice(e.device);
+  ERMOD_CUDA(cudaStreamSynchronize(e.stream));
+  const size_t E = e.ermax;
+  if (edens) ERMOD_CUDA(cudaMemcpy(edens, e.d_edens, sizeof(double) * E, cudaMemcpyDeviceToHost));
+  if (ecorr) {
+    if (!e.d_ecorr) return fail_param("corrcal is off");
+    ERMOD_CUDA(cudaMemcpy(ecorr, e.d_ecorr, sizeof(double) * E * E, cudaMemcpyDeviceToHost));
+  }
+  if (ecorr_count) {
+    if (!e.d_ecorr_n) return fail_param("count_mirror is off");
+    ERMOD_CUDA(cudaMemcpy(ecorr_count, e.d_ecorr_n, sizeof(long long) * E * E, cudaMemcpyDeviceToHost));
+  }
+  if (eself && e.esmax > 0) ERMOD_CUDA(cudaMemcpy(eself, e.d_eself, sizeof(double) * e.esmax, cudaMemcpyDeviceToHost));
+  if (slnuv) ERMOD_CUDA(cudaMemcpy(slnuv, e.d_slnuv, sizeof(double) * e.numslv, cudaMemcpyDeviceToHost));
+  if (minuv) ERMOD_CUDA(cudaMemcpy(minuv, e.d_minuv, sizeof(double) * (e.numslv + 1), cudaMemcpyDeviceToHost));
+  if (maxuv) ERMOD_CUDA(cudaMemcpy(maxuv, e.d_maxuv, sizeof(double) * (e.numslv + 1), cudaMemcpyDeviceToHost));
+  if (scalars) {
+    double s[8];
+    ERMOD_CUDA(cudaMemcpy(s, e.d_scal, sizeof(s), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < 5; ++i) scalars[i] = s[i];
+  }
+  return ERMOD_OK;
+}
+
+int ermod_get_sizes(const ermod_ctx* c, int* slvmax, int* ermax, int* esmax, int* numslv) {
+  if (!c) return fail_param("null context");
+  if (slvmax) *slvmax = c->e.slvmax;
+  if (ermax) *ermax = c->e.ermax;
+  if (esmax) *esmax = c->e.esmax;
+  if (numslv) *numslv = c->e.numslv;
+  return ERMOD_OK;
+}
+
+int ermod_error_info(const ermod_ctx* c, int* placement, int* molecule, double* energy) {
+  if (!c) return fail_param("null context");
+  if (placement) *placement = c->e.err_placement;
+  if (molecule) *molecule = c->e.err_molecule;
+  if (energy) *energy = c->e.err_energy;
+  return ERMOD_OK;
+}
+
+int ermod_timing_enable(ermod_ctx* c, int on) {
+  if (!c) return fail_param("null context");
+  c->e.timing = on != 0;
+  return ERMOD_OK;
+}
+
+int ermod_timing_reset(ermod_ctx* c) {
+  if (!c) return fail_param("null context");
+  Engine& e = c->e;
+  cudaSetDevice(e.device);
+  harvest(e);
+  for (double& v : e.phase_ms) v = 0.0;
+  e.launches = 0;
+  return ERMOD_OK;
+}
+
+int ermod_timing_get(ermod_ctx* c, int max_phases, double* ms, const char** names, int* nphases, int64_t* launches) {
+  if (!c) return fail_param("null context");
+  Engine& e = c->e;
+  cudaSetDevice(e.device);
+  harvest(e);
+  const int n = std::min(max_phases, (int)PH_COUNT);
+  for (int i = 0; i < n; ++i) {
+    if (ms) ms[i] = e.phase_ms[i];
+    if (names) names[i] = kPhaseNames[i];
+  }
+  if (nphases) *nphases = PH_COUNT;
+  if (launches) *launches = e.launches;
+  return ERMOD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,160 @@
+// engine.cuh -- the context behind ermod_ctx (host side state + device buffers).
+#pragma once
+
+#include <cufft.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "../../include/ermod_gpu.h"
+#include "ermod_internal.cuh"
+
+namespace ermod {
+
+enum Phase { PH_FRAME = 0, PH_PREP, PH_SPECTRUM, PH_FFT, PH_MOL, PH_ACCUM, PH_ECORR, PH_COPY, PH_COUNT };
+extern const char* const kPhaseNames[PH_COUNT];
+
+struct Engine {
+  ermod_params P{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  bool mixed = true;
+  int P_order = 4;
+
+  // timing (CUDA events around each phase on the context's stream)
+  bool timing = false;
+  double phase_ms[PH_COUNT] = {};
+  long long launches = 0;
+  std::vector<cudaEvent_t> ev_pool;
+  struct Pending { cudaEvent_t a, b; int phase; };
+  std::vector<Pending> pending;
+  int cur_phase = -1;
+  cudaEvent_t cur_ev = nullptr;
+
+  // ---- topology ----------------------------------------------------------------
+  int nummol = 0, numatm = 0, ljtype_max = 0, slvmax = 0, nsite_phys = 0, max_mol_sites = 0;
+  std::vector<int> mbi0;  // 0-based first atom of each molecule, nummol+1 entries
+  std::vector<int> sluvid, uvspec, tagpt, numsite, ljtype0;
+  std::vector<double> charge, mol_charge;
+  double total_charge_phys = 0.0;
+  bool topo_ready = false;
+  double* d_charge = nullptr;
+  int* d_ljtype = nullptr;       // 0-based
+  double* d_ljene = nullptr;     // [T*T] column-major
+  double* d_ljlensq = nullptr;
+  int* d_mol_atom0 = nullptr;    // [slvmax] first atom (0-based) of physical molecule k
+  int* d_mol_nsite = nullptr;    // [slvmax]
+  int* d_mol_species = nullptr;  // [slvmax] uvspec
+  double* d_mol_qmol = nullptr;  // [slvmax]
+  int* d_mbi0 = nullptr;         // [nummol+1] 0-based first atom of each molecule
+  double* d_qmol_all = nullptr;  // [nummol] molecular charges
+  int* d_mol_to_k = nullptr;     // [nummol] tagpt position (0-based) or -1
+
+  // ---- energy coordinate ---------------------------------------------------------
+  int numslv = 0, ermax = 0, esmax = 0;
+  std::vector<int> uvmax, uvsoft, uvoff;
+  std::vector<double> uvcrd, escrd;
+  bool bins_ready = false;
+  long long* d_uvkey = nullptr;  // ordered keys of uvcrd
+  long long* d_eskey = nullptr;  // ordered keys of escrd
+  int* d_spec = nullptr;         // [numslv][3] {uvoff, uvmax, uvsoft}
+
+  // ---- accumulators ----------------------------------------------------------------
+  double* d_edens = nullptr;
+  double* d_ecorr = nullptr;
+  long long* d_ecorr_n = nullptr;
+  double* d_eself = nullptr;
+  double* d_slnuv = nullptr;
+  double* d_minuv = nullptr;  // [numslv+1]
+  double* d_maxuv = nullptr;
+  double* d_scal = nullptr;   // {engnorm, engsmpl, avslf, voffset, voffset_initialized, usreal, usreal_valid}
+  bool warn_bin_firsttime = true;
+
+  // ---- frame -----------------------------------------------------------------------
+  FrameGeom geom{};
+  double cell[9] = {}, prevcl[9] = {};
+  bool green_valid = false, frame_ready = false;
+  double stat_weight_system = 1.0;
+  double* d_sitepos = nullptr;   // (3, numatm)
+  double* d_engfac = nullptr;    // [K3][K2][H]
+  float* d_engfac_f = nullptr;
+  double* d_splfc = nullptr;     // [K1 + K2 + K3]
+  float2* d_twiddle = nullptr;   // [K1 + K2 + K3] exp(-2 pi i m / K)
+  double* d_wrapped = nullptr;   // (3, numatm) normalised coordinates
+  // spatial sort of physical molecules
+  unsigned int* d_sort_key = nullptr;
+  unsigned int* d_sort_key_alt = nullptr;
+  int* d_sort_val = nullptr;
+  int* d_sort_val_alt = nullptr;
+  void* d_cub_tmp = nullptr;
+  size_t cub_tmp_bytes = 0;
+  // slot-ordered solvent layout
+  int* d_slot_mol = nullptr;      // [slvmax] tagpt index k held by slot m
+  int* d_slot_site = nullptr;     // [slvmax+1] first site of slot m
+  int* d_slot_species = nullptr;  // [slvmax]
+  double* d_slot_qmol = nullptr;  // [slvmax]
+  int4* d_site_pos = nullptr;     // [nsite_phys]
+  float4* d_site_rec = nullptr;
+  int* d_site_grid = nullptr;
+  double* d_site_x = nullptr;     // FP64 path [nsite_phys][3]
+  double* d_site_w = nullptr;     // FP64 path [nsite_phys][3][P]
+  double* d_site_q = nullptr;     // FP64 path
+  float* d_frame_scal = nullptr;  // [0] max molecule radius about its first site (A)
+
+  // ---- batch buffers ---------------------------------------------------------------
+  int Bmax = 1, G = 1, ntile = 1, tile = 256;
+  int* d_tagslt = nullptr;        // [cap_place]
+  double* d_solxyz = nullptr;     // [cap_place][S][3]
+  double* d_sws = nullptr;        // [cap_place]
+  int cap_place = 0;
+  BatchArgs buf{};                // device buffers sized for Bmax (pointers only)
+  // histogram ring for ecorr (corrcal) / per-batch histograms
+  int ring_cap = 0, ring_fill = 0;
+  int* d_ring_hist = nullptr;     // [ring_cap][ermax]
+  double* d_ring_w = nullptr;     // [ring_cap]
+  int* d_ring_nz = nullptr;       // [ring_cap][ermax] packed (bin | count << 16)... see kernels
+  int* d_ring_nnz = nullptr;      // [ring_cap] occupied bins per entry
+  int* d_ring_valid = nullptr;    // [ring_cap] entry accumulated (no error in its batch)
+
+  // ---- status ----------------------------------------------------------------------
+  DevStatus* d_status = nullptr;
+  DevStatus* h_status = nullptr;  // pinned
+  int err_placement = -1, err_molecule = -1;
+  double err_energy = 0.0;
+  int call_b0 = 0;
+
+  // ---- cuFFT -------------------------------------------------------------------------
+  cufftHandle plan_c2r = 0, plan_d2z = 0, plan_z2d = 0;
+  bool plans_ready = false;
+
+  // helpers
+  int H() const { return geom.K[0] / 2 + 1; }
+  size_t grid_real() const { return (size_t)geom.K[0] * geom.K[1] * geom.K[2]; }
+  size_t grid_cplx() const { return (size_t)H() * geom.K[1] * geom.K[2]; }
+  int Kmax() const { return std::max(geom.K[0], std::max(geom.K[1], geom.K[2])); }
+
+  void phase_begin(int ph);
+  void phase_end();
+  void count_launch(int n = 1) { launches += n; }
+};
+
+// sizes shared between the launchers and the host code
+int spectrum_chunk(int H);
+int influence64_blocks();
+int accumulate_max_batch();
+size_t frame_cub_bytes(int n);
+double host_spline_value(int order, double x);
+
+// host utilities (engine.cu)
+void set_error_string(const std::string& s);
+int fail_cuda(cudaError_t e, const char* where);
+
+}  // namespace ermod
+
+#define ERMOD_CUDA(call)                                                              \
+  do {                                                                                \
+    cudaError_t err__ = (call);                                                       \
+    if (err__ != cudaSuccess) return ::ermod::fail_cuda(err__, #call);                \
+  } while (0)

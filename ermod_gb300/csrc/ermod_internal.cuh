@@ -1,0 +1,119 @@
+// ermod_internal.cuh -- device data layout and kernel launchers of the GB300 path.
+//
+// Data layout in HBM (one context):
+//   topology   per-atom charge/ljtype, per physical molecule (tagpt order) species,
+//              molecular charge and site range;
+//   frame      raw sitepos (3, numatm) FP64; per physical site, in the frame's
+//              spatially sorted molecule order ("slot" order):
+//                pos   int4 {X, Y, Z, ljtype}  -- wrapped coordinates as 32-bit fixed
+//                      point, X = x / L * 2^32 (periodic minimum image is an int32
+//                      subtraction);
+//                rec   float4 {t1, t2, t3, q}  -- B-spline fractional offsets and charge;
+//                grid  int, packed base grid point g1 | g2 << 10 | g3 << 20;
+//              FP64 path: wrapped FP64 coordinates, FP64 spline weights, FP64 charge;
+//   green      engfac[K3][K2][K1/2+1] FP64 (+ FP32 copy for the mixed path);
+//   batch      per placement solute sites, 1-D structure-factor vectors, PME spectrum
+//              and potential grids, per-placement energy histograms;
+//   accum      edens, ecorr (+ int64 count mirror), eself, slnuv, minuv/maxuv, scalars.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ermod {
+
+constexpr int kMaxSoluteSites = 256;  // sites of one solute molecule
+constexpr int kMaxSplineOrder = 8;
+constexpr int kMaxSpecies = 16;
+constexpr int kGridBits = 10;         // packed grid coordinates: K <= 1024 per axis
+constexpr double kPi = 3.1415926535897932;
+
+// error key: (placement << 36) | (molecule << 8) | code, minimised atomically so the
+// first failing (placement, molecule) in reference order wins.
+constexpr unsigned long long kNoError = ~0ull;
+__host__ __device__ inline unsigned long long make_err_key(int placement, int molecule, int code) {
+  return ((unsigned long long)placement << 36) | ((unsigned long long)(molecule & 0x0fffffff) << 8) |
+         (unsigned long long)(code & 0xff);
+}
+
+// ordered 64-bit key of a double (total order equal to numeric order, -0 == +0)
+__host__ __device__ inline long long ordered_key(double x) {
+  if (x == 0.0) x = 0.0;
+  long long k;
+#ifdef __CUDA_ARCH__
+  k = __double_as_longlong(x);
+#else
+  __builtin_memcpy(&k, &x, 8);
+#endif
+  return k ^ ((k >> 63) & 0x7fffffffffffffffll);
+}
+
+struct FrameGeom {
+  double L[3];       // cell lengths (cuboid cell)
+  double invL[3];    // 1 / L as dtrtri computes it
+  double invcl[9];   // engproc.F90:898-919, column-major
+  double volume;
+  double fx_scale[3];  // L / 2^32 (fixed point -> Angstrom)
+  int K[3];
+};
+
+// Device status block (one per context, zeroed by ermod_sync).
+struct DevStatus {
+  unsigned long long err_key;  // kNoError when no error
+  int mbin_hit;                // 'mbin' condition met (reported once)
+  int range_fault;             // an index check failed on the device
+};
+
+// One batch of placements, as seen by the kernels.
+struct BatchArgs {
+  int nb;             // placements in this batch
+  int b0;             // index of the batch's first placement within the call
+  int G;              // placements per mol_energy block
+  int n_u_max;        // max solute sites in the batch
+  const int* tagslt;  // [nb] 1-based
+  const double* stat_weight_solute;  // [nb] or null
+  // solute site data per placement, [nb][kMaxSoluteSites]
+  int* u_nsite;        // [nb]
+  double* u_x;         // [nb][S][3] wrapped FP64 coords
+  int4* u_pos;         // [nb][S] fixed point + ljtype
+  double* u_q;         // [nb][S]
+  int* u_grid;         // [nb][S] packed base grid
+  double* u_w;         // [nb][S][3][P] FP64 spline weights
+  float2* u_bvec;      // [nb][S][3][Kmax] 1-D structure factors (mixed)
+  double* u_qmol;      // [nb] molecular charge of the solute
+  double* u_usreal;    // [nb] realcal_self value
+  float* u_radius;     // [nb] solute bounding radius about site 1 (A)
+  // PME
+  float2* spec;        // [nb][K3][K2][H] mixed spectrum (engfac * S)
+  float* phi;          // [nb][K3][K2][K1] mixed potential
+  double2* spec64;     // FP64 path
+  double* phi64;       // FP64 path
+  double* self_part;   // [nb][K3] partial self energies
+  // outputs
+  int* hist;           // [nb][ermax] instantaneous histogram (insdst)
+  double* part;        // [nb][ntile][numslv][3] {sum, min, max}
+  double* uvengy_out;  // [nplace][slvmax+1] or null (device)
+  double* flceng_out;  // [nplace][numslv] or null (device)
+  double* engnmfc;     // [nb] weights (0 for skipped placements)
+};
+
+struct Engine;
+
+// ---- launchers (defined in the .cu files) ---------------------------------------
+// frame preparation
+cudaError_t launch_frame_wrap(Engine& e);
+cudaError_t launch_frame_sort(Engine& e);
+cudaError_t launch_frame_sites(Engine& e);
+cudaError_t launch_greenfunc(Engine& e);
+// placement preparation and PME
+cudaError_t launch_place_prep(Engine& e, const BatchArgs& a, const double* sol_xyz, int self_first_only);
+cudaError_t launch_spectrum(Engine& e, const BatchArgs& a);
+cudaError_t launch_spread64(Engine& e, const BatchArgs& a);
+cudaError_t launch_influence64(Engine& e, const BatchArgs& a);
+// per-molecule energies and histograms
+cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a);
+// accumulation
+cudaError_t launch_accumulate(Engine& e, const BatchArgs& a);
+cudaError_t launch_ecorr_flush(Engine& e);
+
+}  // namespace ermod

@@ -1,0 +1,353 @@
+// kernels_accum.cu -- update_histogram's accumulation (engproc.F90:758-856).
+//
+//   accumulate    one CTA per batch: solute self energy u0 (engproc.F90:711-733), its
+//                 weight engnmfc (wgtslf / volcorrect, engproc.F90:772-796,871-887),
+//                 engnorm/engsmpl/avslf, eself, minuv/maxuv, flceng and slnuv, and
+//                 edens += engnmfc * insdst.  Every FP64 sum runs in placement order, as
+//                 in the reference's sequential loop, so results are bit-reproducible.
+//                 A batch in which any molecule failed a bin check is not accumulated.
+//   ring_compact  per placement, the ascending list of occupied bins (bin, count).
+//   ecorr_rows    ecorr(iduvp, iduv) += engnmfc * insdst(iduv) * insdst(iduvp)
+//                 (engproc.F90:841-853) for the placements buffered in the ring: each
+//                 CTA owns a few rows of the matrix in shared memory and walks the
+//                 placements in order, touching only occupied (row, column) pairs; an
+//                 exact int64 mirror sum insdst(i) insdst(j) is kept beside it.
+#include "engine.cuh"
+
+namespace ermod {
+
+namespace {
+
+struct AccArgs {
+  BatchArgs a;
+  int ntile, numslv, ermax, esmax, nself;
+  int selfcal, wgtslf, soln, estype, rigid, mbin_mode;
+  double temp, volume, volfac;  // volfac = pi Qtot^2 / beta^2 / V / 2 (volcorrect)
+  double screen;                // residual_ene(slt, slt) = -(pi Q Q / beta / beta / V) / 2
+  double stat_weight_system;
+  double* scal;  // {engnorm, engsmpl, avslf, voffset, voffset_init, usreal, usreal_valid}
+  double* edens;
+  double* eself;
+  double* slnuv;
+  double* minuv;
+  double* maxuv;
+  const long long* eskey;
+  int* ring_valid;  // [nb] entries of this batch in the ring
+  double* ring_w;
+  int slvmax;
+  DevStatus* status;
+};
+
+constexpr int kAccThreads = 256;
+constexpr int kMaxBatch = 256;
+
+__global__ void __launch_bounds__(kAccThreads) accumulate_kernel(AccArgs A) {
+  const BatchArgs& a = A.a;
+  const int nb = a.nb;
+  __shared__ double su0[kMaxBatch];
+  __shared__ double sw[kMaxBatch];
+  __shared__ double stw[kMaxBatch];
+  __shared__ int sbin[kMaxBatch];
+  __shared__ int skip;
+  __shared__ double s_voffset;
+  // ---- phase 1: u0 of every placement (parallel over b) ----
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    double self = 0.0;
+    const double* sp = a.self_part + (size_t)b * A.nself;
+    for (int i = 0; i < A.nself; ++i) self += sp[i];
+    double usreal;
+    if (A.rigid)
+      usreal = (A.scal[6] != 0.0) ? A.scal[5] : a.u_usreal[0];
+    else
+      usreal = a.u_usreal[b];
+    const double qm = a.u_qmol[b];
+    double epcl = kPi * qm * qm / A.screen / A.screen / A.volume;
+    epcl = epcl / 2.0;
+    const double residual = -epcl;
+    double u0 = self;
+    u0 = u0 + usreal + residual;  // uvengy(0) = uvengy(0) + pairep + residual
+    su0[b] = u0;
+    sbin[b] = -1;
+    if (a.uvengy_out) a.uvengy_out[(size_t)(a.b0 + b) * (A.slvmax + 1)] = u0;
+    if (A.selfcal) {  // getiduv(0, uvengy(0))
+      int code = 0, ret = 0;
+      if (u0 != u0) {
+        code = ERMOD_E_ENG_MIN;
+      } else {
+        const long long ku = ordered_key(u0);
+        int lo = 0, hi = A.esmax;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (A.eskey[mid] < ku)
+            lo = mid + 1;
+          else
+            hi = mid;
+        }
+        ret = lo;
+        if (ret <= 0)
+          code = ERMOD_E_ENG_MIN;
+        else if (ret == A.esmax && u0 < 1.0e3 && A.mbin_mode != 0) {
+          if (A.mbin_mode == 1)
+            code = ERMOD_W_MBIN;
+          else
+            atomicOr(&A.status->mbin_hit, 1);
+        }
+      }
+      if (code)
+        atomicMin(&A.status->err_key, make_err_key(a.b0 + b, 0, code));
+      else
+        sbin[b] = ret - 1;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const volatile unsigned long long* ek = &A.status->err_key;
+    skip = (*ek != kNoError) ? 1 : 0;
+    if (!skip && A.wgtslf && A.scal[4] == 0.0) {
+      A.scal[3] = su0[0];  // voffset from the first placement ever processed
+      A.scal[4] = 1.0;
+    }
+    if (!skip && A.rigid && A.scal[6] == 0.0) {
+      A.scal[5] = a.u_usreal[0];
+      A.scal[6] = 1.0;
+    }
+    s_voffset = A.scal[3];
+  }
+  __syncthreads();
+  if (skip) {
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+      a.engnmfc[b] = 0.0;
+      A.ring_valid[b] = 0;
+    }
+    return;
+  }
+  // ---- phase 2: weights (parallel), then the ordered scalar sums ----
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    double engnmfc;
+    if (!A.wgtslf) {
+      engnmfc = 1.0;
+    } else {
+      const double factor = su0[b] - s_voffset;
+      engnmfc = A.soln ? exp(factor / A.temp) : exp(-factor / A.temp);
+    }
+    double total_weight = A.stat_weight_system * (a.stat_weight_solute ? a.stat_weight_solute[b] : 1.0);
+    if (A.estype == 2) {
+      total_weight = total_weight * A.volume;
+      total_weight = total_weight * exp(A.volfac / A.temp);
+    }
+    engnmfc = engnmfc * total_weight;
+    sw[b] = engnmfc;
+    stw[b] = total_weight;
+    a.engnmfc[b] = engnmfc;
+    A.ring_w[b] = engnmfc;
+    A.ring_valid[b] = 1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double engnorm = A.scal[0], engsmpl = A.scal[1], avslf = A.scal[2];
+    double mn = A.minuv[0], mx = A.maxuv[0];
+    for (int b = 0; b < nb; ++b) {
+      engnorm = engnorm + sw[b];
+      engsmpl = engsmpl + 1.0;
+      avslf = avslf + stw[b];
+      if (A.selfcal) A.eself[sbin[b]] += sw[b];
+      mn = fmin(mn, su0[b]);
+      mx = fmax(mx, su0[b]);
+    }
+    A.scal[0] = engnorm;
+    A.scal[1] = engsmpl;
+    A.scal[2] = avslf;
+    A.minuv[0] = mn;
+    A.maxuv[0] = mx;
+  }
+  // ---- phase 3: per-species sums over the tiles (fixed order) ----
+  for (int t = threadIdx.x; t < nb * A.numslv; t += blockDim.x) {
+    const int b = t / A.numslv, sp = t % A.numslv;
+    double s = 0.0, mn = 1.0e300, mx = -1.0e300;
+    bool any = false;
+    for (int tile = 0; tile < A.ntile; ++tile) {
+      const double* pt = a.part + (((size_t)b * A.ntile + tile) * A.numslv + sp) * 3;
+      s += pt[0];
+      if (pt[1] <= pt[2]) {
+        mn = any ? fmin(mn, pt[1]) : pt[1];
+        mx = any ? fmax(mx, pt[2]) : pt[2];
+        any = true;
+      }
+    }
+    a.part[(((size_t)b * A.ntile + 0) * A.numslv + sp) * 3 + 0] = s;  // flceng(sp, b)
+    a.part[(((size_t)b * A.ntile + 0) * A.numslv + sp) * 3 + 1] = any ? mn : 1.0e300;
+    a.part[(((size_t)b * A.ntile + 0) * A.numslv + sp) * 3 + 2] = any ? mx : -1.0e300;
+    if (a.flceng_out) a.flceng_out[(size_t)(a.b0 + b) * A.numslv + sp] = s;
+  }
+  __syncthreads();
+  for (int sp = threadIdx.x; sp < A.numslv; sp += blockDim.x) {
+    double mn = A.minuv[sp + 1], mx = A.maxuv[sp + 1], sl = A.soln ? A.slnuv[sp] : 0.0;
+    for (int b = 0; b < nb; ++b) {
+      const double* pt = a.part + (((size_t)b * A.ntile + 0) * A.numslv + sp) * 3;
+      if (pt[1] <= pt[2]) {
+        mn = fmin(mn, pt[1]);
+        mx = fmax(mx, pt[2]);
+      }
+      if (A.soln) sl = sl + pt[0] * sw[b];
+    }
+    A.minuv[sp + 1] = mn;
+    A.maxuv[sp + 1] = mx;
+    if (A.soln) A.slnuv[sp] = sl;
+  }
+  // ---- phase 4: edens += engnmfc * insdst, placements in order ----
+  for (int i = threadIdx.x; i < A.ermax; i += blockDim.x) {
+    double e = A.edens[i];
+    bool touched = false;
+    for (int b = 0; b < nb; ++b) {
+      const int c = a.hist[(size_t)b * A.ermax + i];
+      if (c) {
+        e = e + sw[b] * (double)c;
+        touched = true;
+      }
+    }
+    if (touched) A.edens[i] = e;
+  }
+}
+
+// occupied-bin list per ring entry: entries (bin << 0) with counts beside them
+__global__ void __launch_bounds__(256) ring_compact_kernel(const int* __restrict__ hist, const int* __restrict__ valid,
+                                                         int ermax, int* __restrict__ nz_bin, int* __restrict__ nz_cnt,
+                                                         int* __restrict__ nnz) {
+  const int p = blockIdx.x;
+  const int* h = hist + (size_t)p * ermax;
+  __shared__ int scan[256];
+  const int per = (ermax + blockDim.x - 1) / blockDim.x;
+  const int lo = threadIdx.x * per, hi = min(ermax, lo + per);
+  int cnt = 0;
+  if (valid[p])
+    for (int i = lo; i < hi; ++i) cnt += (h[i] != 0);
+  scan[threadIdx.x] = cnt;
+  __syncthreads();
+  for (int off = 1; off < blockDim.x; off <<= 1) {  // inclusive Hillis-Steele scan
+    const int v = (threadIdx.x >= off) ? scan[threadIdx.x - off] : 0;
+    __syncthreads();
+    scan[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int pos = scan[threadIdx.x] - cnt;
+  if (valid[p])
+    for (int i = lo; i < hi; ++i)
+      if (h[i]) {
+        nz_bin[(size_t)p * ermax + pos] = i;
+        nz_cnt[(size_t)p * ermax + pos] = h[i];
+        ++pos;
+      }
+  if (threadIdx.x == blockDim.x - 1) nnz[p] = valid[p] ? scan[threadIdx.x] : 0;
+}
+
+__global__ void __launch_bounds__(256) ecorr_rows_kernel(const int* __restrict__ hist, const int* __restrict__ nz_bin,
+                                                       const int* __restrict__ nz_cnt, const int* __restrict__ nnz,
+                                                       const double* __restrict__ w, int nring, int ermax, int R,
+                                                       double* __restrict__ ecorr, long long* __restrict__ ecorr_n) {
+  extern __shared__ double srow[];  // [R][ermax] (+ [R][ermax] int64 mirror)
+  long long* srow_n = reinterpret_cast<long long*>(srow + (size_t)R * ermax);
+  const int row0 = blockIdx.x * R;
+  const int nrow = min(R, ermax - row0);
+  __shared__ int any;
+  if (threadIdx.x == 0) any = 0;
+  __syncthreads();
+  for (int t = threadIdx.x; t < nring * nrow; t += blockDim.x) {
+    const int p = t / nrow, r = t % nrow;
+    if (nnz[p] > 0 && hist[(size_t)p * ermax + row0 + r] != 0) any = 1;
+  }
+  __syncthreads();
+  if (!any) return;
+  for (int t = threadIdx.x; t < nrow * ermax; t += blockDim.x) {
+    srow[t] = ecorr[(size_t)row0 * ermax + t];
+    if (ecorr_n) srow_n[t] = ecorr_n[(size_t)row0 * ermax + t];
+  }
+  __syncthreads();
+  for (int p = 0; p < nring; ++p) {
+    const int n = nnz[p];
+    if (n == 0) continue;
+    const int* bins = nz_bin + (size_t)p * ermax;
+    const int* cnts = nz_cnt + (size_t)p * ermax;
+    for (int r = 0; r < nrow; ++r) {
+      const int ci = hist[(size_t)p * ermax + row0 + r];
+      if (ci == 0) continue;
+      const double wi = w[p] * (double)ci;
+      double* row = srow + (size_t)r * ermax;
+      long long* rown = srow_n + (size_t)r * ermax;
+      for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        const int j = bins[t];
+        const int cj = cnts[t];
+        row[j] = row[j] + wi * (double)cj;
+        if (ecorr_n) rown[j] += (long long)ci * (long long)cj;
+      }
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < nrow * ermax; t += blockDim.x) {
+    ecorr[(size_t)row0 * ermax + t] = srow[t];
+    if (ecorr_n) ecorr_n[(size_t)row0 * ermax + t] = srow_n[t];
+  }
+}
+
+}  // namespace
+
+int accumulate_max_batch() { return kMaxBatch; }
+
+cudaError_t launch_accumulate(Engine& e, const BatchArgs& a) {
+  AccArgs A{};
+  A.a = a;
+  A.ntile = e.ntile;
+  A.numslv = e.numslv;
+  A.ermax = e.ermax;
+  A.esmax = e.esmax;
+  const int kc = spectrum_chunk(e.H());
+  A.nself = e.mixed ? e.geom.K[2] * ((e.geom.K[1] + kc - 1) / kc) : influence64_blocks();
+  A.selfcal = e.P.selfcal;
+  A.wgtslf = e.P.wgtslf;
+  A.soln = e.P.slttype == 1;
+  A.estype = e.P.estype;
+  A.rigid = e.P.slttype == 2;
+  A.mbin_mode = e.warn_bin_firsttime ? (e.P.force_calculation ? 2 : 1) : 0;
+  A.temp = e.P.temp;
+  A.volume = e.geom.volume;
+  A.volfac = kPi * (e.total_charge_phys * e.total_charge_phys) / (e.P.screen * e.P.screen) / e.geom.volume / 2.0;
+  A.screen = e.P.screen;
+  A.stat_weight_system = e.stat_weight_system;
+  A.scal = e.d_scal;
+  A.edens = e.d_edens;
+  A.eself = e.d_eself;
+  A.slnuv = e.d_slnuv;
+  A.minuv = e.d_minuv;
+  A.maxuv = e.d_maxuv;
+  A.eskey = e.d_eskey;
+  A.ring_valid = e.d_ring_valid + e.ring_fill;
+  A.ring_w = e.d_ring_w + e.ring_fill;
+  A.slvmax = e.slvmax;
+  A.status = e.d_status;
+  accumulate_kernel<<<1, kAccThreads, 0, e.stream>>>(A);
+  e.count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ecorr_flush(Engine& e) {
+  if (e.ring_fill == 0) return cudaSuccess;
+  const int n = e.ring_fill;
+  int* nz_bin = e.d_ring_nz;
+  int* nz_cnt = e.d_ring_nz + (size_t)e.ring_cap * e.ermax;
+  const int* valid = e.d_ring_valid;
+  ring_compact_kernel<<<n, 256, 0, e.stream>>>(e.d_ring_hist, valid, e.ermax, nz_bin, nz_cnt, e.d_ring_nnz);
+  e.count_launch();
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return err;
+  const size_t per_row = (size_t)e.ermax * (sizeof(double) + (e.d_ecorr_n ? sizeof(long long) : 0));
+  int R = (int)std::max<size_t>(1, std::min<size_t>(8, (96 * 1024) / per_row));
+  const size_t smem = per_row * R;
+  err = cudaFuncSetAttribute(ecorr_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  const int nblk = (e.ermax + R - 1) / R;
+  ecorr_rows_kernel<<<nblk, 256, smem, e.stream>>>(e.d_ring_hist, nz_bin, nz_cnt, e.d_ring_nnz, e.d_ring_w, n,
+                                                   e.ermax, R, e.d_ecorr, e.d_ecorr_n);
+  e.count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace ermod

@@ -1,0 +1,343 @@
+// kernels_frame.cu -- once-per-frame preparation (the engconst prologue).
+//
+//   frame_wrap      realcal_prepare + normalize_periodic (realcal.F90:137-146, 789-885)
+//                   for every atom, FP64, the reference's two wrap passes;
+//   frame_sort      spatial (Morton) order of the physical molecules by the ~4 A cell of
+//                   their first site, so that a CTA's molecules are compact in space
+//                   (coherent near-field branches, PME-grid reuse in L1);
+//   frame_sites     per physical site in slot order: fixed-point coordinates, LJ type,
+//                   charge and the B-spline data of calc_spline_molecule
+//                   (recpcal.F90:408-442) -- replaces recpcal_prepare_solvent
+//                   (engproc.F90:378-382) and the per-placement blockify/sort_block
+//                   rebuild of the reference (realcal.F90:439-525);
+//   greenfunc       recpcal_spline_greenfunc (recpcal.F90:111-152), FP64.
+// All of these are HBM-streaming kernels over O(numatm) or O(K^3) elements.
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include "engine.cuh"
+
+namespace ermod {
+
+namespace {
+
+struct SplineCoef {
+  double c[kMaxSplineOrder + 1];
+  int order;
+};
+
+SplineCoef make_coef(int order) {  // spline_init, spline.F90:26-44
+  SplineCoef s{};
+  s.order = order;
+  for (int i = 0; i <= order; ++i) {
+    double factor = 1.0;
+    for (int k = 1; k <= i; ++k) factor = factor * (double)k;
+    for (int k = 1; k <= order - i; ++k) factor = factor * (double)k;
+    factor = (double)order / factor;
+    if (i % 2 == 1) factor = -factor;
+    s.c[i] = factor;
+  }
+  return s;
+}
+
+__host__ __device__ __forceinline__ double ipow(double x, int e) {
+  double r = 1.0;
+  bool first = true;
+  while (e > 0) {
+    if (e & 1) {
+      r = first ? x : r * x;
+      first = false;
+    }
+    e >>= 1;
+    if (e) x = x * x;
+  }
+  return r;
+}
+
+// spline_value (spline.F90:47-59)
+__device__ __forceinline__ double spline_value(const SplineCoef& s, double rst) {
+  double f = 0.0;
+  if ((rst > 0.0) && (rst < (double)s.order)) {
+    const int k = (int)rst;
+    for (int i = 0; i <= k; ++i) f = f + s.c[i] * ipow(rst - (double)i, s.order - 1);
+  }
+  return f;
+}
+
+// normalize_periodic for a cuboid cell, atom a (0-based); mirrors both passes.
+__device__ __forceinline__ void wrap_atom(const double* __restrict__ pos, int a, const FrameGeom& g, double out[3]) {
+  double x[3];
+  for (int i = 0; i < 3; ++i) {
+    const double v = pos[3 * (size_t)a + i];
+    x[i] = v - g.L[i] * floor(g.invL[i] * v);
+  }
+  // second pass: y by the second cell vector, x by atom 1's current x (realcal.F90:878-883)
+  x[1] = x[1] - g.L[1] * floor(g.invL[1] * x[1]);
+  const double x0 = pos[0] - g.L[0] * floor(g.invL[0] * pos[0]);
+  const double f0 = floor(g.invL[0] * x0);
+  if (a == 0) {
+    x[0] = x[0] - g.L[0] * f0;
+  } else {
+    const double x0b = x0 - g.L[0] * f0;
+    x[0] = x[0] - g.L[0] * floor(g.invL[0] * x0b);
+  }
+  out[0] = x[0];
+  out[1] = x[1];
+  out[2] = x[2];
+}
+
+__global__ void frame_wrap_kernel(const double* __restrict__ pos, int numatm, FrameGeom g, double* __restrict__ out) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= numatm) return;
+  double w[3];
+  wrap_atom(pos, a, g, w);
+  out[3 * (size_t)a + 0] = w[0];
+  out[3 * (size_t)a + 1] = w[1];
+  out[3 * (size_t)a + 2] = w[2];
+}
+
+__device__ __forceinline__ unsigned int spread3(unsigned int v) {
+  v &= 0x3ff;
+  v = (v | (v << 16)) & 0x030000ff;
+  v = (v | (v << 8)) & 0x0300f00f;
+  v = (v | (v << 4)) & 0x030c30c3;
+  v = (v | (v << 2)) & 0x09249249;
+  return v;
+}
+
+__global__ void frame_key_kernel(const double* __restrict__ wrapped, const int* __restrict__ mol_atom0, int slvmax,
+                                 FrameGeom g, int3 ncell, unsigned int* __restrict__ key, int* __restrict__ val) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= slvmax) return;
+  const int a = mol_atom0[k];
+  int c[3];
+  const int n[3] = {ncell.x, ncell.y, ncell.z};
+  for (int i = 0; i < 3; ++i) {
+    int ci = (int)(wrapped[3 * (size_t)a + i] * g.invL[i] * (double)n[i]);
+    c[i] = min(max(ci, 0), n[i] - 1);
+  }
+  key[k] = spread3(c[0]) | (spread3(c[1]) << 1) | (spread3(c[2]) << 2);
+  val[k] = k;
+}
+
+__global__ void frame_slot_kernel(const int* __restrict__ slot_mol, const int* __restrict__ mol_nsite,
+                                  const int* __restrict__ mol_species, const double* __restrict__ mol_qmol,
+                                  int slvmax, int* __restrict__ slot_nsite, int* __restrict__ slot_species,
+                                  double* __restrict__ slot_qmol) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= slvmax) return;
+  const int k = slot_mol[m];
+  slot_nsite[m] = mol_nsite[k];
+  slot_species[m] = mol_species[k];
+  slot_qmol[m] = mol_qmol[k];
+}
+
+struct SiteArgs {
+  const double* pos;      // raw sitepos
+  const double* wrapped;  // normalised sitepos
+  const int* slot_mol;
+  const int* slot_site;
+  const int* mol_atom0;
+  const int* mol_nsite;
+  const double* charge;
+  const int* ljtype;
+  int slvmax;
+  int mixed;
+  FrameGeom g;
+  SplineCoef sc;
+  int4* site_pos;
+  float4* site_rec;
+  int* site_grid;
+  double* site_x;
+  double* site_w;
+  double* site_q;
+  float* frame_scal;
+};
+
+// one thread per slot (molecule): its sites
+__global__ void frame_sites_kernel(SiteArgs A) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= A.slvmax) return;
+  const int k = A.slot_mol[m];
+  const int a0 = A.mol_atom0[k];
+  const int ns = A.mol_nsite[k];
+  const int s0 = A.slot_site[m];
+  const FrameGeom& g = A.g;
+  const int P = A.sc.order;
+  double rmax = 0.0;
+  double w0[3] = {A.wrapped[3 * (size_t)a0], A.wrapped[3 * (size_t)a0 + 1], A.wrapped[3 * (size_t)a0 + 2]};
+  for (int s = 0; s < ns; ++s) {
+    const int a = a0 + s;
+    const int idx = s0 + s;
+    double w[3] = {A.wrapped[3 * (size_t)a], A.wrapped[3 * (size_t)a + 1], A.wrapped[3 * (size_t)a + 2]};
+    // radius about the first site (minimum image)
+    double r2 = 0.0;
+    for (int i = 0; i < 3; ++i) {
+      const double h = 0.5 * g.L[i];
+      const double d = h - fabs(h - fabs(w[i] - w0[i]));
+      r2 += d * d;
+    }
+    rmax = fmax(rmax, sqrt(r2));
+    // calc_spline_molecule (recpcal.F90:408-442) on the raw coordinates
+    const double xst[3] = {A.pos[3 * (size_t)a], A.pos[3 * (size_t)a + 1], A.pos[3 * (size_t)a + 2]};
+    int rci[3];
+    double tfrac[3];
+    for (int kk = 0; kk < 3; ++kk) {
+      double factor = g.invcl[kk + 0] * xst[0] + g.invcl[kk + 3] * xst[1] + g.invcl[kk + 6] * xst[2];
+      factor = factor - floor(factor);
+      const double f2 = factor * (double)g.K[kk];
+      rci[kk] = (int)f2;
+      tfrac[kk] = f2 - (double)rci[kk];
+      if (!A.mixed) {
+        for (int spi = 0; spi < P; ++spi)
+          A.site_w[((size_t)idx * 3 + kk) * P + spi] = spline_value(A.sc, f2 - (double)(rci[kk] - spi));
+      }
+    }
+    A.site_grid[idx] = rci[0] | (rci[1] << kGridBits) | (rci[2] << (2 * kGridBits));
+    const double q = A.charge[a];
+    if (A.mixed) {
+      unsigned int X[3];
+      for (int i = 0; i < 3; ++i) {
+        const double u = w[i] * g.invL[i] * 4294967296.0;
+        X[i] = (unsigned int)(unsigned long long)llrint(u);
+      }
+      A.site_pos[idx] = make_int4((int)X[0], (int)X[1], (int)X[2], A.ljtype[a]);
+      A.site_rec[idx] = make_float4((float)tfrac[0], (float)tfrac[1], (float)tfrac[2], (float)q);
+    } else {
+      A.site_x[3 * (size_t)idx + 0] = w[0];
+      A.site_x[3 * (size_t)idx + 1] = w[1];
+      A.site_x[3 * (size_t)idx + 2] = w[2];
+      A.site_q[idx] = q;
+      A.site_pos[idx] = make_int4(0, 0, 0, A.ljtype[a]);
+    }
+  }
+  atomicMax((int*)&A.frame_scal[0], __float_as_int((float)rmax * 1.0001f + 1e-4f));
+}
+
+// recpcal_spline_greenfunc (recpcal.F90:111-152)
+__global__ void greenfunc_kernel(FrameGeom g, int order, const double* __restrict__ splfc, double screen,
+                                 double* __restrict__ engfac, float* __restrict__ engfac_f) {
+  const int H = g.K[0] / 2 + 1;
+  const size_t n = (size_t)H * g.K[1] * g.K[2];
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int rc1 = (int)(i % H);
+  const int rc2 = (int)((i / H) % g.K[1]);
+  const int rc3 = (int)(i / ((size_t)H * g.K[1]));
+  double factor = 0.0;
+  if (!(rc1 == 0 && rc2 == 0 && rc3 == 0)) {
+    const int rc[3] = {rc1, rc2, rc3};
+    double inm[3];
+    bool zero = false;
+    for (int m = 0; m < 3; ++m) {
+      const int rcimax = g.K[m];
+      if ((order % 2 == 1) && (2 * abs(rc[m]) == rcimax)) zero = true;
+      inm[m] = (rc[m] <= rcimax / 2) ? (double)rc[m] : (double)(rc[m] - rcimax);
+    }
+    if (!zero) {
+      double xst[3];
+      for (int m = 0; m < 3; ++m)
+        xst[m] = g.invcl[0 + 3 * m] * inm[0] + g.invcl[1 + 3 * m] * inm[1] + g.invcl[2 + 3 * m] * inm[2];
+      double rtp2 = xst[0] * xst[0] + xst[1] * xst[1] + xst[2] * xst[2];
+      const double chr = (kPi * kPi) * rtp2 / (screen * screen);
+      factor = exp(-chr) / rtp2 / kPi / g.volume;
+      rtp2 = splfc[rc1] * splfc[g.K[0] + rc2] * splfc[g.K[0] + g.K[1] + rc3];
+      factor = factor / rtp2;
+    }
+  }
+  engfac[i] = factor;
+  engfac_f[i] = (float)factor;
+}
+
+inline int nblk(size_t n, int t) { return (int)((n + t - 1) / t); }
+
+}  // namespace
+
+cudaError_t launch_frame_wrap(Engine& e) {
+  frame_wrap_kernel<<<nblk(e.numatm, 256), 256, 0, e.stream>>>(e.d_sitepos, e.numatm, e.geom, e.d_wrapped);
+  e.count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_frame_sort(Engine& e) {
+  int3 nc;
+  nc.x = std::max(1, std::min(1024, (int)(e.geom.L[0] / 4.0)));
+  nc.y = std::max(1, std::min(1024, (int)(e.geom.L[1] / 4.0)));
+  nc.z = std::max(1, std::min(1024, (int)(e.geom.L[2] / 4.0)));
+  frame_key_kernel<<<nblk(e.slvmax, 256), 256, 0, e.stream>>>(e.d_wrapped, e.d_mol_atom0, e.slvmax, e.geom, nc,
+                                                             e.d_sort_key, e.d_sort_val);
+  e.count_launch();
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return err;
+  size_t bytes = e.cub_tmp_bytes;
+  err = cub::DeviceRadixSort::SortPairs(e.d_cub_tmp, bytes, e.d_sort_key, e.d_sort_key_alt, e.d_sort_val,
+                                        e.d_slot_mol, e.slvmax, 0, 30, e.stream);
+  if (err != cudaSuccess) return err;
+  frame_slot_kernel<<<nblk(e.slvmax, 256), 256, 0, e.stream>>>(e.d_slot_mol, e.d_mol_nsite, e.d_mol_species,
+                                                              e.d_mol_qmol, e.slvmax, e.d_sort_val_alt,
+                                                              e.d_slot_species, e.d_slot_qmol);
+  e.count_launch();
+  err = cudaGetLastError();
+  if (err != cudaSuccess) return err;
+  bytes = e.cub_tmp_bytes;
+  // slot_site = exclusive scan of slot_nsite, with slot_site[slvmax] = total
+  err = cub::DeviceScan::ExclusiveSum(e.d_cub_tmp, bytes, e.d_sort_val_alt, e.d_slot_site, e.slvmax + 1, e.stream);
+  return err;
+}
+
+size_t frame_cub_bytes(int n) {
+  size_t a = 0, b = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, a, (unsigned int*)nullptr, (unsigned int*)nullptr, (int*)nullptr,
+                                  (int*)nullptr, n, 0, 30, (cudaStream_t)0);
+  cub::DeviceScan::ExclusiveSum(nullptr, b, (int*)nullptr, (int*)nullptr, n + 1, (cudaStream_t)0);
+  return std::max(a, b);
+}
+
+cudaError_t launch_frame_sites(Engine& e) {
+  cudaError_t err = cudaMemsetAsync(e.d_frame_scal, 0, sizeof(float) * 4, e.stream);
+  if (err != cudaSuccess) return err;
+  SiteArgs A{};
+  A.pos = e.d_sitepos;
+  A.wrapped = e.d_wrapped;
+  A.slot_mol = e.d_slot_mol;
+  A.slot_site = e.d_slot_site;
+  A.mol_atom0 = e.d_mol_atom0;
+  A.mol_nsite = e.d_mol_nsite;
+  A.charge = e.d_charge;
+  A.ljtype = e.d_ljtype;
+  A.slvmax = e.slvmax;
+  A.mixed = e.mixed ? 1 : 0;
+  A.g = e.geom;
+  A.sc = make_coef(e.P_order);
+  A.site_pos = e.d_site_pos;
+  A.site_rec = e.d_site_rec;
+  A.site_grid = e.d_site_grid;
+  A.site_x = e.d_site_x;
+  A.site_w = e.d_site_w;
+  A.site_q = e.d_site_q;
+  A.frame_scal = e.d_frame_scal;
+  frame_sites_kernel<<<nblk(e.slvmax, 128), 128, 0, e.stream>>>(A);
+  e.count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_greenfunc(Engine& e) {
+  const size_t n = e.grid_cplx();
+  greenfunc_kernel<<<nblk(n, 256), 256, 0, e.stream>>>(e.geom, e.P_order, e.d_splfc, e.P.screen, e.d_engfac,
+                                                       e.d_engfac_f);
+  e.count_launch();
+  return cudaGetLastError();
+}
+
+// host-side spline_value for the splfc tables (init_spline_axis, recpcal.F90:87-109)
+double host_spline_value(int order, double x) {
+  SplineCoef s = make_coef(order);
+  double f = 0.0;
+  if ((x > 0.0) && (x < (double)order)) {
+    const int k = (int)x;
+    for (int i = 0; i <= k; ++i) f = f + s.c[i] * ipow(x - (double)i, order - 1);
+  }
+  return f;
+}
+
+}  // namespace ermod

@@ -1,0 +1,605 @@
+// kernels_mol.cu -- per-molecule solute-solvent energies, fused with the binning.
+//
+// One thread owns one solvent molecule (a "slot" of the frame's spatially sorted
+// order) and G placements of the batch.  For each placement it computes
+//   recip   sum over its sites of q * sum_{c1,c2,c3} theta theta theta phi(g - c)
+//           (recpcal_energy, recpcal.F90:451-502), phi being the solute's PME potential;
+//   real    LJ (4 switch forms) + q q erfc(beta r) / r against every solute site within
+//           the cutoffs (get_pair_energy_block, realcal.F90:585-784), entered only when
+//           the molecule is inside the solute's bounding sphere + cutoff, so the cell
+//           list of the reference (realcal.F90:373-582) is not needed;
+//   resid   -pi Q_u Q_j / (beta^2 V) (residual_ene, engproc.F90:859-869);
+// then the FP64 total u = real + (resid + recip) (get_uv_energy, engproc.F90:736-753)
+// is binned exactly as getiduv/binsearch do (engproc.F90:927-1020), with integer keys
+// of the FP64 values, into a shared-memory histogram per placement (insdst,
+// engproc.F90:813-830).  Per-species sum/min/max go to per-block partials reduced in
+// a fixed tree, so every result is run-to-run deterministic.
+//
+// Mixed path: fixed-point positions, FP32 pair terms and grid gather, FP64 per-site and
+// per-molecule totals.  FP64 path: everything in FP64 with the reference's formulas.
+#include "engine.cuh"
+
+namespace ermod {
+
+struct MolArgs {
+  // frame, slot order
+  const int4* site_pos;
+  const float4* site_rec;
+  const int* site_grid;
+  const double* site_x;
+  const double* site_w;
+  const double* site_q;
+  const int* slot_mol;
+  const int* slot_site;
+  const int* slot_species;
+  const double* slot_qmol;
+  const float* frame_scal;
+  const int* mol_to_k;
+  int slvmax, nummol;
+  // LJ tables
+  const double* ljene;
+  const double* ljlensq;
+  int T;
+  // energy coordinate
+  const long long* uvkey;
+  const int* spec;  // [numslv][3]
+  int numslv, ermax, soln, mbin_mode;  // mbin_mode: 0 off, 1 error, 2 flag only
+  // interaction parameters
+  FrameGeom g;
+  int ljswitch;
+  double elecut, lwljcut, upljcut, screen;
+  double resid_fac;  // pi / screen^2 / volume
+  // batch
+  BatchArgs a;
+  int ntile;
+  DevStatus* status;
+};
+
+namespace {
+
+struct LjK {  // switching constants (realcal.F90:629-642, 888-904)
+  float lw2, up2, lw3, up3, lw6, up6, repA, repB, repC, attA, attB, attC, lw, up, ele2, den3;
+};
+
+template <typename T>
+__device__ __forceinline__ T lj_low(int sw, const LjK& k, T eps, T sg2, T dist) {
+  const T invr2 = sg2 / dist;
+  const T invr6 = invr2 * invr2 * invr2;
+  if (sw <= 1) return T(4) * eps * invr6 * (invr6 - T(1));
+  const T s6 = sg2 * sg2 * sg2;
+  if (sw == 2) {
+    const T vdwa = invr6 * invr6 - s6 * s6 / (T(k.lw6) * T(k.up6));
+    const T vdwb = invr6 - s6 / (T(k.lw3) * T(k.up3));
+    return T(4) * eps * (vdwa - vdwb);
+  }
+  const T vdwa = invr6 * invr6 - s6 * s6 * T(k.repC);
+  const T vdwb = invr6 - s6 * T(k.attC);
+  return T(4) * eps * (vdwa - vdwb);
+}
+
+template <typename T>
+__device__ __forceinline__ T lj_switch(int sw, const LjK& k, T eps, T sg2, T dist) {
+  const T invr2 = sg2 / dist;
+  const T invr6 = invr2 * invr2 * invr2;
+  if (sw == 0) {
+    const T dd = dist - T(k.up2), den = T(k.up2) - T(k.lw2);
+    return T(4) * eps * invr6 * (invr6 - T(1)) * (T(2) * dist + T(k.up2) - T(3) * T(k.lw2)) * (dd * dd) /
+           (den * den * den);
+  }
+  if (sw == 1) {
+    const T swfac = (sqrt(dist) - T(k.lw)) / (T(k.up) - T(k.lw));
+    const T s3 = swfac * swfac * swfac, s4 = s3 * swfac, s5 = s4 * swfac;
+    return T(4) * eps * invr6 * (invr6 - T(1)) * (T(1) - T(10) * s3 + T(15) * s4 - T(6) * s5);
+  }
+  const T s6 = sg2 * sg2 * sg2;
+  if (sw == 2) {
+    const T invr3 = sqrt(invr6), s3 = sqrt(s6);
+    const T a = invr6 - s6 / T(k.up6), b = invr3 - s3 / T(k.up3);
+    const T vdwa = T(k.up6) / (T(k.up6) - T(k.lw6)) * (a * a);
+    const T vdwb = T(k.up3) / (T(k.up3) - T(k.lw3)) * (b * b);
+    return T(4) * eps * (vdwa - vdwb);
+  }
+  const T swfac = sqrt(dist) - T(k.lw);
+  const T f3 = swfac * swfac * swfac, f4 = f3 * swfac;
+  const T vdwa = invr6 * invr6 - s6 * s6 * (T(k.repA) * f3 + T(k.repB) * f4 + T(k.repC));
+  const T vdwb = invr6 - s6 * (T(k.attA) * f3 + T(k.attB) * f4 + T(k.attC));
+  return T(4) * eps * (vdwa - vdwb);
+}
+
+// FP64 switching constants are recomputed in FP64 on the fly from the cutoffs.
+struct LjK64 {
+  double lw2, up2, lw3, up3, lw6, up6, repA, repB, repC, attA, attB, attC, lw, up, ele2;
+};
+
+__device__ __forceinline__ double lj_low64(int sw, const LjK64& k, double eps, double sg2, double dist) {
+  const double invr2 = sg2 / dist;
+  const double invr6 = invr2 * invr2 * invr2;
+  if (sw <= 1) return 4.0 * eps * invr6 * (invr6 - 1.0);
+  const double s6 = sg2 * sg2 * sg2;
+  if (sw == 2) {
+    const double vdwa = invr6 * invr6 - s6 * s6 / (k.lw6 * k.up6);
+    const double vdwb = invr6 - s6 / (k.lw3 * k.up3);
+    return 4.0 * eps * (vdwa - vdwb);
+  }
+  const double vdwa = invr6 * invr6 - s6 * s6 * k.repC;
+  const double vdwb = invr6 - s6 * k.attC;
+  return 4.0 * eps * (vdwa - vdwb);
+}
+
+__device__ __forceinline__ double lj_switch64(int sw, const LjK64& k, double eps, double sg2, double dist) {
+  const double invr2 = sg2 / dist;
+  const double invr6 = invr2 * invr2 * invr2;
+  if (sw == 0) {
+    const double dd = dist - k.up2, den = k.up2 - k.lw2;
+    return 4.0 * eps * invr6 * (invr6 - 1.0) * (2.0 * dist + k.up2 - 3.0 * k.lw2) * (dd * dd) / (den * den * den);
+  }
+  if (sw == 1) {
+    const double swfac = (sqrt(dist) - k.lw) / (k.up - k.lw);
+    const double s3 = swfac * swfac * swfac, s4 = s3 * swfac, s5 = s4 * swfac;
+    return 4.0 * eps * invr6 * (invr6 - 1.0) * (1.0 - 10.0 * s3 + 15.0 * s4 - 6.0 * s5);
+  }
+  const double s6 = sg2 * sg2 * sg2;
+  if (sw == 2) {
+    const double invr3 = sqrt(invr6), s3 = sqrt(s6);
+    const double a = invr6 - s6 / k.up6, b = invr3 - s3 / k.up3;
+    const double vdwa = k.up6 / (k.up6 - k.lw6) * (a * a);
+    const double vdwb = k.up3 / (k.up3 - k.lw3) * (b * b);
+    return 4.0 * eps * (vdwa - vdwb);
+  }
+  const double swfac = sqrt(dist) - k.lw;
+  const double f3 = swfac * swfac * swfac, f4 = f3 * swfac;
+  const double vdwa = invr6 * invr6 - s6 * s6 * (k.repA * f3 + k.repB * f4 + k.repC);
+  const double vdwb = invr6 - s6 * (k.attA * f3 + k.attB * f4 + k.attC);
+  return 4.0 * eps * (vdwa - vdwb);
+}
+
+__device__ __forceinline__ void gmx_params(int pw, double lw, double up, double& A, double& B, double& C) {
+  const double df = up - lw;
+  double upp2 = 1.0, upp = 1.0;
+  for (int i = 0; i < pw + 2; ++i) upp2 *= up;
+  for (int i = 0; i < pw; ++i) upp *= up;
+  A = -(double)pw * ((double)(pw + 4) * up - (double)(pw + 1) * lw) / (upp2 * (df * df)) / 3.0;
+  B = (double)pw * ((double)(pw + 3) * up - (double)(pw + 1) * lw) / (upp2 * (df * df * df)) / 4.0;
+  C = 1.0 / upp - A * (df * df * df) - B * (df * df * df * df);
+}
+
+__device__ __forceinline__ LjK64 make_k64(const MolArgs& A) {
+  LjK64 k;
+  k.lw = A.lwljcut;
+  k.up = A.upljcut;
+  k.lw2 = A.lwljcut * A.lwljcut;
+  k.up2 = A.upljcut * A.upljcut;
+  k.lw3 = A.lwljcut * A.lwljcut * A.lwljcut;
+  k.up3 = A.upljcut * A.upljcut * A.upljcut;
+  k.lw6 = k.lw3 * k.lw3;
+  k.up6 = k.up3 * k.up3;
+  gmx_params(12, A.lwljcut, A.upljcut, k.repA, k.repB, k.repC);
+  gmx_params(6, A.lwljcut, A.upljcut, k.attA, k.attB, k.attC);
+  k.ele2 = A.elecut * A.elecut;
+  return k;
+}
+
+__device__ __forceinline__ LjK to_f32(const LjK64& d) {
+  LjK k;
+  k.lw2 = (float)d.lw2; k.up2 = (float)d.up2; k.lw3 = (float)d.lw3; k.up3 = (float)d.up3;
+  k.lw6 = (float)d.lw6; k.up6 = (float)d.up6; k.repA = (float)d.repA; k.repB = (float)d.repB;
+  k.repC = (float)d.repC; k.attA = (float)d.attA; k.attB = (float)d.attB; k.attC = (float)d.attC;
+  k.lw = (float)d.lw; k.up = (float)d.up; k.ele2 = (float)d.ele2; k.den3 = 0.f;
+  return k;
+}
+
+// B-spline weights M_P(t + j), j = 0..P-1, by the stable Cox-de Boor recursion (FP32)
+template <int P>
+__device__ __forceinline__ void bspline_w(float t, float w[P]) {
+  w[0] = t;
+  w[1] = 1.f - t;
+#pragma unroll
+  for (int j = 2; j < P; ++j) w[j] = 0.f;
+#pragma unroll
+  for (int n = 3; n <= P; ++n) {
+    const float inv = 1.f / (float)(n - 1);
+#pragma unroll
+    for (int j = n - 1; j >= 0; --j) {
+      const float a = (j <= n - 2) ? w[j] : 0.f;
+      const float b = (j >= 1) ? w[j - 1] : 0.f;
+      w[j] = ((t + (float)j) * a + ((float)n - t - (float)j) * b) * inv;
+    }
+  }
+}
+
+__device__ __forceinline__ int wrapi(int x, int K) {
+  if (x < 0) x += K;
+  if (x >= K) x -= K;
+  return x;
+}
+
+// recip gather for one site, FP32
+template <int P>
+__device__ __forceinline__ float gather_site(const float* __restrict__ phi, const float4 rec, int gp, int K1, int K2,
+                                             int K3) {
+  float w1[P], w2[P], w3[P];
+  bspline_w<P>(rec.x, w1);
+  bspline_w<P>(rec.y, w2);
+  bspline_w<P>(rec.z, w3);
+  const int g1 = gp & 1023, g2 = (gp >> 10) & 1023, g3 = (gp >> 20) & 1023;
+  int x[P];
+#pragma unroll
+  for (int c = 0; c < P; ++c) x[c] = wrapi(g1 - c, K1);
+  float acc = 0.f;
+#pragma unroll
+  for (int c3 = 0; c3 < P; ++c3) {
+    const int z = wrapi(g3 - c3, K3);
+    float a3 = 0.f;
+#pragma unroll
+    for (int c2 = 0; c2 < P; ++c2) {
+      const int y = wrapi(g2 - c2, K2);
+      const float* row = phi + ((size_t)z * K2 + y) * K1;
+      float a2 = 0.f;
+#pragma unroll
+      for (int c1 = 0; c1 < P; ++c1) a2 = fmaf(w1[c1], __ldg(row + x[c1]), a2);
+      a3 = fmaf(w2[c2], a2, a3);
+    }
+    acc = fmaf(w3[c3], a3, acc);
+  }
+  return acc;
+}
+
+// fixed-tree block reductions over blockDim.x (power of two) entries
+__device__ __forceinline__ double block_sum(double* sm, double v) {
+  sm[threadIdx.x] = v;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) sm[threadIdx.x] += sm[threadIdx.x + st];
+    __syncthreads();
+  }
+  const double r = sm[0];
+  __syncthreads();
+  return r;
+}
+__device__ __forceinline__ long long block_min(long long* sm, long long v) {
+  sm[threadIdx.x] = v;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) sm[threadIdx.x] = min(sm[threadIdx.x], sm[threadIdx.x + st]);
+    __syncthreads();
+  }
+  const long long r = sm[0];
+  __syncthreads();
+  return r;
+}
+__device__ __forceinline__ long long block_max(long long* sm, long long v) {
+  sm[threadIdx.x] = v;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) sm[threadIdx.x] = max(sm[threadIdx.x], sm[threadIdx.x + st]);
+    __syncthreads();
+  }
+  const long long r = sm[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ double key_to_double(long long k) {
+  k = k ^ ((k >> 63) & 0x7fffffffffffffffll);
+  return __longlong_as_double(k);
+}
+
+constexpr long long kKeyPosInf = 0x7ff0000000000000ll;
+constexpr long long kKeyNegInf = (long long)0x800fffffffffffffull;  // ordered key of -inf
+
+template <bool MIXED, int P>
+__global__ void __launch_bounds__(256) mol_energy_kernel(MolArgs A) {
+  extern __shared__ int smem_hist[];  // [G][ermax]
+  __shared__ double sred[256];
+  __shared__ long long skey[256];
+  const int tile = blockIdx.x;
+  const int bgrp = blockIdx.y;
+  const BatchArgs& a = A.a;
+  const int G = a.G;
+  const int m = tile * blockDim.x + threadIdx.x;
+  const bool valid = m < A.slvmax;
+  for (int i = threadIdx.x; i < G * A.ermax; i += blockDim.x) smem_hist[i] = 0;
+  __syncthreads();
+
+  int k = -1, s0 = 0, ns = 0, species = 0;
+  double qmol = 0.0;
+  if (valid) {
+    k = A.slot_mol[m];
+    s0 = A.slot_site[m];
+    ns = A.slot_site[m + 1] - s0;
+    species = A.slot_species[m];
+    qmol = A.slot_qmol[m];
+  }
+  const FrameGeom& g = A.g;
+  const int K1 = g.K[0], K2 = g.K[1], K3 = g.K[2];
+  const size_t gridn = (size_t)K1 * K2 * K3;
+  const LjK64 k64 = make_k64(A);
+  const LjK k32 = to_f32(k64);
+  const double rc = fmax(A.elecut, A.upljcut);
+  const float mol_r = A.frame_scal[0];
+  int sp_off = 0, sp_n = 1, sp_soft = 1;
+  if (valid && species >= 1 && species <= A.numslv) {
+    sp_off = A.spec[3 * (species - 1)];
+    sp_n = A.spec[3 * (species - 1) + 1];
+    sp_soft = A.spec[3 * (species - 1) + 2];
+  }
+
+  for (int gi = 0; gi < G; ++gi) {
+    const int b = bgrp * G + gi;
+    if (b >= a.nb) break;  // uniform across the block
+    const int tg = a.tagslt[b] - 1;
+    const int kskip = (tg >= 0 && tg < A.nummol) ? A.mol_to_k[tg] : -2;
+    const bool active = valid && (k != kskip);
+    double u = 0.0;
+    if (active) {
+      // ---- reciprocal part ----
+      double recip = 0.0;
+      if (MIXED) {
+        const float* phi = a.phi + (size_t)b * gridn;
+        for (int s = 0; s < ns; ++s) {
+          const float4 rec = A.site_rec[s0 + s];
+          const int gp = A.site_grid[s0 + s];
+          const float acc = gather_site<P>(phi, rec, gp, K1, K2, K3);
+          recip += (double)(rec.w * acc);
+        }
+      } else {
+        const double* phi = a.phi64 + (size_t)b * gridn;
+        for (int s = 0; s < ns; ++s) {
+          const int idx = s0 + s;
+          const double chr = A.site_q[idx];
+          const double* w = A.site_w + (size_t)idx * 3 * P;
+          const int gp = A.site_grid[idx];
+          const int g1 = gp & 1023, g2 = (gp >> 10) & 1023, g3 = (gp >> 20) & 1023;
+          for (int c3 = 0; c3 < P; ++c3) {
+            const double fac1 = chr * w[2 * P + c3];
+            const int z = wrapi(g3 - c3, K3);
+            for (int c2 = 0; c2 < P; ++c2) {
+              const double fac2 = fac1 * w[P + c2];
+              const int y = wrapi(g2 - c2, K2);
+              const double* row = phi + ((size_t)z * K2 + y) * K1;
+              for (int c1 = 0; c1 < P; ++c1) {
+                const double fac3 = fac2 * w[c1];
+                recip = recip + fac3 * row[wrapi(g1 - c1, K1)];
+              }
+            }
+          }
+        }
+      }
+      // ---- real space ----
+      double real = 0.0;
+      const int nu = a.u_nsite[b];
+      const size_t ub = (size_t)b * kMaxSoluteSites;
+      const float rcut = (float)rc + a.u_radius[b] + mol_r;
+      if (MIXED) {
+        const int4 p0 = A.site_pos[s0];
+        const int4 u0 = a.u_pos[ub];
+        const float dx = (float)(int)((unsigned)p0.x - (unsigned)u0.x) * (float)g.fx_scale[0];
+        const float dy = (float)(int)((unsigned)p0.y - (unsigned)u0.y) * (float)g.fx_scale[1];
+        const float dz = (float)(int)((unsigned)p0.z - (unsigned)u0.z) * (float)g.fx_scale[2];
+        if (dx * dx + dy * dy + dz * dz <= rcut * rcut) {
+          const float beta = (float)A.screen;
+          for (int su = 0; su < nu; ++su) {
+            const int4 up = a.u_pos[ub + su];
+            const float qu = (float)a.u_q[ub + su];
+            float e = 0.f;
+            for (int s = 0; s < ns; ++s) {
+              const int4 vp = A.site_pos[s0 + s];
+              const float ex = (float)(int)((unsigned)vp.x - (unsigned)up.x) * (float)g.fx_scale[0];
+              const float ey = (float)(int)((unsigned)vp.y - (unsigned)up.y) * (float)g.fx_scale[1];
+              const float ez = (float)(int)((unsigned)vp.z - (unsigned)up.z) * (float)g.fx_scale[2];
+              const float r2 = ex * ex + ey * ey + ez * ez;
+              const double ljeps = A.ljene[vp.w + A.T * up.w];
+              if (ljeps > 0) {
+                const float sg2 = (float)A.ljlensq[vp.w + A.T * up.w];
+                if (r2 <= k32.lw2)
+                  e += lj_low<float>(A.ljswitch, k32, (float)ljeps, sg2, r2);
+                else if (r2 <= k32.up2)
+                  e += lj_switch<float>(A.ljswitch, k32, (float)ljeps, sg2, r2);
+              }
+              if (r2 <= k32.ele2) {
+                const float r = sqrtf(r2);
+                e += qu * A.site_rec[s0 + s].w * erfcf(beta * r) / r;
+              }
+            }
+            real += (double)e;
+          }
+        }
+      } else {
+        double d0 = 0.0;
+        for (int i = 0; i < 3; ++i) {
+          const double h = 0.5 * g.L[i];
+          const double d = h - fabs(h - fabs(A.site_x[3 * (size_t)s0 + i] - a.u_x[ub * 3 + i]));
+          d0 += d * d;
+        }
+        if (d0 <= (double)rcut * (double)rcut) {
+          for (int su = 0; su < nu; ++su) {
+            const double* ux = a.u_x + (ub + su) * 3;
+            const double qu = a.u_q[ub + su];
+            const int tu = a.u_pos[ub + su].w;
+            for (int s = 0; s < ns; ++s) {
+              const int idx = s0 + s;
+              double dist = 0.0;
+              for (int i = 0; i < 3; ++i) {
+                const double h = 0.5 * g.L[i];
+                const double d = h - fabs(h - fabs(A.site_x[3 * (size_t)idx + i] - ux[i]));
+                dist += d * d;
+              }
+              const int tv = A.site_pos[idx].w;
+              const double ljeps = A.ljene[tv + A.T * tu];
+              if (ljeps > 0) {
+                const double sg2 = A.ljlensq[tv + A.T * tu];
+                if (dist <= k64.lw2)
+                  real += lj_low64(A.ljswitch, k64, ljeps, sg2, dist);
+                else if (dist <= k64.up2)
+                  real += lj_switch64(A.ljswitch, k64, ljeps, sg2, dist);
+              }
+              if (dist <= k64.ele2) {
+                const double r = sqrt(dist);
+                real += qu * A.site_q[idx] * (1.0 - erf(A.screen * r)) / r;
+              }
+            }
+          }
+        }
+      }
+      // residual_ene + assembly (engproc.F90:741-752)
+      double epcl;
+      if (MIXED)
+        epcl = A.resid_fac * a.u_qmol[b] * qmol;
+      else
+        epcl = kPi * a.u_qmol[b] * qmol / A.screen / A.screen / g.volume;
+      double pairep = -epcl;
+      pairep = pairep + recip;
+      u = real + pairep;
+      // ---- getiduv / binsearch ----
+      int code = 0;
+      int ret = 0;
+      if (species < 1 || species > A.numslv) {
+        code = ERMOD_E_ENG_CNS;
+      } else if (u != u) {
+        code = ERMOD_E_ENG_MIN;
+      } else {
+        const long long ku = ordered_key(u);
+        const long long* keys = A.uvkey + sp_off;
+        int lo = 0, hi = sp_n;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (__ldg(keys + mid) < ku)
+            lo = mid + 1;
+          else
+            hi = mid;
+        }
+        ret = lo;
+        if (ret <= 0)
+          code = ERMOD_E_ENG_MIN;
+        else if (A.soln && ret > sp_soft)
+          code = ERMOD_E_ENG_SFT;
+        else if (ret == sp_n && u < 1.0e3 && A.mbin_mode != 0) {
+          if (A.mbin_mode == 1)
+            code = ERMOD_W_MBIN;
+          else
+            atomicOr(&A.status->mbin_hit, 1);
+        }
+      }
+      if (code) {
+        atomicMin(&A.status->err_key, make_err_key(a.b0 + b, k + 1, code));
+      } else {
+        const int bin = sp_off + ret - 1;
+        int* h = smem_hist + gi * A.ermax;
+        const unsigned am = __activemask();
+        const unsigned peers = __match_any_sync(am, bin);
+        const int leader = __ffs(peers) - 1;
+        if ((threadIdx.x & 31) == leader) atomicAdd(&h[bin], __popc(peers));
+      }
+      if (a.uvengy_out) a.uvengy_out[(size_t)(a.b0 + b) * (A.slvmax + 1) + k + 1] = u;
+    } else if (valid && a.uvengy_out) {
+      a.uvengy_out[(size_t)(a.b0 + b) * (A.slvmax + 1) + k + 1] = 0.0;
+    }
+    // per-species partials {sum, min, max} of this block (fixed-tree reductions)
+    for (int sp = 1; sp <= A.numslv; ++sp) {
+      const bool mine = active && species == sp;
+      const double s = block_sum(sred, mine ? u : 0.0);
+      const long long mn = block_min(skey, mine ? ordered_key(u) : kKeyPosInf);
+      const long long mx = block_max(skey, mine ? ordered_key(u) : kKeyNegInf);
+      if (threadIdx.x == 0) {
+        double* pt = a.part + (((size_t)b * A.ntile + tile) * A.numslv + (sp - 1)) * 3;
+        pt[0] = s;
+        pt[1] = key_to_double(mn);
+        pt[2] = key_to_double(mx);
+      }
+    }
+  }
+  __syncthreads();
+  // flush the block's histograms
+  for (int gi = 0; gi < G; ++gi) {
+    const int b = bgrp * G + gi;
+    if (b >= a.nb) break;
+    const int* h = smem_hist + gi * A.ermax;
+    int* out = a.hist + (size_t)b * A.ermax;
+    for (int i = threadIdx.x; i < A.ermax; i += blockDim.x) {
+      const int c = h[i];
+      if (c) atomicAdd(out + i, c);
+    }
+  }
+}
+
+template <bool MIXED>
+cudaError_t launch_p(Engine& e, const MolArgs& A, dim3 grid, size_t smem) {
+  switch (e.P_order) {
+    case 4:
+      mol_energy_kernel<MIXED, 4><<<grid, 256, smem, e.stream>>>(A);
+      break;
+    case 6:
+      mol_energy_kernel<MIXED, 6><<<grid, 256, smem, e.stream>>>(A);
+      break;
+    case 8:
+      mol_energy_kernel<MIXED, 8><<<grid, 256, smem, e.stream>>>(A);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+template <bool MIXED>
+cudaError_t set_smem_attr(size_t smem) {
+  cudaError_t err = cudaSuccess;
+  err = cudaFuncSetAttribute(mol_energy_kernel<MIXED, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  err = cudaFuncSetAttribute(mol_energy_kernel<MIXED, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  return cudaFuncSetAttribute(mol_energy_kernel<MIXED, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+}  // namespace
+
+cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
+  MolArgs A{};
+  A.site_pos = e.d_site_pos;
+  A.site_rec = e.d_site_rec;
+  A.site_grid = e.d_site_grid;
+  A.site_x = e.d_site_x;
+  A.site_w = e.d_site_w;
+  A.site_q = e.d_site_q;
+  A.slot_mol = e.d_slot_mol;
+  A.slot_site = e.d_slot_site;
+  A.slot_species = e.d_slot_species;
+  A.slot_qmol = e.d_slot_qmol;
+  A.frame_scal = e.d_frame_scal;
+  A.mol_to_k = e.d_mol_to_k;
+  A.slvmax = e.slvmax;
+  A.nummol = e.nummol;
+  A.ljene = e.d_ljene;
+  A.ljlensq = e.d_ljlensq;
+  A.T = e.ljtype_max;
+  A.uvkey = e.d_uvkey;
+  A.spec = e.d_spec;
+  A.numslv = e.numslv;
+  A.ermax = e.ermax;
+  A.soln = (e.P.slttype == 1) ? 1 : 0;
+  A.mbin_mode = e.warn_bin_firsttime ? (e.P.force_calculation ? 2 : 1) : 0;
+  A.g = e.geom;
+  A.ljswitch = e.P.ljswitch;
+  A.elecut = e.P.elecut;
+  A.lwljcut = e.P.lwljcut;
+  A.upljcut = e.P.upljcut;
+  A.screen = e.P.screen;
+  A.resid_fac = kPi / e.P.screen / e.P.screen / e.geom.volume;
+  A.a = a;
+  A.ntile = e.ntile;
+  A.status = e.d_status;
+  const size_t smem = sizeof(int) * (size_t)a.G * e.ermax;
+  static bool attr_set[2] = {false, false};
+  static size_t attr_smem[2] = {0, 0};
+  const int mi = e.mixed ? 1 : 0;
+  if (!attr_set[mi] || attr_smem[mi] < smem) {
+    cudaError_t err = e.mixed ? set_smem_attr<true>(smem) : set_smem_attr<false>(smem);
+    if (err != cudaSuccess) return err;
+    attr_set[mi] = true;
+    attr_smem[mi] = smem;
+  }
+  dim3 grid(e.ntile, (a.nb + a.G - 1) / a.G);
+  e.count_launch();
+  return e.mixed ? launch_p<true>(e, A, grid, smem) : launch_p<false>(e, A, grid, smem);
+}
+
+}  // namespace ermod

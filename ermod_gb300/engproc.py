@@ -1,0 +1,167 @@
+"""Host-side front end of the GB300 path, shaped like ERmod's engproc module.
+
+``EnergyRepresentation`` holds one ``ermod_ctx`` and exposes the reference's per-frame
+protocol (engproc.F90): ``engclear`` (:276-288), ``engconst`` = ``frame`` (:355-383)
++ ``placements`` (:388-392), and the accumulators that ``engstore`` (:451-659) turns
+into engsln/engref/corref.  Every call goes through the C ABI of
+``libermod_gb300.so``; a nonzero status raises ``ErmodError`` whose ``name`` is the
+reference's ``halt_with_error`` identity (``eng_min``, ``eng_sft``, ...).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import ErmodError, check  # noqa: F401
+
+PARAM_KEYS = ("slttype", "estype", "ljswitch", "splodr", "ms1max", "ms2max", "ms3max", "wgtslf", "corrcal",
+              "selfcal", "force_calculation", "elecut", "lwljcut", "upljcut", "screen", "temp",
+              "block_threshold")
+
+
+class EnergyRepresentation:
+    def __init__(self, params: dict, topo: dict, bins: dict, precision: str = "mixed", device: int = 0,
+                 batch: int = 0, count_mirror: bool = False):
+        L = _lib.load()
+        p = _lib.Params()
+        L.ermod_default_params(C.byref(p))
+        for k in PARAM_KEYS:
+            if k in params:
+                setattr(p, k, params[k])
+        p.cltype = 2
+        p.precision = _lib.PRECISION_MIXED if precision == "mixed" else _lib.PRECISION_FP64
+        p.batch = int(batch)
+        p.count_mirror = 1 if count_mirror else 0
+        self.params = dict(params)
+        self.precision = precision
+        self.ctx = C.c_void_p()
+        check(L.ermod_create(C.byref(p), int(device), C.byref(self.ctx)), "ermod_create")
+        self.set_topology(topo)
+        self.set_bins(bins)
+
+    # -------------------------------------------------------------------------
+    def close(self):
+        if self.ctx:
+            _lib.load().ermod_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_topology(self, topo: dict):
+        L = _lib.load()
+        self._keep = dict(
+            mbi=np.ascontiguousarray(topo["mol_begin_index"], np.int32),
+            sluvid=np.ascontiguousarray(topo["sluvid"], np.int32),
+            uvspec=np.ascontiguousarray(topo["uvspec"], np.int32),
+            charge=np.ascontiguousarray(topo["charge"], np.float64),
+            ljtype=np.ascontiguousarray(topo["ljtype"], np.int32),
+            ljene=np.asfortranarray(topo["ljene_mat"], np.float64).ravel(order="F").copy(),
+            ljlensq=np.asfortranarray(topo["ljlensq_mat"], np.float64).ravel(order="F").copy())
+        k = self._keep
+        check(L.ermod_set_topology(self.ctx, int(topo["nummol"]), int(topo["numatm"]), _lib.ip(k["mbi"]),
+                                   _lib.ip(k["sluvid"]), _lib.ip(k["uvspec"]), _lib.dp(k["charge"]),
+                                   _lib.ip(k["ljtype"]), int(topo["ljtype_max"]), _lib.dp(k["ljene"]),
+                                   _lib.dp(k["ljlensq"])), "ermod_set_topology")
+        self.topo = topo
+
+    def set_bins(self, bins: dict):
+        L = _lib.load()
+        uvmax = np.ascontiguousarray(bins["uvmax"], np.int32)
+        uvsoft = np.ascontiguousarray(bins["uvsoft"], np.int32)
+        uvcrd = np.ascontiguousarray(bins["uvcrd"], np.float64)
+        escrd = np.ascontiguousarray(bins["escrd"], np.float64)
+        check(L.ermod_set_bins(self.ctx, len(uvmax), _lib.ip(uvmax), _lib.ip(uvsoft), _lib.dp(uvcrd),
+                               int(bins["esmax"]), _lib.dp(escrd)), "ermod_set_bins")
+        self.bins = bins
+        s = self.sizes()
+        self.slvmax, self.ermax, self.esmax, self.numslv = s
+
+    def sizes(self):
+        a, b, c, d = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        check(_lib.load().ermod_get_sizes(self.ctx, C.byref(a), C.byref(b), C.byref(c), C.byref(d)), "sizes")
+        return a.value, b.value, c.value, d.value
+
+    # ---- engconst --------------------------------------------------------------
+    def frame(self, sitepos: np.ndarray, cell: np.ndarray, stat_weight_system: float = 1.0):
+        sp = np.ascontiguousarray(sitepos, np.float64)
+        cl = np.asfortranarray(cell, np.float64).ravel(order="F").copy()
+        check(_lib.load().ermod_frame(self.ctx, _lib.dp(sp), _lib.dp(cl), float(stat_weight_system)),
+              "ermod_frame")
+
+    def placements(self, tagslt, solute_sitepos=None, stat_weight_solute=None, want_uvengy=False,
+                   want_flceng=False):
+        tag = np.ascontiguousarray(np.atleast_1d(tagslt), np.int32)
+        n = len(tag)
+        sx = None if solute_sitepos is None else np.ascontiguousarray(solute_sitepos, np.float64)
+        sw = None if stat_weight_solute is None else np.ascontiguousarray(stat_weight_solute, np.float64)
+        uv = np.zeros((n, self.slvmax + 1)) if want_uvengy else None
+        fl = np.zeros((n, self.numslv)) if want_flceng else None
+        check(_lib.load().ermod_placements(self.ctx, n, _lib.ip(tag), _lib.dp(sx), _lib.dp(sw), _lib.dp(uv),
+                                           _lib.dp(fl)), "ermod_placements")
+        return dict(uvengy=uv, flceng=fl)
+
+    def engconst(self, sitepos, cell, tagslt, solute_sitepos=None, stat_weight_system=1.0, **kw):
+        self.frame(sitepos, cell, stat_weight_system)
+        return self.placements(tagslt, solute_sitepos, **kw)
+
+    def engclear(self):
+        check(_lib.load().ermod_clear(self.ctx), "ermod_clear")
+
+    def accum(self, with_count: bool = False):
+        E, S, N = self.ermax, self.esmax, self.numslv
+        edens = np.zeros(E)
+        ecorr = np.zeros(E * E) if self.params.get("corrcal") else None
+        cnt = np.zeros(E * E, np.int64) if with_count else None
+        eself = np.zeros(max(S, 1))
+        slnuv = np.zeros(N)
+        mn, mx = np.zeros(N + 1), np.zeros(N + 1)
+        sc = np.zeros(5)
+        check(_lib.load().ermod_get_accum(self.ctx, _lib.dp(edens), _lib.dp(ecorr), _lib.dp(eself), _lib.dp(slnuv),
+                                          _lib.dp(mn), _lib.dp(mx), _lib.dp(sc), _lib.i64p(cnt)), "ermod_get_accum")
+        return dict(edens=edens, ecorr=None if ecorr is None else ecorr.reshape(E, E, order="F"),
+                    ecorr_count=None if cnt is None else cnt.reshape(E, E, order="F"), eself=eself[:S],
+                    slnuv=slnuv, minuv=mn, maxuv=mx, engnorm=sc[0], engsmpl=sc[1], avslf=sc[2], voffset=sc[3],
+                    voffset_initialized=bool(sc[4]))
+
+    def error_info(self):
+        p, m, e = C.c_int(), C.c_int(), C.c_double()
+        check(_lib.load().ermod_error_info(self.ctx, C.byref(p), C.byref(m), C.byref(e)), "error_info")
+        return p.value, m.value, e.value
+
+    # ---- instrumentation ---------------------------------------------------------
+    def timing(self, on: bool = True):
+        check(_lib.load().ermod_timing_enable(self.ctx, 1 if on else 0), "timing")
+
+    def timing_reset(self):
+        check(_lib.load().ermod_timing_reset(self.ctx), "timing_reset")
+
+    def timing_get(self):
+        ms = (C.c_double * 16)()
+        names = (C.c_char_p * 16)()
+        n = C.c_int()
+        launches = C.c_int64()
+        check(_lib.load().ermod_timing_get(self.ctx, 16, ms, names, C.byref(n), C.byref(launches)), "timing_get")
+        return {names[i].decode(): ms[i] for i in range(n.value)}, launches.value
+
+    def set_stream(self, stream_handle: int):
+        check(_lib.load().ermod_set_stream(self.ctx, C.c_void_p(stream_handle)), "set_stream")
+
+    # ---- device-resident inputs (pointers as ints) ----------------------------------
+    def frame_device(self, sitepos_ptr: int, cell, stat_weight_system: float = 1.0):
+        cl = np.asfortranarray(cell, np.float64).ravel(order="F").copy()
+        check(_lib.load().ermod_frame_device(self.ctx, C.c_void_p(sitepos_ptr), _lib.dp(cl),
+                                             float(stat_weight_system)), "ermod_frame_device")
+
+    def placements_device(self, n: int, tag_ptr: int, sol_ptr: int = 0, sws_ptr: int = 0):
+        check(_lib.load().ermod_placements_device(self.ctx, int(n), C.c_void_p(tag_ptr),
+                                                  C.c_void_p(sol_ptr or None), C.c_void_p(sws_ptr or None),
+                                                  None, None), "ermod_placements_device")
+
+    def sync(self):
+        check(_lib.load().ermod_sync(self.ctx), "ermod_sync")

@@ -1,0 +1,192 @@
+/*
+ * ermod_gpu.h -- C ABI of the GB300 (sm_103a) energy-representation path.
+ *
+ * The entry points replace the body of ERmod's per-frame driver `engconst`
+ * (engproc.F90:301-448) from the PME set-up (engproc.F90:355-383) through the
+ * placement loop (engproc.F90:388-392: get_uv_energy + update_histogram).  A Fortran
+ * host keeps enganal/setconf/insertion/engstore, the namelists and the output files,
+ * and calls these functions through ISO_C_BINDING (include/ermod_gpu.f90).
+ *
+ * Conventions (those of the Fortran state in engmain.F90:252-301):
+ *   - every array argument is caller-owned HOST memory unless the function name ends
+ *     in `_device`; the library copies what it needs and owns its device memory;
+ *   - arrays are column-major; index VALUES held in arrays are 1-based
+ *     (mol_begin_index, ljtype, tagslt);
+ *   - coordinates in Angstrom, energies in kcal/mol, charges already multiplied by
+ *     18.22261721 (setconf.F90:829), temperature as kT in kcal/mol (setconf.F90:313);
+ *   - every function returns an ermod_status (0 = success); nothing aborts or traps.
+ * Threading: one context per host thread and device; a context is not reentrant.
+ */
+#ifndef ERMOD_GPU_H
+#define ERMOD_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ERMOD_ABI_VERSION 1
+
+/* Status codes.  The 1xx codes map one-to-one to ERmod's halt_with_error / warning
+ * identities (mpiproc.F90:203-264) so that a Fortran wrapper can call
+ * halt_with_error itself with the reference's message. */
+typedef enum ermod_status {
+  ERMOD_OK = 0,
+  ERMOD_E_ENG_MIN = 101,   /* 'eng_min': energy at or below the first bin edge (engproc.F90:992-995) */
+  ERMOD_E_ENG_SFT = 102,   /* 'eng_sft': solution-mode energy beyond the soft region (engproc.F90:999-1005) */
+  ERMOD_E_ENG_BUG = 103,   /* 'eng_bug' (engproc.F90:975,986,997) */
+  ERMOD_E_ENG_CNS = 104,   /* 'eng_cns': solvent with uvspec <= 0 (engproc.F90:817) */
+  ERMOD_E_RCP_CNS = 105,   /* 'rcp_cns' (recpcal.F90:335,474) */
+  ERMOD_E_RCP_FST = 106,   /* 'rcp_fst': the solute is a solvent (recpcal.F90:469) */
+  ERMOD_W_MBIN = 110,      /* 'mbin' warning without force_calculation (engproc.F90:1010-1015) */
+  ERMOD_E_PARAM = 120,     /* invalid argument or call order */
+  ERMOD_E_NONCUBOID = 121, /* non-cuboid cell: the reference stops (realcal.F90:859-866) */
+  ERMOD_E_UNSUPPORTED = 122, /* a mode the GPU path does not implement (cltype != PME) */
+  ERMOD_E_CUDA = 130,      /* CUDA runtime error (see ermod_last_error_string) */
+  ERMOD_E_CUFFT = 131,     /* cuFFT error */
+  ERMOD_E_NOMEM = 132,     /* device allocation failed */
+  ERMOD_E_DEVICE = 133     /* device-side check failed (index out of range) */
+} ermod_status;
+
+/* Arithmetic of the per-placement path. */
+enum {
+  ERMOD_PRECISION_FP64 = 0,  /* plain path: FP64 everywhere, spread + D2Z/Z2D, one placement at a time */
+  ERMOD_PRECISION_MIXED = 1  /* batched path: FP32 grids and pair terms, FP64 totals and sums */
+};
+
+/* &ene_param subset that the path reads (engmain.F90:331-343, defaults setconf.F90:188-303). */
+typedef struct ermod_params {
+  int32_t abi_version;       /* ERMOD_ABI_VERSION */
+  int32_t slttype;           /* 1 solution, 2 reference rigid, 3 reference flexible */
+  int32_t estype;            /* 1 NVT, 2 NPT (volcorrect, engproc.F90:871-887) */
+  int32_t cltype;            /* must be 2 (PME) */
+  int32_t ljswitch;          /* 0 CHARMM pot, 1 GROMACS pot, 2 CHARMM force, 3 GROMACS force */
+  int32_t splodr;            /* PME spline order (4, 6 or 8) */
+  int32_t ms1max, ms2max, ms3max; /* PME grid */
+  int32_t wgtslf;            /* weighting by the solute self energy */
+  int32_t corrcal;           /* accumulate ecorr */
+  int32_t selfcal;           /* accumulate eself */
+  int32_t force_calculation; /* continue after the 'mbin' warning */
+  int32_t precision;         /* ERMOD_PRECISION_* */
+  int32_t batch;             /* placements per batch in the mixed path (0 = automatic) */
+  int32_t count_mirror;      /* also keep an exact int64 unweighted ecorr count matrix */
+  double elecut, lwljcut, upljcut, screen;
+  double temp;               /* kT in kcal/mol */
+  double block_threshold;    /* accepted for interface parity; the GPU path needs no cell list */
+} ermod_params;
+
+typedef struct ermod_ctx ermod_ctx;
+
+/* Fills p with the reference defaults for a PME run (setconf.F90:188-303). */
+void ermod_default_params(ermod_params* p);
+
+/* Context on CUDA device `device`.  Replaces recpcal_init's allocations
+ * (recpcal.F90:42-85); the cuFFT plans are created here. */
+int ermod_create(const ermod_params* p, int device, ermod_ctx** out);
+int ermod_destroy(ermod_ctx* ctx);
+
+/* Optional: run all work of this context on an existing cudaStream_t. */
+int ermod_set_stream(ermod_ctx* ctx, void* cuda_stream);
+
+/* Topology (engmain.F90:252-277).  mol_begin_index has nummol+1 entries (1-based),
+ * sluvid/uvspec one per molecule, charge/ljtype one per site, ljene_mat and
+ * ljlensq_mat are ljtype_max x ljtype_max column-major (setconf.F90:720-823). */
+int ermod_set_topology(ermod_ctx* ctx, int nummol, int numatm, const int* mol_begin_index,
+                       const int* sluvid, const int* uvspec, const double* charge,
+                       const int* ljtype, int ljtype_max, const double* ljene_mat,
+                       const double* ljlensq_mat);
+
+/* Energy coordinate (engproc.F90:122-237, built by the host's enginit so that the
+ * edges are the host's own): uvmax/uvsoft per solvent species, uvcrd(ermax),
+ * escrd(esmax). */
+int ermod_set_bins(ermod_ctx* ctx, int numslv, const int* uvmax, const int* uvsoft,
+                   const double* uvcrd, int esmax, const double* escrd);
+
+/* engconst prologue: cell inverse (engproc.F90:898-919), Green function when the
+ * cell changed (recpcal.F90:111-152), solvent splines (recpcal.F90:328-340,408-442)
+ * and the frame's solvent layout.  sitepos is (3, numatm), cell (3,3). */
+int ermod_frame(ermod_ctx* ctx, const double* sitepos, const double* cell,
+                double stat_weight_system);
+int ermod_frame_device(ermod_ctx* ctx, const double* sitepos_device, const double* cell,
+                       double stat_weight_system);
+
+/* The placement loop (engproc.F90:388-392).  Placement p uses solute molecule
+ * tagslt[p] (1-based).  solute_sitepos (3, nsite, nplace) holds the inserted solute's
+ * coordinates (reference-solvent mode, insertion.F90:44-101) or is NULL (solution mode:
+ * the frame's coordinates).  stat_weight_solute (nplace) may be NULL (all 1).
+ * Optional outputs: uvengy_out (0:slvmax, nplace) -- the per-molecule energies of
+ * get_uv_energy in tagpt order, uvengy(0) the solute self energy -- and
+ * flceng_out (numslv, nplace).  Results accumulate into the context's
+ * accumulators.  On an error status the accumulators keep the state of the last
+ * complete batch and ermod_error_info tells which placement/molecule failed. */
+int ermod_placements(ermod_ctx* ctx, int nplace, const int* tagslt, const double* solute_sitepos,
+                     const double* stat_weight_solute, double* uvengy_out, double* flceng_out);
+/* Same with tagslt/solute_sitepos/stat_weight_solute in device memory; the optional
+ * outputs are device pointers too.  Returns without synchronising: the status of the
+ * queued work is reported by the next ermod_sync. */
+int ermod_placements_device(ermod_ctx* ctx, int nplace, const int* tagslt_device,
+                            const double* solute_sitepos_device,
+                            const double* stat_weight_solute_device, double* uvengy_out_device,
+                            double* flceng_out_device);
+/* Waits for queued work and returns its status. */
+int ermod_sync(ermod_ctx* ctx);
+
+/* engclear (engproc.F90:276-288). */
+int ermod_clear(ermod_ctx* ctx);
+
+/* Accumulators (engmain.F90:283-301), copied to host.  Any pointer may be NULL.
+ * edens(ermax), ecorr(ermax,ermax) column-major, eself(esmax), slnuv(numslv),
+ * minuv/maxuv(0:numslv), scalars[5] = {engnorm, engsmpl, avslf, voffset,
+ * voffset_initialized}; ecorr_count(ermax,ermax) is the unweighted int64 mirror
+ * sum_p insdst_p(i) insdst_p(j) (needs count_mirror). */
+int ermod_get_accum(ermod_ctx* ctx, double* edens, double* ecorr, double* eself, double* slnuv,
+                    double* minuv, double* maxuv, double* scalars, int64_t* ecorr_count);
+
+/* Sizes known to the context: slvmax (physical molecules), ermax, esmax, numslv. */
+int ermod_get_sizes(const ermod_ctx* ctx, int* slvmax, int* ermax, int* esmax, int* numslv);
+
+/* Where the last error happened: placement index within the call, 1-based tagpt
+ * position of the molecule (0 = the solute self energy) and its energy. */
+int ermod_error_info(const ermod_ctx* ctx, int* placement, int* molecule, double* energy);
+
+/* Per-phase device time (ms) accumulated since ermod_timing_reset with timing on;
+ * names[i] are static strings.  Kernel launches issued by this library since the
+ * last reset go to *launches. */
+int ermod_timing_enable(ermod_ctx* ctx, int on);
+int ermod_timing_reset(ermod_ctx* ctx);
+int ermod_timing_get(ermod_ctx* ctx, int max_phases, double* ms, const char** names, int* nphases,
+                     int64_t* launches);
+
+/* Last CUDA/cuFFT error message of this thread. */
+const char* ermod_last_error_string(void);
+const char* ermod_status_string(int status);
+
+/* ---- host-side set-up helpers (the reference's own set-up arithmetic) -------------- */
+
+/* enginit's energy coordinate for one species (engproc.F90:163-218).
+ * hist = {ecdmin, ecfmns, ecdcen, eccore, ecdmax, eclbin, ecfbin, ec0bin, finfac}.
+ * ercrd must hold `large` doubles; writes ercrd[0..pemax-1]. */
+int ermod_enginit_species(const double* hist, int pecore, int large, double* ercrd, int* pemax,
+                          int* pesoft);
+/* getscrn (setconf.F90:515-535): Ewald screening parameter from ewtoler. */
+double ermod_getscrn(double ewtoler, double elecut, int distance_form);
+/* LJ type table of setparam (setconf.F90:720-823).  nsite per-site (eps, len) pairs in
+ * ljformat units -> ljtype(nsite) (1-based) and the ljtype_max x ljtype_max matrices
+ * (column-major, capacity max_types^2). */
+int ermod_lj_tables(int nsite, const double* eps, const double* len, int ljformat, int cmbrule,
+                    int max_types, int* ljtype, int* ljtype_max, double* ljene_mat,
+                    double* ljlensq_mat);
+/* engstore's normalisation and rank merge (engproc.F90:475-560): merges nrank raw
+ * accumulator sets (each as returned by ermod_get_accum) into rank 0's, including
+ * the voffset max and exp rescale, then divides by engnorm.  Arrays are
+ * [nrank][size] contiguous; ecorr may be NULL. */
+int ermod_engstore_merge(int nrank, int slttype, int wgtslf, double temp, int ermax, int esmax,
+                         int numslv, double* edens, double* ecorr, double* eself, double* slnuv,
+                         double* minuv, double* maxuv, double* scalars);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ERMOD_GPU_H */
