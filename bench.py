@@ -1,0 +1,346 @@
+"""Benchmark of the energy-representation hot path on GB300.
+
+Metric: solute-solvent molecule energies per second (one unit = one placement x one
+solvent molecule energy, computed and binned).  Workload (default): reference-solvent
+insertion of a 12-site solute into 33,000 rigid waters in a 99.5 A box, PME 96^3,
+order 4, cutoff 12 A, 50,000 insertions per frame, ecorr accumulated.  One step = one
+frame: the frame preparation plus all of its insertions.
+
+Lines printed (rank 0, one JSON line):
+  value         device-resident inputs (frame coordinates and placements already in
+                HBM), CUDA events on the library's stream, L2 flushed between steps;
+  e2e           the same steps through the host C ABI (ermod_frame / ermod_placements
+                with host arrays, the accumulators read back every step), wall clock;
+  roofline      the dominant kernel of the step against the measured HBM copy peak;
+  plain_fp64_gpu  the plain FP64 GPU path (one placement at a time) on a sample;
+  cpu_baseline  the FP64 CPU oracle on a bounded sample, all host cores.
+`--impl reference` times the reference algorithm's CPU restatement (the oracle: the
+Fortran reference cannot be built here) on the same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SMI_QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="refs_large")
+    ap.add_argument("--insertions", type=int, default=None, help="insertions per frame (default: workload's)")
+    ap.add_argument("--batch", type=int, default=32)
+    ap.add_argument("--cpu-sample", type=int, default=96, help="placements timed on the CPU oracle")
+    ap.add_argument("--plain-sample", type=int, default=48, help="placements timed on the plain FP64 GPU path")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={SMI_QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        try:
+            self.f.close()
+        except Exception:
+            pass
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines()]
+        except Exception:
+            return None
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        busy = [s for s in sm if mx and s > 0.5 * mx] or sm
+        return {"sm_mhz": statistics.median(busy), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def make_workload(args):
+    from ermod_gb300 import synth
+    w = synth.WORKLOADS[args.workload]()
+    if args.insertions:
+        w.ins_per_frame = args.insertions
+    return w
+
+
+def cpu_oracle_rate(w, topo, bins, nplace, frame_index=0):
+    """The FP64 oracle on nplace placements of one frame, all host cores."""
+    from oracle import oracle as O
+    O.build()
+    orc = O.Oracle(w.params, topo, bins)
+    pos, cell = w.frame(frame_index)
+    orc.frame(pos, cell)
+    pl = w.placements(frame_index, nplace)
+    tag = np.full(nplace, topo["nummol"], np.int32)
+    t0 = time.perf_counter()
+    orc.placements(tag, pl, want_uvengy=False, nthreads=0)
+    dt = time.perf_counter() - t0
+    orc.close()
+    return nplace * w.nwater / dt, dt
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from ermod_gb300 import setconf
+    w = make_workload(args)
+    topo = setconf.setparam_topology(w.species(), slttype=w.params["slttype"])
+    bins = setconf.enginit_bins(topo["numslv"])
+    sample = max(1, args.cpu_sample // 4)
+    for i in range(args.warmup):
+        cpu_oracle_rate(w, topo, bins, max(1, sample // 4), i)
+    t_total, units = 0.0, 0
+    for i in range(args.steps):
+        rate, dt = cpu_oracle_rate(w, topo, bins, sample, i)
+        t_total += dt
+        units += sample * w.nwater
+    value = units / t_total
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference", "metric": "solute-solvent molecule energies/s", "value": value,
+        "unit": "molecule-energies/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * t_total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{w.name}: {w.nwater} waters, {w.box} A box, PME {w.params['ms1max']}^3, "
+                               f"{len(w.solute['charge'])}-site solute, {w.ins_per_frame} insertions/frame",
+                   "sample": f"{sample} insertions of one frame per step"},
+        "cpu_baseline": {"value": value, "unit": "molecule-energies/s", "cores": cores, "kind": "port",
+                         "sample": f"{sample} insertions x {args.steps} steps, FP64 oracle restating the "
+                                   f"Fortran reference (which cannot be built here), OpenMP over insertions"},
+        "e2e": {"value": value, "unit": "molecule-energies/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+    from ermod_gb300 import build, roofline, setconf
+    from ermod_gb300.engproc import EnergyRepresentation
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    build.build()
+    w = make_workload(args)
+    topo = setconf.setparam_topology(w.species(), slttype=w.params["slttype"])
+    bins = setconf.enginit_bins(topo["numslv"])
+    nplace = w.ins_per_frame
+    nsite_u = len(w.solute["charge"])
+    nsteps = args.warmup + args.steps
+    # frames of this rank (weak scaling: every rank its own frames)
+    frames = [w.frame(rank * nsteps + i) for i in range(nsteps)]
+    places = [w.placements(rank * nsteps + i, nplace) for i in range(nsteps)]
+    tag_h = np.full(nplace, topo["nummol"], np.int32)
+    cell = frames[0][1]
+
+    eng = EnergyRepresentation(w.params, topo, bins, precision="mixed", device=local, batch=args.batch)
+    stream = torch.cuda.Stream(device=dev)
+    eng.set_stream(stream.cuda_stream)
+    pos_d = [torch.from_numpy(f[0]).to(dev) for f in frames]
+    pl_d = [torch.from_numpy(np.ascontiguousarray(p)).to(dev) for p in places]
+    tag_d = torch.from_numpy(tag_h).to(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+
+    def step(i):
+        eng.frame_device(pos_d[i].data_ptr(), frames[i][1])
+        eng.placements_device(nplace, tag_d.data_ptr(), pl_d[i].data_ptr())
+
+    for i in range(args.warmup):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(i))
+        step(i)
+        eng.sync()
+    eng.timing(True)
+    eng.timing_reset()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            i = args.warmup + k
+            with torch.cuda.stream(stream):
+                flush.fill_(float(i))
+                ev[k][0].record(stream)
+            step(i)
+            ev[k][1].record(stream)
+        eng.sync()
+        torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    phases, launches = eng.timing_get()
+    eng.timing(False)
+    t_local = torch.tensor([ms], device=dev, dtype=torch.float64)
+    if ws > 1:
+        torch.distributed.all_reduce(t_local, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t_local.item())
+    units = nplace * w.nwater * args.steps * ws
+    value = units / (ms_max / 1000.0)
+
+    # ---- roofline of the dominant kernel ----
+    K = w.params["ms1max"]
+    nsite_phys = 3 * w.nwater
+    per_pl = roofline.bytes_per_placement(K, K, K, nsite_phys, G=min(8, args.batch))
+    nbatch = args.steps * ((nplace + args.batch - 1) // args.batch)
+    cand = {k: phases.get(k, 0.0) for k in ("spectrum", "fft_c2r", "mol_energy")}
+    dom = max(cand, key=cand.get)
+    avg_launch_ms = cand[dom] / nbatch
+    bytes_per_launch = per_pl[dom] * args.batch
+    peak, peak_kind = load_peaks()
+    achieved = bytes_per_launch / (avg_launch_ms / 1000.0) / 1e9
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+            "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_ms,
+            "phase_ms_per_step": {k: v / args.steps for k, v in phases.items()}}
+    clocks = clk.summary()
+
+    # ---- end to end through the host C ABI ----
+    e2e = None
+    if not args.no_e2e:
+        eng2 = EnergyRepresentation(w.params, topo, bins, precision="mixed", device=local, batch=args.batch)
+        pinned_pl = [torch.from_numpy(np.ascontiguousarray(p)).pin_memory().numpy() for p in places]
+        pinned_pos = [torch.from_numpy(f[0]).pin_memory().numpy() for f in frames]
+        for i in range(args.warmup):
+            eng2.frame(pinned_pos[i], cell)
+            eng2.placements(tag_h, pinned_pl[i])
+            eng2.accum()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            i = args.warmup + k
+            eng2.frame(pinned_pos[i], cell)
+            eng2.placements(tag_h, pinned_pl[i])
+            acc = eng2.accum()
+        dt = time.perf_counter() - t0
+        eng2.close()
+        h2d = frames[0][0].nbytes + places[0].nbytes + tag_h.nbytes
+        ermax = len(bins["uvcrd"])
+        d2h = (ermax * ermax + ermax + 2 * (topo["numslv"] + 1) + topo["numslv"] + 5) * 8
+        e2e = {"value": nplace * w.nwater * args.steps / dt * ws, "unit": "molecule-energies/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+        del acc
+
+    # ---- plain FP64 GPU path (the comparator of the metric) ----
+    plain = None
+    if rank == 0 and args.plain_sample > 0:
+        eng64 = EnergyRepresentation(w.params, topo, bins, precision="fp64", device=local)
+        eng64.frame(frames[0][0], cell)
+        n = args.plain_sample
+        eng64.placements(tag_h[:4], places[0][:4])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        eng64.placements(tag_h[:n], places[0][:n])
+        dt = time.perf_counter() - t0
+        eng64.close()
+        plain = {"value": n * w.nwater / dt, "unit": "molecule-energies/s", "sample": f"{n} insertions, frame 0",
+                 "dtype": "f64"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        rate, dt = cpu_oracle_rate(w, topo, bins, args.cpu_sample, 0)
+        cpu = {"value": rate, "unit": "molecule-energies/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{args.cpu_sample} insertions of frame 0 ({dt:.1f} s), FP64 oracle, OpenMP over insertions"}
+
+    if rank == 0:
+        line = {
+            "metric": "solute-solvent molecule energies/s", "value": value, "unit": "molecule-energies/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic",
+            "config": {"workload": f"{w.name}: {w.nwater} waters, {w.box} A box, PME {K}^3 order "
+                                   f"{w.params['splodr']}, {nsite_u}-site solute, {nplace} insertions/frame, "
+                                   f"ecorr on", "batch": args.batch, "l2": "flushed between steps (256 MiB write)",
+                       "parallelism": f"frames sharded over {ws} GPU(s)" if ws > 1 else "1 GPU"},
+            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "plain_fp64_gpu": plain,
+            "gpu_launches": int(launches), "clocks": clocks,
+        }
+        print(json.dumps(line))
+    eng.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,44 @@
+"""Algorithmic byte counts of the per-placement path (the roofline numerators).
+
+Units: bytes per placement for a PME grid K1 x K2 x K3 with H = K1/2 + 1 half-complex
+columns, FP32 grids (mixed path), N solvent sites and G placements per mol_energy CTA.
+Each count is the least traffic the kernel's job needs: every value it must read or
+write crosses HBM once.
+
+  spectrum    writes the half spectrum engfac * S(k):            8 H K2 K3
+  fft_c2r     reads it, writes the potential grid:               8 H K2 K3 + 4 K1 K2 K3
+  mol_energy  reads the potential grid once, plus the solvent
+              site records (36 B) once per G placements:          4 K1 K2 K3 + 36 N / G
+  total                                                            16 H K2 K3 + 8 K1 K2 K3 + 36 N / G
+
+The plain FP64 path doubles every grid term and adds the spread grid and the forward
+transform (8 K^3 written by the spread, read by D2Z; 16 H K^2 written by D2Z).
+"""
+from __future__ import annotations
+
+
+def grid_terms(K1: int, K2: int, K3: int):
+    H = K1 // 2 + 1
+    return H * K2 * K3, K1 * K2 * K3
+
+
+def bytes_per_placement(K1: int, K2: int, K3: int, nsite: int, G: int = 8) -> dict:
+    nh, nr = grid_terms(K1, K2, K3)
+    d = {
+        "spectrum": 8.0 * nh,
+        "fft_c2r": 8.0 * nh + 4.0 * nr,
+        "mol_energy": 4.0 * nr + 36.0 * nsite / G,
+    }
+    d["total"] = sum(d.values())
+    return d
+
+
+def bytes_per_placement_fp64(K1: int, K2: int, K3: int, nsite: int) -> dict:
+    nh, nr = grid_terms(K1, K2, K3)
+    d = {
+        "spectrum": 8.0 * nr + 8.0 * nr + 16.0 * nh + 2 * 16.0 * nh,  # spread, D2Z, influence
+        "fft_c2r": 16.0 * nh + 8.0 * nr,
+        "mol_energy": 8.0 * nr + (24 + 96 + 8 + 8) * nsite,
+    }
+    d["total"] = sum(d.values())
+    return d
