@@ -140,6 +140,9 @@ static int free_batch(Engine& e) {
   dfree(e.d_ring_nz);
   dfree(e.d_ring_nnz);
   dfree(e.d_ring_valid);
+  dfree(e.d_u0);
+  dfree(e.d_site_e);
+  dfree(e.d_self_bin);
   e.buf = BatchArgs{};
   return ERMOD_OK;
 }
@@ -171,6 +174,8 @@ static int free_topology(Engine& e) {
   dfree(e.d_ljtype);
   dfree(e.d_ljene);
   dfree(e.d_ljlensq);
+  dfree(e.d_ljene_f);
+  dfree(e.d_ljlensq_f);
   dfree(e.d_mol_atom0);
   dfree(e.d_mol_nsite);
   dfree(e.d_mol_species);
@@ -214,12 +219,14 @@ static int ensure_batch(Engine& e) {
   ERMOD_CUDA(dalloc(&b.u_usreal, B));
   ERMOD_CUDA(dalloc(&b.u_radius, B));
   ERMOD_CUDA(dalloc(&b.engnmfc, B));
+  ERMOD_CUDA(dalloc(&e.d_u0, B));
+  ERMOD_CUDA(dalloc(&e.d_self_bin, B));
   if (e.mixed) {
     ERMOD_CUDA(dalloc(&b.u_bvec, (size_t)B * S * 3 * e.Kmax()));
+    ERMOD_CUDA(dalloc(&e.d_site_e, (size_t)e.nsite_phys * B));
     ERMOD_CUDA(dalloc(&b.spec, nc * B));
     ERMOD_CUDA(dalloc(&b.phi, nr * B));
-    const int kc = spectrum_chunk(e.H());
-    ERMOD_CUDA(dalloc(&b.self_part, (size_t)B * e.geom.K[2] * ((e.geom.K[1] + kc - 1) / kc)));
+    ERMOD_CUDA(dalloc(&b.self_part, (size_t)B * spectrum_partials(e)));
   } else {
     ERMOD_CUDA(dalloc(&b.spec64, nc * B));
     ERMOD_CUDA(dalloc(&b.phi64, nr * B));
@@ -237,11 +244,7 @@ static int ensure_batch(Engine& e) {
   if (!e.plans_ready) {
     int n[3] = {e.geom.K[2], e.geom.K[1], e.geom.K[0]};
     cufftResult r;
-    if (e.mixed) {
-      r = cufftPlanMany(&e.plan_c2r, 3, n, nullptr, 1, (int)nc, nullptr, 1, (int)nr, CUFFT_C2R, B);
-      if (r != CUFFT_SUCCESS) return fail_fft(r, "cufftPlanMany(C2R)");
-      cufftSetStream(e.plan_c2r, e.stream);
-    } else {
+    if (!e.mixed) {
       r = cufftPlanMany(&e.plan_d2z, 3, n, nullptr, 1, (int)nr, nullptr, 1, (int)nc, CUFFT_D2Z, B);
       if (r != CUFFT_SUCCESS) return fail_fft(r, "cufftPlanMany(D2Z)");
       r = cufftPlanMany(&e.plan_z2d, 3, n, nullptr, 1, (int)nc, nullptr, 1, (int)nr, CUFFT_Z2D, B);
@@ -322,14 +325,17 @@ int ermod_create(const ermod_params* p, int device, ermod_ctx** out) {
   const int K[3] = {p->ms1max, p->ms2max, p->ms3max};
   for (int i = 0; i < 3; ++i)
     if (K[i] < p->splodr || K[i] > 1000) return fail_param("PME grid sizes must lie in [splodr, 1000]");
-  if (p->precision == ERMOD_PRECISION_MIXED && K[0] / 2 + 1 > 128)
-    return fail_param("mixed precision needs ms1max <= 254");
+  if (p->precision == ERMOD_PRECISION_MIXED && !pme_fits(K[0], K[1], K[2])) {
+    g_err = "mixed precision: PME grid sizes must be products of 2, 3, 5 whose planes fit in shared memory";
+    return ERMOD_E_UNSUPPORTED;
+  }
   if (!(p->screen > 0) || !(p->temp > 0) || !(p->elecut > 0) || !(p->upljcut > 0) || !(p->lwljcut >= 0) ||
       p->lwljcut >= p->upljcut)
     return fail_param("screen, temp and cutoffs must be positive with lwljcut < upljcut");
   if (p->precision != ERMOD_PRECISION_FP64 && p->precision != ERMOD_PRECISION_MIXED)
     return fail_param("precision must be ERMOD_PRECISION_FP64 or ERMOD_PRECISION_MIXED");
-  if (p->batch < 0 || p->batch > accumulate_max_batch()) return fail_param("batch out of range");
+  if (p->batch < 0 || p->batch > accumulate_max_batch() || (p->batch % 4) != 0)
+    return fail_param("batch must be a multiple of 4 in [4, 256] (0 = automatic)");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
     g_err = "no CUDA device";
@@ -347,7 +353,7 @@ int ermod_create(const ermod_params* p, int device, ermod_ctx** out) {
   e.geom.K[1] = K[1];
   e.geom.K[2] = K[2];
   e.Bmax = e.mixed ? (p->batch > 0 ? p->batch : 32) : 1;
-  e.G = e.mixed ? std::min(8, e.Bmax) : 1;
+  e.G = e.mixed ? (e.Bmax % 8 == 0 ? 8 : 4) : 1;
   cudaError_t err = cudaStreamCreateWithFlags(&e.stream, cudaStreamNonBlocking);
   if (err != cudaSuccess) {
     delete c;
@@ -527,6 +533,13 @@ int ermod_set_topology(ermod_ctx* c, int nummol, int numatm, const int* mbi, con
   ERMOD_CUDA(cudaMemcpy(e.d_ljtype, e.ljtype0.data(), sizeof(int) * numatm, cudaMemcpyHostToDevice));
   ERMOD_CUDA(cudaMemcpy(e.d_ljene, lje.data(), sizeof(double) * lje.size(), cudaMemcpyHostToDevice));
   ERMOD_CUDA(cudaMemcpy(e.d_ljlensq, ljl.data(), sizeof(double) * ljl.size(), cudaMemcpyHostToDevice));
+  {
+    std::vector<float> fe(lje.begin(), lje.end()), fl(ljl.begin(), ljl.end());
+    ERMOD_CUDA(dalloc(&e.d_ljene_f, fe.size()));
+    ERMOD_CUDA(dalloc(&e.d_ljlensq_f, fl.size()));
+    ERMOD_CUDA(cudaMemcpy(e.d_ljene_f, fe.data(), sizeof(float) * fe.size(), cudaMemcpyHostToDevice));
+    ERMOD_CUDA(cudaMemcpy(e.d_ljlensq_f, fl.data(), sizeof(float) * fl.size(), cudaMemcpyHostToDevice));
+  }
   ERMOD_CUDA(cudaMemcpy(e.d_mol_atom0, atom0.data(), sizeof(int) * e.slvmax, cudaMemcpyHostToDevice));
   ERMOD_CUDA(cudaMemcpy(e.d_mol_nsite, nsite.data(), sizeof(int) * e.slvmax, cudaMemcpyHostToDevice));
   ERMOD_CUDA(cudaMemcpy(e.d_mol_species, species.data(), sizeof(int) * e.slvmax, cudaMemcpyHostToDevice));
@@ -735,11 +748,7 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
     e.phase_end();
     if (e.mixed) {
       e.phase_begin(PH_SPECTRUM);
-      ERMOD_CUDA(launch_spectrum(e, a));
-      e.phase_end();
-      e.phase_begin(PH_FFT);
-      cufftResult r = cufftExecC2R(e.plan_c2r, (cufftComplex*)a.spec, a.phi);
-      if (r != CUFFT_SUCCESS) return fail_fft(r, "cufftExecC2R");
+      ERMOD_CUDA(launch_pme_mixed(e, a));  // spectrum + k3 transform, then (FFT phase) k2/k1
       e.phase_end();
     } else {
       e.phase_begin(PH_SPECTRUM);

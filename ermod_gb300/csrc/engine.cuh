@@ -44,6 +44,8 @@ struct Engine {
   int* d_ljtype = nullptr;       // 0-based
   double* d_ljene = nullptr;     // [T*T] column-major
   double* d_ljlensq = nullptr;
+  float* d_ljene_f = nullptr;    // FP32 copies for the mixed pair terms
+  float* d_ljlensq_f = nullptr;
   int* d_mol_atom0 = nullptr;    // [slvmax] first atom (0-based) of physical molecule k
   int* d_mol_nsite = nullptr;    // [slvmax]
   int* d_mol_species = nullptr;  // [slvmax] uvspec
@@ -117,6 +119,9 @@ struct Engine {
   int* d_ring_nz = nullptr;       // [ring_cap][ermax] packed (bin | count << 16)... see kernels
   int* d_ring_nnz = nullptr;      // [ring_cap] occupied bins per entry
   int* d_ring_valid = nullptr;    // [ring_cap] entry accumulated (no error in its batch)
+  double* d_u0 = nullptr;         // [Bmax] solute self energies of the current batch
+  float* d_site_e = nullptr;      // [nsite_phys][Bmax] reciprocal site terms (mixed path)
+  int* d_self_bin = nullptr;      // [Bmax]
 
   // ---- status ----------------------------------------------------------------------
   DevStatus* d_status = nullptr;
@@ -141,7 +146,7 @@ struct Engine {
 };
 
 // sizes shared between the launchers and the host code
-int spectrum_chunk(int H);
+int spectrum_partials(const Engine& e);
 int influence64_blocks();
 int accumulate_max_batch();
 size_t frame_cub_bytes(int n);

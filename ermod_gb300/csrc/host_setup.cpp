@@ -9,7 +9,13 @@
 #include <cstring>
 #include <vector>
 
+#include <string>
+
 #include "../../include/ermod_gpu.h"
+
+namespace ermod {
+void set_error_string(const std::string& s);
+}
 
 namespace {
 double ipow(double x, int e) {  // x**e for a constant integer exponent, binary powering
@@ -51,13 +57,19 @@ int ermod_enginit_species(const double* hist, int pecore, int large, double* erc
   for (int regn = 1; regn <= rglmax; ++regn) {
     const double step = (regn == 1 || regn == 5) ? eclbin : ((regn == 2 || regn == 4) ? ecfbin : ec0bin);
     const double width = region_edge[regn] - region_edge[regn - 1];
-    if (width < step) return ERMOD_E_PARAM;  // 'eng_ecd'
+    if (width < step) {
+      ermod::set_error_string("eng_ecd: an energy-coordinate region is narrower than its bin width");
+      return ERMOD_E_PARAM;
+    }
     first_index[regn] = first_index[regn - 1] + (int)std::lround(width / step);
   }
   const int pesoft = first_index[rglmax] - first_index[0];
   const int pemax = pesoft + pecore;
   first_index[rglmax + 1] = pemax;
-  if (pemax > large) return ERMOD_E_PARAM;  // 'eng_siz'
+  if (pemax > large) {
+    ermod::set_error_string("eng_siz: the number of energy-coordinate meshes is too large");
+    return ERMOD_E_PARAM;
+  }
   std::vector<double> crd(large + 2, 0.0);  // 1-based like ercrd(:, pti)
   for (int r = 0; r <= rglmax + 1; ++r) crd[first_index[r]] = region_edge[r];
   const int nregion = (pecore == 0) ? rglmax : rglmax + 1;

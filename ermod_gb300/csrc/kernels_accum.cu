@@ -35,26 +35,70 @@ struct AccArgs {
   int* ring_valid;  // [nb] entries of this batch in the ring
   double* ring_w;
   int slvmax;
+  double* u0;      // [nb] solute self energies of the batch
+  int* self_bin;   // [nb] eself bin (0-based) or -1
   DevStatus* status;
 };
 
 constexpr int kAccThreads = 256;
 constexpr int kMaxBatch = 256;
 
-__global__ void __launch_bounds__(kAccThreads) accumulate_kernel(AccArgs A) {
+// fixed-order block sum: thread t adds elements t, t+256, ... in order, then a fixed tree
+__device__ __forceinline__ double block_sum_fixed(double* red, const double* x, int n, int stride) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += x[(size_t)i * stride];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
+    __syncthreads();
+  }
+  const double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+// one CTA per placement: self energy u0, the self-energy bin check, and the per-species
+// tile partials reduced to flceng / min / max (written to tile slot 0)
+__global__ void __launch_bounds__(kAccThreads) reduce_kernel(AccArgs A) {
   const BatchArgs& a = A.a;
-  const int nb = a.nb;
-  __shared__ double su0[kMaxBatch];
-  __shared__ double sw[kMaxBatch];
-  __shared__ double stw[kMaxBatch];
-  __shared__ int sbin[kMaxBatch];
-  __shared__ int skip;
-  __shared__ double s_voffset;
-  // ---- phase 1: u0 of every placement (parallel over b) ----
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-    double self = 0.0;
-    const double* sp = a.self_part + (size_t)b * A.nself;
-    for (int i = 0; i < A.nself; ++i) self += sp[i];
+  const int b = blockIdx.x;
+  __shared__ double red[kAccThreads];
+  const double self = block_sum_fixed(red, a.self_part + (size_t)b * A.nself, A.nself, 1);
+  for (int sp = 0; sp < A.numslv; ++sp) {
+    const double* base = a.part + ((size_t)b * A.ntile * A.numslv + sp) * 3;
+    const int stride = A.numslv * 3;
+    const double s = block_sum_fixed(red, base, A.ntile, stride);
+    double mn = INFINITY, mx = -INFINITY;
+    for (int t = threadIdx.x; t < A.ntile; t += blockDim.x) {
+      mn = fmin(mn, base[(size_t)t * stride + 1]);
+      mx = fmax(mx, base[(size_t)t * stride + 2]);
+    }
+    red[threadIdx.x] = mn;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+      if (threadIdx.x < st) red[threadIdx.x] = fmin(red[threadIdx.x], red[threadIdx.x + st]);
+      __syncthreads();
+    }
+    mn = red[0];
+    __syncthreads();
+    red[threadIdx.x] = mx;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+      if (threadIdx.x < st) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + st]);
+      __syncthreads();
+    }
+    mx = red[0];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double* out = a.part + ((size_t)b * A.ntile * A.numslv + sp) * 3;  // tile slot 0
+      out[0] = s;
+      out[1] = mn;
+      out[2] = mx;
+      if (a.flceng_out) a.flceng_out[(size_t)(a.b0 + b) * A.numslv + sp] = s;
+    }
+  }
+  if (threadIdx.x == 0) {
     double usreal;
     if (A.rigid)
       usreal = (A.scal[6] != 0.0) ? A.scal[5] : a.u_usreal[0];
@@ -66,8 +110,8 @@ __global__ void __launch_bounds__(kAccThreads) accumulate_kernel(AccArgs A) {
     const double residual = -epcl;
     double u0 = self;
     u0 = u0 + usreal + residual;  // uvengy(0) = uvengy(0) + pairep + residual
-    su0[b] = u0;
-    sbin[b] = -1;
+    A.u0[b] = u0;
+    A.self_bin[b] = -1;
     if (a.uvengy_out) a.uvengy_out[(size_t)(a.b0 + b) * (A.slvmax + 1)] = u0;
     if (A.selfcal) {  // getiduv(0, uvengy(0))
       int code = 0, ret = 0;
@@ -96,15 +140,23 @@ __global__ void __launch_bounds__(kAccThreads) accumulate_kernel(AccArgs A) {
       if (code)
         atomicMin(&A.status->err_key, make_err_key(a.b0 + b, 0, code));
       else
-        sbin[b] = ret - 1;
+        A.self_bin[b] = ret - 1;
     }
   }
-  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kAccThreads) accumulate_kernel(AccArgs A) {
+  const BatchArgs& a = A.a;
+  const int nb = a.nb;
+  __shared__ double sw[kMaxBatch];
+  __shared__ double stw[kMaxBatch];
+  __shared__ int skip;
+  __shared__ double s_voffset;
   if (threadIdx.x == 0) {
     const volatile unsigned long long* ek = &A.status->err_key;
     skip = (*ek != kNoError) ? 1 : 0;
     if (!skip && A.wgtslf && A.scal[4] == 0.0) {
-      A.scal[3] = su0[0];  // voffset from the first placement ever processed
+      A.scal[3] = A.u0[0];  // voffset from the first placement ever processed
       A.scal[4] = 1.0;
     }
     if (!skip && A.rigid && A.scal[6] == 0.0) {
@@ -121,13 +173,13 @@ __global__ void __launch_bounds__(kAccThreads) accumulate_kernel(AccArgs A) {
     }
     return;
   }
-  // ---- phase 2: weights (parallel), then the ordered scalar sums ----
+  // weights (parallel)
   for (int b = threadIdx.x; b < nb; b += blockDim.x) {
     double engnmfc;
     if (!A.wgtslf) {
       engnmfc = 1.0;
     } else {
-      const double factor = su0[b] - s_voffset;
+      const double factor = A.u0[b] - s_voffset;
       engnmfc = A.soln ? exp(factor / A.temp) : exp(-factor / A.temp);
     }
     double total_weight = A.stat_weight_system * (a.stat_weight_solute ? a.stat_weight_solute[b] : 1.0);
@@ -143,6 +195,7 @@ __global__ void __launch_bounds__(kAccThreads) accumulate_kernel(AccArgs A) {
     A.ring_valid[b] = 1;
   }
   __syncthreads();
+  // ordered scalar sums (placement order, as the reference's loop)
   if (threadIdx.x == 0) {
     double engnorm = A.scal[0], engsmpl = A.scal[1], avslf = A.scal[2];
     double mn = A.minuv[0], mx = A.maxuv[0];
@@ -150,9 +203,9 @@ __global__ void __launch_bounds__(kAccThreads) accumulate_kernel(AccArgs A) {
       engnorm = engnorm + sw[b];
       engsmpl = engsmpl + 1.0;
       avslf = avslf + stw[b];
-      if (A.selfcal) A.eself[sbin[b]] += sw[b];
-      mn = fmin(mn, su0[b]);
-      mx = fmax(mx, su0[b]);
+      if (A.selfcal) A.eself[A.self_bin[b]] += sw[b];
+      mn = fmin(mn, A.u0[b]);
+      mx = fmax(mx, A.u0[b]);
     }
     A.scal[0] = engnorm;
     A.scal[1] = engsmpl;
@@ -160,41 +213,19 @@ __global__ void __launch_bounds__(kAccThreads) accumulate_kernel(AccArgs A) {
     A.minuv[0] = mn;
     A.maxuv[0] = mx;
   }
-  // ---- phase 3: per-species sums over the tiles (fixed order) ----
-  for (int t = threadIdx.x; t < nb * A.numslv; t += blockDim.x) {
-    const int b = t / A.numslv, sp = t % A.numslv;
-    double s = 0.0, mn = 1.0e300, mx = -1.0e300;
-    bool any = false;
-    for (int tile = 0; tile < A.ntile; ++tile) {
-      const double* pt = a.part + (((size_t)b * A.ntile + tile) * A.numslv + sp) * 3;
-      s += pt[0];
-      if (pt[1] <= pt[2]) {
-        mn = any ? fmin(mn, pt[1]) : pt[1];
-        mx = any ? fmax(mx, pt[2]) : pt[2];
-        any = true;
-      }
-    }
-    a.part[(((size_t)b * A.ntile + 0) * A.numslv + sp) * 3 + 0] = s;  // flceng(sp, b)
-    a.part[(((size_t)b * A.ntile + 0) * A.numslv + sp) * 3 + 1] = any ? mn : 1.0e300;
-    a.part[(((size_t)b * A.ntile + 0) * A.numslv + sp) * 3 + 2] = any ? mx : -1.0e300;
-    if (a.flceng_out) a.flceng_out[(size_t)(a.b0 + b) * A.numslv + sp] = s;
-  }
-  __syncthreads();
   for (int sp = threadIdx.x; sp < A.numslv; sp += blockDim.x) {
     double mn = A.minuv[sp + 1], mx = A.maxuv[sp + 1], sl = A.soln ? A.slnuv[sp] : 0.0;
     for (int b = 0; b < nb; ++b) {
-      const double* pt = a.part + (((size_t)b * A.ntile + 0) * A.numslv + sp) * 3;
-      if (pt[1] <= pt[2]) {
-        mn = fmin(mn, pt[1]);
-        mx = fmax(mx, pt[2]);
-      }
+      const double* pt = a.part + ((size_t)b * A.ntile * A.numslv + sp) * 3;
+      mn = fmin(mn, pt[1]);
+      mx = fmax(mx, pt[2]);
       if (A.soln) sl = sl + pt[0] * sw[b];
     }
     A.minuv[sp + 1] = mn;
     A.maxuv[sp + 1] = mx;
     if (A.soln) A.slnuv[sp] = sl;
   }
-  // ---- phase 4: edens += engnmfc * insdst, placements in order ----
+  // edens += engnmfc * insdst, placements in order
   for (int i = threadIdx.x; i < A.ermax; i += blockDim.x) {
     double e = A.edens[i];
     bool touched = false;
@@ -299,8 +330,7 @@ cudaError_t launch_accumulate(Engine& e, const BatchArgs& a) {
   A.numslv = e.numslv;
   A.ermax = e.ermax;
   A.esmax = e.esmax;
-  const int kc = spectrum_chunk(e.H());
-  A.nself = e.mixed ? e.geom.K[2] * ((e.geom.K[1] + kc - 1) / kc) : influence64_blocks();
+  A.nself = e.mixed ? spectrum_partials(e) : influence64_blocks();
   A.selfcal = e.P.selfcal;
   A.wgtslf = e.P.wgtslf;
   A.soln = e.P.slttype == 1;
@@ -322,9 +352,12 @@ cudaError_t launch_accumulate(Engine& e, const BatchArgs& a) {
   A.ring_valid = e.d_ring_valid + e.ring_fill;
   A.ring_w = e.d_ring_w + e.ring_fill;
   A.slvmax = e.slvmax;
+  A.u0 = e.d_u0;
+  A.self_bin = e.d_self_bin;
   A.status = e.d_status;
+  reduce_kernel<<<a.nb, kAccThreads, 0, e.stream>>>(A);
   accumulate_kernel<<<1, kAccThreads, 0, e.stream>>>(A);
-  e.count_launch();
+  e.count_launch(2);
   return cudaGetLastError();
 }
 

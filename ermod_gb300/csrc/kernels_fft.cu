@@ -1,0 +1,593 @@
+// kernels_fft.cu -- the mixed path's PME solute potential: spectrum + 3-D C2R transform
+// written for this path (replaces recpcal_prepare_solute's spread, R2C, engfac
+// multiply and C2R, recpcal.F90:357-402, for a batch of placements).
+//
+//   pme_a   CTA per (k2, placement).  Generates the half-spectrum slab
+//             S(k1, k3) = engfac(k1,k2,k3) sum_s q_s b1_s(k1) b2_s(k2) b3_s(k3)
+//           (the exact R2C transform of the spread solute charges; b_{s,a} are the
+//           1-D structure factors of the B-spline stencils), reduces the self energy
+//           0.5 sum_k engfac |S|^2 (recpcal.F90:385-394) with float-float compensation,
+//           and transforms the slab along k3 (inverse, unnormalised) in shared memory.
+//           Output T1[b][z][k2][k1] (complex FP32).
+//   pme_b   CTA per (z, group of 4 placements).  For each placement: the k2 transform of
+//           the (k2, k1) plane, then the complex-to-real transform along k1, two rows per
+//           complex transform (Z = X + iY).  The four placements' real planes are staged
+//           in shared memory and written as phi[group][z][y][x][4], i.e. interleaved by
+//           placement, with coalesced 16-byte stores.
+// Transforms are self-sorting Stockham passes (radices 2-16, composite radices done in
+// registers), unnormalised, sign +1, exactly the conventions of fft_iface.F90.
+#include "engine.cuh"
+
+namespace ermod {
+
+namespace {
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 mul_i(float2 a) { return make_float2(-a.y, a.x); }  // a * i
+
+// ---- in-register inverse DFTs: Y[q] = sum_r v[r] exp(+2 pi i r q / R) ----------------
+template <int R>
+struct Dft;
+
+template <>
+struct Dft<1> {
+  static __device__ __forceinline__ void run(float2*) {}
+};
+template <>
+struct Dft<2> {
+  static __device__ __forceinline__ void run(float2* v) {
+    const float2 a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+  }
+};
+template <>
+struct Dft<3> {
+  static __device__ __forceinline__ void run(float2* v) {
+    const float c = -0.5f, s = 0.86602540378443864676f;  // exp(2 pi i / 3)
+    const float2 a = v[0], b = v[1], d = v[2];
+    const float2 t = cadd(b, d), u = csub(b, d);
+    v[0] = cadd(a, t);
+    const float2 m = make_float2(a.x + c * t.x, a.y + c * t.y);
+    const float2 n = make_float2(-s * u.y, s * u.x);  // i s (b - d)
+    v[1] = cadd(m, n);
+    v[2] = csub(m, n);
+  }
+};
+template <>
+struct Dft<4> {
+  static __device__ __forceinline__ void run(float2* v) {
+    const float2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
+    const float2 c = cadd(v[1], v[3]), d = mul_i(csub(v[1], v[3]));
+    v[0] = cadd(a, c);
+    v[2] = csub(a, c);
+    v[1] = cadd(b, d);
+    v[3] = csub(b, d);
+  }
+};
+template <>
+struct Dft<5> {
+  static __device__ __forceinline__ void run(float2* v) {
+    const float c1 = 0.30901699437494742410f, c2 = -0.80901699437494742410f;
+    const float s1 = 0.95105651629515357212f, s2 = 0.58778525229247312917f;
+    const float2 a = v[0];
+    const float2 t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]);
+    const float2 u1 = csub(v[1], v[4]), u2 = csub(v[2], v[3]);
+    v[0] = cadd(a, cadd(t1, t2));
+    const float2 m1 = make_float2(a.x + c1 * t1.x + c2 * t2.x, a.y + c1 * t1.y + c2 * t2.y);
+    const float2 m2 = make_float2(a.x + c2 * t1.x + c1 * t2.x, a.y + c2 * t1.y + c1 * t2.y);
+    const float2 n1 = make_float2(s1 * u1.x + s2 * u2.x, s1 * u1.y + s2 * u2.y);  // (s1 u1 + s2 u2)
+    const float2 n2 = make_float2(s2 * u1.x - s1 * u2.x, s2 * u1.y - s1 * u2.y);
+    v[1] = cadd(m1, mul_i(n1));
+    v[4] = csub(m1, mul_i(n1));
+    v[2] = cadd(m2, mul_i(n2));
+    v[3] = csub(m2, mul_i(n2));
+  }
+};
+
+// compile-time cos/sin(pi x) for the in-register twiddles (Taylor series after reduction
+// to [-1/2, 1/2]; |error| < 1e-16, folded to float constants)
+constexpr double ct_pi = 3.14159265358979323846;
+constexpr double ct_taylor_cos(double t) {  // cos(t), |t| <= pi/2
+  double term = 1.0, sum = 1.0;
+  for (int k = 1; k < 16; ++k) {
+    term = -term * t * t / ((2.0 * k - 1.0) * (2.0 * k));
+    sum += term;
+  }
+  return sum;
+}
+constexpr double ct_taylor_sin(double t) {  // sin(t), |t| <= pi/2
+  double term = t, sum = t;
+  for (int k = 1; k < 16; ++k) {
+    term = -term * t * t / ((2.0 * k) * (2.0 * k + 1.0));
+    sum += term;
+  }
+  return sum;
+}
+constexpr double ct_cospi(double x) {  // cos(pi x)
+  while (x > 1.0) x -= 2.0;
+  while (x < -1.0) x += 2.0;
+  if (x > 0.5) return -ct_taylor_cos(ct_pi * (1.0 - x));
+  if (x < -0.5) return -ct_taylor_cos(ct_pi * (1.0 + x));
+  return ct_taylor_cos(ct_pi * x);
+}
+constexpr double ct_sinpi(double x) {  // sin(pi x)
+  while (x > 1.0) x -= 2.0;
+  while (x < -1.0) x += 2.0;
+  if (x > 0.5) return ct_taylor_sin(ct_pi * (1.0 - x));
+  if (x < -0.5) return -ct_taylor_sin(ct_pi * (1.0 + x));
+  return ct_taylor_sin(ct_pi * x);
+}
+
+// composite radix A*B in registers (Cooley-Tukey): B DFTs of size A on stride-B
+// subsequences, twiddles exp(+2 pi i a b / R), then A DFTs of size B
+template <int A, int B>
+struct DftCT {
+  static constexpr int R = A * B;
+  static __device__ __forceinline__ void run(float2* v) {
+    float2 t[R];
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+      float2 s[A];
+#pragma unroll
+      for (int a = 0; a < A; ++a) s[a] = v[a * B + b];
+      Dft<A>::run(s);
+#pragma unroll
+      for (int a = 0; a < A; ++a) {
+        if (a * b != 0) {
+          const float cs = (float)ct_cospi(2.0 * (double)(a * b) / (double)R);
+          const float sn = (float)ct_sinpi(2.0 * (double)(a * b) / (double)R);
+          s[a] = cmul(s[a], make_float2(cs, sn));
+        }
+        t[a * B + b] = s[a];
+      }
+    }
+    // t[a*B + b]: A-point results (index a) of subsequence b; now B-point DFTs over b
+#pragma unroll
+    for (int a = 0; a < A; ++a) {
+      float2 s[B];
+#pragma unroll
+      for (int b = 0; b < B; ++b) s[b] = t[a * B + b];
+      Dft<B>::run(s);
+#pragma unroll
+      for (int b = 0; b < B; ++b) v[b * A + a] = s[b];
+    }
+  }
+};
+template <>
+struct Dft<6> : DftCT<2, 3> {};
+template <>
+struct Dft<8> : DftCT<2, 4> {};
+template <>
+struct Dft<9> : DftCT<3, 3> {};
+template <>
+struct Dft<10> : DftCT<2, 5> {};
+template <>
+struct Dft<12> : DftCT<4, 3> {};
+template <>
+struct Dft<15> : DftCT<3, 5> {};
+template <>
+struct Dft<16> : DftCT<4, 4> {};
+
+// n / d for n < 2^16 by a multiply-high (m = ceil(2^32 / d)); d = 1 handled apart
+struct FastDiv {
+  unsigned d, m;
+};
+__host__ __device__ inline FastDiv make_fastdiv(unsigned d) {
+  return FastDiv{d, d <= 1 ? 0u : (unsigned)((0x100000000ull + d - 1) / d)};
+}
+__device__ __forceinline__ int fdiv(int n, FastDiv f) { return f.d <= 1 ? n : (int)__umulhi((unsigned)n, f.m); }
+
+// One Stockham pass of radix R over ncols transforms of length N (elements estride
+// apart, transforms cstride apart), A -> B; consecutive threads take consecutive
+// transforms, so the caller picks strides that keep shared-memory accesses conflict
+// free.  tw[m] = exp(+2 pi i m / N).
+template <int R>
+__device__ __forceinline__ void stockham_pass(const float2* __restrict__ A, float2* __restrict__ B, int N, int Ns,
+                                              FastDiv fNs, int ncols, FastDiv fcols, int estride, int cstride,
+                                              const float2* __restrict__ tw) {
+  const int NR = N / R;
+  const int total = ncols * NR;
+  const int step = N / (Ns * R);
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    const int j = fdiv(t, fcols);
+    const int col = t - j * ncols;
+    const int jq = fdiv(j, fNs);
+    const int k = j - jq * Ns;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = A[col * cstride + (j + r * NR) * estride];
+    if (k > 0) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[r * k * step]);  // r k step < N
+    }
+    Dft<R>::run(v);
+    const int idxD = jq * Ns * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) B[col * cstride + (idxD + r * Ns) * estride] = v[r];
+  }
+}
+
+__device__ __forceinline__ void run_pass(int R, const float2* A, float2* B, int N, int Ns, FastDiv fNs, int ncols,
+                                         FastDiv fcols, int estride, int cstride, const float2* tw) {
+#define ERMOD_PASS(RR) \
+  case RR: stockham_pass<RR>(A, B, N, Ns, fNs, ncols, fcols, estride, cstride, tw); break;
+  switch (R) {
+    ERMOD_PASS(2)
+    ERMOD_PASS(3)
+    ERMOD_PASS(4)
+    ERMOD_PASS(5)
+    ERMOD_PASS(6)
+    ERMOD_PASS(8)
+    ERMOD_PASS(9)
+    ERMOD_PASS(10)
+    ERMOD_PASS(12)
+    ERMOD_PASS(15)
+    ERMOD_PASS(16)
+    default: break;
+  }
+#undef ERMOD_PASS
+}
+
+}  // namespace
+
+// radix plan: at most kMaxPasses radices from {16,15,12,10,9,8,6,5,4,3,2}, fewest passes
+constexpr int kMaxPasses = 6;
+struct FftPlan {
+  int n, npass, r[kMaxPasses], ns[kMaxPasses];
+  FastDiv fns[kMaxPasses];
+};
+
+bool make_fft_plan(int n, FftPlan& p) {
+  static const int cand[] = {16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2};
+  p.n = n;
+  p.npass = 0;
+  // prefer two balanced passes when possible
+  for (int a : cand)
+    if (n % a == 0) {
+      const int b = n / a;
+      for (int c : cand)
+        if (c == b) {
+          p.npass = 2;
+          p.r[0] = a;
+          p.r[1] = b;
+          return true;
+        }
+    }
+  for (int a : cand)  // a single pass
+    if (a == n) {
+      p.npass = 1;
+      p.r[0] = a;
+      return true;
+    }
+  int m = n;
+  while (m > 1 && p.npass < kMaxPasses) {
+    bool found = false;
+    for (int a : cand)
+      if (m % a == 0) {
+        p.r[p.npass++] = a;
+        m /= a;
+        found = true;
+        break;
+      }
+    if (!found) return false;
+  }
+  if (n == 1) {
+    p.npass = 0;
+    return true;
+  }
+  return m == 1;
+}
+
+static bool finish_plan(FftPlan& p) {
+  int ns = 1;
+  for (int i = 0; i < p.npass; ++i) {
+    p.ns[i] = ns;
+    p.fns[i] = make_fastdiv((unsigned)ns);
+    ns *= p.r[i];
+  }
+  return ns == p.n;
+}
+
+static bool plan(int n, FftPlan& p) { return make_fft_plan(n, p) && finish_plan(p); }
+
+namespace {
+
+// inverse transform of ncols columns; data starts in A, ends in the returned buffer
+__device__ __forceinline__ float2* fft_cols(float2* A, float2* B, const FftPlan& pl, int ncols, FastDiv fcols,
+                                            int estride, int cstride, const float2* tw) {
+  for (int p = 0; p < pl.npass; ++p) {
+    __syncthreads();
+    run_pass(pl.r[p], A, B, pl.n, pl.ns[p], pl.fns[p], ncols, fcols, estride, cstride, tw);
+    float2* t = A;
+    A = B;
+    B = t;
+  }
+  __syncthreads();
+  return A;
+}
+
+struct ff {
+  float hi, lo;
+};
+__device__ __forceinline__ ff ff_add(ff a, float b) {
+  const float s = a.hi + b;
+  const float bb = s - a.hi;
+  const float err = (a.hi - (s - bb)) + (b - bb);
+  const float lo = a.lo + err;
+  const float hi = s + lo;
+  return ff{hi, lo - (hi - s)};
+}
+__device__ __forceinline__ ff ff_add2(ff a, ff b) { return ff_add(ff_add(a, b.hi), b.lo); }
+
+constexpr int kSites = 32;  // solute sites staged per chunk
+constexpr int kR1 = 4, kR3 = 4;
+
+struct PmeArgs {
+  const float2* bvec;   // [nb][S][3][Kmax]
+  const double* u_q;    // [nb][S]
+  const int* u_nsite;
+  const float* engfac;  // [K3][K2][H]
+  const float2* twiddle;  // per axis, exp(-2 pi i m / K): conjugated here for the inverse
+  float2* t1;           // [nb][K3][K2][H]
+  float* phi;           // [nb/4][K3][K2][K1][4]
+  double* self_part;    // [nb][K2]
+  int nb, K1, K2, K3, H, Hp, K1p, Kmax;
+  int chunk;  // solute sites staged per generation chunk (fits the k3 work buffer)
+  FftPlan p1, p2, p3;
+  FastDiv fH, fK1, fHp4, fnpair;
+};
+
+__global__ void __launch_bounds__(256) pme_a_kernel(PmeArgs A) {
+  extern __shared__ float2 sm[];
+  const int k2 = blockIdx.x, b = blockIdx.y;
+  const int K3 = A.K3, H = A.H, Hp = A.Hp;
+  float2* slab = sm;                          // [K3][Hp]
+  float2* work = sm + (size_t)K3 * Hp;        // [K3][Hp]; site staging during generation
+  float2* tw3 = work + (size_t)K3 * Hp;       // [K3]
+  for (int i = threadIdx.x; i < K3; i += blockDim.x) {
+    const float2 t = A.twiddle[A.K1 + A.K2 + i];
+    tw3[i] = make_float2(t.x, -t.y);
+  }
+  const int ns = A.u_nsite[b];
+  const float2* bv = A.bvec + (size_t)b * kMaxSoluteSites * 3 * A.Kmax;
+  const int TX = Hp / kR1, TY = (K3 + kR3 - 1) / kR3;
+  // ---- generation: slab(k3, k1) = sum_s [q_s b2_s(k2) b3_s(k3)] b1_s(k1) ----
+  float2* sd = work;                         // [chunk][K3]
+  float2* sb = work + (size_t)A.chunk * K3;  // [chunk][Hp]  (Hp, chunk*K3 even: 16-byte aligned rows)
+  for (int s0 = 0; s0 < ns; s0 += A.chunk) {
+    const int nsc = min(A.chunk, ns - s0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < nsc * K3; t += blockDim.x) {
+      const int sl = t / K3, k3 = t - sl * K3;
+      const size_t us = (size_t)(s0 + sl);
+      const float q = (float)A.u_q[(size_t)b * kMaxSoluteSites + us];
+      const float2 b2 = bv[(us * 3 + 1) * A.Kmax + k2];
+      const float2 b3 = bv[(us * 3 + 2) * A.Kmax + k3];
+      sd[sl * K3 + k3] = cmul(make_float2(q * b2.x, q * b2.y), b3);
+    }
+    for (int t = threadIdx.x; t < nsc * Hp; t += blockDim.x) {
+      const int sl = t / Hp, k1 = t - sl * Hp;
+      sb[sl * Hp + k1] = (k1 < H) ? bv[((size_t)(s0 + sl) * 3 + 0) * A.Kmax + k1] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    for (int mt = threadIdx.x; mt < TX * TY; mt += blockDim.x) {
+      const int ty = fdiv(mt, A.fHp4), tx = mt - ty * TX;
+      const int k1a = tx * kR1, k3a = ty * kR3;
+      float2 acc[kR3][kR1];
+#pragma unroll
+      for (int j = 0; j < kR3; ++j)
+#pragma unroll
+        for (int i = 0; i < kR1; ++i) acc[j][i] = make_float2(0.f, 0.f);
+      for (int sl = 0; sl < nsc; ++sl) {
+        float2 d[kR3], e[kR1];
+#pragma unroll
+        for (int j = 0; j < kR3; ++j) d[j] = (k3a + j < K3) ? sd[sl * K3 + k3a + j] : make_float2(0.f, 0.f);
+        const float4* e4 = reinterpret_cast<const float4*>(sb + sl * Hp + k1a);
+        const float4 e01 = e4[0], e23 = e4[1];
+        e[0] = make_float2(e01.x, e01.y);
+        e[1] = make_float2(e01.z, e01.w);
+        e[2] = make_float2(e23.x, e23.y);
+        e[3] = make_float2(e23.z, e23.w);
+#pragma unroll
+        for (int j = 0; j < kR3; ++j)
+#pragma unroll
+          for (int i = 0; i < kR1; ++i) {
+            acc[j][i].x = fmaf(d[j].x, e[i].x, fmaf(-d[j].y, e[i].y, acc[j][i].x));
+            acc[j][i].y = fmaf(d[j].x, e[i].y, fmaf(d[j].y, e[i].x, acc[j][i].y));
+          }
+      }
+#pragma unroll
+      for (int j = 0; j < kR3; ++j) {
+        const int k3 = k3a + j;
+        if (k3 >= K3) continue;
+        float4* dst = reinterpret_cast<float4*>(slab + (size_t)k3 * Hp + k1a);
+        float4 v0 = make_float4(acc[j][0].x, acc[j][0].y, acc[j][1].x, acc[j][1].y);
+        float4 v1 = make_float4(acc[j][2].x, acc[j][2].y, acc[j][3].x, acc[j][3].y);
+        if (s0 != 0) {
+          const float4 o0 = dst[0], o1 = dst[1];
+          v0 = make_float4(v0.x + o0.x, v0.y + o0.y, v0.z + o0.z, v0.w + o0.w);
+          v1 = make_float4(v1.x + o1.x, v1.y + o1.y, v1.z + o1.z, v1.w + o1.w);
+        }
+        dst[0] = v0;
+        dst[1] = v1;
+      }
+    }
+  }
+  __syncthreads();
+  // ---- engfac multiply and self energy ----
+  ff self{0.f, 0.f};
+  const bool even = (A.K1 % 2) == 0;
+  for (int t = threadIdx.x; t < K3 * H; t += blockDim.x) {
+    const int k3 = fdiv(t, A.fH), k1 = t - k3 * H;
+    const float f = A.engfac[((size_t)k3 * A.K2 + k2) * H + k1];
+    float2* p = slab + (size_t)k3 * Hp + k1;
+    const float2 q = *p;
+    const float wgt = (k1 == 0 || (even && k1 == H - 1)) ? 0.5f : 1.f;
+    self = ff_add(self, wgt * f * (q.x * q.x + q.y * q.y));
+    *p = make_float2(f * q.x, f * q.y);
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    ff o{__shfl_down_sync(0xffffffffu, self.hi, off), __shfl_down_sync(0xffffffffu, self.lo, off)};
+    self = ff_add2(self, o);
+  }
+  __shared__ double wsum[8];
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = (double)self.hi + (double)self.lo;
+  // ---- inverse transform along k3 (columns k1, element stride Hp) ----
+  float2* res = fft_cols(slab, work, A.p3, H, A.fH, Hp, 1, tw3);
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += wsum[w];
+    A.self_part[(size_t)b * A.K2 + k2] = t;
+  }
+  // ---- T1[b][z][k2][k1] ----
+  float2* out = A.t1 + (size_t)b * K3 * A.K2 * H;
+  for (int t = threadIdx.x; t < K3 * H; t += blockDim.x) {
+    const int z = fdiv(t, A.fH), k1 = t - z * H;
+    out[((size_t)z * A.K2 + k2) * H + k1] = res[(size_t)z * Hp + k1];
+  }
+}
+
+__global__ void __launch_bounds__(512) pme_b_kernel(PmeArgs A) {
+  extern __shared__ float2 sm[];
+  const int z = blockIdx.x, grp = blockIdx.y;
+  const int K1 = A.K1, K2 = A.K2, K3 = A.K3, H = A.H, K1p = A.K1p;
+  const size_t plane = (size_t)K2 * H;
+  const int npair = (K2 + 1) / 2;
+  const size_t bufsz = max(plane, (size_t)npair * K1p);
+  float2* s0 = sm;
+  float2* s1 = sm + bufsz;
+  float* stage = reinterpret_cast<float*>(sm + 2 * bufsz);  // [4][K2][K1]
+  float2* tw1 = reinterpret_cast<float2*>(stage + (size_t)4 * K2 * K1);
+  float2* tw2 = tw1 + K1;
+  const size_t pl = (size_t)K2 * K1;
+  for (int i = threadIdx.x; i < K1 + K2; i += blockDim.x) {
+    const float2 t = A.twiddle[i];
+    if (i < K1)
+      tw1[i] = make_float2(t.x, -t.y);
+    else
+      tw2[i - K1] = make_float2(t.x, -t.y);
+  }
+  for (int bl = 0; bl < 4; ++bl) {
+    const int b = grp * 4 + bl;
+    float* st = stage + bl * pl;
+    __syncthreads();
+    if (b >= A.nb) {  // idle slots of a partial group are written as zeros
+      for (int t = threadIdx.x; t < (int)pl; t += blockDim.x) st[t] = 0.f;
+      continue;
+    }
+    const float2* in = A.t1 + ((size_t)b * K3 + z) * plane;
+    for (int t = threadIdx.x; t < (int)plane; t += blockDim.x) s0[t] = in[t];
+    // k2 transform: columns k1 (stride 1), elements along k2 (stride H)
+    float2* r = fft_cols(s0, s1, A.p2, H, A.fH, H, 1, tw2);
+    float2* w = (r == s0) ? s1 : s0;
+    // pack row pairs: Z_p[k] = X_{2p}[k] + i X_{2p+1}[k], Hermitian-completed in k1;
+    // rows padded to K1p (odd) so the row transforms are bank-conflict free
+    for (int t = threadIdx.x; t < npair * K1; t += blockDim.x) {
+      const int pp = fdiv(t, A.fK1), k = t - pp * K1;
+      const int y0 = 2 * pp, y1 = 2 * pp + 1;
+      float2 x0, x1 = make_float2(0.f, 0.f);
+      const bool self_conj = (k == 0) || ((K1 % 2 == 0) && k == K1 / 2);
+      if (k < H) {
+        x0 = r[(size_t)y0 * H + k];
+        if (y1 < K2) x1 = r[(size_t)y1 * H + k];
+      } else {
+        const float2 a = r[(size_t)y0 * H + (K1 - k)];
+        x0 = make_float2(a.x, -a.y);
+        if (y1 < K2) {
+          const float2 c = r[(size_t)y1 * H + (K1 - k)];
+          x1 = make_float2(c.x, -c.y);
+        }
+      }
+      if (self_conj) {
+        x0.y = 0.f;
+        x1.y = 0.f;
+      }
+      w[(size_t)pp * K1p + k] = make_float2(x0.x - x1.y, x0.y + x1.x);
+    }
+    // row transforms along k1: one transform per row pair (column index), stride K1p
+    float2* res = fft_cols(w, r, A.p1, npair, A.fnpair, 1, K1p, tw1);
+    for (int t = threadIdx.x; t < npair * K1; t += blockDim.x) {
+      const int pp = fdiv(t, A.fK1), x = t - pp * K1;
+      const float2 v = res[(size_t)pp * K1p + x];
+      st[(size_t)(2 * pp) * K1 + x] = v.x;
+      if (2 * pp + 1 < K2) st[(size_t)(2 * pp + 1) * K1 + x] = v.y;
+    }
+  }
+  __syncthreads();
+  float4* dst = reinterpret_cast<float4*>(A.phi + (((size_t)grp * K3 + z) * pl) * 4);
+  for (int t = threadIdx.x; t < (int)pl; t += blockDim.x)
+    dst[t] = make_float4(stage[t], stage[pl + t], stage[2 * pl + t], stage[3 * pl + t]);
+}
+
+size_t pme_a_smem(int K3, int Hp) { return sizeof(float2) * ((size_t)2 * K3 * Hp + K3); }
+size_t pme_b_smem(int K1, int K2, int H) {
+  const size_t plane = (size_t)K2 * H;
+  const size_t npair = (K2 + 1) / 2;
+  const size_t bufsz = std::max(plane, npair * (size_t)(K1 | 1));
+  return sizeof(float2) * 2 * bufsz + sizeof(float) * (size_t)K2 * K1 * 4 + sizeof(float2) * (K1 + K2);
+}
+
+}  // namespace
+
+bool pme_fits(int K1, int K2, int K3) {
+  const int H = K1 / 2 + 1, Hp = ((H + kR1 - 1) / kR1) * kR1;
+  FftPlan a, b, c;
+  if (!plan(K1, a) || !plan(K2, b) || !plan(K3, c)) return false;
+  return pme_a_smem(K3, Hp) <= 227 * 1024 && pme_b_smem(K1, K2, H) <= 227 * 1024;
+}
+
+cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a) {
+  PmeArgs A{};
+  A.bvec = a.u_bvec;
+  A.u_q = a.u_q;
+  A.u_nsite = a.u_nsite;
+  A.engfac = e.d_engfac_f;
+  A.twiddle = e.d_twiddle;
+  A.t1 = a.spec;
+  A.phi = a.phi;
+  A.self_part = a.self_part;
+  A.nb = a.nb;
+  A.K1 = e.geom.K[0];
+  A.K2 = e.geom.K[1];
+  A.K3 = e.geom.K[2];
+  A.H = e.H();
+  A.Hp = ((A.H + kR1 - 1) / kR1) * kR1;
+  A.Kmax = e.Kmax();
+  A.chunk = std::max(1, std::min(kSites, (A.K3 * A.Hp) / (A.K3 + A.Hp)));
+  A.chunk &= ~1;  // even chunk: the b1 staging rows stay 16-byte aligned
+  if (A.chunk < 2) A.chunk = 2;
+  A.K1p = A.K1 | 1;
+  if (!plan(A.K1, A.p1) || !plan(A.K2, A.p2) || !plan(A.K3, A.p3)) return cudaErrorInvalidValue;
+  A.fH = make_fastdiv(A.H);
+  A.fK1 = make_fastdiv(A.K1);
+  A.fHp4 = make_fastdiv(A.Hp / kR1);
+  A.fnpair = make_fastdiv((A.K2 + 1) / 2);
+  const size_t sa = pme_a_smem(A.K3, A.Hp), sb = pme_b_smem(A.K1, A.K2, A.H);
+  static size_t attr_a = 0, attr_b = 0;
+  cudaError_t err;
+  if (attr_a < sa) {
+    if ((err = cudaFuncSetAttribute(pme_a_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sa)) != cudaSuccess)
+      return err;
+    attr_a = sa;
+  }
+  if (attr_b < sb) {
+    if ((err = cudaFuncSetAttribute(pme_b_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb)) != cudaSuccess)
+      return err;
+    attr_b = sb;
+  }
+  pme_a_kernel<<<dim3(A.K2, a.nb), 256, sa, e.stream>>>(A);
+  e.count_launch();
+  if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  e.phase_end();
+  e.phase_begin(PH_FFT);
+  pme_b_kernel<<<dim3(A.K3, (a.nb + 3) / 4), 512, sb, e.stream>>>(A);
+  e.count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace ermod

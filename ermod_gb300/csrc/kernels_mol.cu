@@ -39,7 +39,10 @@ struct MolArgs {
   // LJ tables
   const double* ljene;
   const double* ljlensq;
+  const float* ljene_f;
+  const float* ljlensq_f;
   int T;
+  int ldb;  // interleave stride of the mixed potential grids (placements per grid point)
   // energy coordinate
   const long long* uvkey;
   const int* spec;  // [numslv][3]
@@ -284,6 +287,86 @@ __device__ __forceinline__ double key_to_double(long long k) {
   return __longlong_as_double(k);
 }
 
+
+// getiduv / binsearch for one molecule: returns the status code (0 = binned) and ret,
+// the count of edges strictly below u (bin = sp_off + ret - 1).
+__device__ __forceinline__ int bin_molecule(const MolArgs& A, double u, int species, int sp_off, int sp_n,
+                                            int sp_soft, int& ret) {
+  ret = 0;
+  if (species < 1 || species > A.numslv) return ERMOD_E_ENG_CNS;
+  if (u != u) return ERMOD_E_ENG_MIN;
+  const long long ku = ordered_key(u);
+  const long long* keys = A.uvkey + sp_off;
+  int lo = 0, hi = sp_n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(keys + mid) < ku)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  ret = lo;
+  if (ret <= 0) return ERMOD_E_ENG_MIN;
+  if (A.soln && ret > sp_soft) return ERMOD_E_ENG_SFT;
+  if (ret == sp_n && u < 1.0e3 && A.mbin_mode != 0) {
+    if (A.mbin_mode == 1) return ERMOD_W_MBIN;
+    atomicOr(&A.status->mbin_hit, 1);
+  }
+  return 0;
+}
+
+// warp-aggregated shared-memory histogram increment
+__device__ __forceinline__ void hist_add(int* h, int bin) {
+  const unsigned am = __activemask();
+  const unsigned peers = __match_any_sync(am, bin);
+  const int leader = __ffs(peers) - 1;
+  if ((threadIdx.x & 31) == leader) atomicAdd(&h[bin], __popc(peers));
+}
+
+// real-space LJ + screened Coulomb of one molecule against solute b (mixed path):
+// fixed-point displacements, FP32 pair terms, FP64 sum over solute sites.
+__device__ __forceinline__ double real_mixed(const MolArgs& A, const BatchArgs& a, int b, int s0, int ns,
+                                             const LjK& k32, float rcut) {
+  const FrameGeom& g = A.g;
+  const size_t ub = (size_t)b * kMaxSoluteSites;
+  const int4 p0 = A.site_pos[s0];
+  const int4 u0 = a.u_pos[ub];
+  const float fx = (float)g.fx_scale[0], fy = (float)g.fx_scale[1], fz = (float)g.fx_scale[2];
+  const float dx = (float)(int)((unsigned)p0.x - (unsigned)u0.x) * fx;
+  const float dy = (float)(int)((unsigned)p0.y - (unsigned)u0.y) * fy;
+  const float dz = (float)(int)((unsigned)p0.z - (unsigned)u0.z) * fz;
+  double real = 0.0;
+  if (dx * dx + dy * dy + dz * dz > rcut * rcut) return real;
+  const int nu = a.u_nsite[b];
+  const float beta = (float)A.screen;
+  for (int su = 0; su < nu; ++su) {
+    const int4 up = a.u_pos[ub + su];
+    const float qu = (float)a.u_q[ub + su];
+    float e = 0.f;
+    for (int s = 0; s < ns; ++s) {
+      const int4 vp = A.site_pos[s0 + s];
+      const float ex = (float)(int)((unsigned)vp.x - (unsigned)up.x) * fx;
+      const float ey = (float)(int)((unsigned)vp.y - (unsigned)up.y) * fy;
+      const float ez = (float)(int)((unsigned)vp.z - (unsigned)up.z) * fz;
+      const float r2 = ex * ex + ey * ey + ez * ez;
+      const float ljeps = A.ljene_f[vp.w + A.T * up.w];
+      if (ljeps > 0.f) {
+        const float sg2 = A.ljlensq_f[vp.w + A.T * up.w];
+        if (r2 <= k32.lw2)
+          e += lj_low<float>(A.ljswitch, k32, ljeps, sg2, r2);
+        else if (r2 <= k32.up2)
+          e += lj_switch<float>(A.ljswitch, k32, ljeps, sg2, r2);
+      }
+      if (r2 <= k32.ele2) {
+        const float r = sqrtf(r2);
+        e += qu * A.site_rec[s0 + s].w * erfcf(beta * r) / r;
+      }
+    }
+    real += (double)e;
+  }
+  return real;
+}
+
 constexpr long long kKeyPosInf = 0x7ff0000000000000ll;
 constexpr long long kKeyNegInf = (long long)0x800fffffffffffffull;  // ordered key of -inf
 
@@ -522,6 +605,215 @@ __global__ void __launch_bounds__(256) mol_energy_kernel(MolArgs A) {
   }
 }
 
+
+// Mixed path, step 1 -- gather.  One thread = one solvent site x G placements.  The
+// batch's potential grids are interleaved, phi[(z K2 + y) K1 + x][ldb] with placements
+// innermost, so the G placements of a stencil point are one aligned 32-byte load, and
+// the B-spline weights and grid indices of the site are computed once for all of them.
+// Output: q * sum theta theta theta phi per (site, placement), FP32, [site][ldb].
+template <int P, int G>
+__global__ void __launch_bounds__(256) gather_kernel(const float* __restrict__ phi, const float4* __restrict__ site_rec,
+                                                     const int* __restrict__ site_grid, int nsite, int K1, int K2,
+                                                     int K3, int ldb, float* __restrict__ site_e) {
+  // phi layout: [placement group of 4][z][y][x][4]
+  const size_t gstride = (size_t)K1 * K2 * K3 * 4;
+  const int g0 = blockIdx.x * G;
+  const int i = blockIdx.y * blockDim.x + threadIdx.x;
+  if (i >= nsite) return;
+  const float4 rec = site_rec[i];
+  const int gp = site_grid[i];
+  float w1[P], w2[P], w3[P];
+  bspline_w<P>(rec.x, w1);
+  bspline_w<P>(rec.y, w2);
+  bspline_w<P>(rec.z, w3);
+  const int g1 = gp & 1023, g2 = (gp >> 10) & 1023, g3 = (gp >> 20) & 1023;
+  int xo[P];
+#pragma unroll
+  for (int c = 0; c < P; ++c) xo[c] = wrapi(g1 - c, K1);
+  float acc[G];
+#pragma unroll
+  for (int j = 0; j < G; ++j) acc[j] = 0.f;
+#pragma unroll
+  for (int c3 = 0; c3 < P; ++c3) {
+    const int z = wrapi(g3 - c3, K3);
+#pragma unroll
+    for (int c2 = 0; c2 < P; ++c2) {
+      const int y = wrapi(g2 - c2, K2);
+      const float w32 = w3[c3] * w2[c2];
+      const float* row = phi + (size_t)(g0 / 4) * gstride + (((size_t)z * K2 + y) * K1) * 4;
+#pragma unroll
+      for (int c1 = 0; c1 < P; ++c1) {
+        const float w = w32 * w1[c1];
+        const float* src = row + (size_t)xo[c1] * 4;
+#pragma unroll
+        for (int v = 0; v < G / 4; ++v) {
+          const float4 q = __ldg(reinterpret_cast<const float4*>(src + v * gstride));
+          acc[4 * v + 0] = fmaf(w, q.x, acc[4 * v + 0]);
+          acc[4 * v + 1] = fmaf(w, q.y, acc[4 * v + 1]);
+          acc[4 * v + 2] = fmaf(w, q.z, acc[4 * v + 2]);
+          acc[4 * v + 3] = fmaf(w, q.w, acc[4 * v + 3]);
+        }
+      }
+    }
+  }
+  float4* out = reinterpret_cast<float4*>(site_e + (size_t)i * ldb + g0);
+#pragma unroll
+  for (int v = 0; v < G / 4; ++v)
+    out[v] = make_float4(rec.w * acc[4 * v + 0], rec.w * acc[4 * v + 1], rec.w * acc[4 * v + 2], rec.w * acc[4 * v + 3]);
+}
+
+// Mixed path, step 2 -- per molecule x G placements: FP64 sum of the site terms, real
+// space, residual, then the G bin searches in lockstep (binary lifting over the edge
+// keys staged in shared memory), histograms and per-species partials.
+template <int G>
+__global__ void __launch_bounds__(256) mol_finish_kernel(MolArgs A, const float* __restrict__ site_e) {
+  extern __shared__ int smem_dyn[];
+  int* smem_hist = smem_dyn;                                                  // [G][ermax]
+  long long* skeys = reinterpret_cast<long long*>(smem_dyn + ((G * A.ermax + 1) & ~1));  // [ermax]
+  __shared__ double su[G][256];
+  __shared__ unsigned char sspec[256];
+  const int tile = blockIdx.y;
+  const int g0 = blockIdx.x * G;
+  const BatchArgs& a = A.a;
+  const int ng = min(G, a.nb - g0);
+  const int m = tile * blockDim.x + threadIdx.x;
+  const bool valid = m < A.slvmax;
+  for (int i = threadIdx.x; i < G * A.ermax; i += blockDim.x) smem_hist[i] = 0;
+  for (int i = threadIdx.x; i < A.ermax; i += blockDim.x) skeys[i] = A.uvkey[i];
+  int k = -1, s0 = 0, ns = 0, species = 0;
+  double qmol = 0.0;
+  if (valid) {
+    k = A.slot_mol[m];
+    s0 = A.slot_site[m];
+    ns = A.slot_site[m + 1] - s0;
+    species = A.slot_species[m];
+    qmol = A.slot_qmol[m];
+  }
+  const bool spec_ok = valid && species >= 1 && species <= A.numslv;
+  sspec[threadIdx.x] = (unsigned char)(spec_ok ? species : 0);
+  const int ldb = A.ldb;
+  LjK k32;
+  {
+    const LjK64 k64 = make_k64(A);
+    k32 = to_f32(k64);
+  }
+  int sp_off = 0, sp_n = 1, sp_soft = 1;
+  if (spec_ok) {
+    sp_off = A.spec[3 * (species - 1)];
+    sp_n = A.spec[3 * (species - 1) + 1];
+    sp_soft = A.spec[3 * (species - 1) + 2];
+  }
+  const float rc = (float)fmax(A.elecut, A.upljcut);
+  const float mol_r = A.frame_scal[0];
+  // ---- totals for the G placements ----
+  double uu[G];
+  bool act[G];
+#pragma unroll
+  for (int j = 0; j < G; ++j) {
+    uu[j] = 0.0;
+    act[j] = false;
+    if (j < ng) {
+      const int b = g0 + j;
+      const int tg = a.tagslt[b] - 1;
+      const int kskip = (tg >= 0 && tg < A.nummol) ? A.mol_to_k[tg] : -2;
+      if (valid && k != kskip) {
+        double recip = 0.0;
+        for (int s = 0; s < ns; ++s) recip += (double)site_e[(size_t)(s0 + s) * ldb + b];
+        const double real = real_mixed(A, a, b, s0, ns, k32, rc + a.u_radius[b] + mol_r);
+        const double epcl = A.resid_fac * a.u_qmol[b] * qmol;
+        double pairep = -epcl;
+        pairep = pairep + recip;
+        uu[j] = real + pairep;
+        act[j] = true;
+        if (a.uvengy_out) a.uvengy_out[(size_t)(a.b0 + b) * (A.slvmax + 1) + k + 1] = uu[j];
+      } else if (valid && a.uvengy_out) {
+        a.uvengy_out[(size_t)(a.b0 + b) * (A.slvmax + 1) + k + 1] = 0.0;
+      }
+    }
+  }
+  __syncthreads();  // histograms zeroed, keys staged
+  // ---- getiduv / binsearch for all G at once: ret = #edges < u ----
+  long long ku[G];
+  int pos[G];
+#pragma unroll
+  for (int j = 0; j < G; ++j) {
+    ku[j] = ordered_key(uu[j]);
+    pos[j] = 0;
+  }
+  int step = 1;
+  while ((step << 1) <= sp_n) step <<= 1;
+  const long long* kk = skeys + sp_off;
+  for (; step > 0; step >>= 1) {
+#pragma unroll
+    for (int j = 0; j < G; ++j) {
+      const int q = pos[j] + step;
+      if (q <= sp_n && kk[q - 1] < ku[j]) pos[j] = q;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < G; ++j) {
+    double u = __longlong_as_double(0x7ff8000000000000ll);  // NaN marks "no molecule"
+    if (act[j]) {
+      const double v = uu[j];
+      const int ret = pos[j];
+      int code = 0;
+      if (!spec_ok)
+        code = ERMOD_E_ENG_CNS;
+      else if (v != v || ret <= 0)
+        code = ERMOD_E_ENG_MIN;
+      else if (A.soln && ret > sp_soft)
+        code = ERMOD_E_ENG_SFT;
+      else if (ret == sp_n && v < 1.0e3 && A.mbin_mode != 0) {
+        if (A.mbin_mode == 1)
+          code = ERMOD_W_MBIN;
+        else
+          atomicOr(&A.status->mbin_hit, 1);
+      }
+      if (code)
+        atomicMin(&A.status->err_key, make_err_key(a.b0 + g0 + j, k + 1, code));
+      else
+        hist_add(smem_hist + j * A.ermax, sp_off + ret - 1);
+      u = v;
+    }
+    su[j][threadIdx.x] = u;
+  }
+  __syncthreads();
+  // per-species {sum, min, max} of the block: one warp per (placement, species),
+  // fixed lane order and a fixed shuffle tree
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int pr = warp; pr < ng * A.numslv; pr += blockDim.x / 32) {
+    const int j = pr / A.numslv, sp = pr % A.numslv + 1;
+    double s = 0.0, mn = INFINITY, mx = -INFINITY;
+    for (int t = lane; t < blockDim.x; t += 32) {
+      const double v = su[j][t];
+      if (sspec[t] == sp && v == v) {
+        s += v;
+        mn = fmin(mn, v);
+        mx = fmax(mx, v);
+      }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      s += __shfl_down_sync(0xffffffffu, s, off);
+      mn = fmin(mn, __shfl_down_sync(0xffffffffu, mn, off));
+      mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, off));
+    }
+    if (lane == 0) {
+      double* pt = a.part + (((size_t)(g0 + j) * A.ntile + tile) * A.numslv + (sp - 1)) * 3;
+      pt[0] = s;
+      pt[1] = mn;
+      pt[2] = mx;
+    }
+  }
+  for (int j = 0; j < ng; ++j) {
+    const int* h = smem_hist + j * A.ermax;
+    int* out = a.hist + (size_t)(g0 + j) * A.ermax;
+    for (int i = threadIdx.x; i < A.ermax; i += blockDim.x) {
+      const int c = h[i];
+      if (c) atomicAdd(out + i, c);
+    }
+  }
+}
+
 template <bool MIXED>
 cudaError_t launch_p(Engine& e, const MolArgs& A, dim3 grid, size_t smem) {
   switch (e.P_order) {
@@ -541,7 +833,7 @@ cudaError_t launch_p(Engine& e, const MolArgs& A, dim3 grid, size_t smem) {
 }
 
 template <bool MIXED>
-cudaError_t set_smem_attr(size_t smem) {
+cudaError_t set_smem_attr(size_t smem) {  // FP64 instantiations only
   cudaError_t err = cudaSuccess;
   err = cudaFuncSetAttribute(mol_energy_kernel<MIXED, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
@@ -570,7 +862,10 @@ cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
   A.nummol = e.nummol;
   A.ljene = e.d_ljene;
   A.ljlensq = e.d_ljlensq;
+  A.ljene_f = e.d_ljene_f;
+  A.ljlensq_f = e.d_ljlensq_f;
   A.T = e.ljtype_max;
+  A.ldb = e.Bmax;
   A.uvkey = e.d_uvkey;
   A.spec = e.d_spec;
   A.numslv = e.numslv;
@@ -588,18 +883,53 @@ cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
   A.ntile = e.ntile;
   A.status = e.d_status;
   const size_t smem = sizeof(int) * (size_t)a.G * e.ermax;
-  static bool attr_set[2] = {false, false};
-  static size_t attr_smem[2] = {0, 0};
-  const int mi = e.mixed ? 1 : 0;
-  if (!attr_set[mi] || attr_smem[mi] < smem) {
-    cudaError_t err = e.mixed ? set_smem_attr<true>(smem) : set_smem_attr<false>(smem);
-    if (err != cudaSuccess) return err;
-    attr_set[mi] = true;
-    attr_smem[mi] = smem;
-  }
   dim3 grid(e.ntile, (a.nb + a.G - 1) / a.G);
   e.count_launch();
-  return e.mixed ? launch_p<true>(e, A, grid, smem) : launch_p<false>(e, A, grid, smem);
+  cudaError_t err = cudaSuccess;
+  if (!e.mixed) {
+    static size_t attr = 0;
+    if (attr < smem) {
+      if ((err = set_smem_attr<false>(smem)) != cudaSuccess) return err;
+      attr = smem;
+    }
+    return launch_p<false>(e, A, grid, smem);
+  }
+  if (a.G != 8 && a.G != 4) return cudaErrorInvalidValue;
+  {  // step 1: gather
+    dim3 g1((a.nb + a.G - 1) / a.G, (e.nsite_phys + 255) / 256);
+    const int K1 = e.geom.K[0], K2 = e.geom.K[1], K3 = e.geom.K[2];
+#define ERMOD_GATHER(PP, GG)                                                                                   \
+  if (e.P_order == PP && a.G == GG)                                                                            \
+    gather_kernel<PP, GG><<<g1, 256, 0, e.stream>>>(a.phi, e.d_site_rec, e.d_site_grid, e.nsite_phys, K1, K2, K3, \
+                                                    e.Bmax, e.d_site_e);
+    ERMOD_GATHER(4, 4)
+    ERMOD_GATHER(4, 8)
+    ERMOD_GATHER(6, 4)
+    ERMOD_GATHER(6, 8)
+    ERMOD_GATHER(8, 4)
+    ERMOD_GATHER(8, 8)
+#undef ERMOD_GATHER
+    e.count_launch();
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  }
+  // step 2: per-molecule totals and binning (histograms + edge keys in shared memory)
+  const size_t smem_f = sizeof(int) * (((size_t)a.G * e.ermax + 1) & ~(size_t)1) + sizeof(long long) * e.ermax;
+  dim3 g2((a.nb + a.G - 1) / a.G, e.ntile);
+#define ERMOD_FINISH(GG)                                                                                   \
+  if (a.G == GG) {                                                                                         \
+    static size_t attr = 0;                                                                                \
+    if (attr < smem_f) {                                                                                   \
+      err = cudaFuncSetAttribute(mol_finish_kernel<GG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_f); \
+      if (err != cudaSuccess) return err;                                                                  \
+      attr = smem_f;                                                                                       \
+    }                                                                                                      \
+    mol_finish_kernel<GG><<<g2, 256, smem_f, e.stream>>>(A, e.d_site_e);                                   \
+  }
+  ERMOD_FINISH(4)
+  ERMOD_FINISH(8)
+#undef ERMOD_FINISH
+  e.count_launch();
+  return cudaGetLastError();
 }
 
 }  // namespace ermod

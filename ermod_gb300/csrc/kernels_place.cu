@@ -153,8 +153,7 @@ __global__ void __launch_bounds__(256) place_prep_kernel(PrepArgs A) {
       float re = 0.f, im = 0.f;
       for (int c = 0; c < P; ++c) {
         const float th = (float)a.u_w[(us * 3 + ax) * kMaxSplineOrder + c];
-        long long m = (long long)k * (long long)(grd - c);
-        int mm = (int)(m % K);
+        int mm = (k * (grd - c)) % K;  // |k (grd - c)| < 1000 * 1008 fits in int
         if (mm < 0) mm += K;
         const float2 w = tw[mm];
         re = fmaf(th, w.x, re);
@@ -227,8 +226,8 @@ __device__ __forceinline__ ff ff_add2(ff a, ff b) {
 }
 
 constexpr int kSpecThreads = 256;
-constexpr int kSpecPts = 4;  // points per thread
-constexpr int kSpecChunk = 16;  // solute sites per shared-memory chunk
+constexpr int kSpecChunk = 32;  // solute sites staged in shared memory at once
+constexpr int kR1 = 4, kR2 = 4;  // register micro-tile: 4 k1 x 4 k2 points per thread
 
 struct SpecArgs {
   const float2* bvec;     // [nb][S][3][Kmax]
@@ -236,73 +235,93 @@ struct SpecArgs {
   const int* u_nsite;
   const float* engfac;    // [K3][K2][H]
   float2* spec;           // [nb][K3][K2][H]
-  double* self_part;      // [nb][K3][nchunk]
-  int K1, K2, K3, H, Kmax, kc, nchunk;
+  double* self_part;      // [nb][K3]
+  int K1, K2, K3, H, Kmax;
 };
 
-// grid: (nchunk, K3, nb); block: 256 threads; points (k1, k2) with k2 in [k2c*kc, +kc)
+// grid: (K3, nb); one CTA computes the (k1, k2) plane of one k3 for one placement:
+//   Q(k1,k2,k3) = sum_s [q_s b3_s(k3) b2_s(k2)] b1_s(k1)
+// as a sum of rank-1 updates over register micro-tiles of 4 x 4 points.
 __global__ void __launch_bounds__(kSpecThreads) spectrum_kernel(SpecArgs A) {
-  const int chunk = blockIdx.x, k3 = blockIdx.y, b = blockIdx.z;
+  extern __shared__ float2 smem_spec[];
+  float2* sd = smem_spec;                           // [kSpecChunk][K2]
+  float2* sb = smem_spec + (size_t)kSpecChunk * A.K2;  // [kSpecChunk][H padded to 4]
+  const int k3 = blockIdx.x, b = blockIdx.y;
   const int ns = A.u_nsite[b];
-  const int k2lo = chunk * A.kc;
-  const int k2n = min(A.kc, A.K2 - k2lo);
-  const int npts = A.H * k2n;
-  __shared__ float2 sd[kSpecChunk][64];   // c3_s * b2_s(k2), k2 local (kc <= 64)
-  __shared__ float2 sb1[kSpecChunk][128]; // b1_s(k1), H <= 128 here
-  float2 acc[kSpecPts];
-#pragma unroll
-  for (int j = 0; j < kSpecPts; ++j) acc[j] = make_float2(0.f, 0.f);
+  const int TX = (A.H + kR1 - 1) / kR1, TY = (A.K2 + kR2 - 1) / kR2;
+  const int Hp = TX * kR1;
+  const int ntiles = TX * TY;
   const float2* bv = A.bvec + (size_t)b * kMaxSoluteSites * 3 * A.Kmax;
+  float2* spec = A.spec + (size_t)b * A.K3 * A.K2 * A.H + (size_t)k3 * A.K2 * A.H;
+  const float* ef = A.engfac + (size_t)k3 * A.K2 * A.H;
+  const bool even = (A.K1 % 2) == 0;
+  ff self{0.f, 0.f};
   for (int s0 = 0; s0 < ns; s0 += kSpecChunk) {
     const int nsc = min(kSpecChunk, ns - s0);
+    const bool first = (s0 == 0), last = (s0 + nsc >= ns);
     __syncthreads();
-    for (int t = threadIdx.x; t < nsc * k2n; t += blockDim.x) {
-      const int s = t / k2n, kk = t % k2n;
-      const size_t us = (size_t)(s0 + s);
+    for (int t = threadIdx.x; t < nsc * A.K2; t += blockDim.x) {
+      const int sl = t / A.K2, k2 = t % A.K2;
+      const size_t us = (size_t)(s0 + sl);
       const float q = (float)A.u_q[(size_t)b * kMaxSoluteSites + us];
       const float2 b3 = bv[(us * 3 + 2) * A.Kmax + k3];
-      const float2 b2 = bv[(us * 3 + 1) * A.Kmax + k2lo + kk];
+      const float2 b2 = bv[(us * 3 + 1) * A.Kmax + k2];
       const float2 c3 = make_float2(q * b3.x, q * b3.y);
-      sd[s][kk] = make_float2(c3.x * b2.x - c3.y * b2.y, c3.x * b2.y + c3.y * b2.x);
+      sd[sl * A.K2 + k2] = make_float2(c3.x * b2.x - c3.y * b2.y, c3.x * b2.y + c3.y * b2.x);
     }
-    for (int t = threadIdx.x; t < nsc * A.H; t += blockDim.x) {
-      const int s = t / A.H, k1 = t % A.H;
-      sb1[s][k1] = bv[((size_t)(s0 + s) * 3 + 0) * A.Kmax + k1];
+    for (int t = threadIdx.x; t < nsc * Hp; t += blockDim.x) {
+      const int sl = t / Hp, k1 = t % Hp;
+      sb[sl * Hp + k1] = (k1 < A.H) ? bv[((size_t)(s0 + sl) * 3 + 0) * A.Kmax + k1] : make_float2(0.f, 0.f);
     }
     __syncthreads();
+    for (int mt = threadIdx.x; mt < ntiles; mt += blockDim.x) {
+      const int tx = mt % TX, ty = mt / TX;
+      const int k1a = tx * kR1, k2a = ty * kR2;
+      float2 acc[kR2][kR1];
 #pragma unroll
-    for (int j = 0; j < kSpecPts; ++j) {
-      const int p = threadIdx.x + j * kSpecThreads;
-      if (p < npts) {
-        const int k1 = p % A.H, kk = p / A.H;
-        float re = acc[j].x, im = acc[j].y;
-        for (int s = 0; s < nsc; ++s) {
-          const float2 d = sd[s][kk], e = sb1[s][k1];
-          re = fmaf(d.x, e.x, fmaf(-d.y, e.y, re));
-          im = fmaf(d.x, e.y, fmaf(d.y, e.x, im));
+      for (int j = 0; j < kR2; ++j)
+#pragma unroll
+        for (int i = 0; i < kR1; ++i) acc[j][i] = make_float2(0.f, 0.f);
+      for (int sl = 0; sl < nsc; ++sl) {
+        float2 d[kR2], e[kR1];
+#pragma unroll
+        for (int j = 0; j < kR2; ++j) d[j] = (k2a + j < A.K2) ? sd[sl * A.K2 + k2a + j] : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int i = 0; i < kR1; ++i) e[i] = sb[sl * Hp + k1a + i];
+#pragma unroll
+        for (int j = 0; j < kR2; ++j)
+#pragma unroll
+          for (int i = 0; i < kR1; ++i) {
+            acc[j][i].x = fmaf(d[j].x, e[i].x, fmaf(-d[j].y, e[i].y, acc[j][i].x));
+            acc[j][i].y = fmaf(d[j].x, e[i].y, fmaf(d[j].y, e[i].x, acc[j][i].y));
+          }
+      }
+#pragma unroll
+      for (int j = 0; j < kR2; ++j) {
+        const int k2 = k2a + j;
+        if (k2 >= A.K2) continue;
+#pragma unroll
+        for (int i = 0; i < kR1; ++i) {
+          const int k1 = k1a + i;
+          if (k1 >= A.H) continue;
+          const size_t gi = (size_t)k2 * A.H + k1;
+          float2 q = acc[j][i];
+          if (!first) {  // earlier site chunks left the partial sum in the output
+            const float2 prev = spec[gi];
+            q.x += prev.x;
+            q.y += prev.y;
+          }
+          if (last) {
+            const float f = ef[gi];
+            const float wgt = (k1 == 0 || (even && k1 == A.H - 1)) ? 0.5f : 1.f;
+            self = ff_add(self, wgt * f * (q.x * q.x + q.y * q.y));
+            q = make_float2(f * q.x, f * q.y);
+          }
+          spec[gi] = q;
         }
-        acc[j] = make_float2(re, im);
       }
     }
   }
-  // engfac multiply + self-energy terms
-  ff self{0.f, 0.f};
-  const bool even = (A.K1 % 2) == 0;
-#pragma unroll
-  for (int j = 0; j < kSpecPts; ++j) {
-    const int p = threadIdx.x + j * kSpecThreads;
-    if (p < npts) {
-      const int k1 = p % A.H, k2 = k2lo + p / A.H;
-      const size_t gi = ((size_t)k3 * A.K2 + k2) * A.H + k1;
-      const float ef = A.engfac[gi];
-      const float2 q = acc[j];
-      float wgt = 1.f;
-      if (k1 == 0 || (even && k1 == A.H - 1)) wgt = 0.5f;
-      self = ff_add(self, wgt * ef * (q.x * q.x + q.y * q.y));
-      A.spec[(size_t)b * A.K3 * A.K2 * A.H + gi] = make_float2(ef * q.x, ef * q.y);
-    }
-  }
-  // warp + block reduction (float-float), then FP64 partial
   for (int off = 16; off > 0; off >>= 1) {
     ff o{__shfl_down_sync(0xffffffffu, self.hi, off), __shfl_down_sync(0xffffffffu, self.lo, off)};
     self = ff_add2(self, o);
@@ -313,7 +332,7 @@ __global__ void __launch_bounds__(kSpecThreads) spectrum_kernel(SpecArgs A) {
   if (threadIdx.x == 0) {
     double t = 0.0;
     for (int w = 0; w < kSpecThreads / 32; ++w) t += wsum[w];
-    A.self_part[((size_t)b * A.K3 + k3) * A.nchunk + chunk] = t;
+    A.self_part[(size_t)b * A.K3 + k3] = t;
   }
 }
 
@@ -400,7 +419,7 @@ Coef make_coef(int order, double screen) {
 
 }  // namespace
 
-int spectrum_chunk(int H) { return std::max(1, std::min(64, (kSpecThreads * kSpecPts) / H)); }
+int spectrum_partials(const Engine& e) { return e.geom.K[2]; }
 
 cudaError_t launch_place_prep(Engine& e, const BatchArgs& a, const double* sol_xyz, int self_mode) {
   PrepArgs A{};
@@ -436,10 +455,16 @@ cudaError_t launch_spectrum(Engine& e, const BatchArgs& a) {
   A.K3 = e.geom.K[2];
   A.H = e.H();
   A.Kmax = e.Kmax();
-  A.kc = spectrum_chunk(A.H);
-  A.nchunk = (A.K2 + A.kc - 1) / A.kc;
-  dim3 grid(A.nchunk, A.K3, a.nb);
-  spectrum_kernel<<<grid, kSpecThreads, 0, e.stream>>>(A);
+  const int Hp = ((A.H + kR1 - 1) / kR1) * kR1;
+  const size_t smem = sizeof(float2) * (size_t)kSpecChunk * (A.K2 + Hp);
+  static size_t attr = 0;
+  if (attr < smem) {
+    cudaError_t err = cudaFuncSetAttribute(spectrum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    attr = smem;
+  }
+  dim3 grid(A.K3, a.nb);
+  spectrum_kernel<<<grid, kSpecThreads, smem, e.stream>>>(A);
   e.count_launch();
   return cudaGetLastError();
 }

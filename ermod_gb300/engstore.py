@@ -1,0 +1,52 @@
+"""engstore: merge of per-rank accumulators and normalisation (engproc.F90:451-560).
+
+ERmod shards frames over MPI ranks (plmode = 2) and reduces the accumulators in
+``engstore``: MAX of ``voffset`` with a per-rank rescale exp(+-(voffset_local -
+voffset)/kT), SUM of engnorm/engsmpl/avslf/eself/slnuv/edens/ecorr, MIN/MAX of
+minuv/maxuv, then division by engnorm.  Here every GPU (one process per GPU) owns a
+shard of the frames; the exchange is the same reduction, done on the host through
+``ermod_engstore_merge`` after gathering the raw accumulators with
+``torch.distributed`` (any backend: NCCL between GPU ranks, gloo on CPU).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _lib
+
+
+def merge(accums: list, slttype: int, wgtslf: int, temp: float) -> dict:
+    """accums: raw accumulators (EnergyRepresentation.accum() dicts) of every rank."""
+    n = len(accums)
+    E = len(accums[0]["edens"])
+    S = len(accums[0]["eself"])
+    N = len(accums[0]["slnuv"])
+    has_corr = accums[0].get("ecorr") is not None
+    edens = np.ascontiguousarray(np.stack([a["edens"] for a in accums]), np.float64)
+    ecorr = (np.ascontiguousarray(np.stack([np.asarray(a["ecorr"]).ravel(order="F") for a in accums]), np.float64)
+             if has_corr else None)
+    eself = np.ascontiguousarray(np.stack([a["eself"] for a in accums]), np.float64) if S else None
+    slnuv = np.ascontiguousarray(np.stack([a["slnuv"] for a in accums]), np.float64)
+    minuv = np.ascontiguousarray(np.stack([a["minuv"] for a in accums]), np.float64)
+    maxuv = np.ascontiguousarray(np.stack([a["maxuv"] for a in accums]), np.float64)
+    sc = np.ascontiguousarray(np.stack([[a["engnorm"], a["engsmpl"], a["avslf"], a["voffset"],
+                                         1.0 if a["voffset_initialized"] else 0.0] for a in accums]), np.float64)
+    _lib.check(_lib.load().ermod_engstore_merge(n, int(slttype), int(wgtslf), float(temp), E, S, N, _lib.dp(edens),
+                                                _lib.dp(ecorr), _lib.dp(eself), _lib.dp(slnuv), _lib.dp(minuv),
+                                                _lib.dp(maxuv), _lib.dp(sc)), "ermod_engstore_merge")
+    return dict(edens=edens[0], ecorr=None if ecorr is None else ecorr[0].reshape(E, E, order="F"),
+                eself=eself[0] if S else eself, slnuv=slnuv[0], minuv=minuv[0], maxuv=maxuv[0],
+                engnorm=sc[0, 0], engsmpl=sc[0, 1], avslf=sc[0, 2], voffset=sc[0, 3])
+
+
+def merge_distributed(acc: dict, slttype: int, wgtslf: int, temp: float, group=None):
+    """Gather every rank's raw accumulators to rank 0 and merge there (None elsewhere)."""
+    import torch.distributed as dist
+    world = dist.get_world_size(group)
+    rank = dist.get_rank(group)
+    gathered = [None] * world if rank == 0 else None
+    payload = {k: (np.asarray(v) if isinstance(v, np.ndarray) else v) for k, v in acc.items()}
+    dist.gather_object(payload, gathered, dst=0, group=group)
+    if rank != 0:
+        return None
+    return merge(gathered, slttype, wgtslf, temp)
