@@ -166,6 +166,12 @@ static int free_frame(Engine& e) {
   dfree(e.d_site_w);
   dfree(e.d_site_q);
   dfree(e.d_frame_scal);
+  dfree(e.d_brick_key);
+  dfree(e.d_brick_key_alt);
+  dfree(e.d_brick_val);
+  dfree(e.d_brick_site);
+  dfree(e.d_brick_count);
+  dfree(e.d_brick_start);
   return ERMOD_OK;
 }
 
@@ -201,6 +207,36 @@ static int free_bins(Engine& e) {
   return ERMOD_OK;
 }
 
+// TMA descriptor of the padded potential grids, a 4-D tensor
+// [B][ZP][YP][XP] (x innermost); one box = the gather halo of a brick for 4 placements
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static int make_phi_tmap(Engine& e, float* phi) {
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  cudaError_t err = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+  if (err != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn) {
+    g_err = "cuTensorMapEncodeTiled is not available";
+    return ERMOD_E_CUDA;
+  }
+  const cuuint64_t XP = e.phi_dims[0], YP = e.phi_dims[1], ZP = e.phi_dims[2];
+  const cuuint64_t dims[4] = {XP, YP, ZP, (cuuint64_t)e.Bmax};
+  const cuuint64_t strides[3] = {XP * 4, XP * YP * 4, XP * YP * ZP * 4};
+  const cuuint32_t box[4] = {(cuuint32_t)e.gbox[0], (cuuint32_t)e.gbox[1], (cuuint32_t)e.gbox[2], 4};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  const CUresult r = ((EncodeTiledFn)fn)(&e.phi_tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, phi, dims, strides, box, estr,
+                                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                         CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    g_err = "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")";
+    return ERMOD_E_CUDA;
+  }
+  e.tmap_ready = true;
+  return ERMOD_OK;
+}
+
 // batch buffers: need topology (slvmax), bins (ermax, numslv) and the PME grid
 static int ensure_batch(Engine& e) {
   if (e.buf.u_nsite) return ERMOD_OK;
@@ -225,7 +261,18 @@ static int ensure_batch(Engine& e) {
     ERMOD_CUDA(dalloc(&b.u_bvec, (size_t)B * S * 3 * e.Kmax()));
     ERMOD_CUDA(dalloc(&e.d_site_e, (size_t)e.nsite_phys * B));
     ERMOD_CUDA(dalloc(&b.spec, nc * B));
-    ERMOD_CUDA(dalloc(&b.phi, nr * B));
+    const int h = e.P_order - 1;
+    e.phi_dims[0] = ((e.geom.K[0] + h + 3) / 4) * 4;
+    e.phi_dims[1] = e.geom.K[1] + h;
+    e.phi_dims[2] = e.geom.K[2] + h;
+    e.gbox[0] = ((8 + h + 3) / 4) * 4;
+    e.gbox[1] = 8 + h;
+    e.gbox[2] = 8 + h;
+    const size_t np = (size_t)e.phi_dims[0] * e.phi_dims[1] * e.phi_dims[2];
+    ERMOD_CUDA(dalloc(&b.phi, np * B));
+    ERMOD_CUDA(cudaMemset(b.phi, 0, sizeof(float) * np * B));
+    int st = make_phi_tmap(e, b.phi);
+    if (st) return st;
     ERMOD_CUDA(dalloc(&b.self_part, (size_t)B * spectrum_partials(e)));
   } else {
     ERMOD_CUDA(dalloc(&b.spec64, nc * B));
@@ -555,7 +602,9 @@ int ermod_set_topology(ermod_ctx* c, int nummol, int numatm, const int* mbi, con
   ERMOD_CUDA(dalloc(&e.d_sort_val, e.slvmax));
   ERMOD_CUDA(dalloc(&e.d_sort_val_alt, e.slvmax + 1));
   ERMOD_CUDA(cudaMemset(e.d_sort_val_alt, 0, sizeof(int) * (e.slvmax + 1)));
-  e.cub_tmp_bytes = frame_cub_bytes(e.slvmax);
+  for (int i = 0; i < 3; ++i) e.nbrick[i] = (e.geom.K[i] + 7) / 8;
+  e.nbricks = e.nbrick[0] * e.nbrick[1] * e.nbrick[2];
+  e.cub_tmp_bytes = std::max(frame_cub_bytes(e.slvmax), brick_cub_bytes(e.nsite_phys, e.nbricks));
   ERMOD_CUDA(dalloc((char**)&e.d_cub_tmp, e.cub_tmp_bytes));
   ERMOD_CUDA(dalloc(&e.d_slot_mol, e.slvmax));
   ERMOD_CUDA(dalloc(&e.d_slot_site, e.slvmax + 1));
@@ -565,6 +614,12 @@ int ermod_set_topology(ermod_ctx* c, int nummol, int numatm, const int* mbi, con
   ERMOD_CUDA(dalloc(&e.d_site_grid, e.nsite_phys));
   if (e.mixed) {
     ERMOD_CUDA(dalloc(&e.d_site_rec, e.nsite_phys));
+    ERMOD_CUDA(dalloc(&e.d_brick_key, e.nsite_phys));
+    ERMOD_CUDA(dalloc(&e.d_brick_key_alt, e.nsite_phys));
+    ERMOD_CUDA(dalloc(&e.d_brick_val, e.nsite_phys));
+    ERMOD_CUDA(dalloc(&e.d_brick_site, e.nsite_phys));
+    ERMOD_CUDA(dalloc(&e.d_brick_count, e.nbricks + 1));
+    ERMOD_CUDA(dalloc(&e.d_brick_start, e.nbricks + 1));
   } else {
     ERMOD_CUDA(dalloc(&e.d_site_x, 3 * (size_t)e.nsite_phys));
     ERMOD_CUDA(dalloc(&e.d_site_w, (size_t)e.nsite_phys * 3 * e.P_order));
@@ -693,6 +748,7 @@ static int frame_launch(Engine& e) {
   ERMOD_CUDA(launch_frame_wrap(e));
   ERMOD_CUDA(launch_frame_sort(e));
   ERMOD_CUDA(launch_frame_sites(e));
+  if (e.mixed) ERMOD_CUDA(launch_frame_bricks(e));
   e.phase_end();
   e.frame_ready = true;
   return ERMOD_OK;

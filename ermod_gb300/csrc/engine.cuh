@@ -1,6 +1,7 @@
 // engine.cuh -- the context behind ermod_ctx (host side state + device buffers).
 #pragma once
 
+#include <cuda.h>  // CUtensorMap (types only; the encoder is fetched at run time)
 #include <cufft.h>
 
 #include <algorithm>
@@ -104,6 +105,14 @@ struct Engine {
   double* d_site_w = nullptr;     // FP64 path [nsite_phys][3][P]
   double* d_site_q = nullptr;     // FP64 path
   float* d_frame_scal = nullptr;  // [0] max molecule radius about its first site (A)
+  // sites grouped by 8^3 bricks of the PME grid (the mixed gather's unit of work)
+  int nbrick[3] = {1, 1, 1}, nbricks = 1;
+  unsigned int* d_brick_key = nullptr;
+  unsigned int* d_brick_key_alt = nullptr;
+  int* d_brick_val = nullptr;
+  int* d_brick_site = nullptr;   // [nsite_phys] site indices (slot order) sorted by brick
+  int* d_brick_count = nullptr;  // [nbricks+1]
+  int* d_brick_start = nullptr;  // [nbricks+1]
 
   // ---- batch buffers ---------------------------------------------------------------
   int Bmax = 1, G = 1, ntile = 1, tile = 256;
@@ -130,6 +139,12 @@ struct Engine {
   double err_energy = 0.0;
   int call_b0 = 0;
 
+  // ---- mixed path potential grids: padded periodic layout + TMA descriptor ----------
+  int phi_dims[3] = {0, 0, 0};   // XP (multiple of 4), YP, ZP
+  int gbox[3] = {0, 0, 0};       // gather box: x (multiple of 4), y, z
+  alignas(64) CUtensorMap phi_tmap;
+  bool tmap_ready = false;
+
   // ---- cuFFT -------------------------------------------------------------------------
   cufftHandle plan_c2r = 0, plan_d2z = 0, plan_z2d = 0;
   bool plans_ready = false;
@@ -150,6 +165,8 @@ int spectrum_partials(const Engine& e);
 int influence64_blocks();
 int accumulate_max_batch();
 size_t frame_cub_bytes(int n);
+size_t brick_cub_bytes(int nsite, int nbricks);
+cudaError_t launch_frame_bricks(Engine& e);
 double host_spline_value(int order, double x);
 
 // host utilities (engine.cu)

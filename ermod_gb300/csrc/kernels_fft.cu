@@ -9,11 +9,9 @@
 //           0.5 sum_k engfac |S|^2 (recpcal.F90:385-394) with float-float compensation,
 //           and transforms the slab along k3 (inverse, unnormalised) in shared memory.
 //           Output T1[b][z][k2][k1] (complex FP32).
-//   pme_b   CTA per (z, group of 4 placements).  For each placement: the k2 transform of
-//           the (k2, k1) plane, then the complex-to-real transform along k1, two rows per
-//           complex transform (Z = X + iY).  The four placements' real planes are staged
-//           in shared memory and written as phi[group][z][y][x][4], i.e. interleaved by
-//           placement, with coalesced 16-byte stores.
+//   pme_b   CTA per (z, placement): the k2 transform of the (k2, k1) plane, then the
+//           complex-to-real transform along k1, two rows per complex transform
+//           (Z = X + iY); writes the real plane phi[b][z][y][x] with coalesced stores.
 // Transforms are self-sorting Stockham passes (radices 2-16, composite radices done in
 // registers), unnormalised, sign +1, exactly the conventions of fft_iface.F90.
 #include "engine.cuh"
@@ -334,10 +332,11 @@ struct PmeArgs {
   const float* engfac;  // [K3][K2][H]
   const float2* twiddle;  // per axis, exp(-2 pi i m / K): conjugated here for the inverse
   float2* t1;           // [nb][K3][K2][H]
-  float* phi;           // [nb/4][K3][K2][K1][4]
+  float* phi;           // [nb][K3][K2][K1]
   double* self_part;    // [nb][K2]
   int nb, K1, K2, K3, H, Hp, K1p, Kmax;
   int chunk;  // solute sites staged per generation chunk (fits the k3 work buffer)
+  int halo, XP, YP, ZP;  // padded periodic potential grid (see pme_b)
   FftPlan p1, p2, p3;
   FastDiv fH, fK1, fHp4, fnpair;
 };
@@ -452,19 +451,20 @@ __global__ void __launch_bounds__(256) pme_a_kernel(PmeArgs A) {
   }
 }
 
-__global__ void __launch_bounds__(512) pme_b_kernel(PmeArgs A) {
+// CTA per (z, placement): the k2 transform of the (k2, k1) plane, then the
+// complex-to-real transform along k1, two rows per complex transform; writes the real
+// plane phi[b][z][y][x] with coalesced row stores.
+__global__ void __launch_bounds__(256) pme_b_kernel(PmeArgs A) {
   extern __shared__ float2 sm[];
-  const int z = blockIdx.x, grp = blockIdx.y;
+  const int z = blockIdx.x, b = blockIdx.y;
   const int K1 = A.K1, K2 = A.K2, K3 = A.K3, H = A.H, K1p = A.K1p;
   const size_t plane = (size_t)K2 * H;
   const int npair = (K2 + 1) / 2;
   const size_t bufsz = max(plane, (size_t)npair * K1p);
   float2* s0 = sm;
   float2* s1 = sm + bufsz;
-  float* stage = reinterpret_cast<float*>(sm + 2 * bufsz);  // [4][K2][K1]
-  float2* tw1 = reinterpret_cast<float2*>(stage + (size_t)4 * K2 * K1);
+  float2* tw1 = s1 + bufsz;
   float2* tw2 = tw1 + K1;
-  const size_t pl = (size_t)K2 * K1;
   for (int i = threadIdx.x; i < K1 + K2; i += blockDim.x) {
     const float2 t = A.twiddle[i];
     if (i < K1)
@@ -472,56 +472,73 @@ __global__ void __launch_bounds__(512) pme_b_kernel(PmeArgs A) {
     else
       tw2[i - K1] = make_float2(t.x, -t.y);
   }
-  for (int bl = 0; bl < 4; ++bl) {
-    const int b = grp * 4 + bl;
-    float* st = stage + bl * pl;
-    __syncthreads();
-    if (b >= A.nb) {  // idle slots of a partial group are written as zeros
-      for (int t = threadIdx.x; t < (int)pl; t += blockDim.x) st[t] = 0.f;
-      continue;
-    }
-    const float2* in = A.t1 + ((size_t)b * K3 + z) * plane;
+  const float2* in = A.t1 + ((size_t)b * K3 + z) * plane;
+  if ((plane & 1) == 0) {  // every plane starts 16-byte aligned
+    const float4* in4 = reinterpret_cast<const float4*>(in);
+    float4* s04 = reinterpret_cast<float4*>(s0);
+    for (int t = threadIdx.x; t < (int)(plane / 2); t += blockDim.x) s04[t] = in4[t];
+  } else {
     for (int t = threadIdx.x; t < (int)plane; t += blockDim.x) s0[t] = in[t];
-    // k2 transform: columns k1 (stride 1), elements along k2 (stride H)
-    float2* r = fft_cols(s0, s1, A.p2, H, A.fH, H, 1, tw2);
-    float2* w = (r == s0) ? s1 : s0;
-    // pack row pairs: Z_p[k] = X_{2p}[k] + i X_{2p+1}[k], Hermitian-completed in k1;
-    // rows padded to K1p (odd) so the row transforms are bank-conflict free
-    for (int t = threadIdx.x; t < npair * K1; t += blockDim.x) {
-      const int pp = fdiv(t, A.fK1), k = t - pp * K1;
-      const int y0 = 2 * pp, y1 = 2 * pp + 1;
-      float2 x0, x1 = make_float2(0.f, 0.f);
-      const bool self_conj = (k == 0) || ((K1 % 2 == 0) && k == K1 / 2);
-      if (k < H) {
-        x0 = r[(size_t)y0 * H + k];
-        if (y1 < K2) x1 = r[(size_t)y1 * H + k];
-      } else {
-        const float2 a = r[(size_t)y0 * H + (K1 - k)];
-        x0 = make_float2(a.x, -a.y);
-        if (y1 < K2) {
-          const float2 c = r[(size_t)y1 * H + (K1 - k)];
-          x1 = make_float2(c.x, -c.y);
+  }
+  // k2 transform: columns k1 (stride 1), elements along k2 (stride H)
+  float2* r = fft_cols(s0, s1, A.p2, H, A.fH, H, 1, tw2);
+  float2* w = (r == s0) ? s1 : s0;
+  // pack row pairs: Z_p[k] = X_{2p}[k] + i X_{2p+1}[k], Hermitian-completed in k1;
+  // rows padded to K1p (odd) so the row transforms are bank-conflict free
+  for (int t = threadIdx.x; t < npair * K1; t += blockDim.x) {
+    const int pp = fdiv(t, A.fK1), k = t - pp * K1;
+    const int y0 = 2 * pp, y1 = 2 * pp + 1;
+    float2 x0, x1 = make_float2(0.f, 0.f);
+    const bool self_conj = (k == 0) || ((K1 % 2 == 0) && k == K1 / 2);
+    if (k < H) {
+      x0 = r[(size_t)y0 * H + k];
+      if (y1 < K2) x1 = r[(size_t)y1 * H + k];
+    } else {
+      const float2 a = r[(size_t)y0 * H + (K1 - k)];
+      x0 = make_float2(a.x, -a.y);
+      if (y1 < K2) {
+        const float2 c = r[(size_t)y1 * H + (K1 - k)];
+        x1 = make_float2(c.x, -c.y);
+      }
+    }
+    if (self_conj) {
+      x0.y = 0.f;
+      x1.y = 0.f;
+    }
+    w[(size_t)pp * K1p + k] = make_float2(x0.x - x1.y, x0.y + x1.x);
+  }
+  float2* res = fft_cols(w, r, A.p1, npair, A.fnpair, 1, K1p, tw1);
+  // padded periodic layout: grid point (x, y, z) lives at (x+h, y+h, z+h), h = P-1, and
+  // the last h points of every axis are repeated below 0, so any stencil halo of the
+  // gather is one in-bounds box (rows XP floats, planes YP rows, ZP planes)
+  const int h = A.halo;
+  float* out = A.phi + (size_t)b * A.ZP * A.YP * A.XP;
+  const int z0 = z + h, z1 = (z >= K3 - h) ? z - K3 + h : -1;
+  for (int t = threadIdx.x; t < npair * K1; t += blockDim.x) {
+    const int pp = fdiv(t, A.fK1), x = t - pp * K1;
+    const float2 v = res[(size_t)pp * K1p + x];
+    const int x0 = x + h, x1 = (x >= K1 - h) ? x - K1 + h : -1;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int y = 2 * pp + q;
+      if (y >= K2) break;
+      const float val = q ? v.y : v.x;
+      const int y0 = y + h, y1 = (y >= K2 - h) ? y - K2 + h : -1;
+#pragma unroll
+      for (int cz = 0; cz < 2; ++cz) {
+        const int zz = cz ? z1 : z0;
+        if (zz < 0) continue;
+#pragma unroll
+        for (int cy = 0; cy < 2; ++cy) {
+          const int yy = cy ? y1 : y0;
+          if (yy < 0) continue;
+          float* row = out + ((size_t)zz * A.YP + yy) * A.XP;
+          row[x0] = val;
+          if (x1 >= 0) row[x1] = val;
         }
       }
-      if (self_conj) {
-        x0.y = 0.f;
-        x1.y = 0.f;
-      }
-      w[(size_t)pp * K1p + k] = make_float2(x0.x - x1.y, x0.y + x1.x);
-    }
-    // row transforms along k1: one transform per row pair (column index), stride K1p
-    float2* res = fft_cols(w, r, A.p1, npair, A.fnpair, 1, K1p, tw1);
-    for (int t = threadIdx.x; t < npair * K1; t += blockDim.x) {
-      const int pp = fdiv(t, A.fK1), x = t - pp * K1;
-      const float2 v = res[(size_t)pp * K1p + x];
-      st[(size_t)(2 * pp) * K1 + x] = v.x;
-      if (2 * pp + 1 < K2) st[(size_t)(2 * pp + 1) * K1 + x] = v.y;
     }
   }
-  __syncthreads();
-  float4* dst = reinterpret_cast<float4*>(A.phi + (((size_t)grp * K3 + z) * pl) * 4);
-  for (int t = threadIdx.x; t < (int)pl; t += blockDim.x)
-    dst[t] = make_float4(stage[t], stage[pl + t], stage[2 * pl + t], stage[3 * pl + t]);
 }
 
 size_t pme_a_smem(int K3, int Hp) { return sizeof(float2) * ((size_t)2 * K3 * Hp + K3); }
@@ -529,7 +546,7 @@ size_t pme_b_smem(int K1, int K2, int H) {
   const size_t plane = (size_t)K2 * H;
   const size_t npair = (K2 + 1) / 2;
   const size_t bufsz = std::max(plane, npair * (size_t)(K1 | 1));
-  return sizeof(float2) * 2 * bufsz + sizeof(float) * (size_t)K2 * K1 * 4 + sizeof(float2) * (K1 + K2);
+  return sizeof(float2) * (2 * bufsz + K1 + K2);
 }
 
 }  // namespace
@@ -562,6 +579,10 @@ cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a) {
   A.chunk &= ~1;  // even chunk: the b1 staging rows stay 16-byte aligned
   if (A.chunk < 2) A.chunk = 2;
   A.K1p = A.K1 | 1;
+  A.halo = e.P_order - 1;
+  A.XP = e.phi_dims[0];
+  A.YP = e.phi_dims[1];
+  A.ZP = e.phi_dims[2];
   if (!plan(A.K1, A.p1) || !plan(A.K2, A.p2) || !plan(A.K3, A.p3)) return cudaErrorInvalidValue;
   A.fH = make_fastdiv(A.H);
   A.fK1 = make_fastdiv(A.K1);
@@ -585,7 +606,7 @@ cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a) {
   if ((err = cudaGetLastError()) != cudaSuccess) return err;
   e.phase_end();
   e.phase_begin(PH_FFT);
-  pme_b_kernel<<<dim3(A.K3, (a.nb + 3) / 4), 512, sb, e.stream>>>(A);
+  pme_b_kernel<<<dim3(A.K3, a.nb), 256, sb, e.stream>>>(A);
   e.count_launch();
   return cudaGetLastError();
 }

@@ -214,6 +214,23 @@ __global__ void frame_sites_kernel(SiteArgs A) {
   atomicMax((int*)&A.frame_scal[0], __float_as_int((float)rmax * 1.0001f + 1e-4f));
 }
 
+// brick of every site: the 8^3 block of PME grid points holding its stencil base point
+__global__ void brick_key_kernel(const int* __restrict__ site_grid, int nsite, int K1, int K2, int K3, int nbx,
+                                 int nby, unsigned int* __restrict__ key, int* __restrict__ val,
+                                 int* __restrict__ count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nsite) return;
+  const int gp = site_grid[i];
+  int g1 = gp & 1023, g2 = (gp >> 10) & 1023, g3 = (gp >> 20) & 1023;
+  if (g1 >= K1) g1 -= K1;
+  if (g2 >= K2) g2 -= K2;
+  if (g3 >= K3) g3 -= K3;
+  const unsigned int bk = (unsigned int)(((g3 >> 3) * nby + (g2 >> 3)) * nbx + (g1 >> 3));
+  key[i] = bk;
+  val[i] = i;
+  atomicAdd(&count[bk], 1);
+}
+
 // recpcal_spline_greenfunc (recpcal.F90:111-152)
 __global__ void greenfunc_kernel(FrameGeom g, int order, const double* __restrict__ splfc, double screen,
                                  double* __restrict__ engfac, float* __restrict__ engfac_f) {
@@ -285,11 +302,39 @@ cudaError_t launch_frame_sort(Engine& e) {
   return err;
 }
 
+cudaError_t launch_frame_bricks(Engine& e) {
+  cudaError_t err = cudaMemsetAsync(e.d_brick_count, 0, sizeof(int) * (e.nbricks + 1), e.stream);
+  if (err != cudaSuccess) return err;
+  brick_key_kernel<<<nblk(e.nsite_phys, 256), 256, 0, e.stream>>>(e.d_site_grid, e.nsite_phys, e.geom.K[0],
+                                                                   e.geom.K[1], e.geom.K[2], e.nbrick[0],
+                                                                   e.nbrick[1], e.d_brick_key, e.d_brick_val,
+                                                                   e.d_brick_count);
+  e.count_launch();
+  if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  int bits = 1;
+  while ((1 << bits) < e.nbricks + 1) ++bits;
+  size_t bytes = e.cub_tmp_bytes;
+  err = cub::DeviceRadixSort::SortPairs(e.d_cub_tmp, bytes, e.d_brick_key, e.d_brick_key_alt, e.d_brick_val,
+                                        e.d_brick_site, e.nsite_phys, 0, bits, e.stream);
+  if (err != cudaSuccess) return err;
+  bytes = e.cub_tmp_bytes;
+  return cub::DeviceScan::ExclusiveSum(e.d_cub_tmp, bytes, e.d_brick_count, e.d_brick_start, e.nbricks + 1,
+                                       e.stream);
+}
+
 size_t frame_cub_bytes(int n) {
   size_t a = 0, b = 0;
   cub::DeviceRadixSort::SortPairs(nullptr, a, (unsigned int*)nullptr, (unsigned int*)nullptr, (int*)nullptr,
                                   (int*)nullptr, n, 0, 30, (cudaStream_t)0);
   cub::DeviceScan::ExclusiveSum(nullptr, b, (int*)nullptr, (int*)nullptr, n + 1, (cudaStream_t)0);
+  return std::max(a, b);
+}
+
+size_t brick_cub_bytes(int nsite, int nbricks) {
+  size_t a = 0, b = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, a, (unsigned int*)nullptr, (unsigned int*)nullptr, (int*)nullptr,
+                                  (int*)nullptr, nsite, 0, 32, (cudaStream_t)0);
+  cub::DeviceScan::ExclusiveSum(nullptr, b, (int*)nullptr, (int*)nullptr, nbricks + 1, (cudaStream_t)0);
   return std::max(a, b);
 }
 

@@ -606,60 +606,118 @@ __global__ void __launch_bounds__(256) mol_energy_kernel(MolArgs A) {
 }
 
 
-// Mixed path, step 1 -- gather.  One thread = one solvent site x G placements.  The
-// batch's potential grids are interleaved, phi[(z K2 + y) K1 + x][ldb] with placements
-// innermost, so the G placements of a stencil point are one aligned 32-byte load, and
-// the B-spline weights and grid indices of the site are computed once for all of them.
-// Output: q * sum theta theta theta phi per (site, placement), FP32, [site][ldb].
-template <int P, int G>
-__global__ void __launch_bounds__(256) gather_kernel(const float* __restrict__ phi, const float4* __restrict__ site_rec,
-                                                     const int* __restrict__ site_grid, int nsite, int K1, int K2,
-                                                     int K3, int ldb, float* __restrict__ site_e) {
-  // phi layout: [placement group of 4][z][y][x][4]
-  const size_t gstride = (size_t)K1 * K2 * K3 * 4;
-  const int g0 = blockIdx.x * G;
-  const int i = blockIdx.y * blockDim.x + threadIdx.x;
-  if (i >= nsite) return;
-  const float4 rec = site_rec[i];
-  const int gp = site_grid[i];
-  float w1[P], w2[P], w3[P];
-  bspline_w<P>(rec.x, w1);
-  bspline_w<P>(rec.y, w2);
-  bspline_w<P>(rec.z, w3);
-  const int g1 = gp & 1023, g2 = (gp >> 10) & 1023, g3 = (gp >> 20) & 1023;
-  int xo[P];
+// ---- TMA + mbarrier helpers (inline PTX, sm_90+ forms, valid on sm_103a) -------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_barrier_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+constexpr long kWaitLimit = 1L << 24;  // try_wait rounds before a CTA gives up and flags an error
+
+// Mixed path, step 1 -- gather by bricks.  CTA per (8^3 brick of the PME grid, group of
+// 4 placements).  One TMA 4-D box copy brings the brick's stencil halo of the four
+// placements' padded potential grids into shared memory ([4][z][y][x]); it is then
+// interleaved to [point][4], and each thread takes a site of the brick, computes its
+// B-spline weights once (FP32, stable recursion) and accumulates q theta theta theta phi
+// for the four placements with one 16-byte shared load per stencil point.
+template <int P>
+__global__ void __launch_bounds__(128) gather_tma_kernel(const __grid_constant__ CUtensorMap tmap, int nb,
+                                                         const float4* __restrict__ site_rec,
+                                                         const int* __restrict__ site_grid,
+                                                         const int* __restrict__ brick_site,
+                                                         const int* __restrict__ brick_start, int K1, int K2, int K3,
+                                                         int nbx, int nby, int BX, int ldb,
+                                                         float* __restrict__ site_e, DevStatus* status) {
+  constexpr int BY = 8 + P - 1, BZ = 8 + P - 1;
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ unsigned long long bar;
+  float* box = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
+  const int npt = BZ * BY * BX;
+  float4* halo = reinterpret_cast<float4*>(box + 4 * npt);
+  const int brick = blockIdx.x, b0 = blockIdx.y * 4;
+  const int bx = brick % nbx, by = (brick / nbx) % nby, bz = brick / (nbx * nby);
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_barrier_init();
+    fence_proxy_async_smem();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mbar_expect_tx(&bar, (uint32_t)(4 * npt * sizeof(float)));
+    // padded coordinates: the halo of brick (bx, by, bz) starts at 8 bx (x is a multiple of 4)
+    tma_load_4d(box, &tmap, bx * 8, by * 8, bz * 8, b0, &bar);
+  }
+  bool ok = false;
+  for (long it = 0; it < kWaitLimit; ++it)
+    if (mbar_try_wait(&bar, 0)) {
+      ok = true;
+      break;
+    }
+  if (!ok) {
+    if (threadIdx.x == 0) atomicOr(&status->range_fault, 2);
+    return;
+  }
+  for (int t = threadIdx.x; t < npt; t += blockDim.x)
+    halo[t] = make_float4(box[t], box[npt + t], box[2 * npt + t], box[3 * npt + t]);
+  __syncthreads();
+  const int h = P - 1;
+  const int ox = bx * 8 - h, oy = by * 8 - h, oz = bz * 8 - h;
+  const int s_end = brick_start[brick + 1];
+  for (int i = brick_start[brick] + threadIdx.x; i < s_end; i += blockDim.x) {
+    const int site = brick_site[i];
+    const float4 rec = site_rec[site];
+    const int gp = site_grid[site];
+    float w1[P], w2[P], w3[P];
+    bspline_w<P>(rec.x, w1);
+    bspline_w<P>(rec.y, w2);
+    bspline_w<P>(rec.z, w3);
+    int g1 = gp & 1023, g2 = (gp >> 10) & 1023, g3 = (gp >> 20) & 1023;
+    if (g1 >= K1) g1 -= K1;
+    if (g2 >= K2) g2 -= K2;
+    if (g3 >= K3) g3 -= K3;
+    const int lx0 = g1 - ox, ly0 = g2 - oy, lz0 = g3 - oz;  // stencil c covers l0 - c
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-  for (int c = 0; c < P; ++c) xo[c] = wrapi(g1 - c, K1);
-  float acc[G];
+    for (int c3 = 0; c3 < P; ++c3) {
 #pragma unroll
-  for (int j = 0; j < G; ++j) acc[j] = 0.f;
+      for (int c2 = 0; c2 < P; ++c2) {
+        const float w32 = w3[c3] * w2[c2];
+        const float4* row = halo + ((lz0 - c3) * BY + (ly0 - c2)) * BX + lx0;
 #pragma unroll
-  for (int c3 = 0; c3 < P; ++c3) {
-    const int z = wrapi(g3 - c3, K3);
-#pragma unroll
-    for (int c2 = 0; c2 < P; ++c2) {
-      const int y = wrapi(g2 - c2, K2);
-      const float w32 = w3[c3] * w2[c2];
-      const float* row = phi + (size_t)(g0 / 4) * gstride + (((size_t)z * K2 + y) * K1) * 4;
-#pragma unroll
-      for (int c1 = 0; c1 < P; ++c1) {
-        const float w = w32 * w1[c1];
-        const float* src = row + (size_t)xo[c1] * 4;
-#pragma unroll
-        for (int v = 0; v < G / 4; ++v) {
-          const float4 q = __ldg(reinterpret_cast<const float4*>(src + v * gstride));
-          acc[4 * v + 0] = fmaf(w, q.x, acc[4 * v + 0]);
-          acc[4 * v + 1] = fmaf(w, q.y, acc[4 * v + 1]);
-          acc[4 * v + 2] = fmaf(w, q.z, acc[4 * v + 2]);
-          acc[4 * v + 3] = fmaf(w, q.w, acc[4 * v + 3]);
+        for (int c1 = 0; c1 < P; ++c1) {
+          const float w = w32 * w1[c1];
+          const float4 v = row[-c1];
+          acc.x = fmaf(w, v.x, acc.x);
+          acc.y = fmaf(w, v.y, acc.y);
+          acc.z = fmaf(w, v.z, acc.z);
+          acc.w = fmaf(w, v.w, acc.w);
         }
       }
     }
+    *reinterpret_cast<float4*>(site_e + (size_t)site * ldb + b0) =
+        make_float4(rec.w * acc.x, rec.w * acc.y, rec.w * acc.z, rec.w * acc.w);
   }
-  float4* out = reinterpret_cast<float4*>(site_e + (size_t)i * ldb + g0);
-#pragma unroll
-  for (int v = 0; v < G / 4; ++v)
-    out[v] = make_float4(rec.w * acc[4 * v + 0], rec.w * acc[4 * v + 1], rec.w * acc[4 * v + 2], rec.w * acc[4 * v + 3]);
 }
 
 // Mixed path, step 2 -- per molecule x G placements: FP64 sum of the site terms, real
@@ -895,19 +953,26 @@ cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
     return launch_p<false>(e, A, grid, smem);
   }
   if (a.G != 8 && a.G != 4) return cudaErrorInvalidValue;
-  {  // step 1: gather
-    dim3 g1((a.nb + a.G - 1) / a.G, (e.nsite_phys + 255) / 256);
+  {  // step 1: gather by bricks (TMA-staged halos)
+    dim3 g1(e.nbricks, (a.nb + 3) / 4);
     const int K1 = e.geom.K[0], K2 = e.geom.K[1], K3 = e.geom.K[2];
-#define ERMOD_GATHER(PP, GG)                                                                                   \
-  if (e.P_order == PP && a.G == GG)                                                                            \
-    gather_kernel<PP, GG><<<g1, 256, 0, e.stream>>>(a.phi, e.d_site_rec, e.d_site_grid, e.nsite_phys, K1, K2, K3, \
-                                                    e.Bmax, e.d_site_e);
-    ERMOD_GATHER(4, 4)
-    ERMOD_GATHER(4, 8)
-    ERMOD_GATHER(6, 4)
-    ERMOD_GATHER(6, 8)
-    ERMOD_GATHER(8, 4)
-    ERMOD_GATHER(8, 8)
+    const size_t npt = (size_t)e.gbox[0] * e.gbox[1] * e.gbox[2];
+    const size_t sh = 128 + npt * 4 * sizeof(float) + npt * sizeof(float4);
+#define ERMOD_GATHER(PP)                                                                                        \
+  if (e.P_order == PP) {                                                                                        \
+    static size_t attr = 0;                                                                                     \
+    if (attr < sh) {                                                                                            \
+      err = cudaFuncSetAttribute(gather_tma_kernel<PP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);  \
+      if (err != cudaSuccess) return err;                                                                       \
+      attr = sh;                                                                                                \
+    }                                                                                                           \
+    gather_tma_kernel<PP><<<g1, 128, sh, e.stream>>>(e.phi_tmap, a.nb, e.d_site_rec, e.d_site_grid,               \
+                                                     e.d_brick_site, e.d_brick_start, K1, K2, K3, e.nbrick[0],    \
+                                                     e.nbrick[1], e.gbox[0], e.Bmax, e.d_site_e, e.d_status);   \
+  }
+    ERMOD_GATHER(4)
+    ERMOD_GATHER(6)
+    ERMOD_GATHER(8)
 #undef ERMOD_GATHER
     e.count_launch();
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
