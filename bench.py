@@ -257,7 +257,7 @@ def run_ours(args):
     nsite_phys = 3 * w.nwater
     per_pl = roofline.bytes_per_placement(K, K, K, nsite_phys, G=min(8, args.batch))
     nbatch = args.steps * ((nplace + args.batch - 1) // args.batch)
-    cand = {k: phases.get(k, 0.0) for k in ("spectrum", "fft_c2r", "mol_energy")}
+    cand = {k: phases.get(k, 0.0) for k in ("spectrum", "fft_c2r", "gather")}
     dom = max(cand, key=cand.get)
     avg_launch_ms = cand[dom] / nbatch
     bytes_per_launch = per_pl[dom] * args.batch

@@ -19,8 +19,8 @@
 
 namespace ermod {
 
-const char* const kPhaseNames[PH_COUNT] = {"frame", "place_prep", "spectrum", "fft_c2r", "mol_energy",
-                                           "accumulate", "ecorr", "copy"};
+const char* const kPhaseNames[PH_COUNT] = {"frame", "place_prep", "spectrum", "fft_c2r", "gather",
+                                           "mol_energy", "accumulate", "ecorr", "copy"};
 
 namespace {
 thread_local std::string g_err;
@@ -55,7 +55,7 @@ static int fail_param(const char* what) {
   return ERMOD_E_PARAM;
 }
 
-void Engine::phase_begin(int ph) {
+void Engine::phase_begin_on(int ph, cudaStream_t s) {
   if (!timing) return;
   cudaEvent_t ev;
   if (!ev_pool.empty()) {
@@ -64,13 +64,20 @@ void Engine::phase_begin(int ph) {
   } else {
     cudaEventCreate(&ev);
   }
-  cudaEventRecord(ev, stream);
-  cur_phase = ph;
-  cur_ev = ev;
+  cudaEventRecord(ev, s);
+  if (s == aux) {
+    cur_phase_aux = ph;
+    cur_ev_aux = ev;
+  } else {
+    cur_phase = ph;
+    cur_ev = ev;
+  }
 }
 
-void Engine::phase_end() {
-  if (!timing || cur_phase < 0) return;
+void Engine::phase_end_on(cudaStream_t s) {
+  const bool on_aux = (s == aux);
+  const int ph = on_aux ? cur_phase_aux : cur_phase;
+  if (!timing || ph < 0) return;
   cudaEvent_t ev;
   if (!ev_pool.empty()) {
     ev = ev_pool.back();
@@ -78,9 +85,12 @@ void Engine::phase_end() {
   } else {
     cudaEventCreate(&ev);
   }
-  cudaEventRecord(ev, stream);
-  pending.push_back(Pending{cur_ev, ev, cur_phase});
-  cur_phase = -1;
+  cudaEventRecord(ev, s);
+  pending.push_back(Pending{on_aux ? cur_ev_aux : cur_ev, ev, ph});
+  if (on_aux)
+    cur_phase_aux = -1;
+  else
+    cur_phase = -1;
   if (pending.size() > 8192) {  // harvest to bound the pool
     cudaEventSynchronize(ev);
     for (auto& p : pending) {
@@ -96,7 +106,7 @@ void Engine::phase_end() {
 
 static void harvest(Engine& e) {
   if (e.pending.empty()) return;
-  cudaEventSynchronize(e.pending.back().b);
+  for (auto& p : e.pending) cudaEventSynchronize(p.b);
   for (auto& p : e.pending) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, p.a, p.b);
@@ -251,12 +261,12 @@ static int ensure_batch(Engine& e) {
   ERMOD_CUDA(dalloc(&b.u_q, (size_t)B * S));
   ERMOD_CUDA(dalloc(&b.u_grid, (size_t)B * S));
   ERMOD_CUDA(dalloc(&b.u_w, (size_t)B * S * 3 * kMaxSplineOrder));
-  ERMOD_CUDA(dalloc(&b.u_qmol, B));
-  ERMOD_CUDA(dalloc(&b.u_usreal, B));
+  ERMOD_CUDA(dalloc(&b.u_qmol, 2 * B));    // read by the accumulation: two batch slots
+  ERMOD_CUDA(dalloc(&b.u_usreal, 2 * B));
   ERMOD_CUDA(dalloc(&b.u_radius, B));
-  ERMOD_CUDA(dalloc(&b.engnmfc, B));
-  ERMOD_CUDA(dalloc(&e.d_u0, B));
-  ERMOD_CUDA(dalloc(&e.d_self_bin, B));
+  ERMOD_CUDA(dalloc(&b.engnmfc, 2 * B));
+  ERMOD_CUDA(dalloc(&e.d_u0, 2 * B));
+  ERMOD_CUDA(dalloc(&e.d_self_bin, 2 * B));
   if (e.mixed) {
     ERMOD_CUDA(dalloc(&b.u_bvec, (size_t)B * S * 3 * e.Kmax()));
     ERMOD_CUDA(dalloc(&e.d_site_e, (size_t)e.nsite_phys * B));
@@ -273,14 +283,14 @@ static int ensure_batch(Engine& e) {
     ERMOD_CUDA(cudaMemset(b.phi, 0, sizeof(float) * np * B));
     int st = make_phi_tmap(e, b.phi);
     if (st) return st;
-    ERMOD_CUDA(dalloc(&b.self_part, (size_t)B * spectrum_partials(e)));
+    ERMOD_CUDA(dalloc(&b.self_part, (size_t)2 * B * spectrum_partials(e)));
   } else {
     ERMOD_CUDA(dalloc(&b.spec64, nc * B));
     ERMOD_CUDA(dalloc(&b.phi64, nr * B));
-    ERMOD_CUDA(dalloc(&b.self_part, (size_t)B * influence64_blocks()));
+    ERMOD_CUDA(dalloc(&b.self_part, (size_t)2 * B * influence64_blocks()));
   }
-  ERMOD_CUDA(dalloc(&b.part, (size_t)B * e.ntile * e.numslv * 3));
-  e.ring_cap = e.P.corrcal ? std::max(B, (512 / B) * B) : B;
+  ERMOD_CUDA(dalloc(&b.part, (size_t)2 * B * e.ntile * e.numslv * 3));
+  e.ring_cap = e.P.corrcal ? std::max(2 * B, (512 / B) * B) : 2 * B;
   e.ring_fill = 0;
   ERMOD_CUDA(dalloc(&e.d_ring_hist, (size_t)e.ring_cap * e.ermax));
   ERMOD_CUDA(dalloc(&e.d_ring_w, e.ring_cap));
@@ -407,6 +417,15 @@ int ermod_create(const ermod_params* p, int device, ermod_ctx** out) {
     return fail_cuda(err, "cudaStreamCreate");
   }
   e.own_stream = true;
+  if ((err = cudaStreamCreateWithFlags(&e.aux, cudaStreamNonBlocking)) != cudaSuccess) {
+    ermod_destroy(c);
+    return fail_cuda(err, "cudaStreamCreate");
+  }
+  for (int s = 0; s < 2; ++s) {
+    cudaEventCreateWithFlags(&e.ev_done[s], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&e.ev_acc[s], cudaEventDisableTiming);
+  }
+  cudaEventCreateWithFlags(&e.ev_flush, cudaEventDisableTiming);
   if ((err = dalloc(&e.d_status, 1)) != cudaSuccess || (err = cudaMallocHost(&e.h_status, sizeof(DevStatus))) != cudaSuccess) {
     ermod_destroy(c);
     return fail_cuda(err, "status allocation");
@@ -464,6 +483,13 @@ int ermod_destroy(ermod_ctx* c) {
   harvest(e);
   for (auto ev : e.ev_pool) cudaEventDestroy(ev);
   if (e.own_stream && e.stream) cudaStreamDestroy(e.stream);
+  if (e.aux) cudaStreamSynchronize(e.aux);
+  for (int s = 0; s < 2; ++s) {
+    if (e.ev_done[s]) cudaEventDestroy(e.ev_done[s]);
+    if (e.ev_acc[s]) cudaEventDestroy(e.ev_acc[s]);
+  }
+  if (e.ev_flush) cudaEventDestroy(e.ev_flush);
+  if (e.aux) cudaStreamDestroy(e.aux);
   delete c;
   return ERMOD_OK;
 }
@@ -780,14 +806,22 @@ int ermod_frame_device(ermod_ctx* c, const double* sitepos_d, const double* cell
   return frame_launch(e);
 }
 
-// the placement loop on device-resident inputs
+// the placement loop on device-resident inputs.  Batch i runs its kernels on the main
+// stream with the buffers of slot i%2; its ordered accumulation (and, every ring_cap
+// placements, the ecorr flush) runs on the aux stream, overlapping batch i+1.
 static int run_placements(Engine& e, int nplace, const int* d_tag, const double* d_sol, const double* d_sws,
                           double* d_uv, double* d_fl, int ns_solute) {
   int st = ensure_batch(e);
   if (st) return st;
   const int B = e.Bmax;
-  for (int b0 = 0; b0 < nplace; b0 += B) {
+  const size_t parts = e.mixed ? (size_t)spectrum_partials(e) : (size_t)influence64_blocks();
+  // the aux stream starts after everything already queued on the main stream
+  ERMOD_CUDA(cudaEventRecord(e.ev_done[0], e.stream));
+  ERMOD_CUDA(cudaStreamWaitEvent(e.aux, e.ev_done[0], 0));
+  int ibatch = 0;
+  for (int b0 = 0; b0 < nplace; b0 += B, ++ibatch) {
     const int nb = std::min(B, nplace - b0);
+    const int slot = ibatch & 1;
     BatchArgs a = e.buf;
     a.nb = nb;
     a.b0 = b0;
@@ -797,6 +831,14 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
     a.uvengy_out = d_uv;
     a.flceng_out = d_fl;
     a.hist = e.d_ring_hist + (size_t)e.ring_fill * e.ermax;
+    a.u_qmol = e.buf.u_qmol + (size_t)slot * B;
+    a.u_usreal = e.buf.u_usreal + (size_t)slot * B;
+    a.engnmfc = e.buf.engnmfc + (size_t)slot * B;
+    a.self_part = e.buf.self_part + (size_t)slot * B * parts;
+    a.part = e.buf.part + (size_t)slot * B * e.ntile * e.numslv * 3;
+    a.u0 = e.d_u0 + (size_t)slot * B;
+    a.self_bin = e.d_self_bin + (size_t)slot * B;
+    if (ibatch >= 2) ERMOD_CUDA(cudaStreamWaitEvent(e.stream, e.ev_acc[slot], 0));  // slot free again
     const double* sol = d_sol ? d_sol + (size_t)b0 * ns_solute * 3 : nullptr;
     e.phase_begin(PH_PREP);
     ERMOD_CUDA(cudaMemsetAsync(a.hist, 0, sizeof(int) * (size_t)nb * e.ermax, e.stream));
@@ -818,29 +860,44 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
       if (r != CUFFT_SUCCESS) return fail_fft(r, "cufftExecZ2D");
       e.phase_end();
     }
-    e.phase_begin(PH_MOL);
-    ERMOD_CUDA(launch_mol_energy(e, a));
+    e.phase_begin(e.mixed ? PH_GATHER : PH_MOL);
+    ERMOD_CUDA(launch_mol_energy(e, a));  // mixed: gather, then (mol_energy phase) finish
     e.phase_end();
-    e.phase_begin(PH_ACCUM);
-    ERMOD_CUDA(launch_accumulate(e, a));
-    e.phase_end();
+    ERMOD_CUDA(cudaEventRecord(e.ev_done[slot], e.stream));
+    // ---- ordered accumulation on the aux stream ----
+    ERMOD_CUDA(cudaStreamWaitEvent(e.aux, e.ev_done[slot], 0));
+    e.phase_begin_on(PH_ACCUM, e.aux);
+    ERMOD_CUDA(launch_accumulate(e, a, e.aux));
+    e.phase_end_on(e.aux);
+    bool flushed = false;
     if (e.P.corrcal) {
       e.ring_fill += nb;
       if (e.ring_fill + B > e.ring_cap) {
-        e.phase_begin(PH_ECORR);
-        ERMOD_CUDA(launch_ecorr_flush(e));
-        e.phase_end();
+        e.phase_begin_on(PH_ECORR, e.aux);
+        ERMOD_CUDA(launch_ecorr_flush(e, e.aux));
+        e.phase_end_on(e.aux);
         e.ring_fill = 0;
+        flushed = true;
       }
+    } else {
+      e.ring_fill = (e.ring_fill + B) % e.ring_cap;  // two histogram slots
+    }
+    ERMOD_CUDA(cudaEventRecord(e.ev_acc[slot], e.aux));
+    if (flushed) {  // the ring is rewritten from its start by the next batches
+      ERMOD_CUDA(cudaEventRecord(e.ev_flush, e.aux));
+      ERMOD_CUDA(cudaStreamWaitEvent(e.stream, e.ev_flush, 0));
     }
   }
   if (e.P.corrcal && e.ring_fill > 0) {
-    e.phase_begin(PH_ECORR);
-    ERMOD_CUDA(launch_ecorr_flush(e));
-    e.phase_end();
+    e.phase_begin_on(PH_ECORR, e.aux);
+    ERMOD_CUDA(launch_ecorr_flush(e, e.aux));
+    e.phase_end_on(e.aux);
     e.ring_fill = 0;
   }
-  // status snapshot (read by ermod_sync)
+  e.ring_fill = 0;
+  // join the aux stream back into the main stream, then snapshot the status
+  ERMOD_CUDA(cudaEventRecord(e.ev_flush, e.aux));
+  ERMOD_CUDA(cudaStreamWaitEvent(e.stream, e.ev_flush, 0));
   ERMOD_CUDA(cudaMemcpyAsync(e.h_status, e.d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, e.stream));
   return ERMOD_OK;
 }

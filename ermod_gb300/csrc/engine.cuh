@@ -13,7 +13,7 @@
 
 namespace ermod {
 
-enum Phase { PH_FRAME = 0, PH_PREP, PH_SPECTRUM, PH_FFT, PH_MOL, PH_ACCUM, PH_ECORR, PH_COPY, PH_COUNT };
+enum Phase { PH_FRAME = 0, PH_PREP, PH_SPECTRUM, PH_FFT, PH_GATHER, PH_MOL, PH_ACCUM, PH_ECORR, PH_COPY, PH_COUNT };
 extern const char* const kPhaseNames[PH_COUNT];
 
 struct Engine {
@@ -128,9 +128,9 @@ struct Engine {
   int* d_ring_nz = nullptr;       // [ring_cap][ermax] packed (bin | count << 16)... see kernels
   int* d_ring_nnz = nullptr;      // [ring_cap] occupied bins per entry
   int* d_ring_valid = nullptr;    // [ring_cap] entry accumulated (no error in its batch)
-  double* d_u0 = nullptr;         // [Bmax] solute self energies of the current batch
+  double* d_u0 = nullptr;         // [2][Bmax] solute self energies (two batch slots)
   float* d_site_e = nullptr;      // [nsite_phys][Bmax] reciprocal site terms (mixed path)
-  int* d_self_bin = nullptr;      // [Bmax]
+  int* d_self_bin = nullptr;      // [2][Bmax]
 
   // ---- status ----------------------------------------------------------------------
   DevStatus* d_status = nullptr;
@@ -155,8 +155,18 @@ struct Engine {
   size_t grid_cplx() const { return (size_t)H() * geom.K[1] * geom.K[2]; }
   int Kmax() const { return std::max(geom.K[0], std::max(geom.K[1], geom.K[2])); }
 
-  void phase_begin(int ph);
-  void phase_end();
+  // second stream: the ordered accumulation of batch i overlaps batch i+1's kernels
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_done[2] = {nullptr, nullptr};  // batch kernels finished (slot)
+  cudaEvent_t ev_acc[2] = {nullptr, nullptr};   // accumulation of the slot finished
+  cudaEvent_t ev_flush = nullptr;               // ecorr flush finished
+
+  void phase_begin(int ph) { phase_begin_on(ph, stream); }
+  void phase_end() { phase_end_on(stream); }
+  void phase_begin_on(int ph, cudaStream_t s);
+  void phase_end_on(cudaStream_t s);
+  int cur_phase_aux = -1;
+  cudaEvent_t cur_ev_aux = nullptr;
   void count_launch(int n = 1) { launches += n; }
 };
 

@@ -95,6 +95,8 @@ struct BatchArgs {
   double* uvengy_out;  // [nplace][slvmax+1] or null (device)
   double* flceng_out;  // [nplace][numslv] or null (device)
   double* engnmfc;     // [nb] weights (0 for skipped placements)
+  double* u0;          // [nb] solute self energies
+  int* self_bin;       // [nb] eself bin (0-based) or -1
 };
 
 struct Engine;
@@ -114,7 +116,7 @@ cudaError_t launch_influence64(Engine& e, const BatchArgs& a);
 // per-molecule energies and histograms
 cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a);
 // accumulation
-cudaError_t launch_accumulate(Engine& e, const BatchArgs& a);
-cudaError_t launch_ecorr_flush(Engine& e);
+cudaError_t launch_accumulate(Engine& e, const BatchArgs& a, cudaStream_t s);
+cudaError_t launch_ecorr_flush(Engine& e, cudaStream_t s);
 
 }  // namespace ermod

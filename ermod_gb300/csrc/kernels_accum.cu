@@ -154,7 +154,10 @@ __global__ void __launch_bounds__(kAccThreads) accumulate_kernel(AccArgs A) {
   __shared__ double s_voffset;
   if (threadIdx.x == 0) {
     const volatile unsigned long long* ek = &A.status->err_key;
-    skip = (*ek != kNoError) ? 1 : 0;
+    // an error in this batch or an earlier one of the call; errors of later batches
+    // (already running on the other stream) do not stop this batch's accumulation
+    const unsigned long long k = *ek;
+    skip = (k != kNoError && (long long)(k >> 36) < (long long)a.b0 + nb) ? 1 : 0;
     if (!skip && A.wgtslf && A.scal[4] == 0.0) {
       A.scal[3] = A.u0[0];  // voffset from the first placement ever processed
       A.scal[4] = 1.0;
@@ -323,7 +326,7 @@ __global__ void __launch_bounds__(256) ecorr_rows_kernel(const int* __restrict__
 
 int accumulate_max_batch() { return kMaxBatch; }
 
-cudaError_t launch_accumulate(Engine& e, const BatchArgs& a) {
+cudaError_t launch_accumulate(Engine& e, const BatchArgs& a, cudaStream_t s) {
   AccArgs A{};
   A.a = a;
   A.ntile = e.ntile;
@@ -352,22 +355,22 @@ cudaError_t launch_accumulate(Engine& e, const BatchArgs& a) {
   A.ring_valid = e.d_ring_valid + e.ring_fill;
   A.ring_w = e.d_ring_w + e.ring_fill;
   A.slvmax = e.slvmax;
-  A.u0 = e.d_u0;
-  A.self_bin = e.d_self_bin;
+  A.u0 = a.u0;
+  A.self_bin = a.self_bin;
   A.status = e.d_status;
-  reduce_kernel<<<a.nb, kAccThreads, 0, e.stream>>>(A);
-  accumulate_kernel<<<1, kAccThreads, 0, e.stream>>>(A);
+  reduce_kernel<<<a.nb, kAccThreads, 0, s>>>(A);
+  accumulate_kernel<<<1, kAccThreads, 0, s>>>(A);
   e.count_launch(2);
   return cudaGetLastError();
 }
 
-cudaError_t launch_ecorr_flush(Engine& e) {
+cudaError_t launch_ecorr_flush(Engine& e, cudaStream_t s) {
   if (e.ring_fill == 0) return cudaSuccess;
   const int n = e.ring_fill;
   int* nz_bin = e.d_ring_nz;
   int* nz_cnt = e.d_ring_nz + (size_t)e.ring_cap * e.ermax;
   const int* valid = e.d_ring_valid;
-  ring_compact_kernel<<<n, 256, 0, e.stream>>>(e.d_ring_hist, valid, e.ermax, nz_bin, nz_cnt, e.d_ring_nnz);
+  ring_compact_kernel<<<n, 256, 0, s>>>(e.d_ring_hist, valid, e.ermax, nz_bin, nz_cnt, e.d_ring_nnz);
   e.count_launch();
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;
@@ -377,7 +380,7 @@ cudaError_t launch_ecorr_flush(Engine& e) {
   err = cudaFuncSetAttribute(ecorr_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
   const int nblk = (e.ermax + R - 1) / R;
-  ecorr_rows_kernel<<<nblk, 256, smem, e.stream>>>(e.d_ring_hist, nz_bin, nz_cnt, e.d_ring_nnz, e.d_ring_w, n,
+  ecorr_rows_kernel<<<nblk, 256, smem, s>>>(e.d_ring_hist, nz_bin, nz_cnt, e.d_ring_nnz, e.d_ring_w, n,
                                                    e.ermax, R, e.d_ecorr, e.d_ecorr_n);
   e.count_launch();
   return cudaGetLastError();

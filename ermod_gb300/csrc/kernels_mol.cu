@@ -977,6 +977,8 @@ cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
     e.count_launch();
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
   }
+  e.phase_end();
+  e.phase_begin(PH_MOL);
   // step 2: per-molecule totals and binning (histograms + edge keys in shared memory)
   const size_t smem_f = sizeof(int) * (((size_t)a.G * e.ermax + 1) & ~(size_t)1) + sizeof(long long) * e.ermax;
   dim3 g2((a.nb + a.G - 1) / a.G, e.ntile);

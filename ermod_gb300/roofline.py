@@ -7,9 +7,9 @@ write crosses HBM once.
 
   spectrum    writes the half spectrum engfac * S(k):            8 H K2 K3
   fft_c2r     reads it, writes the potential grid:               8 H K2 K3 + 4 K1 K2 K3
-  mol_energy  reads the potential grid once, plus the solvent
-              site records (36 B) once per G placements:          4 K1 K2 K3 + 36 N / G
-  total                                                            16 H K2 K3 + 8 K1 K2 K3 + 36 N / G
+  gather      reads the potential grid once, plus the solvent
+              site records (20 B) once per 4 placements:          4 K1 K2 K3 + 20 N / 4
+  total                                                            16 H K2 K3 + 8 K1 K2 K3 + 5 N
 
 The plain FP64 path doubles every grid term and adds the spread grid and the forward
 transform (8 K^3 written by the spread, read by D2Z; 16 H K^2 written by D2Z).
@@ -27,7 +27,7 @@ def bytes_per_placement(K1: int, K2: int, K3: int, nsite: int, G: int = 8) -> di
     d = {
         "spectrum": 8.0 * nh,
         "fft_c2r": 8.0 * nh + 4.0 * nr,
-        "mol_energy": 4.0 * nr + 36.0 * nsite / G,
+        "gather": 4.0 * nr + 20.0 * nsite / 4,
     }
     d["total"] = sum(d.values())
     return d
