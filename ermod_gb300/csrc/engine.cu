@@ -1113,4 +1113,22 @@ int ermod_timing_get(ermod_ctx* c, int max_phases, double* ms, const char** name
   return ERMOD_OK;
 }
 
+int ermod_ecorr_add_noalloc(const int* hist, const double* weight, int nplace, int ermax, double* ecorr,
+                            int64_t* ecorr_count, void* stream) {
+  if (nplace < 0 || ermax < 1) return fail_param("ermod_ecorr_add_noalloc: nplace >= 0 and ermax >= 1 required");
+  if (nplace > kNoAllocMaxPlace || ermax > kNoAllocMaxBins || (long long)nplace * ermax > kNoAllocMaxEntries) {
+    set_error_string("ermod_ecorr_add_noalloc: nplace = " + std::to_string(nplace) + ", ermax = " +
+                     std::to_string(ermax) + " exceed its fixed scratch (nplace <= " +
+                     std::to_string(kNoAllocMaxPlace) + ", ermax <= " + std::to_string(kNoAllocMaxBins) +
+                     ", nplace * ermax <= " + std::to_string(kNoAllocMaxEntries) + ")");
+    return ERMOD_E_PARAM;
+  }
+  if (nplace == 0) return ERMOD_OK;
+  if (!hist || !weight || !ecorr) return fail_param("ermod_ecorr_add_noalloc: null hist, weight or ecorr");
+  const cudaError_t err = launch_ecorr_noalloc(hist, weight, nplace, ermax, ecorr, (long long*)ecorr_count,
+                                               (cudaStream_t)stream);
+  if (err != cudaSuccess) return fail_cuda(err, "ermod_ecorr_add_noalloc");
+  return ERMOD_OK;
+}
+
 }  // extern "C"

@@ -118,5 +118,11 @@ cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a);
 // accumulation
 cudaError_t launch_accumulate(Engine& e, const BatchArgs& a, cudaStream_t s);
 cudaError_t launch_ecorr_flush(Engine& e, cudaStream_t s);
+// ecorr from caller histograms with the fixed scratch (no allocation); sizes checked by the caller
+constexpr int kNoAllocMaxPlace = 4096;
+constexpr int kNoAllocMaxBins = 8192;
+constexpr long long kNoAllocMaxEntries = 1LL << 20;  // nplace * ermax
+cudaError_t launch_ecorr_noalloc(const int* hist, const double* weight, int nplace, int ermax, double* ecorr,
+                                 long long* ecorr_count, cudaStream_t s);
 
 }  // namespace ermod

@@ -12,6 +12,8 @@
 //                 CTA owns a few rows of the matrix in shared memory and walks the
 //                 placements in order, touching only occupied (row, column) pairs; an
 //                 exact int64 mirror sum insdst(i) insdst(j) is kept beside it.
+#include <mutex>
+
 #include "engine.cuh"
 
 namespace ermod {
@@ -383,6 +385,99 @@ cudaError_t launch_ecorr_flush(Engine& e, cudaStream_t s) {
   ecorr_rows_kernel<<<nblk, 256, smem, s>>>(e.d_ring_hist, nz_bin, nz_cnt, e.d_ring_nnz, e.d_ring_w, n,
                                                    e.ermax, R, e.d_ecorr, e.d_ecorr_n);
   e.count_launch();
+  return cudaGetLastError();
+}
+
+
+// ---- ecorr from caller-owned histograms, with no allocation -----------------------
+//
+// Some hosts cannot let a library allocate device memory in the middle of their step:
+// an MD engine that has sized its memory pool to the whole card, or one that keeps
+// other streams busy on the same device, where cudaFree would synchronise the device
+// and stall them.  ermod_ecorr_add_noalloc serves such hosts.  Its only scratch (the
+// occupied-bin lists that ring_compact_kernel builds for the ring) lives in one fixed
+// file-scope device array, so a call allocates nothing.
+
+namespace {
+
+constexpr size_t kNoAllocEntries = (size_t)kNoAllocMaxEntries;  // 8 MiB of (bin, count) lists
+constexpr int kNoAllocMaxDevices = 64;
+
+// [kNoAllocEntries] bins, [kNoAllocEntries] counts, [kNoAllocMaxPlace] list lengths.
+// Shared by every call on a device: calls that overlap on the GPU race on it.
+static __device__ __align__(256) int g_noalloc_scratch[2 * kNoAllocEntries + kNoAllocMaxPlace];
+
+std::mutex g_noalloc_mu;
+int* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// ring_compact_kernel for caller histograms: every placement is valid, the lists go to
+// the fixed scratch.  Each list length is written for every placement and each list
+// entry below it, so nothing in the scratch has to start at zero.
+__global__ void __launch_bounds__(256) compact_noalloc_kernel(const int* __restrict__ hist, int ermax,
+                                                              int* __restrict__ nz_bin, int* __restrict__ nz_cnt,
+                                                              int* __restrict__ nnz) {
+  const int p = blockIdx.x;
+  const int* h = hist + (size_t)p * ermax;
+  __shared__ int scan[256];
+  const int per = (ermax + blockDim.x - 1) / blockDim.x;
+  const int lo = threadIdx.x * per, hi = min(ermax, lo + per);
+  int cnt = 0;
+  for (int i = lo; i < hi; ++i) cnt += (h[i] != 0);
+  scan[threadIdx.x] = cnt;
+  __syncthreads();
+  for (int off = 1; off < blockDim.x; off <<= 1) {
+    const int v = (threadIdx.x >= off) ? scan[threadIdx.x - off] : 0;
+    __syncthreads();
+    scan[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int pos = scan[threadIdx.x] - cnt;
+  for (int i = lo; i < hi; ++i)
+    if (h[i]) {
+      nz_bin[(size_t)p * ermax + pos] = i;
+      nz_cnt[(size_t)p * ermax + pos] = h[i];
+      ++pos;
+    }
+  if (threadIdx.x == blockDim.x - 1) nnz[p] = scan[threadIdx.x];
+}
+
+// the scratch address on the current device, looked up once per device
+cudaError_t noalloc_scratch(int** out) {
+  int dev = -1;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return err;
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    int* p = nullptr;
+    err = cudaGetSymbolAddress((void**)&p, g_noalloc_scratch);
+    if (err != cudaSuccess) return err;
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+cudaError_t launch_ecorr_noalloc(const int* hist, const double* weight, int nplace, int ermax, double* ecorr,
+                                 long long* ecorr_count, cudaStream_t s) {
+  int* scratch = nullptr;
+  cudaError_t err = noalloc_scratch(&scratch);
+  if (err != cudaSuccess) return err;
+  int* nz_bin = scratch;
+  int* nz_cnt = scratch + kNoAllocEntries;
+  int* nnz = scratch + 2 * kNoAllocEntries;
+  compact_noalloc_kernel<<<nplace, 256, 0, s>>>(hist, ermax, nz_bin, nz_cnt, nnz);
+  err = cudaGetLastError();
+  if (err != cudaSuccess) return err;
+  const size_t per_row = (size_t)ermax * (sizeof(double) + (ecorr_count ? sizeof(long long) : 0));
+  const int R = (int)std::max<size_t>(1, std::min<size_t>(8, (96 * 1024) / per_row));
+  const size_t smem = per_row * R;
+  err = cudaFuncSetAttribute(ecorr_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  ecorr_rows_kernel<<<(ermax + R - 1) / R, 256, smem, s>>>(hist, nz_bin, nz_cnt, nnz, weight, nplace, ermax, R,
+                                                           ecorr, ecorr_count);
   return cudaGetLastError();
 }
 

@@ -186,6 +186,24 @@ int ermod_engstore_merge(int nrank, int slttype, int wgtslf, double temp, int er
                          int numslv, double* edens, double* ecorr, double* eself, double* slnuv,
                          double* minuv, double* maxuv, double* scalars);
 
+/* ---- no counterpart in the reference ------------------------------------------------
+ * ecorr(i, j) += weight[p] * hist[p][i] * hist[p][j] for p < nplace and, when
+ * ecorr_count is not NULL, ecorr_count(i, j) += hist[p][i] * hist[p][j]: the ecorr update
+ * of update_histogram (engproc.F90:841-853) for per-placement histograms (int32,
+ * [nplace][ermax]) that the caller already holds.  hist, weight, ecorr (ermax x ermax,
+ * symmetric) and ecorr_count are device pointers on the current device; stream is a
+ * cudaStream_t (NULL: the legacy default stream).  Returns without synchronising.
+ *
+ * It allocates no device memory, for hosts that cannot let a library allocate inside
+ * their step (a memory pool sized to the whole card; other streams that the implicit
+ * device synchronisation of cudaFree would stall).  Its scratch is one fixed 8 MiB
+ * device array, so nplace <= 4096, ermax <= 8192 and nplace * ermax <= 1048576, else
+ * ERMOD_E_PARAM.  The first call on each device looks up that array's address: make it
+ * before any stream capture.  All calls on a device share the array, so calls that
+ * overlap on the GPU race. */
+int ermod_ecorr_add_noalloc(const int* hist, const double* weight, int nplace, int ermax,
+                            double* ecorr, int64_t* ecorr_count, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
