@@ -324,6 +324,103 @@ __global__ void __launch_bounds__(256) ecorr_rows_kernel(const int* __restrict__
   }
 }
 
+// Mixed path flush, same sum as ecorr_rows_kernel.  A CTA owns kEcRows rows and 256
+// columns of the matrix; thread t owns one column and keeps the flush's contribution
+// to its kEcRows entries in registers as float-float pairs (exact products by fma,
+// TwoSum additions: ~44 significant bits), walking the ring's placements in order.
+// No two threads share an entry, so the walk needs no barrier and its loads pipeline;
+// the pairs are added to the FP64 matrix once per flush.  The row coefficients
+// hist[p][row0 + r] of every placement are staged in shared memory with a bit mask of
+// the nonzero ones.
+constexpr int kEcRows = 16;
+
+__device__ __forceinline__ void ff_add_prod(float& hi, float& lo, float wh, float wl, float c) {
+  const float p = wh * c;
+  float pe = fmaf(wh, c, -p);  // exact low part of wh * c
+  pe = fmaf(wl, c, pe);
+  const float s = hi + p;  // TwoSum(hi, p)
+  const float bb = s - hi;
+  const float err = (hi - (s - bb)) + (p - bb);
+  lo += err + pe;
+  hi = s;
+}
+
+__global__ void __launch_bounds__(256) ecorr_ff_kernel(const int* __restrict__ hist, const int* __restrict__ valid,
+                                                     const double* __restrict__ w, int nring, int ermax,
+                                                     double* __restrict__ ecorr, long long* __restrict__ ecorr_n) {
+  extern __shared__ int sdyn[];
+  int* sci = sdyn;                      // [nring][kEcRows]
+  unsigned* smask = reinterpret_cast<unsigned*>(sdyn + (size_t)nring * kEcRows);  // [nring]
+  float* swh = reinterpret_cast<float*>(smask + nring);  // [nring] weight, float-float
+  float* swl = swh + nring;
+  const int row0 = blockIdx.y * kEcRows;
+  const int nrow = min(kEcRows, ermax - row0);
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int p = threadIdx.x; p < nring; p += blockDim.x) {
+    unsigned m = 0;
+    const bool ok = valid[p] != 0;
+    for (int r = 0; r < kEcRows; ++r) {
+      const int c = (ok && r < nrow) ? hist[(size_t)p * ermax + row0 + r] : 0;
+      sci[p * kEcRows + r] = c;
+      if (c) m |= 1u << r;
+    }
+    smask[p] = m;
+    const double wd = w[p];
+    const float wh = (float)wd;
+    swh[p] = wh;
+    swl[p] = (float)(wd - (double)wh);
+  }
+  __syncthreads();
+  if (j >= ermax) return;
+  float hi[kEcRows], lo[kEcRows];
+  long long cn[kEcRows];
+#pragma unroll
+  for (int r = 0; r < kEcRows; ++r) {
+    hi[r] = 0.f;
+    lo[r] = 0.f;
+    cn[r] = 0;
+  }
+  bool any = false;
+  constexpr int U = 8;  // loads in flight per thread
+  for (int p0 = 0; p0 < nring; p0 += U) {
+    int cj[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int p = p0 + u;
+      cj[u] = (p < nring && smask[p]) ? __ldg(hist + (size_t)p * ermax + j) : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (cj[u] == 0) continue;
+      const int p = p0 + u;
+      any = true;
+      const unsigned m = smask[p];
+      const float wh = swh[p], wl = swl[p];
+      const float c = (float)cj[u];
+#pragma unroll
+      for (int r = 0; r < kEcRows; ++r) {
+        if (m & (1u << r)) {
+          const int ci = sci[p * kEcRows + r];
+          // w * ci as a float-float pair (ci < 2^24 is exact in FP32)
+          const float fci = (float)ci;
+          const float ph = wh * fci;
+          const float pl = fmaf(wl, fci, fmaf(wh, fci, -ph));
+          ff_add_prod(hi[r], lo[r], ph, pl, c);
+          if (ecorr_n) cn[r] += (long long)ci * (long long)cj[u];
+        }
+      }
+    }
+  }
+  if (!any) return;
+#pragma unroll
+  for (int r = 0; r < kEcRows; ++r) {
+    if (r >= nrow) break;
+    const size_t at = (size_t)(row0 + r) * ermax + j;
+    if (hi[r] != 0.f || lo[r] != 0.f) ecorr[at] = ecorr[at] + ((double)hi[r] + (double)lo[r]);
+    if (ecorr_n && cn[r] != 0) ecorr_n[at] += cn[r];
+  }
+}
+
 }  // namespace
 
 int accumulate_max_batch() { return kMaxBatch; }
@@ -369,6 +466,20 @@ cudaError_t launch_accumulate(Engine& e, const BatchArgs& a, cudaStream_t s) {
 cudaError_t launch_ecorr_flush(Engine& e, cudaStream_t s) {
   if (e.ring_fill == 0) return cudaSuccess;
   const int n = e.ring_fill;
+  if (e.mixed) {
+    const size_t smem = (size_t)n * (kEcRows * sizeof(int) + sizeof(unsigned) + 2 * sizeof(float));
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    if (smem > 48 * 1024) {
+      err = cudaFuncSetAttribute(ecorr_ff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (err != cudaSuccess) return err;
+    }
+    dim3 grid((e.ermax + 255) / 256, (e.ermax + kEcRows - 1) / kEcRows);
+    ecorr_ff_kernel<<<grid, 256, smem, s>>>(e.d_ring_hist, e.d_ring_valid, e.d_ring_w, n, e.ermax, e.d_ecorr,
+                                            e.d_ecorr_n);
+    e.count_launch();
+    return cudaGetLastError();
+  }
   int* nz_bin = e.d_ring_nz;
   int* nz_cnt = e.d_ring_nz + (size_t)e.ring_cap * e.ermax;
   const int* valid = e.d_ring_valid;

@@ -325,8 +325,8 @@ __device__ __forceinline__ void hist_add(int* h, int bin) {
 
 // real-space LJ + screened Coulomb of one molecule against solute b (mixed path):
 // fixed-point displacements, FP32 pair terms, FP64 sum over solute sites.
-__device__ __forceinline__ double real_mixed(const MolArgs& A, const BatchArgs& a, int b, int s0, int ns,
-                                             const LjK& k32, float rcut) {
+__device__ __forceinline__ float real_mixed(const MolArgs& A, const BatchArgs& a, int b, int s0, int ns,
+                                            const LjK& k32, float rcut) {
   const FrameGeom& g = A.g;
   const size_t ub = (size_t)b * kMaxSoluteSites;
   const int4 p0 = A.site_pos[s0];
@@ -335,7 +335,7 @@ __device__ __forceinline__ double real_mixed(const MolArgs& A, const BatchArgs& 
   const float dx = (float)(int)((unsigned)p0.x - (unsigned)u0.x) * fx;
   const float dy = (float)(int)((unsigned)p0.y - (unsigned)u0.y) * fy;
   const float dz = (float)(int)((unsigned)p0.z - (unsigned)u0.z) * fz;
-  double real = 0.0;
+  float real = 0.f;
   if (dx * dx + dy * dy + dz * dz > rcut * rcut) return real;
   const int nu = a.u_nsite[b];
   const float beta = (float)A.screen;
@@ -362,9 +362,28 @@ __device__ __forceinline__ double real_mixed(const MolArgs& A, const BatchArgs& 
         e += qu * A.site_rec[s0 + s].w * erfcf(beta * r) / r;
       }
     }
-    real += (double)e;
+    real += e;
   }
   return real;
+}
+
+// ordered key of (double)f using integer operations only (the FP64 pipe of this part
+// is ~1/60 of its FP32 rate); -0 maps to +0, subnormal floats take the slow branch
+__device__ __forceinline__ long long ordered_key_f(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned ex = (b >> 23) & 0xffu, man = b & 0x7fffffu;
+  const unsigned long long sign = (unsigned long long)(b >> 31) << 63;
+  unsigned long long d;
+  if (ex == 0xffu)
+    d = sign | 0x7ff0000000000000ull | ((unsigned long long)man << 29);
+  else if (ex != 0u)
+    d = sign | ((unsigned long long)(ex + 896u) << 52) | ((unsigned long long)man << 29);
+  else if (man == 0u)
+    d = 0ull;
+  else
+    return ordered_key((double)f);
+  const long long k = (long long)d;
+  return k ^ ((k >> 63) & 0x7fffffffffffffffll);
 }
 
 constexpr long long kKeyPosInf = 0x7ff0000000000000ll;
@@ -728,7 +747,8 @@ __global__ void __launch_bounds__(256) mol_finish_kernel(MolArgs A, const float*
   extern __shared__ int smem_dyn[];
   int* smem_hist = smem_dyn;                                                  // [G][ermax]
   long long* skeys = reinterpret_cast<long long*>(smem_dyn + ((G * A.ermax + 1) & ~1));  // [ermax]
-  __shared__ double su[G][256];
+  __shared__ float su[G][256];
+  __shared__ float squ[G];  // solute charges of the G placements
   __shared__ unsigned char sspec[256];
   const int tile = blockIdx.y;
   const int g0 = blockIdx.x * G;
@@ -738,14 +758,15 @@ __global__ void __launch_bounds__(256) mol_finish_kernel(MolArgs A, const float*
   const bool valid = m < A.slvmax;
   for (int i = threadIdx.x; i < G * A.ermax; i += blockDim.x) smem_hist[i] = 0;
   for (int i = threadIdx.x; i < A.ermax; i += blockDim.x) skeys[i] = A.uvkey[i];
+  if (threadIdx.x < ng) squ[threadIdx.x] = (float)(A.resid_fac * a.u_qmol[g0 + threadIdx.x]);
   int k = -1, s0 = 0, ns = 0, species = 0;
-  double qmol = 0.0;
+  float qmol = 0.f;
   if (valid) {
     k = A.slot_mol[m];
     s0 = A.slot_site[m];
     ns = A.slot_site[m + 1] - s0;
     species = A.slot_species[m];
-    qmol = A.slot_qmol[m];
+    qmol = (float)A.slot_qmol[m];
   }
   const bool spec_ok = valid && species >= 1 && species <= A.numslv;
   sspec[threadIdx.x] = (unsigned char)(spec_ok ? species : 0);
@@ -763,27 +784,28 @@ __global__ void __launch_bounds__(256) mol_finish_kernel(MolArgs A, const float*
   }
   const float rc = (float)fmax(A.elecut, A.upljcut);
   const float mol_r = A.frame_scal[0];
-  // ---- totals for the G placements ----
-  double uu[G];
+  __syncthreads();  // squ staged
+  // ---- totals for the G placements (FP32: the site terms are FP32 already) ----
+  float uu[G];
   bool act[G];
 #pragma unroll
   for (int j = 0; j < G; ++j) {
-    uu[j] = 0.0;
+    uu[j] = 0.f;
     act[j] = false;
     if (j < ng) {
       const int b = g0 + j;
       const int tg = a.tagslt[b] - 1;
       const int kskip = (tg >= 0 && tg < A.nummol) ? A.mol_to_k[tg] : -2;
       if (valid && k != kskip) {
-        double recip = 0.0;
-        for (int s = 0; s < ns; ++s) recip += (double)site_e[(size_t)(s0 + s) * ldb + b];
-        const double real = real_mixed(A, a, b, s0, ns, k32, rc + a.u_radius[b] + mol_r);
-        const double epcl = A.resid_fac * a.u_qmol[b] * qmol;
-        double pairep = -epcl;
+        float recip = 0.f;
+        for (int s = 0; s < ns; ++s) recip += site_e[(size_t)(s0 + s) * ldb + b];
+        const float real = real_mixed(A, a, b, s0, ns, k32, rc + a.u_radius[b] + mol_r);
+        const float epcl = squ[j] * qmol;  // residual_ene: pi Q_u Q_v / (beta^2 V)
+        float pairep = -epcl;
         pairep = pairep + recip;
         uu[j] = real + pairep;
         act[j] = true;
-        if (a.uvengy_out) a.uvengy_out[(size_t)(a.b0 + b) * (A.slvmax + 1) + k + 1] = uu[j];
+        if (a.uvengy_out) a.uvengy_out[(size_t)(a.b0 + b) * (A.slvmax + 1) + k + 1] = (double)uu[j];
       } else if (valid && a.uvengy_out) {
         a.uvengy_out[(size_t)(a.b0 + b) * (A.slvmax + 1) + k + 1] = 0.0;
       }
@@ -795,7 +817,7 @@ __global__ void __launch_bounds__(256) mol_finish_kernel(MolArgs A, const float*
   int pos[G];
 #pragma unroll
   for (int j = 0; j < G; ++j) {
-    ku[j] = ordered_key(uu[j]);
+    ku[j] = ordered_key_f(uu[j]);
     pos[j] = 0;
   }
   int step = 1;
@@ -810,9 +832,9 @@ __global__ void __launch_bounds__(256) mol_finish_kernel(MolArgs A, const float*
   }
 #pragma unroll
   for (int j = 0; j < G; ++j) {
-    double u = __longlong_as_double(0x7ff8000000000000ll);  // NaN marks "no molecule"
+    float u = __uint_as_float(0x7fc00000u);  // NaN marks "no molecule"
     if (act[j]) {
-      const double v = uu[j];
+      const float v = uu[j];
       const int ret = pos[j];
       int code = 0;
       if (!spec_ok)
@@ -821,7 +843,7 @@ __global__ void __launch_bounds__(256) mol_finish_kernel(MolArgs A, const float*
         code = ERMOD_E_ENG_MIN;
       else if (A.soln && ret > sp_soft)
         code = ERMOD_E_ENG_SFT;
-      else if (ret == sp_n && v < 1.0e3 && A.mbin_mode != 0) {
+      else if (ret == sp_n && v < 1.0e3f && A.mbin_mode != 0) {
         if (A.mbin_mode == 1)
           code = ERMOD_W_MBIN;
         else
@@ -841,25 +863,26 @@ __global__ void __launch_bounds__(256) mol_finish_kernel(MolArgs A, const float*
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int pr = warp; pr < ng * A.numslv; pr += blockDim.x / 32) {
     const int j = pr / A.numslv, sp = pr % A.numslv + 1;
-    double s = 0.0, mn = INFINITY, mx = -INFINITY;
+    float mn = INFINITY, mx = -INFINITY;
+    double s = 0.0;  // slnuv terms, SOLN only
     for (int t = lane; t < blockDim.x; t += 32) {
-      const double v = su[j][t];
+      const float v = su[j][t];
       if (sspec[t] == sp && v == v) {
-        s += v;
-        mn = fmin(mn, v);
-        mx = fmax(mx, v);
+        if (A.soln) s += (double)v;
+        mn = fminf(mn, v);
+        mx = fmaxf(mx, v);
       }
     }
     for (int off = 16; off > 0; off >>= 1) {
-      s += __shfl_down_sync(0xffffffffu, s, off);
-      mn = fmin(mn, __shfl_down_sync(0xffffffffu, mn, off));
-      mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, off));
+      if (A.soln) s += __shfl_down_sync(0xffffffffu, s, off);
+      mn = fminf(mn, __shfl_down_sync(0xffffffffu, mn, off));
+      mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, off));
     }
     if (lane == 0) {
       double* pt = a.part + (((size_t)(g0 + j) * A.ntile + tile) * A.numslv + (sp - 1)) * 3;
       pt[0] = s;
-      pt[1] = mn;
-      pt[2] = mx;
+      pt[1] = (double)mn;
+      pt[2] = (double)mx;
     }
   }
   for (int j = 0; j < ng; ++j) {
