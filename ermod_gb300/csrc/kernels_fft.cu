@@ -187,7 +187,7 @@ __device__ __forceinline__ int fdiv(int n, FastDiv f) { return f.d <= 1 ? n : (i
 template <int R>
 __device__ __forceinline__ void stockham_pass(const float2* __restrict__ A, float2* __restrict__ B, int N, int Ns,
                                               FastDiv fNs, int ncols, FastDiv fcols, int estride, int cstride,
-                                              const float2* __restrict__ tw) {
+                                              int oestride, int ocstride, const float2* __restrict__ tw) {
   const int NR = N / R;
   const int total = ncols * NR;
   const int step = N / (Ns * R);
@@ -206,14 +206,15 @@ __device__ __forceinline__ void stockham_pass(const float2* __restrict__ A, floa
     Dft<R>::run(v);
     const int idxD = jq * Ns * R + k;
 #pragma unroll
-    for (int r = 0; r < R; ++r) B[col * cstride + (idxD + r * Ns) * estride] = v[r];
+    for (int r = 0; r < R; ++r) B[(size_t)col * ocstride + (size_t)(idxD + r * Ns) * oestride] = v[r];
   }
 }
 
 __device__ __forceinline__ void run_pass(int R, const float2* A, float2* B, int N, int Ns, FastDiv fNs, int ncols,
-                                         FastDiv fcols, int estride, int cstride, const float2* tw) {
+                                         FastDiv fcols, int estride, int cstride, int oestride, int ocstride,
+                                         const float2* tw) {
 #define ERMOD_PASS(RR) \
-  case RR: stockham_pass<RR>(A, B, N, Ns, fNs, ncols, fcols, estride, cstride, tw); break;
+  case RR: stockham_pass<RR>(A, B, N, Ns, fNs, ncols, fcols, estride, cstride, oestride, ocstride, tw); break;
   switch (R) {
     ERMOD_PASS(2)
     ERMOD_PASS(3)
@@ -300,13 +301,33 @@ __device__ __forceinline__ float2* fft_cols(float2* A, float2* B, const FftPlan&
                                             int estride, int cstride, const float2* tw) {
   for (int p = 0; p < pl.npass; ++p) {
     __syncthreads();
-    run_pass(pl.r[p], A, B, pl.n, pl.ns[p], pl.fns[p], ncols, fcols, estride, cstride, tw);
+    run_pass(pl.r[p], A, B, pl.n, pl.ns[p], pl.fns[p], ncols, fcols, estride, cstride, estride, cstride, tw);
     float2* t = A;
     A = B;
     B = t;
   }
   __syncthreads();
   return A;
+}
+
+// the same with the first pass reading `in` (element/column strides ies/ics, e.g. a
+// plane in global memory) and the last pass writing `out` (strides oes/ocs); the
+// intermediate passes ping-pong between the shared buffers A and B (npass >= 2)
+__device__ __forceinline__ void fft_cols_io(const float2* in, int ies, int ics, float2* A, float2* B,
+                                            const FftPlan& pl, int ncols, FastDiv fcols, int estride, int cstride,
+                                            float2* out, int oes, int ocs, const float2* tw) {
+  const float2* src = in;
+  int se = ies, sc = ics;
+  for (int p = 0; p < pl.npass; ++p) {
+    const bool lastp = (p == pl.npass - 1);
+    float2* dst = lastp ? out : ((p & 1) ? B : A);
+    __syncthreads();
+    run_pass(pl.r[p], src, dst, pl.n, pl.ns[p], pl.fns[p], ncols, fcols, se, sc, lastp ? oes : estride,
+             lastp ? ocs : cstride, tw);
+    src = dst;
+    se = estride;
+    sc = cstride;
+  }
 }
 
 struct ff {
@@ -341,7 +362,9 @@ struct PmeArgs {
   FastDiv fH, fK1, fHp4, fnpair;
 };
 
-__global__ void __launch_bounds__(256) pme_a_kernel(PmeArgs A) {
+constexpr int kPmeThreads = 512;
+
+__global__ void __launch_bounds__(kPmeThreads, 2) pme_a_kernel(PmeArgs A) {
   extern __shared__ float2 sm[];
   const int k2 = blockIdx.x, b = blockIdx.y;
   const int K3 = A.K3, H = A.H, Hp = A.Hp;
@@ -355,11 +378,15 @@ __global__ void __launch_bounds__(256) pme_a_kernel(PmeArgs A) {
   const int ns = A.u_nsite[b];
   const float2* bv = A.bvec + (size_t)b * kMaxSoluteSites * 3 * A.Kmax;
   const int TX = Hp / kR1, TY = (K3 + kR3 - 1) / kR3;
-  // ---- generation: slab(k3, k1) = sum_s [q_s b2_s(k2) b3_s(k3)] b1_s(k1) ----
+  const bool even = (A.K1 % 2) == 0;
+  ff self{0.f, 0.f};
+  // ---- generation: slab(k3, k1) = sum_s [q_s b2_s(k2) b3_s(k3)] b1_s(k1), then (last
+  // chunk) the engfac multiply and the self energy sum 0.5 sum_k engfac |S|^2 ----
   float2* sd = work;                         // [chunk][K3]
   float2* sb = work + (size_t)A.chunk * K3;  // [chunk][Hp]  (Hp, chunk*K3 even: 16-byte aligned rows)
   for (int s0 = 0; s0 < ns; s0 += A.chunk) {
     const int nsc = min(A.chunk, ns - s0);
+    const bool last = s0 + A.chunk >= ns;
     __syncthreads();
     for (int t = threadIdx.x; t < nsc * K3; t += blockDim.x) {
       const int sl = t / K3, k3 = t - sl * K3;
@@ -405,56 +432,51 @@ __global__ void __launch_bounds__(256) pme_a_kernel(PmeArgs A) {
         const int k3 = k3a + j;
         if (k3 >= K3) continue;
         float4* dst = reinterpret_cast<float4*>(slab + (size_t)k3 * Hp + k1a);
-        float4 v0 = make_float4(acc[j][0].x, acc[j][0].y, acc[j][1].x, acc[j][1].y);
-        float4 v1 = make_float4(acc[j][2].x, acc[j][2].y, acc[j][3].x, acc[j][3].y);
         if (s0 != 0) {
           const float4 o0 = dst[0], o1 = dst[1];
-          v0 = make_float4(v0.x + o0.x, v0.y + o0.y, v0.z + o0.z, v0.w + o0.w);
-          v1 = make_float4(v1.x + o1.x, v1.y + o1.y, v1.z + o1.z, v1.w + o1.w);
+          acc[j][0] = cadd(acc[j][0], make_float2(o0.x, o0.y));
+          acc[j][1] = cadd(acc[j][1], make_float2(o0.z, o0.w));
+          acc[j][2] = cadd(acc[j][2], make_float2(o1.x, o1.y));
+          acc[j][3] = cadd(acc[j][3], make_float2(o1.z, o1.w));
         }
-        dst[0] = v0;
-        dst[1] = v1;
+        if (last) {
+          const float* ef = A.engfac + ((size_t)k3 * A.K2 + k2) * H;
+#pragma unroll
+          for (int i = 0; i < kR1; ++i) {
+            const int k1 = k1a + i;
+            const float f = (k1 < H) ? __ldg(ef + k1) : 0.f;
+            const float2 q = acc[j][i];
+            const float wgt = (k1 == 0 || (even && k1 == H - 1)) ? 0.5f : 1.f;
+            self = ff_add(self, wgt * f * (q.x * q.x + q.y * q.y));
+            acc[j][i] = make_float2(f * q.x, f * q.y);
+          }
+        }
+        dst[0] = make_float4(acc[j][0].x, acc[j][0].y, acc[j][1].x, acc[j][1].y);
+        dst[1] = make_float4(acc[j][2].x, acc[j][2].y, acc[j][3].x, acc[j][3].y);
       }
     }
-  }
-  __syncthreads();
-  // ---- engfac multiply and self energy ----
-  ff self{0.f, 0.f};
-  const bool even = (A.K1 % 2) == 0;
-  for (int t = threadIdx.x; t < K3 * H; t += blockDim.x) {
-    const int k3 = fdiv(t, A.fH), k1 = t - k3 * H;
-    const float f = A.engfac[((size_t)k3 * A.K2 + k2) * H + k1];
-    float2* p = slab + (size_t)k3 * Hp + k1;
-    const float2 q = *p;
-    const float wgt = (k1 == 0 || (even && k1 == H - 1)) ? 0.5f : 1.f;
-    self = ff_add(self, wgt * f * (q.x * q.x + q.y * q.y));
-    *p = make_float2(f * q.x, f * q.y);
   }
   for (int off = 16; off > 0; off >>= 1) {
     ff o{__shfl_down_sync(0xffffffffu, self.hi, off), __shfl_down_sync(0xffffffffu, self.lo, off)};
     self = ff_add2(self, o);
   }
-  __shared__ double wsum[8];
+  __shared__ double wsum[kPmeThreads / 32];
   if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = (double)self.hi + (double)self.lo;
-  // ---- inverse transform along k3 (columns k1, element stride Hp) ----
-  float2* res = fft_cols(slab, work, A.p3, H, A.fH, Hp, 1, tw3);
+  // ---- inverse transform along k3 (columns k1, element stride Hp); the last pass
+  // writes T1[b][z][k2][k1] ----
+  float2* out = A.t1 + (size_t)b * K3 * A.K2 * H + (size_t)k2 * H;
+  fft_cols_io(slab, Hp, 1, work, slab, A.p3, H, A.fH, Hp, 1, out, A.K2 * H, 1, tw3);
   if (threadIdx.x == 0) {
     double t = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += wsum[w];
     A.self_part[(size_t)b * A.K2 + k2] = t;
-  }
-  // ---- T1[b][z][k2][k1] ----
-  float2* out = A.t1 + (size_t)b * K3 * A.K2 * H;
-  for (int t = threadIdx.x; t < K3 * H; t += blockDim.x) {
-    const int z = fdiv(t, A.fH), k1 = t - z * H;
-    out[((size_t)z * A.K2 + k2) * H + k1] = res[(size_t)z * Hp + k1];
   }
 }
 
 // CTA per (z, placement): the k2 transform of the (k2, k1) plane, then the
 // complex-to-real transform along k1, two rows per complex transform; writes the real
 // plane phi[b][z][y][x] with coalesced row stores.
-__global__ void __launch_bounds__(256) pme_b_kernel(PmeArgs A) {
+__global__ void __launch_bounds__(kPmeThreads, 2) pme_b_kernel(PmeArgs A) {
   extern __shared__ float2 sm[];
   const int z = blockIdx.x, b = blockIdx.y;
   const int K1 = A.K1, K2 = A.K2, K3 = A.K3, H = A.H, K1p = A.K1p;
@@ -473,15 +495,12 @@ __global__ void __launch_bounds__(256) pme_b_kernel(PmeArgs A) {
       tw2[i - K1] = make_float2(t.x, -t.y);
   }
   const float2* in = A.t1 + ((size_t)b * K3 + z) * plane;
-  if ((plane & 1) == 0) {  // every plane starts 16-byte aligned
-    const float4* in4 = reinterpret_cast<const float4*>(in);
-    float4* s04 = reinterpret_cast<float4*>(s0);
-    for (int t = threadIdx.x; t < (int)(plane / 2); t += blockDim.x) s04[t] = in4[t];
-  } else {
-    for (int t = threadIdx.x; t < (int)plane; t += blockDim.x) s0[t] = in[t];
-  }
-  // k2 transform: columns k1 (stride 1), elements along k2 (stride H)
-  float2* r = fft_cols(s0, s1, A.p2, H, A.fH, H, 1, tw2);
+  // k2 transform: columns k1 (stride 1), elements along k2 (stride H); the first pass
+  // reads the plane from global memory
+  const int np2 = A.p2.npass;
+  float2* r = (np2 == 1) ? s0 : ((((np2 - 2) & 1) ? s0 : s1));  // not the last pass's source
+  fft_cols_io(in, H, 1, s0, s1, A.p2, H, A.fH, H, 1, r, H, 1, tw2);
+  __syncthreads();
   float2* w = (r == s0) ? s1 : s0;
   // pack row pairs: Z_p[k] = X_{2p}[k] + i X_{2p+1}[k], Hermitian-completed in k1;
   // rows padded to K1p (odd) so the row transforms are bank-conflict free
@@ -601,12 +620,12 @@ cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a) {
       return err;
     attr_b = sb;
   }
-  pme_a_kernel<<<dim3(A.K2, a.nb), 256, sa, e.stream>>>(A);
+  pme_a_kernel<<<dim3(A.K2, a.nb), kPmeThreads, sa, e.stream>>>(A);
   e.count_launch();
   if ((err = cudaGetLastError()) != cudaSuccess) return err;
   e.phase_end();
   e.phase_begin(PH_FFT);
-  pme_b_kernel<<<dim3(A.K3, a.nb), 256, sb, e.stream>>>(A);
+  pme_b_kernel<<<dim3(A.K3, a.nb), kPmeThreads, sb, e.stream>>>(A);
   e.count_launch();
   return cudaGetLastError();
 }
