@@ -132,6 +132,7 @@ static int free_batch(Engine& e) {
   dfree(b.u_x);
   dfree(b.u_pos);
   dfree(b.u_q);
+  dfree(b.u_qf);
   dfree(b.u_grid);
   dfree(b.u_w);
   dfree(b.u_bvec);
@@ -259,6 +260,7 @@ static int ensure_batch(Engine& e) {
   ERMOD_CUDA(dalloc(&b.u_x, (size_t)B * S * 3));
   ERMOD_CUDA(dalloc(&b.u_pos, (size_t)B * S));
   ERMOD_CUDA(dalloc(&b.u_q, (size_t)B * S));
+  ERMOD_CUDA(dalloc(&b.u_qf, (size_t)B * S));
   ERMOD_CUDA(dalloc(&b.u_grid, (size_t)B * S));
   ERMOD_CUDA(dalloc(&b.u_w, (size_t)B * S * 3 * kMaxSplineOrder));
   ERMOD_CUDA(dalloc(&b.u_qmol, 2 * B));    // read by the accumulation: two batch slots

@@ -77,6 +77,7 @@ struct BatchArgs {
   double* u_x;         // [nb][S][3] wrapped FP64 coords
   int4* u_pos;         // [nb][S] fixed point + ljtype
   double* u_q;         // [nb][S]
+  float* u_qf;         // [nb][S] FP32 copy for the mixed kernels
   int* u_grid;         // [nb][S] packed base grid
   double* u_w;         // [nb][S][3][P] FP64 spline weights
   float2* u_bvec;      // [nb][S][3][Kmax] 1-D structure factors (mixed)

@@ -348,7 +348,7 @@ constexpr int kR1 = 4, kR3 = 4;
 
 struct PmeArgs {
   const float2* bvec;   // [nb][S][3][Kmax]
-  const double* u_q;    // [nb][S]
+  const float* u_qf;    // [nb][S]
   const int* u_nsite;
   const float* engfac;  // [K3][K2][H]
   const float2* twiddle;  // per axis, exp(-2 pi i m / K): conjugated here for the inverse
@@ -391,7 +391,7 @@ __global__ void __launch_bounds__(kPmeThreads, 2) pme_a_kernel(PmeArgs A) {
     for (int t = threadIdx.x; t < nsc * K3; t += blockDim.x) {
       const int sl = t / K3, k3 = t - sl * K3;
       const size_t us = (size_t)(s0 + sl);
-      const float q = (float)A.u_q[(size_t)b * kMaxSoluteSites + us];
+      const float q = A.u_qf[(size_t)b * kMaxSoluteSites + us];
       const float2 b2 = bv[(us * 3 + 1) * A.Kmax + k2];
       const float2 b3 = bv[(us * 3 + 2) * A.Kmax + k3];
       sd[sl * K3 + k3] = cmul(make_float2(q * b2.x, q * b2.y), b3);
@@ -580,7 +580,7 @@ bool pme_fits(int K1, int K2, int K3) {
 cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a) {
   PmeArgs A{};
   A.bvec = a.u_bvec;
-  A.u_q = a.u_q;
+  A.u_qf = a.u_qf;
   A.u_nsite = a.u_nsite;
   A.engfac = e.d_engfac_f;
   A.twiddle = e.d_twiddle;

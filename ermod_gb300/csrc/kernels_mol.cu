@@ -21,6 +21,10 @@
 
 namespace ermod {
 
+struct LjK {  // switching constants (realcal.F90:629-642, 888-904)
+  float lw2, up2, lw3, up3, lw6, up6, repA, repB, repC, attA, attB, attC, lw, up, ele2, den3;
+};
+
 struct MolArgs {
   // frame, slot order
   const int4* site_pos;
@@ -51,6 +55,11 @@ struct MolArgs {
   FrameGeom g;
   int ljswitch;
   double elecut, lwljcut, upljcut, screen;
+  // FP32 constants of the mixed kernels, computed on the host
+  float fxf[3];    // fixed-point unit per axis (box length / 2^32)
+  float screen_f;  // Ewald beta
+  float rc_f;      // max(elecut, upljcut)
+  LjK k32;         // LJ switching constants
   double resid_fac;  // pi / screen^2 / volume
   // batch
   BatchArgs a;
@@ -59,10 +68,6 @@ struct MolArgs {
 };
 
 namespace {
-
-struct LjK {  // switching constants (realcal.F90:629-642, 888-904)
-  float lw2, up2, lw3, up3, lw6, up6, repA, repB, repC, attA, attB, attC, lw, up, ele2, den3;
-};
 
 template <typename T>
 __device__ __forceinline__ T lj_low(int sw, const LjK& k, T eps, T sg2, T dist) {
@@ -156,7 +161,7 @@ __device__ __forceinline__ double lj_switch64(int sw, const LjK64& k, double eps
   return 4.0 * eps * (vdwa - vdwb);
 }
 
-__device__ __forceinline__ void gmx_params(int pw, double lw, double up, double& A, double& B, double& C) {
+__host__ __device__ __forceinline__ void gmx_params(int pw, double lw, double up, double& A, double& B, double& C) {
   const double df = up - lw;
   double upp2 = 1.0, upp = 1.0;
   for (int i = 0; i < pw + 2; ++i) upp2 *= up;
@@ -166,7 +171,7 @@ __device__ __forceinline__ void gmx_params(int pw, double lw, double up, double&
   C = 1.0 / upp - A * (df * df * df) - B * (df * df * df * df);
 }
 
-__device__ __forceinline__ LjK64 make_k64(const MolArgs& A) {
+__host__ __device__ __forceinline__ LjK64 make_k64(const MolArgs& A) {
   LjK64 k;
   k.lw = A.lwljcut;
   k.up = A.upljcut;
@@ -182,7 +187,7 @@ __device__ __forceinline__ LjK64 make_k64(const MolArgs& A) {
   return k;
 }
 
-__device__ __forceinline__ LjK to_f32(const LjK64& d) {
+__host__ __device__ __forceinline__ LjK to_f32(const LjK64& d) {
   LjK k;
   k.lw2 = (float)d.lw2; k.up2 = (float)d.up2; k.lw3 = (float)d.lw3; k.up3 = (float)d.up3;
   k.lw6 = (float)d.lw6; k.up6 = (float)d.up6; k.repA = (float)d.repA; k.repB = (float)d.repB;
@@ -331,17 +336,17 @@ __device__ __forceinline__ float real_mixed(const MolArgs& A, const BatchArgs& a
   const size_t ub = (size_t)b * kMaxSoluteSites;
   const int4 p0 = A.site_pos[s0];
   const int4 u0 = a.u_pos[ub];
-  const float fx = (float)g.fx_scale[0], fy = (float)g.fx_scale[1], fz = (float)g.fx_scale[2];
+  const float fx = A.fxf[0], fy = A.fxf[1], fz = A.fxf[2];
   const float dx = (float)(int)((unsigned)p0.x - (unsigned)u0.x) * fx;
   const float dy = (float)(int)((unsigned)p0.y - (unsigned)u0.y) * fy;
   const float dz = (float)(int)((unsigned)p0.z - (unsigned)u0.z) * fz;
   float real = 0.f;
   if (dx * dx + dy * dy + dz * dz > rcut * rcut) return real;
   const int nu = a.u_nsite[b];
-  const float beta = (float)A.screen;
+  const float beta = A.screen_f;
   for (int su = 0; su < nu; ++su) {
     const int4 up = a.u_pos[ub + su];
-    const float qu = (float)a.u_q[ub + su];
+    const float qu = a.u_qf[ub + su];
     float e = 0.f;
     for (int s = 0; s < ns; ++s) {
       const int4 vp = A.site_pos[s0 + s];
@@ -654,88 +659,149 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, uint32_t 
 }
 constexpr long kWaitLimit = 1L << 24;  // try_wait rounds before a CTA gives up and flags an error
 
-// Mixed path, step 1 -- gather by bricks.  CTA per (8^3 brick of the PME grid, group of
-// 4 placements).  One TMA 4-D box copy brings the brick's stencil halo of the four
-// placements' padded potential grids into shared memory ([4][z][y][x]); it is then
-// interleaved to [point][4], and each thread takes a site of the brick, computes its
-// B-spline weights once (FP32, stable recursion) and accumulates q theta theta theta phi
+// Mixed path, step 1 -- gather by bricks.  CTA per (8^3 brick of the PME grid, run of
+// placement groups of 4).  TMA 4-D box copies bring the brick's stencil halo of one
+// group's padded potential grids into shared memory ([4][z][y][x]), double-buffered so
+// the next group's copy is in flight while this one is used; the box is interleaved to
+// [point][4] and each thread takes a site of the brick (its B-spline weights computed
+// once for all groups, FP32 stable recursion) and accumulates q theta theta theta phi
 // for the four placements with one 16-byte shared load per stencil point.
+constexpr int kGatherThreads = 128;
+
 template <int P>
-__global__ void __launch_bounds__(128) gather_tma_kernel(const __grid_constant__ CUtensorMap tmap, int nb,
-                                                         const float4* __restrict__ site_rec,
-                                                         const int* __restrict__ site_grid,
-                                                         const int* __restrict__ brick_site,
-                                                         const int* __restrict__ brick_start, int K1, int K2, int K3,
-                                                         int nbx, int nby, int BX, int ldb,
-                                                         float* __restrict__ site_e, DevStatus* status) {
+__device__ __forceinline__ void site_setup(int site, const float4* __restrict__ site_rec,
+                                           const int* __restrict__ site_grid, int K1, int K2, int K3, int ox,
+                                           int oy, int oz, int BX, float (&w1)[P], float (&w2)[P],
+                                           float (&w3)[P], int& base, float& q) {
+  constexpr int BY = 8 + P - 1;
+  const float4 rec = site_rec[site];
+  const int gp = site_grid[site];
+  bspline_w<P>(rec.x, w1);
+  bspline_w<P>(rec.y, w2);
+  bspline_w<P>(rec.z, w3);
+  int g1 = gp & 1023, g2 = (gp >> 10) & 1023, g3 = (gp >> 20) & 1023;
+  if (g1 >= K1) g1 -= K1;
+  if (g2 >= K2) g2 -= K2;
+  if (g3 >= K3) g3 -= K3;
+  base = ((g3 - oz) * BY + (g2 - oy)) * BX + (g1 - ox);  // stencil c covers l0 - c
+  q = rec.w;
+}
+
+template <int P>
+__device__ __forceinline__ float4 site_stencil(const float4* __restrict__ halo, int base, int BX,
+                                               const float (&w1)[P], const float (&w2)[P], const float (&w3)[P]) {
+  constexpr int BY = 8 + P - 1;
+  constexpr int U3 = P <= 4 ? P : 1;  // higher orders: keep the register footprint bounded
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll U3
+  for (int c3 = 0; c3 < P; ++c3) {
+#pragma unroll
+    for (int c2 = 0; c2 < P; ++c2) {
+      const float w32 = w3[c3] * w2[c2];
+      const float4* row = halo + base - (c3 * BY + c2) * BX;
+#pragma unroll
+      for (int c1 = 0; c1 < P; ++c1) {
+        const float w = w32 * w1[c1];
+        const float4 v = row[-c1];
+        acc.x = fmaf(w, v.x, acc.x);
+        acc.y = fmaf(w, v.y, acc.y);
+        acc.z = fmaf(w, v.z, acc.z);
+        acc.w = fmaf(w, v.w, acc.w);
+      }
+    }
+  }
+  return acc;
+}
+
+template <int P>
+__global__ void __launch_bounds__(kGatherThreads) gather_tma_kernel(
+    const __grid_constant__ CUtensorMap tmap, int nb, int groups_per_cta, const float4* __restrict__ site_rec,
+    const int* __restrict__ site_grid, const int* __restrict__ brick_site, const int* __restrict__ brick_start,
+    int K1, int K2, int K3, int nbx, int nby, int BX, int ldb, float* __restrict__ site_e, DevStatus* status) {
   constexpr int BY = 8 + P - 1, BZ = 8 + P - 1;
   extern __shared__ unsigned char smem_raw[];
-  __shared__ unsigned long long bar;
-  float* box = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
+  __shared__ unsigned long long bar[2];
   const int npt = BZ * BY * BX;
-  float4* halo = reinterpret_cast<float4*>(box + 4 * npt);
-  const int brick = blockIdx.x, b0 = blockIdx.y * 4;
+  float* box0 = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
+  const int boxf = (4 * npt + 31) & ~31;  // box stride in floats, rounded up to 128 bytes (TMA destination)
+  float* box1 = box0 + boxf;
+  float4* halo = reinterpret_cast<float4*>(box1 + boxf);
+  const int brick = blockIdx.x;
   const int bx = brick % nbx, by = (brick / nbx) % nby, bz = brick / (nbx * nby);
+  const int g_begin = blockIdx.y * groups_per_cta;
+  const int g_end = min((nb + 3) / 4, g_begin + groups_per_cta);
+  const uint32_t box_bytes = (uint32_t)(4 * npt * sizeof(float));
   if (threadIdx.x == 0) {
-    mbar_init(&bar, 1);
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
     fence_barrier_init();
     fence_proxy_async_smem();
   }
   __syncthreads();
+  // padded coordinates: the halo of brick (bx, by, bz) starts at 8 bx (x is a multiple of 4)
   if (threadIdx.x == 0) {
-    mbar_expect_tx(&bar, (uint32_t)(4 * npt * sizeof(float)));
-    // padded coordinates: the halo of brick (bx, by, bz) starts at 8 bx (x is a multiple of 4)
-    tma_load_4d(box, &tmap, bx * 8, by * 8, bz * 8, b0, &bar);
-  }
-  bool ok = false;
-  for (long it = 0; it < kWaitLimit; ++it)
-    if (mbar_try_wait(&bar, 0)) {
-      ok = true;
-      break;
+    for (int g = g_begin; g < min(g_end, g_begin + 2); ++g) {
+      unsigned long long* br = &bar[(g - g_begin) & 1];
+      mbar_expect_tx(br, box_bytes);
+      tma_load_4d(((g - g_begin) & 1) ? box1 : box0, &tmap, bx * 8, by * 8, bz * 8, 4 * g, br);
     }
-  if (!ok) {
-    if (threadIdx.x == 0) atomicOr(&status->range_fault, 2);
-    return;
   }
-  for (int t = threadIdx.x; t < npt; t += blockDim.x)
-    halo[t] = make_float4(box[t], box[npt + t], box[2 * npt + t], box[3 * npt + t]);
-  __syncthreads();
   const int h = P - 1;
   const int ox = bx * 8 - h, oy = by * 8 - h, oz = bz * 8 - h;
-  const int s_end = brick_start[brick + 1];
-  for (int i = brick_start[brick] + threadIdx.x; i < s_end; i += blockDim.x) {
-    const int site = brick_site[i];
-    const float4 rec = site_rec[site];
-    const int gp = site_grid[site];
-    float w1[P], w2[P], w3[P];
-    bspline_w<P>(rec.x, w1);
-    bspline_w<P>(rec.y, w2);
-    bspline_w<P>(rec.z, w3);
-    int g1 = gp & 1023, g2 = (gp >> 10) & 1023, g3 = (gp >> 20) & 1023;
-    if (g1 >= K1) g1 -= K1;
-    if (g2 >= K2) g2 -= K2;
-    if (g3 >= K3) g3 -= K3;
-    const int lx0 = g1 - ox, ly0 = g2 - oy, lz0 = g3 - oz;  // stencil c covers l0 - c
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-    for (int c3 = 0; c3 < P; ++c3) {
-#pragma unroll
-      for (int c2 = 0; c2 < P; ++c2) {
-        const float w32 = w3[c3] * w2[c2];
-        const float4* row = halo + ((lz0 - c3) * BY + (ly0 - c2)) * BX + lx0;
-#pragma unroll
-        for (int c1 = 0; c1 < P; ++c1) {
-          const float w = w32 * w1[c1];
-          const float4 v = row[-c1];
-          acc.x = fmaf(w, v.x, acc.x);
-          acc.y = fmaf(w, v.y, acc.y);
-          acc.z = fmaf(w, v.z, acc.z);
-          acc.w = fmaf(w, v.w, acc.w);
-        }
+  const int s_begin = brick_start[brick], s_end = brick_start[brick + 1];
+  // this thread's first site, set up once for every group
+  const int i0 = s_begin + threadIdx.x;
+  float w1[P], w2[P], w3[P];
+  int base = 0, site0 = -1;
+  float q = 0.f;
+  if (i0 < s_end) {
+    site0 = brick_site[i0];
+    site_setup<P>(site0, site_rec, site_grid, K1, K2, K3, ox, oy, oz, BX, w1, w2, w3, base, q);
+  }
+  for (int g = g_begin; g < g_end; ++g) {
+    const int slot = (g - g_begin) & 1;
+    const uint32_t parity = (uint32_t)(((g - g_begin) >> 1) & 1);
+    bool ok = false;
+    for (long it = 0; it < kWaitLimit; ++it)
+      if (mbar_try_wait(&bar[slot], parity)) {
+        ok = true;
+        break;
       }
+    if (!ok) {  // flag, let the other copy in flight land (bounded), leave
+      if (threadIdx.x == 0) atomicOr(&status->range_fault, 2);
+      if (g + 1 < g_end) {
+        const uint32_t par1 = (uint32_t)(((g + 1 - g_begin) >> 1) & 1);
+        for (long it = 0; it < kWaitLimit; ++it)
+          if (mbar_try_wait(&bar[slot ^ 1], par1)) break;
+      }
+      return;
     }
-    *reinterpret_cast<float4*>(site_e + (size_t)site * ldb + b0) =
-        make_float4(rec.w * acc.x, rec.w * acc.y, rec.w * acc.z, rec.w * acc.w);
+    const float* box = slot ? box1 : box0;
+    for (int t = threadIdx.x; t < npt; t += blockDim.x)
+      halo[t] = make_float4(box[t], box[npt + t], box[2 * npt + t], box[3 * npt + t]);
+    __syncthreads();  // halo ready; box[slot] consumed
+    if (threadIdx.x == 0 && g + 2 < g_end) {
+      fence_proxy_async_smem();
+      mbar_expect_tx(&bar[slot], box_bytes);
+      tma_load_4d(slot ? box1 : box0, &tmap, bx * 8, by * 8, bz * 8, 4 * (g + 2), &bar[slot]);
+    }
+    const int b0 = 4 * g;
+    if (site0 >= 0) {
+      const float4 acc = site_stencil<P>(halo, base, BX, w1, w2, w3);
+      *reinterpret_cast<float4*>(site_e + (size_t)site0 * ldb + b0) =
+          make_float4(q * acc.x, q * acc.y, q * acc.z, q * acc.w);
+    }
+    for (int i = i0 + blockDim.x; i < s_end; i += blockDim.x) {  // bricks with more sites than threads
+      const int site = brick_site[i];
+      float v1[P], v2[P], v3[P];
+      int bs;
+      float qs;
+      site_setup<P>(site, site_rec, site_grid, K1, K2, K3, ox, oy, oz, BX, v1, v2, v3, bs, qs);
+      const float4 acc = site_stencil<P>(halo, bs, BX, v1, v2, v3);
+      *reinterpret_cast<float4*>(site_e + (size_t)site * ldb + b0) =
+          make_float4(qs * acc.x, qs * acc.y, qs * acc.z, qs * acc.w);
+    }
+    __syncthreads();  // halo reused by the next group
   }
 }
 
@@ -771,18 +837,14 @@ __global__ void __launch_bounds__(256) mol_finish_kernel(MolArgs A, const float*
   const bool spec_ok = valid && species >= 1 && species <= A.numslv;
   sspec[threadIdx.x] = (unsigned char)(spec_ok ? species : 0);
   const int ldb = A.ldb;
-  LjK k32;
-  {
-    const LjK64 k64 = make_k64(A);
-    k32 = to_f32(k64);
-  }
+  const LjK& k32 = A.k32;
   int sp_off = 0, sp_n = 1, sp_soft = 1;
   if (spec_ok) {
     sp_off = A.spec[3 * (species - 1)];
     sp_n = A.spec[3 * (species - 1) + 1];
     sp_soft = A.spec[3 * (species - 1) + 2];
   }
-  const float rc = (float)fmax(A.elecut, A.upljcut);
+  const float rc = A.rc_f;
   const float mol_r = A.frame_scal[0];
   __syncthreads();  // squ staged
   // ---- totals for the G placements (FP32: the site terms are FP32 already) ----
@@ -960,6 +1022,10 @@ cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
   A.upljcut = e.P.upljcut;
   A.screen = e.P.screen;
   A.resid_fac = kPi / e.P.screen / e.P.screen / e.geom.volume;
+  for (int i = 0; i < 3; ++i) A.fxf[i] = (float)e.geom.fx_scale[i];
+  A.screen_f = (float)e.P.screen;
+  A.rc_f = (float)std::max(e.P.elecut, e.P.upljcut);
+  A.k32 = to_f32(make_k64(A));
   A.a = a;
   A.ntile = e.ntile;
   A.status = e.d_status;
@@ -976,11 +1042,14 @@ cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
     return launch_p<false>(e, A, grid, smem);
   }
   if (a.G != 8 && a.G != 4) return cudaErrorInvalidValue;
-  {  // step 1: gather by bricks (TMA-staged halos)
-    dim3 g1(e.nbricks, (a.nb + 3) / 4);
+  {  // step 1: gather by bricks (TMA-staged halos, double-buffered over placement groups)
+    const int ngroups = (a.nb + 3) / 4;
+    const int gpc = std::min(ngroups, 4);
+    dim3 g1(e.nbricks, (ngroups + gpc - 1) / gpc);
     const int K1 = e.geom.K[0], K2 = e.geom.K[1], K3 = e.geom.K[2];
     const size_t npt = (size_t)e.gbox[0] * e.gbox[1] * e.gbox[2];
-    const size_t sh = 128 + npt * 4 * sizeof(float) + npt * sizeof(float4);
+    const size_t boxf = (4 * npt + 31) & ~(size_t)31;  // as in the kernel: 128-byte aligned boxes
+    const size_t sh = 128 + 2 * boxf * sizeof(float) + npt * sizeof(float4);
 #define ERMOD_GATHER(PP)                                                                                        \
   if (e.P_order == PP) {                                                                                        \
     static size_t attr = 0;                                                                                     \
@@ -989,9 +1058,9 @@ cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
       if (err != cudaSuccess) return err;                                                                       \
       attr = sh;                                                                                                \
     }                                                                                                           \
-    gather_tma_kernel<PP><<<g1, 128, sh, e.stream>>>(e.phi_tmap, a.nb, e.d_site_rec, e.d_site_grid,               \
-                                                     e.d_brick_site, e.d_brick_start, K1, K2, K3, e.nbrick[0],    \
-                                                     e.nbrick[1], e.gbox[0], e.Bmax, e.d_site_e, e.d_status);   \
+    gather_tma_kernel<PP><<<g1, kGatherThreads, sh, e.stream>>>(                                                \
+        e.phi_tmap, a.nb, gpc, e.d_site_rec, e.d_site_grid, e.d_brick_site, e.d_brick_start, K1, K2, K3,        \
+        e.nbrick[0], e.nbrick[1], e.gbox[0], e.Bmax, e.d_site_e, e.d_status);                                   \
   }
     ERMOD_GATHER(4)
     ERMOD_GATHER(6)

@@ -120,6 +120,7 @@ __global__ void __launch_bounds__(256) place_prep_kernel(PrepArgs A) {
     for (int i = 0; i < 3; ++i) X[i] = (unsigned int)(unsigned long long)llrint(w[i] * g.invL[i] * 4294967296.0);
     a.u_pos[us] = make_int4((int)X[0], (int)X[1], (int)X[2], A.ljtype[atom0 + s]);
     a.u_q[us] = A.charge[atom0 + s];
+    a.u_qf[us] = (float)A.charge[atom0 + s];
     int rci[3];
     for (int kk = 0; kk < 3; ++kk) {  // calc_spline_molecule on the raw coordinates
       double factor = g.invcl[kk + 0] * raw[0] + g.invcl[kk + 3] * raw[1] + g.invcl[kk + 6] * raw[2];
