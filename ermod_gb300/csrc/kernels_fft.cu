@@ -359,7 +359,7 @@ struct PmeArgs {
   int chunk;  // solute sites staged per generation chunk (fits the k3 work buffer)
   int halo, XP, YP, ZP;  // padded periodic potential grid (see pme_b)
   FftPlan p1, p2, p3;
-  FastDiv fH, fK1, fHp4, fnpair;
+  FastDiv fH, fK1, fHp4, fnpair, fKX;
 };
 
 constexpr int kPmeThreads = 512;
@@ -532,30 +532,17 @@ __global__ void __launch_bounds__(kPmeThreads, 2) pme_b_kernel(PmeArgs A) {
   // gather is one in-bounds box (rows XP floats, planes YP rows, ZP planes)
   const int h = A.halo;
   float* out = A.phi + (size_t)b * A.ZP * A.YP * A.XP;
-  const int z0 = z + h, z1 = (z >= K3 - h) ? z - K3 + h : -1;
-  for (int t = threadIdx.x; t < npair * K1; t += blockDim.x) {
-    const int pp = fdiv(t, A.fK1), x = t - pp * K1;
-    const float2 v = res[(size_t)pp * K1p + x];
-    const int x0 = x + h, x1 = (x >= K1 - h) ? x - K1 + h : -1;
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      const int y = 2 * pp + q;
-      if (y >= K2) break;
-      const float val = q ? v.y : v.x;
-      const int y0 = y + h, y1 = (y >= K2 - h) ? y - K2 + h : -1;
-#pragma unroll
-      for (int cz = 0; cz < 2; ++cz) {
-        const int zz = cz ? z1 : z0;
-        if (zz < 0) continue;
-#pragma unroll
-        for (int cy = 0; cy < 2; ++cy) {
-          const int yy = cy ? y1 : y0;
-          if (yy < 0) continue;
-          float* row = out + ((size_t)zz * A.YP + yy) * A.XP;
-          row[x0] = val;
-          if (x1 >= 0) row[x1] = val;
-        }
-      }
+  const int KX = K1 + h, KY = K2 + h;  // written extent of a padded plane
+  const int ncopy = (z >= K3 - h) ? 2 : 1;
+  for (int c = 0; c < ncopy; ++c) {
+    float* plane_out = out + (size_t)(c ? z - K3 + h : z + h) * A.YP * A.XP;
+    for (int t = threadIdx.x; t < KX * KY; t += blockDim.x) {
+      const int yy = fdiv(t, A.fKX), xx = t - yy * KX;
+      int y = yy - h, x = xx - h;
+      if (y < 0) y += K2;
+      if (x < 0) x += K1;
+      const float2 v = res[(size_t)(y >> 1) * K1p + x];
+      plane_out[(size_t)yy * A.XP + xx] = (y & 1) ? v.y : v.x;
     }
   }
 }
@@ -607,6 +594,7 @@ cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a) {
   A.fK1 = make_fastdiv(A.K1);
   A.fHp4 = make_fastdiv(A.Hp / kR1);
   A.fnpair = make_fastdiv((A.K2 + 1) / 2);
+  A.fKX = make_fastdiv(A.K1 + A.halo);
   const size_t sa = pme_a_smem(A.K3, A.Hp), sb = pme_b_smem(A.K1, A.K2, A.H);
   static size_t attr_a = 0, attr_b = 0;
   cudaError_t err;

@@ -331,11 +331,8 @@ __device__ __forceinline__ void hist_add(int* h, int bin) {
 // real-space LJ + screened Coulomb of one molecule against solute b (mixed path):
 // fixed-point displacements, FP32 pair terms, FP64 sum over solute sites.
 __device__ __forceinline__ float real_mixed(const MolArgs& A, const BatchArgs& a, int b, int s0, int ns,
-                                            const LjK& k32, float rcut) {
-  const FrameGeom& g = A.g;
+                                            const LjK& k32, float rcut, int4 p0, int4 u0) {
   const size_t ub = (size_t)b * kMaxSoluteSites;
-  const int4 p0 = A.site_pos[s0];
-  const int4 u0 = a.u_pos[ub];
   const float fx = A.fxf[0], fy = A.fxf[1], fz = A.fxf[2];
   const float dx = (float)(int)((unsigned)p0.x - (unsigned)u0.x) * fx;
   const float dy = (float)(int)((unsigned)p0.y - (unsigned)u0.y) * fy;
@@ -809,12 +806,15 @@ __global__ void __launch_bounds__(kGatherThreads) gather_tma_kernel(
 // space, residual, then the G bin searches in lockstep (binary lifting over the edge
 // keys staged in shared memory), histograms and per-species partials.
 template <int G>
-__global__ void __launch_bounds__(256) mol_finish_kernel(MolArgs A, const float* __restrict__ site_e) {
+__global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const float* __restrict__ site_e) {
   extern __shared__ int smem_dyn[];
   int* smem_hist = smem_dyn;                                                  // [G][ermax]
   long long* skeys = reinterpret_cast<long long*>(smem_dyn + ((G * A.ermax + 1) & ~1));  // [ermax]
   __shared__ float su[G][256];
-  __shared__ float squ[G];  // solute charges of the G placements
+  __shared__ float squ[G];    // residual factor x solute charge of the G placements
+  __shared__ float srcut[G];  // bounding-sphere cutoff of the real-space sum
+  __shared__ int skskip[G];   // slot of the solute molecule itself (not a solvent)
+  __shared__ int4 supos[G];   // first solute site (fixed point)
   __shared__ unsigned char sspec[256];
   const int tile = blockIdx.y;
   const int g0 = blockIdx.x * G;
@@ -824,7 +824,14 @@ __global__ void __launch_bounds__(256) mol_finish_kernel(MolArgs A, const float*
   const bool valid = m < A.slvmax;
   for (int i = threadIdx.x; i < G * A.ermax; i += blockDim.x) smem_hist[i] = 0;
   for (int i = threadIdx.x; i < A.ermax; i += blockDim.x) skeys[i] = A.uvkey[i];
-  if (threadIdx.x < ng) squ[threadIdx.x] = (float)(A.resid_fac * a.u_qmol[g0 + threadIdx.x]);
+  if (threadIdx.x < ng) {
+    const int b = g0 + threadIdx.x;
+    squ[threadIdx.x] = (float)(A.resid_fac * a.u_qmol[b]);
+    srcut[threadIdx.x] = A.rc_f + a.u_radius[b] + A.frame_scal[0];
+    const int tg = a.tagslt[b] - 1;
+    skskip[threadIdx.x] = (tg >= 0 && tg < A.nummol) ? A.mol_to_k[tg] : -2;
+    supos[threadIdx.x] = a.u_pos[(size_t)b * kMaxSoluteSites];
+  }
   int k = -1, s0 = 0, ns = 0, species = 0;
   float qmol = 0.f;
   if (valid) {
@@ -844,24 +851,45 @@ __global__ void __launch_bounds__(256) mol_finish_kernel(MolArgs A, const float*
     sp_n = A.spec[3 * (species - 1) + 1];
     sp_soft = A.spec[3 * (species - 1) + 2];
   }
-  const float rc = A.rc_f;
-  const float mol_r = A.frame_scal[0];
   __syncthreads();  // squ staged
   // ---- totals for the G placements (FP32: the site terms are FP32 already) ----
   float uu[G];
   bool act[G];
+  // site terms of the G placements: G consecutive floats per site (16-byte aligned when
+  // G, g0 and ldb are multiples of 4)
+  float rsum[G];
+#pragma unroll
+  for (int j = 0; j < G; ++j) rsum[j] = 0.f;
+  int4 p0 = make_int4(0, 0, 0, 0);
+  if (valid) {
+    p0 = A.site_pos[s0];
+    for (int s = 0; s < ns; ++s) {
+      const float* row = site_e + (size_t)(s0 + s) * ldb + g0;
+      if (G % 4 == 0 && ng == G) {
+#pragma unroll
+        for (int j4 = 0; j4 < G; j4 += 4) {
+          const float4 v = __ldg(reinterpret_cast<const float4*>(row + j4));
+          rsum[j4] += v.x;
+          rsum[j4 + 1] += v.y;
+          rsum[j4 + 2] += v.z;
+          rsum[j4 + 3] += v.w;
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < G; ++j)
+          if (j < ng) rsum[j] += __ldg(row + j);
+      }
+    }
+  }
 #pragma unroll
   for (int j = 0; j < G; ++j) {
     uu[j] = 0.f;
     act[j] = false;
     if (j < ng) {
       const int b = g0 + j;
-      const int tg = a.tagslt[b] - 1;
-      const int kskip = (tg >= 0 && tg < A.nummol) ? A.mol_to_k[tg] : -2;
-      if (valid && k != kskip) {
-        float recip = 0.f;
-        for (int s = 0; s < ns; ++s) recip += site_e[(size_t)(s0 + s) * ldb + b];
-        const float real = real_mixed(A, a, b, s0, ns, k32, rc + a.u_radius[b] + mol_r);
+      if (valid && k != skskip[j]) {
+        const float recip = rsum[j];
+        const float real = real_mixed(A, a, b, s0, ns, k32, srcut[j], p0, supos[j]);
         const float epcl = squ[j] * qmol;  // residual_ene: pi Q_u Q_v / (beta^2 V)
         float pairep = -epcl;
         pairep = pairep + recip;
