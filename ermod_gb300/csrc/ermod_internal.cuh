@@ -28,6 +28,25 @@ constexpr int kMaxSpecies = 16;
 constexpr int kGridBits = 10;         // packed grid coordinates: K <= 1024 per axis
 constexpr double kPi = 3.1415926535897932;
 
+// B-spline weights M_P(t + j), j = 0..P-1, by the stable Cox-de Boor recursion (FP32)
+template <int P>
+__host__ __device__ __forceinline__ void bspline_w(float t, float w[P]) {
+  w[0] = t;
+  w[1] = 1.f - t;
+#pragma unroll
+  for (int j = 2; j < P; ++j) w[j] = 0.f;
+#pragma unroll
+  for (int n = 3; n <= P; ++n) {
+    const float inv = 1.f / (float)(n - 1);
+#pragma unroll
+    for (int j = n - 1; j >= 0; --j) {
+      const float a = (j <= n - 2) ? w[j] : 0.f;
+      const float b = (j >= 1) ? w[j - 1] : 0.f;
+      w[j] = ((t + (float)j) * a + ((float)n - t - (float)j) * b) * inv;
+    }
+  }
+}
+
 // error key: (placement << 36) | (molecule << 8) | code, minimised atomically so the
 // first failing (placement, molecule) in reference order wins.
 constexpr unsigned long long kNoError = ~0ull;

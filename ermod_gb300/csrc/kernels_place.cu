@@ -1,18 +1,12 @@
-// kernels_place.cu -- per-placement solute preparation and the PME solute potential.
+// kernels_place.cu -- per-placement solute preparation and the plain FP64 PME path.
 //
 //   place_prep    solute sites of every placement in a batch: wrapped FP64 and
-//                 fixed-point coordinates, calc_spline_molecule (recpcal.F90:408-442),
+//                 fixed-point coordinates, calc_spline_molecule (recpcal.F90:408-442;
+//                 FP64 weights on the FP64 path, FP32 Cox-de Boor weights on the mixed),
 //                 realcal_self (realcal.F90:284-328, FP64) and, for the mixed path,
 //                 the 1-D structure-factor vectors
 //                     b_{s,a}(k) = sum_c theta_{s,a,c} exp(-2 pi i k (g_{s,a} - c) / K_a);
-//   spectrum      mixed path: the spread charge grid of recpcal_prepare_solute
-//                 (recpcal.F90:357-373) followed by its R2C transform (recpcal.F90:377)
-//                 equals S(k) = sum_s q_s b_{s,1}(k1) b_{s,2}(k2) b_{s,3}(k3) exactly; this
-//                 kernel evaluates S on the half-complex grid directly (FP32), multiplies
-//                 by engfac (recpcal.F90:398) and reduces the self energy
-//                 (recpcal.F90:385-394) with float-float compensation into FP64 partials.
-//                 It replaces a K^3 zero-fill, a scattered spread and a forward FFT by a
-//                 compute-bound pass that writes only the half spectrum.
+//                 (the mixed path's spectrum and transforms are in kernels_fft.cu);
 //   spread64 / influence64   the plain FP64 path, literally the reference's order:
 //                 spread, D2Z (cuFFT), self energy + engfac multiply, Z2D (cuFFT).
 #include "engine.cuh"
@@ -64,6 +58,7 @@ struct PrepArgs {
   int mixed;
   int self_mode;  // 0: none, 1: all placements, 2: only placement 0 of the batch
   int nummol;
+  unsigned mK[3], mKmax, m3Kmax;  // ceil(2^32 / d): n / d = umulhi(n, m) for n d < 2^32
   DevStatus* status;
 };
 
@@ -93,6 +88,8 @@ __global__ void __launch_bounds__(256) place_prep_kernel(PrepArgs A) {
   const int P = A.sc.order;
   __shared__ double sx[kMaxSoluteSites][3];
   __shared__ double red[256];
+  __shared__ float swf[kMaxSoluteSites][3][kMaxSplineOrder];  // mixed path: FP32 weights
+  __shared__ int sgrd[kMaxSoluteSites][3];
   if (ns > kMaxSoluteSites) {
     if (threadIdx.x == 0) {
       atomicOr(&A.status->range_fault, 1);
@@ -127,8 +124,24 @@ __global__ void __launch_bounds__(256) place_prep_kernel(PrepArgs A) {
       factor = factor - floor(factor);
       const double f2 = factor * (double)g.K[kk];
       rci[kk] = (int)f2;
-      for (int spi = 0; spi < P; ++spi)
-        a.u_w[(us * 3 + kk) * kMaxSplineOrder + spi] = spline_value(A.sc, f2 - (double)(rci[kk] - spi));
+      double* uw = a.u_w + (us * 3 + kk) * kMaxSplineOrder;
+      if (A.mixed) {  // FP32 Cox-de Boor weights, the recursion the solvent sites use
+        float wf[kMaxSplineOrder];
+        const float t = (float)(f2 - (double)rci[kk]);
+        if (P == 4)
+          bspline_w<4>(t, wf);
+        else if (P == 6)
+          bspline_w<6>(t, wf);
+        else
+          bspline_w<8>(t, wf);
+        for (int spi = 0; spi < P; ++spi) {
+          uw[spi] = (double)wf[spi];
+          swf[s][kk][spi] = wf[spi];
+        }
+        sgrd[s][kk] = rci[kk];
+      } else {
+        for (int spi = 0; spi < P; ++spi) uw[spi] = spline_value(A.sc, f2 - (double)(rci[kk] - spi));
+      }
     }
     a.u_grid[us] = rci[0] | (rci[1] << kGridBits) | (rci[2] << (2 * kGridBits));
   }
@@ -143,19 +156,23 @@ __global__ void __launch_bounds__(256) place_prep_kernel(PrepArgs A) {
     const int Kmax = max(Kx, max(Ky, Kz));
     const int total = ns * 3 * Kmax;
     for (int t = threadIdx.x; t < total; t += blockDim.x) {
-      const int k = t % Kmax;
-      const int ax = (t / Kmax) % 3;
-      const int s = t / (3 * Kmax);
+      const int s = (int)__umulhi((unsigned)t, A.m3Kmax);
+      const int r = t - s * 3 * Kmax;
+      const int ax = (int)__umulhi((unsigned)r, A.mKmax);
+      const int k = r - ax * Kmax;
       const int K = g.K[ax];
       if (k >= K) continue;
       const size_t us = (size_t)b * kMaxSoluteSites + s;
-      const int grd = (a.u_grid[us] >> (ax * kGridBits)) & ((1 << kGridBits) - 1);
+      const int grd = sgrd[s][ax];
       const float2* tw = A.twiddle + (ax == 0 ? 0 : (ax == 1 ? Kx : Kx + Ky));
+      const unsigned mk = A.mK[ax];
       float re = 0.f, im = 0.f;
       for (int c = 0; c < P; ++c) {
-        const float th = (float)a.u_w[(us * 3 + ax) * kMaxSplineOrder + c];
-        int mm = (k * (grd - c)) % K;  // |k (grd - c)| < 1000 * 1008 fits in int
-        if (mm < 0) mm += K;
+        const float th = swf[s][ax][c];
+        int gc = grd - c;  // in (-P, K)
+        if (gc < 0) gc += K;
+        const unsigned x = (unsigned)(k * gc);  // < K^2 <= 10^6
+        const int mm = (int)(x - __umulhi(x, mk) * (unsigned)K);
         const float2 w = tw[mm];
         re = fmaf(th, w.x, re);
         im = fmaf(th, w.y, im);
@@ -163,20 +180,21 @@ __global__ void __launch_bounds__(256) place_prep_kernel(PrepArgs A) {
       a.u_bvec[(us * 3 + ax) * Kmax + k] = make_float2(re, im);
     }
   }
-  // bounding radius about site 1 (minimum image)
-  if (threadIdx.x == 0) {
-    double rmax = 0.0;
-    for (int s = 1; s < ns; ++s) {
-      double r2 = 0.0;
-      for (int i = 0; i < 3; ++i) {
-        const double h = 0.5 * g.L[i];
-        const double d = h - fabs(h - fabs(sx[s][i] - sx[0][i]));
-        r2 += d * d;
-      }
-      rmax = fmax(rmax, sqrt(r2));
+  // bounding radius about site 1 (minimum image; FP32, padded to stay conservative)
+  __shared__ int rmax_bits;
+  if (threadIdx.x == 0) rmax_bits = 0;
+  __syncthreads();
+  for (int s = 1 + threadIdx.x; s < ns; s += blockDim.x) {
+    float r2 = 0.f;
+    for (int i = 0; i < 3; ++i) {
+      const float h = 0.5f * (float)g.L[i];
+      const float d = h - fabsf(h - fabsf((float)(sx[s][i] - sx[0][i])));
+      r2 += d * d;
     }
-    a.u_radius[b] = (float)rmax * 1.0001f + 1e-4f;
+    atomicMax(&rmax_bits, __float_as_int(sqrtf(r2)));  // nonnegative floats order as ints
   }
+  __syncthreads();
+  if (threadIdx.x == 0) a.u_radius[b] = __int_as_float(rmax_bits) * 1.0001f + 1e-4f;
   // realcal_self (realcal.F90:284-328), fixed-order block reduction
   const bool need_self = (A.self_mode == 1) || (A.self_mode == 2 && b == 0);
   if (need_self) {
@@ -206,134 +224,6 @@ __global__ void __launch_bounds__(256) place_prep_kernel(PrepArgs A) {
       __syncthreads();
     }
     if (threadIdx.x == 0) a.u_usreal[b] = red[0];
-  }
-}
-
-// float-float accumulation (Dekker/Knuth TwoSum)
-struct ff {
-  float hi, lo;
-};
-__device__ __forceinline__ ff ff_add(ff a, float b) {
-  const float s = a.hi + b;
-  const float bb = s - a.hi;
-  const float err = (a.hi - (s - bb)) + (b - bb);
-  const float lo = a.lo + err;
-  const float hi = s + lo;
-  return ff{hi, lo - (hi - s)};
-}
-__device__ __forceinline__ ff ff_add2(ff a, ff b) {
-  ff r = ff_add(a, b.hi);
-  return ff_add(r, b.lo);
-}
-
-constexpr int kSpecThreads = 256;
-constexpr int kSpecChunk = 32;  // solute sites staged in shared memory at once
-constexpr int kR1 = 4, kR2 = 4;  // register micro-tile: 4 k1 x 4 k2 points per thread
-
-struct SpecArgs {
-  const float2* bvec;     // [nb][S][3][Kmax]
-  const double* u_q;      // [nb][S]
-  const int* u_nsite;
-  const float* engfac;    // [K3][K2][H]
-  float2* spec;           // [nb][K3][K2][H]
-  double* self_part;      // [nb][K3]
-  int K1, K2, K3, H, Kmax;
-};
-
-// grid: (K3, nb); one CTA computes the (k1, k2) plane of one k3 for one placement:
-//   Q(k1,k2,k3) = sum_s [q_s b3_s(k3) b2_s(k2)] b1_s(k1)
-// as a sum of rank-1 updates over register micro-tiles of 4 x 4 points.
-__global__ void __launch_bounds__(kSpecThreads) spectrum_kernel(SpecArgs A) {
-  extern __shared__ float2 smem_spec[];
-  float2* sd = smem_spec;                           // [kSpecChunk][K2]
-  float2* sb = smem_spec + (size_t)kSpecChunk * A.K2;  // [kSpecChunk][H padded to 4]
-  const int k3 = blockIdx.x, b = blockIdx.y;
-  const int ns = A.u_nsite[b];
-  const int TX = (A.H + kR1 - 1) / kR1, TY = (A.K2 + kR2 - 1) / kR2;
-  const int Hp = TX * kR1;
-  const int ntiles = TX * TY;
-  const float2* bv = A.bvec + (size_t)b * kMaxSoluteSites * 3 * A.Kmax;
-  float2* spec = A.spec + (size_t)b * A.K3 * A.K2 * A.H + (size_t)k3 * A.K2 * A.H;
-  const float* ef = A.engfac + (size_t)k3 * A.K2 * A.H;
-  const bool even = (A.K1 % 2) == 0;
-  ff self{0.f, 0.f};
-  for (int s0 = 0; s0 < ns; s0 += kSpecChunk) {
-    const int nsc = min(kSpecChunk, ns - s0);
-    const bool first = (s0 == 0), last = (s0 + nsc >= ns);
-    __syncthreads();
-    for (int t = threadIdx.x; t < nsc * A.K2; t += blockDim.x) {
-      const int sl = t / A.K2, k2 = t % A.K2;
-      const size_t us = (size_t)(s0 + sl);
-      const float q = (float)A.u_q[(size_t)b * kMaxSoluteSites + us];
-      const float2 b3 = bv[(us * 3 + 2) * A.Kmax + k3];
-      const float2 b2 = bv[(us * 3 + 1) * A.Kmax + k2];
-      const float2 c3 = make_float2(q * b3.x, q * b3.y);
-      sd[sl * A.K2 + k2] = make_float2(c3.x * b2.x - c3.y * b2.y, c3.x * b2.y + c3.y * b2.x);
-    }
-    for (int t = threadIdx.x; t < nsc * Hp; t += blockDim.x) {
-      const int sl = t / Hp, k1 = t % Hp;
-      sb[sl * Hp + k1] = (k1 < A.H) ? bv[((size_t)(s0 + sl) * 3 + 0) * A.Kmax + k1] : make_float2(0.f, 0.f);
-    }
-    __syncthreads();
-    for (int mt = threadIdx.x; mt < ntiles; mt += blockDim.x) {
-      const int tx = mt % TX, ty = mt / TX;
-      const int k1a = tx * kR1, k2a = ty * kR2;
-      float2 acc[kR2][kR1];
-#pragma unroll
-      for (int j = 0; j < kR2; ++j)
-#pragma unroll
-        for (int i = 0; i < kR1; ++i) acc[j][i] = make_float2(0.f, 0.f);
-      for (int sl = 0; sl < nsc; ++sl) {
-        float2 d[kR2], e[kR1];
-#pragma unroll
-        for (int j = 0; j < kR2; ++j) d[j] = (k2a + j < A.K2) ? sd[sl * A.K2 + k2a + j] : make_float2(0.f, 0.f);
-#pragma unroll
-        for (int i = 0; i < kR1; ++i) e[i] = sb[sl * Hp + k1a + i];
-#pragma unroll
-        for (int j = 0; j < kR2; ++j)
-#pragma unroll
-          for (int i = 0; i < kR1; ++i) {
-            acc[j][i].x = fmaf(d[j].x, e[i].x, fmaf(-d[j].y, e[i].y, acc[j][i].x));
-            acc[j][i].y = fmaf(d[j].x, e[i].y, fmaf(d[j].y, e[i].x, acc[j][i].y));
-          }
-      }
-#pragma unroll
-      for (int j = 0; j < kR2; ++j) {
-        const int k2 = k2a + j;
-        if (k2 >= A.K2) continue;
-#pragma unroll
-        for (int i = 0; i < kR1; ++i) {
-          const int k1 = k1a + i;
-          if (k1 >= A.H) continue;
-          const size_t gi = (size_t)k2 * A.H + k1;
-          float2 q = acc[j][i];
-          if (!first) {  // earlier site chunks left the partial sum in the output
-            const float2 prev = spec[gi];
-            q.x += prev.x;
-            q.y += prev.y;
-          }
-          if (last) {
-            const float f = ef[gi];
-            const float wgt = (k1 == 0 || (even && k1 == A.H - 1)) ? 0.5f : 1.f;
-            self = ff_add(self, wgt * f * (q.x * q.x + q.y * q.y));
-            q = make_float2(f * q.x, f * q.y);
-          }
-          spec[gi] = q;
-        }
-      }
-    }
-  }
-  for (int off = 16; off > 0; off >>= 1) {
-    ff o{__shfl_down_sync(0xffffffffu, self.hi, off), __shfl_down_sync(0xffffffffu, self.lo, off)};
-    self = ff_add2(self, o);
-  }
-  __shared__ double wsum[kSpecThreads / 32];
-  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = (double)self.hi + (double)self.lo;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < kSpecThreads / 32; ++w) t += wsum[w];
-    A.self_part[(size_t)b * A.K3 + k3] = t;
   }
 }
 
@@ -438,34 +328,11 @@ cudaError_t launch_place_prep(Engine& e, const BatchArgs& a, const double* sol_x
   A.self_mode = self_mode;
   A.nummol = e.nummol;
   A.status = e.d_status;
+  auto magic = [](unsigned d) { return (unsigned)((0x100000000ull + d - 1) / d); };
+  for (int i = 0; i < 3; ++i) A.mK[i] = magic((unsigned)e.geom.K[i]);
+  A.mKmax = magic((unsigned)e.Kmax());
+  A.m3Kmax = magic(3u * (unsigned)e.Kmax());
   place_prep_kernel<<<a.nb, 256, 0, e.stream>>>(A);
-  e.count_launch();
-  return cudaGetLastError();
-}
-
-cudaError_t launch_spectrum(Engine& e, const BatchArgs& a) {
-  SpecArgs A{};
-  A.bvec = a.u_bvec;
-  A.u_q = a.u_q;
-  A.u_nsite = a.u_nsite;
-  A.engfac = e.d_engfac_f;
-  A.spec = a.spec;
-  A.self_part = a.self_part;
-  A.K1 = e.geom.K[0];
-  A.K2 = e.geom.K[1];
-  A.K3 = e.geom.K[2];
-  A.H = e.H();
-  A.Kmax = e.Kmax();
-  const int Hp = ((A.H + kR1 - 1) / kR1) * kR1;
-  const size_t smem = sizeof(float2) * (size_t)kSpecChunk * (A.K2 + Hp);
-  static size_t attr = 0;
-  if (attr < smem) {
-    cudaError_t err = cudaFuncSetAttribute(spectrum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (err != cudaSuccess) return err;
-    attr = smem;
-  }
-  dim3 grid(A.K3, a.nb);
-  spectrum_kernel<<<grid, kSpecThreads, smem, e.stream>>>(A);
   e.count_launch();
   return cudaGetLastError();
 }
