@@ -65,18 +65,13 @@ void Engine::phase_begin_on(int ph, cudaStream_t s) {
     cudaEventCreate(&ev);
   }
   cudaEventRecord(ev, s);
-  if (s == aux) {
-    cur_phase_aux = ph;
-    cur_ev_aux = ev;
-  } else {
-    cur_phase = ph;
-    cur_ev = ev;
-  }
+  cur_phase[stream_index(s)] = ph;
+  cur_ev[stream_index(s)] = ev;
 }
 
 void Engine::phase_end_on(cudaStream_t s) {
-  const bool on_aux = (s == aux);
-  const int ph = on_aux ? cur_phase_aux : cur_phase;
+  const int si = stream_index(s);
+  const int ph = cur_phase[si];
   if (!timing || ph < 0) return;
   cudaEvent_t ev;
   if (!ev_pool.empty()) {
@@ -86,11 +81,8 @@ void Engine::phase_end_on(cudaStream_t s) {
     cudaEventCreate(&ev);
   }
   cudaEventRecord(ev, s);
-  pending.push_back(Pending{on_aux ? cur_ev_aux : cur_ev, ev, ph});
-  if (on_aux)
-    cur_phase_aux = -1;
-  else
-    cur_phase = -1;
+  pending.push_back(Pending{cur_ev[si], ev, ph});
+  cur_phase[si] = -1;
   if (pending.size() > 8192) {  // harvest to bound the pool
     cudaEventSynchronize(ev);
     for (auto& p : pending) {
@@ -256,21 +248,22 @@ static int ensure_batch(Engine& e) {
   BatchArgs& b = e.buf;
   const size_t nr = e.grid_real(), nc = e.grid_cplx();
   e.ntile = (e.slvmax + e.tile - 1) / e.tile;
-  ERMOD_CUDA(dalloc(&b.u_nsite, B));
-  ERMOD_CUDA(dalloc(&b.u_x, (size_t)B * S * 3));
-  ERMOD_CUDA(dalloc(&b.u_pos, (size_t)B * S));
-  ERMOD_CUDA(dalloc(&b.u_q, (size_t)B * S));
-  ERMOD_CUDA(dalloc(&b.u_qf, (size_t)B * S));
-  ERMOD_CUDA(dalloc(&b.u_grid, (size_t)B * S));
-  ERMOD_CUDA(dalloc(&b.u_w, (size_t)B * S * 3 * kMaxSplineOrder));
-  ERMOD_CUDA(dalloc(&b.u_qmol, 2 * B));    // read by the accumulation: two batch slots
+  // solute data: two batch slots (the preparation of batch i+1 runs during batch i)
+  ERMOD_CUDA(dalloc(&b.u_nsite, 2 * B));
+  ERMOD_CUDA(dalloc(&b.u_x, (size_t)2 * B * S * 3));
+  ERMOD_CUDA(dalloc(&b.u_pos, (size_t)2 * B * S));
+  ERMOD_CUDA(dalloc(&b.u_q, (size_t)2 * B * S));
+  ERMOD_CUDA(dalloc(&b.u_qf, (size_t)2 * B * S));
+  ERMOD_CUDA(dalloc(&b.u_grid, (size_t)2 * B * S));
+  ERMOD_CUDA(dalloc(&b.u_w, (size_t)2 * B * S * 3 * kMaxSplineOrder));
+  ERMOD_CUDA(dalloc(&b.u_qmol, 2 * B));
   ERMOD_CUDA(dalloc(&b.u_usreal, 2 * B));
-  ERMOD_CUDA(dalloc(&b.u_radius, B));
+  ERMOD_CUDA(dalloc(&b.u_radius, 2 * B));
   ERMOD_CUDA(dalloc(&b.engnmfc, 2 * B));
   ERMOD_CUDA(dalloc(&e.d_u0, 2 * B));
   ERMOD_CUDA(dalloc(&e.d_self_bin, 2 * B));
   if (e.mixed) {
-    ERMOD_CUDA(dalloc(&b.u_bvec, (size_t)B * S * 3 * e.Kmax()));
+    ERMOD_CUDA(dalloc(&b.u_bvec, (size_t)2 * B * S * 3 * e.Kmax()));
     ERMOD_CUDA(dalloc(&e.d_site_e, (size_t)e.nsite_phys * B));
     ERMOD_CUDA(dalloc(&b.spec, nc * B));
     const int h = e.P_order - 1;
@@ -419,13 +412,15 @@ int ermod_create(const ermod_params* p, int device, ermod_ctx** out) {
     return fail_cuda(err, "cudaStreamCreate");
   }
   e.own_stream = true;
-  if ((err = cudaStreamCreateWithFlags(&e.aux, cudaStreamNonBlocking)) != cudaSuccess) {
+  if ((err = cudaStreamCreateWithFlags(&e.aux, cudaStreamNonBlocking)) != cudaSuccess ||
+      (err = cudaStreamCreateWithFlags(&e.prep, cudaStreamNonBlocking)) != cudaSuccess) {
     ermod_destroy(c);
     return fail_cuda(err, "cudaStreamCreate");
   }
   for (int s = 0; s < 2; ++s) {
     cudaEventCreateWithFlags(&e.ev_done[s], cudaEventDisableTiming);
     cudaEventCreateWithFlags(&e.ev_acc[s], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&e.ev_prep[s], cudaEventDisableTiming);
   }
   cudaEventCreateWithFlags(&e.ev_flush, cudaEventDisableTiming);
   if ((err = dalloc(&e.d_status, 1)) != cudaSuccess || (err = cudaMallocHost(&e.h_status, sizeof(DevStatus))) != cudaSuccess) {
@@ -486,12 +481,15 @@ int ermod_destroy(ermod_ctx* c) {
   for (auto ev : e.ev_pool) cudaEventDestroy(ev);
   if (e.own_stream && e.stream) cudaStreamDestroy(e.stream);
   if (e.aux) cudaStreamSynchronize(e.aux);
+  if (e.prep) cudaStreamSynchronize(e.prep);
   for (int s = 0; s < 2; ++s) {
     if (e.ev_done[s]) cudaEventDestroy(e.ev_done[s]);
     if (e.ev_acc[s]) cudaEventDestroy(e.ev_acc[s]);
+    if (e.ev_prep[s]) cudaEventDestroy(e.ev_prep[s]);
   }
   if (e.ev_flush) cudaEventDestroy(e.ev_flush);
   if (e.aux) cudaStreamDestroy(e.aux);
+  if (e.prep) cudaStreamDestroy(e.prep);
   delete c;
   return ERMOD_OK;
 }
@@ -809,30 +807,40 @@ int ermod_frame_device(ermod_ctx* c, const double* sitepos_d, const double* cell
 }
 
 // the placement loop on device-resident inputs.  Batch i runs its kernels on the main
-// stream with the buffers of slot i%2; its ordered accumulation (and, every ring_cap
-// placements, the ecorr flush) runs on the aux stream, overlapping batch i+1.
+// stream with the buffers of slot i%2.  Its solute preparation runs on the prep stream
+// during batch i-1; its ordered accumulation (and, every ring_cap placements, the ecorr
+// flush) runs on the aux stream during batch i+1.
 static int run_placements(Engine& e, int nplace, const int* d_tag, const double* d_sol, const double* d_sws,
                           double* d_uv, double* d_fl, int ns_solute) {
   int st = ensure_batch(e);
   if (st) return st;
   const int B = e.Bmax;
+  const int S = kMaxSoluteSites;
+  const int nbatch = (nplace + B - 1) / B;
   const size_t parts = e.mixed ? (size_t)spectrum_partials(e) : (size_t)influence64_blocks();
-  // the aux stream starts after everything already queued on the main stream
+  // the aux and prep streams start after everything already queued on the main stream
   ERMOD_CUDA(cudaEventRecord(e.ev_done[0], e.stream));
   ERMOD_CUDA(cudaStreamWaitEvent(e.aux, e.ev_done[0], 0));
-  int ibatch = 0;
-  for (int b0 = 0; b0 < nplace; b0 += B, ++ibatch) {
-    const int nb = std::min(B, nplace - b0);
-    const int slot = ibatch & 1;
+  ERMOD_CUDA(cudaStreamWaitEvent(e.prep, e.ev_done[0], 0));
+  auto batch_args = [&](int ib) {
+    const int b0 = ib * B, slot = ib & 1;
     BatchArgs a = e.buf;
-    a.nb = nb;
+    a.nb = std::min(B, nplace - b0);
     a.b0 = b0;
     a.G = e.G;
     a.tagslt = d_tag + b0;
     a.stat_weight_solute = d_sws ? d_sws + b0 : nullptr;
     a.uvengy_out = d_uv;
     a.flceng_out = d_fl;
-    a.hist = e.d_ring_hist + (size_t)e.ring_fill * e.ermax;
+    a.u_nsite = e.buf.u_nsite + (size_t)slot * B;
+    a.u_x = e.buf.u_x + (size_t)slot * B * S * 3;
+    a.u_pos = e.buf.u_pos + (size_t)slot * B * S;
+    a.u_q = e.buf.u_q + (size_t)slot * B * S;
+    a.u_qf = e.buf.u_qf + (size_t)slot * B * S;
+    a.u_grid = e.buf.u_grid + (size_t)slot * B * S;
+    a.u_w = e.buf.u_w + (size_t)slot * B * S * 3 * kMaxSplineOrder;
+    if (e.buf.u_bvec) a.u_bvec = e.buf.u_bvec + (size_t)slot * B * S * 3 * e.Kmax();
+    a.u_radius = e.buf.u_radius + (size_t)slot * B;
     a.u_qmol = e.buf.u_qmol + (size_t)slot * B;
     a.u_usreal = e.buf.u_usreal + (size_t)slot * B;
     a.engnmfc = e.buf.engnmfc + (size_t)slot * B;
@@ -840,12 +848,29 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
     a.part = e.buf.part + (size_t)slot * B * e.ntile * e.numslv * 3;
     a.u0 = e.d_u0 + (size_t)slot * B;
     a.self_bin = e.d_self_bin + (size_t)slot * B;
+    return a;
+  };
+  auto issue_prep = [&](int ib) -> int {
+    const int slot = ib & 1;
+    const BatchArgs a = batch_args(ib);
+    if (ib >= 2) ERMOD_CUDA(cudaStreamWaitEvent(e.prep, e.ev_acc[slot], 0));  // slot free again
+    const double* sol = d_sol ? d_sol + (size_t)a.b0 * ns_solute * 3 : nullptr;
+    e.phase_begin_on(PH_PREP, e.prep);
+    ERMOD_CUDA(launch_place_prep(e, a, sol, e.P.slttype == 2 ? 2 : 1, e.prep));
+    e.phase_end_on(e.prep);
+    ERMOD_CUDA(cudaEventRecord(e.ev_prep[slot], e.prep));
+    return ERMOD_OK;
+  };
+  if (nbatch > 0 && (st = issue_prep(0)) != ERMOD_OK) return st;
+  for (int ibatch = 0; ibatch < nbatch; ++ibatch) {
+    const int slot = ibatch & 1;
+    if (ibatch + 1 < nbatch && (st = issue_prep(ibatch + 1)) != ERMOD_OK) return st;
+    BatchArgs a = batch_args(ibatch);
+    const int nb = a.nb;
+    a.hist = e.d_ring_hist + (size_t)e.ring_fill * e.ermax;
     if (ibatch >= 2) ERMOD_CUDA(cudaStreamWaitEvent(e.stream, e.ev_acc[slot], 0));  // slot free again
-    const double* sol = d_sol ? d_sol + (size_t)b0 * ns_solute * 3 : nullptr;
-    e.phase_begin(PH_PREP);
+    ERMOD_CUDA(cudaStreamWaitEvent(e.stream, e.ev_prep[slot], 0));
     ERMOD_CUDA(cudaMemsetAsync(a.hist, 0, sizeof(int) * (size_t)nb * e.ermax, e.stream));
-    ERMOD_CUDA(launch_place_prep(e, a, sol, e.P.slttype == 2 ? 2 : 1));
-    e.phase_end();
     if (e.mixed) {
       e.phase_begin(PH_SPECTRUM);
       ERMOD_CUDA(launch_pme_mixed(e, a));  // spectrum + k3 transform, then (FFT phase) k2/k1

@@ -31,8 +31,8 @@ struct Engine {
   std::vector<cudaEvent_t> ev_pool;
   struct Pending { cudaEvent_t a, b; int phase; };
   std::vector<Pending> pending;
-  int cur_phase = -1;
-  cudaEvent_t cur_ev = nullptr;
+  int cur_phase[3] = {-1, -1, -1};  // per stream: main, aux, prep
+  cudaEvent_t cur_ev[3] = {nullptr, nullptr, nullptr};
 
   // ---- topology ----------------------------------------------------------------
   int nummol = 0, numatm = 0, ljtype_max = 0, slvmax = 0, nsite_phys = 0, max_mol_sites = 0;
@@ -155,8 +155,11 @@ struct Engine {
   size_t grid_cplx() const { return (size_t)H() * geom.K[1] * geom.K[2]; }
   int Kmax() const { return std::max(geom.K[0], std::max(geom.K[1], geom.K[2])); }
 
-  // second stream: the ordered accumulation of batch i overlaps batch i+1's kernels
+  // second stream: the ordered accumulation of batch i overlaps batch i+1's kernels;
+  // third stream: the solute preparation of batch i+1 overlaps batch i's kernels
   cudaStream_t aux = nullptr;
+  cudaStream_t prep = nullptr;
+  cudaEvent_t ev_prep[2] = {nullptr, nullptr};  // preparation of the slot finished
   cudaEvent_t ev_done[2] = {nullptr, nullptr};  // batch kernels finished (slot)
   cudaEvent_t ev_acc[2] = {nullptr, nullptr};   // accumulation of the slot finished
   cudaEvent_t ev_flush = nullptr;               // ecorr flush finished
@@ -165,8 +168,7 @@ struct Engine {
   void phase_end() { phase_end_on(stream); }
   void phase_begin_on(int ph, cudaStream_t s);
   void phase_end_on(cudaStream_t s);
-  int cur_phase_aux = -1;
-  cudaEvent_t cur_ev_aux = nullptr;
+  int stream_index(cudaStream_t s) const { return s == aux ? 1 : (s == prep ? 2 : 0); }
   void count_launch(int n = 1) { launches += n; }
 };
 

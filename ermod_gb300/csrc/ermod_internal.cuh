@@ -128,7 +128,8 @@ cudaError_t launch_frame_sort(Engine& e);
 cudaError_t launch_frame_sites(Engine& e);
 cudaError_t launch_greenfunc(Engine& e);
 // placement preparation and PME
-cudaError_t launch_place_prep(Engine& e, const BatchArgs& a, const double* sol_xyz, int self_first_only);
+cudaError_t launch_place_prep(Engine& e, const BatchArgs& a, const double* sol_xyz, int self_first_only,
+                              cudaStream_t s);
 cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a);
 bool pme_fits(int K1, int K2, int K3);
 cudaError_t launch_spread64(Engine& e, const BatchArgs& a);

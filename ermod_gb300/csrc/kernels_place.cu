@@ -312,7 +312,7 @@ Coef make_coef(int order, double screen) {
 
 int spectrum_partials(const Engine& e) { return e.geom.K[2]; }
 
-cudaError_t launch_place_prep(Engine& e, const BatchArgs& a, const double* sol_xyz, int self_mode) {
+cudaError_t launch_place_prep(Engine& e, const BatchArgs& a, const double* sol_xyz, int self_mode, cudaStream_t s) {
   PrepArgs A{};
   A.a = a;
   A.solxyz = sol_xyz;
@@ -332,7 +332,7 @@ cudaError_t launch_place_prep(Engine& e, const BatchArgs& a, const double* sol_x
   for (int i = 0; i < 3; ++i) A.mK[i] = magic((unsigned)e.geom.K[i]);
   A.mKmax = magic((unsigned)e.Kmax());
   A.m3Kmax = magic(3u * (unsigned)e.Kmax());
-  place_prep_kernel<<<a.nb, 256, 0, e.stream>>>(A);
+  place_prep_kernel<<<a.nb, 256, 0, s>>>(A);
   e.count_launch();
   return cudaGetLastError();
 }
