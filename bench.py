@@ -263,8 +263,12 @@ def run_ours(args):
     bytes_per_launch = per_pl[dom] * args.batch
     peak, peak_kind = load_peaks()
     achieved = bytes_per_launch / (avg_launch_ms / 1000.0) / 1e9
+    traffic = None
+    if args.workload == "refs_large":
+        traffic = roofline.MEASURED_TRAFFIC_REFS_LARGE[dom] * args.batch
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+            "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+            "traffic_note": "ncu DRAM read+write per launch (one capture, scaled to the launch's placements)",
             "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_ms,
             "phase_ms_per_step": {k: v / args.steps for k, v in phases.items()}}
     clocks = clk.summary()

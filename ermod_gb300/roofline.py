@@ -16,6 +16,16 @@ transform (8 K^3 written by the spread, read by D2Z; 16 H K^2 written by D2Z).
 """
 from __future__ import annotations
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per placement of each mixed
+# kernel, from one ncu --set full capture of a 32-placement launch of refs_large
+# (33,000 waters, PME 96^3, order 4, 12-site solute).  Traffic grows in proportion to
+# the placements of a launch, so a launch of B placements moves B times these bytes.
+MEASURED_TRAFFIC_REFS_LARGE = {
+    "spectrum": (2.67e6 + 55.45e6) / 32,  # pme_a: T1 stays partly in L2 for pme_b
+    "fft_c2r": (123.20e6 + 71.54e6) / 32,  # pme_b
+    "gather": (129.24e6 + 7.59e6) / 32,  # gather_tma
+}
+
 
 def grid_terms(K1: int, K2: int, K3: int):
     H = K1 // 2 + 1
