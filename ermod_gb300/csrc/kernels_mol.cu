@@ -727,15 +727,48 @@ __global__ void __launch_bounds__(kGatherThreads) gather_tma_kernel(
   const int h = P - 1;
   const int ox = bx * 8 - h, oy = by * 8 - h, oz = bz * 8 - h;
   const int s_begin = brick_start[brick], s_end = brick_start[brick + 1];
-  // this thread's first site, set up once for every group
-  const int i0 = s_begin + threadIdx.x;
-  float w1[P], w2[P], w3[P];
-  int base = 0, site0 = -1;
-  float q = 0.f;
-  if (i0 < s_end) {
-    site0 = brick_site[i0];
-    site_setup<P>(site0, site_rec, site_grid, K1, K2, K3, ox, oy, oz, BX, w1, w2, w3, base, q);
+  const int n = s_end - s_begin;
+  // Site-to-thread map.  A 16-byte shared load is served 8 lanes at a time, and the
+  // 8 lanes are conflict free when their halo indices differ mod 8; every stencil
+  // point shifts all lanes' indices by the same offset.  So the brick's sites are
+  // bucketed by (stencil base index mod 8), and lane t takes entry t / 8 of bucket t % 8.
+  // Bricks with more sites than threads keep the plain order.
+  __shared__ int sbucket[8][kGatherThreads / 8];
+  __shared__ int scnt[8];
+  __shared__ int sovf[kGatherThreads];
+  __shared__ int novf;
+  const bool bucketed = n <= (int)blockDim.x;
+  int site0 = -1;
+  if (bucketed) {
+    if (threadIdx.x < 8) scnt[threadIdx.x] = 0;
+    if (threadIdx.x == 0) novf = 0;
+    __syncthreads();
+    if ((int)threadIdx.x < n) {
+      const int site = brick_site[s_begin + threadIdx.x];
+      const int gp = site_grid[site];
+      int g1 = gp & 1023, g2 = (gp >> 10) & 1023, g3 = (gp >> 20) & 1023;
+      if (g1 >= K1) g1 -= K1;
+      if (g2 >= K2) g2 -= K2;
+      if (g3 >= K3) g3 -= K3;
+      const int r = ((((g3 - oz) * BY + (g2 - oy)) * BX + (g1 - ox)) & 7);
+      const int pos = atomicAdd(&scnt[r], 1);
+      if (pos < (int)(kGatherThreads / 8))
+        sbucket[r][pos] = site;
+      else
+        sovf[atomicAdd(&novf, 1)] = site;
+    }
+    __syncthreads();
+    const int r = threadIdx.x & 7, k = threadIdx.x >> 3;
+    if (k < scnt[r] && k < (int)(kGatherThreads / 8)) site0 = sbucket[r][k];
+  } else if ((int)threadIdx.x < n) {
+    site0 = brick_site[s_begin + threadIdx.x];
   }
+  // this thread's site, set up once for every group
+  float w1[P], w2[P], w3[P];
+  int base = 0;
+  float q = 0.f;
+  if (site0 >= 0) site_setup<P>(site0, site_rec, site_grid, K1, K2, K3, ox, oy, oz, BX, w1, w2, w3, base, q);
+  const int n_extra = bucketed ? novf : max(0, n - (int)blockDim.x);
   for (int g = g_begin; g < g_end; ++g) {
     const int slot = (g - g_begin) & 1;
     const uint32_t parity = (uint32_t)(((g - g_begin) >> 1) & 1);
@@ -769,8 +802,8 @@ __global__ void __launch_bounds__(kGatherThreads) gather_tma_kernel(
       *reinterpret_cast<float4*>(site_e + (size_t)site0 * ldb + b0) =
           make_float4(q * acc.x, q * acc.y, q * acc.z, q * acc.w);
     }
-    for (int i = i0 + blockDim.x; i < s_end; i += blockDim.x) {  // bricks with more sites than threads
-      const int site = brick_site[i];
+    for (int i = threadIdx.x; i < n_extra; i += blockDim.x) {  // bucket overflow / crowded bricks
+      const int site = bucketed ? sovf[i] : brick_site[s_begin + blockDim.x + i];
       float v1[P], v2[P], v3[P];
       int bs;
       float qs;
