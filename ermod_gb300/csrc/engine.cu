@@ -216,7 +216,7 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-static int make_phi_tmap(Engine& e, float* phi) {
+static int make_phi_tmap(Engine& e, float* phi, CUtensorMap* map) {
   void* fn = nullptr;
   cudaDriverEntryPointQueryResult q;
   cudaError_t err = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
@@ -229,7 +229,7 @@ static int make_phi_tmap(Engine& e, float* phi) {
   const cuuint64_t strides[3] = {XP * 4, XP * YP * 4, XP * YP * ZP * 4};
   const cuuint32_t box[4] = {(cuuint32_t)e.gbox[0], (cuuint32_t)e.gbox[1], (cuuint32_t)e.gbox[2], 4};
   const cuuint32_t estr[4] = {1, 1, 1, 1};
-  const CUresult r = ((EncodeTiledFn)fn)(&e.phi_tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, phi, dims, strides, box, estr,
+  const CUresult r = ((EncodeTiledFn)fn)(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, phi, dims, strides, box, estr,
                                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
@@ -264,8 +264,9 @@ static int ensure_batch(Engine& e) {
   ERMOD_CUDA(dalloc(&e.d_self_bin, 2 * B));
   if (e.mixed) {
     ERMOD_CUDA(dalloc(&b.u_bvec, (size_t)2 * B * S * 3 * e.Kmax()));
-    ERMOD_CUDA(dalloc(&e.d_site_e, (size_t)e.nsite_phys * B));
-    ERMOD_CUDA(dalloc(&b.spec, nc * B));
+    // PME intermediate, padded potential grids and site terms: one set per batch slot
+    ERMOD_CUDA(dalloc(&e.d_site_e, (size_t)2 * e.nsite_phys * B));
+    ERMOD_CUDA(dalloc(&b.spec, 2 * nc * B));
     const int h = e.P_order - 1;
     e.phi_dims[0] = ((e.geom.K[0] + h + 3) / 4) * 4;
     e.phi_dims[1] = e.geom.K[1] + h;
@@ -274,10 +275,12 @@ static int ensure_batch(Engine& e) {
     e.gbox[1] = 8 + h;
     e.gbox[2] = 8 + h;
     const size_t np = (size_t)e.phi_dims[0] * e.phi_dims[1] * e.phi_dims[2];
-    ERMOD_CUDA(dalloc(&b.phi, np * B));
-    ERMOD_CUDA(cudaMemset(b.phi, 0, sizeof(float) * np * B));
-    int st = make_phi_tmap(e, b.phi);
-    if (st) return st;
+    ERMOD_CUDA(dalloc(&b.phi, 2 * np * B));
+    ERMOD_CUDA(cudaMemset(b.phi, 0, sizeof(float) * 2 * np * B));
+    for (int s = 0; s < 2; ++s) {
+      const int st = make_phi_tmap(e, b.phi + (size_t)s * np * B, &e.phi_tmap[s]);
+      if (st) return st;
+    }
     ERMOD_CUDA(dalloc(&b.self_part, (size_t)2 * B * spectrum_partials(e)));
   } else {
     ERMOD_CUDA(dalloc(&b.spec64, nc * B));
@@ -413,7 +416,9 @@ int ermod_create(const ermod_params* p, int device, ermod_ctx** out) {
   }
   e.own_stream = true;
   if ((err = cudaStreamCreateWithFlags(&e.aux, cudaStreamNonBlocking)) != cudaSuccess ||
-      (err = cudaStreamCreateWithFlags(&e.prep, cudaStreamNonBlocking)) != cudaSuccess) {
+      (err = cudaStreamCreateWithFlags(&e.prep, cudaStreamNonBlocking)) != cudaSuccess ||
+      (err = cudaStreamCreateWithFlags(&e.bs[0], cudaStreamNonBlocking)) != cudaSuccess ||
+      (err = cudaStreamCreateWithFlags(&e.bs[1], cudaStreamNonBlocking)) != cudaSuccess) {
     ermod_destroy(c);
     return fail_cuda(err, "cudaStreamCreate");
   }
@@ -423,6 +428,7 @@ int ermod_create(const ermod_params* p, int device, ermod_ctx** out) {
     cudaEventCreateWithFlags(&e.ev_prep[s], cudaEventDisableTiming);
   }
   cudaEventCreateWithFlags(&e.ev_flush, cudaEventDisableTiming);
+  for (int s = 0; s < 4; ++s) cudaEventCreateWithFlags(&e.ev_join[s], cudaEventDisableTiming);
   if ((err = dalloc(&e.d_status, 1)) != cudaSuccess || (err = cudaMallocHost(&e.h_status, sizeof(DevStatus))) != cudaSuccess) {
     ermod_destroy(c);
     return fail_cuda(err, "status allocation");
@@ -482,6 +488,8 @@ int ermod_destroy(ermod_ctx* c) {
   if (e.own_stream && e.stream) cudaStreamDestroy(e.stream);
   if (e.aux) cudaStreamSynchronize(e.aux);
   if (e.prep) cudaStreamSynchronize(e.prep);
+  for (int s = 0; s < 2; ++s)
+    if (e.bs[s]) cudaStreamSynchronize(e.bs[s]);
   for (int s = 0; s < 2; ++s) {
     if (e.ev_done[s]) cudaEventDestroy(e.ev_done[s]);
     if (e.ev_acc[s]) cudaEventDestroy(e.ev_acc[s]);
@@ -490,6 +498,10 @@ int ermod_destroy(ermod_ctx* c) {
   if (e.ev_flush) cudaEventDestroy(e.ev_flush);
   if (e.aux) cudaStreamDestroy(e.aux);
   if (e.prep) cudaStreamDestroy(e.prep);
+  for (int s = 0; s < 2; ++s)
+    if (e.bs[s]) cudaStreamDestroy(e.bs[s]);
+  for (int s = 0; s < 4; ++s)
+    if (e.ev_join[s]) cudaEventDestroy(e.ev_join[s]);
   delete c;
   return ERMOD_OK;
 }
@@ -818,10 +830,17 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
   const int S = kMaxSoluteSites;
   const int nbatch = (nplace + B - 1) / B;
   const size_t parts = e.mixed ? (size_t)spectrum_partials(e) : (size_t)influence64_blocks();
-  // the aux and prep streams start after everything already queued on the main stream
+  // batches run on two alternating streams (mixed path) or on the caller's stream (FP64
+  // path, whose cuFFT plans are bound to it); every stream starts after what is
+  // already queued on the caller's stream
+  const bool dual = e.mixed;
   ERMOD_CUDA(cudaEventRecord(e.ev_done[0], e.stream));
   ERMOD_CUDA(cudaStreamWaitEvent(e.aux, e.ev_done[0], 0));
   ERMOD_CUDA(cudaStreamWaitEvent(e.prep, e.ev_done[0], 0));
+  if (dual) {
+    ERMOD_CUDA(cudaStreamWaitEvent(e.bs[0], e.ev_done[0], 0));
+    ERMOD_CUDA(cudaStreamWaitEvent(e.bs[1], e.ev_done[0], 0));
+  }
   auto batch_args = [&](int ib) {
     const int b0 = ib * B, slot = ib & 1;
     BatchArgs a = e.buf;
@@ -848,8 +867,17 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
     a.part = e.buf.part + (size_t)slot * B * e.ntile * e.numslv * 3;
     a.u0 = e.d_u0 + (size_t)slot * B;
     a.self_bin = e.d_self_bin + (size_t)slot * B;
+    a.slot = slot;
+    a.stream = dual ? e.bs[slot] : e.stream;
+    if (e.mixed) {
+      const size_t np = (size_t)e.phi_dims[0] * e.phi_dims[1] * e.phi_dims[2];
+      a.spec = e.buf.spec + (size_t)slot * e.grid_cplx() * B;
+      a.phi = e.buf.phi + (size_t)slot * np * B;
+      a.site_e = e.d_site_e + (size_t)slot * e.nsite_phys * B;
+    }
     return a;
   };
+  bool flush_pending = false;  // the next batch rewrites the ring from its start
   auto issue_prep = [&](int ib) -> int {
     const int slot = ib & 1;
     const BatchArgs a = batch_args(ib);
@@ -868,29 +896,34 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
     BatchArgs a = batch_args(ibatch);
     const int nb = a.nb;
     a.hist = e.d_ring_hist + (size_t)e.ring_fill * e.ermax;
-    if (ibatch >= 2) ERMOD_CUDA(cudaStreamWaitEvent(e.stream, e.ev_acc[slot], 0));  // slot free again
-    ERMOD_CUDA(cudaStreamWaitEvent(e.stream, e.ev_prep[slot], 0));
-    ERMOD_CUDA(cudaMemsetAsync(a.hist, 0, sizeof(int) * (size_t)nb * e.ermax, e.stream));
+    cudaStream_t bst = a.stream;
+    if (ibatch >= 2) ERMOD_CUDA(cudaStreamWaitEvent(bst, e.ev_acc[slot], 0));  // slot free again
+    ERMOD_CUDA(cudaStreamWaitEvent(bst, e.ev_prep[slot], 0));
+    if (flush_pending) {
+      ERMOD_CUDA(cudaStreamWaitEvent(bst, e.ev_flush, 0));
+      flush_pending = false;
+    }
+    ERMOD_CUDA(cudaMemsetAsync(a.hist, 0, sizeof(int) * (size_t)nb * e.ermax, bst));
     if (e.mixed) {
-      e.phase_begin(PH_SPECTRUM);
+      e.phase_begin_on(PH_SPECTRUM, bst);
       ERMOD_CUDA(launch_pme_mixed(e, a));  // spectrum + k3 transform, then (FFT phase) k2/k1
-      e.phase_end();
+      e.phase_end_on(bst);
     } else {
-      e.phase_begin(PH_SPECTRUM);
+      e.phase_begin_on(PH_SPECTRUM, bst);
       ERMOD_CUDA(launch_spread64(e, a));
       cufftResult r = cufftExecD2Z(e.plan_d2z, a.phi64, (cufftDoubleComplex*)a.spec64);
       if (r != CUFFT_SUCCESS) return fail_fft(r, "cufftExecD2Z");
       ERMOD_CUDA(launch_influence64(e, a));
-      e.phase_end();
-      e.phase_begin(PH_FFT);
+      e.phase_end_on(bst);
+      e.phase_begin_on(PH_FFT, bst);
       r = cufftExecZ2D(e.plan_z2d, (cufftDoubleComplex*)a.spec64, a.phi64);
       if (r != CUFFT_SUCCESS) return fail_fft(r, "cufftExecZ2D");
-      e.phase_end();
+      e.phase_end_on(bst);
     }
-    e.phase_begin(e.mixed ? PH_GATHER : PH_MOL);
+    e.phase_begin_on(e.mixed ? PH_GATHER : PH_MOL, bst);
     ERMOD_CUDA(launch_mol_energy(e, a));  // mixed: gather, then (mol_energy phase) finish
-    e.phase_end();
-    ERMOD_CUDA(cudaEventRecord(e.ev_done[slot], e.stream));
+    e.phase_end_on(bst);
+    ERMOD_CUDA(cudaEventRecord(e.ev_done[slot], bst));
     // ---- ordered accumulation on the aux stream ----
     ERMOD_CUDA(cudaStreamWaitEvent(e.aux, e.ev_done[slot], 0));
     e.phase_begin_on(PH_ACCUM, e.aux);
@@ -912,7 +945,7 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
     ERMOD_CUDA(cudaEventRecord(e.ev_acc[slot], e.aux));
     if (flushed) {  // the ring is rewritten from its start by the next batches
       ERMOD_CUDA(cudaEventRecord(e.ev_flush, e.aux));
-      ERMOD_CUDA(cudaStreamWaitEvent(e.stream, e.ev_flush, 0));
+      flush_pending = true;
     }
   }
   if (e.P.corrcal && e.ring_fill > 0) {
@@ -922,9 +955,12 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
     e.ring_fill = 0;
   }
   e.ring_fill = 0;
-  // join the aux stream back into the main stream, then snapshot the status
-  ERMOD_CUDA(cudaEventRecord(e.ev_flush, e.aux));
-  ERMOD_CUDA(cudaStreamWaitEvent(e.stream, e.ev_flush, 0));
+  // join every stream back into the caller's stream, then snapshot the status
+  cudaStream_t others[4] = {e.aux, e.prep, e.bs[0], e.bs[1]};
+  for (int k = 0; k < (dual ? 4 : 2); ++k) {
+    ERMOD_CUDA(cudaEventRecord(e.ev_join[k], others[k]));
+    ERMOD_CUDA(cudaStreamWaitEvent(e.stream, e.ev_join[k], 0));
+  }
   ERMOD_CUDA(cudaMemcpyAsync(e.h_status, e.d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, e.stream));
   return ERMOD_OK;
 }

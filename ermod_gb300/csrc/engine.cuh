@@ -31,8 +31,8 @@ struct Engine {
   std::vector<cudaEvent_t> ev_pool;
   struct Pending { cudaEvent_t a, b; int phase; };
   std::vector<Pending> pending;
-  int cur_phase[3] = {-1, -1, -1};  // per stream: main, aux, prep
-  cudaEvent_t cur_ev[3] = {nullptr, nullptr, nullptr};
+  int cur_phase[5] = {-1, -1, -1, -1, -1};  // per stream: caller's, aux, prep, batch 0/1
+  cudaEvent_t cur_ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 
   // ---- topology ----------------------------------------------------------------
   int nummol = 0, numatm = 0, ljtype_max = 0, slvmax = 0, nsite_phys = 0, max_mol_sites = 0;
@@ -129,7 +129,7 @@ struct Engine {
   int* d_ring_nnz = nullptr;      // [ring_cap] occupied bins per entry
   int* d_ring_valid = nullptr;    // [ring_cap] entry accumulated (no error in its batch)
   double* d_u0 = nullptr;         // [2][Bmax] solute self energies (two batch slots)
-  float* d_site_e = nullptr;      // [nsite_phys][Bmax] reciprocal site terms (mixed path)
+  float* d_site_e = nullptr;      // [2][nsite_phys][Bmax] reciprocal site terms (mixed path)
   int* d_self_bin = nullptr;      // [2][Bmax]
 
   // ---- status ----------------------------------------------------------------------
@@ -142,7 +142,7 @@ struct Engine {
   // ---- mixed path potential grids: padded periodic layout + TMA descriptor ----------
   int phi_dims[3] = {0, 0, 0};   // XP (multiple of 4), YP, ZP
   int gbox[3] = {0, 0, 0};       // gather box: x (multiple of 4), y, z
-  alignas(64) CUtensorMap phi_tmap;
+  alignas(64) CUtensorMap phi_tmap[2];  // per slot
   bool tmap_ready = false;
 
   // ---- cuFFT -------------------------------------------------------------------------
@@ -160,6 +160,10 @@ struct Engine {
   cudaStream_t aux = nullptr;
   cudaStream_t prep = nullptr;
   cudaEvent_t ev_prep[2] = {nullptr, nullptr};  // preparation of the slot finished
+  // mixed path: batches alternate between two streams (their PME grids and site terms
+  // are double-buffered), so one batch's kernels fill the other's partial waves
+  cudaStream_t bs[2] = {nullptr, nullptr};
+  cudaEvent_t ev_join[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t ev_done[2] = {nullptr, nullptr};  // batch kernels finished (slot)
   cudaEvent_t ev_acc[2] = {nullptr, nullptr};   // accumulation of the slot finished
   cudaEvent_t ev_flush = nullptr;               // ecorr flush finished
@@ -168,7 +172,9 @@ struct Engine {
   void phase_end() { phase_end_on(stream); }
   void phase_begin_on(int ph, cudaStream_t s);
   void phase_end_on(cudaStream_t s);
-  int stream_index(cudaStream_t s) const { return s == aux ? 1 : (s == prep ? 2 : 0); }
+  int stream_index(cudaStream_t s) const {
+    return s == aux ? 1 : (s == prep ? 2 : (s == bs[0] && s ? 3 : (s == bs[1] && s ? 4 : 0)));
+  }
   void count_launch(int n = 1) { launches += n; }
 };
 

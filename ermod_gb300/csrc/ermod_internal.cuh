@@ -89,6 +89,9 @@ struct BatchArgs {
   int b0;             // index of the batch's first placement within the call
   int G;              // placements per mol_energy block
   int n_u_max;        // max solute sites in the batch
+  int slot;           // batch parity: selects the double-buffered PME grids
+  cudaStream_t stream;  // stream of the batch's PME, gather and finish kernels
+  float* site_e;      // [nsite_phys][Bmax] reciprocal site terms of this slot (mixed)
   const int* tagslt;  // [nb] 1-based
   const double* stat_weight_solute;  // [nb] or null
   // solute site data per placement, [nb][kMaxSoluteSites]

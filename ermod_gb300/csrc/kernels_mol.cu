@@ -1003,13 +1003,13 @@ template <bool MIXED>
 cudaError_t launch_p(Engine& e, const MolArgs& A, dim3 grid, size_t smem) {
   switch (e.P_order) {
     case 4:
-      mol_energy_kernel<MIXED, 4><<<grid, 256, smem, e.stream>>>(A);
+      mol_energy_kernel<MIXED, 4><<<grid, 256, smem, A.a.stream>>>(A);
       break;
     case 6:
-      mol_energy_kernel<MIXED, 6><<<grid, 256, smem, e.stream>>>(A);
+      mol_energy_kernel<MIXED, 6><<<grid, 256, smem, A.a.stream>>>(A);
       break;
     case 8:
-      mol_energy_kernel<MIXED, 8><<<grid, 256, smem, e.stream>>>(A);
+      mol_energy_kernel<MIXED, 8><<<grid, 256, smem, A.a.stream>>>(A);
       break;
     default:
       return cudaErrorInvalidValue;
@@ -1100,9 +1100,9 @@ cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
       if (err != cudaSuccess) return err;                                                                       \
       attr = sh;                                                                                                \
     }                                                                                                           \
-    gather_tma_kernel<PP><<<g1, kGatherThreads, sh, e.stream>>>(                                                \
-        e.phi_tmap, a.nb, gpc, e.d_site_rec, e.d_site_grid, e.d_brick_site, e.d_brick_start, K1, K2, K3,        \
-        e.nbrick[0], e.nbrick[1], e.gbox[0], e.Bmax, e.d_site_e, e.d_status);                                   \
+    gather_tma_kernel<PP><<<g1, kGatherThreads, sh, a.stream>>>(                                                \
+        e.phi_tmap[a.slot], a.nb, gpc, e.d_site_rec, e.d_site_grid, e.d_brick_site, e.d_brick_start, K1, K2, K3,        \
+        e.nbrick[0], e.nbrick[1], e.gbox[0], e.Bmax, a.site_e, e.d_status);                                   \
   }
     ERMOD_GATHER(4)
     ERMOD_GATHER(6)
@@ -1111,8 +1111,8 @@ cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
     e.count_launch();
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
   }
-  e.phase_end();
-  e.phase_begin(PH_MOL);
+  e.phase_end_on(a.stream);
+  e.phase_begin_on(PH_MOL, a.stream);
   // step 2: per-molecule totals and binning (histograms + edge keys in shared memory)
   const size_t smem_f = sizeof(int) * (((size_t)a.G * e.ermax + 1) & ~(size_t)1) + sizeof(long long) * e.ermax;
   dim3 g2((a.nb + a.G - 1) / a.G, e.ntile);
@@ -1124,7 +1124,7 @@ cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
       if (err != cudaSuccess) return err;                                                                  \
       attr = smem_f;                                                                                       \
     }                                                                                                      \
-    mol_finish_kernel<GG><<<g2, 256, smem_f, e.stream>>>(A, e.d_site_e);                                   \
+    mol_finish_kernel<GG><<<g2, 256, smem_f, a.stream>>>(A, a.site_e);                                   \
   }
   ERMOD_FINISH(4)
   ERMOD_FINISH(8)

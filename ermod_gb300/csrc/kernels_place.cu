@@ -348,9 +348,9 @@ cudaError_t launch_spread64(Engine& e, const BatchArgs& a) {
   A.K2 = e.geom.K[1];
   A.K3 = e.geom.K[2];
   A.P = e.P_order;
-  cudaError_t err = cudaMemsetAsync(a.phi64, 0, sizeof(double) * e.grid_real() * a.nb, e.stream);
+  cudaError_t err = cudaMemsetAsync(a.phi64, 0, sizeof(double) * e.grid_real() * a.nb, a.stream);
   if (err != cudaSuccess) return err;
-  spread64_kernel<<<a.nb, 128, 0, e.stream>>>(A);
+  spread64_kernel<<<a.nb, 128, 0, a.stream>>>(A);
   e.count_launch();
   return cudaGetLastError();
 }
@@ -369,7 +369,7 @@ cudaError_t launch_influence64(Engine& e, const BatchArgs& a) {
   A.n = e.grid_cplx();
   A.nblk = influence64_blocks();
   dim3 grid(A.nblk, a.nb);
-  influence64_kernel<<<grid, 256, 0, e.stream>>>(A);
+  influence64_kernel<<<grid, 256, 0, a.stream>>>(A);
   e.count_launch();
   return cudaGetLastError();
 }
