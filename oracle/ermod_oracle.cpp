@@ -1354,6 +1354,164 @@ int orc_recip_parts(const orc_ctx* c, int tagslt, const double* solute_sitepos, 
   return ORC_OK;
 }
 
+// Per-molecule derivatives of uvengy(k) (get_uv_energy, engproc.F90:662-756) with
+// respect to the solute's per-site parameters, FP64.  For solute site s and solvent
+// molecule k (tagpt order), out[k * 3 ns + 3 s + {0, 1, 2}] holds du_k / d{q_s, eps_s,
+// sigma_s}: q_s the charge as the topology holds it (e x 18.22261721), eps_s and sigma_s
+// the site's LJ parameters under ljene = sqrt(eps_s eps_t) and ljlensq =
+// ((sigma_s + sigma_t) / 2)^2 (cmbrule 0) or sigma_s sigma_t (cmbrule 1), setconf.F90:779-823.
+//   d/dq_s:  sum_t q_t erfc(beta r)/r within elecut (realcal.F90:700-710), plus
+//            sum_t q_t phi_s(r_t) with phi_s the PME potential of a unit charge on s
+//            (recpcal_prepare_solute + recpcal_energy with one site), plus
+//            -pi Q_k / (beta^2 V) (residual_ene, engproc.F90:859-869);
+//   the LJ term of every switching form is 4 eps (vdwa - vdwb) with vdwa ~ sigma^12 and
+//   vdwb ~ sigma^6 (realcal.F90:686-770), so dLJ/deps_s = LJ / (2 eps_s) and
+//   dLJ/d(sigma^2) = 4 eps (6 vdwa - 3 vdwb) / sigma^2.
+// The sum over pairs is a direct minimum-image loop (the cell list only selects pairs
+// within the cutoffs).  eps_s = 0 or sigma_s = 0 report 0 for that parameter.
+}  // extern "C"
+namespace {
+void lj_parts(const orc_params& p, const LjConsts& k, double x, double dist, double& vdwa, double& vdwb) {
+  const double invr2 = x / dist;
+  const double invr6 = invr2 * invr2 * invr2;
+  const double s6 = x * x * x;
+  if (dist <= k.lw2) {
+    switch (p.ljswitch) {
+      case 0:
+      case 1:
+        vdwa = invr6 * invr6;
+        vdwb = invr6;
+        return;
+      case 2:
+        vdwa = invr6 * invr6 - s6 * s6 / (k.lw6 * k.up6);
+        vdwb = invr6 - s6 / (k.lw3 * k.up3);
+        return;
+      default:
+        vdwa = invr6 * invr6 - s6 * s6 * k.repC;
+        vdwb = invr6 - s6 * k.attC;
+        return;
+    }
+  }
+  switch (p.ljswitch) {
+    case 0: {
+      const double dd = dist - k.up2, den = k.up2 - k.lw2;
+      const double sw = (2.0 * dist + k.up2 - 3.0 * k.lw2) * (dd * dd) / (den * den * den);
+      vdwa = invr6 * invr6 * sw;
+      vdwb = invr6 * sw;
+      return;
+    }
+    case 1: {
+      const double swfac = (std::sqrt(dist) - p.lwljcut) / (p.upljcut - p.lwljcut);
+      const double s3 = cube(swfac), s4 = s3 * swfac, s5 = s4 * swfac;
+      const double sw = 1.0 - 10.0 * s3 + 15.0 * s4 - 6.0 * s5;
+      vdwa = invr6 * invr6 * sw;
+      vdwb = invr6 * sw;
+      return;
+    }
+    case 2: {
+      const double invr3 = std::sqrt(invr6), s3 = std::sqrt(s6);
+      const double a = invr6 - s6 / k.up6, b = invr3 - s3 / k.up3;
+      vdwa = k.up6 / (k.up6 - k.lw6) * (a * a);
+      vdwb = k.up3 / (k.up3 - k.lw3) * (b * b);
+      return;
+    }
+    default: {
+      const double swfac = std::sqrt(dist) - p.lwljcut;
+      const double f3 = cube(swfac), f4 = f3 * swfac;
+      vdwa = invr6 * invr6 - s6 * s6 * (k.repA * f3 + k.repB * f4 + k.repC);
+      vdwb = invr6 - s6 * (k.attA * f3 + k.attB * f4 + k.attC);
+      return;
+    }
+  }
+}
+
+// PME potential on the grid of a unit charge at xyz (recpcal.F90:342-406 for one site)
+void unit_site_potential(const orc_ctx* c, const double* xyz, std::vector<double>& cnv) {
+  const int p = c->p.splodr;
+  const int K1 = c->p.ms1max, K2 = c->p.ms2max, K3 = c->p.ms3max, h = K1 / 2 + 1;
+  std::vector<double> spl(3 * (size_t)p);
+  int grd[3];
+  calc_spline_sites(c, xyz, 1, spl.data(), grd);
+  cnv.assign((size_t)K1 * K2 * K3, 0.0);
+  for (int cg3 = 0; cg3 < p; ++cg3)
+    for (int cg2 = 0; cg2 < p; ++cg2)
+      for (int cg1 = 0; cg1 < p; ++cg1) {
+        const int r1 = modulo(grd[0] - cg1, K1), r2 = modulo(grd[1] - cg2, K2), r3 = modulo(grd[2] - cg3, K3);
+        cnv[((size_t)r3 * K2 + r2) * K1 + r1] += spl[cg1] * spl[p + cg2] * spl[2 * p + cg3];
+      }
+  std::vector<cd> rcp((size_t)h * K2 * K3);
+  c->fft.r2c(cnv.data(), rcp.data());
+  for (size_t i = 0; i < rcp.size(); ++i) rcp[i] = c->engfac[i] * rcp[i];
+  c->fft.c2r(rcp.data(), cnv.data());
+}
+}  // namespace
+extern "C" {
+
+int orc_adjoint(const orc_ctx* c, int tagslt, const double* solute_sitepos, int cmbrule, double* out) {
+  if (!c || !c->frame_ready || !out || tagslt < 1 || tagslt > c->nummol || cmbrule < 0 || cmbrule > 1)
+    return ORC_E_PARAM;
+  const int ns = c->numsite[tagslt - 1];
+  const int b = c->mbi[tagslt - 1];
+  const int P = 3 * ns;
+  std::vector<double> sx(3 * (size_t)ns);
+  if (solute_sitepos)
+    std::memcpy(sx.data(), solute_sitepos, sizeof(double) * 3 * ns);
+  else
+    std::memcpy(sx.data(), &c->sitepos[3 * (size_t)(b - 1)], sizeof(double) * 3 * ns);
+  std::fill(out, out + (size_t)c->slvmax * P, 0.0);
+  const LjConsts k = lj_consts(c->p);
+  const int T = c->ljtype_max;
+  const double L[3] = {c->cell[0], c->cell[4], c->cell[8]};
+  auto wrap = [&](double v, int a) { return v - L[a] * std::floor(v / L[a]); };
+  const double resid = PI / c->p.screen / c->p.screen / c->volume;
+  // reciprocal space: one unit-charge potential per solute site
+  std::vector<std::vector<double>> cnv(ns);
+  for (int s = 0; s < ns; ++s) unit_site_potential(c, &sx[3 * (size_t)s], cnv[s]);
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int kk = 0; kk < c->slvmax; ++kk) {
+    const int i = c->tagpt[kk];
+    if (i == tagslt) continue;
+    double* o = out + (size_t)kk * P;
+    const double qk = c->mol_charge[i - 1];
+    for (int s = 0; s < ns; ++s) {
+      const int ats = b + s;  // 1-based atom of solute site s
+      const int ts = c->ljtype[ats - 1];
+      const double eps_s = c->ljene[(ts - 1) + (size_t)T * (ts - 1)];
+      const double sig_s = std::sqrt(c->ljlensq[(ts - 1) + (size_t)T * (ts - 1)]);
+      double dq = recpcal_energy(c, tagslt, i, cnv[s]) - resid * qk;
+      double deps = 0.0, dsig = 0.0;
+      for (int at = c->mbi[i - 1]; at < c->mbi[i]; ++at) {
+        double d2 = 0.0;
+        for (int a = 0; a < 3; ++a) {
+          const double hh = 0.5 * L[a];
+          const double d = hh - std::fabs(hh - std::fabs(wrap(c->pos(a + 1, at), a) - wrap(sx[3 * s + a], a)));
+          d2 += d * d;
+        }
+        const int tt = c->ljtype[at - 1];
+        const double ljeps = c->ljene[(tt - 1) + (size_t)T * (ts - 1)];
+        const double x = c->ljlensq[(tt - 1) + (size_t)T * (ts - 1)];
+        if (ljeps > 0.0 && d2 <= k.up2) {
+          double vdwa, vdwb;
+          lj_parts(c->p, k, x, d2, vdwa, vdwb);
+          const double lj = 4.0 * ljeps * (vdwa - vdwb);
+          if (eps_s > 0.0) deps += lj / (2.0 * eps_s);
+          const double dldx = 4.0 * ljeps * (6.0 * vdwa - 3.0 * vdwb) / x;
+          const double dxds = (cmbrule == 0) ? std::sqrt(x) : (sig_s > 0.0 ? x / sig_s : 0.0);
+          dsig += dldx * dxds;
+        }
+        if (d2 <= k.ele2) {
+          const double r = std::sqrt(d2);
+          dq += c->charge[at - 1] * (1.0 - std::erf(c->p.screen * r)) / r;
+        }
+      }
+      o[3 * s + 0] = dq;
+      o[3 * s + 1] = deps;
+      o[3 * s + 2] = dsig;
+    }
+  }
+  return ORC_OK;
+}
+
 int orc_direct_ewald(const orc_ctx* c, int tagslt, const double* solute_sitepos, int mmax, double* out,
                      double* self_out) {
   // E(u, j) = sum_{m != 0} exp(-pi^2 |m|^2 / beta^2) / (pi V |m|^2) Re[S_u(m) conj(S_j(m))]

@@ -103,6 +103,10 @@ int orc_get_accum(const orc_ctx* c, double* edens, double* ecorr, double* eself,
 int orc_last_cnvslt(const orc_ctx* c, double* out, double* self_energy);
 /* PME reciprocal energies alone: recpcal_prepare_solute + recpcal_energy for every
  * physical molecule (0 for the solute itself), plus the solute's reciprocal self energy. */
+/* Per-molecule derivatives of uvengy(k) with respect to the solute's per-site charge,
+ * LJ epsilon and LJ sigma (cmbrule 0 arithmetic / 1 geometric sigma), FP64:
+ * out[k][3 s + {0,1,2}] for k < slvmax (tagpt order) and solute site s. */
+int orc_adjoint(const orc_ctx* c, int tagslt, const double* solute_sitepos, int cmbrule, double* out);
 int orc_recip_parts(const orc_ctx* c, int tagslt, const double* solute_sitepos, double* out,
                     double* self_out);
 /* Direct Ewald reciprocal-space energy between the solute (positions xs, charges qs)

@@ -87,6 +87,7 @@ def lib():
         L.orc_last_cnvslt.argtypes = [C.c_void_p, dp, dp]
         L.orc_direct_ewald.argtypes = [C.c_void_p, C.c_int, dp, C.c_int, dp, dp]
         L.orc_recip_parts.argtypes = [C.c_void_p, C.c_int, dp, dp, dp]
+        L.orc_adjoint.argtypes = [C.c_void_p, C.c_int, dp, C.c_int, dp]
         _lib = L
     return _lib
 
@@ -356,3 +357,11 @@ class Oracle:
         _check(lib().orc_direct_ewald(self.ctx, int(tagslt), _dp(sx), int(mmax), _dp(out), C.byref(s)),
                "direct_ewald")
         return out, s.value
+
+    def adjoint(self, tagslt, solute_sitepos=None, cmbrule=0):
+        """(slvmax, 3 nsite) FP64 derivatives du_k / d{q_s, eps_s, sigma_s} (engine charge units)."""
+        ns = int(self.topo["mol_begin_index"][tagslt] - self.topo["mol_begin_index"][tagslt - 1])
+        out = np.zeros((self.slvmax, 3 * ns))
+        sx = None if solute_sitepos is None else np.ascontiguousarray(solute_sitepos, np.float64)
+        _check(lib().orc_adjoint(self.ctx, int(tagslt), _dp(sx), int(cmbrule), _dp(out)), "adjoint")
+        return out
