@@ -42,7 +42,7 @@ EXPORTS = [
     "ermod_sync", "ermod_clear", "ermod_get_accum", "ermod_get_sizes", "ermod_error_info",
     "ermod_timing_enable", "ermod_timing_reset", "ermod_timing_get", "ermod_last_error_string",
     "ermod_status_string", "ermod_enginit_species", "ermod_getscrn", "ermod_lj_tables", "ermod_engstore_merge",
-    "ermod_ecorr_add_noalloc",
+    "ermod_ecorr_add_noalloc", "ermod_adjoint_enable", "ermod_adjoint_get",
 ]
 
 _lib = None
@@ -88,6 +88,8 @@ def load(path: str = LIB_PATH):
     L.ermod_engstore_merge.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, dp, dp,
                                        dp, dp, dp, dp, dp]
     L.ermod_ecorr_add_noalloc.argtypes = [vp, vp, C.c_int, C.c_int, vp, vp, vp]
+    L.ermod_adjoint_enable.argtypes = [vp, C.c_int, C.c_int]
+    L.ermod_adjoint_get.argtypes = [vp, dp, dp, ip]
     _lib = L
     return L
 

@@ -20,7 +20,7 @@
 namespace ermod {
 
 const char* const kPhaseNames[PH_COUNT] = {"frame", "place_prep", "spectrum", "fft_c2r", "gather",
-                                           "mol_energy", "accumulate", "ecorr", "copy"};
+                                           "mol_energy", "accumulate", "ecorr", "adjoint", "copy"};
 
 namespace {
 thread_local std::string g_err;
@@ -465,11 +465,14 @@ int ermod_create(const ermod_params* p, int device, ermod_ctx** out) {
   return ERMOD_OK;
 }
 
+static void free_adjoint(Engine& e);
+
 int ermod_destroy(ermod_ctx* c) {
   if (!c) return ERMOD_OK;
   Engine& e = c->e;
   cudaSetDevice(e.device);
   if (e.stream) cudaStreamSynchronize(e.stream);
+  free_adjoint(e);
   free_batch(e);
   free_frame(e);
   free_topology(e);
@@ -528,6 +531,7 @@ int ermod_set_topology(ermod_ctx* c, int nummol, int numatm, const int* mbi, con
   Engine& e = c->e;
   cudaSetDevice(e.device);
   cudaStreamSynchronize(e.stream);
+  free_adjoint(e);  // sized by the topology: enable it again afterwards
   if (mbi[0] != 1 || mbi[nummol] - 1 != numatm) return fail_param("mol_begin_index must run from 1 to numatm+1");
   for (int i = 0; i < nummol; ++i) {
     if (mbi[i + 1] <= mbi[i]) return fail_param("every molecule needs at least one site");
@@ -677,6 +681,7 @@ int ermod_set_bins(ermod_ctx* c, int numslv, const int* uvmax, const int* uvsoft
   Engine& e = c->e;
   cudaSetDevice(e.device);
   cudaStreamSynchronize(e.stream);
+  free_adjoint(e);  // sized by the bins: enable it again afterwards
   int ermax = 0;
   for (int s = 0; s < numslv; ++s) {
     if (uvmax[s] <= 0 || uvsoft[s] < 0 || uvsoft[s] > uvmax[s]) return fail_param("uvmax/uvsoft inconsistent");
@@ -869,6 +874,8 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
     a.self_bin = e.d_self_bin + (size_t)slot * B;
     a.slot = slot;
     a.stream = dual ? e.bs[slot] : e.stream;
+    a.phases = 1;
+    a.mol_u = e.adj_on ? e.d_mol_u + (size_t)slot * B * e.slvmax : nullptr;
     if (e.mixed) {
       const size_t np = (size_t)e.phi_dims[0] * e.phi_dims[1] * e.phi_dims[2];
       a.spec = e.buf.spec + (size_t)slot * e.grid_cplx() * B;
@@ -929,6 +936,11 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
     e.phase_begin_on(PH_ACCUM, e.aux);
     ERMOD_CUDA(launch_accumulate(e, a, e.aux));
     e.phase_end_on(e.aux);
+    if (e.adj_on) {  // after the weights engnmfc of the batch exist
+      e.phase_begin_on(PH_ADJOINT, e.aux);
+      ERMOD_CUDA(launch_adjoint(e, a, e.aux));
+      e.phase_end_on(e.aux);
+    }
     bool flushed = false;
     if (e.P.corrcal) {
       e.ring_fill += nb;
@@ -1095,7 +1107,94 @@ int ermod_clear(ermod_ctx* c) {  // engclear (engproc.F90:276-288)
   ERMOD_CUDA(cudaMemsetAsync(e.d_eself, 0, sizeof(double) * std::max(e.esmax, 1), e.stream));
   ERMOD_CUDA(cudaMemsetAsync(e.d_slnuv, 0, sizeof(double) * e.numslv, e.stream));
   ERMOD_CUDA(cudaMemsetAsync(e.d_scal, 0, sizeof(double) * 3, e.stream));  // engnorm, engsmpl, avslf
+  if (e.adj_on) {
+    ERMOD_CUDA(cudaMemsetAsync(e.d_adj_grad, 0, sizeof(double) * 3 * (size_t)e.adj_ns * e.ermax, e.stream));
+    ERMOD_CUDA(cudaMemsetAsync(e.d_adj_w, 0, sizeof(double) * e.ermax, e.stream));
+  }
   ERMOD_CUDA(cudaStreamSynchronize(e.stream));
+  return ERMOD_OK;
+}
+
+static void free_adjoint(Engine& e) {
+  dfree(e.d_adj_grad);
+  dfree(e.d_adj_w);
+  dfree(e.d_adj_par);
+  dfree(e.d_adj_du);
+  dfree(e.d_adj_key);
+  dfree(e.d_adj_seg);
+  if (e.d_adj_cub) cudaFree(e.d_adj_cub);
+  e.d_adj_cub = nullptr;
+  dfree(e.d_mol_u);
+  dfree(e.d_ps_nsite);
+  dfree(e.d_ps_qf);
+  dfree(e.d_ps_bvec);
+  dfree(e.d_ps_self);
+  e.adj_on = false;
+}
+
+int ermod_adjoint_enable(ermod_ctx* c, int solute_mol, int cmbrule) {
+  if (!c) return fail_param("null context");
+  Engine& e = c->e;
+  if (!e.mixed) {
+    g_err = "the adjoint runs on the mixed-precision path only";
+    return ERMOD_E_UNSUPPORTED;
+  }
+  if (!e.topo_ready) return fail_param("ermod_set_topology must come first");
+  if (!e.bins_ready) return fail_param("ermod_set_bins must come first");
+  if (solute_mol < 1 || solute_mol > e.nummol) return fail_param("solute_mol out of range");
+  if (cmbrule < 0 || cmbrule > 1) return fail_param("cmbrule must be 0 or 1");
+  cudaSetDevice(e.device);
+  ERMOD_CUDA(cudaStreamSynchronize(e.stream));
+  free_adjoint(e);
+  const int ns = e.numsite[solute_mol - 1];
+  if (ns < 1 || ns > kMaxSoluteSites) return fail_param("the solute has no sites or too many");
+  int st = ensure_batch(e);
+  if (st) return st;
+  const int T = e.ljtype_max;
+  std::vector<double> lje((size_t)T * T), ljl((size_t)T * T);
+  ERMOD_CUDA(cudaMemcpy(lje.data(), e.d_ljene, sizeof(double) * lje.size(), cudaMemcpyDeviceToHost));
+  ERMOD_CUDA(cudaMemcpy(ljl.data(), e.d_ljlensq, sizeof(double) * ljl.size(), cudaMemcpyDeviceToHost));
+  std::vector<float2> par(ns);
+  for (int s = 0; s < ns; ++s) {  // eps_s = ljene(t,t), sigma_s^2 = ljlensq(t,t) under either rule
+    const int t = e.ljtype0[e.mbi0[solute_mol - 1] + s];
+    par[s] = make_float2((float)lje[(size_t)t * T + t], (float)std::sqrt(ljl[(size_t)t * T + t]));
+  }
+  const int B = e.Bmax;
+  ERMOD_CUDA(dalloc(&e.d_adj_grad, 3 * (size_t)ns * e.ermax));
+  ERMOD_CUDA(dalloc(&e.d_adj_w, (size_t)e.ermax));
+  ERMOD_CUDA(dalloc(&e.d_adj_par, (size_t)ns));
+  ERMOD_CUDA(dalloc(&e.d_adj_du, (size_t)e.slvmax * 3 * ns));
+  ERMOD_CUDA(dalloc(&e.d_adj_key, 4 * (size_t)e.slvmax));
+  ERMOD_CUDA(dalloc(&e.d_adj_seg, 2 * (size_t)e.ermax));
+  e.adj_cub_bytes = adjoint_cub_bytes(e.slvmax);
+  ERMOD_CUDA(cudaMalloc(&e.d_adj_cub, std::max<size_t>(e.adj_cub_bytes, 16)));
+  ERMOD_CUDA(dalloc(&e.d_mol_u, 2 * (size_t)B * e.slvmax));
+  ERMOD_CUDA(dalloc(&e.d_ps_nsite, (size_t)B));
+  ERMOD_CUDA(dalloc(&e.d_ps_qf, (size_t)B * kMaxSoluteSites));
+  ERMOD_CUDA(dalloc(&e.d_ps_bvec, (size_t)B * kMaxSoluteSites * 3 * e.Kmax()));
+  ERMOD_CUDA(dalloc(&e.d_ps_self, (size_t)B * spectrum_partials(e)));
+  ERMOD_CUDA(cudaMemcpy(e.d_adj_par, par.data(), sizeof(float2) * ns, cudaMemcpyHostToDevice));
+  ERMOD_CUDA(cudaMemset(e.d_adj_grad, 0, sizeof(double) * 3 * (size_t)ns * e.ermax));
+  ERMOD_CUDA(cudaMemset(e.d_adj_w, 0, sizeof(double) * e.ermax));
+  ERMOD_CUDA(cudaMemset(e.d_ps_qf, 0, sizeof(float) * (size_t)B * kMaxSoluteSites));
+  e.adj_mol = solute_mol;
+  e.adj_ns = ns;
+  e.adj_cmbrule = cmbrule;
+  e.adj_on = true;
+  return ERMOD_OK;
+}
+
+int ermod_adjoint_get(ermod_ctx* c, double* grad, double* weight, int* nparam) {
+  if (!c) return fail_param("null context");
+  Engine& e = c->e;
+  if (!e.adj_on) return fail_param("ermod_adjoint_enable must come first");
+  cudaSetDevice(e.device);
+  ERMOD_CUDA(cudaStreamSynchronize(e.stream));
+  if (nparam) *nparam = 3 * e.adj_ns;
+  if (grad)
+    ERMOD_CUDA(cudaMemcpy(grad, e.d_adj_grad, sizeof(double) * 3 * (size_t)e.adj_ns * e.ermax,
+                          cudaMemcpyDeviceToHost));
+  if (weight) ERMOD_CUDA(cudaMemcpy(weight, e.d_adj_w, sizeof(double) * e.ermax, cudaMemcpyDeviceToHost));
   return ERMOD_OK;
 }
 

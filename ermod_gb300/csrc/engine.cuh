@@ -13,7 +13,7 @@
 
 namespace ermod {
 
-enum Phase { PH_FRAME = 0, PH_PREP, PH_SPECTRUM, PH_FFT, PH_GATHER, PH_MOL, PH_ACCUM, PH_ECORR, PH_COPY, PH_COUNT };
+enum Phase { PH_FRAME = 0, PH_PREP, PH_SPECTRUM, PH_FFT, PH_GATHER, PH_MOL, PH_ACCUM, PH_ECORR, PH_ADJOINT, PH_COPY, PH_COUNT };
 extern const char* const kPhaseNames[PH_COUNT];
 
 struct Engine {
@@ -143,6 +143,27 @@ struct Engine {
   int phi_dims[3] = {0, 0, 0};   // XP (multiple of 4), YP, ZP
   int gbox[3] = {0, 0, 0};       // gather box: x (multiple of 4), y, z
   alignas(64) CUtensorMap phi_tmap[2];  // per slot
+
+  // adjoint mode (mixed path): bin-resolved derivatives of the solvent molecules'
+  // energies with respect to the per-site charge, LJ epsilon and LJ sigma of a solute
+  bool adj_on = false;
+  int adj_mol = 0;      // 1-based molecule whose placements are differentiated
+  int adj_ns = 0;       // its sites: 3 adj_ns parameters
+  int adj_cmbrule = 0;  // sigma combination: 0 arithmetic, 1 geometric
+  double* d_adj_grad = nullptr;  // [3 adj_ns][ermax] FP64 accumulators
+  double* d_adj_w = nullptr;     // [ermax] weight of the molecules summed per bin
+  float2* d_adj_par = nullptr;   // [adj_ns] {eps_s, sigma_s} of the solute sites
+  float* d_adj_du = nullptr;     // [slvmax][3 adj_ns] per-molecule derivatives (one placement)
+  int* d_adj_key = nullptr;      // [4][slvmax] bin keys and molecule slots, sorted copies
+  int* d_adj_seg = nullptr;      // [2][ermax] segment begin / end in the sorted order
+  void* d_adj_cub = nullptr;
+  size_t adj_cub_bytes = 0;
+  float* d_mol_u = nullptr;      // [2][Bmax][slvmax] per-molecule totals (slot order)
+  // unit-charge single-site "placements" whose potentials give d u / d q_s
+  int* d_ps_nsite = nullptr;     // [Bmax]
+  float* d_ps_qf = nullptr;      // [Bmax][256]
+  float2* d_ps_bvec = nullptr;   // [Bmax][256][3][Kmax]
+  double* d_ps_self = nullptr;   // [Bmax][K2]
   bool tmap_ready = false;
 
   // ---- cuFFT -------------------------------------------------------------------------

@@ -92,6 +92,8 @@ struct BatchArgs {
   int slot;           // batch parity: selects the double-buffered PME grids
   cudaStream_t stream;  // stream of the batch's PME, gather and finish kernels
   float* site_e;      // [nsite_phys][Bmax] reciprocal site terms of this slot (mixed)
+  int phases;         // 1: the launchers split the caller's timing phase (gather/finish...)
+  float* mol_u;       // [nb][slvmax] per-molecule totals in slot order (adjoint mode) or null
   const int* tagslt;  // [nb] 1-based
   const double* stat_weight_solute;  // [nb] or null
   // solute site data per placement, [nb][kMaxSoluteSites]
@@ -139,6 +141,10 @@ cudaError_t launch_spread64(Engine& e, const BatchArgs& a);
 cudaError_t launch_influence64(Engine& e, const BatchArgs& a);
 // per-molecule energies and histograms
 cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a);
+cudaError_t launch_gather(Engine& e, const BatchArgs& a);
+// adjoint mode: bin-resolved solute-parameter derivatives of the batch's placements
+cudaError_t launch_adjoint(Engine& e, const BatchArgs& a, cudaStream_t s);
+size_t adjoint_cub_bytes(int n);
 // accumulation
 cudaError_t launch_accumulate(Engine& e, const BatchArgs& a, cudaStream_t s);
 cudaError_t launch_ecorr_flush(Engine& e, cudaStream_t s);

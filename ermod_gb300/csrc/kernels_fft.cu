@@ -611,8 +611,10 @@ cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a) {
   pme_a_kernel<<<dim3(A.K2, a.nb), kPmeThreads, sa, a.stream>>>(A);
   e.count_launch();
   if ((err = cudaGetLastError()) != cudaSuccess) return err;
-  e.phase_end_on(a.stream);
-  e.phase_begin_on(PH_FFT, a.stream);
+  if (a.phases) {
+    e.phase_end_on(a.stream);
+    e.phase_begin_on(PH_FFT, a.stream);
+  }
   pme_b_kernel<<<dim3(A.K3, a.nb), kPmeThreads, sb, a.stream>>>(A);
   e.count_launch();
   return cudaGetLastError();

@@ -17,6 +17,8 @@
 //
 // Mixed path: fixed-point positions, FP32 pair terms and grid gather, FP64 per-site and
 // per-molecule totals.  FP64 path: everything in FP64 with the reference's formulas.
+#include <cub/device/device_radix_sort.cuh>
+
 #include "engine.cuh"
 
 namespace ermod {
@@ -915,6 +917,11 @@ __global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const flo
       }
     }
   }
+  if (a.mol_u && valid) {  // adjoint mode: the totals in slot order (NaN: no molecule)
+#pragma unroll
+    for (int j = 0; j < G; ++j)
+      if (j < ng) a.mol_u[(size_t)(g0 + j) * A.slvmax + m] = act[j] ? uu[j] : __uint_as_float(0x7fc00000u);
+  }
   __syncthreads();  // histograms zeroed, keys staged
   // ---- getiduv / binsearch for all G at once: ret = #edges < u ----
   long long ku[G];
@@ -1029,7 +1036,7 @@ cudaError_t set_smem_attr(size_t smem) {  // FP64 instantiations only
 
 }  // namespace
 
-cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
+static MolArgs make_mol_args(Engine& e, const BatchArgs& a) {
   MolArgs A{};
   A.site_pos = e.d_site_pos;
   A.site_rec = e.d_site_rec;
@@ -1071,6 +1078,42 @@ cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
   A.a = a;
   A.ntile = e.ntile;
   A.status = e.d_status;
+  return A;
+}
+
+// step 1 of the mixed path: gather by bricks (TMA-staged halos, double-buffered over
+// placement groups) into a.site_e
+cudaError_t launch_gather(Engine& e, const BatchArgs& a) {
+  cudaError_t err = cudaSuccess;
+  const int ngroups = (a.nb + 3) / 4;
+  const int gpc = std::min(ngroups, 4);
+  dim3 g1(e.nbricks, (ngroups + gpc - 1) / gpc);
+  const int K1 = e.geom.K[0], K2 = e.geom.K[1], K3 = e.geom.K[2];
+  const size_t npt = (size_t)e.gbox[0] * e.gbox[1] * e.gbox[2];
+  const size_t boxf = (4 * npt + 31) & ~(size_t)31;  // as in the kernel: 128-byte aligned boxes
+  const size_t sh = 128 + 2 * boxf * sizeof(float) + npt * sizeof(float4);
+#define ERMOD_GATHER(PP)                                                                                        \
+  if (e.P_order == PP) {                                                                                        \
+    static size_t attr = 0;                                                                                     \
+    if (attr < sh) {                                                                                            \
+      err = cudaFuncSetAttribute(gather_tma_kernel<PP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);  \
+      if (err != cudaSuccess) return err;                                                                       \
+      attr = sh;                                                                                                \
+    }                                                                                                           \
+    gather_tma_kernel<PP><<<g1, kGatherThreads, sh, a.stream>>>(                                                \
+        e.phi_tmap[a.slot], a.nb, gpc, e.d_site_rec, e.d_site_grid, e.d_brick_site, e.d_brick_start, K1, K2, K3,  \
+        e.nbrick[0], e.nbrick[1], e.gbox[0], e.Bmax, a.site_e, e.d_status);                                     \
+  }
+  ERMOD_GATHER(4)
+  ERMOD_GATHER(6)
+  ERMOD_GATHER(8)
+#undef ERMOD_GATHER
+  e.count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
+  const MolArgs A = make_mol_args(e, a);
   const size_t smem = sizeof(int) * (size_t)a.G * e.ermax;
   dim3 grid(e.ntile, (a.nb + a.G - 1) / a.G);
   e.count_launch();
@@ -1084,35 +1127,11 @@ cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
     return launch_p<false>(e, A, grid, smem);
   }
   if (a.G != 8 && a.G != 4) return cudaErrorInvalidValue;
-  {  // step 1: gather by bricks (TMA-staged halos, double-buffered over placement groups)
-    const int ngroups = (a.nb + 3) / 4;
-    const int gpc = std::min(ngroups, 4);
-    dim3 g1(e.nbricks, (ngroups + gpc - 1) / gpc);
-    const int K1 = e.geom.K[0], K2 = e.geom.K[1], K3 = e.geom.K[2];
-    const size_t npt = (size_t)e.gbox[0] * e.gbox[1] * e.gbox[2];
-    const size_t boxf = (4 * npt + 31) & ~(size_t)31;  // as in the kernel: 128-byte aligned boxes
-    const size_t sh = 128 + 2 * boxf * sizeof(float) + npt * sizeof(float4);
-#define ERMOD_GATHER(PP)                                                                                        \
-  if (e.P_order == PP) {                                                                                        \
-    static size_t attr = 0;                                                                                     \
-    if (attr < sh) {                                                                                            \
-      err = cudaFuncSetAttribute(gather_tma_kernel<PP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);  \
-      if (err != cudaSuccess) return err;                                                                       \
-      attr = sh;                                                                                                \
-    }                                                                                                           \
-    gather_tma_kernel<PP><<<g1, kGatherThreads, sh, a.stream>>>(                                                \
-        e.phi_tmap[a.slot], a.nb, gpc, e.d_site_rec, e.d_site_grid, e.d_brick_site, e.d_brick_start, K1, K2, K3,        \
-        e.nbrick[0], e.nbrick[1], e.gbox[0], e.Bmax, a.site_e, e.d_status);                                   \
+  if ((err = launch_gather(e, a)) != cudaSuccess) return err;
+  if (a.phases) {
+    e.phase_end_on(a.stream);
+    e.phase_begin_on(PH_MOL, a.stream);
   }
-    ERMOD_GATHER(4)
-    ERMOD_GATHER(6)
-    ERMOD_GATHER(8)
-#undef ERMOD_GATHER
-    e.count_launch();
-    if ((err = cudaGetLastError()) != cudaSuccess) return err;
-  }
-  e.phase_end_on(a.stream);
-  e.phase_begin_on(PH_MOL, a.stream);
   // step 2: per-molecule totals and binning (histograms + edge keys in shared memory)
   const size_t smem_f = sizeof(int) * (((size_t)a.G * e.ermax + 1) & ~(size_t)1) + sizeof(long long) * e.ermax;
   dim3 g2((a.nb + a.G - 1) / a.G, e.ntile);
@@ -1131,6 +1150,274 @@ cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
 #undef ERMOD_FINISH
   e.count_launch();
   return cudaGetLastError();
+}
+
+
+// ---- adjoint mode -------------------------------------------------------------------
+//
+// For a placement b of the differentiated solute and every solvent molecule k, the
+// derivatives of u_k = real(k) + residual(k) + recip(k) (get_uv_energy,
+// engproc.F90:662-756) with respect to each solute site's charge q_s (topology units),
+// LJ epsilon eps_s and LJ sigma sigma_s:
+//   du/dq_s     = sum_t q_t erfc(beta r)/r (r <= elecut) + sum_t q_t phi_s(r_t) - pi Q_k/(beta^2 V)
+//   du/deps_s   = sum_t LJ_st / (2 eps_s)                       (eps_st = sqrt(eps_s eps_t))
+//   du/dsigma_s = sum_t 4 eps_st (6 vdwa - 3 vdwb)/sigma_st^2 * d(sigma_st^2)/d(sigma_s)
+// where phi_s is the PME potential of a unit charge on site s (computed by the mixed
+// kernels as a batch of single-site "placements") and LJ_st = 4 eps_st (vdwa - vdwb) in
+// every switching form (realcal.F90:686-770), vdwa ~ sigma^12 and vdwb ~ sigma^6.  Each
+// molecule's derivatives (FP32) are then summed per energy bin of u_k in FP64, in a fixed
+// order (molecules stably sorted by bin), times the placement's weight engnmfc.
+namespace {
+
+__device__ __forceinline__ void lj_parts_f(int sw, const LjK& k, float x, float r2, float& vdwa, float& vdwb) {
+  const float invr2 = x / r2;
+  const float invr6 = invr2 * invr2 * invr2;
+  const float s6 = x * x * x;
+  if (r2 <= k.lw2) {
+    if (sw <= 1) {
+      vdwa = invr6 * invr6;
+      vdwb = invr6;
+    } else if (sw == 2) {
+      vdwa = invr6 * invr6 - s6 * s6 / (k.lw6 * k.up6);
+      vdwb = invr6 - s6 / (k.lw3 * k.up3);
+    } else {
+      vdwa = invr6 * invr6 - s6 * s6 * k.repC;
+      vdwb = invr6 - s6 * k.attC;
+    }
+    return;
+  }
+  if (sw == 0) {
+    const float dd = r2 - k.up2, den = k.up2 - k.lw2;
+    const float f = (2.f * r2 + k.up2 - 3.f * k.lw2) * (dd * dd) / (den * den * den);
+    vdwa = invr6 * invr6 * f;
+    vdwb = invr6 * f;
+  } else if (sw == 1) {
+    const float t = (sqrtf(r2) - k.lw) / (k.up - k.lw);
+    const float t3 = t * t * t, t4 = t3 * t, t5 = t4 * t;
+    const float f = 1.f - 10.f * t3 + 15.f * t4 - 6.f * t5;
+    vdwa = invr6 * invr6 * f;
+    vdwb = invr6 * f;
+  } else if (sw == 2) {
+    const float invr3 = sqrtf(invr6), s3 = sqrtf(s6);
+    const float a = invr6 - s6 / k.up6, b = invr3 - s3 / k.up3;
+    vdwa = k.up6 / (k.up6 - k.lw6) * (a * a);
+    vdwb = k.up3 / (k.up3 - k.lw3) * (b * b);
+  } else {
+    const float f = sqrtf(r2) - k.lw;
+    const float f3 = f * f * f, f4 = f3 * f;
+    vdwa = invr6 * invr6 - s6 * s6 * (k.repA * f3 + k.repB * f4 + k.repC);
+    vdwb = invr6 - s6 * (k.attA * f3 + k.attB * f4 + k.attC);
+  }
+}
+
+struct AdjArgs {
+  int b;          // placement within the batch
+  int s_begin;    // first solute site of this chunk of unit-charge potentials
+  int nchunk;     // sites in the chunk
+  int nsu;        // solute sites: 3 nsu parameters
+  int adj_mol;    // 1-based molecule whose placements are differentiated
+  int cmbrule;
+  int first;      // first chunk: also writes the bin keys
+  const float* site_e_ps;  // [nsite][ldb] q_t phi_s(r_t) of the chunk's sites
+  const float* mol_u;      // [slvmax] totals of placement b, slot order
+  const float2* par;       // [nsu] {eps_s, sigma_s}
+  float* du;               // [slvmax][3 nsu]
+  int* key;                // [slvmax] global bin, or ermax to leave the molecule out
+  int* val;                // [slvmax] slot index
+};
+
+__global__ void __launch_bounds__(256) adjoint_mol_kernel(MolArgs A, AdjArgs J) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= A.slvmax) return;
+  const BatchArgs& a = A.a;
+  const int b = J.b;
+  const int k = A.slot_mol[m];
+  const int s0 = A.slot_site[m];
+  const int ns = A.slot_site[m + 1] - s0;
+  const int species = A.slot_species[m];
+  const int tg = a.tagslt[b] - 1;
+  const int kskip = (tg >= 0 && tg < A.nummol) ? A.mol_to_k[tg] : -2;
+  bool take = (tg + 1 == J.adj_mol) && (k != kskip) && species >= 1 && species <= A.numslv;
+  if (J.first) {
+    int key = A.ermax;
+    const float u = J.mol_u[m];
+    if (take && u == u) {  // getiduv on the FP64 value of the FP32 total, as the finish kernel bins it
+      const int sp_off = A.spec[3 * (species - 1)], sp_n = A.spec[3 * (species - 1) + 1];
+      const int sp_soft = A.spec[3 * (species - 1) + 2];
+      const long long ku = ordered_key_f(u);
+      int lo = 0, hi = sp_n;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(A.uvkey + sp_off + mid) < ku)
+          lo = mid + 1;
+        else
+          hi = mid;
+      }
+      if (lo > 0 && !(A.soln && lo > sp_soft)) key = sp_off + lo - 1;
+    }
+    J.key[m] = key;
+    J.val[m] = m;
+  }
+  if (!take) return;
+  const size_t ub = (size_t)b * kMaxSoluteSites;
+  const int P = 3 * J.nsu;
+  const float fx = A.fxf[0], fy = A.fxf[1], fz = A.fxf[2];
+  const LjK& k32 = A.k32;
+  const float beta = A.screen_f;
+  const float rq = (float)A.resid_fac * (float)A.slot_qmol[m];
+  // the molecule is near the solute when its first site lies within the solute's
+  // bounding sphere plus the cutoff (the finish kernel's test)
+  const int4 p0 = A.site_pos[s0];
+  const int4 q0 = a.u_pos[ub];
+  const float dx0 = (float)(int)((unsigned)p0.x - (unsigned)q0.x) * fx;
+  const float dy0 = (float)(int)((unsigned)p0.y - (unsigned)q0.y) * fy;
+  const float dz0 = (float)(int)((unsigned)p0.z - (unsigned)q0.z) * fz;
+  const float rcut = A.rc_f + a.u_radius[b] + A.frame_scal[0];
+  const bool near = dx0 * dx0 + dy0 * dy0 + dz0 * dz0 <= rcut * rcut;
+  for (int j = 0; j < J.nchunk; ++j) {
+    const int s = J.s_begin + j;
+    float dq = -rq, deps = 0.f, dsig = 0.f;
+    for (int t = 0; t < ns; ++t) dq += J.site_e_ps[(size_t)(s0 + t) * A.ldb + j];
+    if (near) {
+      const int4 up = a.u_pos[ub + s];
+      const float2 par = J.par[s];
+      for (int t = 0; t < ns; ++t) {
+        const int4 vp = A.site_pos[s0 + t];
+        const float ex = (float)(int)((unsigned)vp.x - (unsigned)up.x) * fx;
+        const float ey = (float)(int)((unsigned)vp.y - (unsigned)up.y) * fy;
+        const float ez = (float)(int)((unsigned)vp.z - (unsigned)up.z) * fz;
+        const float r2 = ex * ex + ey * ey + ez * ez;
+        const float ljeps = A.ljene_f[vp.w + A.T * up.w];
+        if (ljeps > 0.f && r2 <= k32.up2) {
+          const float x = A.ljlensq_f[vp.w + A.T * up.w];
+          float va, vb;
+          lj_parts_f(A.ljswitch, k32, x, r2, va, vb);
+          if (par.x > 0.f) deps += 4.f * ljeps * (va - vb) / (2.f * par.x);
+          const float dldx = 4.f * ljeps * (6.f * va - 3.f * vb) / x;
+          const float dxds = (J.cmbrule == 0) ? sqrtf(x) : (par.y > 0.f ? x / par.y : 0.f);
+          dsig += dldx * dxds;
+        }
+        if (r2 <= k32.ele2) {
+          const float r = sqrtf(r2);
+          dq += A.site_rec[s0 + t].w * erfcf(beta * r) / r;
+        }
+      }
+    }
+    float* o = J.du + (size_t)m * P + 3 * s;
+    o[0] = dq;
+    o[1] = deps;
+    o[2] = dsig;
+  }
+}
+
+// the chunk's unit-charge single-site placements: site s_begin + j of placement b
+__global__ void adjoint_pseudo_kernel(const float2* __restrict__ bvec, int b, int s_begin, int Kmax, int* nsite,
+                                      float* qf, float2* ps_bvec) {
+  const int j = blockIdx.x;
+  if (threadIdx.x == 0) {
+    nsite[j] = 1;
+    qf[(size_t)j * kMaxSoluteSites] = 1.f;
+  }
+  const float2* src = bvec + ((size_t)b * kMaxSoluteSites + s_begin + j) * 3 * Kmax;
+  float2* dst = ps_bvec + (size_t)j * kMaxSoluteSites * 3 * Kmax;
+  for (int i = threadIdx.x; i < 3 * Kmax; i += blockDim.x) dst[i] = src[i];
+}
+
+__global__ void adjoint_bounds_kernel(const int* __restrict__ key, int n, int ermax, int* seg_b, int* seg_e) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int kk = key[i];
+  if (kk >= ermax) return;
+  if (i == 0 || key[i - 1] != kk) seg_b[kk] = i;
+  if (i == n - 1 || key[i + 1] != kk) seg_e[kk] = i + 1;
+}
+
+// one CTA per bin, one thread per parameter: FP64 sums in the sorted (bin, slot) order
+__global__ void adjoint_reduce_kernel(const int* __restrict__ val, const float* __restrict__ du, int P,
+                                      const int* __restrict__ seg_b, const int* __restrict__ seg_e,
+                                      const double* __restrict__ engnmfc, int b, int ermax, double* grad,
+                                      double* wsum) {
+  const int bin = blockIdx.x;
+  const int i0 = seg_b[bin], i1 = seg_e[bin];
+  if (i0 >= i1) return;
+  const double w = engnmfc[b];
+  for (int p = threadIdx.x; p < P; p += blockDim.x) {
+    double acc = 0.0;
+    for (int i = i0; i < i1; ++i) acc += (double)du[(size_t)val[i] * P + p];
+    grad[(size_t)p * ermax + bin] += w * acc;
+  }
+  if (threadIdx.x == 0) wsum[bin] += w * (double)(i1 - i0);
+}
+
+int key_bits(int ermax) {
+  int bits = 1;
+  while ((1 << bits) <= ermax) ++bits;
+  return bits;
+}
+
+}  // namespace
+
+size_t adjoint_cub_bytes(int n) {
+  size_t bytes = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, bytes, (int*)nullptr, (int*)nullptr, (int*)nullptr, (int*)nullptr, n);
+  return bytes;
+}
+
+cudaError_t launch_adjoint(Engine& e, const BatchArgs& a, cudaStream_t s) {
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return err;
+  const int n = e.slvmax;
+  const int P = 3 * e.adj_ns;
+  const int chunk = e.Bmax;
+  int* key = e.d_adj_key;
+  int* val = key + n;
+  int* key_s = val + n;
+  int* val_s = key_s + n;
+  for (int b = 0; b < a.nb; ++b) {
+    for (int s0 = 0; s0 < e.adj_ns; s0 += chunk) {
+      const int nch = std::min(chunk, e.adj_ns - s0);
+      adjoint_pseudo_kernel<<<nch, 128, 0, s>>>(a.u_bvec, b, s0, e.Kmax(), e.d_ps_nsite, e.d_ps_qf, e.d_ps_bvec);
+      e.count_launch();
+      BatchArgs pa = a;  // unit charges on single sites, this slot's grids and site terms
+      pa.nb = nch;
+      pa.u_nsite = e.d_ps_nsite;
+      pa.u_qf = e.d_ps_qf;
+      pa.u_bvec = e.d_ps_bvec;
+      pa.self_part = e.d_ps_self;
+      pa.stream = s;
+      pa.phases = 0;
+      if ((err = launch_pme_mixed(e, pa)) != cudaSuccess) return err;
+      if ((err = launch_gather(e, pa)) != cudaSuccess) return err;
+      MolArgs A = make_mol_args(e, a);
+      AdjArgs J{};
+      J.b = b;
+      J.s_begin = s0;
+      J.nchunk = nch;
+      J.nsu = e.adj_ns;
+      J.adj_mol = e.adj_mol;
+      J.cmbrule = e.adj_cmbrule;
+      J.first = (s0 == 0);
+      J.site_e_ps = a.site_e;
+      J.mol_u = a.mol_u + (size_t)b * n;
+      J.par = e.d_adj_par;
+      J.du = e.d_adj_du;
+      J.key = key;
+      J.val = val;
+      adjoint_mol_kernel<<<(n + 255) / 256, 256, 0, s>>>(A, J);
+      e.count_launch();
+      if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    }
+    size_t bytes = e.adj_cub_bytes;
+    err = cub::DeviceRadixSort::SortPairs(e.d_adj_cub, bytes, key, key_s, val, val_s, n, 0, key_bits(e.ermax), s);
+    if (err != cudaSuccess) return err;
+    if ((err = cudaMemsetAsync(e.d_adj_seg, 0, sizeof(int) * 2 * (size_t)e.ermax, s)) != cudaSuccess) return err;
+    adjoint_bounds_kernel<<<(n + 255) / 256, 256, 0, s>>>(key_s, n, e.ermax, e.d_adj_seg, e.d_adj_seg + e.ermax);
+    adjoint_reduce_kernel<<<e.ermax, 64, 0, s>>>(val_s, e.d_adj_du, P, e.d_adj_seg, e.d_adj_seg + e.ermax, a.engnmfc,
+                                                 b, e.ermax, e.d_adj_grad, e.d_adj_w);
+    e.count_launch(2);
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  }
+  return cudaSuccess;
 }
 
 }  // namespace ermod

@@ -129,6 +129,24 @@ class EnergyRepresentation:
                     slnuv=slnuv, minuv=mn, maxuv=mx, engnorm=sc[0], engsmpl=sc[1], avslf=sc[2], voffset=sc[3],
                     voffset_initialized=bool(sc[4]))
 
+    # ---- adjoint mode ------------------------------------------------------------
+    def adjoint_enable(self, solute_mol: int = None, cmbrule: int = 0):
+        """Accumulate bin-resolved d u / d(q_s, eps_s, sigma_s) for placements of solute_mol
+        (1-based; default the last molecule, the solute of an MDinfo-ordered topology)."""
+        mol = self.topo["nummol"] if solute_mol is None else int(solute_mol)
+        check(_lib.load().ermod_adjoint_enable(self.ctx, mol, int(cmbrule)), "ermod_adjoint_enable")
+        ns = int(self.topo["mol_begin_index"][mol] - self.topo["mol_begin_index"][mol - 1])
+        self._adj_nparam = 3 * ns
+
+    def adjoint_get(self):
+        """(grad [3 nsite, ermax], weight [ermax]); <du/dtheta_p> in bin i is grad[p, i] / weight[i]."""
+        P = self._adj_nparam
+        grad = np.zeros(P * self.ermax)
+        w = np.zeros(self.ermax)
+        n = C.c_int()
+        check(_lib.load().ermod_adjoint_get(self.ctx, _lib.dp(grad), _lib.dp(w), C.byref(n)), "ermod_adjoint_get")
+        return grad.reshape(P, self.ermax), w
+
     def error_info(self):
         p, m, e = C.c_int(), C.c_int(), C.c_double()
         check(_lib.load().ermod_error_info(self.ctx, C.byref(p), C.byref(m), C.byref(e)), "error_info")

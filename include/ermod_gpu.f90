@@ -81,5 +81,16 @@ module ermod_gpu
        integer(c_int), intent(out) :: placement, molecule
        real(c_double), intent(out) :: energy
      end function
+     integer(c_int) function ermod_adjoint_enable(ctx, solute_mol, cmbrule) bind(C, name="ermod_adjoint_enable")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: solute_mol, cmbrule
+     end function
+     integer(c_int) function ermod_adjoint_get(ctx, grad, weight, nparam) bind(C, name="ermod_adjoint_get")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), intent(out) :: grad(*), weight(*)   ! grad(ermax, 3*nsite) in Fortran order
+       integer(c_int), intent(out) :: nparam
+     end function
   end interface
 end module ermod_gpu

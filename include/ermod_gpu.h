@@ -163,6 +163,25 @@ int ermod_timing_get(ermod_ctx* ctx, int max_phases, double* ms, const char** na
 const char* ermod_last_error_string(void);
 const char* ermod_status_string(int status);
 
+/* ---- adjoint mode (mixed precision) --------------------------------------------------
+ * Bin-resolved derivatives of the solute-solvent energy with respect to the solute's
+ * per-site parameters.  For every placement of molecule solute_mol (1-based), every
+ * solvent molecule k with energy u_k in bin iduv (getiduv, engproc.F90:927-1020) and
+ * every solute site s:
+ *   grad[p][iduv] += engnmfc * d u_k / d theta_p,   weight[iduv] += engnmfc
+ * with theta_{3s} = q_s (charge in topology units, e x 18.22261721), theta_{3s+1} = LJ
+ * epsilon of the site (ljene = sqrt(eps_s eps_t)), theta_{3s+2} = LJ sigma of the site
+ * (ljlensq = ((sigma_s + sigma_t)/2)^2 for cmbrule 0, sigma_s sigma_t for cmbrule 1;
+ * setconf.F90:779-823).  u_k is uvengy(k) of get_uv_energy (engproc.F90:662-756):
+ * real-space LJ and erfc Coulomb, the PME reciprocal term and residual_ene.  The
+ * conditional average <du/dtheta> in bin iduv is grad[p][iduv] / weight[iduv].
+ * Per-molecule derivatives are FP32 and their sums FP64 in a fixed order.  Enable after
+ * ermod_set_topology and ermod_set_bins (either one disables the mode again); ermod_clear
+ * zeroes grad and weight; engstore-style merging treats them as it treats edens. */
+int ermod_adjoint_enable(ermod_ctx* ctx, int solute_mol, int cmbrule);
+/* grad: [3 nsite][ermax] (parameter-major), weight: [ermax]; *nparam = 3 nsite. */
+int ermod_adjoint_get(ermod_ctx* ctx, double* grad, double* weight, int* nparam);
+
 /* ---- host-side set-up helpers (the reference's own set-up arithmetic) -------------- */
 
 /* enginit's energy coordinate for one species (engproc.F90:163-218).
