@@ -42,7 +42,8 @@ EXPORTS = [
     "ermod_sync", "ermod_clear", "ermod_get_accum", "ermod_get_sizes", "ermod_error_info",
     "ermod_timing_enable", "ermod_timing_reset", "ermod_timing_get", "ermod_last_error_string",
     "ermod_status_string", "ermod_enginit_species", "ermod_getscrn", "ermod_lj_tables", "ermod_engstore_merge",
-    "ermod_ecorr_add_noalloc", "ermod_adjoint_enable", "ermod_adjoint_get",
+    "ermod_ecorr_add_noalloc", "ermod_adjoint_enable", "ermod_adjoint_get", "ermod_graph_create",
+    "ermod_graph_launch", "ermod_graph_sync", "ermod_graph_destroy",
 ]
 
 _lib = None
@@ -90,6 +91,11 @@ def load(path: str = LIB_PATH):
     L.ermod_ecorr_add_noalloc.argtypes = [vp, vp, C.c_int, C.c_int, vp, vp, vp]
     L.ermod_adjoint_enable.argtypes = [vp, C.c_int, C.c_int]
     L.ermod_adjoint_get.argtypes = [vp, dp, dp, ip]
+    vpp = C.POINTER(vp)
+    L.ermod_graph_create.argtypes = [C.c_int, vpp, vpp, dp, dp, ip, ip, vpp, vpp, vpp, C.POINTER(vp)]
+    L.ermod_graph_launch.argtypes = [vp, vp]
+    L.ermod_graph_sync.argtypes = [vp]
+    L.ermod_graph_destroy.argtypes = [vp]
     _lib = L
     return L
 

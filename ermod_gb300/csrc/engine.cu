@@ -985,18 +985,15 @@ static int check_ready(Engine& e, int nplace) {
   return ERMOD_OK;
 }
 
-static int reset_status(Engine& e) {
-  DevStatus s0{kNoError, 0, 0};
-  ERMOD_CUDA(cudaMemcpyAsync(e.d_status, &s0, sizeof(s0), cudaMemcpyHostToDevice, e.stream));
-  *e.h_status = s0;
+static int reset_status(Engine& e) {  // memsets only, so that a graph capture can hold it
+  static_assert(sizeof(DevStatus) == 16, "DevStatus layout: err_key, mbin_hit, range_fault");
+  ERMOD_CUDA(cudaMemsetAsync(&e.d_status->err_key, 0xff, sizeof(unsigned long long), e.stream));  // kNoError
+  ERMOD_CUDA(cudaMemsetAsync(&e.d_status->mbin_hit, 0, 2 * sizeof(int), e.stream));
+  *e.h_status = DevStatus{kNoError, 0, 0};
   return ERMOD_OK;
 }
 
-int ermod_sync(ermod_ctx* c) {
-  if (!c) return fail_param("null context");
-  Engine& e = c->e;
-  cudaSetDevice(e.device);
-  ERMOD_CUDA(cudaStreamSynchronize(e.stream));
+static int decode_status(Engine& e) {
   const DevStatus s = *e.h_status;
   if (s.mbin_hit || (s.err_key != kNoError && (int)(s.err_key & 0xff) == ERMOD_W_MBIN)) e.warn_bin_firsttime = false;
   if (s.err_key != kNoError) {
@@ -1007,6 +1004,14 @@ int ermod_sync(ermod_ctx* c) {
   }
   if (s.range_fault) return ERMOD_E_DEVICE;
   return ERMOD_OK;
+}
+
+int ermod_sync(ermod_ctx* c) {
+  if (!c) return fail_param("null context");
+  Engine& e = c->e;
+  cudaSetDevice(e.device);
+  ERMOD_CUDA(cudaStreamSynchronize(e.stream));
+  return decode_status(e);
 }
 
 int ermod_placements_device(ermod_ctx* c, int nplace, const int* tag_d, const double* sol_d, const double* sws_d,
@@ -1291,6 +1296,145 @@ int ermod_ecorr_add_noalloc(const int* hist, const double* weight, int nplace, i
                                                (cudaStream_t)stream);
   if (err != cudaSuccess) return fail_cuda(err, "ermod_ecorr_add_noalloc");
   return ERMOD_OK;
+}
+
+// ---- several systems in one CUDA graph --------------------------------------------
+struct ermod_graph {
+  int device = 0;
+  std::vector<ermod_ctx*> ctx;
+  std::vector<cudaStream_t> fork;  // one capture stream per system
+  cudaStream_t origin = nullptr;
+  cudaEvent_t ev_fork = nullptr;
+  std::vector<cudaEvent_t> ev_sys;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t launched = nullptr;
+};
+
+int ermod_graph_destroy(ermod_graph* g) {
+  if (!g) return ERMOD_OK;
+  cudaSetDevice(g->device);
+  if (g->exec) cudaStreamSynchronize(g->launched);
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  for (cudaEvent_t ev : g->ev_sys)
+    if (ev) cudaEventDestroy(ev);
+  if (g->ev_fork) cudaEventDestroy(g->ev_fork);
+  for (cudaStream_t st : g->fork)
+    if (st) cudaStreamDestroy(st);
+  if (g->origin) cudaStreamDestroy(g->origin);
+  delete g;
+  return ERMOD_OK;
+}
+
+int ermod_graph_create(int nctx, ermod_ctx* const* ctx, const double* const* sitepos_d, const double* cells,
+                       const double* stat_weight_system, const int* nplace, const int* solute_mol,
+                       const int* const* tag_d, const double* const* sol_d, const double* const* sws_d,
+                       ermod_graph** out) {
+  if (!out || nctx <= 0 || !ctx || !sitepos_d || !cells || !nplace || !solute_mol || !tag_d)
+    return fail_param("null argument or no systems");
+  *out = nullptr;
+  const int device = ctx[0] ? ctx[0]->e.device : 0;
+  for (int i = 0; i < nctx; ++i) {
+    if (!ctx[i] || !sitepos_d[i] || (nplace[i] > 0 && !tag_d[i])) return fail_param("null context or input");
+    Engine& e = ctx[i]->e;
+    if (e.device != device) return fail_param("all systems of a graph need the same device");
+    if (!e.mixed) {
+      g_err = "graph capture runs the mixed-precision path only";
+      return ERMOD_E_UNSUPPORTED;
+    }
+    if (!e.topo_ready || !e.bins_ready || !e.frame_ready || !e.buf.u_nsite)
+      return fail_param("every system needs one ordinary frame + placements step before capture");
+    if (solute_mol[i] < 1 || solute_mol[i] > e.nummol) return fail_param("solute_mol out of range");
+    if (e.numsite[solute_mol[i] - 1] > kMaxSoluteSites) {
+      g_err = "solute larger than 256 sites";
+      return ERMOD_E_UNSUPPORTED;
+    }
+    if (e.P.slttype != 1 && nplace[i] > 0 && !(sol_d && sol_d[i]))
+      return fail_param("reference mode needs solute_sitepos");
+  }
+  cudaSetDevice(device);
+  ermod_graph* g = new ermod_graph();
+  g->device = device;
+  g->ctx.assign(ctx, ctx + nctx);
+  g->fork.assign(nctx, nullptr);
+  g->ev_sys.assign(nctx, nullptr);
+  cudaError_t err;
+#define ERMOD_G(call)                        \
+  do {                                       \
+    if ((err = (call)) != cudaSuccess) {     \
+      const int st_ = fail_cuda(err, #call); \
+      ermod_graph_destroy(g);                \
+      return st_;                            \
+    }                                        \
+  } while (0)
+  ERMOD_G(cudaStreamCreateWithFlags(&g->origin, cudaStreamNonBlocking));
+  ERMOD_G(cudaEventCreateWithFlags(&g->ev_fork, cudaEventDisableTiming));
+  for (int i = 0; i < nctx; ++i) {
+    ERMOD_G(cudaStreamCreateWithFlags(&g->fork[i], cudaStreamNonBlocking));
+    ERMOD_G(cudaEventCreateWithFlags(&g->ev_sys[i], cudaEventDisableTiming));
+  }
+  // every context finishes its queued work before its streams join the capture
+  for (int i = 0; i < nctx; ++i) ERMOD_G(cudaStreamSynchronize(ctx[i]->e.stream));
+  ERMOD_G(cudaStreamBeginCapture(g->origin, cudaStreamCaptureModeThreadLocal));
+  int st = ERMOD_OK;
+  if ((err = cudaEventRecord(g->ev_fork, g->origin)) != cudaSuccess) st = fail_cuda(err, "fork");
+  for (int i = 0; i < nctx && st == ERMOD_OK; ++i) {
+    Engine& e = ctx[i]->e;
+    const cudaStream_t saved = e.stream;
+    const bool saved_timing = e.timing;
+    e.stream = g->fork[i];
+    e.timing = false;
+    if ((err = cudaStreamWaitEvent(e.stream, g->ev_fork, 0)) != cudaSuccess) st = fail_cuda(err, "fork");
+    if (st == ERMOD_OK)
+      st = frame_common(e, cells + 9 * (size_t)i, stat_weight_system ? stat_weight_system[i] : 1.0);
+    if (st == ERMOD_OK &&
+        (err = cudaMemcpyAsync(e.d_sitepos, sitepos_d[i], sizeof(double) * 3 * e.numatm, cudaMemcpyDeviceToDevice,
+                               e.stream)) != cudaSuccess)
+      st = fail_cuda(err, "frame copy");
+    if (st == ERMOD_OK) st = frame_launch(e);
+    if (st == ERMOD_OK && nplace[i] > 0) st = reset_status(e);
+    if (st == ERMOD_OK && nplace[i] > 0)
+      st = run_placements(e, nplace[i], tag_d[i], sol_d ? sol_d[i] : nullptr, sws_d ? sws_d[i] : nullptr, nullptr,
+                          nullptr, e.numsite[solute_mol[i] - 1]);
+    if (st == ERMOD_OK && (err = cudaEventRecord(g->ev_sys[i], e.stream)) != cudaSuccess) st = fail_cuda(err, "join");
+    if (st == ERMOD_OK && (err = cudaStreamWaitEvent(g->origin, g->ev_sys[i], 0)) != cudaSuccess)
+      st = fail_cuda(err, "join");
+    e.stream = saved;
+    e.timing = saved_timing;
+  }
+  cudaGraph_t graph = nullptr;
+  err = cudaStreamEndCapture(g->origin, &graph);
+  g->graph = graph;
+  if (st != ERMOD_OK) {
+    ermod_graph_destroy(g);
+    return st;
+  }
+  ERMOD_G(err);
+  ERMOD_G(cudaGraphInstantiate(&g->exec, g->graph, 0));
+#undef ERMOD_G
+  *out = g;
+  return ERMOD_OK;
+}
+
+int ermod_graph_launch(ermod_graph* g, void* stream) {
+  if (!g || !g->exec) return fail_param("null graph");
+  cudaSetDevice(g->device);
+  g->launched = (cudaStream_t)stream;
+  ERMOD_CUDA(cudaGraphLaunch(g->exec, g->launched));
+  return ERMOD_OK;
+}
+
+int ermod_graph_sync(ermod_graph* g) {
+  if (!g) return fail_param("null graph");
+  cudaSetDevice(g->device);
+  ERMOD_CUDA(cudaStreamSynchronize(g->launched));
+  int first = ERMOD_OK;
+  for (ermod_ctx* c : g->ctx) {
+    const int st = decode_status(c->e);
+    if (st != ERMOD_OK && first == ERMOD_OK) first = st;
+  }
+  return first;
 }
 
 }  // extern "C"

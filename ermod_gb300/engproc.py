@@ -36,6 +36,7 @@ class EnergyRepresentation:
         p.count_mirror = 1 if count_mirror else 0
         self.params = dict(params)
         self.precision = precision
+        self.device = int(device)
         self.ctx = C.c_void_p()
         check(L.ermod_create(C.byref(p), int(device), C.byref(self.ctx)), "ermod_create")
         self.set_topology(topo)

@@ -182,6 +182,36 @@ int ermod_adjoint_enable(ermod_ctx* ctx, int solute_mol, int cmbrule);
 /* grad: [3 nsite][ermax] (parameter-major), weight: [ermax]; *nparam = 3 nsite. */
 int ermod_adjoint_get(ermod_ctx* ctx, double* grad, double* weight, int* nparam);
 
+/* ---- several systems in one CUDA graph ------------------------------------------------
+ * One step of nctx systems of uneven size (ermod_frame_device + ermod_placements_device
+ * of each context: device coordinates sitepos_d[i], cell cells[9 i .. 9 i + 8], weight
+ * stat_weight_system[i] (NULL: 1), nplace[i] placements of molecule solute_mol[i] with
+ * device tags tag_d[i], solute coordinates sol_d[i] and weights sws_d[i] (NULL entries
+ * allowed as in ermod_placements_device)) recorded once into a CUDA graph in which the
+ * systems run concurrently, each with its own streams; ermod_graph_launch replays the
+ * whole step as one launch.  This replaces, for a set of independent systems, the
+ * per-system frame loop of enganal (enganal.F90:91-94) driving engconst.
+ * Contract:
+ *   - mixed precision only; every context has run one ordinary frame + placements step
+ *     (its buffers and kernel attributes exist) and has no work queued;
+ *   - the graph keeps device addresses and the host-side values given here (cells,
+ *     counts, solute sizes); a launch reads whatever the device buffers hold, so new
+ *     coordinates are written into the same buffers between launches; a new cell or
+ *     count needs a new graph;
+ *   - accumulators keep accumulating over launches (ermod_clear / ermod_get_accum as
+ *     usual, between launches after ermod_graph_sync). */
+typedef struct ermod_graph ermod_graph;
+int ermod_graph_create(int nctx, ermod_ctx* const* ctx, const double* const* sitepos_d, const double* cells,
+                       const double* stat_weight_system, const int* nplace, const int* solute_mol,
+                       const int* const* tag_d, const double* const* sol_d, const double* const* sws_d,
+                       ermod_graph** out);
+/* Asynchronous on stream (a cudaStream_t; NULL: legacy default stream). */
+int ermod_graph_launch(ermod_graph* g, void* stream);
+/* Waits for the last launch; returns the first nonzero status of the systems in order
+ * (as ermod_sync would for each; ermod_error_info on that context locates it). */
+int ermod_graph_sync(ermod_graph* g);
+int ermod_graph_destroy(ermod_graph* g);
+
 /* ---- host-side set-up helpers (the reference's own set-up arithmetic) -------------- */
 
 /* enginit's energy coordinate for one species (engproc.F90:163-218).
