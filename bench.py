@@ -338,10 +338,136 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def _timed(fn, steps, warmup, stream):
+    """CUDA-event time (ms) of `steps` calls of fn(i) after `warmup` calls, on stream."""
+    import torch
+    for i in range(warmup):
+        fn(i)
+    torch.cuda.synchronize()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for k in range(steps):
+        fn(warmup + k)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    return t0.elapsed_time(t1)
+
+
+def run_uneven(args):
+    """16 water systems of uneven size (2k-60k waters), each with its own solute, grid and
+    insertion count, one step of all of them replayed as one CUDA graph launch; the batch
+    (placements per PME launch) of every system picked by the autotuner."""
+    import torch
+    from ermod_gb300 import build, setconf, synth
+    from ermod_gb300.engproc import EnergyRepresentation
+    from ermod_gb300.multisystem import SystemGraph, autotune_batch
+    build.build()
+    torch.cuda.set_device(0)
+    systems = synth.uneven()
+    engines, tops, frames, places, batches = [], [], [], [], []
+    for w in systems:
+        topo = setconf.setparam_topology(w.species(), slttype=2)
+        bins = setconf.enginit_bins(topo["numslv"], w.hist)
+        f0, f1 = w.frame(0), w.frame(1)
+        p0, p1 = w.placements(0), w.placements(1)
+        B = autotune_batch(w.params, topo, bins, f0, p0[:256], topo["nummol"], candidates=(16, 32, 64))
+        eng = EnergyRepresentation(w.params, topo, bins, precision="mixed", batch=B)
+        eng.frame(*f0)
+        eng.placements(np.full(len(p0), topo["nummol"], np.int32), p0)
+        engines.append(eng)
+        tops.append(topo)
+        frames.append(f1)
+        places.append(p1)
+        batches.append(B)
+    g = SystemGraph(engines, frames, places, [t["nummol"] for t in tops])
+    stream = torch.cuda.Stream()
+
+    def step(i):
+        g.launch(stream.cuda_stream)
+
+    with ClockSampler(0) as clk:
+        ms = _timed(step, args.steps, args.warmup, stream)
+    g.sync()
+    units = sum(w.ins_per_frame * w.nwater for w in systems) * args.steps
+    line = {"metric": "solute-solvent molecule energies/s", "value": units / (ms / 1e3),
+            "unit": "molecule-energies/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": "uneven: 16 systems, 2k-60k waters, own solutes (6-40 sites), grids and "
+                                   "1k-20k insertions, one CUDA graph launch per step",
+                       "systems": [{"waters": w.nwater, "K": w.params["ms1max"], "insertions": w.ins_per_frame,
+                                    "solute_sites": len(w.solute["charge"]), "batch": b}
+                                   for w, b in zip(systems, batches)]},
+            "clocks": clk.summary()}
+    print(json.dumps(line))
+    g.close()
+    for e in engines:
+        e.close()
+
+
+def run_adjoint(args):
+    """Solution mode of 8,000 waters with a 16-site solute (PME 64^3): frames per second of
+    the energies plus the bin-resolved derivatives for all 48 solute parameters."""
+    import torch
+    from ermod_gb300 import build, setconf, synth
+    from ermod_gb300.engproc import EnergyRepresentation
+    build.build()
+    torch.cuda.set_device(0)
+    w = synth.soln_adjoint(frames=args.warmup + args.steps)
+    topo = setconf.setparam_topology(w.species(), slttype=1)
+    bins = setconf.enginit_bins(topo["numslv"])
+    dev = torch.device("cuda", 0)
+    nsteps = args.warmup + args.steps
+    pos_d = [torch.from_numpy(w.frame(i)[0]).to(dev) for i in range(nsteps)]
+    cell = w.frame(0)[1]
+    tag_d = torch.tensor([topo["nummol"]], dtype=torch.int32, device=dev)
+    rates = {}
+    for adj in (False, True):
+        eng = EnergyRepresentation(w.params, topo, bins, precision="mixed")
+        if adj:
+            eng.adjoint_enable()
+        stream = torch.cuda.Stream()
+        eng.set_stream(stream.cuda_stream)
+
+        def step(i):
+            eng.frame_device(pos_d[i].data_ptr(), cell)
+            eng.placements_device(1, tag_d.data_ptr())
+
+        ms = _timed(step, args.steps, args.warmup, stream)
+        eng.sync()
+        rates[adj] = ms / args.steps
+        eng.close()
+    units = w.nwater * args.steps
+    line = {"metric": "solute-solvent molecule energies/s", "value": units / (rates[True] * args.steps / 1e3),
+            "unit": "molecule-energies/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": rates[True], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": "soln_adjoint: 8000 waters, 62 A box, 16-site solute, PME 64^3, "
+                                   "48 parameters, one frame per step"},
+            "ms_per_frame_without_adjoint": rates[False]}
+    if not args.no_cpu:
+        from oracle import oracle as O
+        O.build()
+        orc = O.Oracle(w.params, topo, bins)
+        pos, cl = w.frame(0)
+        t0 = time.perf_counter()
+        orc.frame(pos, cl)
+        orc.placements([topo["nummol"]])
+        orc.adjoint(topo["nummol"])
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": w.nwater / dt, "unit": "molecule-energies/s", "cores": os.cpu_count(),
+                                "kind": "port", "sample": "1 frame: energies + analytic FP64 derivatives"}
+    print(json.dumps(line))
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "uneven":
+        run_uneven(args)
+    elif args.workload == "soln_adjoint":
+        run_adjoint(args)
     else:
         run_ours(args)
 

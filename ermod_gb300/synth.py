@@ -210,8 +210,12 @@ def uneven(seed: int = 4):
         K = fft_friendly(int(math.ceil(box / 1.0)))
         lat = int(math.ceil(n ** (1.0 / 3.0)))
         sol = random_solute(rng, nsite)
+        # gen_input's --minenergy: solutes of up to 40 charged sites bind some waters
+        # below the default -20 kcal/mol first edge, which the reference stops on (eng_min)
+        hist = dict(ecdmin=-200.0, ecfmns=-0.20, ecdcen=0.0, eccore=20.0, ecdmax=1.0e11,
+                    eclbin=5.0e-2, ecfbin=2.0e-3, ec0bin=2.0e-4, finfac=10.0, pecore=200)
         out.append(Workload(f"uneven_{s}", "refs", box, n, sol, _params(2, K, corrcal=1, wgtslf=1),
-                            seed * 100 + s, 1, ins, lat))
+                            seed * 100 + s, 1, ins, lat, hist=hist))
     return out
 
 
