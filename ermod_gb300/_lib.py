@@ -43,7 +43,8 @@ EXPORTS = [
     "ermod_timing_enable", "ermod_timing_reset", "ermod_timing_get", "ermod_last_error_string",
     "ermod_status_string", "ermod_enginit_species", "ermod_getscrn", "ermod_lj_tables", "ermod_engstore_merge",
     "ermod_ecorr_add_noalloc", "ermod_adjoint_enable", "ermod_adjoint_get", "ermod_graph_create",
-    "ermod_graph_launch", "ermod_graph_sync", "ermod_graph_destroy",
+    "ermod_graph_launch", "ermod_graph_sync", "ermod_graph_destroy", "ermod_write_engdist",
+    "ermod_write_selfdist", "ermod_write_corr", "ermod_write_uvrange", "ermod_format_g",
 ]
 
 _lib = None
@@ -96,6 +97,11 @@ def load(path: str = LIB_PATH):
     L.ermod_graph_launch.argtypes = [vp, vp]
     L.ermod_graph_sync.argtypes = [vp]
     L.ermod_graph_destroy.argtypes = [vp]
+    L.ermod_write_engdist.argtypes = [C.c_char_p, C.c_int, ip, ip, dp, dp]
+    L.ermod_write_selfdist.argtypes = [C.c_char_p, C.c_int, dp, dp]
+    L.ermod_write_corr.argtypes = [C.c_char_p, C.c_int, dp]
+    L.ermod_write_uvrange.argtypes = [C.c_char_p, C.c_int, dp, dp]
+    L.ermod_format_g.argtypes = [C.c_double, C.c_int, C.c_int, C.c_char_p, C.c_int]
     _lib = L
     return L
 

@@ -5,11 +5,14 @@
 //   ermod_getscrn           Ewald screening from ewtoler (setconf.F90:515-535)
 //   ermod_lj_tables         LJ type deduplication + combination rules (setconf.F90:720-823)
 //   ermod_engstore_merge    engstore's rank merge and normalisation (engproc.F90:475-560)
+//   ermod_write_*           engstore's output files (engproc.F90:594-657), readable by slvfe
 #include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
-#include <vector>
-
 #include <string>
+#include <vector>
 
 #include "../../include/ermod_gpu.h"
 
@@ -31,9 +34,142 @@ double ipow(double x, int e) {  // x**e for a constant integer exponent, binary 
   }
   return r;
 }
+// Fortran Gw.d output (no exponent width) with gfortran's conventions: values whose
+// magnitude, rounded to d significant digits, lies in [0.1, 10^d) are written as
+// F(w-4).(d-s) followed by 4 blanks (s = digits before the point); zero as
+// F(w-4).(d-1) + 4 blanks; anything else as Ew.d, 0.ddd..E+xx (3-digit exponents
+// drop the E).  The digits come from the C library's correctly rounded conversion.
+std::string fortran_g(double x, int w, int d) {
+  char buf[128];
+  if (x == 0.0) {
+    std::snprintf(buf, sizeof buf, "%*.*f    ", w - 4, d - 1, x);
+    return buf;
+  }
+  std::snprintf(buf, sizeof buf, "%.*e", d - 1, std::fabs(x));
+  const char* ep = std::strchr(buf, 'e');
+  const int e10 = std::atoi(ep + 1);
+  if (e10 >= -1 && e10 <= d - 1) {
+    const int s = e10 + 1;
+    std::snprintf(buf, sizeof buf, "%*.*f    ", w - 4, d - s, x);
+    return buf;
+  }
+  std::string digits;
+  for (const char* c = buf; c < ep; ++c)
+    if (*c >= '0' && *c <= '9') digits += *c;
+  const int ex = e10 + 1;  // 0.d1d2... x 10^ex
+  char tail[16];
+  if (std::abs(ex) <= 99)
+    std::snprintf(tail, sizeof tail, "E%c%02d", ex < 0 ? '-' : '+', std::abs(ex));
+  else
+    std::snprintf(tail, sizeof tail, "%c%03d", ex < 0 ? '-' : '+', std::abs(ex));
+  std::string body = std::string(x < 0 ? "-" : "") + "0." + digits + tail;
+  if ((int)body.size() > w) body.erase(x < 0 ? 1 : 0, 1);  // drop the optional leading zero
+  if ((int)body.size() < w) body.insert(0, (size_t)(w - body.size()), ' ');
+  return body;
+}
+
+// repval('intn') (engproc.F90:1185-1223): the representative energy of bin iduv (0-based)
+double repval_intn(int iduv, int numslv, const int* uvmax, const int* uvsoft, const double* uvcrd, int* spec) {
+  int idmin = 0, cnt = 0;
+  for (cnt = 0; cnt < numslv; ++cnt) {
+    if (iduv < idmin + uvmax[cnt]) break;
+    idmin += uvmax[cnt];
+  }
+  if (cnt == numslv) cnt = numslv - 1;
+  *spec = cnt + 1;
+  const int idpt = iduv - idmin + 1;  // 1-based within the species
+  if (idpt <= uvsoft[cnt]) return (uvcrd[iduv] + uvcrd[iduv + 1]) / 2.0;
+  if (idpt < uvmax[cnt]) return std::sqrt(uvcrd[iduv] * uvcrd[iduv + 1]);
+  return uvcrd[iduv];
+}
+
 }  // namespace
 
 extern "C" {
+
+int ermod_format_g(double x, int w, int d, char* out, int cap) {
+  if (!out || w <= 4 || d <= 0 || cap <= w) return ERMOD_E_PARAM;
+  const std::string s = fortran_g(x, w, d);
+  std::snprintf(out, (size_t)cap, "%s", s.c_str());
+  return ERMOD_OK;
+}
+
+int ermod_write_engdist(const char* path, int numslv, const int* uvmax, const int* uvsoft, const double* uvcrd,
+                        const double* edens) {
+  if (!path || numslv <= 0 || !uvmax || !uvsoft || !uvcrd || !edens) return ERMOD_E_PARAM;
+  int ermax = 0;
+  for (int i = 0; i < numslv; ++i) ermax += uvmax[i];
+  std::FILE* f = std::fopen(path, "w");
+  if (!f) {
+    ermod::set_error_string(std::string("cannot open ") + path);
+    return ERMOD_E_PARAM;
+  }
+  for (int iduv = 0; iduv < ermax; ++iduv) {  // '(g15.7,i5,g25.15)'
+    int pti = 0;
+    const double factor = repval_intn(iduv, numslv, uvmax, uvsoft, uvcrd, &pti);
+    std::fprintf(f, "%s%5d%s\n", fortran_g(factor, 15, 7).c_str(), pti, fortran_g(edens[iduv], 25, 15).c_str());
+  }
+  return std::fclose(f) == 0 ? ERMOD_OK : ERMOD_E_PARAM;
+}
+
+int ermod_write_selfdist(const char* path, int esmax, const double* escrd, const double* eself) {
+  if (!path || esmax <= 0 || !escrd || !eself) return ERMOD_E_PARAM;
+  std::FILE* f = std::fopen(path, "w");
+  if (!f) {
+    ermod::set_error_string(std::string("cannot open ") + path);
+    return ERMOD_E_PARAM;
+  }
+  for (int iduv = 0; iduv < esmax; ++iduv) {  // repval('self'), '(g15.7,g25.15)'
+    const double factor = (iduv + 1 < esmax) ? (escrd[iduv] + escrd[iduv + 1]) / 2.0 : escrd[esmax - 1];
+    std::fprintf(f, "%s%s\n", fortran_g(factor, 15, 7).c_str(), fortran_g(eself[iduv], 25, 15).c_str());
+  }
+  return std::fclose(f) == 0 ? ERMOD_OK : ERMOD_E_PARAM;
+}
+
+int ermod_write_corr(const char* path, int ermax, const double* ecorr) {
+  if (!path || ermax <= 0 || !ecorr) return ERMOD_E_PARAM;
+  const uint64_t bytes = (uint64_t)ermax * (uint64_t)ermax * sizeof(double);
+  if (bytes > 2147483639ull) {  // one record, one 4-byte marker each side
+    ermod::set_error_string("ecorr larger than one 2 GiB unformatted record");
+    return ERMOD_E_UNSUPPORTED;
+  }
+  std::FILE* f = std::fopen(path, "wb");
+  if (!f) {
+    ermod::set_error_string(std::string("cannot open ") + path);
+    return ERMOD_E_PARAM;
+  }
+  const uint32_t mk = (uint32_t)bytes;
+  unsigned char m[4] = {(unsigned char)(mk & 0xff), (unsigned char)((mk >> 8) & 0xff),
+                        (unsigned char)((mk >> 16) & 0xff), (unsigned char)(mk >> 24)};  // little endian
+  bool ok = std::fwrite(m, 1, 4, f) == 4;
+  for (size_t i = 0; ok && i < (size_t)ermax * ermax; ++i) {
+    uint64_t v;
+    std::memcpy(&v, &ecorr[i], 8);
+    unsigned char b[8];
+    for (int k = 0; k < 8; ++k) b[k] = (unsigned char)((v >> (8 * k)) & 0xff);
+    ok = std::fwrite(b, 1, 8, f) == 8;
+  }
+  ok = ok && std::fwrite(m, 1, 4, f) == 4;
+  return (std::fclose(f) == 0 && ok) ? ERMOD_OK : ERMOD_E_PARAM;
+}
+
+int ermod_write_uvrange(const char* path, int numslv, const double* minuv, const double* maxuv) {
+  if (!path || numslv <= 0 || !minuv || !maxuv) return ERMOD_E_PARAM;
+  std::FILE* f = std::fopen(path, "w");
+  if (!f) {
+    ermod::set_error_string(std::string("cannot open ") + path);
+    return ERMOD_E_PARAM;
+  }
+  std::fprintf(f, " species     minimum        maximum\n");
+  for (int pti = 0; pti <= numslv; ++pti) {
+    if (maxuv[pti] < 1.0e5)  // '(i5,2f15.5)'
+      std::fprintf(f, "%5d%15.5f%15.5f\n", pti, minuv[pti], maxuv[pti]);
+    else  // '(i5,f15.5,g18.5)'
+      std::fprintf(f, "%5d%15.5f%s\n", pti, minuv[pti], fortran_g(maxuv[pti], 18, 5).c_str());
+  }
+  return std::fclose(f) == 0 ? ERMOD_OK : ERMOD_E_PARAM;
+}
+
 
 int ermod_enginit_species(const double* hist, int pecore, int large, double* ercrd_out, int* pemax_out,
                           int* pesoft_out) {

@@ -50,3 +50,47 @@ def merge_distributed(acc: dict, slttype: int, wgtslf: int, temp: float, group=N
     if rank != 0:
         return None
     return merge(gathered, slttype, wgtslf, temp)
+
+
+def write_outputs(directory: str, merged: dict, bins: dict, slttype: int, corrcal: int, selfcal: int,
+                  suffix: str = ".tt") -> list:
+    """engstore's files from merged accumulators (engproc.F90:594-657): engsln/engref,
+    corsln/corref (corrcal), slfeng (selfcal), uvrange.tt.  Returns the paths written."""
+    import os
+    L = _lib.load()
+    soln = int(slttype) == 1
+    paths = []
+
+    def path(name):
+        p = os.path.join(directory, name)
+        paths.append(p)
+        return p.encode()
+
+    uvmax = np.ascontiguousarray(bins["uvmax"], np.int32)
+    uvsoft = np.ascontiguousarray(bins["uvsoft"], np.int32)
+    uvcrd = np.ascontiguousarray(bins["uvcrd"], np.float64)
+    edens = np.ascontiguousarray(merged["edens"], np.float64)
+    _lib.check(L.ermod_write_engdist(path(("engsln" if soln else "engref") + suffix), len(uvmax), _lib.ip(uvmax),
+                                     _lib.ip(uvsoft), _lib.dp(uvcrd), _lib.dp(edens)), "ermod_write_engdist")
+    if corrcal and merged.get("ecorr") is not None:
+        ec = np.asfortranarray(merged["ecorr"], np.float64).ravel(order="F").copy()
+        _lib.check(L.ermod_write_corr(path(("corsln" if soln else "corref") + suffix), len(edens), _lib.dp(ec)),
+                   "ermod_write_corr")
+    if selfcal and merged.get("eself") is not None and len(merged["eself"]):
+        es = np.ascontiguousarray(merged["eself"], np.float64)
+        escrd = np.ascontiguousarray(bins["escrd"], np.float64)
+        _lib.check(L.ermod_write_selfdist(path("slfeng" + suffix), len(es), _lib.dp(escrd), _lib.dp(es)),
+                   "ermod_write_selfdist")
+    mn = np.ascontiguousarray(merged["minuv"], np.float64)
+    mx = np.ascontiguousarray(merged["maxuv"], np.float64)
+    _lib.check(L.ermod_write_uvrange(path("uvrange.tt"), len(mn) - 1, _lib.dp(mn), _lib.dp(mx)),
+               "ermod_write_uvrange")
+    return paths
+
+
+def format_g(x: float, w: int, d: int) -> str:
+    """The Fortran Gw.d field the writers produce."""
+    import ctypes as C
+    buf = C.create_string_buffer(w + 8)
+    _lib.check(_lib.load().ermod_format_g(float(x), int(w), int(d), buf, w + 8), "ermod_format_g")
+    return buf.value.decode()

@@ -253,6 +253,26 @@ int ermod_engstore_merge(int nrank, int slttype, int wgtslf, double temp, int er
 int ermod_ecorr_add_noalloc(const int* hist, const double* weight, int nplace, int ermax,
                             double* ecorr, int64_t* ecorr_count, void* stream);
 
+/* ---- engstore's output files (engproc.F90:594-657), for slvfe ------------------------
+ * Written from merged, normalised accumulators (ermod_engstore_merge) in the
+ * reference's layouts, with gfortran's edit conventions:
+ *   engsln.xx / engref.xx  per bin '(g15.7,i5,g25.15)': repval('intn') energy
+ *                          (engproc.F90:1185-1223), species, edens;
+ *   slfeng.xx              per bin '(g15.7,g25.15)': repval('self'), eself;
+ *   corsln.xx / corref.xx  one unformatted sequential record of ecorr(ermax, ermax)
+ *                          (column major, little-endian 4-byte length markers);
+ *   uvrange.tt             ' species     minimum        maximum' then '(i5,2f15.5)'
+ *                          (or '(i5,f15.5,g18.5)' for maxuv >= 1e5) per species 0..numslv.
+ * slvfe reads the text files list-directed and the record with one unformatted read
+ * (slvfe.F90:466-488). */
+int ermod_write_engdist(const char* path, int numslv, const int* uvmax, const int* uvsoft, const double* uvcrd,
+                        const double* edens);
+int ermod_write_selfdist(const char* path, int esmax, const double* escrd, const double* eself);
+int ermod_write_corr(const char* path, int ermax, const double* ecorr);
+int ermod_write_uvrange(const char* path, int numslv, const double* minuv, const double* maxuv);
+/* The Gw.d field the writers use, into out (cap bytes, cap > w). */
+int ermod_format_g(double x, int w, int d, char* out, int cap);
+
 #ifdef __cplusplus
 }
 #endif
