@@ -36,6 +36,12 @@ class Params(C.Structure):
     ]
 
 
+class InsertParams(C.Structure):
+    _fields_ = [("insposition", C.c_int32), ("insorient", C.c_int32), ("insorigin", C.c_int32),
+                ("pad_", C.c_int32), ("lwreg", C.c_double), ("upreg", C.c_double), ("seed", C.c_uint64),
+                ("offset", C.c_uint64)]
+
+
 EXPORTS = [
     "ermod_default_params", "ermod_create", "ermod_destroy", "ermod_set_stream", "ermod_set_topology",
     "ermod_set_bins", "ermod_frame", "ermod_frame_device", "ermod_placements", "ermod_placements_device",
@@ -45,6 +51,7 @@ EXPORTS = [
     "ermod_ecorr_add_noalloc", "ermod_adjoint_enable", "ermod_adjoint_get", "ermod_graph_create",
     "ermod_graph_launch", "ermod_graph_sync", "ermod_graph_destroy", "ermod_write_engdist",
     "ermod_write_selfdist", "ermod_write_corr", "ermod_write_uvrange", "ermod_format_g",
+    "ermod_generate_placements",
 ]
 
 _lib = None
@@ -102,6 +109,7 @@ def load(path: str = LIB_PATH):
     L.ermod_write_corr.argtypes = [C.c_char_p, C.c_int, dp]
     L.ermod_write_uvrange.argtypes = [C.c_char_p, C.c_int, dp, dp]
     L.ermod_format_g.argtypes = [C.c_double, C.c_int, C.c_int, C.c_char_p, C.c_int]
+    L.ermod_generate_placements.argtypes = [vp, C.c_int, C.c_int, dp, dp, C.POINTER(InsertParams), vp, vp]
     _lib = L
     return L
 

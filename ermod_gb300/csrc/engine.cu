@@ -473,6 +473,7 @@ int ermod_destroy(ermod_ctx* c) {
   cudaSetDevice(e.device);
   if (e.stream) cudaStreamSynchronize(e.stream);
   free_adjoint(e);
+  dfree(e.d_ins);
   free_batch(e);
   free_frame(e);
   free_topology(e);
@@ -1295,6 +1296,28 @@ int ermod_ecorr_add_noalloc(const int* hist, const double* weight, int nplace, i
   const cudaError_t err = launch_ecorr_noalloc(hist, weight, nplace, ermax, ecorr, (long long*)ecorr_count,
                                                (cudaStream_t)stream);
   if (err != cudaSuccess) return fail_cuda(err, "ermod_ecorr_add_noalloc");
+  return ERMOD_OK;
+}
+
+int ermod_generate_placements(ermod_ctx* c, int nplace, int nsite, const double* bfcoord, const double* mass,
+                              const ermod_insert_params* ip, double* sol_d, double* sws_d) {
+  if (!c || !bfcoord || !mass || !ip || (nplace > 0 && !sol_d)) return fail_param("null argument");
+  Engine& e = c->e;
+  if (!e.frame_ready) return fail_param("ermod_frame must come first (its cell is used)");
+  if (nsite < 1 || nsite > kMaxSoluteSites) return fail_param("nsite must be 1..256");
+  if (ip->insposition < 0 || ip->insposition > 6 || ip->insorient < 0 || ip->insorient > 1 || ip->insorigin < 0 ||
+      ip->insorigin > 1)
+    return fail_param("insposition 0..6, insorient 0..1, insorigin 0..1");
+  if ((ip->insposition == 2 || ip->insposition == 3 || ip->insposition == 4) && !(ip->upreg >= ip->lwreg))
+    return fail_param("upreg < lwreg");
+  if ((ip->insposition == 5 || ip->insposition == 6) && !(ip->upreg > 0.0)) return fail_param("upreg must be > 0");
+  if (nplace <= 0) return ERMOD_OK;
+  cudaSetDevice(e.device);
+  if (!e.d_ins) ERMOD_CUDA(dalloc(&e.d_ins, 4 * (size_t)kMaxSoluteSites));
+  ERMOD_CUDA(cudaMemcpyAsync(e.d_ins, bfcoord, sizeof(double) * 3 * nsite, cudaMemcpyHostToDevice, e.stream));
+  ERMOD_CUDA(cudaMemcpyAsync(e.d_ins + 3 * kMaxSoluteSites, mass, sizeof(double) * nsite, cudaMemcpyHostToDevice,
+                             e.stream));
+  ERMOD_CUDA(launch_insert(e, nplace, nsite, *ip, e.d_ins, e.d_ins + 3 * kMaxSoluteSites, sol_d, sws_d));
   return ERMOD_OK;
 }
 

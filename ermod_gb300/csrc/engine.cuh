@@ -164,6 +164,7 @@ struct Engine {
   float* d_ps_qf = nullptr;      // [Bmax][256]
   float2* d_ps_bvec = nullptr;   // [Bmax][256][3][Kmax]
   double* d_ps_self = nullptr;   // [Bmax][K2]
+  double* d_ins = nullptr;       // [4][256] solute reference coordinates and masses (placement generator)
   bool tmap_ready = false;
 
   // ---- cuFFT -------------------------------------------------------------------------

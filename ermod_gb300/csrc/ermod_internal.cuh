@@ -145,6 +145,9 @@ cudaError_t launch_gather(Engine& e, const BatchArgs& a);
 // adjoint mode: bin-resolved solute-parameter derivatives of the batch's placements
 cudaError_t launch_adjoint(Engine& e, const BatchArgs& a, cudaStream_t s);
 size_t adjoint_cub_bytes(int n);
+// device placements (kernels_insert.cu)
+cudaError_t launch_insert(Engine& e, int nplace, int ns, const ermod_insert_params& ip, const double* bf_d,
+                          const double* mass_d, double* out, double* weight);
 // accumulation
 cudaError_t launch_accumulate(Engine& e, const BatchArgs& a, cudaStream_t s);
 cudaError_t launch_ecorr_flush(Engine& e, cudaStream_t s);

@@ -130,6 +130,35 @@ class EnergyRepresentation:
                     slnuv=slnuv, minuv=mn, maxuv=mx, engnorm=sc[0], engsmpl=sc[1], avslf=sc[2], voffset=sc[3],
                     voffset_initialized=bool(sc[4]))
 
+    # ---- placements generated on the device ----------------------------------------
+    def generate_placements(self, n: int, bfcoord, mass, insposition: int = 0, insorient: int = 0,
+                            insorigin: int = 0, lwreg: float = 0.0, upreg: float = 0.0, seed: int = 1,
+                            offset: int = 0, weights: bool = False):
+        """n placements of a solute with reference coordinates bfcoord (nsite, 3) and masses,
+        generated on the device in the cell of the last frame (insertion.F90 modes).
+        Returns torch tensors (placements (n, nsite, 3) float64, weights (n,) or None)."""
+        import torch
+        bf = np.ascontiguousarray(bfcoord, np.float64)
+        m = np.ascontiguousarray(mass, np.float64)
+        ns = len(m)
+        dev = torch.device("cuda", self.device)
+        sol = torch.empty((n, ns, 3), dtype=torch.float64, device=dev)
+        sws = torch.empty(n, dtype=torch.float64, device=dev) if weights else None
+        torch.cuda.synchronize(dev)
+        ip = _lib.InsertParams(int(insposition), int(insorient), int(insorigin), 0, float(lwreg), float(upreg),
+                               int(seed), int(offset))
+        check(_lib.load().ermod_generate_placements(self.ctx, int(n), ns, _lib.dp(bf), _lib.dp(m), C.byref(ip),
+                                                    C.c_void_p(sol.data_ptr()),
+                                                    C.c_void_p(sws.data_ptr()) if weights else None),
+              "ermod_generate_placements")
+        self.sync_stream()
+        return sol, sws
+
+    def sync_stream(self):
+        """Wait for the context's stream (no status decode)."""
+        import torch
+        torch.cuda.synchronize(torch.device("cuda", self.device))
+
     # ---- adjoint mode ------------------------------------------------------------
     def adjoint_enable(self, solute_mol: int = None, cmbrule: int = 0):
         """Accumulate bin-resolved d u / d(q_s, eps_s, sigma_s) for placements of solute_mol

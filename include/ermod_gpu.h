@@ -253,6 +253,28 @@ int ermod_engstore_merge(int nrank, int slttype, int wgtslf, double temp, int er
 int ermod_ecorr_add_noalloc(const int* hist, const double* weight, int nplace, int ermax,
                             double* ecorr, int64_t* ecorr_count, void* stream);
 
+/* ---- placements generated on the device (instslt, insertion.F90:76-99) --------------
+ * insorigin 0: solute COM to the origin (1: as given); insposition 0 random in the cell,
+ * 1 as given, 2 spherical shell lwreg..upreg, 3 slab in z, 4 symmetric slab, 5 random
+ * translation within upreg + 3 x solute size, 6 uniform/Gaussian mixture with its
+ * weight (engmain.F90:320-326, insertion.F90:133-316); insorient 0: random rotation
+ * about the COM (rejection-sampled unit quaternion, q v q*), 1 none.  The random
+ * stream is counter-based (Philox4x32-10): placement p uses counter offset + p under
+ * key seed, so results do not depend on batching.  (The reference's Fortran
+ * random_number stream is compiler specific and is not reproduced.) */
+typedef struct ermod_insert_params {
+  int32_t insposition, insorient, insorigin, pad_;
+  double lwreg, upreg;
+  uint64_t seed, offset;
+} ermod_insert_params;
+/* Writes nplace placements of an nsite solute (bfcoord (3, nsite) and mass host arrays,
+ * the coordinates before insertion) into device sol_d (3, nsite, nplace) and, when not
+ * NULL, their weights into device sws_d (1 except insposition 6).  Uses the cell of the
+ * last ermod_frame*; asynchronous on the context's stream, ready for
+ * ermod_placements_device. */
+int ermod_generate_placements(ermod_ctx* ctx, int nplace, int nsite, const double* bfcoord, const double* mass,
+                              const ermod_insert_params* ip, double* sol_d, double* sws_d);
+
 /* ---- engstore's output files (engproc.F90:594-657), for slvfe ------------------------
  * Written from merged, normalised accumulators (ermod_engstore_merge) in the
  * reference's layouts, with gfortran's edit conventions:

@@ -1,0 +1,101 @@
+"""NumPy restatement of the device placement generator (test infrastructure): the
+Philox4x32-10 stream and the insertion.F90 placement steps, placement by placement."""
+import math
+
+import numpy as np
+
+M0, M1, W0, W1 = 0xD2511F53, 0xCD9E8D57, 0x9E3779B9, 0xBB67AE85
+MASK = 0xFFFFFFFF
+
+
+def philox4x32_10(ctr, key):
+    c0, c1, c2, c3 = ctr
+    k0, k1 = key
+    for _ in range(10):
+        p0, p1 = M0 * c0, M1 * c2
+        c0, c1, c2, c3 = ((p1 >> 32) ^ c1 ^ k0) & MASK, p1 & MASK, ((p0 >> 32) ^ c3 ^ k1) & MASK, p0 & MASK
+        k0, k1 = (k0 + W0) & MASK, (k1 + W1) & MASK
+    return c0, c1, c2, c3
+
+
+class Stream:
+    def __init__(self, seed, g):
+        self.key = (seed & MASK, (seed >> 32) & MASK)
+        self.c2, self.c3 = g & MASK, (g >> 32) & MASK
+        self.draw = 0
+        self.buf = []
+
+    def u32(self):
+        if not self.buf:
+            self.buf = list(philox4x32_10((self.draw, 0, self.c2, self.c3), self.key))
+            self.draw += 1
+        return self.buf.pop(0)
+
+    def uniform(self):
+        a, b = self.u32() >> 5, self.u32() >> 6
+        return (a * 67108864.0 + b) * (1.0 / 9007199254740992.0)
+
+
+def place(bf, mass, cell, p, insposition=0, insorient=0, insorigin=0, lwreg=0.0, upreg=0.0, seed=1, offset=0):
+    g = offset + p
+    rng = Stream(seed, g)
+    x = np.array(bf, dtype=float)
+    com = lambda y: (mass[:, None] * y).sum(0) / mass.sum()
+    if insorigin == 0:
+        x = x - com(x)
+    w = 1.0
+    shift = np.zeros(3)
+    if insposition == 0:
+        r = np.array([rng.uniform() for _ in range(3)])
+        shift = cell @ r - com(x)
+    elif insposition == 2:
+        t = rng.uniform()
+        t = (t * (upreg ** 3 - lwreg ** 3) + lwreg ** 3) ** (1.0 / 3.0)
+        for _ in range(256):
+            r = np.array([rng.uniform() * 2.0 - 1.0 for _ in range(3)])
+            n2 = float(r @ r)
+            if 0 < n2 <= 1:
+                break
+        shift = t * r / math.sqrt(n2)
+    elif insposition in (3, 4):
+        r = np.array([rng.uniform(), rng.uniform(), 0.0])
+        t = rng.uniform() * (upreg - lwreg) + lwreg
+        if insposition == 4 and rng.uniform() > 0.5:
+            t = -t
+        r[2] = t / np.linalg.norm(cell[:, 2])
+        shift = cell @ r
+    elif insposition == 5:
+        c = com(x)
+        movmax = upreg + 3.0 * math.sqrt(max(float(((x - c) ** 2).sum(1).max()), 0.0))
+        shift = np.array([movmax * (2.0 * rng.uniform() - 1.0) for _ in range(3)])
+    elif insposition == 6:
+        ls = np.linalg.norm(cell, axis=0) / 2.0 / upreg
+        z0 = 8 * ls.prod()
+        z1 = math.sqrt(math.pi) ** 3 * math.erf(ls[0]) * math.erf(ls[1]) * math.erf(ls[2])
+        if g % 2 == 0:
+            sc = np.array([(2 * rng.uniform() - 1) * ls[i] for i in range(3)])
+        else:
+            sc = np.zeros(3)
+            for i in range(3):
+                for _ in range(256):
+                    r1, r2 = 1 - rng.uniform(), rng.uniform()
+                    r = math.sqrt(-2 * math.log(r1)) * math.cos(2 * math.pi * r2) / math.sqrt(2.0)
+                    if abs(r) < ls[i]:
+                        break
+                sc[i] = r
+        w = w / (0.5 / z0 + 0.5 * math.exp(-float(sc @ sc)) / z1)
+        shift = cell @ (sc / (ls * 2))
+    x = x + shift
+    if insorient == 0:
+        for _ in range(256):
+            q = np.array([rng.uniform() * 2.0 - 1.0 for _ in range(4)])
+            n2 = float(q @ q)
+            if n2 < 1:
+                break
+        q = q / math.sqrt(n2)
+        c = com(x)
+        v = x - c
+        u = q[1:]
+        t = 2.0 * np.cross(u, v)
+        x = v + q[0] * t + np.cross(u, t) + c
+    return x, w

@@ -1,0 +1,59 @@
+"""Placements generated on the device (insertion.F90 modes, Philox4x32-10 stream).
+
+CPU: the NumPy restatement's Philox against the published Philox4x32-10 known-answer
+vectors.  GPU (marked gpu): the device generator against the restatement, placement by
+placement (|dx| <= 1e-11 A), rigid-body distances preserved, mode geometry."""
+import numpy as np
+import pytest
+
+from tests import insert_ref
+
+
+def test_philox_known_answers():
+    assert insert_ref.philox4x32_10((0, 0, 0, 0), (0, 0)) == (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)
+    assert insert_ref.philox4x32_10((0xFFFFFFFF,) * 4, (0xFFFFFFFF,) * 2) == \
+        (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)
+    assert insert_ref.philox4x32_10((0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344), (0xA4093822, 0x299F31D0)) == \
+        (0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", [dict(insposition=0), dict(insposition=2, lwreg=3.0, upreg=9.0),
+                                  dict(insposition=4, lwreg=2.0, upreg=6.0), dict(insposition=5, upreg=2.0),
+                                  dict(insposition=6, upreg=5.0), dict(insposition=1, insorient=1, insorigin=1)])
+def test_device_placements_match_restatement(gpu_lib, mode):
+    from ermod_gb300 import setconf, synth
+    from ermod_gb300.engproc import EnergyRepresentation
+    w = synth.refs_small()
+    w.nwater, w.lattice_n, w.box = 300, 7, 22.0
+    topo, bins = setconf.setparam_topology(w.species(), slttype=2), None
+    bins = setconf.enginit_bins(topo["numslv"])
+    eng = EnergyRepresentation(w.params, topo, bins, precision="mixed", batch=8)
+    pos, cell = w.frame(0)
+    eng.frame(pos, cell)
+    bf = w.solute["xyz"] + np.array([1.0, -2.0, 0.5])
+    mass = np.asarray(w.solute["mass"], float)
+    n = 300
+    sol, sws = eng.generate_placements(n, bf, mass, seed=12345, offset=77, weights=True, **mode)
+    sol, sws = sol.cpu().numpy(), sws.cpu().numpy()
+    for p in range(0, n, 7):
+        x, wt = insert_ref.place(bf, mass, cell, p, seed=12345, offset=77, **mode)
+        np.testing.assert_allclose(sol[p], x, atol=1e-11, rtol=0)
+        np.testing.assert_allclose(sws[p], wt, rtol=1e-12)
+    d0 = np.linalg.norm(bf[:, None] - bf[None], axis=-1)
+    d = np.linalg.norm(sol[:, :, None] - sol[:, None, :], axis=-1)
+    np.testing.assert_allclose(d, np.broadcast_to(d0, d.shape), atol=1e-10)
+    com = (mass[None, :, None] * sol).sum(1) / mass.sum()
+    if mode["insposition"] == 0:
+        frac = com / w.box
+        assert np.all((frac >= 0) & (frac < 1)) and abs(frac.mean() - 0.5) < 0.05
+    if mode["insposition"] == 2:
+        r = np.linalg.norm(com, axis=1)
+        assert np.all((r >= 3.0 - 1e-9) & (r <= 9.0 + 1e-9))
+    if mode["insposition"] == 4:
+        assert np.all((np.abs(com[:, 2]) >= 2.0 - 1e-9) & (np.abs(com[:, 2]) <= 6.0 + 1e-9))
+    # the generated placements run through the engine like host-given ones
+    tag = np.full(n, topo["nummol"], np.int32)
+    if mode["insposition"] in (0, 6):
+        eng.placements(tag, sol)
+    eng.close()
