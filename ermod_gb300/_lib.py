@@ -51,7 +51,7 @@ EXPORTS = [
     "ermod_ecorr_add_noalloc", "ermod_adjoint_enable", "ermod_adjoint_get", "ermod_graph_create",
     "ermod_graph_launch", "ermod_graph_sync", "ermod_graph_destroy", "ermod_write_engdist",
     "ermod_write_selfdist", "ermod_write_corr", "ermod_write_uvrange", "ermod_format_g",
-    "ermod_generate_placements",
+    "ermod_generate_placements", "ermod_intermediate_enable", "ermod_intermediate_get",
 ]
 
 _lib = None
@@ -110,6 +110,8 @@ def load(path: str = LIB_PATH):
     L.ermod_write_uvrange.argtypes = [C.c_char_p, C.c_int, dp, dp]
     L.ermod_format_g.argtypes = [C.c_double, C.c_int, C.c_int, C.c_char_p, C.c_int]
     L.ermod_generate_placements.argtypes = [vp, C.c_int, C.c_int, dp, dp, C.POINTER(InsertParams), vp, vp]
+    L.ermod_intermediate_enable.argtypes = [vp, dp]
+    L.ermod_intermediate_get.argtypes = [vp, dp, dp, dp]
     _lib = L
     return L
 

@@ -466,6 +466,7 @@ int ermod_create(const ermod_params* p, int device, ermod_ctx** out) {
 }
 
 static void free_adjoint(Engine& e);
+static void free_intermediate(Engine& e);
 
 int ermod_destroy(ermod_ctx* c) {
   if (!c) return ERMOD_OK;
@@ -473,6 +474,7 @@ int ermod_destroy(ermod_ctx* c) {
   cudaSetDevice(e.device);
   if (e.stream) cudaStreamSynchronize(e.stream);
   free_adjoint(e);
+  free_intermediate(e);
   dfree(e.d_ins);
   free_batch(e);
   free_frame(e);
@@ -683,6 +685,7 @@ int ermod_set_bins(ermod_ctx* c, int numslv, const int* uvmax, const int* uvsoft
   cudaSetDevice(e.device);
   cudaStreamSynchronize(e.stream);
   free_adjoint(e);  // sized by the bins: enable it again afterwards
+  free_intermediate(e);
   int ermax = 0;
   for (int s = 0; s < numslv; ++s) {
     if (uvmax[s] <= 0 || uvsoft[s] < 0 || uvsoft[s] > uvmax[s]) return fail_param("uvmax/uvsoft inconsistent");
@@ -1113,11 +1116,49 @@ int ermod_clear(ermod_ctx* c) {  // engclear (engproc.F90:276-288)
   ERMOD_CUDA(cudaMemsetAsync(e.d_eself, 0, sizeof(double) * std::max(e.esmax, 1), e.stream));
   ERMOD_CUDA(cudaMemsetAsync(e.d_slnuv, 0, sizeof(double) * e.numslv, e.stream));
   ERMOD_CUDA(cudaMemsetAsync(e.d_scal, 0, sizeof(double) * 3, e.stream));  // engnorm, engsmpl, avslf
+  if (e.d_edintm)  // engclear's hunk of the intermediate-state extension
+    ERMOD_CUDA(cudaMemsetAsync(e.d_edintm, 0, sizeof(double) * ((size_t)e.ermax + e.numslv + 3), e.stream));
   if (e.adj_on) {
     ERMOD_CUDA(cudaMemsetAsync(e.d_adj_grad, 0, sizeof(double) * 3 * (size_t)e.adj_ns * e.ermax, e.stream));
     ERMOD_CUDA(cudaMemsetAsync(e.d_adj_w, 0, sizeof(double) * e.ermax, e.stream));
   }
   ERMOD_CUDA(cudaStreamSynchronize(e.stream));
+  return ERMOD_OK;
+}
+
+static void free_intermediate(Engine& e) {
+  dfree(e.d_int_mask);
+  dfree(e.d_edintm);
+}
+
+int ermod_intermediate_enable(ermod_ctx* c, const double* refs_density) {
+  if (!c || !refs_density) return fail_param("null argument");
+  Engine& e = c->e;
+  if (!e.bins_ready) return fail_param("ermod_set_bins must come first");
+  if (e.P.slttype != 1) return fail_param("the intermediate state applies to solution mode only");
+  cudaSetDevice(e.device);
+  ERMOD_CUDA(cudaStreamSynchronize(e.stream));
+  free_intermediate(e);
+  std::vector<unsigned char> mask(e.ermax);
+  for (int i = 0; i < e.ermax; ++i) mask[i] = (refs_density[i] > 1.0e-30) ? 0 : 1;  // tiny, engproc.F90:23
+  ERMOD_CUDA(dalloc(&e.d_int_mask, (size_t)e.ermax));
+  ERMOD_CUDA(dalloc(&e.d_edintm, (size_t)e.ermax + e.numslv + 3));
+  ERMOD_CUDA(cudaMemcpy(e.d_int_mask, mask.data(), e.ermax, cudaMemcpyHostToDevice));
+  ERMOD_CUDA(cudaMemset(e.d_edintm, 0, sizeof(double) * ((size_t)e.ermax + e.numslv + 3)));
+  return ERMOD_OK;
+}
+
+int ermod_intermediate_get(ermod_ctx* c, double* edintm, double* uvintm, double* totals) {
+  if (!c) return fail_param("null context");
+  Engine& e = c->e;
+  if (!e.d_edintm) return fail_param("ermod_intermediate_enable must come first");
+  cudaSetDevice(e.device);
+  ERMOD_CUDA(cudaStreamSynchronize(e.stream));
+  std::vector<double> h((size_t)e.ermax + e.numslv + 3);
+  ERMOD_CUDA(cudaMemcpy(h.data(), e.d_edintm, sizeof(double) * h.size(), cudaMemcpyDeviceToHost));
+  if (edintm) std::copy(h.begin(), h.begin() + e.ermax, edintm);
+  if (uvintm) std::copy(h.begin() + e.ermax, h.begin() + e.ermax + e.numslv, uvintm);
+  if (totals) std::copy(h.begin() + e.ermax + e.numslv, h.end(), totals);
   return ERMOD_OK;
 }
 

@@ -164,6 +164,8 @@ struct Engine {
   float* d_ps_qf = nullptr;      // [Bmax][256]
   float2* d_ps_bvec = nullptr;   // [Bmax][256][3][Kmax]
   double* d_ps_self = nullptr;   // [Bmax][K2]
+  unsigned char* d_int_mask = nullptr;  // intermediate state: [ermax] zero-density bins
+  double* d_edintm = nullptr;            // [ermax] edintm, [numslv] uvintm, [3] totals
   double* d_ins = nullptr;       // [4][256] solute reference coordinates and masses (placement generator)
   bool tmap_ready = false;
 

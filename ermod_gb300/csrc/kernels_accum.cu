@@ -40,6 +40,11 @@ struct AccArgs {
   double* u0;      // [nb] solute self energies of the batch
   int* self_bin;   // [nb] eself bin (0-based) or -1
   DevStatus* status;
+  // intermediate-state extension (solution mode), null when off
+  const unsigned char* zmask;  // [ermax] 1 where the reference-solvent density is zero
+  double* edintm;              // [ermax]
+  double* uvintm;              // [numslv]
+  double* iscal;               // {soln_total, soln_intm, norm_intm}
 };
 
 constexpr int kAccThreads = 256;
@@ -242,6 +247,47 @@ __global__ void __launch_bounds__(kAccThreads) accumulate_kernel(AccArgs A) {
       }
     }
     if (touched) A.edens[i] = e;
+  }
+  // intermediate state (extensions/Intermediate/engproc.F90, update_histogram hunk):
+  // a placement belongs to it when none of its occupied bins has zero density in the
+  // reference solvent; its weight, histogram and flceng then accumulate separately
+  if (A.zmask) {
+    __shared__ unsigned char sout[kMaxBatch];
+    for (int b = 0; b < nb; ++b) {
+      int out = 0;
+      for (int i = threadIdx.x; i < A.ermax; i += blockDim.x)
+        if (A.zmask[i] && a.hist[(size_t)b * A.ermax + i] > 0) out = 1;
+      out = __syncthreads_or(out);
+      if (threadIdx.x == 0) sout[b] = (unsigned char)out;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double tot = A.iscal[0], in = A.iscal[1], nrm = A.iscal[2];
+      for (int b = 0; b < nb; ++b) {
+        tot = tot + sw[b];
+        if (!sout[b]) {
+          in = in + sw[b];
+          nrm = nrm + sw[b];
+        }
+      }
+      A.iscal[0] = tot;
+      A.iscal[1] = in;
+      A.iscal[2] = nrm;
+    }
+    for (int i = threadIdx.x; i < A.ermax; i += blockDim.x) {
+      double e = A.edintm[i];
+      for (int b = 0; b < nb; ++b) {
+        const int c = a.hist[(size_t)b * A.ermax + i];
+        if (c > 0 && !sout[b]) e = e + sw[b] * (double)c;
+      }
+      A.edintm[i] = e;
+    }
+    for (int sp = threadIdx.x; sp < A.numslv; sp += blockDim.x) {
+      double u = A.uvintm[sp];
+      for (int b = 0; b < nb; ++b)
+        if (!sout[b]) u = u + a.part[((size_t)b * A.ntile * A.numslv + sp) * 3] * sw[b];
+      A.uvintm[sp] = u;
+    }
   }
 }
 
@@ -457,6 +503,12 @@ cudaError_t launch_accumulate(Engine& e, const BatchArgs& a, cudaStream_t s) {
   A.u0 = a.u0;
   A.self_bin = a.self_bin;
   A.status = e.d_status;
+  if (e.d_int_mask) {
+    A.zmask = e.d_int_mask;
+    A.edintm = e.d_edintm;
+    A.uvintm = e.d_edintm + e.ermax;
+    A.iscal = e.d_edintm + e.ermax + e.numslv;
+  }
   reduce_kernel<<<a.nb, kAccThreads, 0, s>>>(A);
   accumulate_kernel<<<1, kAccThreads, 0, s>>>(A);
   e.count_launch(2);

@@ -159,6 +159,19 @@ class EnergyRepresentation:
         import torch
         torch.cuda.synchronize(torch.device("cuda", self.device))
 
+    # ---- intermediate-state extension ------------------------------------------------
+    def intermediate_enable(self, refs_density):
+        """Solution mode: the zero-density bins of the reference-solvent distribution."""
+        check(_lib.load().ermod_intermediate_enable(self.ctx, _lib.dp(np.ascontiguousarray(refs_density,
+                                                                                          np.float64))),
+              "ermod_intermediate_enable")
+
+    def intermediate_get(self):
+        ed, uv, tot = np.zeros(self.ermax), np.zeros(self.numslv), np.zeros(3)
+        check(_lib.load().ermod_intermediate_get(self.ctx, _lib.dp(ed), _lib.dp(uv), _lib.dp(tot)),
+              "ermod_intermediate_get")
+        return dict(edintm=ed, uvintm=uv, soln_total=tot[0], soln_intm=tot[1], norm_intm=tot[2])
+
     # ---- adjoint mode ------------------------------------------------------------
     def adjoint_enable(self, solute_mol: int = None, cmbrule: int = 0):
         """Accumulate bin-resolved d u / d(q_s, eps_s, sigma_s) for placements of solute_mol

@@ -94,3 +94,60 @@ def format_g(x: float, w: int, d: int) -> str:
     buf = C.create_string_buffer(w + 8)
     _lib.check(_lib.load().ermod_format_g(float(x), int(w), int(d), buf, w + 8), "ermod_format_g")
     return buf.value.decode()
+
+
+def read_engdist(path: str) -> np.ndarray:
+    """The third column (density) of an engsln/engref file, read list-directed as slvfe does."""
+    return np.array([float(ln.split()[2]) for ln in open(path) if ln.strip()])
+
+
+def refs_density_for_intermediate(prefix: str) -> np.ndarray:
+    """The reference-solvent density the intermediate-state extension tests against:
+    prefix + '.tt' when it exists, else the largest over prefix + '.01' .. '.99'
+    (extensions/Intermediate/engproc.F90:286-316)."""
+    import os
+    if os.path.exists(prefix + ".tt"):
+        return read_engdist(prefix + ".tt")
+    out = None
+    for k in range(1, 100):
+        p = f"{prefix}.{k:02d}"
+        if os.path.exists(p):
+            d = read_engdist(p)
+            out = d if out is None else np.maximum(out, d)
+    if out is None:
+        raise FileNotFoundError(prefix)
+    return out
+
+
+def write_intermediate(directory: str, intm: dict, bins: dict, temp: float, division: int, engdiv: int,
+                       avintm_rows: list = None) -> list:
+    """The extension's outputs: engint.xx (edintm / norm_intm in engsln's layout), and at
+    the last division Prob_Result and avint.tt (extensions/Intermediate/engproc.F90:623-693).
+    avintm_rows: uvintm / norm_intm of every division so far (for avint.tt)."""
+    import os
+    L = _lib.load()
+    suffix = ".tt" if engdiv == 1 else f".{division:02d}"
+    paths = []
+    uvmax = np.ascontiguousarray(bins["uvmax"], np.int32)
+    uvsoft = np.ascontiguousarray(bins["uvsoft"], np.int32)
+    uvcrd = np.ascontiguousarray(bins["uvcrd"], np.float64)
+    ed = np.ascontiguousarray(intm["edintm"] / intm["norm_intm"], np.float64)
+    p = os.path.join(directory, "engint" + suffix)
+    _lib.check(L.ermod_write_engdist(p.encode(), len(uvmax), _lib.ip(uvmax), _lib.ip(uvsoft), _lib.dp(uvcrd),
+                                     _lib.dp(ed)), "ermod_write_engdist")
+    paths.append(p)
+    if division == engdiv:
+        factor = intm["soln_intm"] / intm["soln_total"]
+        p = os.path.join(directory, "Prob_Result")
+        with open(p, "w") as f:
+            f.write(" Probability to find the system in the intermediate state = %12.6f\n" % factor)
+            f.write(" Free-energy change from the intermediate state to the simulated state\n")
+            f.write("                                                = %12.6f kcal/mol\n" % (temp * np.log(factor)))
+        paths.append(p)
+        rows = avintm_rows if avintm_rows is not None else [intm["uvintm"] / intm["norm_intm"]]
+        p = os.path.join(directory, "avint.tt")
+        with open(p, "w") as f:
+            for k, row in enumerate(rows, start=1):  # format(i5, 9999f15.5)
+                f.write("%5d" % k + "".join("%15.5f" % v for v in row) + "\n")
+        paths.append(p)
+    return paths

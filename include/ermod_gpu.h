@@ -253,6 +253,18 @@ int ermod_engstore_merge(int nrank, int slttype, int wgtslf, double temp, int er
 int ermod_ecorr_add_noalloc(const int* hist, const double* weight, int nplace, int ermax,
                             double* ecorr, int64_t* ecorr_count, void* stream);
 
+/* ---- intermediate-state extension (extensions/Intermediate/engproc.F90) ---------------
+ * Solution mode.  refs_density[ermax] is the reference-solvent distribution (engref's
+ * third column, the largest over its .tt / .01-.99 files); its bins at or below 1e-30
+ * form the zero-density set.  A placement none of whose occupied bins is in that set
+ * belongs to the intermediate state: its engnmfc adds to soln_intm and norm_intm, its
+ * histogram to edintm and its flceng to uvintm; every placement adds to soln_total
+ * (the extension's update_histogram hunk).  ermod_clear zeroes edintm, uvintm and
+ * norm_intm (its engclear hunk; soln_total and soln_intm run over the whole job). */
+int ermod_intermediate_enable(ermod_ctx* ctx, const double* refs_density);
+/* edintm[ermax], uvintm[numslv], totals[3] = {soln_total, soln_intm, norm_intm}. */
+int ermod_intermediate_get(ermod_ctx* ctx, double* edintm, double* uvintm, double* totals);
+
 /* ---- placements generated on the device (instslt, insertion.F90:76-99) --------------
  * insorigin 0: solute COM to the origin (1: as given); insposition 0 random in the cell,
  * 1 as given, 2 spherical shell lwreg..upreg, 3 slab in z, 4 symmetric slab, 5 random

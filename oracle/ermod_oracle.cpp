@@ -283,6 +283,11 @@ struct orc_ctx {
   // realcal_self reuse (engproc.F90:716-724)
   bool usreal_valid = false;
   double usreal = 0.0;
+  // intermediate-state extension (extensions/Intermediate/engproc.F90), solution mode
+  bool do_intermediate = false;
+  std::vector<char> zerodns_crd;          // (ermax)
+  std::vector<double> edintm, uvintm;     // (ermax), (numslv)
+  double soln_total = 0, soln_intm = 0, norm_intm = 0;
   // last placement PME potential (for cross-checks)
   std::vector<double> last_cnv;
   double last_self = 0.0;
@@ -987,6 +992,21 @@ int update_histogram(orc_ctx* c, int tagslt, double stat_weight_solute, const do
       }
     }
   }
+  if (c->do_intermediate) {  // the extension's update_histogram hunk (diff lines 198-211)
+    c->soln_total = c->soln_total + engnmfc;
+    bool outside = false;
+    for (int iduv = 0; iduv < c->ermax; ++iduv)
+      if (insdst[iduv] > 0 && c->zerodns_crd[iduv]) outside = true;
+    if (!outside) {
+      c->soln_intm = c->soln_intm + engnmfc;
+      c->norm_intm = c->norm_intm + engnmfc;
+      for (int iduv = 0; iduv < c->ermax; ++iduv) {
+        const int kk = insdst[iduv];
+        if (kk > 0) c->edintm[iduv] = c->edintm[iduv] + engnmfc * (double)kk;
+      }
+      for (int s = 0; s < c->numslv; ++s) c->uvintm[s] = c->uvintm[s] + flceng[s] * engnmfc;
+    }
+  }
   return ORC_OK;
 }
 
@@ -1177,6 +1197,11 @@ int orc_set_bins(orc_ctx* c, int numslv, const int* uvmax, const int* uvsoft, co
 int orc_clear(orc_ctx* c) {  // engclear, engproc.F90:276-288
   std::fill(c->edens.begin(), c->edens.end(), 0.0);
   std::fill(c->ecorr.begin(), c->ecorr.end(), 0.0);
+  if (c->do_intermediate) {  // engclear hunk of the intermediate-state extension
+    std::fill(c->edintm.begin(), c->edintm.end(), 0.0);
+    std::fill(c->uvintm.begin(), c->uvintm.end(), 0.0);
+    c->norm_intm = 0.0;
+  }
   std::fill(c->eself.begin(), c->eself.end(), 0.0);
   std::fill(c->slnuv.begin(), c->slnuv.end(), 0.0);
   c->avslf = 0.0;
@@ -1508,6 +1533,32 @@ int orc_adjoint(const orc_ctx* c, int tagslt, const double* solute_sitepos, int 
       o[3 * s + 1] = deps;
       o[3 * s + 2] = dsig;
     }
+  }
+  return ORC_OK;
+}
+
+// the intermediate-state extension: bins where refs_density <= tiny (1e-30) form the
+// zero-density set read from engref (extensions/Intermediate/engproc.F90:275-318)
+int orc_intermediate_enable(orc_ctx* c, const double* refs_density) {
+  if (!c || !refs_density || c->ermax <= 0 || c->p.slttype != 1) return ORC_E_PARAM;
+  c->do_intermediate = true;
+  c->zerodns_crd.assign(c->ermax, 1);
+  for (int i = 0; i < c->ermax; ++i)
+    if (refs_density[i] > 1.0e-30) c->zerodns_crd[i] = 0;
+  c->edintm.assign(c->ermax, 0.0);
+  c->uvintm.assign(c->numslv, 0.0);
+  c->soln_total = c->soln_intm = c->norm_intm = 0.0;
+  return ORC_OK;
+}
+
+int orc_intermediate_get(const orc_ctx* c, double* edintm, double* uvintm, double* totals) {
+  if (!c || !c->do_intermediate) return ORC_E_PARAM;
+  if (edintm) std::copy(c->edintm.begin(), c->edintm.end(), edintm);
+  if (uvintm) std::copy(c->uvintm.begin(), c->uvintm.end(), uvintm);
+  if (totals) {
+    totals[0] = c->soln_total;
+    totals[1] = c->soln_intm;
+    totals[2] = c->norm_intm;
   }
   return ORC_OK;
 }

@@ -106,6 +106,11 @@ int orc_last_cnvslt(const orc_ctx* c, double* out, double* self_energy);
 /* Per-molecule derivatives of uvengy(k) with respect to the solute's per-site charge,
  * LJ epsilon and LJ sigma (cmbrule 0 arithmetic / 1 geometric sigma), FP64:
  * out[k][3 s + {0,1,2}] for k < slvmax (tagpt order) and solute site s. */
+/* Intermediate-state extension (extensions/Intermediate/engproc.F90, solution mode):
+ * refs_density[ermax] marks the zero-density bins (<= 1e-30); totals = {soln_total,
+ * soln_intm, norm_intm}. */
+int orc_intermediate_enable(orc_ctx* c, const double* refs_density);
+int orc_intermediate_get(const orc_ctx* c, double* edintm, double* uvintm, double* totals);
 int orc_adjoint(const orc_ctx* c, int tagslt, const double* solute_sitepos, int cmbrule, double* out);
 int orc_recip_parts(const orc_ctx* c, int tagslt, const double* solute_sitepos, double* out,
                     double* self_out);

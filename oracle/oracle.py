@@ -88,6 +88,8 @@ def lib():
         L.orc_direct_ewald.argtypes = [C.c_void_p, C.c_int, dp, C.c_int, dp, dp]
         L.orc_recip_parts.argtypes = [C.c_void_p, C.c_int, dp, dp, dp]
         L.orc_adjoint.argtypes = [C.c_void_p, C.c_int, dp, C.c_int, dp]
+        L.orc_intermediate_enable.argtypes = [C.c_void_p, dp]
+        L.orc_intermediate_get.argtypes = [C.c_void_p, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -365,3 +367,12 @@ class Oracle:
         sx = None if solute_sitepos is None else np.ascontiguousarray(solute_sitepos, np.float64)
         _check(lib().orc_adjoint(self.ctx, int(tagslt), _dp(sx), int(cmbrule), _dp(out)), "adjoint")
         return out
+
+    def intermediate_enable(self, refs_density):
+        _check(lib().orc_intermediate_enable(self.ctx, _dp(np.ascontiguousarray(refs_density, np.float64))),
+               "intermediate_enable")
+
+    def intermediate_get(self):
+        ed, uv, tot = np.zeros(self.ermax), np.zeros(self.numslv), np.zeros(3)
+        _check(lib().orc_intermediate_get(self.ctx, _dp(ed), _dp(uv), _dp(tot)), "intermediate_get")
+        return dict(edintm=ed, uvintm=uv, soln_total=tot[0], soln_intm=tot[1], norm_intm=tot[2])
