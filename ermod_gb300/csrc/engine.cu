@@ -367,10 +367,11 @@ int ermod_create(const ermod_params* p, int device, ermod_ctx** out) {
   if (!p || !out) return fail_param("null argument");
   *out = nullptr;
   if (p->abi_version != ERMOD_ABI_VERSION) return fail_param("abi_version mismatch");
-  if (p->cltype != 2) {
-    g_err = "only cltype = 2 (PME) is implemented on the GPU";
+  if (p->cltype != 2 && p->cltype != 3) {
+    g_err = "cltype 2 (PME) and 3 (PPPM) are implemented on the GPU";
     return ERMOD_E_UNSUPPORTED;
   }
+  if (p->cltype == 3 && p->splodr % 2 == 1) return fail_param("interpolation order for PPPM must be even");
   if (p->slttype < 1 || p->slttype > 3) return fail_param("slttype must be 1, 2 or 3");
   if (p->ljswitch < 0 || p->ljswitch > 3) return fail_param("ljswitch must be 0..3");
   if (p->splodr != 4 && p->splodr != 6 && p->splodr != 8) {

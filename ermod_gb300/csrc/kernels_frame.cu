@@ -10,7 +10,8 @@
 //                   (recpcal.F90:408-442) -- replaces recpcal_prepare_solvent
 //                   (engproc.F90:378-382) and the per-placement blockify/sort_block
 //                   rebuild of the reference (realcal.F90:439-525);
-//   greenfunc       recpcal_spline_greenfunc (recpcal.F90:111-152), FP64.
+//   greenfunc       recpcal_spline_greenfunc (recpcal.F90:111-152), FP64; for PPPM
+//                   (cltype 3) recpcal_pppm_greenfunc (recpcal.F90:205-319).
 // All of these are HBM-streaming kernels over O(numatm) or O(K^3) elements.
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
@@ -266,6 +267,77 @@ __global__ void greenfunc_kernel(FrameGeom g, int order, const double* __restric
   engfac_f[i] = (float)factor;
 }
 
+// recpcal_pppm_greenfunc (recpcal.F90:205-319): the optimal influence function of PPPM,
+// summed over the aliases mx, my, mz in [-m_max, m_max] (m_max from cell . LAMMPS'
+// estimate); mN(3) = mz * ms2max as the reference writes it.
+struct PppmArgs {
+  FrameGeom g;
+  int order;
+  int mmax[3];
+  double screen;
+  double gf_b[kMaxSplineOrder + 1];  // calc_gfb_pppm, 0-based
+};
+
+__device__ __forceinline__ double ipow_int(double x, int e) {
+  double r = 1.0;
+  for (int i = 0; i < e; ++i) r *= x;
+  return r;
+}
+
+__global__ void pppm_greenfunc_kernel(PppmArgs A, double* __restrict__ engfac, float* __restrict__ engfac_f) {
+  const FrameGeom& g = A.g;
+  const int H = g.K[0] / 2 + 1;
+  const size_t n = (size_t)H * g.K[1] * g.K[2];
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int rc[3] = {(int)(i % H), (int)((i / H) % g.K[1]), (int)(i / ((size_t)H * g.K[1]))};
+  double factor = 0.0;
+  if (!(rc[0] == 0 && rc[1] == 0 && rc[2] == 0)) {
+    double inm[3], s2[3], k[3];
+    for (int a = 0; a < 3; ++a) {
+      inm[a] = (rc[a] <= g.K[a] / 2) ? (double)rc[a] : (double)(rc[a] - g.K[a]);
+      const double sn = sin(kPi * inm[a] / g.K[a]);
+      s2[a] = sn * sn;
+    }
+    for (int a = 0; a < 3; ++a)
+      k[a] = 2 * kPi * (g.invcl[0 + 3 * a] * inm[0] + g.invcl[1 + 3 * a] * inm[1] + g.invcl[2 + 3 * a] * inm[2]);
+    const double k2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
+    if (k2 > 0.0) {
+      double sum = 0.0;
+      for (int mx = -A.mmax[0]; mx <= A.mmax[0]; ++mx) {
+        double t = kPi * (inm[0] / g.K[0] + mx);
+        const double u1 = (t == 0.0) ? 1.0 : ipow_int(sin(t) / t, 2 * A.order);
+        for (int my = -A.mmax[1]; my <= A.mmax[1]; ++my) {
+          t = kPi * (inm[1] / g.K[1] + my);
+          const double u2 = (t == 0.0) ? 1.0 : ipow_int(sin(t) / t, 2 * A.order);
+          for (int mz = -A.mmax[2]; mz <= A.mmax[2]; ++mz) {
+            t = kPi * (inm[2] / g.K[2] + mz);
+            const double u3 = (t == 0.0) ? 1.0 : ipow_int(sin(t) / t, 2 * A.order);
+            const double mN[3] = {(double)(mx * g.K[0]), (double)(my * g.K[1]), (double)(mz * g.K[1])};
+            double km[3], gam = 1.0;
+            for (int a = 0; a < 3; ++a) {
+              km[a] = k[a] + 2 * kPi * (g.invcl[0 + 3 * a] * mN[0] + g.invcl[1 + 3 * a] * mN[1] +
+                                        g.invcl[2 + 3 * a] * mN[2]);
+              const double q = km[a] / A.screen;
+              gam *= exp(-0.25 * (q * q));
+            }
+            const double kkm = k[0] * km[0] + k[1] * km[1] + k[2] * km[2];
+            const double km2 = km[0] * km[0] + km[1] * km[1] + km[2] * km[2];
+            sum = sum + kkm * gam * (u1 * u2 * u3) / km2;
+          }
+        }
+      }
+      double den[3] = {0.0, 0.0, 0.0};  // gf_denom
+      for (int l = A.order - 1; l >= 0; --l)
+        for (int a = 0; a < 3; ++a) den[a] = A.gf_b[l] + den[a] * s2[a];
+      const double d = den[0] * den[1] * den[2];
+      factor = sum * 4.0 * kPi / (k2 * (d * d)) / g.volume;
+    }
+  }
+  engfac[i] = factor;
+  engfac_f[i] = (float)factor;
+}
+
 inline int nblk(size_t n, int t) { return (int)((n + t - 1) / t); }
 
 }  // namespace
@@ -366,7 +438,40 @@ cudaError_t launch_frame_sites(Engine& e) {
   return cudaGetLastError();
 }
 
+// calc_gfb_pppm (recpcal.F90:170-188), including its use of the inner loop variable
+// after the loop (l = 0)
+static void pppm_gfb(int p, double* out) {
+  std::vector<double> b(p + 2, 0.0);  // 1-based
+  b[1] = 1.0;
+  for (int m = 1; m <= p - 1; ++m) {
+    for (int l = m; l >= 1; --l)
+      b[l + 1] = 4.0 * (b[l + 1] * (double)(l - m) * ((double)(l - m) - 0.5) - b[l] * (double)((l - m - 1) * (l - m - 1)));
+    const int l = 0;
+    b[1] = 4.0 * (b[1] * (double)(l - m) * ((double)(l - m) - 0.5));
+  }
+  double fact = 1.0;
+  for (int i = 1; i <= 2 * p - 1; ++i) fact *= (double)i;
+  const double gaminv = 1.0 / fact;
+  for (int m = 1; m <= p; ++m) out[m - 1] = b[m] * gaminv;
+}
+
 cudaError_t launch_greenfunc(Engine& e) {
+  if (e.P.cltype == 3) {
+    PppmArgs A{};
+    A.g = e.geom;
+    A.order = e.P_order;
+    A.screen = e.P.screen;
+    pppm_gfb(e.P_order, A.gf_b);
+    const double eps_hoc = 0.0000001;  // LAMMPS' value, recpcal.F90:213
+    double mmax[3];
+    for (int a = 0; a < 3; ++a) mmax[a] = e.P.screen / (kPi * e.geom.K[a]) * std::pow(-std::log(eps_hoc), 0.25);
+    for (int j = 0; j < 3; ++j)  // int(dot_product(cell(:, j), m_max(:)))
+      A.mmax[j] = (int)(e.cell[3 * j] * mmax[0] + e.cell[3 * j + 1] * mmax[1] + e.cell[3 * j + 2] * mmax[2]);
+    const size_t n = e.grid_cplx();
+    pppm_greenfunc_kernel<<<nblk(n, 128), 128, 0, e.stream>>>(A, e.d_engfac, e.d_engfac_f);
+    e.count_launch();
+    return cudaGetLastError();
+  }
   const size_t n = e.grid_cplx();
   greenfunc_kernel<<<nblk(n, 256), 256, 0, e.stream>>>(e.geom, e.P_order, e.d_splfc, e.P.screen, e.d_engfac,
                                                        e.d_engfac_f);

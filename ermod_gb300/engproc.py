@@ -30,7 +30,7 @@ class EnergyRepresentation:
         for k in PARAM_KEYS:
             if k in params:
                 setattr(p, k, params[k])
-        p.cltype = 2
+        p.cltype = int(params.get("cltype", 2))  # 2 PME, 3 PPPM
         p.precision = _lib.PRECISION_MIXED if precision == "mixed" else _lib.PRECISION_FP64
         p.batch = int(batch)
         p.count_mirror = 1 if count_mirror else 0

@@ -370,6 +370,84 @@ void spline_greenfunc(orc_ctx* c) {
   c->engfac[0] = 0.0;
 }
 
+// --- recpcal.F90:169-201 calc_gfb_pppm / gf_denom, :205-319 recpcal_pppm_greenfunc ---
+void pppm_greenfunc(orc_ctx* c) {
+  const int K[3] = {c->p.ms1max, c->p.ms2max, c->p.ms3max};
+  const int p = c->p.splodr;
+  const int h = K[0] / 2 + 1;
+  std::vector<double> gf(p + 2, 0.0);  // gf_b(1:p)
+  gf[1] = 1.0;
+  for (int m = 1; m <= p - 1; ++m) {
+    int l;
+    for (l = m; l >= 1; --l)
+      gf[l + 1] = 4.0 * (gf[l + 1] * (l - m) * (l - m - 0.5) - gf[l] * (double)((l - m - 1) * (l - m - 1)));
+    gf[1] = 4.0 * (gf[1] * (l - m) * (l - m - 0.5));  // l = 0 after the loop
+  }
+  double fact = 1.0;
+  for (int i = 1; i <= 2 * p - 1; ++i) fact *= i;
+  for (int m = 1; m <= p; ++m) gf[m] = gf[m] / fact;
+  auto denom = [&](double x, double y, double z) {
+    double s[3] = {0, 0, 0};
+    for (int l = p; l >= 1; --l) {
+      s[0] = gf[l] + s[0] * x;
+      s[1] = gf[l] + s[1] * y;
+      s[2] = gf[l] + s[2] * z;
+    }
+    const double pr = s[0] * s[1] * s[2];
+    return pr * pr;
+  };
+  const double eps_hoc = 0.0000001;
+  double m_max[3];
+  for (int a = 0; a < 3; ++a) m_max[a] = c->p.screen / (PI * K[a]) * std::pow(-std::log(eps_hoc), 0.25);
+  int mm[3];
+  for (int j = 0; j < 3; ++j)
+    mm[j] = (int)(c->cell[3 * j] * m_max[0] + c->cell[3 * j + 1] * m_max[1] + c->cell[3 * j + 2] * m_max[2]);
+  c->engfac.assign((size_t)h * K[1] * K[2], 0.0);
+  for (int rc3 = 0; rc3 < K[2]; ++rc3)
+    for (int rc2 = 0; rc2 < K[1]; ++rc2)
+      for (int rc1 = 0; rc1 < h; ++rc1) {
+        if (rc1 == 0 && rc2 == 0 && rc3 == 0) continue;
+        const int rc[3] = {rc1, rc2, rc3};
+        double inm[3], s2[3], k[3];
+        for (int a = 0; a < 3; ++a) {
+          inm[a] = (rc[a] <= K[a] / 2) ? rc[a] : rc[a] - K[a];
+          const double sn = std::sin(PI * inm[a] / K[a]);
+          s2[a] = sn * sn;
+        }
+        for (int a = 0; a < 3; ++a)
+          k[a] = 2 * PI * (c->invcl[0 + 3 * a] * inm[0] + c->invcl[1 + 3 * a] * inm[1] + c->invcl[2 + 3 * a] * inm[2]);
+        const double k2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
+        double factor = 0.0;
+        if (k2 > 0.0) {
+          double sum = 0.0;
+          for (int mx = -mm[0]; mx <= mm[0]; ++mx) {
+            double t = PI * (inm[0] / K[0] + mx);
+            const double u1 = (t == 0.0) ? 1.0 : std::pow(std::sin(t) / t, 2 * p);
+            for (int my = -mm[1]; my <= mm[1]; ++my) {
+              t = PI * (inm[1] / K[1] + my);
+              const double u2 = (t == 0.0) ? 1.0 : std::pow(std::sin(t) / t, 2 * p);
+              for (int mz = -mm[2]; mz <= mm[2]; ++mz) {
+                t = PI * (inm[2] / K[2] + mz);
+                const double u3 = (t == 0.0) ? 1.0 : std::pow(std::sin(t) / t, 2 * p);
+                const double mN[3] = {(double)mx * K[0], (double)my * K[1], (double)mz * K[1]};  // as written
+                double km[3], gam = 1.0;
+                for (int a = 0; a < 3; ++a) {
+                  km[a] = k[a] + 2 * PI * (c->invcl[0 + 3 * a] * mN[0] + c->invcl[1 + 3 * a] * mN[1] +
+                                           c->invcl[2 + 3 * a] * mN[2]);
+                  gam *= std::exp(-0.25 * (km[a] / c->p.screen) * (km[a] / c->p.screen));
+                }
+                sum += (k[0] * km[0] + k[1] * km[1] + k[2] * km[2]) * gam * (u1 * u2 * u3) /
+                       (km[0] * km[0] + km[1] * km[1] + km[2] * km[2]);
+              }
+            }
+          }
+          factor = sum * 4.0 * PI / (k2 * denom(s2[0], s2[1], s2[2])) / c->volume;
+        }
+        c->engfac[((size_t)rc3 * K[1] + rc2) * h + rc1] = factor;
+      }
+  c->engfac[0] = 0.0;
+}
+
 // --- recpcal.F90:408-442 calc_spline_molecule -------------------------------------
 void calc_spline_sites(const orc_ctx* c, const double* xyz /*(3,n)*/, int n, double* store_spline,
                        int* store_grid) {
@@ -1237,7 +1315,12 @@ int orc_frame(orc_ctx* c, const double* sitepos, const double* cell, double stat
   }
   bool changed = !c->pme_initialized;
   for (int i = 0; i < 9; ++i) changed = changed || (c->prevcl[i] != c->cell[i]);
-  if (changed) spline_greenfunc(c);
+  if (changed) {
+    if (c->p.pppm)
+      pppm_greenfunc(c);
+    else
+      spline_greenfunc(c);
+  }
   std::memcpy(c->prevcl, c->cell, sizeof(double) * 9);
   c->pme_initialized = true;
   // recpcal_prepare_solvent for every physical molecule (engproc.F90:378-382)

@@ -160,3 +160,24 @@ def test_bin_errors(oracle):
     orc = oracle.Oracle(w.params, topo, bins)
     orc.frame(pos, cell)
     assert orc.placements([topo["nummol"]], raise_on_error=False)["status"] == oracle.E_ENG_SFT
+
+
+def test_pppm_converges_to_direct_ewald(oracle):
+    """PPPM (cltype 3: the optimal influence function of recpcal_pppm_greenfunc in place
+    of PME's engfac) -> direct Ewald sum, as the grid refines."""
+    from tests import helpers
+    from ermod_gb300 import synth
+    errs = []
+    for K, order in [(32, 4), (48, 6), (64, 8)]:
+        w = synth.Workload("t", "refs", 20.0, 250, synth.methanol_like(), synth._params(2, K, 0, 0), 9, 1, 4, 7)
+        w.params["splodr"] = order
+        w.params["cltype"] = 3
+        topo, bins = helpers.build_inputs(w)
+        orc = oracle.Oracle(w.params, topo, bins)
+        pos, cell = w.frame(0)
+        orc.frame(pos, cell)
+        pl = w.placements(0, 1)
+        rp, rself = orc.recip_parts(topo["nummol"], pl[0])
+        de, dself = orc.direct_ewald(topo["nummol"], pl[0], mmax=14)
+        errs.append(max(np.abs(rp - de).max(), abs(rself - dself)))
+    assert errs[0] < 1e-3 and errs[1] < 1e-6 and errs[2] < 1e-9, errs

@@ -168,3 +168,22 @@ def test_run_to_run_deterministic(gpu_lib):
         np.testing.assert_array_equal(out[0][k], out[1][k])
     np.testing.assert_array_equal(out[0]["edens"], out[2]["edens"])
     assert out[0]["engnorm"] == out[1]["engnorm"]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_pppm_soln_frames(gpu_lib, oracle, precision):
+    """cltype 3 (PPPM): the optimal influence function replaces engfac; the rest of the path is PME's."""
+    from ermod_gb300 import synth
+    w = synth.soln_small()
+    w.params["cltype"] = 3
+    topo, bins = helpers.build_inputs(w)
+    gpu, orc = _engines(gpu_lib, oracle, w, topo, bins, precision)
+    tag = [topo["nummol"]]
+    for f in range(2):
+        pos, cell = w.frame(f)
+        orc.frame(pos, cell)
+        ro = orc.placements(tag)
+        gpu.frame(pos, cell)
+        rg = gpu.placements(tag, want_uvengy=True)
+        _check_energies(rg["uvengy"], ro["uvengy"], precision)
+    gpu.close()
