@@ -367,8 +367,8 @@ int ermod_create(const ermod_params* p, int device, ermod_ctx** out) {
   if (!p || !out) return fail_param("null argument");
   *out = nullptr;
   if (p->abi_version != ERMOD_ABI_VERSION) return fail_param("abi_version mismatch");
-  if (p->cltype != 2 && p->cltype != 3) {
-    g_err = "cltype 2 (PME) and 3 (PPPM) are implemented on the GPU";
+  if (p->cltype != 0 && p->cltype != 2 && p->cltype != 3) {  // 1 (Ewald) stops in the reference (set_prs)
+    g_err = "cltype 0 (bare Coulomb), 2 (PME) and 3 (PPPM) are implemented on the GPU";
     return ERMOD_E_UNSUPPORTED;
   }
   if (p->cltype == 3 && p->splodr % 2 == 1) return fail_param("interpolation order for PPPM must be even");
@@ -790,7 +790,7 @@ static int frame_launch(Engine& e) {
   e.phase_begin(PH_FRAME);
   bool changed = !e.green_valid;
   for (int i = 0; i < 9; ++i) changed = changed || (e.prevcl[i] != e.cell[i]);
-  if (changed) ERMOD_CUDA(launch_greenfunc(e));
+  if (changed && e.P.cltype != 0) ERMOD_CUDA(launch_greenfunc(e));
   std::memcpy(e.prevcl, e.cell, sizeof(e.cell));
   e.green_valid = true;
   ERMOD_CUDA(launch_frame_wrap(e));
@@ -916,7 +916,9 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
       flush_pending = false;
     }
     ERMOD_CUDA(cudaMemsetAsync(a.hist, 0, sizeof(int) * (size_t)nb * e.ermax, bst));
-    if (e.mixed) {
+    if (e.P.cltype == 0) {
+      // bare Coulomb (realcal_bare): no reciprocal space
+    } else if (e.mixed) {
       e.phase_begin_on(PH_SPECTRUM, bst);
       ERMOD_CUDA(launch_pme_mixed(e, a));  // spectrum + k3 transform, then (FFT phase) k2/k1
       e.phase_end_on(bst);
@@ -1183,8 +1185,8 @@ static void free_adjoint(Engine& e) {
 int ermod_adjoint_enable(ermod_ctx* c, int solute_mol, int cmbrule) {
   if (!c) return fail_param("null context");
   Engine& e = c->e;
-  if (!e.mixed) {
-    g_err = "the adjoint runs on the mixed-precision path only";
+  if (!e.mixed || e.P.cltype == 0) {
+    g_err = "the adjoint runs on the mixed-precision PME/PPPM path only";
     return ERMOD_E_UNSUPPORTED;
   }
   if (!e.topo_ready) return fail_param("ermod_set_topology must come first");

@@ -27,6 +27,7 @@ struct AccArgs {
   double temp, volume, volfac;  // volfac = pi Qtot^2 / beta^2 / V / 2 (volcorrect)
   double screen;                // residual_ene(slt, slt) = -(pi Q Q / beta / beta / V) / 2
   double stat_weight_system;
+  int bare;      // cltype 0: no reciprocal self energy, no residual, volcorrect without its factor
   double* scal;  // {engnorm, engsmpl, avslf, voffset, voffset_init, usreal, usreal_valid}
   double* edens;
   double* eself;
@@ -71,7 +72,7 @@ __global__ void __launch_bounds__(kAccThreads) reduce_kernel(AccArgs A) {
   const BatchArgs& a = A.a;
   const int b = blockIdx.x;
   __shared__ double red[kAccThreads];
-  const double self = block_sum_fixed(red, a.self_part + (size_t)b * A.nself, A.nself, 1);
+  const double self = A.bare ? 0.0 : block_sum_fixed(red, a.self_part + (size_t)b * A.nself, A.nself, 1);
   for (int sp = 0; sp < A.numslv; ++sp) {
     const double* base = a.part + ((size_t)b * A.ntile * A.numslv + sp) * 3;
     const int stride = A.numslv * 3;
@@ -112,7 +113,7 @@ __global__ void __launch_bounds__(kAccThreads) reduce_kernel(AccArgs A) {
     else
       usreal = a.u_usreal[b];
     const double qm = a.u_qmol[b];
-    double epcl = kPi * qm * qm / A.screen / A.screen / A.volume;
+    double epcl = A.bare ? 0.0 : kPi * qm * qm / A.screen / A.screen / A.volume;
     epcl = epcl / 2.0;
     const double residual = -epcl;
     double u0 = self;
@@ -487,7 +488,9 @@ cudaError_t launch_accumulate(Engine& e, const BatchArgs& a, cudaStream_t s) {
   A.mbin_mode = e.warn_bin_firsttime ? (e.P.force_calculation ? 2 : 1) : 0;
   A.temp = e.P.temp;
   A.volume = e.geom.volume;
-  A.volfac = kPi * (e.total_charge_phys * e.total_charge_phys) / (e.P.screen * e.P.screen) / e.geom.volume / 2.0;
+  A.bare = (e.P.cltype == 0) ? 1 : 0;
+  A.volfac = A.bare ? 0.0  // volcorrect multiplies by the volume only (engproc.F90:871-887)
+                    : kPi * (e.total_charge_phys * e.total_charge_phys) / (e.P.screen * e.P.screen) / e.geom.volume / 2.0;
   A.screen = e.P.screen;
   A.stat_weight_system = e.stat_weight_system;
   A.scal = e.d_scal;

@@ -61,6 +61,7 @@ struct MolArgs {
   float fxf[3];    // fixed-point unit per axis (box length / 2^32)
   float screen_f;  // Ewald beta
   float rc_f;      // max(elecut, upljcut)
+  int bare;        // cltype 0: bare Coulomb within elecut, no reciprocal space or residual
   LjK k32;         // LJ switching constants
   double resid_fac;  // pi / screen^2 / volume
   // batch
@@ -342,7 +343,9 @@ __device__ __forceinline__ float real_mixed(const MolArgs& A, const BatchArgs& a
         else if (r2 <= k32.up2)
           e += lj_switch<float>(A.ljswitch, k32, ljeps, sg2, r2);
       }
-      if (r2 <= k32.ele2) {
+      if (A.bare) {
+        if (r2 < k32.ele2) e += qu * A.site_rec[s0 + s].w / sqrtf(r2);  // realcal_bare
+      } else if (r2 <= k32.ele2) {
         const float r = sqrtf(r2);
         e += qu * A.site_rec[s0 + s].w * erfcf(beta * r) / r;
       }
@@ -421,7 +424,9 @@ __global__ void __launch_bounds__(256) mol_energy_kernel(MolArgs A) {
     if (active) {
       // ---- reciprocal part ----
       double recip = 0.0;
-      if (MIXED) {
+      if (A.bare) {
+        // bare Coulomb: no reciprocal part
+      } else if (MIXED) {
         const float* phi = a.phi + (size_t)b * gridn;
         for (int s = 0; s < ns; ++s) {
           const float4 rec = A.site_rec[s0 + s];
@@ -520,7 +525,9 @@ __global__ void __launch_bounds__(256) mol_energy_kernel(MolArgs A) {
                 else if (dist <= k64.up2)
                   real += lj_switch64(A.ljswitch, k64, ljeps, sg2, dist);
               }
-              if (dist <= k64.ele2) {
+              if (A.bare) {
+                if (dist < k64.ele2) real += qu * A.site_q[idx] / sqrt(dist);  // realcal_bare
+              } else if (dist <= k64.ele2) {
                 const double r = sqrt(dist);
                 real += qu * A.site_q[idx] * (1.0 - erf(A.screen * r)) / r;
               }
@@ -530,7 +537,9 @@ __global__ void __launch_bounds__(256) mol_energy_kernel(MolArgs A) {
       }
       // residual_ene + assembly (engproc.F90:741-752)
       double epcl;
-      if (MIXED)
+      if (A.bare)
+        epcl = 0.0;  // residual_ene returns without a term for bare Coulomb
+      else if (MIXED)
         epcl = A.resid_fac * a.u_qmol[b] * qmol;
       else
         epcl = kPi * a.u_qmol[b] * qmol / A.screen / A.screen / g.volume;
@@ -879,7 +888,7 @@ __global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const flo
   int4 p0 = make_int4(0, 0, 0, 0);
   if (valid) {
     p0 = A.site_pos[s0];
-    for (int s = 0; s < ns; ++s) {
+    for (int s = 0; s < (A.bare ? 0 : ns); ++s) {
       const float* row = site_e + (size_t)(s0 + s) * ldb + g0;
       if (G % 4 == 0 && ng == G) {
 #pragma unroll
@@ -1070,7 +1079,8 @@ static MolArgs make_mol_args(Engine& e, const BatchArgs& a) {
   A.lwljcut = e.P.lwljcut;
   A.upljcut = e.P.upljcut;
   A.screen = e.P.screen;
-  A.resid_fac = kPi / e.P.screen / e.P.screen / e.geom.volume;
+  A.bare = (e.P.cltype == 0) ? 1 : 0;
+  A.resid_fac = A.bare ? 0.0 : kPi / e.P.screen / e.P.screen / e.geom.volume;
   for (int i = 0; i < 3; ++i) A.fxf[i] = (float)e.geom.fx_scale[i];
   A.screen_f = (float)e.P.screen;
   A.rc_f = (float)std::max(e.P.elecut, e.P.upljcut);
@@ -1127,7 +1137,7 @@ cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
     return launch_p<false>(e, A, grid, smem);
   }
   if (a.G != 8 && a.G != 4) return cudaErrorInvalidValue;
-  if ((err = launch_gather(e, a)) != cudaSuccess) return err;
+  if (e.P.cltype != 0 && (err = launch_gather(e, a)) != cudaSuccess) return err;
   if (a.phases) {
     e.phase_end_on(a.stream);
     e.phase_begin_on(PH_MOL, a.stream);

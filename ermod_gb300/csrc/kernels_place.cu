@@ -58,6 +58,7 @@ struct PrepArgs {
   int mixed;
   int self_mode;  // 0: none, 1: all placements, 2: only placement 0 of the batch
   int nummol;
+  int bare;  // cltype 0
   unsigned mK[3], mKmax, m3Kmax;  // ceil(2^32 / d): n / d = umulhi(n, m) for n d < 2^32
   DevStatus* status;
 };
@@ -197,6 +198,10 @@ __global__ void __launch_bounds__(256) place_prep_kernel(PrepArgs A) {
   if (threadIdx.x == 0) a.u_radius[b] = __int_as_float(rmax_bits) * 1.0001f + 1e-4f;
   // realcal_self (realcal.F90:284-328), fixed-order block reduction
   const bool need_self = (A.self_mode == 1) || (A.self_mode == 2 && b == 0);
+  if (need_self && A.bare) {  // realcal_self returns 0 for bare Coulomb (realcal.F90:294)
+    if (threadIdx.x == 0) a.u_usreal[b] = 0.0;
+    return;
+  }
   if (need_self) {
     double acc = 0.0;
     const int npair = ns * ns;  // (is, js) with js >= is; diagonal gives the atom residual
@@ -326,6 +331,7 @@ cudaError_t launch_place_prep(Engine& e, const BatchArgs& a, const double* sol_x
   A.sc = make_coef(e.P_order, e.P.screen);
   A.mixed = e.mixed ? 1 : 0;
   A.self_mode = self_mode;
+  A.bare = (e.P.cltype == 0) ? 1 : 0;
   A.nummol = e.nummol;
   A.status = e.d_status;
   auto magic = [](unsigned d) { return (unsigned)((0x100000000ull + d - 1) / d); };

@@ -822,6 +822,7 @@ void realcal_proc(const orc_ctx* c, int tagslt, RealWork& w, double* uvengy /*0:
 // realcal_self (realcal.F90:284-328)
 double realcal_self(const orc_ctx* c, int tagslt, const RealWork& w) {
   double pairep = 0.0;
+  if (c->p.elmode == 2) return pairep;  // bare Coulomb (realcal.F90:294)
   double half[3];
   for (int i = 0; i < 3; ++i) half[i] = 0.5 * w.cell_len[i];
   const int ismax = c->numsite[tagslt - 1];
@@ -845,6 +846,7 @@ double realcal_self(const orc_ctx* c, int tagslt, const RealWork& w) {
 
 // residual_ene (engproc.F90:859-869)
 inline double residual_ene(const orc_ctx* c, int i, int j) {
+  if (c->p.elmode == 2) return 0.0;  // engproc.F90:865
   double epcl = PI * c->mol_charge[i - 1] * c->mol_charge[j - 1] / c->p.screen / c->p.screen / c->volume;
   if (i == j) epcl = epcl / 2.0;
   return -epcl;
@@ -950,6 +952,40 @@ int get_uv_energy(const orc_ctx* c, int tagslt, const double* solute_xyz, double
   std::memcpy(sxyz.data(), sitepos + 3 * (size_t)(b - 1), sizeof(double) * 3 * ns);
   realcal_prepare(c, sitepos, w);
   for (int k = 0; k <= c->slvmax; ++k) uvengy[k] = 0.0;
+  if (c->p.elmode == 2) {  // bare Coulomb: realcal_bare per molecule (realcal.F90:155-281)
+    if (self_out) *self_out = 0.0;
+    if (c->sluvid[tagslt - 1] == 0) return ORC_E_RCP_FST;
+    const LjConsts k = lj_consts(c->p);
+    double half[3];
+    for (int i = 0; i < 3; ++i) half[i] = 0.5 * w.cell_len[i];
+    const int T = c->ljtype_max;
+#pragma omp parallel for schedule(dynamic, 64) if (parallel_inner)
+    for (int kk = 1; kk <= c->slvmax; ++kk) {
+      const int i = c->tagpt[kk - 1];
+      if (i == tagslt) continue;
+      double pairep = 0.0;
+      for (int ati = c->mbi[tagslt - 1]; ati < c->mbi[tagslt]; ++ati)
+        for (int atj = c->mbi[i - 1]; atj < c->mbi[i]; ++atj) {
+          double dis2 = 0.0;
+          for (int a = 0; a < 3; ++a) {
+            const double x = w.sitepos_normal[3 * (size_t)(ati - 1) + a] - w.sitepos_normal[3 * (size_t)(atj - 1) + a];
+            const double d = half[a] - std::fabs(half[a] - std::fabs(x));
+            dis2 += d * d;
+          }
+          const double rst = std::sqrt(dis2);
+          const int ti = c->ljtype[ati - 1], tj = c->ljtype[atj - 1];
+          const double ljeps = c->ljene[(ti - 1) + (size_t)T * (tj - 1)];
+          const double ljsgm2 = c->ljlensq[(ti - 1) + (size_t)T * (tj - 1)];
+          double eplj = 0.0;
+          if (rst <= c->p.upljcut)
+            eplj = (dis2 <= k.lw2) ? lj_low(c->p, k, ljeps, ljsgm2, dis2) : lj_switch(c->p, k, ljeps, ljsgm2, dis2);
+          const double epcl = (rst >= c->p.elecut) ? 0.0 : c->charge[ati - 1] * c->charge[atj - 1] / rst;
+          pairep = pairep + eplj + epcl;
+        }
+      uvengy[kk] = pairep;
+    }
+    return ORC_OK;
+  }
   const double self_recip = recpcal_prepare_solute(c, tagslt, sxyz.data(), w);
   realcal_proc(c, tagslt, w, uvengy);
   uvengy[0] = self_recip;
@@ -980,6 +1016,7 @@ double volcorrect(const orc_ctx* c, double weight) {
   double total_charge = 0.0;
   for (int i = 0; i < c->nummol; ++i)
     if (c->sluvid[i] == 0 || c->sluvid[i] == 1) total_charge += c->mol_charge[i];
+  if (c->p.elmode == 2) return weight;  // the charge factor only with Ewald, PME and PPPM
   const double factor = PI * (total_charge * total_charge) / (c->p.screen * c->p.screen) / c->volume / 2.0;
   return weight * std::exp(factor / c->p.temp);
 }
@@ -1316,7 +1353,7 @@ int orc_frame(orc_ctx* c, const double* sitepos, const double* cell, double stat
   bool changed = !c->pme_initialized;
   for (int i = 0; i < 9; ++i) changed = changed || (c->prevcl[i] != c->cell[i]);
   if (changed) {
-    if (c->p.pppm)
+    if (c->p.elmode == 1)
       pppm_greenfunc(c);
     else
       spline_greenfunc(c);

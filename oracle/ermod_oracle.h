@@ -45,7 +45,7 @@ typedef struct orc_params {
   int32_t splodr;
   int32_t ms1max, ms2max, ms3max;
   int32_t wgtslf, corrcal, selfcal, force_calculation;
-  int32_t pppm;     /* 0: PME Green function, 1: PPPM (cltype 3, recpcal.F90:205-319) */
+  int32_t elmode;   /* 0: PME (cltype 2), 1: PPPM (cltype 3, recpcal.F90:205-319), 2: bare Coulomb (cltype 0) */
   double elecut, lwljcut, upljcut, screen;
   double temp;            /* kT in kcal/mol (setconf.F90:313) */
   double block_threshold; /* realcal cell size (setconf.F90:219) */

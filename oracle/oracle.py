@@ -41,7 +41,7 @@ class OrcParams(C.Structure):
         ("slttype", C.c_int32), ("estype", C.c_int32), ("ljswitch", C.c_int32),
         ("splodr", C.c_int32), ("ms1max", C.c_int32), ("ms2max", C.c_int32),
         ("ms3max", C.c_int32), ("wgtslf", C.c_int32), ("corrcal", C.c_int32),
-        ("selfcal", C.c_int32), ("force_calculation", C.c_int32), ("pppm", C.c_int32),
+        ("selfcal", C.c_int32), ("force_calculation", C.c_int32), ("elmode", C.c_int32),
         ("elecut", C.c_double), ("lwljcut", C.c_double), ("upljcut", C.c_double),
         ("screen", C.c_double), ("temp", C.c_double), ("block_threshold", C.c_double),
     ]
@@ -267,7 +267,7 @@ class Oracle:
         for name, _ in OrcParams._fields_:
             if name in params:
                 setattr(p, name, params[name])
-        p.pppm = 1 if int(params.get("cltype", 2)) == 3 else 0
+        p.elmode = {2: 0, 3: 1, 0: 2}[int(params.get("cltype", 2))]
         self.params = dict(params)
         self.ctx = C.c_void_p()
         _check(L.orc_create(C.byref(p), C.byref(self.ctx)), "create")

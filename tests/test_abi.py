@@ -44,7 +44,7 @@ def test_create_rejects_bad_parameters_before_touching_a_device(gpu_lib):
     gpu_lib.ermod_default_params(C.byref(p))
     ctx = C.c_void_p()
     bad = _lib.Params.from_buffer_copy(p)
-    bad.cltype = 0  # bare Coulomb has no GPU path
+    bad.cltype = 1  # Ewald: the reference itself stops on it (setconf.F90:329-331)
     assert gpu_lib.ermod_create(C.byref(bad), 0, C.byref(ctx)) == _lib.E_UNSUPPORTED
     bad = _lib.Params.from_buffer_copy(p)
     bad.abi_version = 99

@@ -187,3 +187,26 @@ def test_pppm_soln_frames(gpu_lib, oracle, precision):
         rg = gpu.placements(tag, want_uvengy=True)
         _check_energies(rg["uvengy"], ro["uvengy"], precision)
     gpu.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_bare_coulomb_refs_accumulators(gpu_lib, oracle, precision):
+    """cltype 0: realcal_bare (LJ + q q / r within elecut), no reciprocal space, no
+    residual, volcorrect without its Ewald factor."""
+    w = helpers.small_refs(wgtslf=0)
+    w.params["cltype"] = 0
+    topo, bins = helpers.build_inputs(w)
+    gpu, orc = _engines(gpu_lib, oracle, w, topo, bins, precision)
+    pos, cell = w.frame(0)
+    pl = w.placements(0, 24)
+    tag = np.full(len(pl), topo["nummol"], np.int32)
+    orc.frame(pos, cell)
+    ro = orc.placements(tag, pl)
+    gpu.frame(pos, cell)
+    rg = gpu.placements(tag, pl, want_uvengy=True)
+    _check_energies(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], precision)
+    assert np.all(rg["uvengy"][:, 0] == 0.0)
+    ag, ao = gpu.accum(), orc.accum()
+    np.testing.assert_allclose(ag["engnorm"], ao["engnorm"], rtol=1e-12)
+    np.testing.assert_allclose(ag["edens"].sum(), ao["edens"].sum(), rtol=1e-12)
+    gpu.close()
