@@ -330,6 +330,61 @@ __device__ __forceinline__ void fft_cols_io(const float2* in, int ies, int ics, 
   }
 }
 
+// ---- compile-time plans for cubic grids of a few common sizes ----------------------
+// The same two Stockham passes as fft_cols_io, with the transform length, radices,
+// column count, strides and thread count known to the compiler, so that the index
+// arithmetic (the ALU share of the transforms) folds into constants.
+constexpr int kPmeThreads = 512;  // pme_b (and pme_a)
+
+constexpr bool radix_ok(int r) {
+  return r == 16 || r == 15 || r == 12 || r == 10 || r == 9 || r == 8 || r == 6 || r == 5 || r == 4 || r == 3 ||
+         r == 2;
+}
+constexpr int first_radix(int n) {  // make_fft_plan's two-pass choice (first radix from the top)
+  return (n % 16 == 0 && radix_ok(n / 16)) ? 16
+       : (n % 15 == 0 && radix_ok(n / 15)) ? 15
+       : (n % 12 == 0 && radix_ok(n / 12)) ? 12
+       : (n % 10 == 0 && radix_ok(n / 10)) ? 10
+       : (n % 9 == 0 && radix_ok(n / 9))   ? 9
+       : (n % 8 == 0 && radix_ok(n / 8))   ? 8
+       : (n % 6 == 0 && radix_ok(n / 6))   ? 6
+                                           : 0;
+}
+
+template <int R, int N, int NS, int NCOLS, int IES, int ICS, int OES, int OCS, int NT>
+__device__ __forceinline__ void stockham_pass_t(const float2* __restrict__ A, float2* __restrict__ B,
+                                                const float2* __restrict__ tw) {
+  constexpr int NR = N / R, TOTAL = NCOLS * NR, STEP = N / (NS * R);
+  for (int t = threadIdx.x; t < TOTAL; t += NT) {
+    const int j = t / NCOLS;
+    const int col = t - j * NCOLS;
+    const int jq = j / NS;
+    const int k = j - jq * NS;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = A[col * ICS + (j + r * NR) * IES];
+    if (NS > 1 && k > 0) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[r * k * STEP]);
+    }
+    Dft<R>::run(v);
+    const int idxD = jq * NS * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) B[(size_t)col * OCS + (size_t)(idxD + r * NS) * OES] = v[r];
+  }
+}
+
+// two passes: in (IES, ICS) -> mid (ES, CS) -> out (OES, OCS); each pass starts with a barrier
+template <int N, int NCOLS, int IES, int ICS, int ES, int CS, int OES, int OCS, int NT>
+__device__ __forceinline__ void fft2_t(const float2* in, float2* mid, float2* out, const float2* tw) {
+  constexpr int R0 = first_radix(N), R1 = N / R0;
+  static_assert(R0 > 0 && radix_ok(R1), "no two-pass plan");
+  __syncthreads();
+  stockham_pass_t<R0, N, 1, NCOLS, IES, ICS, ES, CS, NT>(in, mid, tw);
+  __syncthreads();
+  stockham_pass_t<R1, N, R0, NCOLS, ES, CS, OES, OCS, NT>(mid, out, tw);
+}
+
 struct ff {
   float hi, lo;
 };
@@ -362,8 +417,8 @@ struct PmeArgs {
   FastDiv fH, fK1, fHp4, fnpair, fKX;
 };
 
-constexpr int kPmeThreads = 512;
-
+// KC > 0: a K^3 grid with K = KC and compile-time transforms; KC = 0: any grid
+template <int KC>
 __global__ void __launch_bounds__(kPmeThreads, 2) pme_a_kernel(PmeArgs A) {
   extern __shared__ float2 sm[];
   const int k2 = blockIdx.x, b = blockIdx.y;
@@ -465,7 +520,12 @@ __global__ void __launch_bounds__(kPmeThreads, 2) pme_a_kernel(PmeArgs A) {
   // ---- inverse transform along k3 (columns k1, element stride Hp); the last pass
   // writes T1[b][z][k2][k1] ----
   float2* out = A.t1 + (size_t)b * K3 * A.K2 * H + (size_t)k2 * H;
-  fft_cols_io(slab, Hp, 1, work, slab, A.p3, H, A.fH, Hp, 1, out, A.K2 * H, 1, tw3);
+  if constexpr (KC > 0) {
+    constexpr int HC = KC / 2 + 1, HPC = ((HC + kR1 - 1) / kR1) * kR1;
+    fft2_t<KC, HC, HPC, 1, HPC, 1, KC * HC, 1, kPmeThreads>(slab, work, out, tw3);
+  } else {
+    fft_cols_io(slab, Hp, 1, work, slab, A.p3, H, A.fH, Hp, 1, out, A.K2 * H, 1, tw3);
+  }
   if (threadIdx.x == 0) {
     double t = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += wsum[w];
@@ -476,6 +536,7 @@ __global__ void __launch_bounds__(kPmeThreads, 2) pme_a_kernel(PmeArgs A) {
 // CTA per (z, placement): the k2 transform of the (k2, k1) plane, then the
 // complex-to-real transform along k1, two rows per complex transform; writes the real
 // plane phi[b][z][y][x] with coalesced row stores.
+template <int KC>
 __global__ void __launch_bounds__(kPmeThreads, 2) pme_b_kernel(PmeArgs A) {
   extern __shared__ float2 sm[];
   const int z = blockIdx.x, b = blockIdx.y;
@@ -499,7 +560,12 @@ __global__ void __launch_bounds__(kPmeThreads, 2) pme_b_kernel(PmeArgs A) {
   // reads the plane from global memory
   const int np2 = A.p2.npass;
   float2* r = (np2 == 1) ? s0 : ((((np2 - 2) & 1) ? s0 : s1));  // not the last pass's source
-  fft_cols_io(in, H, 1, s0, s1, A.p2, H, A.fH, H, 1, r, H, 1, tw2);
+  if constexpr (KC > 0) {
+    constexpr int HC = KC / 2 + 1;
+    fft2_t<KC, HC, HC, 1, HC, 1, HC, 1, kPmeThreads>(in, s0, r, tw2);
+  } else {
+    fft_cols_io(in, H, 1, s0, s1, A.p2, H, A.fH, H, 1, r, H, 1, tw2);
+  }
   __syncthreads();
   float2* w = (r == s0) ? s1 : s0;
   // pack row pairs: Z_p[k] = X_{2p}[k] + i X_{2p+1}[k], Hermitian-completed in k1;
@@ -526,7 +592,14 @@ __global__ void __launch_bounds__(kPmeThreads, 2) pme_b_kernel(PmeArgs A) {
     }
     w[(size_t)pp * K1p + k] = make_float2(x0.x - x1.y, x0.y + x1.x);
   }
-  float2* res = fft_cols(w, r, A.p1, npair, A.fnpair, 1, K1p, tw1);
+  float2* res;
+  if constexpr (KC > 0) {  // in place: w -> r -> w
+    fft2_t<KC, KC / 2, 1, KC + 1, 1, KC + 1, 1, KC + 1, kPmeThreads>(w, r, w, tw1);
+    __syncthreads();
+    res = w;
+  } else {
+    res = fft_cols(w, r, A.p1, npair, A.fnpair, 1, K1p, tw1);
+  }
   // padded periodic layout: grid point (x, y, z) lives at (x+h, y+h, z+h), h = P-1, and
   // the last h points of every axis are repeated below 0, so any stencil halo of the
   // gather is one in-bounds box (rows XP floats, planes YP rows, ZP planes)
@@ -596,26 +669,37 @@ cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a) {
   A.fnpair = make_fastdiv((A.K2 + 1) / 2);
   A.fKX = make_fastdiv(A.K1 + A.halo);
   const size_t sa = pme_a_smem(A.K3, A.Hp), sb = pme_b_smem(A.K1, A.K2, A.H);
-  static size_t attr_a = 0, attr_b = 0;
   cudaError_t err;
-  if (attr_a < sa) {
-    if ((err = cudaFuncSetAttribute(pme_a_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sa)) != cudaSuccess)
+  // cubic grids of common sizes take the compile-time transforms
+  const bool cubic = A.K1 == A.K2 && A.K2 == A.K3;
+  const int KC = (cubic && (A.K1 == 32 || A.K1 == 48 || A.K1 == 64 || A.K1 == 96 || A.K1 == 128)) ? A.K1 : 0;
+  void (*ka)(PmeArgs) = pme_a_kernel<0>;
+  void (*kb)(PmeArgs) = pme_b_kernel<0>;
+  if (KC == 32) ka = pme_a_kernel<32>, kb = pme_b_kernel<32>;
+  if (KC == 48) ka = pme_a_kernel<48>, kb = pme_b_kernel<48>;
+  if (KC == 64) ka = pme_a_kernel<64>, kb = pme_b_kernel<64>;
+  if (KC == 96) ka = pme_a_kernel<96>, kb = pme_b_kernel<96>;
+  if (KC == 128) ka = pme_a_kernel<128>, kb = pme_b_kernel<128>;
+  static size_t attr_a[6] = {}, attr_b[6] = {};  // per specialisation: largest size set so far
+  const int slot = KC == 0 ? 0 : (KC == 32 ? 1 : (KC == 48 ? 2 : (KC == 64 ? 3 : (KC == 96 ? 4 : 5))));
+  if (attr_a[slot] < sa) {
+    if ((err = cudaFuncSetAttribute(ka, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sa)) != cudaSuccess)
       return err;
-    attr_a = sa;
+    attr_a[slot] = sa;
   }
-  if (attr_b < sb) {
-    if ((err = cudaFuncSetAttribute(pme_b_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb)) != cudaSuccess)
+  if (attr_b[slot] < sb) {
+    if ((err = cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb)) != cudaSuccess)
       return err;
-    attr_b = sb;
+    attr_b[slot] = sb;
   }
-  pme_a_kernel<<<dim3(A.K2, a.nb), kPmeThreads, sa, a.stream>>>(A);
+  ka<<<dim3(A.K2, a.nb), kPmeThreads, sa, a.stream>>>(A);
   e.count_launch();
   if ((err = cudaGetLastError()) != cudaSuccess) return err;
   if (a.phases) {
     e.phase_end_on(a.stream);
     e.phase_begin_on(PH_FFT, a.stream);
   }
-  pme_b_kernel<<<dim3(A.K3, a.nb), kPmeThreads, sb, a.stream>>>(A);
+  kb<<<dim3(A.K3, a.nb), kPmeThreads, sb, a.stream>>>(A);
   e.count_launch();
   return cudaGetLastError();
 }
