@@ -422,7 +422,9 @@ template <int KC>
 __global__ void __launch_bounds__(kPmeThreads, 2) pme_a_kernel(PmeArgs A) {
   extern __shared__ float2 sm[];
   const int k2 = blockIdx.x, b = blockIdx.y;
-  const int K3 = A.K3, H = A.H, Hp = A.Hp;
+  // compile-time sizes when specialised (the runtime values are then equal)
+  const int K3 = KC ? KC : A.K3, H = KC ? KC / 2 + 1 : A.H;
+  const int Hp = KC ? ((KC / 2 + 1 + kR1 - 1) / kR1) * kR1 : A.Hp;
   float2* slab = sm;                          // [K3][Hp]
   float2* work = sm + (size_t)K3 * Hp;        // [K3][Hp]; site staging during generation
   float2* tw3 = work + (size_t)K3 * Hp;       // [K3]
@@ -457,7 +459,7 @@ __global__ void __launch_bounds__(kPmeThreads, 2) pme_a_kernel(PmeArgs A) {
     }
     __syncthreads();
     for (int mt = threadIdx.x; mt < TX * TY; mt += blockDim.x) {
-      const int ty = fdiv(mt, A.fHp4), tx = mt - ty * TX;
+      const int ty = KC ? mt / TX : fdiv(mt, A.fHp4), tx = mt - ty * TX;
       const int k1a = tx * kR1, k3a = ty * kR3;
       float2 acc[kR3][kR1];
 #pragma unroll
@@ -540,7 +542,8 @@ template <int KC>
 __global__ void __launch_bounds__(kPmeThreads, 2) pme_b_kernel(PmeArgs A) {
   extern __shared__ float2 sm[];
   const int z = blockIdx.x, b = blockIdx.y;
-  const int K1 = A.K1, K2 = A.K2, K3 = A.K3, H = A.H, K1p = A.K1p;
+  const int K1 = KC ? KC : A.K1, K2 = KC ? KC : A.K2, K3 = KC ? KC : A.K3;
+  const int H = KC ? KC / 2 + 1 : A.H, K1p = KC ? KC + 1 : A.K1p;
   const size_t plane = (size_t)K2 * H;
   const int npair = (K2 + 1) / 2;
   const size_t bufsz = max(plane, (size_t)npair * K1p);
@@ -571,7 +574,7 @@ __global__ void __launch_bounds__(kPmeThreads, 2) pme_b_kernel(PmeArgs A) {
   // pack row pairs: Z_p[k] = X_{2p}[k] + i X_{2p+1}[k], Hermitian-completed in k1;
   // rows padded to K1p (odd) so the row transforms are bank-conflict free
   for (int t = threadIdx.x; t < npair * K1; t += blockDim.x) {
-    const int pp = fdiv(t, A.fK1), k = t - pp * K1;
+    const int pp = KC ? t / KC : fdiv(t, A.fK1), k = t - pp * K1;
     const int y0 = 2 * pp, y1 = 2 * pp + 1;
     float2 x0, x1 = make_float2(0.f, 0.f);
     const bool self_conj = (k == 0) || ((K1 % 2 == 0) && k == K1 / 2);
