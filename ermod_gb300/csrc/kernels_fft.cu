@@ -573,27 +573,29 @@ __global__ void __launch_bounds__(kPmeThreads, 2) pme_b_kernel(PmeArgs A) {
   float2* w = (r == s0) ? s1 : s0;
   // pack row pairs: Z_p[k] = X_{2p}[k] + i X_{2p+1}[k], Hermitian-completed in k1;
   // rows padded to K1p (odd) so the row transforms are bank-conflict free
-  for (int t = threadIdx.x; t < npair * K1; t += blockDim.x) {
-    const int pp = KC ? t / KC : fdiv(t, A.fK1), k = t - pp * K1;
-    const int y0 = 2 * pp, y1 = 2 * pp + 1;
-    float2 x0, x1 = make_float2(0.f, 0.f);
-    const bool self_conj = (k == 0) || ((K1 % 2 == 0) && k == K1 / 2);
-    if (k < H) {
-      x0 = r[(size_t)y0 * H + k];
-      if (y1 < K2) x1 = r[(size_t)y1 * H + k];
-    } else {
-      const float2 a = r[(size_t)y0 * H + (K1 - k)];
-      x0 = make_float2(a.x, -a.y);
-      if (y1 < K2) {
-        const float2 c = r[(size_t)y1 * H + (K1 - k)];
-        x1 = make_float2(c.x, -c.y);
+  // one warp per row pair, lanes along k1 (no division); the upper half of k1 is the
+  // conjugate of the stored half
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+  for (int pp = warp; pp < npair; pp += nwarp) {
+    const float2* r0 = r + (size_t)(2 * pp) * H;
+    const float2* r1 = r0 + H;
+    const bool has1 = 2 * pp + 1 < K2;
+    float2* wrow = w + (size_t)pp * K1p;
+    for (int k = lane; k < K1; k += 32) {
+      const bool lo = k < H;
+      const int kk = lo ? k : K1 - k;
+      float2 x0 = r0[kk];
+      float2 x1 = has1 ? r1[kk] : make_float2(0.f, 0.f);
+      if (!lo) {
+        x0.y = -x0.y;
+        x1.y = -x1.y;
       }
+      if (k == 0 || ((K1 % 2 == 0) && k == K1 / 2)) {  // self-conjugate points
+        x0.y = 0.f;
+        x1.y = 0.f;
+      }
+      wrow[k] = make_float2(x0.x - x1.y, x0.y + x1.x);
     }
-    if (self_conj) {
-      x0.y = 0.f;
-      x1.y = 0.f;
-    }
-    w[(size_t)pp * K1p + k] = make_float2(x0.x - x1.y, x0.y + x1.x);
   }
   float2* res;
   if constexpr (KC > 0) {  // in place: w -> r -> w
@@ -610,15 +612,17 @@ __global__ void __launch_bounds__(kPmeThreads, 2) pme_b_kernel(PmeArgs A) {
   float* out = A.phi + (size_t)b * A.ZP * A.YP * A.XP;
   const int KX = K1 + h, KY = K2 + h;  // written extent of a padded plane
   const int ncopy = (z >= K3 - h) ? 2 : 1;
+  const float* resf = reinterpret_cast<const float*>(res);  // row pair p: (y = 2p, 2p+1) interleaved
   for (int c = 0; c < ncopy; ++c) {
     float* plane_out = out + (size_t)(c ? z - K3 + h : z + h) * A.YP * A.XP;
-    for (int t = threadIdx.x; t < KX * KY; t += blockDim.x) {
-      const int yy = fdiv(t, A.fKX), xx = t - yy * KX;
-      int y = yy - h, x = xx - h;
-      if (y < 0) y += K2;
-      if (x < 0) x += K1;
-      const float2 v = res[(size_t)(y >> 1) * K1p + x];
-      plane_out[(size_t)yy * A.XP + xx] = (y & 1) ? v.y : v.x;
+    for (int yy = warp; yy < KY; yy += nwarp) {  // one warp per padded row
+      const int y = (yy < h) ? yy - h + K2 : yy - h;
+      const float* src = resf + 2 * (size_t)(y >> 1) * K1p + (y & 1);
+      float* dst = plane_out + (size_t)yy * A.XP;
+      for (int xx = lane; xx < KX; xx += 32) {
+        const int x = (xx < h) ? xx - h + K1 : xx - h;
+        dst[xx] = src[2 * x];
+      }
     }
   }
 }
