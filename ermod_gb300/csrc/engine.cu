@@ -408,7 +408,7 @@ int ermod_create(const ermod_params* p, int device, ermod_ctx** out) {
   e.geom.K[0] = K[0];
   e.geom.K[1] = K[1];
   e.geom.K[2] = K[2];
-  e.Bmax = e.mixed ? (p->batch > 0 ? p->batch : 32) : 1;
+  e.Bmax = e.mixed ? (p->batch > 0 ? p->batch : 64) : 1;
   e.G = e.mixed ? (e.Bmax % 8 == 0 ? 8 : 4) : 1;
   cudaError_t err = cudaStreamCreateWithFlags(&e.stream, cudaStreamNonBlocking);
   if (err != cudaSuccess) {
