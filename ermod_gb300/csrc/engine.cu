@@ -210,8 +210,9 @@ static int free_bins(Engine& e) {
   return ERMOD_OK;
 }
 
-// TMA descriptor of the padded potential grids, a 4-D tensor
-// [B][ZP][YP][XP] (x innermost); one box = the gather halo of a brick for 4 placements
+// TMA descriptor of the padded potential grids, a 5-D tensor [B/4][ZP][YP][XP][4] (four
+// placements interleaved innermost); one box = the gather halo of a brick for 4
+// placements, landing in shared memory as [z][y][x][4]
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -225,11 +226,11 @@ static int make_phi_tmap(Engine& e, float* phi, CUtensorMap* map) {
     return ERMOD_E_CUDA;
   }
   const cuuint64_t XP = e.phi_dims[0], YP = e.phi_dims[1], ZP = e.phi_dims[2];
-  const cuuint64_t dims[4] = {XP, YP, ZP, (cuuint64_t)e.Bmax};
-  const cuuint64_t strides[3] = {XP * 4, XP * YP * 4, XP * YP * ZP * 4};
-  const cuuint32_t box[4] = {(cuuint32_t)e.gbox[0], (cuuint32_t)e.gbox[1], (cuuint32_t)e.gbox[2], 4};
-  const cuuint32_t estr[4] = {1, 1, 1, 1};
-  const CUresult r = ((EncodeTiledFn)fn)(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, phi, dims, strides, box, estr,
+  const cuuint64_t dims[5] = {4, XP, YP, ZP, (cuuint64_t)((e.Bmax + 3) / 4)};
+  const cuuint64_t strides[4] = {16, XP * 16, XP * YP * 16, XP * YP * ZP * 16};
+  const cuuint32_t box[5] = {4, (cuuint32_t)e.gbox[0], (cuuint32_t)e.gbox[1], (cuuint32_t)e.gbox[2], 1};
+  const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  const CUresult r = ((EncodeTiledFn)fn)(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, phi, dims, strides, box, estr,
                                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {

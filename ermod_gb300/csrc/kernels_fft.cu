@@ -541,7 +541,10 @@ __global__ void __launch_bounds__(kPmeThreads, 2) pme_a_kernel(PmeArgs A) {
 template <int KC>
 __global__ void __launch_bounds__(kPmeThreads, 2) pme_b_kernel(PmeArgs A) {
   extern __shared__ float2 sm[];
-  const int z = blockIdx.x, b = blockIdx.y;
+  // grid (4, K3, ceil(nb / 4)): the four placements that share an interleaved potential
+  // grid run side by side, so their 4-byte stores meet in L2
+  const int z = blockIdx.y, b = 4 * blockIdx.z + blockIdx.x;
+  if (b >= A.nb) return;
   const int K1 = KC ? KC : A.K1, K2 = KC ? KC : A.K2, K3 = KC ? KC : A.K3;
   const int H = KC ? KC / 2 + 1 : A.H, K1p = KC ? KC + 1 : A.K1p;
   const size_t plane = (size_t)K2 * H;
@@ -609,19 +612,20 @@ __global__ void __launch_bounds__(kPmeThreads, 2) pme_b_kernel(PmeArgs A) {
   // the last h points of every axis are repeated below 0, so any stencil halo of the
   // gather is one in-bounds box (rows XP floats, planes YP rows, ZP planes)
   const int h = A.halo;
-  float* out = A.phi + (size_t)b * A.ZP * A.YP * A.XP;
+  // potential grids of 4 placements interleaved: phi[b/4][zp][yp][xp][b%4]
+  float* out = A.phi + (size_t)(b >> 2) * A.ZP * A.YP * A.XP * 4 + (b & 3);
   const int KX = K1 + h, KY = K2 + h;  // written extent of a padded plane
   const int ncopy = (z >= K3 - h) ? 2 : 1;
   const float* resf = reinterpret_cast<const float*>(res);  // row pair p: (y = 2p, 2p+1) interleaved
   for (int c = 0; c < ncopy; ++c) {
-    float* plane_out = out + (size_t)(c ? z - K3 + h : z + h) * A.YP * A.XP;
+    float* plane_out = out + (size_t)(c ? z - K3 + h : z + h) * A.YP * A.XP * 4;
     for (int yy = warp; yy < KY; yy += nwarp) {  // one warp per padded row
       const int y = (yy < h) ? yy - h + K2 : yy - h;
       const float* src = resf + 2 * (size_t)(y >> 1) * K1p + (y & 1);
-      float* dst = plane_out + (size_t)yy * A.XP;
+      float* dst = plane_out + (size_t)yy * A.XP * 4;
       for (int xx = lane; xx < KX; xx += 32) {
         const int x = (xx < h) ? xx - h + K1 : xx - h;
-        dst[xx] = src[2 * x];
+        dst[4 * xx] = src[2 * x];
       }
     }
   }
@@ -706,7 +710,7 @@ cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a) {
     e.phase_end_on(a.stream);
     e.phase_begin_on(PH_FFT, a.stream);
   }
-  kb<<<dim3(A.K3, a.nb), kPmeThreads, sb, a.stream>>>(A);
+  kb<<<dim3(4, A.K3, (a.nb + 3) / 4), kPmeThreads, sb, a.stream>>>(A);
   e.count_launch();
   return cudaGetLastError();
 }

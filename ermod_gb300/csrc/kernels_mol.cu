@@ -637,6 +637,14 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, i
       "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
       : "memory");
 }
+__device__ __forceinline__ void tma_load_5d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            int c4, unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+      "%6}], [%7];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(smem_u32(bar))
+      : "memory");
+}
 __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, uint32_t phase) {
   uint32_t ok;
   asm volatile(
@@ -711,15 +719,15 @@ __global__ void __launch_bounds__(kGatherThreads) gather_tma_kernel(
   extern __shared__ unsigned char smem_raw[];
   __shared__ unsigned long long bar[2];
   const int npt = BZ * BY * BX;
-  float* box0 = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
-  const int boxf = (4 * npt + 31) & ~31;  // box stride in floats, rounded up to 128 bytes (TMA destination)
-  float* box1 = box0 + boxf;
-  float4* halo = reinterpret_cast<float4*>(box1 + boxf);
+  // two halo buffers [z][y][x] of float4 (the four placements of a group), 128-byte aligned
+  float4* halo0 = reinterpret_cast<float4*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
+  const int hstride = (npt + 7) & ~7;  // float4 elements, a multiple of 128 bytes
+  float4* halo1 = halo0 + hstride;
   const int brick = blockIdx.x;
   const int bx = brick % nbx, by = (brick / nbx) % nby, bz = brick / (nbx * nby);
   const int g_begin = blockIdx.y * groups_per_cta;
   const int g_end = min((nb + 3) / 4, g_begin + groups_per_cta);
-  const uint32_t box_bytes = (uint32_t)(4 * npt * sizeof(float));
+  const uint32_t box_bytes = (uint32_t)(npt * sizeof(float4));
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
@@ -727,12 +735,13 @@ __global__ void __launch_bounds__(kGatherThreads) gather_tma_kernel(
     fence_proxy_async_smem();
   }
   __syncthreads();
-  // padded coordinates: the halo of brick (bx, by, bz) starts at 8 bx (x is a multiple of 4)
+  // padded coordinates: the halo of brick (bx, by, bz) starts at (8 bx, 8 by, 8 bz); the
+  // innermost box coordinate (the placement within the group) is 0
   if (threadIdx.x == 0) {
     for (int g = g_begin; g < min(g_end, g_begin + 2); ++g) {
       unsigned long long* br = &bar[(g - g_begin) & 1];
       mbar_expect_tx(br, box_bytes);
-      tma_load_4d(((g - g_begin) & 1) ? box1 : box0, &tmap, bx * 8, by * 8, bz * 8, 4 * g, br);
+      tma_load_5d(((g - g_begin) & 1) ? halo1 : halo0, &tmap, 0, bx * 8, by * 8, bz * 8, g, br);
     }
   }
   const int h = P - 1;
@@ -798,15 +807,7 @@ __global__ void __launch_bounds__(kGatherThreads) gather_tma_kernel(
       }
       return;
     }
-    const float* box = slot ? box1 : box0;
-    for (int t = threadIdx.x; t < npt; t += blockDim.x)
-      halo[t] = make_float4(box[t], box[npt + t], box[2 * npt + t], box[3 * npt + t]);
-    __syncthreads();  // halo ready; box[slot] consumed
-    if (threadIdx.x == 0 && g + 2 < g_end) {
-      fence_proxy_async_smem();
-      mbar_expect_tx(&bar[slot], box_bytes);
-      tma_load_4d(slot ? box1 : box0, &tmap, bx * 8, by * 8, bz * 8, 4 * (g + 2), &bar[slot]);
-    }
+    const float4* halo = slot ? halo1 : halo0;
     const int b0 = 4 * g;
     if (site0 >= 0) {
       const float4 acc = site_stencil<P>(halo, base, BX, w1, w2, w3);
@@ -823,7 +824,12 @@ __global__ void __launch_bounds__(kGatherThreads) gather_tma_kernel(
       *reinterpret_cast<float4*>(site_e + (size_t)site * ldb + b0) =
           make_float4(qs * acc.x, qs * acc.y, qs * acc.z, qs * acc.w);
     }
-    __syncthreads();  // halo reused by the next group
+    __syncthreads();  // halo[slot] consumed: the copy of group g + 2 may land in it
+    if (threadIdx.x == 0 && g + 2 < g_end) {
+      fence_proxy_async_smem();
+      mbar_expect_tx(&bar[slot], box_bytes);
+      tma_load_5d(slot ? halo1 : halo0, &tmap, 0, bx * 8, by * 8, bz * 8, g + 2, &bar[slot]);
+    }
   }
 }
 
@@ -1100,8 +1106,8 @@ cudaError_t launch_gather(Engine& e, const BatchArgs& a) {
   dim3 g1(e.nbricks, (ngroups + gpc - 1) / gpc);
   const int K1 = e.geom.K[0], K2 = e.geom.K[1], K3 = e.geom.K[2];
   const size_t npt = (size_t)e.gbox[0] * e.gbox[1] * e.gbox[2];
-  const size_t boxf = (4 * npt + 31) & ~(size_t)31;  // as in the kernel: 128-byte aligned boxes
-  const size_t sh = 128 + 2 * boxf * sizeof(float) + npt * sizeof(float4);
+  const size_t hstride = (npt + 7) & ~(size_t)7;  // as in the kernel: 128-byte aligned halos
+  const size_t sh = 128 + 2 * hstride * sizeof(float4);
 #define ERMOD_GATHER(PP)                                                                                        \
   if (e.P_order == PP) {                                                                                        \
     static size_t attr = 0;                                                                                     \
