@@ -334,7 +334,8 @@ __device__ __forceinline__ void fft_cols_io(const float2* in, int ies, int ics, 
 // The same two Stockham passes as fft_cols_io, with the transform length, radices,
 // column count, strides and thread count known to the compiler, so that the index
 // arithmetic (the ALU share of the transforms) folds into constants.
-constexpr int kPmeThreads = 512;  // pme_b (and pme_a)
+constexpr int kPmeAThreads = 512, kPmeAMinBlocks = 2;  // pme_a
+constexpr int kPmeBThreads = 512, kPmeBMinBlocks = 2;  // pme_b
 
 constexpr bool radix_ok(int r) {
   return r == 16 || r == 15 || r == 12 || r == 10 || r == 9 || r == 8 || r == 6 || r == 5 || r == 4 || r == 3 ||
@@ -419,7 +420,7 @@ struct PmeArgs {
 
 // KC > 0: a K^3 grid with K = KC and compile-time transforms; KC = 0: any grid
 template <int KC>
-__global__ void __launch_bounds__(kPmeThreads, 2) pme_a_kernel(PmeArgs A) {
+__global__ void __launch_bounds__(kPmeAThreads, kPmeAMinBlocks) pme_a_kernel(PmeArgs A) {
   extern __shared__ float2 sm[];
   const int k2 = blockIdx.x, b = blockIdx.y;
   // compile-time sizes when specialised (the runtime values are then equal)
@@ -440,7 +441,9 @@ __global__ void __launch_bounds__(kPmeThreads, 2) pme_a_kernel(PmeArgs A) {
   // ---- generation: slab(k3, k1) = sum_s [q_s b2_s(k2) b3_s(k3)] b1_s(k1), then (last
   // chunk) the engfac multiply and the self energy sum 0.5 sum_k engfac |S|^2 ----
   float2* sd = work;                         // [chunk][K3]
-  float2* sb = work + (size_t)A.chunk * K3;  // [chunk][Hp]  (Hp, chunk*K3 even: 16-byte aligned rows)
+  // [chunk][kR1][TX]: b1(k1 = kR1 tx + i) at [i][tx], so that the lanes of a warp (consecutive
+  // tx) read consecutive words
+  float2* sb = work + (size_t)A.chunk * K3;
   for (int s0 = 0; s0 < ns; s0 += A.chunk) {
     const int nsc = min(A.chunk, ns - s0);
     const bool last = s0 + A.chunk >= ns;
@@ -455,7 +458,8 @@ __global__ void __launch_bounds__(kPmeThreads, 2) pme_a_kernel(PmeArgs A) {
     }
     for (int t = threadIdx.x; t < nsc * Hp; t += blockDim.x) {
       const int sl = t / Hp, k1 = t - sl * Hp;
-      sb[sl * Hp + k1] = (k1 < H) ? bv[((size_t)(s0 + sl) * 3 + 0) * A.Kmax + k1] : make_float2(0.f, 0.f);
+      sb[sl * Hp + (k1 % kR1) * TX + k1 / kR1] =
+          (k1 < H) ? bv[((size_t)(s0 + sl) * 3 + 0) * A.Kmax + k1] : make_float2(0.f, 0.f);
     }
     __syncthreads();
     for (int mt = threadIdx.x; mt < TX * TY; mt += blockDim.x) {
@@ -470,12 +474,8 @@ __global__ void __launch_bounds__(kPmeThreads, 2) pme_a_kernel(PmeArgs A) {
         float2 d[kR3], e[kR1];
 #pragma unroll
         for (int j = 0; j < kR3; ++j) d[j] = (k3a + j < K3) ? sd[sl * K3 + k3a + j] : make_float2(0.f, 0.f);
-        const float4* e4 = reinterpret_cast<const float4*>(sb + sl * Hp + k1a);
-        const float4 e01 = e4[0], e23 = e4[1];
-        e[0] = make_float2(e01.x, e01.y);
-        e[1] = make_float2(e01.z, e01.w);
-        e[2] = make_float2(e23.x, e23.y);
-        e[3] = make_float2(e23.z, e23.w);
+#pragma unroll
+        for (int i = 0; i < kR1; ++i) e[i] = sb[sl * Hp + i * TX + tx];
 #pragma unroll
         for (int j = 0; j < kR3; ++j)
 #pragma unroll
@@ -517,14 +517,14 @@ __global__ void __launch_bounds__(kPmeThreads, 2) pme_a_kernel(PmeArgs A) {
     ff o{__shfl_down_sync(0xffffffffu, self.hi, off), __shfl_down_sync(0xffffffffu, self.lo, off)};
     self = ff_add2(self, o);
   }
-  __shared__ double wsum[kPmeThreads / 32];
+  __shared__ double wsum[kPmeAThreads / 32];
   if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = (double)self.hi + (double)self.lo;
   // ---- inverse transform along k3 (columns k1, element stride Hp); the last pass
   // writes T1[b][z][k2][k1] ----
   float2* out = A.t1 + (size_t)b * K3 * A.K2 * H + (size_t)k2 * H;
   if constexpr (KC > 0) {
     constexpr int HC = KC / 2 + 1, HPC = ((HC + kR1 - 1) / kR1) * kR1;
-    fft2_t<KC, HC, HPC, 1, HPC, 1, KC * HC, 1, kPmeThreads>(slab, work, out, tw3);
+    fft2_t<KC, HC, HPC, 1, HPC, 1, KC * HC, 1, kPmeAThreads>(slab, work, out, tw3);
   } else {
     fft_cols_io(slab, Hp, 1, work, slab, A.p3, H, A.fH, Hp, 1, out, A.K2 * H, 1, tw3);
   }
@@ -539,7 +539,7 @@ __global__ void __launch_bounds__(kPmeThreads, 2) pme_a_kernel(PmeArgs A) {
 // complex-to-real transform along k1, two rows per complex transform; writes the real
 // plane phi[b][z][y][x] with coalesced row stores.
 template <int KC>
-__global__ void __launch_bounds__(kPmeThreads, 2) pme_b_kernel(PmeArgs A) {
+__global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(PmeArgs A) {
   extern __shared__ float2 sm[];
   // grid (4, K3, ceil(nb / 4)): the four placements that share an interleaved potential
   // grid run side by side, so their 4-byte stores meet in L2
@@ -568,7 +568,7 @@ __global__ void __launch_bounds__(kPmeThreads, 2) pme_b_kernel(PmeArgs A) {
   float2* r = (np2 == 1) ? s0 : ((((np2 - 2) & 1) ? s0 : s1));  // not the last pass's source
   if constexpr (KC > 0) {
     constexpr int HC = KC / 2 + 1;
-    fft2_t<KC, HC, HC, 1, HC, 1, HC, 1, kPmeThreads>(in, s0, r, tw2);
+    fft2_t<KC, HC, HC, 1, HC, 1, HC, 1, kPmeBThreads>(in, s0, r, tw2);
   } else {
     fft_cols_io(in, H, 1, s0, s1, A.p2, H, A.fH, H, 1, r, H, 1, tw2);
   }
@@ -602,7 +602,7 @@ __global__ void __launch_bounds__(kPmeThreads, 2) pme_b_kernel(PmeArgs A) {
   }
   float2* res;
   if constexpr (KC > 0) {  // in place: w -> r -> w
-    fft2_t<KC, KC / 2, 1, KC + 1, 1, KC + 1, 1, KC + 1, kPmeThreads>(w, r, w, tw1);
+    fft2_t<KC, KC / 2, 1, KC + 1, 1, KC + 1, 1, KC + 1, kPmeBThreads>(w, r, w, tw1);
     __syncthreads();
     res = w;
   } else {
@@ -666,8 +666,6 @@ cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a) {
   A.Hp = ((A.H + kR1 - 1) / kR1) * kR1;
   A.Kmax = e.Kmax();
   A.chunk = std::max(1, std::min(kSites, (A.K3 * A.Hp) / (A.K3 + A.Hp)));
-  A.chunk &= ~1;  // even chunk: the b1 staging rows stay 16-byte aligned
-  if (A.chunk < 2) A.chunk = 2;
   A.K1p = A.K1 | 1;
   A.halo = e.P_order - 1;
   A.XP = e.phi_dims[0];
@@ -703,14 +701,14 @@ cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a) {
       return err;
     attr_b[slot] = sb;
   }
-  ka<<<dim3(A.K2, a.nb), kPmeThreads, sa, a.stream>>>(A);
+  ka<<<dim3(A.K2, a.nb), kPmeAThreads, sa, a.stream>>>(A);
   e.count_launch();
   if ((err = cudaGetLastError()) != cudaSuccess) return err;
   if (a.phases) {
     e.phase_end_on(a.stream);
     e.phase_begin_on(PH_FFT, a.stream);
   }
-  kb<<<dim3(4, A.K3, (a.nb + 3) / 4), kPmeThreads, sb, a.stream>>>(A);
+  kb<<<dim3(4, A.K3, (a.nb + 3) / 4), kPmeBThreads, sb, a.stream>>>(A);
   e.count_launch();
   return cudaGetLastError();
 }
