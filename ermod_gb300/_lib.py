@@ -13,15 +13,17 @@ LIB_PATH = os.path.join(HERE, "libermod_gb300.so")
 
 OK = 0
 E_ENG_MIN, E_ENG_SFT, E_ENG_BUG, E_ENG_CNS, E_RCP_CNS, E_RCP_FST = 101, 102, 103, 104, 105, 106
+E_INS_GEO, E_SET_PRS = 107, 108
 W_MBIN = 110
 E_PARAM, E_NONCUBOID, E_UNSUPPORTED = 120, 121, 122
 E_CUDA, E_CUFFT, E_NOMEM, E_DEVICE = 130, 131, 132, 133
 PRECISION_FP64, PRECISION_MIXED = 0, 1
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 # halt_with_error identities (mpiproc.F90:203-264) of the status codes
 REFERENCE_CODE = {E_ENG_MIN: "eng_min", E_ENG_SFT: "eng_sft", E_ENG_BUG: "eng_bug", E_ENG_CNS: "eng_cns",
-                  E_RCP_CNS: "rcp_cns", E_RCP_FST: "rcp_fst", W_MBIN: "mbin"}
+                  E_RCP_CNS: "rcp_cns", E_RCP_FST: "rcp_fst", E_INS_GEO: "ins_geo", E_SET_PRS: "set_prs",
+                  W_MBIN: "mbin"}
 
 
 class Params(C.Structure):
@@ -32,7 +34,7 @@ class Params(C.Structure):
         ("force_calculation", C.c_int32), ("precision", C.c_int32), ("batch", C.c_int32),
         ("count_mirror", C.c_int32),
         ("elecut", C.c_double), ("lwljcut", C.c_double), ("upljcut", C.c_double), ("screen", C.c_double),
-        ("temp", C.c_double), ("block_threshold", C.c_double),
+        ("temp", C.c_double), ("block_threshold", C.c_double), ("boxshp", C.c_int32), ("reserved_", C.c_int32),
     ]
 
 

@@ -10,6 +10,7 @@
 #include <cufft.h>
 
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -327,6 +328,8 @@ const char* ermod_status_string(int s) {
     case ERMOD_E_ENG_CNS: return "eng_cns: inconsistency in the species assignment";
     case ERMOD_E_RCP_CNS: return "rcp_cns: inconsistency in the reciprocal-space set-up";
     case ERMOD_E_RCP_FST: return "rcp_fst: the solute must not be a solvent";
+    case ERMOD_E_INS_GEO: return "ins_geo: the system geometry is incorrectly set";
+    case ERMOD_E_SET_PRS: return "set_prs: the system parameters are incorrectly set";
     case ERMOD_W_MBIN: return "mbin: the maximum binning energy is too low for this species";
     case ERMOD_E_PARAM: return "invalid argument";
     case ERMOD_E_NONCUBOID: return "a non-cuboidal cell is not supported";
@@ -362,12 +365,30 @@ void ermod_default_params(ermod_params* p) {
   p->screen = 0.0;
   p->temp = 300.0 * 8.314510e-3 / 4.184;
   p->block_threshold = 4.0;
+  p->boxshp = 1;
+  p->reserved_ = 0;
 }
 
-int ermod_create(const ermod_params* p, int device, ermod_ctx** out) {
-  if (!p || !out) return fail_param("null argument");
+int ermod_create(const ermod_params* p_in, int device, ermod_ctx** out) {
+  if (!p_in || !out) return fail_param("null argument");
   *out = nullptr;
-  if (p->abi_version != ERMOD_ABI_VERSION) return fail_param("abi_version mismatch");
+  // version 1 of the struct ends before boxshp: copy what it has, periodic system
+  ermod_params pv{};
+  if (p_in->abi_version == 1) {
+    std::memcpy(&pv, p_in, offsetof(ermod_params, boxshp));
+    pv.abi_version = ERMOD_ABI_VERSION;
+    pv.boxshp = 1;
+  } else if (p_in->abi_version == ERMOD_ABI_VERSION) {
+    pv = *p_in;
+  } else {
+    return fail_param("abi_version mismatch");
+  }
+  const ermod_params* p = &pv;
+  if (p->boxshp != 0 && p->boxshp != 1) return fail_param("boxshp must be 0 (non-periodic) or 1 (periodic)");
+  if (p->boxshp == 0 && (p->estype == 2 || p->cltype != 0)) {  // setconf.F90:368-372
+    g_err = "set_prs: a non-periodic system needs estype 1 (NVT) and cltype 0 (bare Coulomb)";
+    return ERMOD_E_SET_PRS;
+  }
   if (p->cltype != 0 && p->cltype != 2 && p->cltype != 3) {  // 1 (Ewald) stops in the reference (set_prs)
     g_err = "cltype 0 (bare Coulomb), 2 (PME) and 3 (PPPM) are implemented on the GPU";
     return ERMOD_E_UNSUPPORTED;
@@ -751,7 +772,31 @@ int ermod_set_bins(ermod_ctx* c, int numslv, const int* uvmax, const int* uvsoft
   return ERMOD_OK;
 }
 
-static int frame_common(Engine& e, const double* cell, double sws) {
+static int frame_common(Engine& e, const double* cell, double sws, double extent) {
+  if (e.P.boxshp == 0) {
+    // non-periodic: the cell is not used (NVT, bare Coulomb).  The fixed-point
+    // coordinates and the spatial sort take a virtual cube, a power of two at least
+    // 8 x the largest |coordinate|, so that pair differences of the frame's sites and of
+    // solute sites within `reach` of the origin stay below half of it
+    if (!std::isfinite(extent)) return fail_param("non-finite coordinates");
+    std::memcpy(e.cell, cell, sizeof(double) * 9);
+    e.stat_weight_system = sws;
+    FrameGeom& g = e.geom;
+    const double ext = std::max(extent, 16.0);
+    double Lv = 128.0;
+    while (Lv < 8.0 * ext) Lv *= 2.0;
+    for (int i = 0; i < 9; ++i) g.invcl[i] = 0.0;
+    for (int i = 0; i < 3; ++i) {
+      g.L[i] = Lv;
+      g.invL[i] = 1.0 / Lv;
+      g.fx_scale[i] = Lv / 4294967296.0;
+      g.invcl[4 * i] = 1.0 / Lv;
+    }
+    g.volume = Lv * Lv * Lv;
+    g.periodic = 0;
+    g.reach = 0.5 * Lv - ext;
+    return ERMOD_OK;
+  }
   // cuboid cells only (realcal.F90:859-866); lower off-diagonals too, since the QR
   // rotation of normalize_periodic is not applied
   if (std::fabs(cell[3]) > 1e-8 || std::fabs(cell[6]) > 1e-8 || std::fabs(cell[7]) > 1e-8 ||
@@ -784,6 +829,8 @@ static int frame_common(Engine& e, const double* cell, double sws) {
     g.invL[i] = 1.0 / g.L[i];
     g.fx_scale[i] = g.L[i] / 4294967296.0;
   }
+  g.periodic = 1;
+  g.reach = 0.0;
   return ERMOD_OK;
 }
 
@@ -808,7 +855,16 @@ int ermod_frame(ermod_ctx* c, const double* sitepos, const double* cell, double 
   Engine& e = c->e;
   if (!e.topo_ready) return fail_param("ermod_set_topology must come first");
   cudaSetDevice(e.device);
-  int st = frame_common(e, cell, sws);
+  double extent = 0.0;
+  if (e.P.boxshp == 0) {
+    bool finite = true;
+    for (size_t i = 0; i < 3 * (size_t)e.numatm; ++i) {
+      finite = finite && std::isfinite(sitepos[i]);
+      extent = std::max(extent, std::fabs(sitepos[i]));
+    }
+    if (!finite) extent = std::nan("");
+  }
+  int st = frame_common(e, cell, sws, extent);
   if (st) return st;
   ERMOD_CUDA(cudaMemcpyAsync(e.d_sitepos, sitepos, sizeof(double) * 3 * e.numatm, cudaMemcpyHostToDevice, e.stream));
   st = frame_launch(e);
@@ -822,7 +878,9 @@ int ermod_frame_device(ermod_ctx* c, const double* sitepos_d, const double* cell
   Engine& e = c->e;
   if (!e.topo_ready) return fail_param("ermod_set_topology must come first");
   cudaSetDevice(e.device);
-  int st = frame_common(e, cell, sws);
+  double extent = 0.0;
+  if (e.P.boxshp == 0) ERMOD_CUDA(launch_max_abs(e, sitepos_d, 3 * (size_t)e.numatm, &extent));
+  int st = frame_common(e, cell, sws, extent);
   if (st) return st;
   ERMOD_CUDA(cudaMemcpyAsync(e.d_sitepos, sitepos_d, sizeof(double) * 3 * e.numatm, cudaMemcpyDeviceToDevice,
                              e.stream));
@@ -1004,13 +1062,17 @@ static int reset_status(Engine& e) {  // memsets only, so that a graph capture c
 static int decode_status(Engine& e) {
   const DevStatus s = *e.h_status;
   if (s.mbin_hit || (s.err_key != kNoError && (int)(s.err_key & 0xff) == ERMOD_W_MBIN)) e.warn_bin_firsttime = false;
+  if (s.range_fault) {  // the inputs of the batch were out of range: its energies mean nothing
+    if (s.range_fault & 4)
+      g_err = "non-periodic system: a solute coordinate lies beyond the reach of the frame's fixed-point cube";
+    return ERMOD_E_DEVICE;
+  }
   if (s.err_key != kNoError) {
     e.err_placement = (int)(s.err_key >> 36);
     e.err_molecule = (int)((s.err_key >> 8) & 0x0fffffff);
     e.err_energy = std::nan("");
     return (int)(s.err_key & 0xff);
   }
-  if (s.range_fault) return ERMOD_E_DEVICE;
   return ERMOD_OK;
 }
 
@@ -1356,6 +1418,10 @@ int ermod_generate_placements(ermod_ctx* c, int nplace, int nsite, const double*
   if ((ip->insposition == 2 || ip->insposition == 3 || ip->insposition == 4) && !(ip->upreg >= ip->lwreg))
     return fail_param("upreg < lwreg");
   if ((ip->insposition == 5 || ip->insposition == 6) && !(ip->upreg > 0.0)) return fail_param("upreg must be > 0");
+  if (e.P.boxshp == 0 && (ip->insposition == 0 || ip->insposition == 3 || ip->insposition == 4)) {
+    g_err = "ins_geo: random and slab insertion need a periodic system";  // insertion.F90:155,186
+    return ERMOD_E_INS_GEO;
+  }
   if (nplace <= 0) return ERMOD_OK;
   cudaSetDevice(e.device);
   if (!e.d_ins) ERMOD_CUDA(dalloc(&e.d_ins, 4 * (size_t)kMaxSoluteSites));
@@ -1411,6 +1477,10 @@ int ermod_graph_create(int nctx, ermod_ctx* const* ctx, const double* const* sit
       g_err = "graph capture runs the mixed-precision path only";
       return ERMOD_E_UNSUPPORTED;
     }
+    if (e.P.boxshp == 0) {  // its frame set-up reads the coordinate extent back to the host
+      g_err = "graph capture takes periodic systems only";
+      return ERMOD_E_UNSUPPORTED;
+    }
     if (!e.topo_ready || !e.bins_ready || !e.frame_ready || !e.buf.u_nsite)
       return fail_param("every system needs one ordinary frame + placements step before capture");
     if (solute_mol[i] < 1 || solute_mol[i] > e.nummol) return fail_param("solute_mol out of range");
@@ -1455,7 +1525,7 @@ int ermod_graph_create(int nctx, ermod_ctx* const* ctx, const double* const* sit
     e.timing = false;
     if ((err = cudaStreamWaitEvent(e.stream, g->ev_fork, 0)) != cudaSuccess) st = fail_cuda(err, "fork");
     if (st == ERMOD_OK)
-      st = frame_common(e, cells + 9 * (size_t)i, stat_weight_system ? stat_weight_system[i] : 1.0);
+      st = frame_common(e, cells + 9 * (size_t)i, stat_weight_system ? stat_weight_system[i] : 1.0, 0.0);
     if (st == ERMOD_OK &&
         (err = cudaMemcpyAsync(e.d_sitepos, sitepos_d[i], sizeof(double) * 3 * e.numatm, cudaMemcpyDeviceToDevice,
                                e.stream)) != cudaSuccess)

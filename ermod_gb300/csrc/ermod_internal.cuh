@@ -74,6 +74,12 @@ struct FrameGeom {
   double volume;
   double fx_scale[3];  // L / 2^32 (fixed point -> Angstrom)
   int K[3];
+  // boxshp: 1 periodic; 0 non-periodic (realcal.F90:174,202): coordinates are not wrapped
+  // and distances take no minimum image.  L is then a virtual cube for the fixed-point
+  // coordinates and the spatial sort, large enough that no pair difference wraps, and
+  // every solute coordinate must satisfy |x| < reach.
+  int periodic;
+  double reach;
 };
 
 // Device status block (one per context, zeroed by ermod_sync).
@@ -129,6 +135,7 @@ struct Engine;
 // ---- launchers (defined in the .cu files) ---------------------------------------
 // frame preparation
 cudaError_t launch_frame_wrap(Engine& e);
+cudaError_t launch_max_abs(Engine& e, const double* x_d, size_t n, double* host_out);  // syncs e.stream
 cudaError_t launch_frame_sort(Engine& e);
 cudaError_t launch_frame_sites(Engine& e);
 cudaError_t launch_greenfunc(Engine& e);

@@ -15,6 +15,7 @@
 // All of these are HBM-streaming kernels over O(numatm) or O(K^3) elements.
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
+#include <cstring>
 
 #include "engine.cuh"
 
@@ -91,7 +92,11 @@ __global__ void frame_wrap_kernel(const double* __restrict__ pos, int numatm, Fr
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= numatm) return;
   double w[3];
-  wrap_atom(pos, a, g, w);
+  if (g.periodic) {
+    wrap_atom(pos, a, g, w);
+  } else {  // non-periodic: realcal_prepare copies the coordinates as they are
+    for (int i = 0; i < 3; ++i) w[i] = pos[3 * (size_t)a + i];
+  }
   out[3 * (size_t)a + 0] = w[0];
   out[3 * (size_t)a + 1] = w[1];
   out[3 * (size_t)a + 2] = w[2];
@@ -114,7 +119,9 @@ __global__ void frame_key_kernel(const double* __restrict__ wrapped, const int* 
   int c[3];
   const int n[3] = {ncell.x, ncell.y, ncell.z};
   for (int i = 0; i < 3; ++i) {
-    int ci = (int)(wrapped[3 * (size_t)a + i] * g.invL[i] * (double)n[i]);
+    // non-periodic coordinates lie in (-L/2, L/2) of the virtual cube
+    const double f = wrapped[3 * (size_t)a + i] * g.invL[i] + (g.periodic ? 0.0 : 0.5);
+    int ci = (int)(f * (double)n[i]);
     c[i] = min(max(ci, 0), n[i] - 1);
   }
   key[k] = spread3(c[0]) | (spread3(c[1]) << 1) | (spread3(c[2]) << 2);
@@ -340,7 +347,32 @@ __global__ void pppm_greenfunc_kernel(PppmArgs A, double* __restrict__ engfac, f
 
 inline int nblk(size_t n, int t) { return (int)((n + t - 1) / t); }
 
+// largest |x| of n doubles (non-finite values give a non-finite result): one block, the
+// bit patterns of nonnegative doubles order as unsigned integers, NaN above infinity
+__global__ void max_abs_kernel(const double* __restrict__ x, size_t n, unsigned long long* __restrict__ out) {
+  unsigned long long m = 0ull;
+  for (size_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(fabs(x[i]));
+    m = b > m ? b : m;
+  }
+  atomicMax(out, m);
+}
+
 }  // namespace
+
+cudaError_t launch_max_abs(Engine& e, const double* x_d, size_t n, double* host_out) {
+  unsigned long long* d = reinterpret_cast<unsigned long long*>(e.d_frame_scal + 2);  // 8-byte aligned scratch
+  cudaError_t err = cudaMemsetAsync(d, 0, sizeof(unsigned long long), e.stream);
+  if (err != cudaSuccess) return err;
+  max_abs_kernel<<<1, 1024, 0, e.stream>>>(x_d, n, d);
+  e.count_launch();
+  if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  unsigned long long h = 0ull;
+  if ((err = cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, e.stream)) != cudaSuccess) return err;
+  if ((err = cudaStreamSynchronize(e.stream)) != cudaSuccess) return err;
+  std::memcpy(host_out, &h, sizeof(h));
+  return cudaSuccess;
+}
 
 cudaError_t launch_frame_wrap(Engine& e) {
   frame_wrap_kernel<<<nblk(e.numatm, 256), 256, 0, e.stream>>>(e.d_sitepos, e.numatm, e.geom, e.d_wrapped);

@@ -61,7 +61,8 @@ struct MolArgs {
   float fxf[3];    // fixed-point unit per axis (box length / 2^32)
   float screen_f;  // Ewald beta
   float rc_f;      // max(elecut, upljcut)
-  int bare;        // cltype 0: bare Coulomb within elecut, no reciprocal space or residual
+  int bare;        // cltype 0: bare Coulomb within elecut (no cutoff when non-periodic), no reciprocal space
+                   // or residual
   LjK k32;         // LJ switching constants
   double resid_fac;  // pi / screen^2 / volume
   // batch
@@ -205,37 +206,6 @@ __device__ __forceinline__ int wrapi(int x, int K) {
   return x;
 }
 
-// recip gather for one site, FP32
-template <int P>
-__device__ __forceinline__ float gather_site(const float* __restrict__ phi, const float4 rec, int gp, int K1, int K2,
-                                             int K3) {
-  float w1[P], w2[P], w3[P];
-  bspline_w<P>(rec.x, w1);
-  bspline_w<P>(rec.y, w2);
-  bspline_w<P>(rec.z, w3);
-  const int g1 = gp & 1023, g2 = (gp >> 10) & 1023, g3 = (gp >> 20) & 1023;
-  int x[P];
-#pragma unroll
-  for (int c = 0; c < P; ++c) x[c] = wrapi(g1 - c, K1);
-  float acc = 0.f;
-#pragma unroll
-  for (int c3 = 0; c3 < P; ++c3) {
-    const int z = wrapi(g3 - c3, K3);
-    float a3 = 0.f;
-#pragma unroll
-    for (int c2 = 0; c2 < P; ++c2) {
-      const int y = wrapi(g2 - c2, K2);
-      const float* row = phi + ((size_t)z * K2 + y) * K1;
-      float a2 = 0.f;
-#pragma unroll
-      for (int c1 = 0; c1 < P; ++c1) a2 = fmaf(w1[c1], __ldg(row + x[c1]), a2);
-      a3 = fmaf(w2[c2], a2, a3);
-    }
-    acc = fmaf(w3[c3], a3, acc);
-  }
-  return acc;
-}
-
 // fixed-tree block reductions over blockDim.x (power of two) entries
 __device__ __forceinline__ double block_sum(double* sm, double v) {
   sm[threadIdx.x] = v;
@@ -377,7 +347,8 @@ __device__ __forceinline__ long long ordered_key_f(float f) {
 constexpr long long kKeyPosInf = 0x7ff0000000000000ll;
 constexpr long long kKeyNegInf = (long long)0x800fffffffffffffull;  // ordered key of -inf
 
-template <bool MIXED, int P>
+// the plain FP64 path: one placement group per block row, one solvent molecule per thread
+template <int P>
 __global__ void __launch_bounds__(256) mol_energy_kernel(MolArgs A) {
   extern __shared__ int smem_hist[];  // [G][ermax]
   __shared__ double sred[256];
@@ -404,7 +375,6 @@ __global__ void __launch_bounds__(256) mol_energy_kernel(MolArgs A) {
   const int K1 = g.K[0], K2 = g.K[1], K3 = g.K[2];
   const size_t gridn = (size_t)K1 * K2 * K3;
   const LjK64 k64 = make_k64(A);
-  const LjK k32 = to_f32(k64);
   const double rc = fmax(A.elecut, A.upljcut);
   const float mol_r = A.frame_scal[0];
   int sp_off = 0, sp_n = 1, sp_soft = 1;
@@ -424,17 +394,7 @@ __global__ void __launch_bounds__(256) mol_energy_kernel(MolArgs A) {
     if (active) {
       // ---- reciprocal part ----
       double recip = 0.0;
-      if (A.bare) {
-        // bare Coulomb: no reciprocal part
-      } else if (MIXED) {
-        const float* phi = a.phi + (size_t)b * gridn;
-        for (int s = 0; s < ns; ++s) {
-          const float4 rec = A.site_rec[s0 + s];
-          const int gp = A.site_grid[s0 + s];
-          const float acc = gather_site<P>(phi, rec, gp, K1, K2, K3);
-          recip += (double)(rec.w * acc);
-        }
-      } else {
+      if (!A.bare) {  // bare Coulomb: no reciprocal part
         const double* phi = a.phi64 + (size_t)b * gridn;
         for (int s = 0; s < ns; ++s) {
           const int idx = s0 + s;
@@ -462,75 +422,41 @@ __global__ void __launch_bounds__(256) mol_energy_kernel(MolArgs A) {
       const int nu = a.u_nsite[b];
       const size_t ub = (size_t)b * kMaxSoluteSites;
       const float rcut = (float)rc + a.u_radius[b] + mol_r;
-      if (MIXED) {
-        const int4 p0 = A.site_pos[s0];
-        const int4 u0 = a.u_pos[ub];
-        const float dx = (float)(int)((unsigned)p0.x - (unsigned)u0.x) * (float)g.fx_scale[0];
-        const float dy = (float)(int)((unsigned)p0.y - (unsigned)u0.y) * (float)g.fx_scale[1];
-        const float dz = (float)(int)((unsigned)p0.z - (unsigned)u0.z) * (float)g.fx_scale[2];
-        if (dx * dx + dy * dy + dz * dz <= rcut * rcut) {
-          const float beta = (float)A.screen;
-          for (int su = 0; su < nu; ++su) {
-            const int4 up = a.u_pos[ub + su];
-            const float qu = (float)a.u_q[ub + su];
-            float e = 0.f;
-            for (int s = 0; s < ns; ++s) {
-              const int4 vp = A.site_pos[s0 + s];
-              const float ex = (float)(int)((unsigned)vp.x - (unsigned)up.x) * (float)g.fx_scale[0];
-              const float ey = (float)(int)((unsigned)vp.y - (unsigned)up.y) * (float)g.fx_scale[1];
-              const float ez = (float)(int)((unsigned)vp.z - (unsigned)up.z) * (float)g.fx_scale[2];
-              const float r2 = ex * ex + ey * ey + ez * ez;
-              const double ljeps = A.ljene[vp.w + A.T * up.w];
-              if (ljeps > 0) {
-                const float sg2 = (float)A.ljlensq[vp.w + A.T * up.w];
-                if (r2 <= k32.lw2)
-                  e += lj_low<float>(A.ljswitch, k32, (float)ljeps, sg2, r2);
-                else if (r2 <= k32.up2)
-                  e += lj_switch<float>(A.ljswitch, k32, (float)ljeps, sg2, r2);
-              }
-              if (r2 <= k32.ele2) {
-                const float r = sqrtf(r2);
-                e += qu * A.site_rec[s0 + s].w * erfcf(beta * r) / r;
-              }
+      double d0 = 0.0;
+      for (int i = 0; i < 3; ++i) {
+        const double h = 0.5 * g.L[i];
+        const double x = fabs(A.site_x[3 * (size_t)s0 + i] - a.u_x[ub * 3 + i]);
+        const double d = g.periodic ? h - fabs(h - x) : x;
+        d0 += d * d;
+      }
+      if (d0 <= (double)rcut * (double)rcut) {
+        for (int su = 0; su < nu; ++su) {
+          const double* ux = a.u_x + (ub + su) * 3;
+          const double qu = a.u_q[ub + su];
+          const int tu = a.u_pos[ub + su].w;
+          for (int s = 0; s < ns; ++s) {
+            const int idx = s0 + s;
+            double dist = 0.0;
+            for (int i = 0; i < 3; ++i) {  // minimum image only when periodic (realcal.F90:202-209)
+              const double h = 0.5 * g.L[i];
+              const double x = fabs(A.site_x[3 * (size_t)idx + i] - ux[i]);
+              const double d = g.periodic ? h - fabs(h - x) : x;
+              dist += d * d;
             }
-            real += (double)e;
-          }
-        }
-      } else {
-        double d0 = 0.0;
-        for (int i = 0; i < 3; ++i) {
-          const double h = 0.5 * g.L[i];
-          const double d = h - fabs(h - fabs(A.site_x[3 * (size_t)s0 + i] - a.u_x[ub * 3 + i]));
-          d0 += d * d;
-        }
-        if (d0 <= (double)rcut * (double)rcut) {
-          for (int su = 0; su < nu; ++su) {
-            const double* ux = a.u_x + (ub + su) * 3;
-            const double qu = a.u_q[ub + su];
-            const int tu = a.u_pos[ub + su].w;
-            for (int s = 0; s < ns; ++s) {
-              const int idx = s0 + s;
-              double dist = 0.0;
-              for (int i = 0; i < 3; ++i) {
-                const double h = 0.5 * g.L[i];
-                const double d = h - fabs(h - fabs(A.site_x[3 * (size_t)idx + i] - ux[i]));
-                dist += d * d;
-              }
-              const int tv = A.site_pos[idx].w;
-              const double ljeps = A.ljene[tv + A.T * tu];
-              if (ljeps > 0) {
-                const double sg2 = A.ljlensq[tv + A.T * tu];
-                if (dist <= k64.lw2)
-                  real += lj_low64(A.ljswitch, k64, ljeps, sg2, dist);
-                else if (dist <= k64.up2)
-                  real += lj_switch64(A.ljswitch, k64, ljeps, sg2, dist);
-              }
-              if (A.bare) {
-                if (dist < k64.ele2) real += qu * A.site_q[idx] / sqrt(dist);  // realcal_bare
-              } else if (dist <= k64.ele2) {
-                const double r = sqrt(dist);
-                real += qu * A.site_q[idx] * (1.0 - erf(A.screen * r)) / r;
-              }
+            const int tv = A.site_pos[idx].w;
+            const double ljeps = A.ljene[tv + A.T * tu];
+            if (ljeps > 0) {
+              const double sg2 = A.ljlensq[tv + A.T * tu];
+              if (dist <= k64.lw2)
+                real += lj_low64(A.ljswitch, k64, ljeps, sg2, dist);
+              else if (dist <= k64.up2)
+                real += lj_switch64(A.ljswitch, k64, ljeps, sg2, dist);
+            }
+            if (A.bare) {
+              if (dist < k64.ele2) real += qu * A.site_q[idx] / sqrt(dist);  // realcal_bare
+            } else if (dist <= k64.ele2) {
+              const double r = sqrt(dist);
+              real += qu * A.site_q[idx] * (1.0 - erf(A.screen * r)) / r;
             }
           }
         }
@@ -539,8 +465,6 @@ __global__ void __launch_bounds__(256) mol_energy_kernel(MolArgs A) {
       double epcl;
       if (A.bare)
         epcl = 0.0;  // residual_ene returns without a term for bare Coulomb
-      else if (MIXED)
-        epcl = A.resid_fac * a.u_qmol[b] * qmol;
       else
         epcl = kPi * a.u_qmol[b] * qmol / A.screen / A.screen / g.volume;
       double pairep = -epcl;
@@ -1021,17 +945,16 @@ __global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const flo
   }
 }
 
-template <bool MIXED>
 cudaError_t launch_p(Engine& e, const MolArgs& A, dim3 grid, size_t smem) {
   switch (e.P_order) {
     case 4:
-      mol_energy_kernel<MIXED, 4><<<grid, 256, smem, A.a.stream>>>(A);
+      mol_energy_kernel<4><<<grid, 256, smem, A.a.stream>>>(A);
       break;
     case 6:
-      mol_energy_kernel<MIXED, 6><<<grid, 256, smem, A.a.stream>>>(A);
+      mol_energy_kernel<6><<<grid, 256, smem, A.a.stream>>>(A);
       break;
     case 8:
-      mol_energy_kernel<MIXED, 8><<<grid, 256, smem, A.a.stream>>>(A);
+      mol_energy_kernel<8><<<grid, 256, smem, A.a.stream>>>(A);
       break;
     default:
       return cudaErrorInvalidValue;
@@ -1039,14 +962,13 @@ cudaError_t launch_p(Engine& e, const MolArgs& A, dim3 grid, size_t smem) {
   return cudaGetLastError();
 }
 
-template <bool MIXED>
-cudaError_t set_smem_attr(size_t smem) {  // FP64 instantiations only
+cudaError_t set_smem_attr(size_t smem) {
   cudaError_t err = cudaSuccess;
-  err = cudaFuncSetAttribute(mol_energy_kernel<MIXED, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  err = cudaFuncSetAttribute(mol_energy_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
-  err = cudaFuncSetAttribute(mol_energy_kernel<MIXED, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  err = cudaFuncSetAttribute(mol_energy_kernel<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
-  return cudaFuncSetAttribute(mol_energy_kernel<MIXED, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  return cudaFuncSetAttribute(mol_energy_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
 }  // namespace
@@ -1081,7 +1003,8 @@ static MolArgs make_mol_args(Engine& e, const BatchArgs& a) {
   A.mbin_mode = e.warn_bin_firsttime ? (e.P.force_calculation ? 2 : 1) : 0;
   A.g = e.geom;
   A.ljswitch = e.P.ljswitch;
-  A.elecut = e.P.elecut;
+  // non-periodic: the Coulomb cutoff is infinite (realcal.F90:174)
+  A.elecut = e.geom.periodic ? e.P.elecut : HUGE_VAL;
   A.lwljcut = e.P.lwljcut;
   A.upljcut = e.P.upljcut;
   A.screen = e.P.screen;
@@ -1089,7 +1012,7 @@ static MolArgs make_mol_args(Engine& e, const BatchArgs& a) {
   A.resid_fac = A.bare ? 0.0 : kPi / e.P.screen / e.P.screen / e.geom.volume;
   for (int i = 0; i < 3; ++i) A.fxf[i] = (float)e.geom.fx_scale[i];
   A.screen_f = (float)e.P.screen;
-  A.rc_f = (float)std::max(e.P.elecut, e.P.upljcut);
+  A.rc_f = (float)std::max(A.elecut, e.P.upljcut);
   A.k32 = to_f32(make_k64(A));
   A.a = a;
   A.ntile = e.ntile;
@@ -1137,10 +1060,10 @@ cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
   if (!e.mixed) {
     static size_t attr = 0;
     if (attr < smem) {
-      if ((err = set_smem_attr<false>(smem)) != cudaSuccess) return err;
+      if ((err = set_smem_attr(smem)) != cudaSuccess) return err;
       attr = smem;
     }
-    return launch_p<false>(e, A, grid, smem);
+    return launch_p(e, A, grid, smem);
   }
   if (a.G != 8 && a.G != 4) return cudaErrorInvalidValue;
   if (e.P.cltype != 0 && (err = launch_gather(e, a)) != cudaSuccess) return err;

@@ -102,7 +102,12 @@ __global__ void __launch_bounds__(256) place_prep_kernel(PrepArgs A) {
     const double* raw = A.solxyz ? A.solxyz + ((size_t)b * ns + s) * 3 : A.sitepos + 3 * (size_t)(atom0 + s);
     double w[3];
     const bool is_atom1 = (A.solxyz == nullptr) && (atom0 + s == 0);
-    if (is_atom1) {  // atom 1 itself takes the first-pass x shift of its own x
+    if (!g.periodic) {  // non-periodic: coordinates as they are, within the fixed-point reach
+      for (int i = 0; i < 3; ++i) {
+        w[i] = raw[i];
+        if (!(fabs(raw[i]) < g.reach)) atomicOr(&A.status->range_fault, 4);
+      }
+    } else if (is_atom1) {  // atom 1 itself takes the first-pass x shift of its own x
       for (int i = 0; i < 3; ++i) w[i] = raw[i] - g.L[i] * floor(g.invL[i] * raw[i]);
       w[1] = w[1] - g.L[1] * floor(g.invL[1] * w[1]);
       w[0] = w[0] - g.L[0] * floor(g.invL[0] * w[0]);

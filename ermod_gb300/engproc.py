@@ -18,7 +18,7 @@ from ._lib import ErmodError, check  # noqa: F401
 
 PARAM_KEYS = ("slttype", "estype", "ljswitch", "splodr", "ms1max", "ms2max", "ms3max", "wgtslf", "corrcal",
               "selfcal", "force_calculation", "elecut", "lwljcut", "upljcut", "screen", "temp",
-              "block_threshold")
+              "block_threshold", "boxshp")
 
 
 class EnergyRepresentation:

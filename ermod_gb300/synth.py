@@ -114,10 +114,13 @@ class Workload:
     lattice_n: int
     cavity: float = 0.0
     hist: dict = None
+    droplet: float = 0.0      # > 0: non-periodic droplet of this radius, centred on the origin
 
     # ------------------------------------------------------------------
     @property
     def cell(self) -> np.ndarray:
+        if self.droplet > 0:  # non-periodic: the cell is not used; a zero cell is passed
+            return np.zeros((3, 3))
         return np.diag([self.box] * 3)
 
     def species(self):
@@ -135,6 +138,9 @@ class Workload:
         if self.mode == "soln" and self.cavity > 0:
             c = np.full(3, self.box / 2)
             keep = np.linalg.norm(pts - c, axis=1) > self.cavity
+            pts = pts[keep]
+        if self.droplet > 0:
+            keep = np.linalg.norm(pts - np.full(3, self.box / 2), axis=1) < self.droplet
             pts = pts[keep]
         if len(pts) > self.nwater:
             pick = np.sort(rng.choice(len(pts), self.nwater, replace=False))
@@ -156,6 +162,8 @@ class Workload:
         sl = self.solute["xyz"] - insertion.center_of_mass(self.solute["xyz"], self.solute["mass"])
         sl = sl + self.box / 2
         pos = np.concatenate([wat.reshape(-1, 3), sl], axis=0)
+        if self.droplet > 0:
+            pos = pos - self.box / 2
         return np.ascontiguousarray(pos), self.cell
 
     def placements(self, i: int, n: int = None):
@@ -190,6 +198,15 @@ def refs_large(seed: int = 3, frames: int = 20, ins: int = 50000) -> Workload:
     rng = np.random.default_rng((seed, 11))
     return Workload("refs_large", "refs", 99.5, 33000, random_solute(rng, 12),
                     _params(2, 96, corrcal=1, wgtslf=1), seed, frames, ins, 33)
+
+
+def droplet(seed: int = 6, frames: int = 20) -> Workload:
+    """Non-periodic (boxshp 0) water droplet of radius 13 A around the methanol-like
+    solute, centred on the origin: bare Coulomb without cutoff, NVT."""
+    p = _params(1, 32, corrcal=0, wgtslf=0, estype=1)
+    p.update(cltype=0, boxshp=0)
+    return Workload("droplet", "soln", 31.0, 300, methanol_like(), p, seed, frames, 1, 11, cavity=4.5,
+                    droplet=13.0)
 
 
 def soln_adjoint(seed: int = 5, frames: int = 200) -> Workload:

@@ -8,10 +8,10 @@ module ermod_gpu
   use, intrinsic :: iso_c_binding
   implicit none
 
-  integer(c_int), parameter :: ERMOD_ABI_VERSION = 1
+  integer(c_int), parameter :: ERMOD_ABI_VERSION = 2
   integer(c_int), parameter :: ERMOD_OK = 0, ERMOD_E_ENG_MIN = 101, ERMOD_E_ENG_SFT = 102, &
        ERMOD_E_ENG_BUG = 103, ERMOD_E_ENG_CNS = 104, ERMOD_E_RCP_CNS = 105, ERMOD_E_RCP_FST = 106, &
-       ERMOD_W_MBIN = 110
+       ERMOD_E_INS_GEO = 107, ERMOD_E_SET_PRS = 108, ERMOD_W_MBIN = 110
   integer(c_int), parameter :: ERMOD_PRECISION_FP64 = 0, ERMOD_PRECISION_MIXED = 1
 
   type, bind(C) :: ermod_params
@@ -19,6 +19,7 @@ module ermod_gpu
      integer(c_int32_t) :: ms1max, ms2max, ms3max, wgtslf, corrcal, selfcal
      integer(c_int32_t) :: force_calculation, precision, batch, count_mirror
      real(c_double) :: elecut, lwljcut, upljcut, screen, temp, block_threshold
+     integer(c_int32_t) :: boxshp, reserved_
   end type ermod_params
 
   interface

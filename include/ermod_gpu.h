@@ -27,7 +27,9 @@
 extern "C" {
 #endif
 
-#define ERMOD_ABI_VERSION 1
+/* 2 added ermod_params.boxshp; a version-1 struct (without it) is still accepted and
+ * means a periodic system. */
+#define ERMOD_ABI_VERSION 2
 
 /* Status codes.  The 1xx codes map one-to-one to ERmod's halt_with_error / warning
  * identities (mpiproc.F90:203-264) so that a Fortran wrapper can call
@@ -40,6 +42,8 @@ typedef enum ermod_status {
   ERMOD_E_ENG_CNS = 104,   /* 'eng_cns': solvent with uvspec <= 0 (engproc.F90:817) */
   ERMOD_E_RCP_CNS = 105,   /* 'rcp_cns' (recpcal.F90:335,474) */
   ERMOD_E_RCP_FST = 106,   /* 'rcp_fst': the solute is a solvent (recpcal.F90:469) */
+  ERMOD_E_INS_GEO = 107,   /* 'ins_geo': random or slab insertion in a non-periodic system (insertion.F90:155,186) */
+  ERMOD_E_SET_PRS = 108,   /* 'set_prs': a non-periodic system needs NVT and bare Coulomb (setconf.F90:368-372) */
   ERMOD_W_MBIN = 110,      /* 'mbin' warning without force_calculation (engproc.F90:1010-1015) */
   ERMOD_E_PARAM = 120,     /* invalid argument or call order */
   ERMOD_E_NONCUBOID = 121, /* non-cuboid cell: the reference stops (realcal.F90:859-866) */
@@ -75,6 +79,8 @@ typedef struct ermod_params {
   double elecut, lwljcut, upljcut, screen;
   double temp;               /* kT in kcal/mol */
   double block_threshold;    /* accepted for interface parity; the GPU path needs no cell list */
+  int32_t boxshp;            /* 1 periodic, 0 non-periodic (bare Coulomb, NVT; engmain.F90:306) */
+  int32_t reserved_;
 } ermod_params;
 
 typedef struct ermod_ctx ermod_ctx;

@@ -581,10 +581,12 @@ struct RealWork {
   std::vector<cd> rcp;
 };
 
-// realcal_prepare + normalize_periodic (realcal.F90:137-146, 789-885), cuboid cells
+// realcal_prepare + normalize_periodic (realcal.F90:137-146, 789-885), cuboid cells;
+// a non-periodic system keeps its coordinates as they are (realcal.F90:145)
 void realcal_prepare(const orc_ctx* c, const double* sitepos, RealWork& w) {
   const int n = c->numatm;
   w.sitepos_normal.assign(sitepos, sitepos + 3 * (size_t)n);
+  if (c->p.boxshp == 0) return;
   for (int i = 0; i < 3; ++i) {
     w.cell_len[i] = std::fabs(c->cell[i + 3 * i]);
     w.invlen[i] = 1.0 / w.cell_len[i];
@@ -956,8 +958,12 @@ int get_uv_energy(const orc_ctx* c, int tagslt, const double* solute_xyz, double
     if (self_out) *self_out = 0.0;
     if (c->sluvid[tagslt - 1] == 0) return ORC_E_RCP_FST;
     const LjConsts k = lj_consts(c->p);
-    double half[3];
-    for (int i = 0; i < 3; ++i) half[i] = 0.5 * w.cell_len[i];
+    const bool periodic = c->p.boxshp != 0;
+    double half[3] = {0.0, 0.0, 0.0};
+    if (periodic)
+      for (int i = 0; i < 3; ++i) half[i] = 0.5 * w.cell_len[i];
+    // reelcut: elecut when periodic, "infinity" (1e50) otherwise (realcal.F90:170-178)
+    const double reelcut = periodic ? c->p.elecut : 1.0e50;
     const int T = c->ljtype_max;
 #pragma omp parallel for schedule(dynamic, 64) if (parallel_inner)
     for (int kk = 1; kk <= c->slvmax; ++kk) {
@@ -969,7 +975,7 @@ int get_uv_energy(const orc_ctx* c, int tagslt, const double* solute_xyz, double
           double dis2 = 0.0;
           for (int a = 0; a < 3; ++a) {
             const double x = w.sitepos_normal[3 * (size_t)(ati - 1) + a] - w.sitepos_normal[3 * (size_t)(atj - 1) + a];
-            const double d = half[a] - std::fabs(half[a] - std::fabs(x));
+            const double d = periodic ? half[a] - std::fabs(half[a] - std::fabs(x)) : x;
             dis2 += d * d;
           }
           const double rst = std::sqrt(dis2);
@@ -979,7 +985,7 @@ int get_uv_energy(const orc_ctx* c, int tagslt, const double* solute_xyz, double
           double eplj = 0.0;
           if (rst <= c->p.upljcut)
             eplj = (dis2 <= k.lw2) ? lj_low(c->p, k, ljeps, ljsgm2, dis2) : lj_switch(c->p, k, ljeps, ljsgm2, dis2);
-          const double epcl = (rst >= c->p.elecut) ? 0.0 : c->charge[ati - 1] * c->charge[atj - 1] / rst;
+          const double epcl = (rst >= reelcut) ? 0.0 : c->charge[ati - 1] * c->charge[atj - 1] / rst;
           pairep = pairep + eplj + epcl;
         }
       uvengy[kk] = pairep;
@@ -1239,6 +1245,9 @@ int orc_create(const orc_params* p, orc_ctx** out) {
   if (!p || !out) return ORC_E_PARAM;
   if (p->splodr < 2 || p->ms1max < 2 || p->ms2max < 2 || p->ms3max < 2) return ORC_E_PARAM;
   if (p->ljswitch < 0 || p->ljswitch > 3 || p->slttype < 1 || p->slttype > 3) return ORC_E_PARAM;
+  if (p->boxshp != 0 && p->boxshp != 1) return ORC_E_PARAM;
+  // setconf.F90:368-372: a non-periodic system needs NVT and bare Coulomb
+  if (p->boxshp == 0 && (p->estype == 2 || p->elmode != 2)) return ORC_E_SET_PRS;
   auto* c = new orc_ctx();
   c->p = *p;
   c->spl.init(p->splodr);
@@ -1329,6 +1338,12 @@ int orc_frame(orc_ctx* c, const double* sitepos, const double* cell, double stat
   if (!c || c->numatm <= 0 || c->ermax <= 0) return ORC_E_PARAM;
   c->sitepos.assign(sitepos, sitepos + 3 * (size_t)c->numatm);
   std::memcpy(c->cell, cell, sizeof(double) * 9);
+  if (c->p.boxshp == 0) {  // non-periodic: bare Coulomb only, no cell, no reciprocal set-up
+    c->stat_weight_system = stat_weight_system;
+    get_inverted_cell(c);
+    c->frame_ready = true;
+    return ORC_OK;
+  }
   // non-cuboid cells stop the reference (realcal.F90:859-866)
   if (std::fabs(cell[3]) > 1e-8 || std::fabs(cell[6]) > 1e-8 || std::fabs(cell[7]) > 1e-8 ||
       std::fabs(cell[1]) > 1e-8 || std::fabs(cell[2]) > 1e-8 || std::fabs(cell[5]) > 1e-8 ||

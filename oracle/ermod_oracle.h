@@ -33,6 +33,7 @@ enum {
   ORC_E_ENG_CNS = 104, /* uvspec <= 0 for a solvent (engproc.F90:817) */
   ORC_E_RCP_CNS = 105, /* recpcal.F90:335,474 */
   ORC_E_RCP_FST = 106, /* solute listed as solvent (recpcal.F90:469) */
+  ORC_E_SET_PRS = 108, /* non-periodic with NPT or a non-bare Coulomb (setconf.F90:368-372) */
   ORC_W_MBIN = 110,    /* last-bin warning without force_calculation (engproc.F90:1010-1015) */
   ORC_E_PARAM = 120,   /* invalid argument */
   ORC_E_NONCUBOID = 121 /* realcal.F90:859-866 */
@@ -49,6 +50,8 @@ typedef struct orc_params {
   double elecut, lwljcut, upljcut, screen;
   double temp;            /* kT in kcal/mol (setconf.F90:313) */
   double block_threshold; /* realcal cell size (setconf.F90:219) */
+  int32_t boxshp;         /* 1 periodic, 0 non-periodic (engmain.F90:306) */
+  int32_t reserved_;
 } orc_params;
 
 typedef struct orc_ctx orc_ctx;

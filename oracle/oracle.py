@@ -44,6 +44,7 @@ class OrcParams(C.Structure):
         ("selfcal", C.c_int32), ("force_calculation", C.c_int32), ("elmode", C.c_int32),
         ("elecut", C.c_double), ("lwljcut", C.c_double), ("upljcut", C.c_double),
         ("screen", C.c_double), ("temp", C.c_double), ("block_threshold", C.c_double),
+        ("boxshp", C.c_int32), ("reserved_", C.c_int32),
     ]
 
 
@@ -268,6 +269,7 @@ class Oracle:
             if name in params:
                 setattr(p, name, params[name])
         p.elmode = {2: 0, 3: 1, 0: 2}[int(params.get("cltype", 2))]
+        p.boxshp = int(params.get("boxshp", 1))
         self.params = dict(params)
         self.ctx = C.c_void_p()
         _check(L.orc_create(C.byref(p), C.byref(self.ctx)), "create")
