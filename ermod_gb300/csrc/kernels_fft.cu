@@ -579,25 +579,60 @@ __global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(Pme
   // one warp per row pair, lanes along k1 (no division); the upper half of k1 is the
   // conjugate of the stored half
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
-  for (int pp = warp; pp < npair; pp += nwarp) {
-    const float2* r0 = r + (size_t)(2 * pp) * H;
-    const float2* r1 = r0 + H;
-    const bool has1 = 2 * pp + 1 < K2;
-    float2* wrow = w + (size_t)pp * K1p;
-    for (int k = lane; k < K1; k += 32) {
-      const bool lo = k < H;
-      const int kk = lo ? k : K1 - k;
-      float2 x0 = r0[kk];
-      float2 x1 = has1 ? r1[kk] : make_float2(0.f, 0.f);
-      if (!lo) {
-        x0.y = -x0.y;
-        x1.y = -x1.y;
+  if constexpr (KC > 0) {
+    // the lane's columns k = lane + 32 i, their mirrored source and flags, set up once
+    constexpr int NK = (KC + 31) / 32, HC = KC / 2 + 1;
+    int kk[NK];
+    unsigned conj = 0u, real = 0u;
+#pragma unroll
+    for (int i = 0; i < NK; ++i) {
+      const int k = lane + 32 * i;
+      kk[i] = k < HC ? k : KC - k;
+      if (k >= HC) conj |= 1u << i;
+      if (k == 0 || ((KC % 2 == 0) && k == KC / 2)) real |= 1u << i;  // self-conjugate points
+    }
+    for (int pp = warp; pp < npair; pp += nwarp) {
+      const float2* r0 = r + (size_t)(2 * pp) * HC;
+      const float2* r1 = r0 + HC;
+      const bool has1 = 2 * pp + 1 < KC;
+      float2* wrow = w + (size_t)pp * (KC + 1) + lane;
+#pragma unroll
+      for (int i = 0; i < NK; ++i) {
+        if (KC % 32 != 0 && lane + 32 * i >= KC) break;
+        float2 x0 = r0[kk[i]];
+        float2 x1 = has1 ? r1[kk[i]] : make_float2(0.f, 0.f);
+        if (conj & (1u << i)) {
+          x0.y = -x0.y;
+          x1.y = -x1.y;
+        }
+        if (real & (1u << i)) {
+          x0.y = 0.f;
+          x1.y = 0.f;
+        }
+        wrow[32 * i] = make_float2(x0.x - x1.y, x0.y + x1.x);
       }
-      if (k == 0 || ((K1 % 2 == 0) && k == K1 / 2)) {  // self-conjugate points
-        x0.y = 0.f;
-        x1.y = 0.f;
+    }
+  } else {
+    for (int pp = warp; pp < npair; pp += nwarp) {
+      const float2* r0 = r + (size_t)(2 * pp) * H;
+      const float2* r1 = r0 + H;
+      const bool has1 = 2 * pp + 1 < K2;
+      float2* wrow = w + (size_t)pp * K1p;
+      for (int k = lane; k < K1; k += 32) {
+        const bool lo = k < H;
+        const int kk = lo ? k : K1 - k;
+        float2 x0 = r0[kk];
+        float2 x1 = has1 ? r1[kk] : make_float2(0.f, 0.f);
+        if (!lo) {
+          x0.y = -x0.y;
+          x1.y = -x1.y;
+        }
+        if (k == 0 || ((K1 % 2 == 0) && k == K1 / 2)) {  // self-conjugate points
+          x0.y = 0.f;
+          x1.y = 0.f;
+        }
+        wrow[k] = make_float2(x0.x - x1.y, x0.y + x1.x);
       }
-      wrow[k] = make_float2(x0.x - x1.y, x0.y + x1.x);
     }
   }
   float2* res;
@@ -617,15 +652,39 @@ __global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(Pme
   const int KX = K1 + h, KY = K2 + h;  // written extent of a padded plane
   const int ncopy = (z >= K3 - h) ? 2 : 1;
   const float* resf = reinterpret_cast<const float*>(res);  // row pair p: (y = 2p, 2p+1) interleaved
-  for (int c = 0; c < ncopy; ++c) {
-    float* plane_out = out + (size_t)(c ? z - K3 + h : z + h) * A.YP * A.XP * 4;
-    for (int yy = warp; yy < KY; yy += nwarp) {  // one warp per padded row
-      const int y = (yy < h) ? yy - h + K2 : yy - h;
-      const float* src = resf + 2 * (size_t)(y >> 1) * K1p + (y & 1);
-      float* dst = plane_out + (size_t)yy * A.XP * 4;
-      for (int xx = lane; xx < KX; xx += 32) {
-        const int x = (xx < h) ? xx - h + K1 : xx - h;
-        dst[4 * xx] = src[2 * x];
+  if constexpr (KC > 0) {
+    // the lane's padded columns xx = lane + 32 i and their source offsets, set up once
+    constexpr int NX = (KC + 7 + 31) / 32;  // h <= 7
+    int sx[NX];
+    unsigned ok = 0u;
+#pragma unroll
+    for (int i = 0; i < NX; ++i) {
+      const int xx = lane + 32 * i;
+      sx[i] = 2 * ((xx < h) ? xx - h + KC : xx - h);
+      if (xx < KX) ok |= 1u << i;
+    }
+    for (int c = 0; c < ncopy; ++c) {
+      float* plane_out = out + (size_t)(c ? z - K3 + h : z + h) * A.YP * A.XP * 4 + 4 * lane;
+      for (int yy = warp; yy < KY; yy += nwarp) {  // one warp per padded row
+        const int y = (yy < h) ? yy - h + K2 : yy - h;
+        const float* src = resf + 2 * (size_t)(y >> 1) * K1p + (y & 1);
+        float* dst = plane_out + (size_t)yy * A.XP * 4;
+#pragma unroll
+        for (int i = 0; i < NX; ++i)
+          if (ok & (1u << i)) dst[128 * i] = src[sx[i]];
+      }
+    }
+  } else {
+    for (int c = 0; c < ncopy; ++c) {
+      float* plane_out = out + (size_t)(c ? z - K3 + h : z + h) * A.YP * A.XP * 4;
+      for (int yy = warp; yy < KY; yy += nwarp) {  // one warp per padded row
+        const int y = (yy < h) ? yy - h + K2 : yy - h;
+        const float* src = resf + 2 * (size_t)(y >> 1) * K1p + (y & 1);
+        float* dst = plane_out + (size_t)yy * A.XP * 4;
+        for (int xx = lane; xx < KX; xx += 32) {
+          const int x = (xx < h) ? xx - h + K1 : xx - h;
+          dst[4 * xx] = src[2 * x];
+        }
       }
     }
   }
