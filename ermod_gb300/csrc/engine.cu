@@ -198,6 +198,7 @@ static int free_topology(Engine& e) {
 
 static int free_bins(Engine& e) {
   dfree(e.d_uvkey);
+  dfree(e.d_uvkey_f);
   dfree(e.d_eskey);
   dfree(e.d_spec);
   dfree(e.d_edens);
@@ -736,12 +737,20 @@ int ermod_set_bins(ermod_ctx* c, int numslv, const int* uvmax, const int* uvsoft
   e.uvcrd.assign(uvcrd, uvcrd + ermax);
   e.escrd.assign(escrd ? escrd : uvcrd, (escrd ? escrd : uvcrd) + esmax);
   std::vector<long long> uk(ermax), ek(std::max(esmax, 1));
-  for (int i = 0; i < ermax; ++i) uk[i] = ordered_key(uvcrd[i]);
+  std::vector<int> ukf(ermax);
+  for (int i = 0; i < ermax; ++i) {
+    uk[i] = ordered_key(uvcrd[i]);
+    float f = (float)uvcrd[i];  // round down to a float
+    if ((double)f > uvcrd[i]) f = std::nextafter(f, -INFINITY);
+    ukf[i] = ordered_key32(f);
+  }
   for (int i = 0; i < esmax; ++i) ek[i] = ordered_key(escrd[i]);
   ERMOD_CUDA(dalloc(&e.d_uvkey, ermax));
   ERMOD_CUDA(dalloc(&e.d_eskey, ek.size()));
   ERMOD_CUDA(dalloc(&e.d_spec, spec.size()));
   ERMOD_CUDA(cudaMemcpy(e.d_uvkey, uk.data(), sizeof(long long) * ermax, cudaMemcpyHostToDevice));
+  ERMOD_CUDA(dalloc(&e.d_uvkey_f, ermax));
+  ERMOD_CUDA(cudaMemcpy(e.d_uvkey_f, ukf.data(), sizeof(int) * ermax, cudaMemcpyHostToDevice));
   ERMOD_CUDA(cudaMemcpy(e.d_eskey, ek.data(), sizeof(long long) * ek.size(), cudaMemcpyHostToDevice));
   ERMOD_CUDA(cudaMemcpy(e.d_spec, spec.data(), sizeof(int) * spec.size(), cudaMemcpyHostToDevice));
   ERMOD_CUDA(dalloc(&e.d_edens, ermax));

@@ -61,6 +61,7 @@ struct Engine {
   std::vector<double> uvcrd, escrd;
   bool bins_ready = false;
   long long* d_uvkey = nullptr;  // ordered keys of uvcrd
+  int* d_uvkey_f = nullptr;      // ordered 32-bit keys of uvcrd rounded down to floats (mixed binning)
   long long* d_eskey = nullptr;  // ordered keys of escrd
   int* d_spec = nullptr;         // [numslv][3] {uvoff, uvmax, uvsoft}
 

@@ -67,6 +67,21 @@ __host__ __device__ inline long long ordered_key(double x) {
   return k ^ ((k >> 63) & 0x7fffffffffffffffll);
 }
 
+// ordered 32-bit key of a float (-0 == +0).  For a float u and a double edge e,
+// u <= e exactly when u <= rd(e), the largest float not above e, and u > e exactly when
+// u > rd(e); so an FP32 total binned on the keys of rd(edges) lands in the bin that its
+// exact double value takes against the FP64 edges.
+__host__ __device__ inline int ordered_key32(float f) {
+  if (f == 0.0f) f = 0.0f;
+  int k;
+#ifdef __CUDA_ARCH__
+  k = __float_as_int(f);
+#else
+  __builtin_memcpy(&k, &f, 4);
+#endif
+  return k ^ ((k >> 31) & 0x7fffffff);
+}
+
 struct FrameGeom {
   double L[3];       // cell lengths (cuboid cell)
   double invL[3];    // 1 / L as dtrtri computes it

@@ -51,6 +51,7 @@ struct MolArgs {
   int ldb;  // interleave stride of the mixed potential grids (placements per grid point)
   // energy coordinate
   const long long* uvkey;
+  const int* uvkey_f;  // 32-bit keys of the edges rounded down to floats (FP32 totals)
   const int* spec;  // [numslv][3]
   int numslv, ermax, soln, mbin_mode;  // mbin_mode: 0 off, 1 error, 2 flag only
   // interaction parameters
@@ -588,6 +589,7 @@ constexpr long kWaitLimit = 1L << 24;  // try_wait rounds before a CTA gives up 
 // once for all groups, FP32 stable recursion) and accumulates q theta theta theta phi
 // for the four placements with one 16-byte shared load per stencil point.
 constexpr int kGatherThreads = 128;
+constexpr int kGatherStages = 2;  // halo buffers (TMA copies in flight) per gather CTA
 
 template <int P>
 __device__ __forceinline__ void site_setup(int site, const float4* __restrict__ site_rec,
@@ -641,20 +643,19 @@ __global__ void __launch_bounds__(kGatherThreads) gather_tma_kernel(
     int K1, int K2, int K3, int nbx, int nby, int BX, int ldb, float* __restrict__ site_e, DevStatus* status) {
   constexpr int BY = 8 + P - 1, BZ = 8 + P - 1;
   extern __shared__ unsigned char smem_raw[];
-  __shared__ unsigned long long bar[2];
+  __shared__ unsigned long long bar[kGatherStages];
   const int npt = BZ * BY * BX;
-  // two halo buffers [z][y][x] of float4 (the four placements of a group), 128-byte aligned
-  float4* halo0 = reinterpret_cast<float4*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
+  // kGatherStages halo buffers [z][y][x] of float4 (the four placements of a group),
+  // 128-byte aligned; group g lands in buffer (g - g_begin) % kGatherStages
+  float4* halo_base = reinterpret_cast<float4*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
   const int hstride = (npt + 7) & ~7;  // float4 elements, a multiple of 128 bytes
-  float4* halo1 = halo0 + hstride;
   const int brick = blockIdx.x;
   const int bx = brick % nbx, by = (brick / nbx) % nby, bz = brick / (nbx * nby);
   const int g_begin = blockIdx.y * groups_per_cta;
   const int g_end = min((nb + 3) / 4, g_begin + groups_per_cta);
   const uint32_t box_bytes = (uint32_t)(npt * sizeof(float4));
   if (threadIdx.x == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+    for (int i = 0; i < kGatherStages; ++i) mbar_init(&bar[i], 1);
     fence_barrier_init();
     fence_proxy_async_smem();
   }
@@ -662,10 +663,10 @@ __global__ void __launch_bounds__(kGatherThreads) gather_tma_kernel(
   // padded coordinates: the halo of brick (bx, by, bz) starts at (8 bx, 8 by, 8 bz); the
   // innermost box coordinate (the placement within the group) is 0
   if (threadIdx.x == 0) {
-    for (int g = g_begin; g < min(g_end, g_begin + 2); ++g) {
-      unsigned long long* br = &bar[(g - g_begin) & 1];
-      mbar_expect_tx(br, box_bytes);
-      tma_load_5d(((g - g_begin) & 1) ? halo1 : halo0, &tmap, 0, bx * 8, by * 8, bz * 8, g, br);
+    for (int g = g_begin; g < min(g_end, g_begin + kGatherStages); ++g) {
+      const int st = g - g_begin;
+      mbar_expect_tx(&bar[st], box_bytes);
+      tma_load_5d(halo_base + (size_t)st * hstride, &tmap, 0, bx * 8, by * 8, bz * 8, g, &bar[st]);
     }
   }
   const int h = P - 1;
@@ -714,24 +715,25 @@ __global__ void __launch_bounds__(kGatherThreads) gather_tma_kernel(
   if (site0 >= 0) site_setup<P>(site0, site_rec, site_grid, K1, K2, K3, ox, oy, oz, BX, w1, w2, w3, base, q);
   const int n_extra = bucketed ? novf : max(0, n - (int)blockDim.x);
   for (int g = g_begin; g < g_end; ++g) {
-    const int slot = (g - g_begin) & 1;
-    const uint32_t parity = (uint32_t)(((g - g_begin) >> 1) & 1);
+    const int slot = (g - g_begin) % kGatherStages;
+    const uint32_t parity = (uint32_t)(((g - g_begin) / kGatherStages) & 1);
     bool ok = false;
     for (long it = 0; it < kWaitLimit; ++it)
       if (mbar_try_wait(&bar[slot], parity)) {
         ok = true;
         break;
       }
-    if (!ok) {  // flag, let the other copy in flight land (bounded), leave
+    if (!ok) {  // flag, let the other copies in flight land (bounded), leave
       if (threadIdx.x == 0) atomicOr(&status->range_fault, 2);
-      if (g + 1 < g_end) {
-        const uint32_t par1 = (uint32_t)(((g + 1 - g_begin) >> 1) & 1);
+      for (int g2 = g + 1; g2 < min(g_end, g + kGatherStages); ++g2) {
+        const int s2 = (g2 - g_begin) % kGatherStages;
+        const uint32_t p2 = (uint32_t)(((g2 - g_begin) / kGatherStages) & 1);
         for (long it = 0; it < kWaitLimit; ++it)
-          if (mbar_try_wait(&bar[slot ^ 1], par1)) break;
+          if (mbar_try_wait(&bar[s2], p2)) break;
       }
       return;
     }
-    const float4* halo = slot ? halo1 : halo0;
+    const float4* halo = halo_base + (size_t)slot * hstride;
     const int b0 = 4 * g;
     if (site0 >= 0) {
       const float4 acc = site_stencil<P>(halo, base, BX, w1, w2, w3);
@@ -748,11 +750,12 @@ __global__ void __launch_bounds__(kGatherThreads) gather_tma_kernel(
       *reinterpret_cast<float4*>(site_e + (size_t)site * ldb + b0) =
           make_float4(qs * acc.x, qs * acc.y, qs * acc.z, qs * acc.w);
     }
-    __syncthreads();  // halo[slot] consumed: the copy of group g + 2 may land in it
-    if (threadIdx.x == 0 && g + 2 < g_end) {
+    __syncthreads();  // halo[slot] consumed: the copy of group g + kGatherStages may land in it
+    if (threadIdx.x == 0 && g + kGatherStages < g_end) {
       fence_proxy_async_smem();
       mbar_expect_tx(&bar[slot], box_bytes);
-      tma_load_5d(slot ? halo1 : halo0, &tmap, 0, bx * 8, by * 8, bz * 8, g + 2, &bar[slot]);
+      tma_load_5d(halo_base + (size_t)slot * hstride, &tmap, 0, bx * 8, by * 8, bz * 8, g + kGatherStages,
+                  &bar[slot]);
     }
   }
 }
@@ -764,7 +767,7 @@ template <int G>
 __global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const float* __restrict__ site_e) {
   extern __shared__ int smem_dyn[];
   int* smem_hist = smem_dyn;                                                  // [G][ermax]
-  long long* skeys = reinterpret_cast<long long*>(smem_dyn + ((G * A.ermax + 1) & ~1));  // [ermax]
+  int* skeys = smem_dyn + G * A.ermax;  // [ermax] 32-bit edge keys
   __shared__ float su[G][256];
   __shared__ float squ[G];    // residual factor x solute charge of the G placements
   __shared__ float srcut[G];  // bounding-sphere cutoff of the real-space sum
@@ -778,7 +781,7 @@ __global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const flo
   const int m = tile * blockDim.x + threadIdx.x;
   const bool valid = m < A.slvmax;
   for (int i = threadIdx.x; i < G * A.ermax; i += blockDim.x) smem_hist[i] = 0;
-  for (int i = threadIdx.x; i < A.ermax; i += blockDim.x) skeys[i] = A.uvkey[i];
+  for (int i = threadIdx.x; i < A.ermax; i += blockDim.x) skeys[i] = A.uvkey_f[i];
   if (threadIdx.x < ng) {
     const int b = g0 + threadIdx.x;
     squ[threadIdx.x] = (float)(A.resid_fac * a.u_qmol[b]);
@@ -862,17 +865,18 @@ __global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const flo
       if (j < ng) a.mol_u[(size_t)(g0 + j) * A.slvmax + m] = act[j] ? uu[j] : __uint_as_float(0x7fc00000u);
   }
   __syncthreads();  // histograms zeroed, keys staged
-  // ---- getiduv / binsearch for all G at once: ret = #edges < u ----
-  long long ku[G];
+  // ---- getiduv / binsearch for all G at once: ret = #edges < u (32-bit keys of the
+  // FP32 totals against the edges rounded down to floats: the same count as FP64) ----
+  int ku[G];
   int pos[G];
 #pragma unroll
   for (int j = 0; j < G; ++j) {
-    ku[j] = ordered_key_f(uu[j]);
+    ku[j] = ordered_key32(uu[j]);
     pos[j] = 0;
   }
   int step = 1;
   while ((step << 1) <= sp_n) step <<= 1;
-  const long long* kk = skeys + sp_off;
+  const int* kk = skeys + sp_off;
   for (; step > 0; step >>= 1) {
 #pragma unroll
     for (int j = 0; j < G; ++j) {
@@ -996,6 +1000,7 @@ static MolArgs make_mol_args(Engine& e, const BatchArgs& a) {
   A.T = e.ljtype_max;
   A.ldb = e.Bmax;
   A.uvkey = e.d_uvkey;
+  A.uvkey_f = e.d_uvkey_f;
   A.spec = e.d_spec;
   A.numslv = e.numslv;
   A.ermax = e.ermax;
@@ -1025,12 +1030,12 @@ static MolArgs make_mol_args(Engine& e, const BatchArgs& a) {
 cudaError_t launch_gather(Engine& e, const BatchArgs& a) {
   cudaError_t err = cudaSuccess;
   const int ngroups = (a.nb + 3) / 4;
-  const int gpc = std::min(ngroups, 4);
+  const int gpc = std::min(ngroups, 8);
   dim3 g1(e.nbricks, (ngroups + gpc - 1) / gpc);
   const int K1 = e.geom.K[0], K2 = e.geom.K[1], K3 = e.geom.K[2];
   const size_t npt = (size_t)e.gbox[0] * e.gbox[1] * e.gbox[2];
   const size_t hstride = (npt + 7) & ~(size_t)7;  // as in the kernel: 128-byte aligned halos
-  const size_t sh = 128 + 2 * hstride * sizeof(float4);
+  const size_t sh = 128 + kGatherStages * hstride * sizeof(float4);
 #define ERMOD_GATHER(PP)                                                                                        \
   if (e.P_order == PP) {                                                                                        \
     static size_t attr = 0;                                                                                     \
@@ -1072,7 +1077,7 @@ cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
     e.phase_begin_on(PH_MOL, a.stream);
   }
   // step 2: per-molecule totals and binning (histograms + edge keys in shared memory)
-  const size_t smem_f = sizeof(int) * (((size_t)a.G * e.ermax + 1) & ~(size_t)1) + sizeof(long long) * e.ermax;
+  const size_t smem_f = sizeof(int) * ((size_t)a.G * e.ermax + e.ermax);
   dim3 g2((a.nb + a.G - 1) / a.G, e.ntile);
 #define ERMOD_FINISH(GG)                                                                                   \
   if (a.G == GG) {                                                                                         \
