@@ -653,25 +653,37 @@ __global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(Pme
   const int ncopy = (z >= K3 - h) ? 2 : 1;
   const float* resf = reinterpret_cast<const float*>(res);  // row pair p: (y = 2p, 2p+1) interleaved
   if constexpr (KC > 0) {
-    // the lane's padded columns xx = lane + 32 i and their source offsets, set up once
+    // the lane's padded columns xx = lane + 32 i and their source columns, set up once
     constexpr int NX = (KC + 7 + 31) / 32;  // h <= 7
     int sx[NX];
     unsigned ok = 0u;
 #pragma unroll
     for (int i = 0; i < NX; ++i) {
       const int xx = lane + 32 * i;
-      sx[i] = 2 * ((xx < h) ? xx - h + KC : xx - h);
+      sx[i] = (xx < h) ? xx - h + KC : xx - h;
       if (xx < KX) ok |= 1u << i;
     }
     for (int c = 0; c < ncopy; ++c) {
       float* plane_out = out + (size_t)(c ? z - K3 + h : z + h) * A.YP * A.XP * 4 + 4 * lane;
-      for (int yy = warp; yy < KY; yy += nwarp) {  // one warp per padded row
-        const int y = (yy < h) ? yy - h + K2 : yy - h;
-        const float* src = resf + 2 * (size_t)(y >> 1) * K1p + (y & 1);
-        float* dst = plane_out + (size_t)yy * A.XP * 4;
+      // one warp per row pair: one 8-byte load gives rows y = 2p (.x) and 2p + 1 (.y);
+      // row y is stored at padded row y + h and, when y >= K2 - h, also at y + h - K2
+      for (int pp = warp; pp < npair; pp += nwarp) {
+        const float2* src = res + (size_t)pp * (KC + 1);
+        float2 v[NX];
 #pragma unroll
-        for (int i = 0; i < NX; ++i)
-          if (ok & (1u << i)) dst[128 * i] = src[sx[i]];
+        for (int i = 0; i < NX; ++i) v[i] = (ok & (1u << i)) ? src[sx[i]] : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          const int y = 2 * pp + e;
+          if (y >= KC) break;
+          for (int rep = 0; rep < 2; ++rep) {
+            if (rep && y < KC - h) break;
+            float* dst = plane_out + (size_t)(rep ? y + h - KC : y + h) * A.XP * 4;
+#pragma unroll
+            for (int i = 0; i < NX; ++i)
+              if (ok & (1u << i)) dst[128 * i] = e ? v[i].y : v[i].x;
+          }
+        }
       }
     }
   } else {
