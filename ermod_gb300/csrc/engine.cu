@@ -2,10 +2,12 @@
 // per-frame preparation and the batched placement loop that replaces engconst's
 // `do cntdst` (engproc.F90:388-392).
 //
-// Per batch of B placements the stream carries:
-//   place_prep -> [mixed] spectrum -> cuFFT C2R (batched)      -> mol_energy -> accumulate
-//              -> [fp64]  spread64 -> D2Z -> influence64 -> Z2D -> mol_energy -> accumulate
-// and every `ring_cap` placements (reference-solvent mode) the ecorr flush.
+// Per batch of B placements:
+//   [mixed] place_prep (prep stream) -> pme_a -> pme_b -> gather -> finish (one of two
+//           batch streams) -> reduce + accumulate (aux stream)
+//   [fp64]  place_prep -> spread64 -> D2Z -> influence64 -> Z2D -> mol_energy -> accumulate
+// and, when ecorr is on, a flush of the histogram ring every `ring_half` placements on
+// the aux stream while the next batches fill the ring's other half.
 // Status is reported once per call (host API) or per ermod_sync (device API).
 #include <cufft.h>
 
@@ -291,8 +293,11 @@ static int ensure_batch(Engine& e) {
     ERMOD_CUDA(dalloc(&b.self_part, (size_t)2 * B * influence64_blocks()));
   }
   ERMOD_CUDA(dalloc(&b.part, (size_t)2 * B * e.ntile * e.numslv * 3));
-  e.ring_cap = e.P.corrcal ? std::max(2 * B, (512 / B) * B) : 2 * B;
+  e.ring_half = e.P.corrcal ? std::max(2 * B, (512 / B) * B) : B;
+  e.ring_cap = 2 * e.ring_half;
   e.ring_fill = 0;
+  e.ring_off = 0;
+  e.flush_pend[0] = e.flush_pend[1] = false;
   ERMOD_CUDA(dalloc(&e.d_ring_hist, (size_t)e.ring_cap * e.ermax));
   ERMOD_CUDA(dalloc(&e.d_ring_w, e.ring_cap));
   ERMOD_CUDA(dalloc(&e.d_ring_nnz, e.ring_cap));
@@ -451,7 +456,8 @@ int ermod_create(const ermod_params* p_in, int device, ermod_ctx** out) {
     cudaEventCreateWithFlags(&e.ev_acc[s], cudaEventDisableTiming);
     cudaEventCreateWithFlags(&e.ev_prep[s], cudaEventDisableTiming);
   }
-  cudaEventCreateWithFlags(&e.ev_flush, cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&e.ev_flush[0], cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&e.ev_flush[1], cudaEventDisableTiming);
   for (int s = 0; s < 4; ++s) cudaEventCreateWithFlags(&e.ev_join[s], cudaEventDisableTiming);
   if ((err = dalloc(&e.d_status, 1)) != cudaSuccess || (err = cudaMallocHost(&e.h_status, sizeof(DevStatus))) != cudaSuccess) {
     ermod_destroy(c);
@@ -525,7 +531,8 @@ int ermod_destroy(ermod_ctx* c) {
     if (e.ev_acc[s]) cudaEventDestroy(e.ev_acc[s]);
     if (e.ev_prep[s]) cudaEventDestroy(e.ev_prep[s]);
   }
-  if (e.ev_flush) cudaEventDestroy(e.ev_flush);
+  for (int s = 0; s < 2; ++s)
+    if (e.ev_flush[s]) cudaEventDestroy(e.ev_flush[s]);
   if (e.aux) cudaStreamDestroy(e.aux);
   if (e.prep) cudaStreamDestroy(e.prep);
   for (int s = 0; s < 2; ++s)
@@ -898,7 +905,7 @@ int ermod_frame_device(ermod_ctx* c, const double* sitepos_d, const double* cell
 
 // the placement loop on device-resident inputs.  Batch i runs its kernels on the main
 // stream with the buffers of slot i%2.  Its solute preparation runs on the prep stream
-// during batch i-1; its ordered accumulation (and, every ring_cap placements, the ecorr
+// during batch i-1; its ordered accumulation (and, every ring_half placements, the ecorr
 // flush) runs on the aux stream during batch i+1.
 static int run_placements(Engine& e, int nplace, const int* d_tag, const double* d_sol, const double* d_sws,
                           double* d_uv, double* d_fl, int ns_solute) {
@@ -957,7 +964,6 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
     }
     return a;
   };
-  bool flush_pending = false;  // the next batch rewrites the ring from its start
   auto issue_prep = [&](int ib) -> int {
     const int slot = ib & 1;
     const BatchArgs a = batch_args(ib);
@@ -975,13 +981,14 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
     if (ibatch + 1 < nbatch && (st = issue_prep(ibatch + 1)) != ERMOD_OK) return st;
     BatchArgs a = batch_args(ibatch);
     const int nb = a.nb;
-    a.hist = e.d_ring_hist + (size_t)e.ring_fill * e.ermax;
+    a.hist = e.d_ring_hist + (size_t)(e.ring_off + e.ring_fill) * e.ermax;
     cudaStream_t bst = a.stream;
     if (ibatch >= 2) ERMOD_CUDA(cudaStreamWaitEvent(bst, e.ev_acc[slot], 0));  // slot free again
     ERMOD_CUDA(cudaStreamWaitEvent(bst, e.ev_prep[slot], 0));
-    if (flush_pending) {
-      ERMOD_CUDA(cudaStreamWaitEvent(bst, e.ev_flush, 0));
-      flush_pending = false;
+    const int half = e.ring_off ? 1 : 0;
+    if (e.flush_pend[half]) {  // the first batch in this half waits for its previous flush
+      ERMOD_CUDA(cudaStreamWaitEvent(bst, e.ev_flush[half], 0));
+      e.flush_pend[half] = false;
     }
     ERMOD_CUDA(cudaMemsetAsync(a.hist, 0, sizeof(int) * (size_t)nb * e.ermax, bst));
     if (e.P.cltype == 0) {
@@ -1016,32 +1023,31 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
       ERMOD_CUDA(launch_adjoint(e, a, e.aux));
       e.phase_end_on(e.aux);
     }
-    bool flushed = false;
     if (e.P.corrcal) {
       e.ring_fill += nb;
-      if (e.ring_fill + B > e.ring_cap) {
+      if (e.ring_fill + B > e.ring_half) {  // flush this half; the next batches fill the other
         e.phase_begin_on(PH_ECORR, e.aux);
         ERMOD_CUDA(launch_ecorr_flush(e, e.aux));
         e.phase_end_on(e.aux);
+        ERMOD_CUDA(cudaEventRecord(e.ev_flush[half], e.aux));
+        e.flush_pend[half] = true;
+        e.ring_off = e.ring_half - e.ring_off;
         e.ring_fill = 0;
-        flushed = true;
       }
     } else {
-      e.ring_fill = (e.ring_fill + B) % e.ring_cap;  // two histogram slots
+      e.ring_off = e.ring_half - e.ring_off;  // two histogram slots, ordered by ev_acc
     }
     ERMOD_CUDA(cudaEventRecord(e.ev_acc[slot], e.aux));
-    if (flushed) {  // the ring is rewritten from its start by the next batches
-      ERMOD_CUDA(cudaEventRecord(e.ev_flush, e.aux));
-      flush_pending = true;
-    }
   }
   if (e.P.corrcal && e.ring_fill > 0) {
     e.phase_begin_on(PH_ECORR, e.aux);
     ERMOD_CUDA(launch_ecorr_flush(e, e.aux));
     e.phase_end_on(e.aux);
-    e.ring_fill = 0;
   }
+  // the join below orders every flush before the next call's work
   e.ring_fill = 0;
+  e.ring_off = 0;
+  e.flush_pend[0] = e.flush_pend[1] = false;
   // join every stream back into the caller's stream, then snapshot the status
   cudaStream_t others[4] = {e.aux, e.prep, e.bs[0], e.bs[1]};
   for (int k = 0; k < (dual ? 4 : 2); ++k) {

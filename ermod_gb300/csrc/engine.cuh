@@ -123,7 +123,10 @@ struct Engine {
   int cap_place = 0;
   BatchArgs buf{};                // device buffers sized for Bmax (pointers only)
   // histogram ring for ecorr (corrcal) / per-batch histograms
-  int ring_cap = 0, ring_fill = 0;
+  // histogram ring of the ecorr flush: two halves of ring_half entries; batches fill the
+  // half at ring_off while the aux stream flushes the other one
+  int ring_cap = 0, ring_fill = 0, ring_half = 0, ring_off = 0;
+  bool flush_pend[2] = {false, false};  // a flush of that half may still be running
   int* d_ring_hist = nullptr;     // [ring_cap][ermax]
   double* d_ring_w = nullptr;     // [ring_cap]
   int* d_ring_nz = nullptr;       // [ring_cap][ermax] packed (bin | count << 16)... see kernels
@@ -191,7 +194,7 @@ struct Engine {
   cudaEvent_t ev_join[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t ev_done[2] = {nullptr, nullptr};  // batch kernels finished (slot)
   cudaEvent_t ev_acc[2] = {nullptr, nullptr};   // accumulation of the slot finished
-  cudaEvent_t ev_flush = nullptr;               // ecorr flush finished
+  cudaEvent_t ev_flush[2] = {nullptr, nullptr};  // ecorr flush of ring half 0 / 1 finished
 
   void phase_begin(int ph) { phase_begin_on(ph, stream); }
   void phase_end() { phase_end_on(stream); }

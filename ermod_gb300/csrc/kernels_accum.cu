@@ -500,8 +500,8 @@ cudaError_t launch_accumulate(Engine& e, const BatchArgs& a, cudaStream_t s) {
   A.minuv = e.d_minuv;
   A.maxuv = e.d_maxuv;
   A.eskey = e.d_eskey;
-  A.ring_valid = e.d_ring_valid + e.ring_fill;
-  A.ring_w = e.d_ring_w + e.ring_fill;
+  A.ring_valid = e.d_ring_valid + e.ring_off + e.ring_fill;
+  A.ring_w = e.d_ring_w + e.ring_off + e.ring_fill;
   A.slvmax = e.slvmax;
   A.u0 = a.u0;
   A.self_bin = a.self_bin;
@@ -530,15 +530,16 @@ cudaError_t launch_ecorr_flush(Engine& e, cudaStream_t s) {
       if (err != cudaSuccess) return err;
     }
     dim3 grid((e.ermax + 255) / 256, (e.ermax + kEcRows - 1) / kEcRows);
-    ecorr_ff_kernel<<<grid, 256, smem, s>>>(e.d_ring_hist, e.d_ring_valid, e.d_ring_w, n, e.ermax, e.d_ecorr,
-                                            e.d_ecorr_n);
+    ecorr_ff_kernel<<<grid, 256, smem, s>>>(e.d_ring_hist + (size_t)e.ring_off * e.ermax, e.d_ring_valid + e.ring_off,
+                                            e.d_ring_w + e.ring_off, n, e.ermax, e.d_ecorr, e.d_ecorr_n);
     e.count_launch();
     return cudaGetLastError();
   }
   int* nz_bin = e.d_ring_nz;
   int* nz_cnt = e.d_ring_nz + (size_t)e.ring_cap * e.ermax;
-  const int* valid = e.d_ring_valid;
-  ring_compact_kernel<<<n, 256, 0, s>>>(e.d_ring_hist, valid, e.ermax, nz_bin, nz_cnt, e.d_ring_nnz);
+  const int* valid = e.d_ring_valid + e.ring_off;
+  const int* hist = e.d_ring_hist + (size_t)e.ring_off * e.ermax;
+  ring_compact_kernel<<<n, 256, 0, s>>>(hist, valid, e.ermax, nz_bin, nz_cnt, e.d_ring_nnz);
   e.count_launch();
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;
@@ -548,7 +549,7 @@ cudaError_t launch_ecorr_flush(Engine& e, cudaStream_t s) {
   err = cudaFuncSetAttribute(ecorr_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
   const int nblk = (e.ermax + R - 1) / R;
-  ecorr_rows_kernel<<<nblk, 256, smem, s>>>(e.d_ring_hist, nz_bin, nz_cnt, e.d_ring_nnz, e.d_ring_w, n,
+  ecorr_rows_kernel<<<nblk, 256, smem, s>>>(hist, nz_bin, nz_cnt, e.d_ring_nnz, e.d_ring_w + e.ring_off, n,
                                                    e.ermax, R, e.d_ecorr, e.d_ecorr_n);
   e.count_launch();
   return cudaGetLastError();
