@@ -444,8 +444,13 @@ int ermod_create(const ermod_params* p_in, int device, ermod_ctx** out) {
     return fail_cuda(err, "cudaStreamCreate");
   }
   e.own_stream = true;
-  if ((err = cudaStreamCreateWithFlags(&e.aux, cudaStreamNonBlocking)) != cudaSuccess ||
-      (err = cudaStreamCreateWithFlags(&e.prep, cudaStreamNonBlocking)) != cudaSuccess ||
+  // the short kernels of the prep and aux streams (solute preparation, ordered
+  // accumulation, ecorr flush) take priority over the batch streams' pending blocks, so
+  // the slots they free are not held up behind a whole PME launch
+  int prio_lo = 0, prio_hi = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+  if ((err = cudaStreamCreateWithPriority(&e.aux, cudaStreamNonBlocking, prio_hi)) != cudaSuccess ||
+      (err = cudaStreamCreateWithPriority(&e.prep, cudaStreamNonBlocking, prio_hi)) != cudaSuccess ||
       (err = cudaStreamCreateWithFlags(&e.bs[0], cudaStreamNonBlocking)) != cudaSuccess ||
       (err = cudaStreamCreateWithFlags(&e.bs[1], cudaStreamNonBlocking)) != cudaSuccess) {
     ermod_destroy(c);

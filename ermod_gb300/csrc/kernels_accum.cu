@@ -158,6 +158,10 @@ __global__ void __launch_bounds__(kAccThreads) accumulate_kernel(AccArgs A) {
   const int nb = a.nb;
   __shared__ double sw[kMaxBatch];
   __shared__ double stw[kMaxBatch];
+  __shared__ double su0[kMaxBatch];
+  __shared__ int sbin[kMaxBatch];
+  __shared__ double sterm[kMaxBatch];
+  __shared__ double sred[2][kAccThreads];
   __shared__ int skip;
   __shared__ double s_voffset;
   if (threadIdx.x == 0) {
@@ -184,13 +188,15 @@ __global__ void __launch_bounds__(kAccThreads) accumulate_kernel(AccArgs A) {
     }
     return;
   }
-  // weights (parallel)
+  // weights (parallel); u0 and the eself bins staged for the ordered sums
   for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    su0[b] = A.u0[b];
+    sbin[b] = A.self_bin[b];
     double engnmfc;
     if (!A.wgtslf) {
       engnmfc = 1.0;
     } else {
-      const double factor = A.u0[b] - s_voffset;
+      const double factor = su0[b] - s_voffset;
       engnmfc = A.soln ? exp(factor / A.temp) : exp(-factor / A.temp);
     }
     double total_weight = A.stat_weight_system * (a.stat_weight_solute ? a.stat_weight_solute[b] : 1.0);
@@ -214,9 +220,9 @@ __global__ void __launch_bounds__(kAccThreads) accumulate_kernel(AccArgs A) {
       engnorm = engnorm + sw[b];
       engsmpl = engsmpl + 1.0;
       avslf = avslf + stw[b];
-      if (A.selfcal) A.eself[A.self_bin[b]] += sw[b];
-      mn = fmin(mn, A.u0[b]);
-      mx = fmax(mx, A.u0[b]);
+      if (A.selfcal) A.eself[sbin[b]] += sw[b];
+      mn = fmin(mn, su0[b]);
+      mx = fmax(mx, su0[b]);
     }
     A.scal[0] = engnorm;
     A.scal[1] = engsmpl;
@@ -224,18 +230,37 @@ __global__ void __launch_bounds__(kAccThreads) accumulate_kernel(AccArgs A) {
     A.minuv[0] = mn;
     A.maxuv[0] = mx;
   }
-  for (int sp = threadIdx.x; sp < A.numslv; sp += blockDim.x) {
-    double mn = A.minuv[sp + 1], mx = A.maxuv[sp + 1], sl = A.soln ? A.slnuv[sp] : 0.0;
-    for (int b = 0; b < nb; ++b) {
+  // per species: min/max over the batch (order-free tree), slnuv in placement order
+  for (int sp = 0; sp < A.numslv; ++sp) {
+    double mn = INFINITY, mx = -INFINITY;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
       const double* pt = a.part + ((size_t)b * A.ntile * A.numslv + sp) * 3;
       mn = fmin(mn, pt[1]);
       mx = fmax(mx, pt[2]);
-      if (A.soln) sl = sl + pt[0] * sw[b];
+      if (A.soln) sterm[b] = pt[0] * sw[b];
     }
-    A.minuv[sp + 1] = mn;
-    A.maxuv[sp + 1] = mx;
-    if (A.soln) A.slnuv[sp] = sl;
+    sred[0][threadIdx.x] = mn;
+    sred[1][threadIdx.x] = mx;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+      if (threadIdx.x < st) {
+        sred[0][threadIdx.x] = fmin(sred[0][threadIdx.x], sred[0][threadIdx.x + st]);
+        sred[1][threadIdx.x] = fmax(sred[1][threadIdx.x], sred[1][threadIdx.x + st]);
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      A.minuv[sp + 1] = fmin(A.minuv[sp + 1], sred[0][0]);
+      A.maxuv[sp + 1] = fmax(A.maxuv[sp + 1], sred[1][0]);
+      if (A.soln) {
+        double sl = A.slnuv[sp];
+        for (int b = 0; b < nb; ++b) sl = sl + sterm[b];
+        A.slnuv[sp] = sl;
+      }
+    }
+    __syncthreads();
   }
+  if (!A.zmask) return;  // edens: accumulate_bins_kernel
   // edens += engnmfc * insdst, placements in order
   for (int i = threadIdx.x; i < A.ermax; i += blockDim.x) {
     double e = A.edens[i];
@@ -290,6 +315,44 @@ __global__ void __launch_bounds__(kAccThreads) accumulate_kernel(AccArgs A) {
       A.uvintm[sp] = u;
     }
   }
+}
+
+// edens += engnmfc * insdst (engproc.F90:836-838), one thread per bin, the batch's
+// placements in order (so the FP64 sums are those of the reference's loop); the
+// intermediate-state mode does this inside accumulate_kernel instead
+__global__ void __launch_bounds__(128) accumulate_bins_kernel(AccArgs A) {
+  const BatchArgs& a = A.a;
+  const int nb = a.nb;
+  if (nb <= 0 || A.ring_valid[0] == 0) return;  // the batch was not accumulated (an error)
+  __shared__ double sw[kMaxBatch];
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) sw[b] = a.engnmfc[b];
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= A.ermax) return;
+  const int* h = a.hist + i;
+  const size_t E = (size_t)A.ermax;
+  double e = A.edens[i];
+  bool touched = false;
+  int b = 0;
+  for (; b + 8 <= nb; b += 8) {
+    int c[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) c[u] = __ldg(h + (size_t)(b + u) * E);
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      if (c[u]) {
+        e = e + sw[b + u] * (double)c[u];
+        touched = true;
+      }
+  }
+  for (; b < nb; ++b) {
+    const int c = __ldg(h + (size_t)b * E);
+    if (c) {
+      e = e + sw[b] * (double)c;
+      touched = true;
+    }
+  }
+  if (touched) A.edens[i] = e;
 }
 
 // occupied-bin list per ring entry: entries (bin << 0) with counts beside them
@@ -515,6 +578,10 @@ cudaError_t launch_accumulate(Engine& e, const BatchArgs& a, cudaStream_t s) {
   reduce_kernel<<<a.nb, kAccThreads, 0, s>>>(A);
   accumulate_kernel<<<1, kAccThreads, 0, s>>>(A);
   e.count_launch(2);
+  if (!A.zmask) {
+    accumulate_bins_kernel<<<(e.ermax + 127) / 128, 128, 0, s>>>(A);
+    e.count_launch();
+  }
   return cudaGetLastError();
 }
 
