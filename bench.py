@@ -45,7 +45,7 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="refs_large")
     ap.add_argument("--insertions", type=int, default=None, help="insertions per frame (default: workload's)")
-    ap.add_argument("--batch", type=int, default=128, help="placements per PME launch")
+    ap.add_argument("--batch", type=int, default=256, help="placements per PME launch")
     ap.add_argument("--cpu-sample", type=int, default=96, help="placements timed on the CPU oracle")
     ap.add_argument("--plain-sample", type=int, default=48, help="placements timed on the plain FP64 GPU path")
     ap.add_argument("--no-cpu", action="store_true")

@@ -419,7 +419,7 @@ int ermod_create(const ermod_params* p_in, int device, ermod_ctx** out) {
   if (p->precision != ERMOD_PRECISION_FP64 && p->precision != ERMOD_PRECISION_MIXED)
     return fail_param("precision must be ERMOD_PRECISION_FP64 or ERMOD_PRECISION_MIXED");
   if (p->batch < 0 || p->batch > accumulate_max_batch() || (p->batch % 4) != 0)
-    return fail_param("batch must be a multiple of 4 in [4, 256] (0 = automatic)");
+    return fail_param("batch must be a multiple of 4 in [4, 512] (0 = automatic)");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
     g_err = "no CUDA device";

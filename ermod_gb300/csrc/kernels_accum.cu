@@ -49,7 +49,7 @@ struct AccArgs {
 };
 
 constexpr int kAccThreads = 256;
-constexpr int kMaxBatch = 256;
+constexpr int kMaxBatch = 512;
 
 // fixed-order block sum: thread t adds elements t, t+256, ... in order, then a fixed tree
 __device__ __forceinline__ double block_sum_fixed(double* red, const double* x, int n, int stride) {
