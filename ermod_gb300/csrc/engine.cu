@@ -468,7 +468,7 @@ int ermod_create(const ermod_params* p_in, int device, ermod_ctx** out) {
     ermod_destroy(c);
     return fail_cuda(err, "status allocation");
   }
-  DevStatus s0{kNoError, 0, 0};
+  DevStatus s0{kNoError, kNoError, 0, 0};
   cudaMemcpy(e.d_status, &s0, sizeof(s0), cudaMemcpyHostToDevice);
   *e.h_status = s0;
   // splfc tables (init_spline_axis, recpcal.F90:87-109) and FFT twiddles
@@ -1072,10 +1072,10 @@ static int check_ready(Engine& e, int nplace) {
 }
 
 static int reset_status(Engine& e) {  // memsets only, so that a graph capture can hold it
-  static_assert(sizeof(DevStatus) == 16, "DevStatus layout: err_key, mbin_hit, range_fault");
-  ERMOD_CUDA(cudaMemsetAsync(&e.d_status->err_key, 0xff, sizeof(unsigned long long), e.stream));  // kNoError
+  static_assert(sizeof(DevStatus) == 24, "DevStatus layout: err_key, first_key, mbin_hit, range_fault");
+  ERMOD_CUDA(cudaMemsetAsync(&e.d_status->err_key, 0xff, 2 * sizeof(unsigned long long), e.stream));  // kNoError
   ERMOD_CUDA(cudaMemsetAsync(&e.d_status->mbin_hit, 0, 2 * sizeof(int), e.stream));
-  *e.h_status = DevStatus{kNoError, 0, 0};
+  *e.h_status = DevStatus{kNoError, kNoError, 0, 0};
   return ERMOD_OK;
 }
 
@@ -1087,11 +1087,13 @@ static int decode_status(Engine& e) {
       g_err = "non-periodic system: a solute coordinate lies beyond the reach of the frame's fixed-point cube";
     return ERMOD_E_DEVICE;
   }
-  if (s.err_key != kNoError) {
-    e.err_placement = (int)(s.err_key >> 36);
-    e.err_molecule = (int)((s.err_key >> 8) & 0x0fffffff);
+  // the error of the earliest call wins (device API: later calls stopped at their start)
+  const unsigned long long key = (s.first_key != kNoError) ? s.first_key : s.err_key;
+  if (key != kNoError) {
+    e.err_placement = (int)(key >> 36);
+    e.err_molecule = (int)((key >> 8) & 0x0fffffff);
     e.err_energy = std::nan("");
-    return (int)(s.err_key & 0xff);
+    return (int)(key & 0xff);
   }
   return ERMOD_OK;
 }
@@ -1101,7 +1103,9 @@ int ermod_sync(ermod_ctx* c) {
   Engine& e = c->e;
   cudaSetDevice(e.device);
   ERMOD_CUDA(cudaStreamSynchronize(e.stream));
-  return decode_status(e);
+  const int st = decode_status(e);
+  const int rs = reset_status(e);  // the next calls start a new sequence
+  return st ? st : rs;
 }
 
 int ermod_placements_device(ermod_ctx* c, int nplace, const int* tag_d, const double* sol_d, const double* sws_d,
@@ -1123,8 +1127,9 @@ int ermod_placements_device(ermod_ctx* c, int nplace, const int* tag_d, const do
     g_err = "solute larger than 256 sites";
     return ERMOD_E_UNSUPPORTED;
   }
-  st = reset_status(e);
-  if (st) return st;
+  // the status stays until ermod_sync: an error of an earlier call stops this one, as
+  // the reference stops at the first error
+  ERMOD_CUDA(launch_carry_status(e));
   return run_placements(e, nplace, tag_d, sol_d, sws_d, uv_d, fl_d, ns);
 }
 

@@ -97,11 +97,13 @@ struct FrameGeom {
   double reach;
 };
 
-// Device status block (one per context, zeroed by ermod_sync).
+// Device status block (one per context).  The host API resets it at every call; the
+// device API keeps it across calls until ermod_sync reads and resets it.
 struct DevStatus {
-  unsigned long long err_key;  // kNoError when no error
-  int mbin_hit;                // 'mbin' condition met (reported once)
-  int range_fault;             // an index check failed on the device
+  unsigned long long err_key;    // first error of the current call (kNoError when none)
+  unsigned long long first_key;  // device API: first error of an earlier call since the last sync
+  int mbin_hit;                  // 'mbin' condition met (reported once)
+  int range_fault;               // an index check failed on the device
 };
 
 // One batch of placements, as seen by the kernels.
@@ -150,6 +152,7 @@ struct Engine;
 // ---- launchers (defined in the .cu files) ---------------------------------------
 // frame preparation
 cudaError_t launch_frame_wrap(Engine& e);
+cudaError_t launch_carry_status(Engine& e);  // device API: an earlier call's error stops this call
 cudaError_t launch_max_abs(Engine& e, const double* x_d, size_t n, double* host_out);  // syncs e.stream
 cudaError_t launch_frame_sort(Engine& e);
 cudaError_t launch_frame_sites(Engine& e);

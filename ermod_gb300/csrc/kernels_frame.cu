@@ -358,7 +358,24 @@ __global__ void max_abs_kernel(const double* __restrict__ x, size_t n, unsigned 
   atomicMax(out, m);
 }
 
+// device API, at the start of a call: an error left by an earlier call moves to
+// first_key, and err_key keeps it with placement index 0 so that every batch of this
+// call is skipped by the accumulation (its skip test compares the placement index)
+__global__ void carry_status_kernel(DevStatus* s) {
+  const unsigned long long k = s->err_key;
+  if (k != kNoError) {
+    if (s->first_key == kNoError) s->first_key = k;
+    s->err_key = s->first_key & ((1ull << 36) - 1);
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_carry_status(Engine& e) {
+  carry_status_kernel<<<1, 1, 0, e.stream>>>(e.d_status);
+  e.count_launch();
+  return cudaGetLastError();
+}
 
 cudaError_t launch_max_abs(Engine& e, const double* x_d, size_t n, double* host_out) {
   unsigned long long* d = reinterpret_cast<unsigned long long*>(e.d_frame_scal + 2);  // 8-byte aligned scratch

@@ -211,8 +211,10 @@ def droplet(seed: int = 6, frames: int = 20) -> Workload:
 
 def soln_adjoint(seed: int = 5, frames: int = 200) -> Workload:
     rng = np.random.default_rng((seed, 11))
+    # a 7.5 A cavity around the 4.2 A solute: with 6.0 A a water of some frames (frame 7
+    # of seed 5) comes within 2.5 A of a solute site, where the reference stops (eng_sft)
     return Workload("soln_adjoint", "soln", 62.0, 8000, random_solute(rng, 16),
-                    _params(1, 64, corrcal=0, wgtslf=0), seed, frames, 1, 21, cavity=6.0)
+                    _params(1, 64, corrcal=0, wgtslf=0), seed, frames, 1, 21, cavity=7.5)
 
 
 def uneven(seed: int = 4):

@@ -131,12 +131,14 @@ int ermod_placements(ermod_ctx* ctx, int nplace, const int* tagslt, const double
                      const double* stat_weight_solute, double* uvengy_out, double* flceng_out);
 /* Same with tagslt/solute_sitepos/stat_weight_solute in device memory; the optional
  * outputs are device pointers too.  Returns without synchronising: the status of the
- * queued work is reported by the next ermod_sync. */
+ * queued work is reported by the next ermod_sync.  Several calls may be queued between
+ * two syncs: the first error among them is kept, and the calls after the failing one
+ * accumulate nothing (the reference stops at its first error). */
 int ermod_placements_device(ermod_ctx* ctx, int nplace, const int* tagslt_device,
                             const double* solute_sitepos_device,
                             const double* stat_weight_solute_device, double* uvengy_out_device,
                             double* flceng_out_device);
-/* Waits for queued work and returns its status. */
+/* Waits for queued work, returns its status and starts a new sequence of calls. */
 int ermod_sync(ermod_ctx* ctx);
 
 /* engclear (engproc.F90:276-288). */

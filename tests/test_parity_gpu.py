@@ -210,3 +210,47 @@ def test_bare_coulomb_refs_accumulators(gpu_lib, oracle, precision):
     np.testing.assert_allclose(ag["engnorm"], ao["engnorm"], rtol=1e-12)
     np.testing.assert_allclose(ag["edens"].sum(), ao["edens"].sum(), rtol=1e-12)
     gpu.close()
+
+
+def test_device_api_status_kept_until_sync(gpu_lib, oracle):
+    """Device API: an error stays until ermod_sync reads it, later calls queued before the
+    sync are stopped by it (the reference stops at its first error), and ermod_sync
+    starts a new sequence.  Frame 7 of this workload stops the reference with eng_sft
+    (a water jittered into the solute's core)."""
+    import torch
+    from ermod_gb300 import _lib, setconf, synth
+    from ermod_gb300.engproc import EnergyRepresentation
+    w = synth.Workload("status", "soln", 62.0, 8000, synth.random_solute(np.random.default_rng((5, 11)), 16),
+                       synth._params(1, 64, corrcal=0, wgtslf=0), 5, 9, 1, 21, cavity=6.0)
+    topo = setconf.setparam_topology(w.species(), slttype=1)
+    bins = setconf.enginit_bins(topo["numslv"])
+    orc = oracle.Oracle(w.params, topo, bins)
+    st = []
+    for f in (6, 7, 8):
+        pos, cell = w.frame(f)
+        orc.frame(pos, cell)
+        st.append(orc.placements([topo["nummol"]], raise_on_error=False)["status"])
+    assert st == [0, _lib.E_ENG_SFT, 0]
+    dev = torch.device("cuda", 0)
+    tag = torch.tensor([topo["nummol"]], dtype=torch.int32, device=dev)
+    pos_d = {f: torch.from_numpy(w.frame(f)[0]).to(dev) for f in (6, 7, 8)}
+    cell = w.frame(6)[1]
+    eng = EnergyRepresentation(w.params, topo, bins, precision="mixed")
+    torch.cuda.synchronize()
+    eng.frame_device(pos_d[6].data_ptr(), cell)
+    eng.placements_device(1, tag.data_ptr())
+    eng.sync()
+    a6 = eng.accum()
+    for f in (7, 8):  # queued without a sync in between
+        eng.frame_device(pos_d[f].data_ptr(), cell)
+        eng.placements_device(1, tag.data_ptr())
+    with pytest.raises(_lib.ErmodError) as ei:
+        eng.sync()
+    assert ei.value.code == _lib.E_ENG_SFT
+    a = eng.accum()
+    assert a["engnorm"] == a6["engnorm"] and np.array_equal(a["edens"], a6["edens"])
+    eng.frame_device(pos_d[8].data_ptr(), cell)  # a new sequence after the sync
+    eng.placements_device(1, tag.data_ptr())
+    eng.sync()
+    assert eng.accum()["engnorm"] == 2.0 * a6["engnorm"]  # one more placement of the same weight
+    eng.close()
