@@ -254,3 +254,23 @@ def test_device_api_status_kept_until_sync(gpu_lib, oracle):
     eng.sync()
     assert eng.accum()["engnorm"] == 2.0 * a6["engnorm"]  # one more placement of the same weight
     eng.close()
+
+
+@pytest.mark.parametrize("K,order", [(48, 4), (64, 6), (96, 8), (128, 4)])
+def test_compile_time_grid_sizes(gpu_lib, oracle, K, order):
+    """The cubic grids with compile-time transforms (48, 64, 96, 128) against the oracle,
+    with spline orders 4, 6 and 8 (the other grids take the generic kernels)."""
+    w = helpers.small_refs(K=K, corrcal=0, wgtslf=0)
+    w.params["splodr"] = order
+    topo, bins = helpers.build_inputs(w)
+    gpu, orc = _engines(gpu_lib, oracle, w, topo, bins, "mixed")
+    pos, cell = w.frame(0)
+    pl = w.placements(0, 12)
+    tag = np.full(len(pl), topo["nummol"], np.int32)
+    orc.frame(pos, cell)
+    ro = orc.placements(tag, pl)
+    gpu.frame(pos, cell)
+    rg = gpu.placements(tag, pl, want_uvengy=True)
+    _check_energies(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], "mixed")
+    np.testing.assert_allclose(rg["uvengy"][:, 0], ro["uvengy"][:, 0], rtol=1e-6, atol=1e-4)
+    gpu.close()
