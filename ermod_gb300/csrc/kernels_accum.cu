@@ -455,40 +455,45 @@ __device__ __forceinline__ void ff_add_prod(float& hi, float& lo, float wh, floa
   hi = s;
 }
 
-__global__ void __launch_bounds__(256) ecorr_ff_kernel(const int* __restrict__ hist, const int* __restrict__ valid,
-                                                     const double* __restrict__ w, int nring, int ermax,
-                                                     double* __restrict__ ecorr, long long* __restrict__ ecorr_n) {
-  extern __shared__ int sdyn[];
-  int* sci = sdyn;                      // [nring][kEcRows]
-  unsigned* smask = reinterpret_cast<unsigned*>(sdyn + (size_t)nring * kEcRows);  // [nring]
-  float* swh = reinterpret_cast<float*>(smask + nring);  // [nring] weight, float-float
-  float* swl = swh + nring;
+template <bool COUNT>
+__global__ void __launch_bounds__(256, 2) ecorr_ff_kernel(const int* __restrict__ hist, const int* __restrict__ valid,
+                                                        const double* __restrict__ w, int nring, int ermax,
+                                                        double* __restrict__ ecorr, long long* __restrict__ ecorr_n) {
+  extern __shared__ float2 sdyn2[];
+  float2* sa = sdyn2;  // [nring][kEcRows]: w_p * hist[p][row0 + r] as a float-float pair
+  unsigned* smask = reinterpret_cast<unsigned*>(sa + (size_t)nring * kEcRows);  // [nring]
+  int* sci = reinterpret_cast<int*>(smask + nring);  // [nring][kEcRows] counts (count mirror only)
   const int row0 = blockIdx.y * kEcRows;
   const int nrow = min(kEcRows, ermax - row0);
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   for (int p = threadIdx.x; p < nring; p += blockDim.x) {
     unsigned m = 0;
     const bool ok = valid[p] != 0;
+    const double wd = w[p];
+    const float wh = (float)wd;
+    const float wl = (float)(wd - (double)wh);
     for (int r = 0; r < kEcRows; ++r) {
       const int c = (ok && r < nrow) ? hist[(size_t)p * ermax + row0 + r] : 0;
-      sci[p * kEcRows + r] = c;
+      // w * c as a float-float pair (c < 2^24 is exact in FP32; the high product is
+      // split exactly by fma)
+      const float fc = (float)c;
+      const float ah = wh * fc;
+      const float al = fmaf(wl, fc, fmaf(wh, fc, -ah));
+      sa[p * kEcRows + r] = make_float2(ah, al);
+      if (COUNT) sci[p * kEcRows + r] = c;
       if (c) m |= 1u << r;
     }
     smask[p] = m;
-    const double wd = w[p];
-    const float wh = (float)wd;
-    swh[p] = wh;
-    swl[p] = (float)(wd - (double)wh);
   }
   __syncthreads();
   if (j >= ermax) return;
   float hi[kEcRows], lo[kEcRows];
-  long long cn[kEcRows];
+  long long cn[COUNT ? kEcRows : 1];
 #pragma unroll
   for (int r = 0; r < kEcRows; ++r) {
     hi[r] = 0.f;
     lo[r] = 0.f;
-    cn[r] = 0;
+    if (COUNT) cn[r] = 0;
   }
   bool any = false;
   constexpr int U = 8;  // loads in flight per thread
@@ -505,18 +510,14 @@ __global__ void __launch_bounds__(256) ecorr_ff_kernel(const int* __restrict__ h
       const int p = p0 + u;
       any = true;
       const unsigned m = smask[p];
-      const float wh = swh[p], wl = swl[p];
       const float c = (float)cj[u];
+      const float2* ap = sa + p * kEcRows;
 #pragma unroll
       for (int r = 0; r < kEcRows; ++r) {
         if (m & (1u << r)) {
-          const int ci = sci[p * kEcRows + r];
-          // w * ci as a float-float pair (ci < 2^24 is exact in FP32)
-          const float fci = (float)ci;
-          const float ph = wh * fci;
-          const float pl = fmaf(wl, fci, fmaf(wh, fci, -ph));
-          ff_add_prod(hi[r], lo[r], ph, pl, c);
-          if (ecorr_n) cn[r] += (long long)ci * (long long)cj[u];
+          const float2 a = ap[r];
+          ff_add_prod(hi[r], lo[r], a.x, a.y, c);
+          if (COUNT) cn[r] += (long long)sci[p * kEcRows + r] * (long long)cj[u];
         }
       }
     }
@@ -527,7 +528,7 @@ __global__ void __launch_bounds__(256) ecorr_ff_kernel(const int* __restrict__ h
     if (r >= nrow) break;
     const size_t at = (size_t)(row0 + r) * ermax + j;
     if (hi[r] != 0.f || lo[r] != 0.f) ecorr[at] = ecorr[at] + ((double)hi[r] + (double)lo[r]);
-    if (ecorr_n && cn[r] != 0) ecorr_n[at] += cn[r];
+    if (COUNT && cn[r] != 0) ecorr_n[at] += cn[r];
   }
 }
 
@@ -589,16 +590,20 @@ cudaError_t launch_ecorr_flush(Engine& e, cudaStream_t s) {
   if (e.ring_fill == 0) return cudaSuccess;
   const int n = e.ring_fill;
   if (e.mixed) {
-    const size_t smem = (size_t)n * (kEcRows * sizeof(int) + sizeof(unsigned) + 2 * sizeof(float));
+    const bool count = e.d_ecorr_n != nullptr;
+    const size_t smem =
+        (size_t)n * (kEcRows * sizeof(float2) + sizeof(unsigned) + (count ? kEcRows * sizeof(int) : 0));
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return err;
+    void (*kern)(const int*, const int*, const double*, int, int, double*, long long*) =
+        count ? ecorr_ff_kernel<true> : ecorr_ff_kernel<false>;
     if (smem > 48 * 1024) {
-      err = cudaFuncSetAttribute(ecorr_ff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (err != cudaSuccess) return err;
     }
     dim3 grid((e.ermax + 255) / 256, (e.ermax + kEcRows - 1) / kEcRows);
-    ecorr_ff_kernel<<<grid, 256, smem, s>>>(e.d_ring_hist + (size_t)e.ring_off * e.ermax, e.d_ring_valid + e.ring_off,
-                                            e.d_ring_w + e.ring_off, n, e.ermax, e.d_ecorr, e.d_ecorr_n);
+    kern<<<grid, 256, smem, s>>>(e.d_ring_hist + (size_t)e.ring_off * e.ermax, e.d_ring_valid + e.ring_off,
+                                 e.d_ring_w + e.ring_off, n, e.ermax, e.d_ecorr, e.d_ecorr_n);
     e.count_launch();
     return cudaGetLastError();
   }
