@@ -277,8 +277,8 @@ static int ensure_batch(Engine& e) {
     e.phi_dims[1] = e.geom.K[1] + h;
     e.phi_dims[2] = e.geom.K[2] + h;
     e.gbox[0] = ((kBrickX + h + 3) / 4) * 4;
-    e.gbox[1] = kBrickYZ + h;
-    e.gbox[2] = kBrickYZ + h;
+    e.gbox[1] = kBrickY + h;
+    e.gbox[2] = kBrickZ + h;
     const size_t np = (size_t)e.phi_dims[0] * e.phi_dims[1] * e.phi_dims[2];
     ERMOD_CUDA(dalloc(&b.phi, 2 * np * B));
     ERMOD_CUDA(cudaMemset(b.phi, 0, sizeof(float) * 2 * np * B));
@@ -684,7 +684,8 @@ int ermod_set_topology(ermod_ctx* c, int nummol, int numatm, const int* mbi, con
   ERMOD_CUDA(dalloc(&e.d_sort_val_alt, e.slvmax + 1));
   ERMOD_CUDA(cudaMemset(e.d_sort_val_alt, 0, sizeof(int) * (e.slvmax + 1)));
   e.nbrick[0] = (e.geom.K[0] + kBrickX - 1) / kBrickX;
-  for (int i = 1; i < 3; ++i) e.nbrick[i] = (e.geom.K[i] + kBrickYZ - 1) / kBrickYZ;
+  e.nbrick[1] = (e.geom.K[1] + kBrickY - 1) / kBrickY;
+  e.nbrick[2] = (e.geom.K[2] + kBrickZ - 1) / kBrickZ;
   e.nbricks = e.nbrick[0] * e.nbrick[1] * e.nbrick[2];
   e.cub_tmp_bytes = std::max(frame_cub_bytes(e.slvmax), brick_cub_bytes(e.nsite_phys, e.nbricks));
   ERMOD_CUDA(dalloc((char**)&e.d_cub_tmp, e.cub_tmp_bytes));

@@ -67,8 +67,8 @@ __host__ __device__ inline long long ordered_key(double x) {
   return k ^ ((k >> 63) & 0x7fffffffffffffffll);
 }
 
-// bricks of the mixed path's gather: kBrickX x kBrickYZ x kBrickYZ PME grid points
-constexpr int kBrickX = 16, kBrickYZ = 8;
+// bricks of the mixed path's gather: kBrickX x kBrickY x kBrickZ PME grid points
+constexpr int kBrickX = 16, kBrickY = 8, kBrickZ = 8;
 
 // ordered 32-bit key of a float (-0 == +0).  For a float u and a double edge e,
 // u <= e exactly when u <= rd(e), the largest float not above e, and u > e exactly when

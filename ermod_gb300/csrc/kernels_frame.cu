@@ -222,7 +222,7 @@ __global__ void frame_sites_kernel(SiteArgs A) {
   atomicMax((int*)&A.frame_scal[0], __float_as_int((float)rmax * 1.0001f + 1e-4f));
 }
 
-// brick of every site: the kBrickX x kBrickYZ^2 block of PME grid points holding its
+// brick of every site: the kBrickX x kBrickY x kBrickZ block of PME grid points holding its
 // stencil base point
 __global__ void brick_key_kernel(const int* __restrict__ site_grid, int nsite, int K1, int K2, int K3, int nbx,
                                  int nby, unsigned int* __restrict__ key, int* __restrict__ val,
@@ -234,7 +234,7 @@ __global__ void brick_key_kernel(const int* __restrict__ site_grid, int nsite, i
   if (g1 >= K1) g1 -= K1;
   if (g2 >= K2) g2 -= K2;
   if (g3 >= K3) g3 -= K3;
-  const unsigned int bk = (unsigned int)(((g3 / kBrickYZ) * nby + (g2 / kBrickYZ)) * nbx + (g1 / kBrickX));
+  const unsigned int bk = (unsigned int)(((g3 / kBrickZ) * nby + (g2 / kBrickY)) * nbx + (g1 / kBrickX));
   key[i] = bk;
   val[i] = i;
   atomicAdd(&count[bk], 1);

@@ -581,7 +581,7 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, uint32_t 
 }
 constexpr long kWaitLimit = 1L << 24;  // try_wait rounds before a CTA gives up and flags an error
 
-// Mixed path, step 1 -- gather by bricks.  CTA per (kBrickX x kBrickYZ^2 brick of the
+// Mixed path, step 1 -- gather by bricks.  CTA per (kBrickX x kBrickY x kBrickZ brick of the
 // PME grid, run of placement groups of 4).  One 5-D TMA box copy per group brings the
 // brick's stencil halo of the group's interleaved potential grids into shared memory as
 // [z][y][x][4], in kGatherStages buffers so that the next groups' copies are in flight
@@ -597,7 +597,7 @@ __device__ __forceinline__ void site_setup(int site, const float4* __restrict__ 
                                            const int* __restrict__ site_grid, int K1, int K2, int K3, int ox,
                                            int oy, int oz, int BX, float (&w1)[P], float (&w2)[P],
                                            float (&w3)[P], int& base, float& q) {
-  constexpr int BY = kBrickYZ + P - 1;
+  constexpr int BY = kBrickY + P - 1;
   const float4 rec = site_rec[site];
   const int gp = site_grid[site];
   bspline_w<P>(rec.x, w1);
@@ -614,7 +614,7 @@ __device__ __forceinline__ void site_setup(int site, const float4* __restrict__ 
 template <int P>
 __device__ __forceinline__ float4 site_stencil(const float4* __restrict__ halo, int base, int BX,
                                                const float (&w1)[P], const float (&w2)[P], const float (&w3)[P]) {
-  constexpr int BY = kBrickYZ + P - 1;
+  constexpr int BY = kBrickY + P - 1;
   constexpr int U3 = P <= 4 ? P : 1;  // higher orders: keep the register footprint bounded
   float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll U3
@@ -642,7 +642,7 @@ __global__ void __launch_bounds__(kGatherThreads) gather_tma_kernel(
     const __grid_constant__ CUtensorMap tmap, int nb, int groups_per_cta, const float4* __restrict__ site_rec,
     const int* __restrict__ site_grid, const int* __restrict__ brick_site, const int* __restrict__ brick_start,
     int K1, int K2, int K3, int nbx, int nby, int BX, int ldb, float* __restrict__ site_e, DevStatus* status) {
-  constexpr int BY = kBrickYZ + P - 1, BZ = kBrickYZ + P - 1;
+  constexpr int BY = kBrickY + P - 1, BZ = kBrickZ + P - 1;
   extern __shared__ unsigned char smem_raw[];
   __shared__ unsigned long long bar[kGatherStages];
   const int npt = BZ * BY * BX;
@@ -662,17 +662,17 @@ __global__ void __launch_bounds__(kGatherThreads) gather_tma_kernel(
   }
   __syncthreads();
   // padded coordinates: the halo of brick (bx, by, bz) starts at (kBrickX bx,
-  // kBrickYZ by, kBrickYZ bz); the innermost box coordinate (the placement within the
+  // kBrickY by, kBrickZ bz); the innermost box coordinate (the placement within the
   // group) is 0
   if (threadIdx.x == 0) {
     for (int g = g_begin; g < min(g_end, g_begin + kGatherStages); ++g) {
       const int st = g - g_begin;
       mbar_expect_tx(&bar[st], box_bytes);
-      tma_load_5d(halo_base + (size_t)st * hstride, &tmap, 0, bx * kBrickX, by * kBrickYZ, bz * kBrickYZ, g, &bar[st]);
+      tma_load_5d(halo_base + (size_t)st * hstride, &tmap, 0, bx * kBrickX, by * kBrickY, bz * kBrickZ, g, &bar[st]);
     }
   }
   const int h = P - 1;
-  const int ox = bx * kBrickX - h, oy = by * kBrickYZ - h, oz = bz * kBrickYZ - h;
+  const int ox = bx * kBrickX - h, oy = by * kBrickY - h, oz = bz * kBrickZ - h;
   const int s_begin = brick_start[brick], s_end = brick_start[brick + 1];
   const int n = s_end - s_begin;
   // Site-to-thread map.  A 16-byte shared load is served 8 lanes at a time, and the
@@ -756,7 +756,7 @@ __global__ void __launch_bounds__(kGatherThreads) gather_tma_kernel(
     if (threadIdx.x == 0 && g + kGatherStages < g_end) {
       fence_proxy_async_smem();
       mbar_expect_tx(&bar[slot], box_bytes);
-      tma_load_5d(halo_base + (size_t)slot * hstride, &tmap, 0, bx * kBrickX, by * kBrickYZ, bz * kBrickYZ, g + kGatherStages,
+      tma_load_5d(halo_base + (size_t)slot * hstride, &tmap, 0, bx * kBrickX, by * kBrickY, bz * kBrickZ, g + kGatherStages,
                   &bar[slot]);
     }
   }
