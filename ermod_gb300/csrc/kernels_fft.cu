@@ -553,8 +553,8 @@ __global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(Pme
   float2* s0 = sm;
   float2* s1 = sm + bufsz;
   float2* tw1 = s1 + bufsz;
-  float2* tw2 = tw1 + K1;
-  for (int i = threadIdx.x; i < K1 + K2; i += blockDim.x) {
+  float2* tw2 = KC ? tw1 : tw1 + K1;  // one table for a cubic grid (K1 = K2)
+  for (int i = threadIdx.x; i < (KC ? K1 : K1 + K2); i += blockDim.x) {
     const float2 t = A.twiddle[i];
     if (i < K1)
       tw1[i] = make_float2(t.x, -t.y);
@@ -703,11 +703,12 @@ __global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(Pme
 }
 
 size_t pme_a_smem(int K3, int Hp) { return sizeof(float2) * ((size_t)2 * K3 * Hp + K3); }
-size_t pme_b_smem(int K1, int K2, int H) {
+// shared_tw: a cubic grid with compile-time sizes keeps one twiddle table for k1 and k2
+size_t pme_b_smem(int K1, int K2, int H, bool shared_tw) {
   const size_t plane = (size_t)K2 * H;
   const size_t npair = (K2 + 1) / 2;
   const size_t bufsz = std::max(plane, npair * (size_t)(K1 | 1));
-  return sizeof(float2) * (2 * bufsz + K1 + K2);
+  return sizeof(float2) * (2 * bufsz + K1 + (shared_tw ? 0 : K2));
 }
 
 }  // namespace
@@ -716,7 +717,7 @@ bool pme_fits(int K1, int K2, int K3) {
   const int H = K1 / 2 + 1, Hp = ((H + kR1 - 1) / kR1) * kR1;
   FftPlan a, b, c;
   if (!plan(K1, a) || !plan(K2, b) || !plan(K3, c)) return false;
-  return pme_a_smem(K3, Hp) <= 227 * 1024 && pme_b_smem(K1, K2, H) <= 227 * 1024;
+  return pme_a_smem(K3, Hp) <= 227 * 1024 && pme_b_smem(K1, K2, H, false) <= 227 * 1024;
 }
 
 cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a) {
@@ -748,11 +749,11 @@ cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a) {
   A.fHp4 = make_fastdiv(A.Hp / kR1);
   A.fnpair = make_fastdiv((A.K2 + 1) / 2);
   A.fKX = make_fastdiv(A.K1 + A.halo);
-  const size_t sa = pme_a_smem(A.K3, A.Hp), sb = pme_b_smem(A.K1, A.K2, A.H);
   cudaError_t err;
   // cubic grids of common sizes take the compile-time transforms
   const bool cubic = A.K1 == A.K2 && A.K2 == A.K3;
   const int KC = (cubic && (A.K1 == 32 || A.K1 == 48 || A.K1 == 64 || A.K1 == 96 || A.K1 == 128)) ? A.K1 : 0;
+  const size_t sa = pme_a_smem(A.K3, A.Hp), sb = pme_b_smem(A.K1, A.K2, A.H, KC > 0);
   void (*ka)(PmeArgs) = pme_a_kernel<0>;
   void (*kb)(PmeArgs) = pme_b_kernel<0>;
   if (KC == 32) ka = pme_a_kernel<32>, kb = pme_b_kernel<32>;
