@@ -400,7 +400,7 @@ __device__ __forceinline__ ff ff_add(ff a, float b) {
 __device__ __forceinline__ ff ff_add2(ff a, ff b) { return ff_add(ff_add(a, b.hi), b.lo); }
 
 constexpr int kSites = 32;  // solute sites staged per chunk
-constexpr int kR1 = 4, kR3 = 4;
+constexpr int kR1 = 4, kR3 = 3;  // generation tile: kR3 k3 values x kR1 k1 values per thread
 
 struct PmeArgs {
   const float2* bvec;   // [nb][S][3][Kmax]

@@ -17,14 +17,14 @@ transform (8 K^3 written by the spread, read by D2Z; 16 H K^2 written by D2Z).
 from __future__ import annotations
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per placement of each mixed
-# kernel, from one ncu --set full capture of a 128-placement launch of refs_large
+# kernel, from one ncu --set full capture of a 256-placement launch of refs_large
 # (33,000 waters, PME 96^3, order 4, 12-site solute).  At this batch the PME
-# intermediate no longer stays in L2, so these are close to the launch's full traffic;
+# intermediate does not stay in L2, so these are close to the launch's full traffic;
 # a launch of B placements moves about B times these bytes.
 MEASURED_TRAFFIC_REFS_LARGE = {
-    "spectrum": (5.21e6 + 403.27e6) / 128,  # pme_a: writes the half spectrum after the k3 transform
-    "fft_c2r": (501.23e6 + 449.01e6) / 128,  # pme_b: reads it, writes the padded potential grid
-    "gather": (516.57e6 + 44.88e6) / 128,  # gather_tma: reads the grid (halo boxes) and site data
+    "spectrum": (8.2e6 + 866.1e6) / 256,  # pme_a: writes the half spectrum after the k3 transform
+    "fft_c2r": (954.4e6 + 955.4e6) / 256,  # pme_b: reads it, writes the padded potential grid
+    "gather": (1022.9e6 + 96.4e6) / 256,  # gather_tma: reads the grid (halo boxes) and site data
 }
 
 
