@@ -729,7 +729,11 @@ int ermod_set_bins(ermod_ctx* c, int numslv, const int* uvmax, const int* uvsoft
     if (uvmax[s] <= 0 || uvsoft[s] < 0 || uvsoft[s] > uvmax[s]) return fail_param("uvmax/uvsoft inconsistent");
     ermax += uvmax[s];
   }
-  for (int i = 1; i < ermax; ++i) (void)uvcrd;
+  // binsearch (engproc.F90:927-957) needs each species' edges in increasing order
+  for (int sp = 0, off = 0; sp < numslv; off += uvmax[sp], ++sp)
+    for (int i = off; i < off + uvmax[sp]; ++i)
+      if (!(uvcrd[i] == uvcrd[i]) || (i > off && !(uvcrd[i] > uvcrd[i - 1])))
+        return fail_param("uvcrd must increase within each species");
   free_batch(e);
   free_bins(e);
   e.bins_ready = false;

@@ -274,3 +274,19 @@ def test_compile_time_grid_sizes(gpu_lib, oracle, K, order):
     _check_energies(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], "mixed")
     np.testing.assert_allclose(rg["uvengy"][:, 0], ro["uvengy"][:, 0], rtol=1e-6, atol=1e-4)
     gpu.close()
+
+
+def test_set_bins_rejects_unsorted_edges(gpu_lib):
+    """binsearch (engproc.F90:927-957) needs each species' edges in increasing order."""
+    from ermod_gb300 import _lib
+    from ermod_gb300.engproc import EnergyRepresentation
+    w = helpers.small_refs(corrcal=0, wgtslf=0)
+    topo, bins = helpers.build_inputs(w)
+    gpu = EnergyRepresentation(w.params, topo, bins, precision="mixed")
+    bad = dict(bins)
+    bad["uvcrd"] = np.array(bins["uvcrd"], np.float64).copy()
+    bad["uvcrd"][10], bad["uvcrd"][11] = bad["uvcrd"][11], bad["uvcrd"][10]
+    with pytest.raises(_lib.ErmodError) as ei:
+        gpu.set_bins(bad)
+    assert ei.value.code == _lib.E_PARAM
+    gpu.close()
