@@ -146,7 +146,7 @@ struct Engine {
   // ---- mixed path potential grids: padded periodic layout + TMA descriptor ----------
   int phi_dims[3] = {0, 0, 0};   // XP (multiple of 4), YP, ZP
   int gbox[3] = {0, 0, 0};       // gather box: x (multiple of 4), y, z
-  alignas(64) CUtensorMap phi_tmap[2];  // per slot
+  CUtensorMap phi_tmap[2];  // per slot (the type carries its alignment)
 
   // adjoint mode (mixed path): bin-resolved derivatives of the solvent molecules'
   // energies with respect to the per-site charge, LJ epsilon and LJ sigma of a solute

@@ -32,10 +32,6 @@ template <int R>
 struct Dft;
 
 template <>
-struct Dft<1> {
-  static __device__ __forceinline__ void run(float2*) {}
-};
-template <>
 struct Dft<2> {
   static __device__ __forceinline__ void run(float2* v) {
     const float2 a = v[0], b = v[1];

@@ -473,45 +473,12 @@ __global__ void __launch_bounds__(256) mol_energy_kernel(MolArgs A) {
       pairep = pairep + recip;
       u = real + pairep;
       // ---- getiduv / binsearch ----
-      int code = 0;
       int ret = 0;
-      if (species < 1 || species > A.numslv) {
-        code = ERMOD_E_ENG_CNS;
-      } else if (u != u) {
-        code = ERMOD_E_ENG_MIN;
-      } else {
-        const long long ku = ordered_key(u);
-        const long long* keys = A.uvkey + sp_off;
-        int lo = 0, hi = sp_n;
-        while (lo < hi) {
-          const int mid = (lo + hi) >> 1;
-          if (__ldg(keys + mid) < ku)
-            lo = mid + 1;
-          else
-            hi = mid;
-        }
-        ret = lo;
-        if (ret <= 0)
-          code = ERMOD_E_ENG_MIN;
-        else if (A.soln && ret > sp_soft)
-          code = ERMOD_E_ENG_SFT;
-        else if (ret == sp_n && u < 1.0e3 && A.mbin_mode != 0) {
-          if (A.mbin_mode == 1)
-            code = ERMOD_W_MBIN;
-          else
-            atomicOr(&A.status->mbin_hit, 1);
-        }
-      }
-      if (code) {
+      const int code = bin_molecule(A, u, species, sp_off, sp_n, sp_soft, ret);
+      if (code)
         atomicMin(&A.status->err_key, make_err_key(a.b0 + b, k + 1, code));
-      } else {
-        const int bin = sp_off + ret - 1;
-        int* h = smem_hist + gi * A.ermax;
-        const unsigned am = __activemask();
-        const unsigned peers = __match_any_sync(am, bin);
-        const int leader = __ffs(peers) - 1;
-        if ((threadIdx.x & 31) == leader) atomicAdd(&h[bin], __popc(peers));
-      }
+      else
+        hist_add(smem_hist + gi * A.ermax, sp_off + ret - 1);
       if (a.uvengy_out) a.uvengy_out[(size_t)(a.b0 + b) * (A.slvmax + 1) + k + 1] = u;
     } else if (valid && a.uvengy_out) {
       a.uvengy_out[(size_t)(a.b0 + b) * (A.slvmax + 1) + k + 1] = 0.0;
