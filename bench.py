@@ -133,13 +133,16 @@ def make_workload(args):
 
 
 def cpu_oracle_rate(w, topo, bins, nplace, frame_index=0):
-    """The FP64 oracle on nplace placements of one frame, all host cores."""
+    """The FP64 oracle on nplace placements of one frame, all host cores (solution mode:
+    the frame's own solute, once)."""
     from oracle import oracle as O
     O.build()
     orc = O.Oracle(w.params, topo, bins)
     pos, cell = w.frame(frame_index)
     orc.frame(pos, cell)
-    pl = w.placements(frame_index, nplace)
+    if w.mode == "soln":
+        nplace = 1
+    pl = None if w.mode == "soln" else w.placements(frame_index, nplace)
     tag = np.full(nplace, topo["nummol"], np.int32)
     t0 = time.perf_counter()
     orc.placements(tag, pl, want_uvengy=False, nthreads=0)
@@ -156,7 +159,7 @@ def run_reference(args):
     w = make_workload(args)
     topo = setconf.setparam_topology(w.species(), slttype=w.params["slttype"])
     bins = setconf.enginit_bins(topo["numslv"])
-    sample = max(1, args.cpu_sample // 4)
+    sample = 1 if w.mode == "soln" else max(1, args.cpu_sample // 4)  # solution mode: the frame's solute
     for i in range(args.warmup):
         cpu_oracle_rate(w, topo, bins, max(1, sample // 4), i)
     t_total, units = 0.0, 0
@@ -202,7 +205,8 @@ def run_ours(args):
     nsteps = args.warmup + args.steps
     # frames of this rank (weak scaling: every rank its own frames)
     frames = [w.frame(rank * nsteps + i) for i in range(nsteps)]
-    places = [w.placements(rank * nsteps + i, nplace) for i in range(nsteps)]
+    soln = w.mode == "soln"  # solution mode: the solute is the frame's own molecule
+    places = None if soln else [w.placements(rank * nsteps + i, nplace) for i in range(nsteps)]
     tag_h = np.full(nplace, topo["nummol"], np.int32)
     cell = frames[0][1]
 
@@ -210,14 +214,14 @@ def run_ours(args):
     stream = torch.cuda.Stream(device=dev)
     eng.set_stream(stream.cuda_stream)
     pos_d = [torch.from_numpy(f[0]).to(dev) for f in frames]
-    pl_d = [torch.from_numpy(np.ascontiguousarray(p)).to(dev) for p in places]
+    pl_d = None if soln else [torch.from_numpy(np.ascontiguousarray(p)).to(dev) for p in places]
     tag_d = torch.from_numpy(tag_h).to(dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     torch.cuda.synchronize()
 
     def step(i):
         eng.frame_device(pos_d[i].data_ptr(), frames[i][1])
-        eng.placements_device(nplace, tag_d.data_ptr(), pl_d[i].data_ptr())
+        eng.placements_device(nplace, tag_d.data_ptr(), 0 if soln else pl_d[i].data_ptr())
 
     for i in range(args.warmup):
         with torch.cuda.stream(stream):
@@ -260,12 +264,13 @@ def run_ours(args):
     cand = {k: phases.get(k, 0.0) for k in ("spectrum", "fft_c2r", "gather")}
     dom = max(cand, key=cand.get)
     avg_launch_ms = cand[dom] / nbatch
-    bytes_per_launch = per_pl[dom] * args.batch
+    per_launch = nplace / ((nplace + args.batch - 1) // args.batch)  # placements per PME launch
+    bytes_per_launch = per_pl[dom] * per_launch
     peak, peak_kind = load_peaks()
     achieved = bytes_per_launch / (avg_launch_ms / 1000.0) / 1e9
     traffic = None
     if args.workload == "refs_large":
-        traffic = roofline.MEASURED_TRAFFIC_REFS_LARGE[dom] * args.batch
+        traffic = roofline.MEASURED_TRAFFIC_REFS_LARGE[dom] * per_launch
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
             "traffic_note": "ncu DRAM read+write per launch (one capture, scaled to the launch's placements)",
@@ -277,7 +282,8 @@ def run_ours(args):
     e2e = None
     if not args.no_e2e:
         eng2 = EnergyRepresentation(w.params, topo, bins, precision="mixed", device=local, batch=args.batch)
-        pinned_pl = [torch.from_numpy(np.ascontiguousarray(p)).pin_memory().numpy() for p in places]
+        pinned_pl = [None] * nsteps if soln else [torch.from_numpy(np.ascontiguousarray(p)).pin_memory().numpy()
+                                                  for p in places]
         pinned_pos = [torch.from_numpy(f[0]).pin_memory().numpy() for f in frames]
         for i in range(args.warmup):
             eng2.frame(pinned_pos[i], cell)
@@ -291,7 +297,7 @@ def run_ours(args):
             acc = eng2.accum()
         dt = time.perf_counter() - t0
         eng2.close()
-        h2d = frames[0][0].nbytes + places[0].nbytes + tag_h.nbytes
+        h2d = frames[0][0].nbytes + (0 if soln else places[0].nbytes) + tag_h.nbytes
         ermax = len(bins["uvcrd"])
         d2h = (ermax * ermax + ermax + 2 * (topo["numslv"] + 1) + topo["numslv"] + 5) * 8
         e2e = {"value": nplace * w.nwater * args.steps / dt * ws, "unit": "molecule-energies/s",
@@ -303,21 +309,22 @@ def run_ours(args):
     if rank == 0 and args.plain_sample > 0:
         eng64 = EnergyRepresentation(w.params, topo, bins, precision="fp64", device=local)
         eng64.frame(frames[0][0], cell)
-        n = args.plain_sample
-        eng64.placements(tag_h[:4], places[0][:4])
+        n = min(args.plain_sample, nplace)
+        eng64.placements(tag_h[:4], None if soln else places[0][:4])
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        eng64.placements(tag_h[:n], places[0][:n])
+        eng64.placements(tag_h[:n], None if soln else places[0][:n])
         dt = time.perf_counter() - t0
         eng64.close()
-        plain = {"value": n * w.nwater / dt, "unit": "molecule-energies/s", "sample": f"{n} insertions, frame 0",
+        plain = {"value": n * w.nwater / dt, "unit": "molecule-energies/s", "sample": f"{n} placements, frame 0",
                  "dtype": "f64"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        rate, dt = cpu_oracle_rate(w, topo, bins, args.cpu_sample, 0)
+        ncpu = 1 if soln else args.cpu_sample
+        rate, dt = cpu_oracle_rate(w, topo, bins, ncpu, 0)
         cpu = {"value": rate, "unit": "molecule-energies/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"{args.cpu_sample} insertions of frame 0 ({dt:.1f} s), FP64 oracle, OpenMP over insertions"}
+               "sample": f"{ncpu} placements of frame 0 ({dt:.2f} s), FP64 oracle, OpenMP"}
 
     if rank == 0:
         line = {
@@ -326,8 +333,9 @@ def run_ours(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic",
             "config": {"workload": f"{w.name}: {w.nwater} waters, {w.box} A box, PME {K}^3 order "
-                                   f"{w.params['splodr']}, {nsite_u}-site solute, {nplace} insertions/frame, "
-                                   f"ecorr on", "batch": args.batch, "l2": "flushed between steps (256 MiB write)",
+                                   f"{w.params['splodr']}, {nsite_u}-site solute, "
+                                   + (f"solution mode" if soln else f"{nplace} insertions/frame")
+                                   + (", ecorr on" if w.params.get("corrcal") else ""), "batch": args.batch, "l2": "flushed between steps (256 MiB write)",
                        "parallelism": f"frames sharded over {ws} GPU(s)" if ws > 1 else "1 GPU"},
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "plain_fp64_gpu": plain,
             "gpu_launches": int(launches), "clocks": clocks,
