@@ -850,20 +850,23 @@ __global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const flo
   // per-species {sum, min, max} of the block: one warp per (placement, species),
   // fixed lane order and a fixed shuffle tree
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // the species sums are flceng (engproc.F90:822-825): needed for slnuv (solution mode)
+  // and when the caller asks for flceng
+  const bool want_sum = A.soln || a.flceng_out != nullptr;
   for (int pr = warp; pr < ng * A.numslv; pr += blockDim.x / 32) {
     const int j = pr / A.numslv, sp = pr % A.numslv + 1;
     float mn = INFINITY, mx = -INFINITY;
-    double s = 0.0;  // slnuv terms, SOLN only
+    double s = 0.0;
     for (int t = lane; t < blockDim.x; t += 32) {
       const float v = su[j][t];
       if (sspec[t] == sp && v == v) {
-        if (A.soln) s += (double)v;
+        if (want_sum) s += (double)v;
         mn = fminf(mn, v);
         mx = fmaxf(mx, v);
       }
     }
     for (int off = 16; off > 0; off >>= 1) {
-      if (A.soln) s += __shfl_down_sync(0xffffffffu, s, off);
+      if (want_sum) s += __shfl_down_sync(0xffffffffu, s, off);
       mn = fminf(mn, __shfl_down_sync(0xffffffffu, mn, off));
       mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, off));
     }
