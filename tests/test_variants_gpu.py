@@ -1,0 +1,120 @@
+"""Parameter variants against the oracle (GPU, both precisions):
+
+* the four LJ forms of realcal.F90 (ljswitch 0-3: CHARMM / GROMACS potential switch,
+  CHARMM / GROMACS force switch, :667-770);
+* reference-solvent mode with a flexible solute (slttype 3: realcal_self for every
+  placement, engproc.F90:716-730) and caller-given solute weights;
+* selfcal = 1 (the eself histogram of the solute self energy, engproc.F90:786-800) with a
+  frame weight stat_weight_system != 1;
+* spline orders 6 and 8 on the plain FP64 path.
+"""
+import numpy as np
+import pytest
+
+from tests import helpers
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp64": (1e-9, 1e-11), "mixed": (1e-4, 2e-6)}
+
+
+def _engines(oracle, params, topo, bins, precision, **kw):
+    from ermod_gb300.engproc import EnergyRepresentation
+    return EnergyRepresentation(params, topo, bins, precision=precision, **kw), oracle.Oracle(params, topo, bins)
+
+
+def _check(ug, uo, precision):
+    atol, rtol = TOL[precision]
+    huge = np.abs(uo) >= 1e10
+    assert np.all(ug[huge] >= 1e10)
+    err = np.abs(ug - uo)[~huge]
+    bound = atol + rtol * np.abs(uo[~huge])
+    assert np.all(err <= bound), f"max err {err.max():.3e}"
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("ljswitch", [0, 1, 2, 3])
+def test_lj_forms(gpu_lib, oracle, ljswitch, precision):
+    w = helpers.small_refs(corrcal=0, wgtslf=0)
+    w.params["ljswitch"] = ljswitch
+    topo, bins = helpers.build_inputs(w)
+    gpu, orc = _engines(oracle, w.params, topo, bins, precision)
+    pos, cell = w.frame(0)
+    pl = w.placements(0, 24)
+    tag = np.full(len(pl), topo["nummol"], np.int32)
+    orc.frame(pos, cell)
+    gpu.frame(pos, cell)
+    ro, rg = orc.placements(tag, pl), gpu.placements(tag, pl, want_uvengy=True)
+    _check(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], precision)
+    gpu.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_flexible_solute_with_weights(gpu_lib, oracle, precision):
+    """slttype 3: each placement's own conformation (sites jittered by 0.05 A), so
+    realcal_self differs per placement; stat_weight_solute per placement."""
+    w = helpers.small_refs(corrcal=1, wgtslf=1)
+    w.params["slttype"] = 3
+    topo, bins = helpers.build_inputs(w)
+    gpu, orc = _engines(oracle, w.params, topo, bins, precision, batch=16)
+    rng = np.random.default_rng(7)
+    for f in range(2):
+        pos, cell = w.frame(f)
+        pl = w.placements(f, 40) + rng.normal(0.0, 0.05, (40, len(w.solute["charge"]), 3))
+        sws = rng.uniform(0.5, 2.0, 40)
+        tag = np.full(len(pl), topo["nummol"], np.int32)
+        orc.frame(pos, cell)
+        gpu.frame(pos, cell)
+        ro = orc.placements(tag, pl, stat_weight_solute=sws)
+        rg = gpu.placements(tag, pl, stat_weight_solute=sws, want_uvengy=True)
+        _check(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], precision)
+        # the self energies differ between placements and match the oracle's
+        assert np.ptp(ro["uvengy"][:, 0]) > 1e-3
+        np.testing.assert_allclose(rg["uvengy"][:, 0], ro["uvengy"][:, 0], atol=1e-9 if precision == "fp64" else 2e-4)
+    ag, ao = gpu.accum(), orc.accum()
+    rtol = 1e-10 if precision == "fp64" else 5e-4
+    for key in ("engnorm", "avslf"):
+        np.testing.assert_allclose(ag[key], ao[key], rtol=rtol)
+    np.testing.assert_allclose(ag["edens"].sum(), ao["edens"].sum(), rtol=rtol)
+    np.testing.assert_allclose(ag["ecorr"].sum(), ao["ecorr"].sum(), rtol=rtol)
+    gpu.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_selfcal_and_frame_weight(gpu_lib, oracle, precision):
+    w = helpers.small_refs(corrcal=0, wgtslf=1)
+    w.params["selfcal"] = 1
+    topo, bins = helpers.build_inputs(w)
+    gpu, orc = _engines(oracle, w.params, topo, bins, precision)
+    pos, cell = w.frame(0)
+    pl = w.placements(0, 32)
+    tag = np.full(len(pl), topo["nummol"], np.int32)
+    orc.frame(pos, cell, stat_weight_system=0.37)
+    gpu.frame(pos, cell, stat_weight_system=0.37)
+    orc.placements(tag, pl)
+    gpu.placements(tag, pl)
+    ag, ao = gpu.accum(), orc.accum()
+    rtol = 1e-10 if precision == "fp64" else 5e-4
+    np.testing.assert_allclose(ag["engnorm"], ao["engnorm"], rtol=rtol)
+    np.testing.assert_allclose(ag["avslf"], ao["avslf"], rtol=1e-12)
+    np.testing.assert_allclose(ag["eself"].sum(), ao["eself"].sum(), rtol=rtol)
+    assert np.count_nonzero(ao["eself"]) > 0
+    if precision == "fp64":
+        np.testing.assert_allclose(ag["eself"], ao["eself"], rtol=1e-10, atol=0)
+    gpu.close()
+
+
+@pytest.mark.parametrize("order", [6, 8])
+def test_fp64_spline_orders(gpu_lib, oracle, order):
+    w = helpers.small_refs(corrcal=0, wgtslf=0)
+    w.params["splodr"] = order
+    topo, bins = helpers.build_inputs(w)
+    gpu, orc = _engines(oracle, w.params, topo, bins, "fp64")
+    pos, cell = w.frame(0)
+    pl = w.placements(0, 6)
+    tag = np.full(len(pl), topo["nummol"], np.int32)
+    orc.frame(pos, cell)
+    gpu.frame(pos, cell)
+    ro, rg = orc.placements(tag, pl), gpu.placements(tag, pl, want_uvengy=True)
+    _check(rg["uvengy"], ro["uvengy"], "fp64")
+    gpu.close()
