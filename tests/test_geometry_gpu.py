@@ -1,0 +1,79 @@
+"""Geometry variants against the oracle (GPU, both precisions):
+
+* an orthorhombic box (24 x 28 x 32 A) with a non-cubic PME grid (30 x 32 x 36): the
+  generic transform kernels, per-axis fixed-point scales and B-spline moduli;
+* solution mode with two solute molecules (sltlist of two entries; one placement per
+  solute molecule, engproc.F90:677-684), each binned against the other as a solvent.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _box_system(lengths, nwater, seed, solutes):
+    """Waters on a jittered orthorhombic lattice plus the given solute molecules (each a
+    dict of synth.random_solute form with a 'centre'); returns species, sitepos, cell."""
+    from ermod_gb300 import insertion, synth
+    rng = np.random.default_rng(seed)
+    L = np.asarray(lengths, np.float64)
+    n = np.ceil(L / 2.8).astype(int)  # ~2.8 A lattice spacing
+    axes = [(np.arange(k) + 0.5) * (l / k) for k, l in zip(n, L)]
+    pts = np.stack(np.meshgrid(*axes, indexing="ij"), -1).reshape(-1, 3)
+    for s in solutes:
+        pts = pts[np.linalg.norm(pts - s["centre"], axis=1) > 5.5]
+    pts = pts[rng.choice(len(pts), nwater, replace=False)]
+    body = synth.water_body() - insertion.center_of_mass(synth.water_body(), synth.WATER_MASS)
+    q = insertion.random_quaternions(rng, nwater)
+    wat = insertion.quat_rotate(q, np.broadcast_to(body, (nwater, 3, 3))) + (pts + rng.uniform(-0.3, 0.3, pts.shape))[:, None]
+    parts = [wat.reshape(-1, 3)]
+    species = [dict(count=nwater, sluvid=0, charge=synth.WATER_CHARGE, eps=synth.WATER_EPS, len=synth.WATER_SIG)]
+    for s in solutes:
+        parts.append(s["xyz"] - insertion.center_of_mass(s["xyz"], s["mass"]) + s["centre"])
+    species.append(dict(count=len(solutes), sluvid=1, charge=solutes[0]["charge"], eps=solutes[0]["eps"],
+                        len=solutes[0]["sig"]))
+    return species, np.ascontiguousarray(np.concatenate(parts)), np.diag(L)
+
+
+def _run(oracle, params, species, pos, cell, nsolute, precision):
+    """One placement for each of the last nsolute molecules (the solutes), in order."""
+    from ermod_gb300 import setconf
+    from ermod_gb300.engproc import EnergyRepresentation
+    topo = setconf.setparam_topology(species, slttype=params["slttype"])
+    bins = setconf.enginit_bins(topo["numslv"])
+    gpu = EnergyRepresentation(params, topo, bins, precision=precision)
+    orc = oracle.Oracle(params, topo, bins)
+    orc.frame(pos, cell)
+    gpu.frame(pos, cell)
+    tag = np.arange(topo["nummol"] - nsolute + 1, topo["nummol"] + 1, dtype=np.int32)
+    ro = orc.placements(tag)
+    rg = gpu.placements(tag, want_uvengy=True)
+    atol, rtol = (1e-9, 1e-11) if precision == "fp64" else (1e-4, 2e-6)
+    err = np.abs(rg["uvengy"] - ro["uvengy"])
+    assert np.all(err <= atol + rtol * np.abs(ro["uvengy"])), err.max()
+    ag, ao = gpu.accum(), orc.accum()
+    np.testing.assert_allclose(ag["edens"].sum(), ao["edens"].sum(), rtol=1e-12)
+    gpu.close()
+    return ro
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_orthorhombic_box_noncubic_grid(gpu_lib, oracle, precision):
+    from ermod_gb300 import synth
+    sol = synth.methanol_like()
+    species, pos, cell = _box_system((24.0, 28.0, 32.0), 600, 41, [dict(sol, centre=np.array([12.0, 14.0, 16.0]))])
+    params = synth._params(1, 32, corrcal=0, wgtslf=0)
+    params.update(ms1max=30, ms2max=32, ms3max=36)
+    _run(oracle, params, species, pos, cell, 1, precision)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_solution_two_solute_molecules(gpu_lib, oracle, precision):
+    from ermod_gb300 import synth
+    sol = synth.methanol_like()
+    centres = [np.array([8.0, 13.0, 13.0]), np.array([18.0, 13.0, 13.0])]
+    species, pos, cell = _box_system((26.0, 26.0, 26.0), 520, 43, [dict(sol, centre=c) for c in centres])
+    params = synth._params(1, 32, corrcal=0, wgtslf=0)
+    ro = _run(oracle, params, species, pos, cell, 2, precision)
+    # each solute sees the other one as a solvent molecule (its slot is not the self slot)
+    assert np.count_nonzero(ro["uvengy"][0, 1:]) == 520 + 1
