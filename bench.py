@@ -46,6 +46,7 @@ def parse_args():
     ap.add_argument("--workload", default="refs_large")
     ap.add_argument("--insertions", type=int, default=None, help="insertions per frame (default: workload's)")
     ap.add_argument("--batch", type=int, default=256, help="placements per PME launch")
+    ap.add_argument("--grid", type=int, default=None, help="PME grid points per axis (default: workload's)")
     ap.add_argument("--cpu-sample", type=int, default=96, help="placements timed on the CPU oracle")
     ap.add_argument("--plain-sample", type=int, default=48, help="placements timed on the plain FP64 GPU path")
     ap.add_argument("--no-cpu", action="store_true")
@@ -129,6 +130,8 @@ def make_workload(args):
     w = synth.WORKLOADS[args.workload]()
     if args.insertions:
         w.ins_per_frame = args.insertions
+    if args.grid:
+        w.params.update(ms1max=args.grid, ms2max=args.grid, ms3max=args.grid)
     return w
 
 
@@ -378,7 +381,7 @@ def run_uneven(args):
         bins = setconf.enginit_bins(topo["numslv"], w.hist)
         f0, f1 = w.frame(0), w.frame(1)
         p0, p1 = w.placements(0), w.placements(1)
-        B = autotune_batch(w.params, topo, bins, f0, p0[:256], topo["nummol"], candidates=(16, 32, 64))
+        B = autotune_batch(w.params, topo, bins, f0, p0[:1024], topo["nummol"], candidates=(32, 64, 128, 256))
         eng = EnergyRepresentation(w.params, topo, bins, precision="mixed", batch=B)
         eng.frame(*f0)
         eng.placements(np.full(len(p0), topo["nummol"], np.int32), p0)

@@ -542,7 +542,7 @@ __global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(Pme
   const int z = blockIdx.y, b = 4 * blockIdx.z + blockIdx.x;
   if (b >= A.nb) return;
   const int K1 = KC ? KC : A.K1, K2 = KC ? KC : A.K2, K3 = KC ? KC : A.K3;
-  const int H = KC ? KC / 2 + 1 : A.H, K1p = KC ? KC + 1 : A.K1p;
+  const int H = KC ? KC / 2 + 1 : A.H, K1p = KC ? (KC | 1) : A.K1p;
   const size_t plane = (size_t)K2 * H;
   const int npair = (K2 + 1) / 2;
   const size_t bufsz = max(plane, (size_t)npair * K1p);
@@ -591,7 +591,7 @@ __global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(Pme
       const float2* r0 = r + (size_t)(2 * pp) * HC;
       const float2* r1 = r0 + HC;
       const bool has1 = 2 * pp + 1 < KC;
-      float2* wrow = w + (size_t)pp * (KC + 1) + lane;
+      float2* wrow = w + (size_t)pp * (KC | 1) + lane;
 #pragma unroll
       for (int i = 0; i < NK; ++i) {
         if (KC % 32 != 0 && lane + 32 * i >= KC) break;
@@ -633,7 +633,8 @@ __global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(Pme
   }
   float2* res;
   if constexpr (KC > 0) {  // in place: w -> r -> w
-    fft2_t<KC, KC / 2, 1, KC + 1, 1, KC + 1, 1, KC + 1, kPmeBThreads>(w, r, w, tw1);
+    // (KC + 1) / 2 row pairs (the last one a single row when KC is odd), rows KC | 1 apart
+    fft2_t<KC, (KC + 1) / 2, 1, (KC | 1), 1, (KC | 1), 1, (KC | 1), kPmeBThreads>(w, r, w, tw1);
     __syncthreads();
     res = w;
   } else {
@@ -664,7 +665,7 @@ __global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(Pme
       // one warp per row pair: one 8-byte load gives rows y = 2p (.x) and 2p + 1 (.y);
       // row y is stored at padded row y + h and, when y >= K2 - h, also at y + h - K2
       for (int pp = warp; pp < npair; pp += nwarp) {
-        const float2* src = res + (size_t)pp * (KC + 1);
+        const float2* src = res + (size_t)pp * (KC | 1);
         float2 v[NX];
 #pragma unroll
         for (int i = 0; i < NX; ++i) v[i] = (ok & (1u << i)) ? src[sx[i]] : make_float2(0.f, 0.f);
@@ -747,18 +748,31 @@ cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a) {
   A.fKX = make_fastdiv(A.K1 + A.halo);
   cudaError_t err;
   // cubic grids of common sizes take the compile-time transforms
+  struct Sized {
+    int K;
+    void (*a)(PmeArgs);
+    void (*b)(PmeArgs);
+  };
+#define ERMOD_PME_SIZE(KK) Sized{KK, pme_a_kernel<KK>, pme_b_kernel<KK>}
+  static const Sized sized[] = {ERMOD_PME_SIZE(32),  ERMOD_PME_SIZE(40),  ERMOD_PME_SIZE(45),  ERMOD_PME_SIZE(48),
+                                ERMOD_PME_SIZE(50),  ERMOD_PME_SIZE(60),  ERMOD_PME_SIZE(64),  ERMOD_PME_SIZE(72),
+                                ERMOD_PME_SIZE(80),  ERMOD_PME_SIZE(90),  ERMOD_PME_SIZE(96),  ERMOD_PME_SIZE(100),
+                                ERMOD_PME_SIZE(108), ERMOD_PME_SIZE(120), ERMOD_PME_SIZE(128), ERMOD_PME_SIZE(144)};
+#undef ERMOD_PME_SIZE
+  constexpr int nsized = (int)(sizeof(sized) / sizeof(sized[0]));
   const bool cubic = A.K1 == A.K2 && A.K2 == A.K3;
-  const int KC = (cubic && (A.K1 == 32 || A.K1 == 48 || A.K1 == 64 || A.K1 == 96 || A.K1 == 128)) ? A.K1 : 0;
-  const size_t sa = pme_a_smem(A.K3, A.Hp), sb = pme_b_smem(A.K1, A.K2, A.H, KC > 0);
+  int slot = 0;  // 0: the generic kernels, 1 + i: sized[i]
   void (*ka)(PmeArgs) = pme_a_kernel<0>;
   void (*kb)(PmeArgs) = pme_b_kernel<0>;
-  if (KC == 32) ka = pme_a_kernel<32>, kb = pme_b_kernel<32>;
-  if (KC == 48) ka = pme_a_kernel<48>, kb = pme_b_kernel<48>;
-  if (KC == 64) ka = pme_a_kernel<64>, kb = pme_b_kernel<64>;
-  if (KC == 96) ka = pme_a_kernel<96>, kb = pme_b_kernel<96>;
-  if (KC == 128) ka = pme_a_kernel<128>, kb = pme_b_kernel<128>;
-  static size_t attr_a[6] = {}, attr_b[6] = {};  // per specialisation: largest size set so far
-  const int slot = KC == 0 ? 0 : (KC == 32 ? 1 : (KC == 48 ? 2 : (KC == 64 ? 3 : (KC == 96 ? 4 : 5))));
+  for (int i = 0; i < nsized && cubic; ++i)
+    if (sized[i].K == A.K1) {
+      slot = 1 + i;
+      ka = sized[i].a;
+      kb = sized[i].b;
+    }
+  const int KC = slot ? A.K1 : 0;
+  const size_t sa = pme_a_smem(A.K3, A.Hp), sb = pme_b_smem(A.K1, A.K2, A.H, KC > 0);
+  static size_t attr_a[1 + nsized] = {}, attr_b[1 + nsized] = {};  // per kernel: largest size set so far
   if (attr_a[slot] < sa) {
     if ((err = cudaFuncSetAttribute(ka, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sa)) != cudaSuccess)
       return err;

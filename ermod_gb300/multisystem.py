@@ -81,7 +81,7 @@ class SystemGraph:
             pass
 
 
-def autotune_batch(params, topo, bins, frame, placements, tag, candidates=(8, 16, 32, 64), device=0):
+def autotune_batch(params, topo, bins, frame, placements, tag, candidates=(32, 64, 128, 256), device=0):
     """The batch size (placements per PME launch) with the highest placements/s on one
     step of this system, timed with CUDA events after a warm-up step."""
     import torch

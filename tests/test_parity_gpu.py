@@ -256,10 +256,11 @@ def test_device_api_status_kept_until_sync(gpu_lib, oracle):
     eng.close()
 
 
-@pytest.mark.parametrize("K,order", [(48, 4), (64, 6), (96, 8), (128, 4)])
+@pytest.mark.parametrize("K,order", [(40, 4), (45, 6), (48, 4), (64, 6), (72, 8), (96, 8), (100, 4), (128, 4),
+                                     (144, 4)])
 def test_compile_time_grid_sizes(gpu_lib, oracle, K, order):
-    """The cubic grids with compile-time transforms (48, 64, 96, 128) against the oracle,
-    with spline orders 4, 6 and 8 (the other grids take the generic kernels)."""
+    """Cubic grids with compile-time transforms (an odd one among them) against the
+    oracle, with spline orders 4, 6 and 8 (other grids take the generic kernels)."""
     w = helpers.small_refs(K=K, corrcal=0, wgtslf=0)
     w.params["splodr"] = order
     topo, bins = helpers.build_inputs(w)
