@@ -382,6 +382,27 @@ __device__ __forceinline__ void fft2_t(const float2* in, float2* mid, float2* ou
   stockham_pass_t<R1, N, R0, NCOLS, ES, CS, OES, OCS, NT>(mid, out, tw);
 }
 
+// lengths without a two-pass plan: make_fft_plan's greedy radices (largest first)
+constexpr int greedy_radix(int n) {
+  return n % 16 == 0 ? 16 : n % 15 == 0 ? 15 : n % 12 == 0 ? 12 : n % 10 == 0 ? 10 : n % 9 == 0 ? 9
+       : n % 8 == 0 ? 8 : n % 6 == 0 ? 6 : n % 5 == 0 ? 5 : n % 4 == 0 ? 4 : n % 3 == 0 ? 3 : n % 2 == 0 ? 2 : 0;
+}
+constexpr bool two_pass(int n) { return first_radix(n) > 0; }
+
+// three passes: in -> mid -> mid2 -> out (mid2 may be the buffer `in` when that is shared
+// memory the first pass has consumed)
+template <int N, int NCOLS, int IES, int ICS, int ES, int CS, int OES, int OCS, int NT>
+__device__ __forceinline__ void fft3_t(const float2* in, float2* mid, float2* mid2, float2* out, const float2* tw) {
+  constexpr int R0 = greedy_radix(N), R1 = greedy_radix(N / R0), R2 = N / (R0 * R1);
+  static_assert(R0 > 0 && R1 > 0 && radix_ok(R2) && R0 * R1 * R2 == N, "no three-pass plan");
+  __syncthreads();
+  stockham_pass_t<R0, N, 1, NCOLS, IES, ICS, ES, CS, NT>(in, mid, tw);
+  __syncthreads();
+  stockham_pass_t<R1, N, R0, NCOLS, ES, CS, ES, CS, NT>(mid, mid2, tw);
+  __syncthreads();
+  stockham_pass_t<R2, N, R0 * R1, NCOLS, ES, CS, OES, OCS, NT>(mid2, out, tw);
+}
+
 struct ff {
   float hi, lo;
 };
@@ -520,7 +541,10 @@ __global__ void __launch_bounds__(kPmeAThreads, kPmeAMinBlocks) pme_a_kernel(Pme
   float2* out = A.t1 + (size_t)b * K3 * A.K2 * H + (size_t)k2 * H;
   if constexpr (KC > 0) {
     constexpr int HC = KC / 2 + 1, HPC = ((HC + kR1 - 1) / kR1) * kR1;
-    fft2_t<KC, HC, HPC, 1, HPC, 1, KC * HC, 1, kPmeAThreads>(slab, work, out, tw3);
+    if constexpr (two_pass(KC))
+      fft2_t<KC, HC, HPC, 1, HPC, 1, KC * HC, 1, kPmeAThreads>(slab, work, out, tw3);
+    else
+      fft3_t<KC, HC, HPC, 1, HPC, 1, KC * HC, 1, kPmeAThreads>(slab, work, slab, out, tw3);
   } else {
     fft_cols_io(slab, Hp, 1, work, slab, A.p3, H, A.fH, Hp, 1, out, A.K2 * H, 1, tw3);
   }
@@ -564,7 +588,10 @@ __global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(Pme
   float2* r = (np2 == 1) ? s0 : ((((np2 - 2) & 1) ? s0 : s1));  // not the last pass's source
   if constexpr (KC > 0) {
     constexpr int HC = KC / 2 + 1;
-    fft2_t<KC, HC, HC, 1, HC, 1, HC, 1, kPmeBThreads>(in, s0, r, tw2);
+    if constexpr (two_pass(KC))
+      fft2_t<KC, HC, HC, 1, HC, 1, HC, 1, kPmeBThreads>(in, s0, r, tw2);
+    else  // r is s0 for three passes (the runtime plan's count)
+      fft3_t<KC, HC, HC, 1, HC, 1, HC, 1, kPmeBThreads>(in, s0, s1, r, tw2);
   } else {
     fft_cols_io(in, H, 1, s0, s1, A.p2, H, A.fH, H, 1, r, H, 1, tw2);
   }
@@ -632,11 +659,16 @@ __global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(Pme
     }
   }
   float2* res;
-  if constexpr (KC > 0) {  // in place: w -> r -> w
+  if constexpr (KC > 0) {  // ping-pong between w and r: w -> r -> w (-> r)
     // (KC + 1) / 2 row pairs (the last one a single row when KC is odd), rows KC | 1 apart
-    fft2_t<KC, (KC + 1) / 2, 1, (KC | 1), 1, (KC | 1), 1, (KC | 1), kPmeBThreads>(w, r, w, tw1);
+    if constexpr (two_pass(KC)) {
+      fft2_t<KC, (KC + 1) / 2, 1, (KC | 1), 1, (KC | 1), 1, (KC | 1), kPmeBThreads>(w, r, w, tw1);
+      res = w;
+    } else {
+      fft3_t<KC, (KC + 1) / 2, 1, (KC | 1), 1, (KC | 1), 1, (KC | 1), kPmeBThreads>(w, r, w, r, tw1);
+      res = r;
+    }
     __syncthreads();
-    res = w;
   } else {
     res = fft_cols(w, r, A.p1, npair, A.fnpair, 1, K1p, tw1);
   }
@@ -757,7 +789,8 @@ cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a) {
   static const Sized sized[] = {ERMOD_PME_SIZE(32),  ERMOD_PME_SIZE(40),  ERMOD_PME_SIZE(45),  ERMOD_PME_SIZE(48),
                                 ERMOD_PME_SIZE(50),  ERMOD_PME_SIZE(60),  ERMOD_PME_SIZE(64),  ERMOD_PME_SIZE(72),
                                 ERMOD_PME_SIZE(80),  ERMOD_PME_SIZE(90),  ERMOD_PME_SIZE(96),  ERMOD_PME_SIZE(100),
-                                ERMOD_PME_SIZE(108), ERMOD_PME_SIZE(120), ERMOD_PME_SIZE(128), ERMOD_PME_SIZE(144)};
+                                ERMOD_PME_SIZE(108), ERMOD_PME_SIZE(120), ERMOD_PME_SIZE(125), ERMOD_PME_SIZE(128),
+                                ERMOD_PME_SIZE(144)};
 #undef ERMOD_PME_SIZE
   constexpr int nsized = (int)(sizeof(sized) / sizeof(sized[0]));
   const bool cubic = A.K1 == A.K2 && A.K2 == A.K3;

@@ -256,7 +256,7 @@ def test_device_api_status_kept_until_sync(gpu_lib, oracle):
     eng.close()
 
 
-@pytest.mark.parametrize("K,order", [(40, 4), (45, 6), (48, 4), (64, 6), (72, 8), (96, 8), (100, 4), (128, 4),
+@pytest.mark.parametrize("K,order", [(40, 4), (45, 6), (48, 4), (64, 6), (72, 8), (96, 8), (100, 4), (125, 6), (128, 4),
                                      (144, 4)])
 def test_compile_time_grid_sizes(gpu_lib, oracle, K, order):
     """Cubic grids with compile-time transforms (an odd one among them) against the
