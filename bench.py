@@ -127,7 +127,10 @@ def load_peaks():
 
 def make_workload(args):
     from ermod_gb300 import synth
-    w = synth.WORKLOADS[args.workload]()
+    if args.workload.startswith("uneven_"):  # one system of the uneven set, alone
+        w = synth.uneven()[int(args.workload.split("_")[1])]
+    else:
+        w = synth.WORKLOADS[args.workload]()
     if args.insertions:
         w.ins_per_frame = args.insertions
     if args.grid:
@@ -161,7 +164,7 @@ def run_reference(args):
     from ermod_gb300 import setconf
     w = make_workload(args)
     topo = setconf.setparam_topology(w.species(), slttype=w.params["slttype"])
-    bins = setconf.enginit_bins(topo["numslv"])
+    bins = setconf.enginit_bins(topo["numslv"], w.hist)
     sample = 1 if w.mode == "soln" else max(1, args.cpu_sample // 4)  # solution mode: the frame's solute
     for i in range(args.warmup):
         cpu_oracle_rate(w, topo, bins, max(1, sample // 4), i)
@@ -202,7 +205,7 @@ def run_ours(args):
     build.build()
     w = make_workload(args)
     topo = setconf.setparam_topology(w.species(), slttype=w.params["slttype"])
-    bins = setconf.enginit_bins(topo["numslv"])
+    bins = setconf.enginit_bins(topo["numslv"], w.hist)
     nplace = w.ins_per_frame
     nsite_u = len(w.solute["charge"])
     nsteps = args.warmup + args.steps
@@ -426,7 +429,7 @@ def run_adjoint(args):
     torch.cuda.set_device(0)
     w = synth.soln_adjoint(frames=args.warmup + args.steps)
     topo = setconf.setparam_topology(w.species(), slttype=1)
-    bins = setconf.enginit_bins(topo["numslv"])
+    bins = setconf.enginit_bins(topo["numslv"], w.hist)
     dev = torch.device("cuda", 0)
     nsteps = args.warmup + args.steps
     pos_d = [torch.from_numpy(w.frame(i)[0]).to(dev) for i in range(nsteps)]
