@@ -55,6 +55,7 @@ struct MolArgs {
   const int* uvkey_f;  // 32-bit keys of the edges rounded down to floats (FP32 totals)
   const int* spec;  // [numslv][3]
   int numslv, ermax, soln, mbin_mode;  // mbin_mode: 0 off, 1 error, 2 flag only
+  int hist_global;  // finish kernel: histogram atomics straight into global memory (large ermax)
   // interaction parameters
   FrameGeom g;
   int ljswitch;
@@ -701,8 +702,10 @@ __global__ void __launch_bounds__(kGatherThreads) gather_tma_kernel(
 template <int G>
 __global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const float* __restrict__ site_e) {
   extern __shared__ int smem_dyn[];
-  int* smem_hist = smem_dyn;                                                  // [G][ermax]
-  int* skeys = smem_dyn + G * A.ermax;  // [ermax] 32-bit edge keys
+  // [G][ermax] block histograms, or none when they would not fit beside other blocks: the
+  // molecules' counts then go to the batch histograms in global memory (warp-aggregated)
+  int* smem_hist = A.hist_global ? nullptr : smem_dyn;
+  int* skeys = smem_dyn + (A.hist_global ? 0 : G * A.ermax);  // [ermax] 32-bit edge keys
   __shared__ float su[G][256];
   __shared__ float squ[G];    // residual factor x solute charge of the G placements
   __shared__ float srcut[G];  // bounding-sphere cutoff of the real-space sum
@@ -715,7 +718,8 @@ __global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const flo
   const int ng = min(G, a.nb - g0);
   const int m = tile * blockDim.x + threadIdx.x;
   const bool valid = m < A.slvmax;
-  for (int i = threadIdx.x; i < G * A.ermax; i += blockDim.x) smem_hist[i] = 0;
+  if (!A.hist_global)
+    for (int i = threadIdx.x; i < G * A.ermax; i += blockDim.x) smem_hist[i] = 0;
   for (int i = threadIdx.x; i < A.ermax; i += blockDim.x) skeys[i] = A.uvkey_f[i];
   if (threadIdx.x < ng) {
     const int b = g0 + threadIdx.x;
@@ -841,7 +845,7 @@ __global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const flo
       if (code)
         atomicMin(&A.status->err_key, make_err_key(a.b0 + g0 + j, k + 1, code));
       else
-        hist_add(smem_hist + j * A.ermax, sp_off + ret - 1);
+        hist_add(A.hist_global ? a.hist + (size_t)(g0 + j) * A.ermax : smem_hist + j * A.ermax, sp_off + ret - 1);
       u = v;
     }
     su[j][threadIdx.x] = u;
@@ -877,6 +881,7 @@ __global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const flo
       pt[2] = (double)mx;
     }
   }
+  if (A.hist_global) return;
   for (int j = 0; j < ng; ++j) {
     const int* h = smem_hist + j * A.ermax;
     int* out = a.hist + (size_t)(g0 + j) * A.ermax;
@@ -939,6 +944,9 @@ static MolArgs make_mol_args(Engine& e, const BatchArgs& a) {
   A.ldb = e.Bmax;
   A.uvkey = e.d_uvkey;
   A.uvkey_f = e.d_uvkey_f;
+  // finish kernel: block histograms in shared memory up to 64 KB (three blocks per SM
+  // fit); beyond that the counts go straight to global memory
+  A.hist_global = (size_t)a.G * e.ermax * sizeof(int) > 64 * 1024 ? 1 : 0;
   A.spec = e.d_spec;
   A.numslv = e.numslv;
   A.ermax = e.ermax;
@@ -1015,7 +1023,7 @@ cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
     e.phase_begin_on(PH_MOL, a.stream);
   }
   // step 2: per-molecule totals and binning (histograms + edge keys in shared memory)
-  const size_t smem_f = sizeof(int) * ((size_t)a.G * e.ermax + e.ermax);
+  const size_t smem_f = sizeof(int) * ((A.hist_global ? 0 : (size_t)a.G * e.ermax) + e.ermax);
   dim3 g2((a.nb + a.G - 1) / a.G, e.ntile);
 #define ERMOD_FINISH(GG)                                                                                   \
   if (a.G == GG) {                                                                                         \

@@ -6,7 +6,8 @@
   placement, engproc.F90:716-730) and caller-given solute weights;
 * selfcal = 1 (the eself histogram of the solute self energy, engproc.F90:786-800) with a
   frame weight stat_weight_system != 1;
-* spline orders 6 and 8 on the plain FP64 path.
+* spline orders 6 and 8 on the plain FP64 path;
+* an energy coordinate of about 5,000 bins (first edge -200 kcal/mol).
 """
 import numpy as np
 import pytest
@@ -117,4 +118,36 @@ def test_fp64_spline_orders(gpu_lib, oracle, order):
     gpu.frame(pos, cell)
     ro, rg = orc.placements(tag, pl), gpu.placements(tag, pl, want_uvengy=True)
     _check(rg["uvengy"], ro["uvengy"], "fp64")
+    gpu.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_large_energy_coordinate(gpu_lib, oracle, precision):
+    """A first edge at -200 kcal/mol (about 5,000 bins): the finish kernel then counts
+    straight into global memory instead of shared-memory block histograms.  Unit weights,
+    so edens and the int64 ecorr counts are exact off the bin edges."""
+    from ermod_gb300 import setconf
+    w = helpers.small_refs(corrcal=1, wgtslf=0)
+    w.params["estype"] = 1
+    hist = dict(setconf.HIST_DEFAULT, ecdmin=-200.0)
+    topo, bins = helpers.build_inputs(w, hist)
+    assert len(bins["uvcrd"]) > 4000  # G x ermax x 4 B > 64 KB: global-memory counts
+    gpu, orc = _engines(oracle, w.params, topo, bins, precision, count_mirror=True)
+    pos, cell = w.frame(0)
+    pl = w.placements(0, 48)
+    tag = np.full(len(pl), topo["nummol"], np.int32)
+    orc.frame(pos, cell)
+    gpu.frame(pos, cell)
+    ro, rg = orc.placements(tag, pl), gpu.placements(tag, pl, want_uvengy=True)
+    ug, uo = rg["uvengy"][:, 1:], ro["uvengy"][:, 1:]
+    _check(ug, uo, precision)
+    # the device's own bins of its own energies (unit weights: edens = summed counts)
+    edges = np.asarray(bins["uvcrd"])
+    model = sum(helpers.histogram(u, edges) for u in ug).astype(np.float64)
+    ag, ao = gpu.accum(with_count=True), orc.accum()
+    np.testing.assert_array_equal(ag["edens"], model)
+    np.testing.assert_allclose(ag["edens"].sum(), ao["edens"].sum(), rtol=1e-12)
+    # the int64 count mirror is the exact sum of count products
+    h = np.stack([helpers.histogram(u, edges) for u in ug]).astype(np.int64)
+    np.testing.assert_array_equal(ag["ecorr_count"], h.T @ h)
     gpu.close()
