@@ -20,6 +20,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 namespace ermod {
 
 constexpr int kMaxSoluteSites = 256;  // sites of one solute molecule
@@ -66,6 +68,29 @@ __host__ __device__ inline long long ordered_key(double x) {
 #endif
   return k ^ ((k >> 63) & 0x7fffffffffffffffll);
 }
+
+// The dynamic shared memory a kernel may use, raised with cudaFuncSetAttribute when a
+// launch needs more than before.  The attribute belongs to the device current at the call,
+// so the largest size set so far is kept per device (contexts of one process may sit on
+// several devices and several host threads).
+struct SmemAttr {
+  static constexpr int kMaxDevices = 64;
+  std::atomic<size_t> set[kMaxDevices];
+  template <typename F>
+  cudaError_t ensure(F* f, size_t bytes) {
+    int dev = 0;
+    cudaError_t err = cudaGetDevice(&dev);
+    if (err != cudaSuccess) return err;
+    const bool cached = dev >= 0 && dev < kMaxDevices;
+    size_t cur = cached ? set[dev].load() : 0;
+    if (cached && cur >= bytes) return cudaSuccess;
+    err = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (err == cudaSuccess && cached)
+      while (cur < bytes && !set[dev].compare_exchange_weak(cur, bytes)) {
+      }
+    return err;
+  }
+};
 
 // bricks of the mixed path's gather: kBrickX x kBrickY x kBrickZ PME grid points
 constexpr int kBrickX = 16, kBrickY = 8, kBrickZ = 8;

@@ -805,17 +805,9 @@ cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a) {
     }
   const int KC = slot ? A.K1 : 0;
   const size_t sa = pme_a_smem(A.K3, A.Hp), sb = pme_b_smem(A.K1, A.K2, A.H, KC > 0);
-  static size_t attr_a[1 + nsized] = {}, attr_b[1 + nsized] = {};  // per kernel: largest size set so far
-  if (attr_a[slot] < sa) {
-    if ((err = cudaFuncSetAttribute(ka, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sa)) != cudaSuccess)
-      return err;
-    attr_a[slot] = sa;
-  }
-  if (attr_b[slot] < sb) {
-    if ((err = cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb)) != cudaSuccess)
-      return err;
-    attr_b[slot] = sb;
-  }
+  static SmemAttr attr_a[1 + nsized], attr_b[1 + nsized];  // per kernel
+  if ((err = attr_a[slot].ensure(ka, sa)) != cudaSuccess) return err;
+  if ((err = attr_b[slot].ensure(kb, sb)) != cudaSuccess) return err;
   ka<<<dim3(A.K2, a.nb), kPmeAThreads, sa, a.stream>>>(A);
   e.count_launch();
   if ((err = cudaGetLastError()) != cudaSuccess) return err;

@@ -909,15 +909,6 @@ cudaError_t launch_p(Engine& e, const MolArgs& A, dim3 grid, size_t smem) {
   return cudaGetLastError();
 }
 
-cudaError_t set_smem_attr(size_t smem) {
-  cudaError_t err = cudaSuccess;
-  err = cudaFuncSetAttribute(mol_energy_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (err != cudaSuccess) return err;
-  err = cudaFuncSetAttribute(mol_energy_kernel<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (err != cudaSuccess) return err;
-  return cudaFuncSetAttribute(mol_energy_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-}
-
 }  // namespace
 
 static MolArgs make_mol_args(Engine& e, const BatchArgs& a) {
@@ -984,12 +975,8 @@ cudaError_t launch_gather(Engine& e, const BatchArgs& a) {
   const size_t sh = 128 + kGatherStages * hstride * sizeof(float4);
 #define ERMOD_GATHER(PP)                                                                                        \
   if (e.P_order == PP) {                                                                                        \
-    static size_t attr = 0;                                                                                     \
-    if (attr < sh) {                                                                                            \
-      err = cudaFuncSetAttribute(gather_tma_kernel<PP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);  \
-      if (err != cudaSuccess) return err;                                                                       \
-      attr = sh;                                                                                                \
-    }                                                                                                           \
+    static SmemAttr attr;                                                                                       \
+    if ((err = attr.ensure(gather_tma_kernel<PP>, sh)) != cudaSuccess) return err;                              \
     gather_tma_kernel<PP><<<g1, kGatherThreads, sh, a.stream>>>(                                                \
         e.phi_tmap[a.slot], a.nb, gpc, e.d_site_rec, e.d_site_grid, e.d_brick_site, e.d_brick_start, K1, K2, K3,  \
         e.nbrick[0], e.nbrick[1], e.gbox[0], e.Bmax, a.site_e, e.d_status);                                     \
@@ -1009,11 +996,11 @@ cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
   e.count_launch();
   cudaError_t err = cudaSuccess;
   if (!e.mixed) {
-    static size_t attr = 0;
-    if (attr < smem) {
-      if ((err = set_smem_attr(smem)) != cudaSuccess) return err;
-      attr = smem;
-    }
+    static SmemAttr attr4, attr6, attr8;
+    if ((err = attr4.ensure(mol_energy_kernel<4>, smem)) != cudaSuccess ||
+        (err = attr6.ensure(mol_energy_kernel<6>, smem)) != cudaSuccess ||
+        (err = attr8.ensure(mol_energy_kernel<8>, smem)) != cudaSuccess)
+      return err;
     return launch_p(e, A, grid, smem);
   }
   if (a.G != 8 && a.G != 4) return cudaErrorInvalidValue;
@@ -1027,12 +1014,8 @@ cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
   dim3 g2((a.nb + a.G - 1) / a.G, e.ntile);
 #define ERMOD_FINISH(GG)                                                                                   \
   if (a.G == GG) {                                                                                         \
-    static size_t attr = 0;                                                                                \
-    if (attr < smem_f) {                                                                                   \
-      err = cudaFuncSetAttribute(mol_finish_kernel<GG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_f); \
-      if (err != cudaSuccess) return err;                                                                  \
-      attr = smem_f;                                                                                       \
-    }                                                                                                      \
+    static SmemAttr attr;                                                                                  \
+    if ((err = attr.ensure(mol_finish_kernel<GG>, smem_f)) != cudaSuccess) return err;                     \
     mol_finish_kernel<GG><<<g2, 256, smem_f, a.stream>>>(A, a.site_e);                                   \
   }
   ERMOD_FINISH(4)
