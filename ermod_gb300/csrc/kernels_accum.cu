@@ -442,7 +442,7 @@ __global__ void __launch_bounds__(256) ecorr_rows_kernel(const int* __restrict__
 // the pairs are added to the FP64 matrix once per flush.  The row coefficients
 // hist[p][row0 + r] of every placement are staged in shared memory with a bit mask of
 // the nonzero ones.
-constexpr int kEcRows = 16;
+constexpr int kEcRows = 8;
 
 __device__ __forceinline__ void ff_add_prod(float& hi, float& lo, float wh, float wl, float c) {
   const float p = wh * c;
@@ -496,7 +496,7 @@ __global__ void __launch_bounds__(256, 2) ecorr_ff_kernel(const int* __restrict_
     if (COUNT) cn[r] = 0;
   }
   bool any = false;
-  constexpr int U = 8;  // loads in flight per thread
+  constexpr int U = 4;  // loads in flight per thread
   for (int p0 = 0; p0 < nring; p0 += U) {
     int cj[U];
 #pragma unroll
