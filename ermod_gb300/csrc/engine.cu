@@ -276,7 +276,9 @@ static int ensure_batch(Engine& e) {
     e.phi_dims[0] = ((e.geom.K[0] + h + 3) / 4) * 4;
     e.phi_dims[1] = e.geom.K[1] + h;
     e.phi_dims[2] = e.geom.K[2] + h;
-    e.gbox[0] = ((kBrickX + h + 3) / 4) * 4;
+    // gather halo box: the brick plus the stencil reach below it, no wider (every element
+    // is a 16-byte float4, so any x extent is a legal TMA box)
+    e.gbox[0] = kBrickX + h;
     e.gbox[1] = kBrickY + h;
     e.gbox[2] = kBrickZ + h;
     const size_t np = (size_t)e.phi_dims[0] * e.phi_dims[1] * e.phi_dims[2];

@@ -371,6 +371,30 @@ __device__ __forceinline__ void stockham_pass_t(const float2* __restrict__ A, fl
   }
 }
 
+// the same pass with caller-supplied element access: ld(col, e) returns element e of
+// transform col, st(col, e, v) stores output element e
+template <int R, int N, int NS, int NCOLS, int NT, class Ld, class St>
+__device__ __forceinline__ void stockham_pass_f(Ld ld, St st, const float2* __restrict__ tw) {
+  constexpr int NR = N / R, TOTAL = NCOLS * NR, STEP = N / (NS * R);
+  for (int t = threadIdx.x; t < TOTAL; t += NT) {
+    const int j = t / NCOLS;
+    const int col = t - j * NCOLS;
+    const int jq = j / NS;
+    const int k = j - jq * NS;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = ld(col, j + r * NR);
+    if (NS > 1 && k > 0) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[r * k * STEP]);
+    }
+    Dft<R>::run(v);
+    const int idxD = jq * NS * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) st(col, idxD + r * NS, v[r]);
+  }
+}
+
 // two passes: in (IES, ICS) -> mid (ES, CS) -> out (OES, OCS); each pass starts with a barrier
 template <int N, int NCOLS, int IES, int ICS, int ES, int CS, int OES, int OCS, int NT>
 __device__ __forceinline__ void fft2_t(const float2* in, float2* mid, float2* out, const float2* tw) {
@@ -555,33 +579,50 @@ __global__ void __launch_bounds__(kPmeAThreads, kPmeAMinBlocks) pme_a_kernel(Pme
   }
 }
 
-// CTA per (z, placement): the k2 transform of the (k2, k1) plane, then the
-// complex-to-real transform along k1, two rows per complex transform; writes the real
-// plane phi[b][z][y][x] with coalesced row stores.
+// pme_b_planes for cubic two-pass grids with K a multiple of 4 (H odd): the k2 transform
+// leaves rows 2p and 2p + 1 interleaved point by point ([p][k1][2], pairs 2H apart), and
+// the first pass of the row transforms packs the pairs while it loads them (one 16-byte
+// load per point, conflict free as H is odd), so there is no separate packing pass.
 template <int KC>
-__global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(PmeArgs A) {
-  extern __shared__ float2 sm[];
-  // grid (4, K3, ceil(nb / 4)): the four placements that share an interleaved potential
-  // grid run side by side, so their 4-byte stores meet in L2
-  const int z = blockIdx.y, b = 4 * blockIdx.z + blockIdx.x;
-  if (b >= A.nb) return;
-  const int K1 = KC ? KC : A.K1, K2 = KC ? KC : A.K2, K3 = KC ? KC : A.K3;
+__device__ __forceinline__ float2* pme_b_planes_fused(const float2* in, float2* s0, float2* s1, const float2* tw) {
+  constexpr int HC = KC / 2 + 1, R0 = first_radix(KC), R1 = KC / R0, SP = 2 * HC, RS = KC | 1;
+  __syncthreads();
+  stockham_pass_t<R0, KC, 1, HC, HC, 1, HC, 1, kPmeBThreads>(in, s0, tw);
+  __syncthreads();
+  stockham_pass_f<R1, KC, R0, HC, kPmeBThreads>(
+      [&](int c, int e) { return s0[c + e * HC]; },
+      [&](int c, int e, float2 v) { s1[(e >> 1) * SP + 2 * c + (e & 1)] = v; }, tw);
+  __syncthreads();
+  stockham_pass_f<R0, KC, 1, KC / 2, kPmeBThreads>(
+      [&](int p, int k) {
+        const int kk = k < HC ? k : KC - k;
+        const float4 v = *reinterpret_cast<const float4*>(s1 + p * SP + 2 * kk);
+        float2 x0 = make_float2(v.x, v.y), x1 = make_float2(v.z, v.w);
+        if (k >= HC) {  // upper half of k1: the conjugate of the stored half
+          x0.y = -x0.y;
+          x1.y = -x1.y;
+        }
+        if (k == 0 || k == KC / 2) {  // self-conjugate points
+          x0.y = 0.f;
+          x1.y = 0.f;
+        }
+        return make_float2(x0.x - x1.y, x0.y + x1.x);
+      },
+      [&](int p, int k, float2 v) { s0[p * RS + k] = v; }, tw);
+  __syncthreads();
+  stockham_pass_t<R1, KC, R0, KC / 2, 1, RS, 1, RS, kPmeBThreads>(s0, s1, tw);
+  __syncthreads();
+  return s1;
+}
+
+// the plane's k2 transforms, a separate pass that packs row pairs (Hermitian-completed in
+// k1) into rows K1p apart, and the row transforms; returns the buffer holding the result
+template <int KC>
+__device__ __forceinline__ float2* pme_b_planes(const PmeArgs& A, const float2* in, float2* s0, float2* s1,
+                                                const float2* tw1, const float2* tw2) {
+  const int K1 = KC ? KC : A.K1, K2 = KC ? KC : A.K2;
   const int H = KC ? KC / 2 + 1 : A.H, K1p = KC ? (KC | 1) : A.K1p;
-  const size_t plane = (size_t)K2 * H;
   const int npair = (K2 + 1) / 2;
-  const size_t bufsz = max(plane, (size_t)npair * K1p);
-  float2* s0 = sm;
-  float2* s1 = sm + bufsz;
-  float2* tw1 = s1 + bufsz;
-  float2* tw2 = KC ? tw1 : tw1 + K1;  // one table for a cubic grid (K1 = K2)
-  for (int i = threadIdx.x; i < (KC ? K1 : K1 + K2); i += blockDim.x) {
-    const float2 t = A.twiddle[i];
-    if (i < K1)
-      tw1[i] = make_float2(t.x, -t.y);
-    else
-      tw2[i - K1] = make_float2(t.x, -t.y);
-  }
-  const float2* in = A.t1 + ((size_t)b * K3 + z) * plane;
   // k2 transform: columns k1 (stride 1), elements along k2 (stride H); the first pass
   // reads the plane from global memory
   const int np2 = A.p2.npass;
@@ -672,10 +713,48 @@ __global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(Pme
   } else {
     res = fft_cols(w, r, A.p1, npair, A.fnpair, 1, K1p, tw1);
   }
+  return res;
+}
+
+// CTA per (z, placement): the k2 transform of the (k2, k1) plane, then the
+// complex-to-real transform along k1, two rows per complex transform; writes the real
+// plane phi[b][z][y][x] with coalesced row stores.
+template <int KC>
+__global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(PmeArgs A) {
+  extern __shared__ __align__(16) float2 sm[];  // 16-byte loads of row pairs
+  // grid (4, K3, ceil(nb / 4)): the four placements that share an interleaved potential
+  // grid run side by side, so their 4-byte stores meet in L2
+  const int z = blockIdx.y, b = 4 * blockIdx.z + blockIdx.x;
+  if (b >= A.nb) return;
+  const int K1 = KC ? KC : A.K1, K2 = KC ? KC : A.K2, K3 = KC ? KC : A.K3;
+  const int H = KC ? KC / 2 + 1 : A.H, K1p = KC ? (KC | 1) : A.K1p;
+  const size_t plane = (size_t)K2 * H;
+  const int npair = (K2 + 1) / 2;
+  const size_t bufsz = max(plane, (size_t)npair * K1p);
+  float2* s0 = sm;
+  float2* s1 = sm + bufsz;
+  float2* tw1 = s1 + bufsz;
+  float2* tw2 = KC ? tw1 : tw1 + K1;  // one table for a cubic grid (K1 = K2)
+  for (int i = threadIdx.x; i < (KC ? K1 : K1 + K2); i += blockDim.x) {
+    const float2 t = A.twiddle[i];
+    if (i < K1)
+      tw1[i] = make_float2(t.x, -t.y);
+    else
+      tw2[i - K1] = make_float2(t.x, -t.y);
+  }
+  const float2* in = A.t1 + ((size_t)b * K3 + z) * plane;
+  // k2 transforms, row-pair packing and the complex-to-real row transforms; res holds
+  // the real rows, pair p (rows 2p, 2p + 1 interleaved) K1p apart
+  float2* res;
+  if constexpr (KC > 0 && two_pass(KC) && KC % 4 == 0)
+    res = pme_b_planes_fused<KC>(in, s0, s1, tw1);
+  else
+    res = pme_b_planes<KC>(A, in, s0, s1, tw1, tw2);
   // padded periodic layout: grid point (x, y, z) lives at (x+h, y+h, z+h), h = P-1, and
   // the last h points of every axis are repeated below 0, so any stencil halo of the
   // gather is one in-bounds box (rows XP floats, planes YP rows, ZP planes)
   const int h = A.halo;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
   // potential grids of 4 placements interleaved: phi[b/4][zp][yp][xp][b%4]
   float* out = A.phi + (size_t)(b >> 2) * A.ZP * A.YP * A.XP * 4 + (b & 3);
   const int KX = K1 + h, KY = K2 + h;  // written extent of a padded plane
