@@ -492,7 +492,8 @@ int ermod_create(const ermod_params* p_in, int device, ermod_ctx** out) {
   }
   if ((err = dalloc(&e.d_splfc, splfc.size())) != cudaSuccess || (err = dalloc(&e.d_twiddle, tw.size())) != cudaSuccess ||
       (err = dalloc(&e.d_engfac, e.grid_cplx())) != cudaSuccess ||
-      (err = dalloc(&e.d_engfac_f, e.grid_cplx())) != cudaSuccess) {
+      (err = dalloc(&e.d_engfac_f, (size_t)e.Hp4() * e.geom.K[1] * e.geom.K[2])) != cudaSuccess ||
+      (err = cudaMemset(e.d_engfac_f, 0, sizeof(float) * e.Hp4() * e.geom.K[1] * e.geom.K[2])) != cudaSuccess) {
     ermod_destroy(c);
     return fail_cuda(err, "PME tables");
   }

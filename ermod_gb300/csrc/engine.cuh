@@ -181,6 +181,8 @@ struct Engine {
   int H() const { return geom.K[0] / 2 + 1; }
   size_t grid_real() const { return (size_t)geom.K[0] * geom.K[1] * geom.K[2]; }
   size_t grid_cplx() const { return (size_t)H() * geom.K[1] * geom.K[2]; }
+  // FP32 engfac rows padded to a multiple of 4 points (16-byte loads in pme_a)
+  int Hp4() const { return ((H() + 3) / 4) * 4; }
   int Kmax() const { return std::max(geom.K[0], std::max(geom.K[1], geom.K[2])); }
 
   // second stream: the ordered accumulation of batch i overlaps batch i+1's kernels;

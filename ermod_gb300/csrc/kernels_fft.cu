@@ -6,8 +6,9 @@
 //             S(k1, k3) = engfac(k1,k2,k3) sum_s q_s b1_s(k1) b2_s(k2) b3_s(k3)
 //           (the exact R2C transform of the spread solute charges; b_{s,a} are the
 //           1-D structure factors of the B-spline stencils), reduces the self energy
-//           0.5 sum_k engfac |S|^2 (recpcal.F90:385-394) with float-float compensation,
-//           and transforms the slab along k3 (inverse, unnormalised) in shared memory.
+//           0.5 sum_k engfac |S|^2 (recpcal.F90:385-394; FP32 within a thread's tile,
+//           float-float across tiles), and transforms the slab along k3 (inverse,
+//           unnormalised) in shared memory.
 //           Output T1[b][z][k2][k1] (complex FP32).
 //   pme_b   CTA per (z, placement): the k2 transform of the (k2, k1) plane, then the
 //           complex-to-real transform along k1, two rows per complex transform
@@ -442,12 +443,13 @@ __device__ __forceinline__ ff ff_add2(ff a, ff b) { return ff_add(ff_add(a, b.hi
 
 constexpr int kSites = 32;  // solute sites staged per chunk
 constexpr int kR1 = 4, kR3 = 3;  // generation tile: kR3 k3 values x kR1 k1 values per thread
+static_assert(kR1 == 4, "pme_a reads a tile row's engfac values as one float4");
 
 struct PmeArgs {
   const float2* bvec;   // [nb][S][3][Kmax]
   const float* u_qf;    // [nb][S]
   const int* u_nsite;
-  const float* engfac;  // [K3][K2][H]
+  const float* engfac;  // [K3][K2][Hp], zeros beyond H
   const float2* twiddle;  // per axis, exp(-2 pi i m / K): conjugated here for the inverse
   float2* t1;           // [nb][K3][K2][H]
   float* phi;           // [nb][K3][K2][K1]
@@ -525,6 +527,7 @@ __global__ void __launch_bounds__(kPmeAThreads, kPmeAMinBlocks) pme_a_kernel(Pme
             acc[j][i].y = fmaf(d[j].x, e[i].y, fmaf(d[j].y, e[i].x, acc[j][i].y));
           }
       }
+      float tile_self = 0.f;  // the tile's self-energy terms (all >= 0), summed in FP32
 #pragma unroll
       for (int j = 0; j < kR3; ++j) {
         const int k3 = k3a + j;
@@ -537,21 +540,23 @@ __global__ void __launch_bounds__(kPmeAThreads, kPmeAMinBlocks) pme_a_kernel(Pme
           acc[j][2] = cadd(acc[j][2], make_float2(o1.x, o1.y));
           acc[j][3] = cadd(acc[j][3], make_float2(o1.z, o1.w));
         }
-        if (last) {
-          const float* ef = A.engfac + ((size_t)k3 * A.K2 + k2) * H;
+        if (last) {  // FP32 engfac rows are Hp points long, zeros beyond H
+          const float4 f4 = __ldg(reinterpret_cast<const float4*>(A.engfac + ((size_t)k3 * A.K2 + k2) * Hp + k1a));
+          const float fv[kR1] = {f4.x, f4.y, f4.z, f4.w};
 #pragma unroll
           for (int i = 0; i < kR1; ++i) {
             const int k1 = k1a + i;
-            const float f = (k1 < H) ? __ldg(ef + k1) : 0.f;
+            const float f = fv[i];
             const float2 q = acc[j][i];
             const float wgt = (k1 == 0 || (even && k1 == H - 1)) ? 0.5f : 1.f;
-            self = ff_add(self, wgt * f * (q.x * q.x + q.y * q.y));
+            tile_self += wgt * f * (q.x * q.x + q.y * q.y);
             acc[j][i] = make_float2(f * q.x, f * q.y);
           }
         }
         dst[0] = make_float4(acc[j][0].x, acc[j][0].y, acc[j][1].x, acc[j][1].y);
         dst[1] = make_float4(acc[j][2].x, acc[j][2].y, acc[j][3].x, acc[j][3].y);
       }
+      if (last) self = ff_add(self, tile_self);
     }
   }
   for (int off = 16; off > 0; off >>= 1) {

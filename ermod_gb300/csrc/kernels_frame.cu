@@ -240,6 +240,11 @@ __global__ void brick_key_kernel(const int* __restrict__ site_grid, int nsite, i
   atomicAdd(&count[bk], 1);
 }
 
+// the FP32 copy of engfac keeps rows of H points padded to a multiple of 4 (zeros)
+__device__ __forceinline__ size_t padded_row_index(size_t i, int H) {
+  return (i / H) * (size_t)(((H + 3) / 4) * 4) + i % H;
+}
+
 // recpcal_spline_greenfunc (recpcal.F90:111-152)
 __global__ void greenfunc_kernel(FrameGeom g, int order, const double* __restrict__ splfc, double screen,
                                  double* __restrict__ engfac, float* __restrict__ engfac_f) {
@@ -272,7 +277,7 @@ __global__ void greenfunc_kernel(FrameGeom g, int order, const double* __restric
     }
   }
   engfac[i] = factor;
-  engfac_f[i] = (float)factor;
+  engfac_f[padded_row_index(i, H)] = (float)factor;
 }
 
 // recpcal_pppm_greenfunc (recpcal.F90:205-319): the optimal influence function of PPPM,
@@ -343,7 +348,7 @@ __global__ void pppm_greenfunc_kernel(PppmArgs A, double* __restrict__ engfac, f
     }
   }
   engfac[i] = factor;
-  engfac_f[i] = (float)factor;
+  engfac_f[padded_row_index(i, H)] = (float)factor;
 }
 
 inline int nblk(size_t n, int t) { return (int)((n + t - 1) / t); }
