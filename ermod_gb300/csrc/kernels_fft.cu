@@ -372,30 +372,6 @@ __device__ __forceinline__ void stockham_pass_t(const float2* __restrict__ A, fl
   }
 }
 
-// the same pass with caller-supplied element access: ld(col, e) returns element e of
-// transform col, st(col, e, v) stores output element e
-template <int R, int N, int NS, int NCOLS, int NT, class Ld, class St>
-__device__ __forceinline__ void stockham_pass_f(Ld ld, St st, const float2* __restrict__ tw) {
-  constexpr int NR = N / R, TOTAL = NCOLS * NR, STEP = N / (NS * R);
-  for (int t = threadIdx.x; t < TOTAL; t += NT) {
-    const int j = t / NCOLS;
-    const int col = t - j * NCOLS;
-    const int jq = j / NS;
-    const int k = j - jq * NS;
-    float2 v[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = ld(col, j + r * NR);
-    if (NS > 1 && k > 0) {
-#pragma unroll
-      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[r * k * STEP]);
-    }
-    Dft<R>::run(v);
-    const int idxD = jq * NS * R + k;
-#pragma unroll
-    for (int r = 0; r < R; ++r) st(col, idxD + r * NS, v[r]);
-  }
-}
-
 // two passes: in (IES, ICS) -> mid (ES, CS) -> out (OES, OCS); each pass starts with a barrier
 template <int N, int NCOLS, int IES, int ICS, int ES, int CS, int OES, int OCS, int NT>
 __device__ __forceinline__ void fft2_t(const float2* in, float2* mid, float2* out, const float2* tw) {
@@ -584,36 +560,77 @@ __global__ void __launch_bounds__(kPmeAThreads, kPmeAMinBlocks) pme_a_kernel(Pme
   }
 }
 
+// The two passes around the row-pair layout of pme_b_planes_fused.  pass_to_pairs: the
+// second k2 pass (radix R1 = K / R0, NS = R0, columns k1) storing element (k2, k1) at
+// [k2 / 2][k1][k2 % 2], pairs 2H apart.
+template <int KC>
+__device__ __forceinline__ void pass_to_pairs(const float2* __restrict__ A, float2* __restrict__ B,
+                                              const float2* __restrict__ tw) {
+  constexpr int HC = KC / 2 + 1, R0 = first_radix(KC), R = KC / R0, NR = KC / R, SP = 2 * HC;
+  for (int t = threadIdx.x; t < HC * NR; t += kPmeBThreads) {
+    const int j = t / HC;  // < NR = R0 = NS, so the pass's k is j
+    const int col = t - j * HC;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = A[col + (j + r * NR) * HC];
+    if (j > 0) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[r * j]);
+    }
+    Dft<R>::run(v);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int e = j + r * R0;
+      B[(e >> 1) * SP + 2 * col + (e & 1)] = v[r];
+    }
+  }
+}
+
+// pass_from_pairs: the first row pass (radix R0, no twiddles, K / 2 row pairs) packing
+// Z_p[k] = X_{2p}[k] + i X_{2p+1}[k] while it loads, Hermitian-completed in k1 (the upper
+// half of k1 is the conjugate of the stored half); rows K | 1 apart in B
+template <int KC>
+__device__ __forceinline__ void pass_from_pairs(const float2* __restrict__ A, float2* __restrict__ B) {
+  constexpr int HC = KC / 2 + 1, R = first_radix(KC), NR = KC / R, NP = KC / 2, SP = 2 * HC, RS = KC | 1;
+  for (int t = threadIdx.x; t < NP * NR; t += kPmeBThreads) {
+    const int j = t / NP;
+    const int p = t - j * NP;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int k = j + r * NR;
+      const int kk = k < HC ? k : KC - k;
+      const float4 q = *reinterpret_cast<const float4*>(A + p * SP + 2 * kk);
+      float2 x0 = make_float2(q.x, q.y), x1 = make_float2(q.z, q.w);
+      if (k >= HC) {
+        x0.y = -x0.y;
+        x1.y = -x1.y;
+      }
+      if (k == 0 || k == KC / 2) {  // self-conjugate points
+        x0.y = 0.f;
+        x1.y = 0.f;
+      }
+      v[r] = make_float2(x0.x - x1.y, x0.y + x1.x);
+    }
+    Dft<R>::run(v);
+#pragma unroll
+    for (int r = 0; r < R; ++r) B[p * RS + j * R + r] = v[r];
+  }
+}
+
 // pme_b_planes for cubic two-pass grids with K a multiple of 4 (H odd): the k2 transform
 // leaves rows 2p and 2p + 1 interleaved point by point ([p][k1][2], pairs 2H apart), and
 // the first pass of the row transforms packs the pairs while it loads them (one 16-byte
 // load per point, conflict free as H is odd), so there is no separate packing pass.
 template <int KC>
 __device__ __forceinline__ float2* pme_b_planes_fused(const float2* in, float2* s0, float2* s1, const float2* tw) {
-  constexpr int HC = KC / 2 + 1, R0 = first_radix(KC), R1 = KC / R0, SP = 2 * HC, RS = KC | 1;
+  constexpr int HC = KC / 2 + 1, R0 = first_radix(KC), R1 = KC / R0, RS = KC | 1;
   __syncthreads();
   stockham_pass_t<R0, KC, 1, HC, HC, 1, HC, 1, kPmeBThreads>(in, s0, tw);
   __syncthreads();
-  stockham_pass_f<R1, KC, R0, HC, kPmeBThreads>(
-      [&](int c, int e) { return s0[c + e * HC]; },
-      [&](int c, int e, float2 v) { s1[(e >> 1) * SP + 2 * c + (e & 1)] = v; }, tw);
+  pass_to_pairs<KC>(s0, s1, tw);
   __syncthreads();
-  stockham_pass_f<R0, KC, 1, KC / 2, kPmeBThreads>(
-      [&](int p, int k) {
-        const int kk = k < HC ? k : KC - k;
-        const float4 v = *reinterpret_cast<const float4*>(s1 + p * SP + 2 * kk);
-        float2 x0 = make_float2(v.x, v.y), x1 = make_float2(v.z, v.w);
-        if (k >= HC) {  // upper half of k1: the conjugate of the stored half
-          x0.y = -x0.y;
-          x1.y = -x1.y;
-        }
-        if (k == 0 || k == KC / 2) {  // self-conjugate points
-          x0.y = 0.f;
-          x1.y = 0.f;
-        }
-        return make_float2(x0.x - x1.y, x0.y + x1.x);
-      },
-      [&](int p, int k, float2 v) { s0[p * RS + k] = v; }, tw);
+  pass_from_pairs<KC>(s1, s0);
   __syncthreads();
   stockham_pass_t<R1, KC, R0, KC / 2, 1, RS, 1, RS, kPmeBThreads>(s0, s1, tw);
   __syncthreads();
