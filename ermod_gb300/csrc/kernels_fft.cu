@@ -567,21 +567,49 @@ template <int KC>
 __device__ __forceinline__ void pass_to_pairs(const float2* __restrict__ A, float2* __restrict__ B,
                                               const float2* __restrict__ tw) {
   constexpr int HC = KC / 2 + 1, R0 = first_radix(KC), R = KC / R0, NR = KC / R, SP = 2 * HC;
-  for (int t = threadIdx.x; t < HC * NR; t += kPmeBThreads) {
-    const int j = t / HC;  // < NR = R0 = NS, so the pass's k is j
-    const int col = t - j * HC;
-    float2 v[R];
+  if constexpr (R0 % 2 == 0) {
+    // a thread transforms the adjacent columns j, j + 1 (j even): their outputs e, e + 1
+    // are the two rows of one pair, stored with one 16-byte, conflict-free store
+    for (int t = threadIdx.x; t < HC * (NR / 2); t += kPmeBThreads) {
+      const int jp = t / HC;
+      const int col = t - jp * HC;
+      const int j = 2 * jp;
+      float2 v0[R], v1[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = A[col + (j + r * NR) * HC];
-    if (j > 0) {
+      for (int r = 0; r < R; ++r) {
+        v0[r] = A[col + (j + r * NR) * HC];
+        v1[r] = A[col + (j + 1 + r * NR) * HC];
+      }
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[r * j]);
+      for (int r = 1; r < R; ++r) {
+        if (j > 0) v0[r] = cmul(v0[r], tw[r * j]);
+        v1[r] = cmul(v1[r], tw[r * (j + 1)]);
+      }
+      Dft<R>::run(v0);
+      Dft<R>::run(v1);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int e = j + r * R0;  // even
+        *reinterpret_cast<float4*>(B + (e >> 1) * SP + 2 * col) = make_float4(v0[r].x, v0[r].y, v1[r].x, v1[r].y);
+      }
     }
-    Dft<R>::run(v);
+  } else {
+    for (int t = threadIdx.x; t < HC * NR; t += kPmeBThreads) {
+      const int j = t / HC;  // < NR = R0 = NS, so the pass's k is j
+      const int col = t - j * HC;
+      float2 v[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const int e = j + r * R0;
-      B[(e >> 1) * SP + 2 * col + (e & 1)] = v[r];
+      for (int r = 0; r < R; ++r) v[r] = A[col + (j + r * NR) * HC];
+      if (j > 0) {
+#pragma unroll
+        for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[r * j]);
+      }
+      Dft<R>::run(v);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int e = j + r * R0;
+        B[(e >> 1) * SP + 2 * col + (e & 1)] = v[r];
+      }
     }
   }
 }
