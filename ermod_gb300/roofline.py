@@ -22,9 +22,9 @@ from __future__ import annotations
 # intermediate does not stay in L2, so these are close to the launch's full traffic;
 # a launch of B placements moves about B times these bytes.
 MEASURED_TRAFFIC_REFS_LARGE = {
-    "spectrum": (8.2e6 + 866.1e6) / 256,  # pme_a: writes the half spectrum after the k3 transform
-    "fft_c2r": (954.4e6 + 955.4e6) / 256,  # pme_b: reads it, writes the padded potential grid
-    "gather": (1022.9e6 + 96.4e6) / 256,  # gather_tma: reads the grid (halo boxes) and site data
+    "spectrum": (8.3e6 + 866.2e6) / 256,  # pme_a: writes the half spectrum after the k3 transform
+    "fft_c2r": (955.8e6 + 955.8e6) / 256,  # pme_b: reads it, writes the padded potential grid
+    "gather": (1023.2e6 + 96.7e6) / 256,  # gather_tma: reads the grid (halo boxes) and site data
 }
 
 
