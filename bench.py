@@ -24,6 +24,7 @@ import json
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -62,10 +63,14 @@ def dist_env():
 
 
 class ClockSampler:
+    """nvidia-smi samples (200 ms) of one GPU while the timed region runs, written as CSV to
+    $ERMOD_CLOCK_LOG_DIR/clocks_<pid>.csv when that variable is set (else a temporary file)."""
+
     def __init__(self, device_index: int):
         self.dev = device_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        d = os.environ.get("ERMOD_CLOCK_LOG_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(d, f"clocks_{os.getpid()}.csv")
 
     def __enter__(self):
         try:
