@@ -4,7 +4,8 @@
 * ragged batches: 53 placements in batches of 16 (three full, one of 5) give the
   oracle's accumulators, and the same accumulators as one batch of 64;
 * the largest solute, 256 sites (kMaxSoluteSites): the spectrum generation then runs
-  over several site chunks; a 257-site solute is refused with ERMOD_E_UNSUPPORTED.
+  over several site chunks; a 257-site solute is refused with ERMOD_E_UNSUPPORTED;
+* the largest system of the 16-system set (58,329 waters, PME 125^3).
 """
 import numpy as np
 import pytest
@@ -128,4 +129,32 @@ def test_solute_above_the_limit_is_refused(gpu_lib):
     with pytest.raises(_lib.ErmodError) as ex:
         gpu.placements(np.full(len(pl), topo["nummol"], np.int32), pl)
     assert ex.value.code == _lib.E_UNSUPPORTED
+    gpu.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_largest_uneven_system(gpu_lib, oracle, precision):
+    """The largest system of the 16-system set: 58,329 waters in a 120 A box, PME 125^3
+    (three-pass transforms), a 15-site solute and an energy coordinate from -200 kcal/mol
+    (4,996 bins: global-memory counts in the finish kernel)."""
+    from ermod_gb300 import setconf, synth
+    from ermod_gb300.engproc import EnergyRepresentation
+    w = max(synth.uneven(), key=lambda x: x.nwater)
+    assert w.nwater > 58000 and w.params["ms1max"] == 125
+    topo = setconf.setparam_topology(w.species(), slttype=w.params["slttype"])
+    bins = setconf.enginit_bins(topo["numslv"], w.hist)
+    gpu = EnergyRepresentation(w.params, topo, bins, precision=precision)
+    orc = oracle.Oracle(w.params, topo, bins)
+    pos, cell = w.frame(0)
+    orc.frame(pos, cell)
+    gpu.frame(pos, cell)
+    pl = w.placements(0, 4)
+    tag = np.full(len(pl), topo["nummol"], np.int32)
+    ro, rg = orc.placements(tag, pl), gpu.placements(tag, pl, want_uvengy=True)
+    _check_uv(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], precision)
+    ag, ao = gpu.accum(), orc.accum()
+    wtol = 1e-10 if precision == "fp64" else 5e-4  # wgtslf = 1: FP32-based weights when mixed
+    np.testing.assert_allclose(ag["engnorm"], ao["engnorm"], rtol=wtol)
+    np.testing.assert_allclose(ag["edens"].sum(), ao["edens"].sum(), rtol=wtol)
+    np.testing.assert_allclose(ag["ecorr"].sum(), ao["ecorr"].sum(), rtol=wtol)
     gpu.close()
