@@ -320,7 +320,9 @@ Coef make_coef(int order, double screen) {
 
 }  // namespace
 
-int spectrum_partials(const Engine& e) { return e.geom.K[2]; }
+// self-energy partials per placement of the mixed path: one per k2 (the pme_a CTA of
+// (k2, placement) writes self_part[b][k2])
+int spectrum_partials(const Engine& e) { return e.geom.K[1]; }
 
 cudaError_t launch_place_prep(Engine& e, const BatchArgs& a, const double* sol_xyz, int self_mode, cudaStream_t s) {
   PrepArgs A{};

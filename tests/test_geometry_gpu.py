@@ -2,6 +2,8 @@
 
 * an orthorhombic box (24 x 28 x 32 A) with a non-cubic PME grid (30 x 32 x 36): the
   generic transform kernels, per-axis fixed-point scales and B-spline moduli;
+* a non-cubic grid with K2 != K3 and many placements: each placement's self energy is the
+  sum of its own K2 spectrum partials;
 * solution mode with two solute molecules (sltlist of two entries; one placement per
   solute molecule, engproc.F90:677-684), each binned against the other as a solvent.
 """
@@ -77,3 +79,27 @@ def test_solution_two_solute_molecules(gpu_lib, oracle, precision):
     ro = _run(oracle, params, species, pos, cell, 2, precision)
     # each solute sees the other one as a solvent molecule (its slot is not the self slot)
     assert np.count_nonzero(ro["uvengy"][0, 1:]) == 520 + 1
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_noncubic_grid_self_energies(gpu_lib, oracle, precision):
+    from ermod_gb300.engproc import EnergyRepresentation
+    from tests import helpers
+    w = helpers.small_refs(corrcal=0, wgtslf=0)
+    w.params.update(ms1max=30, ms2max=32, ms3max=36)
+    topo, bins = helpers.build_inputs(w)
+    gpu = EnergyRepresentation(w.params, topo, bins, precision=precision, batch=16)
+    orc = oracle.Oracle(w.params, topo, bins)
+    pos, cell = w.frame(0)
+    orc.frame(pos, cell)
+    gpu.frame(pos, cell)
+    pl = w.placements(0, 20)
+    tag = np.full(len(pl), topo["nummol"], np.int32)
+    ro, rg = orc.placements(tag, pl), gpu.placements(tag, pl, want_uvengy=True)
+    atol, rtol = (1e-9, 1e-11) if precision == "fp64" else (2e-4, 2e-6)
+    np.testing.assert_allclose(rg["uvengy"][:, 0], ro["uvengy"][:, 0], rtol=rtol, atol=atol)
+    uo, ug = ro["uvengy"][:, 1:], rg["uvengy"][:, 1:]
+    huge = np.abs(uo) >= 1e10
+    assert np.all(ug[huge] >= 1e10)
+    assert np.all(np.abs(ug - uo)[~huge] <= atol + rtol * np.abs(uo[~huge]))
+    gpu.close()
