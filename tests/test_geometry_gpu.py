@@ -2,8 +2,8 @@
 
 * an orthorhombic box (24 x 28 x 32 A) with a non-cubic PME grid (30 x 32 x 36): the
   generic transform kernels, per-axis fixed-point scales and B-spline moduli;
-* a non-cubic grid with K2 != K3 and many placements: each placement's self energy is the
-  sum of its own K2 spectrum partials;
+* non-cubic grids with K2 != K3 (one with odd K1) and many placements: each placement's
+  self energy is the sum of its own K2 spectrum partials;
 * solution mode with two solute molecules (sltlist of two entries; one placement per
   solute molecule, engproc.F90:677-684), each binned against the other as a solvent.
 """
@@ -82,11 +82,12 @@ def test_solution_two_solute_molecules(gpu_lib, oracle, precision):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_noncubic_grid_self_energies(gpu_lib, oracle, precision):
+@pytest.mark.parametrize("grid", [(30, 32, 36), (45, 48, 50)])  # the second: odd K1, generic kernels
+def test_noncubic_grid_self_energies(gpu_lib, oracle, precision, grid):
     from ermod_gb300.engproc import EnergyRepresentation
     from tests import helpers
     w = helpers.small_refs(corrcal=0, wgtslf=0)
-    w.params.update(ms1max=30, ms2max=32, ms3max=36)
+    w.params.update(ms1max=grid[0], ms2max=grid[1], ms3max=grid[2])
     topo, bins = helpers.build_inputs(w)
     gpu = EnergyRepresentation(w.params, topo, bins, precision=precision, batch=16)
     orc = oracle.Oracle(w.params, topo, bins)
