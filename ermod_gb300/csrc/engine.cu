@@ -476,6 +476,7 @@ int ermod_create(const ermod_params* p_in, int device, ermod_ctx** out) {
   // splfc tables (init_spline_axis, recpcal.F90:87-109) and FFT twiddles
   std::vector<double> splfc;
   std::vector<float2> tw;
+  std::vector<double2> tw64;
   for (int ax = 0; ax < 3; ++ax) {
     for (int rci = 0; rci < K[ax]; ++rci) {
       double re = 0.0, im = 0.0;
@@ -488,9 +489,11 @@ int ermod_create(const ermod_params* p_in, int device, ermod_ctx** out) {
       splfc.push_back(re * re + im * im);
       const double ang = 2.0 * kPi * (double)rci / (double)K[ax];
       tw.push_back(make_float2((float)std::cos(ang), (float)(-std::sin(ang))));
+      tw64.push_back(make_double2(std::cos(ang), -std::sin(ang)));
     }
   }
   if ((err = dalloc(&e.d_splfc, splfc.size())) != cudaSuccess || (err = dalloc(&e.d_twiddle, tw.size())) != cudaSuccess ||
+      (err = dalloc(&e.d_twiddle64, tw64.size())) != cudaSuccess ||
       (err = dalloc(&e.d_engfac, e.grid_cplx())) != cudaSuccess ||
       (err = dalloc(&e.d_engfac_f, (size_t)e.Hp4() * e.geom.K[1] * e.geom.K[2])) != cudaSuccess ||
       (err = cudaMemset(e.d_engfac_f, 0, sizeof(float) * e.Hp4() * e.geom.K[1] * e.geom.K[2])) != cudaSuccess) {
@@ -499,6 +502,7 @@ int ermod_create(const ermod_params* p_in, int device, ermod_ctx** out) {
   }
   cudaMemcpy(e.d_splfc, splfc.data(), sizeof(double) * splfc.size(), cudaMemcpyHostToDevice);
   cudaMemcpy(e.d_twiddle, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(e.d_twiddle64, tw64.data(), sizeof(double2) * tw64.size(), cudaMemcpyHostToDevice);
   *out = c;
   return ERMOD_OK;
 }
@@ -522,9 +526,9 @@ int ermod_destroy(ermod_ctx* c) {
   dfree(e.d_engfac_f);
   dfree(e.d_splfc);
   dfree(e.d_twiddle);
+  dfree(e.d_twiddle64);
   dfree(e.d_status);
   if (e.h_status) cudaFreeHost(e.h_status);
-  if (e.plan_c2r) cufftDestroy(e.plan_c2r);
   if (e.plan_d2z) cufftDestroy(e.plan_d2z);
   if (e.plan_z2d) cufftDestroy(e.plan_z2d);
   harvest(e);
@@ -559,7 +563,6 @@ int ermod_set_stream(ermod_ctx* c, void* stream) {
   if (e.own_stream && e.stream) cudaStreamDestroy(e.stream);
   e.stream = (cudaStream_t)stream;
   e.own_stream = false;
-  if (e.plan_c2r) cufftSetStream(e.plan_c2r, e.stream);
   if (e.plan_d2z) cufftSetStream(e.plan_d2z, e.stream);
   if (e.plan_z2d) cufftSetStream(e.plan_z2d, e.stream);
   return ERMOD_OK;
@@ -707,10 +710,10 @@ int ermod_set_topology(ermod_ctx* c, int nummol, int numatm, const int* mbi, con
     ERMOD_CUDA(dalloc(&e.d_brick_count, e.nbricks + 1));
     ERMOD_CUDA(dalloc(&e.d_brick_start, e.nbricks + 1));
   } else {
-    ERMOD_CUDA(dalloc(&e.d_site_x, 3 * (size_t)e.nsite_phys));
     ERMOD_CUDA(dalloc(&e.d_site_w, (size_t)e.nsite_phys * 3 * e.P_order));
-    ERMOD_CUDA(dalloc(&e.d_site_q, e.nsite_phys));
   }
+  ERMOD_CUDA(dalloc(&e.d_site_x, 3 * (size_t)e.nsite_phys));
+  ERMOD_CUDA(dalloc(&e.d_site_q, e.nsite_phys));
   ERMOD_CUDA(dalloc(&e.d_frame_scal, 4));
   e.green_valid = false;
   e.topo_ready = true;
@@ -969,7 +972,7 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
     a.slot = slot;
     a.stream = dual ? e.bs[slot] : e.stream;
     a.phases = 1;
-    a.mol_u = e.adj_on ? e.d_mol_u + (size_t)slot * B * e.slvmax : nullptr;
+    a.mol_bin = e.adj_on ? e.d_mol_bin + (size_t)slot * B * e.slvmax : nullptr;
     if (e.mixed) {
       const size_t np = (size_t)e.phi_dims[0] * e.phi_dims[1] * e.phi_dims[2];
       a.spec = e.buf.spec + (size_t)slot * e.grid_cplx() * B;
@@ -1271,7 +1274,7 @@ static void free_adjoint(Engine& e) {
   dfree(e.d_adj_seg);
   if (e.d_adj_cub) cudaFree(e.d_adj_cub);
   e.d_adj_cub = nullptr;
-  dfree(e.d_mol_u);
+  dfree(e.d_mol_bin);
   dfree(e.d_ps_nsite);
   dfree(e.d_ps_qf);
   dfree(e.d_ps_bvec);
@@ -1315,7 +1318,7 @@ int ermod_adjoint_enable(ermod_ctx* c, int solute_mol, int cmbrule) {
   ERMOD_CUDA(dalloc(&e.d_adj_seg, 2 * (size_t)e.ermax));
   e.adj_cub_bytes = adjoint_cub_bytes(e.slvmax);
   ERMOD_CUDA(cudaMalloc(&e.d_adj_cub, std::max<size_t>(e.adj_cub_bytes, 16)));
-  ERMOD_CUDA(dalloc(&e.d_mol_u, 2 * (size_t)B * e.slvmax));
+  ERMOD_CUDA(dalloc(&e.d_mol_bin, 2 * (size_t)B * e.slvmax));
   ERMOD_CUDA(dalloc(&e.d_ps_nsite, (size_t)B));
   ERMOD_CUDA(dalloc(&e.d_ps_qf, (size_t)B * kMaxSoluteSites));
   ERMOD_CUDA(dalloc(&e.d_ps_bvec, (size_t)B * kMaxSoluteSites * 3 * e.Kmax()));

@@ -86,6 +86,7 @@ struct Engine {
   float* d_engfac_f = nullptr;
   double* d_splfc = nullptr;     // [K1 + K2 + K3]
   float2* d_twiddle = nullptr;   // [K1 + K2 + K3] exp(-2 pi i m / K)
+  double2* d_twiddle64 = nullptr;  // the same in FP64 (solute structure factors)
   double* d_wrapped = nullptr;   // (3, numatm) normalised coordinates
   // spatial sort of physical molecules
   unsigned int* d_sort_key = nullptr;
@@ -102,9 +103,9 @@ struct Engine {
   int4* d_site_pos = nullptr;     // [nsite_phys]
   float4* d_site_rec = nullptr;
   int* d_site_grid = nullptr;
-  double* d_site_x = nullptr;     // FP64 path [nsite_phys][3]
+  double* d_site_x = nullptr;     // [nsite_phys][3] FP64 wrapped coordinates (both paths)
   double* d_site_w = nullptr;     // FP64 path [nsite_phys][3][P]
-  double* d_site_q = nullptr;     // FP64 path
+  double* d_site_q = nullptr;     // [nsite_phys] FP64 charges (both paths)
   float* d_frame_scal = nullptr;  // [0] max molecule radius about its first site (A)
   // sites grouped by 8^3 bricks of the PME grid (the mixed gather's unit of work)
   int nbrick[3] = {1, 1, 1}, nbricks = 1;
@@ -162,7 +163,7 @@ struct Engine {
   int* d_adj_seg = nullptr;      // [2][ermax] segment begin / end in the sorted order
   void* d_adj_cub = nullptr;
   size_t adj_cub_bytes = 0;
-  float* d_mol_u = nullptr;      // [2][Bmax][slvmax] per-molecule totals (slot order)
+  int* d_mol_bin = nullptr;      // [2][Bmax][slvmax] per-molecule bins (slot order)
   // unit-charge single-site "placements" whose potentials give d u / d q_s
   int* d_ps_nsite = nullptr;     // [Bmax]
   float* d_ps_qf = nullptr;      // [Bmax][256]
@@ -174,7 +175,7 @@ struct Engine {
   bool tmap_ready = false;
 
   // ---- cuFFT -------------------------------------------------------------------------
-  cufftHandle plan_c2r = 0, plan_d2z = 0, plan_z2d = 0;
+  cufftHandle plan_d2z = 0, plan_z2d = 0;
   bool plans_ready = false;
 
   // helpers

@@ -10,7 +10,8 @@
 //                      subtraction);
 //                rec   float4 {t1, t2, t3, q}  -- B-spline fractional offsets and charge;
 //                grid  int, packed base grid point g1 | g2 << 10 | g3 << 20;
-//              FP64 path: wrapped FP64 coordinates, FP64 spline weights, FP64 charge;
+//              wrapped FP64 coordinates and FP64 charge (both paths), FP64 spline
+//              weights (FP64 path);
 //   green      engfac[K3][K2][K1/2+1] FP64 (+ FP32 copy for the mixed path);
 //   batch      per placement solute sites, 1-D structure-factor vectors, PME spectrum
 //              and potential grids, per-placement energy histograms;
@@ -48,6 +49,29 @@ __host__ __device__ __forceinline__ void bspline_w(float t, float w[P]) {
     }
   }
 }
+
+// Float-float numbers: the value hi + lo with |lo| <= ulp(hi) / 2, about 48 significant
+// bits from FP32 operations only (Knuth's TwoSum, then a renormalisation).  The sums of
+// the mixed path's per-molecule energies use them, so that the total that decides a bin
+// carries no FP32 rounding of its own and no FP64 instruction is issued per molecule.
+struct ff {
+  float hi, lo;
+};
+__host__ __device__ __forceinline__ ff ff_add(ff a, float b) {
+  const float s = a.hi + b;
+  const float bb = s - a.hi;
+  const float err = (a.hi - (s - bb)) + (b - bb);
+  const float lo = a.lo + err;
+  const float hi = s + lo;
+  return ff{hi, lo - (hi - s)};
+}
+__host__ __device__ __forceinline__ ff ff_add2(ff a, ff b) { return ff_add(ff_add(a, b.hi), b.lo); }
+// a double as a float-float (exact to 48 bits: hi = rn(d), lo = rn(d - hi))
+__host__ __device__ __forceinline__ ff ff_from_double(double d) {
+  const float hi = (float)d;
+  return ff{hi, (float)(d - (double)hi)};
+}
+__host__ __device__ __forceinline__ double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
 
 // error key: (placement << 36) | (molecule << 8) | code, minimised atomically so the
 // first failing (placement, molecule) in reference order wins.
@@ -97,8 +121,9 @@ constexpr int kBrickX = 16, kBrickY = 8, kBrickZ = 8;
 
 // ordered 32-bit key of a float (-0 == +0).  For a float u and a double edge e,
 // u <= e exactly when u <= rd(e), the largest float not above e, and u > e exactly when
-// u > rd(e); so an FP32 total binned on the keys of rd(edges) lands in the bin that its
-// exact double value takes against the FP64 edges.
+// u > rd(e); so a search of the keys of rd(edges) with the key of a float-float total's
+// hi part finds its bin up to the edges within one float step of hi, which the finish
+// kernel then compares exactly.
 __host__ __device__ inline int ordered_key32(float f) {
   if (f == 0.0f) f = 0.0f;
   int k;
@@ -144,7 +169,8 @@ struct BatchArgs {
   cudaStream_t stream;  // stream of the batch's PME, gather and finish kernels
   float* site_e;      // [nsite_phys][Bmax] reciprocal site terms of this slot (mixed)
   int phases;         // 1: the launchers split the caller's timing phase (gather/finish...)
-  float* mol_u;       // [nb][slvmax] per-molecule totals in slot order (adjoint mode) or null
+  int* mol_bin;       // [nb][slvmax] bin (0-based) of each molecule in slot order, ermax when
+                      // not binned (adjoint mode), or null
   const int* tagslt;  // [nb] 1-based
   const double* stat_weight_solute;  // [nb] or null
   // solute site data per placement, [nb][kMaxSoluteSites]
@@ -164,7 +190,7 @@ struct BatchArgs {
   float* phi;          // [nb][K3][K2][K1] mixed potential
   double2* spec64;     // FP64 path
   double* phi64;       // FP64 path
-  double* self_part;   // [nb][K3] partial self energies
+  double* self_part;   // [nb][K2] (mixed) or [nb][influence64_blocks] (FP64) partial self energies
   // outputs
   int* hist;           // [nb][ermax] instantaneous histogram (insdst)
   double* part;        // [nb][ntile][numslv][3] {sum, min, max}

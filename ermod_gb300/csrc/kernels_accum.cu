@@ -434,6 +434,14 @@ __global__ void __launch_bounds__(256) ecorr_rows_kernel(const int* __restrict__
   }
 }
 
+// the dynamic shared memory of ecorr_rows_kernel, shared by the FP64 flush and the
+// no-allocation entry point: one record, so that a caller needing less never lowers the
+// size another caller has set
+SmemAttr& ecorr_rows_attr() {
+  static SmemAttr attr;
+  return attr;
+}
+
 // Mixed path flush, same sum as ecorr_rows_kernel.  A CTA owns kEcRows rows and 256
 // columns of the matrix; thread t owns one column and keeps the flush's contribution
 // to its kEcRows entries in registers as float-float pairs (exact products by fma,
@@ -597,10 +605,8 @@ cudaError_t launch_ecorr_flush(Engine& e, cudaStream_t s) {
     if (err != cudaSuccess) return err;
     void (*kern)(const int*, const int*, const double*, int, int, double*, long long*) =
         count ? ecorr_ff_kernel<true> : ecorr_ff_kernel<false>;
-    if (smem > 48 * 1024) {
-      err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (err != cudaSuccess) return err;
-    }
+    static SmemAttr attr_ff[2];  // per instantiation; the size set only ever grows
+    if ((err = attr_ff[count ? 1 : 0].ensure(kern, smem)) != cudaSuccess) return err;
     dim3 grid((e.ermax + 255) / 256, (e.ermax + kEcRows - 1) / kEcRows);
     kern<<<grid, 256, smem, s>>>(e.d_ring_hist + (size_t)e.ring_off * e.ermax, e.d_ring_valid + e.ring_off,
                                  e.d_ring_w + e.ring_off, n, e.ermax, e.d_ecorr, e.d_ecorr_n);
@@ -618,8 +624,7 @@ cudaError_t launch_ecorr_flush(Engine& e, cudaStream_t s) {
   const size_t per_row = (size_t)e.ermax * (sizeof(double) + (e.d_ecorr_n ? sizeof(long long) : 0));
   int R = (int)std::max<size_t>(1, std::min<size_t>(8, (96 * 1024) / per_row));
   const size_t smem = per_row * R;
-  err = cudaFuncSetAttribute(ecorr_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (err != cudaSuccess) return err;
+  if ((err = ecorr_rows_attr().ensure(ecorr_rows_kernel, smem)) != cudaSuccess) return err;
   const int nblk = (e.ermax + R - 1) / R;
   ecorr_rows_kernel<<<nblk, 256, smem, s>>>(hist, nz_bin, nz_cnt, e.d_ring_nnz, e.d_ring_w + e.ring_off, n,
                                                    e.ermax, R, e.d_ecorr, e.d_ecorr_n);
@@ -713,7 +718,7 @@ cudaError_t launch_ecorr_noalloc(const int* hist, const double* weight, int npla
   const size_t per_row = (size_t)ermax * (sizeof(double) + (ecorr_count ? sizeof(long long) : 0));
   const int R = (int)std::max<size_t>(1, std::min<size_t>(8, (96 * 1024) / per_row));
   const size_t smem = per_row * R;
-  err = cudaFuncSetAttribute(ecorr_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  err = ecorr_rows_attr().ensure(ecorr_rows_kernel, smem);
   if (err != cudaSuccess) return err;
   ecorr_rows_kernel<<<(ermax + R - 1) / R, 256, smem, s>>>(hist, nz_bin, nz_cnt, nnz, weight, nplace, ermax, R,
                                                            ecorr, ecorr_count);

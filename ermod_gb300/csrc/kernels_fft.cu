@@ -404,19 +404,6 @@ __device__ __forceinline__ void fft3_t(const float2* in, float2* mid, float2* mi
   stockham_pass_t<R2, N, R0 * R1, NCOLS, ES, CS, OES, OCS, NT>(mid2, out, tw);
 }
 
-struct ff {
-  float hi, lo;
-};
-__device__ __forceinline__ ff ff_add(ff a, float b) {
-  const float s = a.hi + b;
-  const float bb = s - a.hi;
-  const float err = (a.hi - (s - bb)) + (b - bb);
-  const float lo = a.lo + err;
-  const float hi = s + lo;
-  return ff{hi, lo - (hi - s)};
-}
-__device__ __forceinline__ ff ff_add2(ff a, ff b) { return ff_add(ff_add(a, b.hi), b.lo); }
-
 constexpr int kSites = 32;  // solute sites staged per chunk
 constexpr int kR1 = 4, kR3 = 3;  // generation tile: kR3 k3 values x kR1 k1 values per thread
 static_assert(kR1 == 4, "pme_a reads a tile row's engfac values as one float4");

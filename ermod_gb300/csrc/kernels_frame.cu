@@ -203,6 +203,12 @@ __global__ void frame_sites_kernel(SiteArgs A) {
     }
     A.site_grid[idx] = rci[0] | (rci[1] << kGridBits) | (rci[2] << (2 * kGridBits));
     const double q = A.charge[a];
+    // FP64 wrapped coordinates and charge: the FP64 path's pair terms, and the mixed
+    // path's FP64 terms of close pairs
+    A.site_x[3 * (size_t)idx + 0] = w[0];
+    A.site_x[3 * (size_t)idx + 1] = w[1];
+    A.site_x[3 * (size_t)idx + 2] = w[2];
+    A.site_q[idx] = q;
     if (A.mixed) {
       unsigned int X[3];
       for (int i = 0; i < 3; ++i) {
@@ -212,10 +218,6 @@ __global__ void frame_sites_kernel(SiteArgs A) {
       A.site_pos[idx] = make_int4((int)X[0], (int)X[1], (int)X[2], A.ljtype[a]);
       A.site_rec[idx] = make_float4((float)tfrac[0], (float)tfrac[1], (float)tfrac[2], (float)q);
     } else {
-      A.site_x[3 * (size_t)idx + 0] = w[0];
-      A.site_x[3 * (size_t)idx + 1] = w[1];
-      A.site_x[3 * (size_t)idx + 2] = w[2];
-      A.site_q[idx] = q;
       A.site_pos[idx] = make_int4(0, 0, 0, A.ljtype[a]);
     }
   }

@@ -27,6 +27,10 @@ namespace ermod {
 struct LjK {  // switching constants (realcal.F90:629-642, 888-904)
   float lw2, up2, lw3, up3, lw6, up6, repA, repB, repC, attA, attB, attC, lw, up, ele2, den3;
 };
+// the same in FP64 (the FP64 path, and the mixed path's FP64 pair terms)
+struct LjK64 {
+  double lw2, up2, lw3, up3, lw6, up6, repA, repB, repC, attA, attB, attC, lw, up, ele2;
+};
 
 struct MolArgs {
   // frame, slot order
@@ -67,6 +71,7 @@ struct MolArgs {
   int bare;        // cltype 0: bare Coulomb within elecut (no cutoff when non-periodic), no reciprocal space
                    // or residual
   LjK k32;         // LJ switching constants
+  LjK64 k64;
   double resid_fac;  // pi / screen^2 / volume
   // batch
   BatchArgs a;
@@ -120,11 +125,6 @@ __device__ __forceinline__ T lj_switch(int sw, const LjK& k, T eps, T sg2, T dis
   const T vdwb = invr6 - s6 * (T(k.attA) * f3 + T(k.attB) * f4 + T(k.attC));
   return T(4) * eps * (vdwa - vdwb);
 }
-
-// FP64 switching constants are recomputed in FP64 on the fly from the cutoffs.
-struct LjK64 {
-  double lw2, up2, lw3, up3, lw6, up6, repA, repB, repC, attA, attB, attC, lw, up, ele2;
-};
 
 __device__ __forceinline__ double lj_low64(int sw, const LjK64& k, double eps, double sg2, double dist) {
   const double invr2 = sg2 / dist;
@@ -285,66 +285,118 @@ __device__ __forceinline__ void hist_add(int* h, int bin) {
   if ((threadIdx.x & 31) == leader) atomicAdd(&h[bin], __popc(peers));
 }
 
+// FP32 pair terms larger than this (kcal/mol) are recomputed in FP64.  Below it an FP32
+// term is within a few units in the last place (6 for the sigma^12 of the LJ term), about
+// 5e-6 kcal/mol; above it the FP32 rounding, and the fixed-point quantisation of the
+// displacement (2.3e-8 A at L = 99.5 A), would grow with the term up to the 1e10 kcal/mol
+// of overlapping pairs.
+constexpr float kFp64Term = 8.0f;
+
+// one solute-solvent site pair in FP64, as the FP64 path computes it: minimum image of
+// the FP64 wrapped coordinates (realcal.F90:202-209), LJ with the switch form
+// (realcal.F90:686-770) and the screened or bare Coulomb term (realcal.F90:771-782, 245)
+__device__ __forceinline__ double pair_fp64(const MolArgs& A, int idx, const double* __restrict__ ux, double qu,
+                                         int tu) {
+  double dist = 0.0;
+  for (int i = 0; i < 3; ++i) {
+    const double h = 0.5 * A.g.L[i];
+    const double x = fabs(A.site_x[3 * (size_t)idx + i] - ux[i]);
+    const double d = A.g.periodic ? h - fabs(h - x) : x;
+    dist += d * d;
+  }
+  const int tv = A.site_pos[idx].w;
+  double e = 0.0;
+  const double ljeps = A.ljene[tv + A.T * tu];
+  if (ljeps > 0) {
+    const double sg2 = A.ljlensq[tv + A.T * tu];
+    if (dist <= A.k64.lw2)
+      e += lj_low64(A.ljswitch, A.k64, ljeps, sg2, dist);
+    else if (dist <= A.k64.up2)
+      e += lj_switch64(A.ljswitch, A.k64, ljeps, sg2, dist);
+  }
+  if (A.bare) {
+    if (dist < A.k64.ele2) e += qu * A.site_q[idx] / sqrt(dist);
+  } else if (dist <= A.k64.ele2) {
+    const double r = sqrt(dist);
+    e += qu * A.site_q[idx] * (1.0 - erf(A.screen * r)) / r;
+  }
+  return e;
+}
+
+// FP64 pairs recorded per thread by the finish kernel's first pass (see mol_finish_kernel)
+constexpr int kBigPerThread = 8;
+// that pass's scratch (ints): the recorded pairs, their compacted list (16-bit), the
+// threads' first sites and one double per thread
+constexpr int kFinishScratchInts = 256 * kBigPerThread + 256 * kBigPerThread / 2 + 256 + 2 * 256;
+// the dynamic shared memory of the finish kernel before its edge keys: the block
+// histograms (when in shared memory) or the FP64 pass's scratch, whichever is larger
+__host__ __device__ __forceinline__ int finish_region_ints(int G, int ermax, int hist_global) {
+  const int h = hist_global ? 0 : G * ermax;
+  return h > kFinishScratchInts ? h : kFinishScratchInts;
+}
+// a recorded pair: placement j of the block (3 bits), solute site (8 bits), site of the
+// solvent molecule (13 bits)
+__device__ __forceinline__ int big_item(int j, int su, int s) { return (j << 21) | (su << 13) | s; }
+
 // real-space LJ + screened Coulomb of one molecule against solute b (mixed path):
-// fixed-point displacements, FP32 pair terms, FP64 sum over solute sites.
-__device__ __forceinline__ float real_mixed(const MolArgs& A, const BatchArgs& a, int b, int s0, int ns,
-                                            const LjK& k32, float rcut, int4 p0, int4 u0) {
+// fixed-point displacements and FP32 pair terms, summed as a float-float number.  A pair
+// whose FP32 LJ or Coulomb term exceeds kFp64Term in magnitude (or is not finite) is left
+// out: the first pass (!kBig) records it in items[nbig] (up to kBigPerThread of them; nbig
+// counts them all) and sets bit j of fix; the second pass (kBig) sums exactly those pairs
+// in FP64.
+template <bool kBig>
+__device__ __forceinline__ ff real_mixed(const MolArgs& A, const BatchArgs& a, int b, int s0, int ns,
+                                         const LjK& k32, float rcut, int4 p0, int4 u0, int j, int* items,
+                                         int& nbig, unsigned& fix) {
   const size_t ub = (size_t)b * kMaxSoluteSites;
   const float fx = A.fxf[0], fy = A.fxf[1], fz = A.fxf[2];
   const float dx = (float)(int)((unsigned)p0.x - (unsigned)u0.x) * fx;
   const float dy = (float)(int)((unsigned)p0.y - (unsigned)u0.y) * fy;
   const float dz = (float)(int)((unsigned)p0.z - (unsigned)u0.z) * fz;
-  float real = 0.f;
+  ff real{0.f, 0.f};
   if (dx * dx + dy * dy + dz * dz > rcut * rcut) return real;
   const int nu = a.u_nsite[b];
   const float beta = A.screen_f;
   for (int su = 0; su < nu; ++su) {
     const int4 up = a.u_pos[ub + su];
     const float qu = a.u_qf[ub + su];
-    float e = 0.f;
     for (int s = 0; s < ns; ++s) {
       const int4 vp = A.site_pos[s0 + s];
       const float ex = (float)(int)((unsigned)vp.x - (unsigned)up.x) * fx;
       const float ey = (float)(int)((unsigned)vp.y - (unsigned)up.y) * fy;
       const float ez = (float)(int)((unsigned)vp.z - (unsigned)up.z) * fz;
       const float r2 = ex * ex + ey * ey + ez * ez;
+      float elj = 0.f, eco = 0.f;
       const float ljeps = A.ljene_f[vp.w + A.T * up.w];
       if (ljeps > 0.f) {
         const float sg2 = A.ljlensq_f[vp.w + A.T * up.w];
         if (r2 <= k32.lw2)
-          e += lj_low<float>(A.ljswitch, k32, ljeps, sg2, r2);
+          elj = lj_low<float>(A.ljswitch, k32, ljeps, sg2, r2);
         else if (r2 <= k32.up2)
-          e += lj_switch<float>(A.ljswitch, k32, ljeps, sg2, r2);
+          elj = lj_switch<float>(A.ljswitch, k32, ljeps, sg2, r2);
       }
       if (A.bare) {
-        if (r2 < k32.ele2) e += qu * A.site_rec[s0 + s].w / sqrtf(r2);  // realcal_bare
+        if (r2 < k32.ele2) eco = qu * A.site_rec[s0 + s].w / sqrtf(r2);  // realcal_bare
       } else if (r2 <= k32.ele2) {
         const float r = sqrtf(r2);
-        e += qu * A.site_rec[s0 + s].w * erfcf(beta * r) / r;
+        eco = qu * A.site_rec[s0 + s].w * erfcf(beta * r) / r;
+      }
+      const bool small = fabsf(elj) <= kFp64Term && fabsf(eco) <= kFp64Term;  // false for NaN, inf
+      if (!kBig) {
+        if (small) {
+          real = ff_add(real, elj);
+          real = ff_add(real, eco);
+        } else {
+          if (nbig < kBigPerThread) items[nbig] = big_item(j, su, s);
+          ++nbig;
+          fix |= 1u << j;
+        }
+      } else if (!small) {
+        real = ff_add2(real, ff_from_double(pair_fp64(A, s0 + s, a.u_x + (ub + su) * 3, a.u_q[ub + su], up.w)));
       }
     }
-    real += e;
   }
   return real;
-}
-
-// ordered key of (double)f using integer operations only (the FP64 pipe of this part
-// is ~1/60 of its FP32 rate); -0 maps to +0, subnormal floats take the slow branch
-__device__ __forceinline__ long long ordered_key_f(float f) {
-  const unsigned b = __float_as_uint(f);
-  const unsigned ex = (b >> 23) & 0xffu, man = b & 0x7fffffu;
-  const unsigned long long sign = (unsigned long long)(b >> 31) << 63;
-  unsigned long long d;
-  if (ex == 0xffu)
-    d = sign | 0x7ff0000000000000ull | ((unsigned long long)man << 29);
-  else if (ex != 0u)
-    d = sign | ((unsigned long long)(ex + 896u) << 52) | ((unsigned long long)man << 29);
-  else if (man == 0u)
-    d = 0ull;
-  else
-    return ordered_key((double)f);
-  const long long k = (long long)d;
-  return k ^ ((k >> 63) & 0x7fffffffffffffffll);
 }
 
 constexpr long long kKeyPosInf = 0x7ff0000000000000ll;
@@ -696,21 +748,64 @@ __global__ void __launch_bounds__(kGatherThreads) gather_tma_kernel(
   }
 }
 
-// Mixed path, step 2 -- per molecule x G placements: FP64 sum of the site terms, real
-// space, residual, then the G bin searches in lockstep (binary lifting over the edge
-// keys staged in shared memory), histograms and per-species partials.
+// float of an ordered 32-bit key (the inverse of ordered_key32)
+__device__ __forceinline__ float key32_to_float(int k) { return __int_as_float(k ^ ((k >> 31) & 0x7fffffff)); }
+
+// ordered 64-bit key of a float-float number (hi, lo): hi first, then lo; the order of
+// the keys is the order of the values hi + lo
+__device__ __forceinline__ long long ff_key(float hi, float lo) {
+  return (long long)(((unsigned long long)(unsigned)ordered_key32(hi) << 32) |
+                     (unsigned long long)((unsigned)ordered_key32(lo) ^ 0x80000000u));
+}
+__device__ __forceinline__ double ff_key_to_double(long long k) {
+  const float hi = key32_to_float((int)(k >> 32));
+  const float lo = key32_to_float((int)((unsigned)k ^ 0x80000000u));
+  return (double)hi + (double)lo;
+}
+
+// The number of a species' edges e below u = hi + lo, given pos, the number of edges
+// whose float keys rd(e) lie below key32(hi) (kk: the species' float keys, uvkey: its
+// FP64 edges as ordered keys).  The two counts can differ only for an edge within one
+// float step of hi; such an edge is compared exactly in FP64 (e - hi is exact there, and
+// lo is a float), so the bin is the one the FP64 value hi + lo takes against the FP64
+// edges (getiduv/binsearch, engproc.F90:927-1020).
+__device__ __forceinline__ int exact_count(const long long* __restrict__ uvkey, const int* kk, int n, int pos,
+                                           int khi, float hi, float lo) {
+  while (pos > 0 && kk[pos - 1] >= khi - 2) {  // counted, but maybe not below u
+    if (key_to_double(__ldg(uvkey + pos - 1)) - (double)hi < (double)lo) break;
+    --pos;
+  }
+  while (pos < n && kk[pos] <= khi + 2) {  // not counted, but maybe below u
+    if (!(key_to_double(__ldg(uvkey + pos)) - (double)hi < (double)lo)) break;
+    ++pos;
+  }
+  return pos;
+}
+
+// Mixed path, step 2 -- per molecule x G placements: float-float sums of the site terms
+// and of the real-space pair terms, the residual, then the G bin searches in lockstep
+// (binary lifting over the float keys of the edges staged in shared memory, finished
+// exactly against the FP64 edges), histograms and per-species partials.
 template <int G>
 __global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const float* __restrict__ site_e) {
   extern __shared__ int smem_dyn[];
   // [G][ermax] block histograms, or none when they would not fit beside other blocks: the
-  // molecules' counts then go to the batch histograms in global memory (warp-aggregated)
+  // molecules' counts then go to the batch histograms in global memory (warp-aggregated).
+  // Before the histograms are zeroed, the same region holds the FP64 pass's scratch
+  // (finish_scratch_ints ints).
   int* smem_hist = A.hist_global ? nullptr : smem_dyn;
-  int* skeys = smem_dyn + (A.hist_global ? 0 : G * A.ermax);  // [ermax] 32-bit edge keys
-  __shared__ float su[G][256];
-  __shared__ float squ[G];    // residual factor x solute charge of the G placements
-  __shared__ float srcut[G];  // bounding-sphere cutoff of the real-space sum
-  __shared__ int skskip[G];   // slot of the solute molecule itself (not a solvent)
-  __shared__ int4 supos[G];   // first solute site (fixed point)
+  int* skeys = smem_dyn + finish_region_ints(G, A.ermax, A.hist_global);  // [ermax] 32-bit edge keys
+  int* sitem = smem_dyn;                                                     // [256][kBigPerThread]
+  unsigned short* slist = reinterpret_cast<unsigned short*>(sitem + 256 * kBigPerThread);
+  int* ss0 = reinterpret_cast<int*>(slist + 256 * kBigPerThread);           // [256]
+  double* sbuf = reinterpret_cast<double*>(ss0 + 256);                      // [256]
+  __shared__ int swarp[8];
+  __shared__ float su[G][256];   // totals, hi part (NaN: no molecule)
+  __shared__ float sul[G][256];  // totals, lo part
+  __shared__ double sres[G];     // residual factor x solute charge of the G placements
+  __shared__ float srcut[G];     // bounding-sphere cutoff of the real-space sum
+  __shared__ int skskip[G];      // slot of the solute molecule itself (not a solvent)
+  __shared__ int4 supos[G];      // first solute site (fixed point)
   __shared__ unsigned char sspec[256];
   const int tile = blockIdx.y;
   const int g0 = blockIdx.x * G;
@@ -718,25 +813,23 @@ __global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const flo
   const int ng = min(G, a.nb - g0);
   const int m = tile * blockDim.x + threadIdx.x;
   const bool valid = m < A.slvmax;
-  if (!A.hist_global)
-    for (int i = threadIdx.x; i < G * A.ermax; i += blockDim.x) smem_hist[i] = 0;
   for (int i = threadIdx.x; i < A.ermax; i += blockDim.x) skeys[i] = A.uvkey_f[i];
   if (threadIdx.x < ng) {
     const int b = g0 + threadIdx.x;
-    squ[threadIdx.x] = (float)(A.resid_fac * a.u_qmol[b]);
+    sres[threadIdx.x] = A.resid_fac * a.u_qmol[b];
     srcut[threadIdx.x] = A.rc_f + a.u_radius[b] + A.frame_scal[0];
     const int tg = a.tagslt[b] - 1;
     skskip[threadIdx.x] = (tg >= 0 && tg < A.nummol) ? A.mol_to_k[tg] : -2;
     supos[threadIdx.x] = a.u_pos[(size_t)b * kMaxSoluteSites];
   }
   int k = -1, s0 = 0, ns = 0, species = 0;
-  float qmol = 0.f;
+  double qmol = 0.0;
   if (valid) {
     k = A.slot_mol[m];
     s0 = A.slot_site[m];
     ns = A.slot_site[m + 1] - s0;
     species = A.slot_species[m];
-    qmol = (float)A.slot_qmol[m];
+    qmol = A.slot_qmol[m];
   }
   const bool spec_ok = valid && species >= 1 && species <= A.numslv;
   sspec[threadIdx.x] = (unsigned char)(spec_ok ? species : 0);
@@ -748,71 +841,136 @@ __global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const flo
     sp_n = A.spec[3 * (species - 1) + 1];
     sp_soft = A.spec[3 * (species - 1) + 2];
   }
-  __syncthreads();  // squ staged
-  // ---- totals for the G placements (FP32: the site terms are FP32 already) ----
-  float uu[G];
-  bool act[G];
-  // site terms of the G placements: G consecutive floats per site (16-byte aligned when
-  // G, g0 and ldb are multiples of 4)
-  float rsum[G];
+  __syncthreads();  // sres staged
+  // ---- totals of the G placements, as float-float numbers, four placements at a time:
+  // the site terms of placements g0 + j4 .. g0 + j4 + 3 are 4 consecutive floats per site
+  // (one 16-byte load when g0, j4 and ldb are multiples of 4) ----
+  // the totals wait in this thread's entries of su (hi) and sul (lo) until the bin search
+  unsigned actm = 0u;  // placements whose total is a solvent molecule's energy
+  unsigned fix = 0u;   // placements with pairs left for the FP64 pass
+  int nbig = 0;       // such pairs of this thread (the first kBigPerThread recorded in sitem)
+  int* items = sitem + threadIdx.x * kBigPerThread;
+  const int4 p0 = valid ? A.site_pos[s0] : make_int4(0, 0, 0, 0);
 #pragma unroll
-  for (int j = 0; j < G; ++j) rsum[j] = 0.f;
-  int4 p0 = make_int4(0, 0, 0, 0);
-  if (valid) {
-    p0 = A.site_pos[s0];
-    for (int s = 0; s < (A.bare ? 0 : ns); ++s) {
-      const float* row = site_e + (size_t)(s0 + s) * ldb + g0;
-      if (G % 4 == 0 && ng == G) {
+  for (int j4 = 0; j4 < G; j4 += 4) {
+    ff rs[4];
 #pragma unroll
-        for (int j4 = 0; j4 < G; j4 += 4) {
-          const float4 v = __ldg(reinterpret_cast<const float4*>(row + j4));
-          rsum[j4] += v.x;
-          rsum[j4 + 1] += v.y;
-          rsum[j4 + 2] += v.z;
-          rsum[j4 + 3] += v.w;
+    for (int i = 0; i < 4; ++i) rs[i] = ff{0.f, 0.f};
+    if (valid) {
+      for (int s = 0; s < (A.bare ? 0 : ns); ++s) {
+        const float* row = site_e + (size_t)(s0 + s) * ldb + g0 + j4;
+        if (j4 + 4 <= ng) {
+          const float4 v = __ldg(reinterpret_cast<const float4*>(row));
+          rs[0] = ff_add(rs[0], v.x);
+          rs[1] = ff_add(rs[1], v.y);
+          rs[2] = ff_add(rs[2], v.z);
+          rs[3] = ff_add(rs[3], v.w);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+            if (j4 + i < ng) rs[i] = ff_add(rs[i], __ldg(row + i));
         }
-      } else {
-#pragma unroll
-        for (int j = 0; j < G; ++j)
-          if (j < ng) rsum[j] += __ldg(row + j);
       }
     }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int j = j4 + i;
+      ff t{0.f, 0.f};
+      if (j < ng && valid && k != skskip[j]) {
+        // get_uv_energy (engproc.F90:736-753): real + residual + recip
+        t = ff_add2(rs[i], real_mixed<false>(A, a, g0 + j, s0, ns, k32, srcut[j], p0, supos[j], j, items, nbig,
+                                             fix));
+        if (qmol != 0.0) t = ff_add2(t, ff_from_double(-sres[j] * qmol));  // residual_ene
+        actm |= 1u << j;
+      }
+      su[j][threadIdx.x] = t.hi;
+      sul[j][threadIdx.x] = t.lo;
+    }
   }
+  // ---- FP64 pass over the pairs left out above (overlapping pairs).  The block's
+  // recorded pairs are compacted (an exclusive scan over the threads) and evaluated one
+  // per thread, so that every FP64 instruction of the pass runs on full warps; each owner
+  // then adds its pairs' values in the order it found them.  A thread with more pairs
+  // than it could record sums its own in FP64.  The totals wait in su/sul meanwhile. ----
+  if (__syncthreads_or(fix != 0u)) {
+    ss0[threadIdx.x] = s0;
+    const bool ovf = nbig > kBigPerThread;
+    const int cnt = ovf ? 0 : nbig;
+    // exclusive scan of cnt over the block
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int incl = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    if (lane == 31) swarp[wid] = incl;
+    __syncthreads();
+    int off = incl - cnt, total = 0;
+    for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) {
+      if (w2 < wid) off += swarp[w2];
+      total += swarp[w2];
+    }
+    for (int i = 0; i < cnt; ++i) slist[off + i] = (unsigned short)(threadIdx.x * kBigPerThread + i);
+    __syncthreads();
+    for (int base = 0; base < total; base += blockDim.x) {
+      const int q = base + threadIdx.x;
+      double v = 0.0;
+      if (q < total) {
+        const int slot = slist[q];
+        const int t = slot / kBigPerThread, it = sitem[slot];
+        const int j = it >> 21, su_ = (it >> 13) & 0xff, sv = it & 0x1fff;
+        const size_t us = (size_t)(g0 + j) * kMaxSoluteSites + su_;
+        v = pair_fp64(A, ss0[t] + sv, a.u_x + us * 3, a.u_q[us], a.u_pos[us].w);
+      }
+      sbuf[threadIdx.x] = v;
+      __syncthreads();
+      for (int i = 0; i < cnt; ++i) {
+        const int qq = off + i - base;
+        if (qq < 0 || qq >= (int)blockDim.x) continue;
+        const int j = items[i] >> 21;
+        const ff t = ff_add2(ff{su[j][threadIdx.x], sul[j][threadIdx.x]}, ff_from_double(sbuf[qq]));
+        su[j][threadIdx.x] = t.hi;
+        sul[j][threadIdx.x] = t.lo;
+      }
+      __syncthreads();
+    }
+    if (ovf) {
+      int nb2 = 0;
+      unsigned f2 = 0u;
+      for (int j = 0; j < G; ++j)
+        if (fix & (1u << j)) {
+          const ff t = ff_add2(ff{su[j][threadIdx.x], sul[j][threadIdx.x]},
+                               real_mixed<true>(A, a, g0 + j, s0, ns, k32, srcut[j], p0, supos[j], j, nullptr,
+                                                nb2, f2));
+          su[j][threadIdx.x] = t.hi;
+          sul[j][threadIdx.x] = t.lo;
+        }
+    }
+    __syncthreads();  // the scratch is free: the histograms may take the region
+  }
+  if (!A.hist_global)
+    for (int i = threadIdx.x; i < G * A.ermax; i += blockDim.x) smem_hist[i] = 0;
+  int ku[G];     // ordered key of the total's hi part
+  float ulo[G];  // the total's lo part
 #pragma unroll
   for (int j = 0; j < G; ++j) {
-    uu[j] = 0.f;
-    act[j] = false;
-    if (j < ng) {
-      const int b = g0 + j;
-      if (valid && k != skskip[j]) {
-        const float recip = rsum[j];
-        const float real = real_mixed(A, a, b, s0, ns, k32, srcut[j], p0, supos[j]);
-        const float epcl = squ[j] * qmol;  // residual_ene: pi Q_u Q_v / (beta^2 V)
-        float pairep = -epcl;
-        pairep = pairep + recip;
-        uu[j] = real + pairep;
-        act[j] = true;
-        if (a.uvengy_out) a.uvengy_out[(size_t)(a.b0 + b) * (A.slvmax + 1) + k + 1] = (double)uu[j];
-      } else if (valid && a.uvengy_out) {
-        a.uvengy_out[(size_t)(a.b0 + b) * (A.slvmax + 1) + k + 1] = 0.0;
-      }
-    }
+    ku[j] = ordered_key32(su[j][threadIdx.x]);
+    ulo[j] = sul[j][threadIdx.x];
   }
-  if (a.mol_u && valid) {  // adjoint mode: the totals in slot order (NaN: no molecule)
+  if (valid && a.uvengy_out) {
 #pragma unroll
-    for (int j = 0; j < G; ++j)
-      if (j < ng) a.mol_u[(size_t)(g0 + j) * A.slvmax + m] = act[j] ? uu[j] : __uint_as_float(0x7fc00000u);
+    for (int j = 0; j < G; ++j) {
+      if (j >= ng) break;
+      a.uvengy_out[(size_t)(a.b0 + g0 + j) * (A.slvmax + 1) + k + 1] =
+          (actm & (1u << j)) ? (double)key32_to_float(ku[j]) + (double)ulo[j] : 0.0;
+    }
   }
   __syncthreads();  // histograms zeroed, keys staged
-  // ---- getiduv / binsearch for all G at once: ret = #edges < u (32-bit keys of the
-  // FP32 totals against the edges rounded down to floats: the same count as FP64) ----
-  int ku[G];
+  // ---- getiduv / binsearch for all G at once: pos = #edges whose float keys lie below
+  // the key of the total's hi part ----
   int pos[G];
 #pragma unroll
-  for (int j = 0; j < G; ++j) {
-    ku[j] = ordered_key32(uu[j]);
-    pos[j] = 0;
-  }
+  for (int j = 0; j < G; ++j) pos[j] = 0;
   int step = 1;
   while ((step << 1) <= sp_n) step <<= 1;
   const int* kk = skeys + sp_off;
@@ -825,60 +983,75 @@ __global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const flo
   }
 #pragma unroll
   for (int j = 0; j < G; ++j) {
-    float u = __uint_as_float(0x7fc00000u);  // NaN marks "no molecule"
-    if (act[j]) {
-      const float v = uu[j];
-      const int ret = pos[j];
+    float hv = __uint_as_float(0x7fc00000u);  // NaN marks "no molecule"
+    float lv = 0.f;
+    if (actm & (1u << j)) {
+      const float v = key32_to_float(ku[j]), lo = ulo[j];
+      int ret = pos[j];
       int code = 0;
-      if (!spec_ok)
+      if (!spec_ok) {
         code = ERMOD_E_ENG_CNS;
-      else if (v != v || ret <= 0)
+      } else if (v != v) {
         code = ERMOD_E_ENG_MIN;
-      else if (A.soln && ret > sp_soft)
-        code = ERMOD_E_ENG_SFT;
-      else if (ret == sp_n && v < 1.0e3f && A.mbin_mode != 0) {
-        if (A.mbin_mode == 1)
-          code = ERMOD_W_MBIN;
-        else
-          atomicOr(&A.status->mbin_hit, 1);
+      } else {
+        ret = exact_count(A.uvkey + sp_off, kk, sp_n, ret, ku[j], v, lo);
+        if (ret <= 0)
+          code = ERMOD_E_ENG_MIN;
+        else if (A.soln && ret > sp_soft)
+          code = ERMOD_E_ENG_SFT;
+        else if (ret == sp_n && (v < 1.0e3f || (v == 1.0e3f && lo < 0.f)) && A.mbin_mode != 0) {
+          if (A.mbin_mode == 1)
+            code = ERMOD_W_MBIN;
+          else
+            atomicOr(&A.status->mbin_hit, 1);
+        }
       }
       if (code)
         atomicMin(&A.status->err_key, make_err_key(a.b0 + g0 + j, k + 1, code));
       else
         hist_add(A.hist_global ? a.hist + (size_t)(g0 + j) * A.ermax : smem_hist + j * A.ermax, sp_off + ret - 1);
-      u = v;
+      if (a.mol_bin) a.mol_bin[(size_t)(g0 + j) * A.slvmax + m] = code ? A.ermax : sp_off + ret - 1;
+      hv = v;
+      lv = lo;
+    } else if (a.mol_bin && valid && j < ng) {
+      a.mol_bin[(size_t)(g0 + j) * A.slvmax + m] = A.ermax;
     }
-    su[j][threadIdx.x] = u;
+    su[j][threadIdx.x] = hv;
+    sul[j][threadIdx.x] = lv;
   }
   __syncthreads();
   // per-species {sum, min, max} of the block: one warp per (placement, species),
-  // fixed lane order and a fixed shuffle tree
+  // fixed lane order and a fixed shuffle tree; min and max on ordered keys of the
+  // float-float totals
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // the species sums are flceng (engproc.F90:822-825): needed for slnuv (solution mode)
   // and when the caller asks for flceng
   const bool want_sum = A.soln || a.flceng_out != nullptr;
+  constexpr long long kKeyMax = 0x7fffffffffffffffll, kKeyMin = (long long)0x8000000000000000ull;
   for (int pr = warp; pr < ng * A.numslv; pr += blockDim.x / 32) {
     const int j = pr / A.numslv, sp = pr % A.numslv + 1;
-    float mn = INFINITY, mx = -INFINITY;
+    long long mn = kKeyMax, mx = kKeyMin;
     double s = 0.0;
     for (int t = lane; t < blockDim.x; t += 32) {
       const float v = su[j][t];
       if (sspec[t] == sp && v == v) {
-        if (want_sum) s += (double)v;
-        mn = fminf(mn, v);
-        mx = fmaxf(mx, v);
+        const float lo = sul[j][t];
+        if (want_sum) s += (double)v + (double)lo;
+        const long long key = ff_key(v, lo);
+        mn = min(mn, key);
+        mx = max(mx, key);
       }
     }
     for (int off = 16; off > 0; off >>= 1) {
       if (want_sum) s += __shfl_down_sync(0xffffffffu, s, off);
-      mn = fminf(mn, __shfl_down_sync(0xffffffffu, mn, off));
-      mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, off));
+      mn = min(mn, __shfl_down_sync(0xffffffffu, mn, off));
+      mx = max(mx, __shfl_down_sync(0xffffffffu, mx, off));
     }
     if (lane == 0) {
       double* pt = a.part + (((size_t)(g0 + j) * A.ntile + tile) * A.numslv + (sp - 1)) * 3;
       pt[0] = s;
-      pt[1] = (double)mn;
-      pt[2] = (double)mx;
+      pt[1] = (mn == kKeyMax) ? HUGE_VAL : ff_key_to_double(mn);
+      pt[2] = (mx == kKeyMin) ? -HUGE_VAL : ff_key_to_double(mx);
     }
   }
   if (A.hist_global) return;
@@ -955,7 +1128,8 @@ static MolArgs make_mol_args(Engine& e, const BatchArgs& a) {
   for (int i = 0; i < 3; ++i) A.fxf[i] = (float)e.geom.fx_scale[i];
   A.screen_f = (float)e.P.screen;
   A.rc_f = (float)std::max(A.elecut, e.P.upljcut);
-  A.k32 = to_f32(make_k64(A));
+  A.k64 = make_k64(A);
+  A.k32 = to_f32(A.k64);
   A.a = a;
   A.ntile = e.ntile;
   A.status = e.d_status;
@@ -1010,7 +1184,7 @@ cudaError_t launch_mol_energy(Engine& e, const BatchArgs& a) {
     e.phase_begin_on(PH_MOL, a.stream);
   }
   // step 2: per-molecule totals and binning (histograms + edge keys in shared memory)
-  const size_t smem_f = sizeof(int) * ((A.hist_global ? 0 : (size_t)a.G * e.ermax) + e.ermax);
+  const size_t smem_f = sizeof(int) * ((size_t)finish_region_ints(a.G, e.ermax, A.hist_global) + e.ermax);
   dim3 g2((a.nb + a.G - 1) / a.G, e.ntile);
 #define ERMOD_FINISH(GG)                                                                                   \
   if (a.G == GG) {                                                                                         \
@@ -1092,7 +1266,7 @@ struct AdjArgs {
   int cmbrule;
   int first;      // first chunk: also writes the bin keys
   const float* site_e_ps;  // [nsite][ldb] q_t phi_s(r_t) of the chunk's sites
-  const float* mol_u;      // [slvmax] totals of placement b, slot order
+  const int* mol_bin;      // [slvmax] bins of placement b's molecules, slot order (ermax: none)
   const float2* par;       // [nsu] {eps_s, sigma_s}
   float* du;               // [slvmax][3 nsu]
   int* key;                // [slvmax] global bin, or ermax to leave the molecule out
@@ -1112,22 +1286,8 @@ __global__ void __launch_bounds__(256) adjoint_mol_kernel(MolArgs A, AdjArgs J) 
   const int kskip = (tg >= 0 && tg < A.nummol) ? A.mol_to_k[tg] : -2;
   bool take = (tg + 1 == J.adj_mol) && (k != kskip) && species >= 1 && species <= A.numslv;
   if (J.first) {
-    int key = A.ermax;
-    const float u = J.mol_u[m];
-    if (take && u == u) {  // getiduv on the FP64 value of the FP32 total, as the finish kernel bins it
-      const int sp_off = A.spec[3 * (species - 1)], sp_n = A.spec[3 * (species - 1) + 1];
-      const int sp_soft = A.spec[3 * (species - 1) + 2];
-      const long long ku = ordered_key_f(u);
-      int lo = 0, hi = sp_n;
-      while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (__ldg(A.uvkey + sp_off + mid) < ku)
-          lo = mid + 1;
-        else
-          hi = mid;
-      }
-      if (lo > 0 && !(A.soln && lo > sp_soft)) key = sp_off + lo - 1;
-    }
+    // the molecule's bin as the finish kernel found it (ermax: not binned)
+    const int key = take ? J.mol_bin[m] : A.ermax;
     J.key[m] = key;
     J.val[m] = m;
   }
@@ -1271,7 +1431,7 @@ cudaError_t launch_adjoint(Engine& e, const BatchArgs& a, cudaStream_t s) {
       J.cmbrule = e.adj_cmbrule;
       J.first = (s0 == 0);
       J.site_e_ps = a.site_e;
-      J.mol_u = a.mol_u + (size_t)b * n;
+      J.mol_bin = a.mol_bin + (size_t)b * n;
       J.par = e.d_adj_par;
       J.du = e.d_adj_du;
       J.key = key;

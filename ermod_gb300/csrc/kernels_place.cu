@@ -1,8 +1,8 @@
 // kernels_place.cu -- per-placement solute preparation and the plain FP64 PME path.
 //
 //   place_prep    solute sites of every placement in a batch: wrapped FP64 and
-//                 fixed-point coordinates, calc_spline_molecule (recpcal.F90:408-442;
-//                 FP64 weights on the FP64 path, FP32 Cox-de Boor weights on the mixed),
+//                 fixed-point coordinates, calc_spline_molecule (recpcal.F90:408-442,
+//                 FP64 weights on both paths),
 //                 realcal_self (realcal.F90:284-328, FP64) and, for the mixed path,
 //                 the 1-D structure-factor vectors
 //                     b_{s,a}(k) = sum_c theta_{s,a,c} exp(-2 pi i k (g_{s,a} - c) / K_a);
@@ -52,7 +52,7 @@ struct PrepArgs {
   const double* charge;
   const int* ljtype;
   const double* mol_qmol_all;  // [nummol]
-  const float2* twiddle;       // [K1+K2+K3]
+  const double2* twiddle64;    // [K1+K2+K3] exp(-2 pi i m / K)
   FrameGeom g;
   Coef sc;
   int mixed;
@@ -89,7 +89,6 @@ __global__ void __launch_bounds__(256) place_prep_kernel(PrepArgs A) {
   const int P = A.sc.order;
   __shared__ double sx[kMaxSoluteSites][3];
   __shared__ double red[256];
-  __shared__ float swf[kMaxSoluteSites][3][kMaxSplineOrder];  // mixed path: FP32 weights
   __shared__ int sgrd[kMaxSoluteSites][3];
   if (ns > kMaxSoluteSites) {
     if (threadIdx.x == 0) {
@@ -131,23 +130,10 @@ __global__ void __launch_bounds__(256) place_prep_kernel(PrepArgs A) {
       const double f2 = factor * (double)g.K[kk];
       rci[kk] = (int)f2;
       double* uw = a.u_w + (us * 3 + kk) * kMaxSplineOrder;
-      if (A.mixed) {  // FP32 Cox-de Boor weights, the recursion the solvent sites use
-        float wf[kMaxSplineOrder];
-        const float t = (float)(f2 - (double)rci[kk]);
-        if (P == 4)
-          bspline_w<4>(t, wf);
-        else if (P == 6)
-          bspline_w<6>(t, wf);
-        else
-          bspline_w<8>(t, wf);
-        for (int spi = 0; spi < P; ++spi) {
-          uw[spi] = (double)wf[spi];
-          swf[s][kk][spi] = wf[spi];
-        }
-        sgrd[s][kk] = rci[kk];
-      } else {
-        for (int spi = 0; spi < P; ++spi) uw[spi] = spline_value(A.sc, f2 - (double)(rci[kk] - spi));
-      }
+      // FP64 weights on both paths: on the mixed path they set the 1-D structure factors,
+      // whose accuracy bounds that of the solute self energy (the weights of placements)
+      for (int spi = 0; spi < P; ++spi) uw[spi] = spline_value(A.sc, f2 - (double)(rci[kk] - spi));
+      sgrd[s][kk] = rci[kk];
     }
     a.u_grid[us] = rci[0] | (rci[1] << kGridBits) | (rci[2] << (2 * kGridBits));
   }
@@ -156,7 +142,8 @@ __global__ void __launch_bounds__(256) place_prep_kernel(PrepArgs A) {
     a.u_qmol[b] = A.mol_qmol_all[mol];
   }
   __syncthreads();
-  // 1-D structure-factor vectors (mixed path)
+  // 1-D structure-factor vectors (mixed path): FP64 weights and twiddles, rounded to FP32
+  // once at the end, so that their errors are independent roundings
   if (A.mixed) {
     const int Kx = g.K[0], Ky = g.K[1], Kz = g.K[2];
     const int Kmax = max(Kx, max(Ky, Kz));
@@ -170,20 +157,20 @@ __global__ void __launch_bounds__(256) place_prep_kernel(PrepArgs A) {
       if (k >= K) continue;
       const size_t us = (size_t)b * kMaxSoluteSites + s;
       const int grd = sgrd[s][ax];
-      const float2* tw = A.twiddle + (ax == 0 ? 0 : (ax == 1 ? Kx : Kx + Ky));
+      const double2* tw = A.twiddle64 + (ax == 0 ? 0 : (ax == 1 ? Kx : Kx + Ky));
+      const double* th = a.u_w + (us * 3 + ax) * kMaxSplineOrder;
       const unsigned mk = A.mK[ax];
-      float re = 0.f, im = 0.f;
+      double re = 0.0, im = 0.0;
       for (int c = 0; c < P; ++c) {
-        const float th = swf[s][ax][c];
         int gc = grd - c;  // in (-P, K)
         if (gc < 0) gc += K;
         const unsigned x = (unsigned)(k * gc);  // < K^2 <= 10^6
         const int mm = (int)(x - __umulhi(x, mk) * (unsigned)K);
-        const float2 w = tw[mm];
-        re = fmaf(th, w.x, re);
-        im = fmaf(th, w.y, im);
+        const double2 w = tw[mm];
+        re = fma(th[c], w.x, re);
+        im = fma(th[c], w.y, im);
       }
-      a.u_bvec[(us * 3 + ax) * Kmax + k] = make_float2(re, im);
+      a.u_bvec[(us * 3 + ax) * Kmax + k] = make_float2((float)re, (float)im);
     }
   }
   // bounding radius about site 1 (minimum image; FP32, padded to stay conservative)
@@ -333,7 +320,7 @@ cudaError_t launch_place_prep(Engine& e, const BatchArgs& a, const double* sol_x
   A.charge = e.d_charge;
   A.ljtype = e.d_ljtype;
   A.mol_qmol_all = e.d_qmol_all;
-  A.twiddle = e.d_twiddle;
+  A.twiddle64 = e.d_twiddle64;
   A.g = e.geom;
   A.sc = make_coef(e.P_order, e.P.screen);
   A.mixed = e.mixed ? 1 : 0;

@@ -256,8 +256,10 @@ int ermod_engstore_merge(int nrank, int slttype, int wgtslf, double temp, int er
  * device synchronisation of cudaFree would stall).  Its scratch is one fixed 8 MiB
  * device array, so nplace <= 4096, ermax <= 8192 and nplace * ermax <= 1048576, else
  * ERMOD_E_PARAM.  The first call on each device looks up that array's address: make it
- * before any stream capture.  All calls on a device share the array, so calls that
- * overlap on the GPU race. */
+ * before any stream capture.  The address is then kept for the life of the process, so
+ * a host that resets the device (cudaDeviceReset) or tears down its primary context
+ * must not call this entry point again afterwards.  All calls on a device share the
+ * array, so calls that overlap on the GPU race. */
 int ermod_ecorr_add_noalloc(const int* hist, const double* weight, int nplace, int ermax,
                             double* ecorr, int64_t* ecorr_count, void* stream);
 
