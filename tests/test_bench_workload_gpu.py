@@ -1,54 +1,86 @@
-"""The benchmark's own workload at full size (GPU): 33,000 waters in a 99.5 A box, a
-12-site solute, PME 96^3, ecorr on, wgtslf and NPT weights.
+"""The benchmark's own workloads at full size (GPU).
 
-* 8 placements of frame 0 against the oracle, both precisions;
-* all 50,000 insertions of frame 0 on the mixed path, checked by size-independent
+* refs_large (33,000 waters in a 99.5 A box, a 12-site solute, PME 96^3, ecorr on,
+  wgtslf and NPT weights): 8 placements of frame 0 against the oracle in both precisions,
+  per-molecule energies, per-placement histograms and edens/ecorr bin by bin; and all
+  50,000 insertions of frame 0 on the mixed path, checked by size-independent
   invariants: every placement bins all 33,000 molecules, so sum(edens) = 33,000 engnorm,
   each ecorr row sums to 33,000 times that bin's edens, ecorr is symmetric, and the
   int64 count mirror is symmetric and sums to exactly 50,000 x 33,000^2.
+* refs_small at its own size (4,000 waters in a 49.3 A box, the 6-site solute, PME 48^3,
+  ecorr on, weighted): 256 insertions of a frame against the oracle, per placement.
+* soln_small (1,000 waters, PME 32^3, solution mode): several frames against the oracle.
 """
 import numpy as np
 import pytest
 
+from tests import helpers
+from tests.test_parity_gpu import _check_weighted
+
 pytestmark = pytest.mark.gpu
 
 
-def _setup(precision, **kw):
+def _setup(name, precision, **kw):
     from ermod_gb300 import setconf, synth
     from ermod_gb300.engproc import EnergyRepresentation
-    w = synth.refs_large()
+    w = synth.WORKLOADS[name]()
     topo = setconf.setparam_topology(w.species(), slttype=w.params["slttype"])
     bins = setconf.enginit_bins(topo["numslv"])
     return w, topo, bins, EnergyRepresentation(w.params, topo, bins, precision=precision, **kw)
 
 
+def _against_oracle(oracle, name, precision, nplace, frames=(0,)):
+    w, topo, bins, gpu = _setup(name, precision)
+    orc = oracle.Oracle(w.params, topo, bins)
+    uo_all = []
+    for f in frames:
+        pos, cell = w.frame(f)
+        orc.frame(pos, cell)
+        gpu.frame(pos, cell)
+        if w.mode == "soln":
+            tag, pl = [topo["nummol"]], None
+        else:
+            pl = w.placements(f, nplace)
+            tag = np.full(len(pl), topo["nummol"], np.int32)
+        ro, rg = orc.placements(tag, pl), gpu.placements(tag, pl, want_uvengy=True)
+        uo, ug = ro["uvengy"], rg["uvengy"]
+        err, err_soft = helpers.check_energies(ug[:, 1:], uo[:, 1:], precision, name)
+        np.testing.assert_allclose(ug[:, 0], uo[:, 0], rtol=0, atol=helpers.self_tol(precision, len(w.solute["charge"])))
+        helpers.check_histograms(ug[:, 1:], uo[:, 1:], bins["uvcrd"], precision, f"{name} frame {f}")
+        print(f"[parity] {name} {precision} frame {f}: max |du| {err:.3e} (|u| < 20: {err_soft:.3e}), "
+              f"self energy max |du0| {np.abs(ug[:, 0] - uo[:, 0]).max():.3e}")
+        uo_all.append(uo)
+    ag, ao = gpu.accum(), orc.accum()
+    if precision == "fp64":
+        np.testing.assert_allclose(ag["engnorm"], ao["engnorm"], rtol=1e-10)
+        np.testing.assert_allclose(ag["edens"], ao["edens"], rtol=1e-10, atol=0)
+        if ao["ecorr"] is not None:
+            np.testing.assert_allclose(ag["ecorr"], ao["ecorr"], rtol=1e-10, atol=0)
+    else:
+        _check_weighted(ag, ao, np.concatenate(uo_all), bins["uvcrd"], w, corr=ao["ecorr"] is not None, label=name)
+    gpu.close()
+    orc.close()
+    return w, topo
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_refs_large_against_oracle(gpu_lib, oracle, precision):
-    w, topo, bins, gpu = _setup(precision)
-    assert gpu.slvmax == 33000 and w.params["ms1max"] == 96
-    orc = oracle.Oracle(w.params, topo, bins)
-    pos, cell = w.frame(0)
-    orc.frame(pos, cell)
-    gpu.frame(pos, cell)
-    pl = w.placements(0, 8)
-    tag = np.full(len(pl), topo["nummol"], np.int32)
-    ro, rg = orc.placements(tag, pl), gpu.placements(tag, pl, want_uvengy=True)
-    atol, rtol = (1e-9, 1e-11) if precision == "fp64" else (1e-4, 2e-6)
-    uo, ug = ro["uvengy"][:, 1:], rg["uvengy"][:, 1:]
-    huge = np.abs(uo) >= 1e10
-    assert np.all(ug[huge] >= 1e10)
-    err = np.abs(ug - uo)[~huge]
-    assert np.all(err <= atol + rtol * np.abs(uo[~huge])), f"max err {err.max():.3e}"
-    ag, ao = gpu.accum(), orc.accum()
-    wtol = 1e-10 if precision == "fp64" else 5e-4  # FP32-based self energies in the weights
-    np.testing.assert_allclose(ag["engnorm"], ao["engnorm"], rtol=wtol)
-    np.testing.assert_allclose(ag["edens"].sum(), ao["edens"].sum(), rtol=wtol)
-    np.testing.assert_allclose(ag["ecorr"].sum(), ao["ecorr"].sum(), rtol=wtol)
-    gpu.close()
+    w, topo = _against_oracle(oracle, "refs_large", precision, 8)
+    assert topo["nummol"] - 1 == 33000 and w.params["ms1max"] == 96
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_refs_small_full_size_against_oracle(gpu_lib, oracle, precision):
+    w, topo = _against_oracle(oracle, "refs_small", precision, 256)
+    assert topo["nummol"] - 1 == 4000 and w.params["ms1max"] == 48 and w.params["corrcal"] == 1
+
+
+def test_soln_small_frames_full_size(gpu_lib, oracle):
+    _against_oracle(oracle, "soln_small", "mixed", 1, frames=range(8))
 
 
 def test_refs_large_full_frame_invariants(gpu_lib):
-    w, topo, bins, gpu = _setup("mixed", batch=256, count_mirror=True)
+    w, topo, bins, gpu = _setup("refs_large", "mixed", batch=256, count_mirror=True)
     pos, cell = w.frame(0)
     gpu.frame(pos, cell)
     n = w.ins_per_frame

@@ -11,10 +11,9 @@ import numpy as np
 import pytest
 
 from tests import helpers
+from tests.test_parity_gpu import _check_weighted
 
 pytestmark = pytest.mark.gpu
-
-TOL = {"fp64": (1e-9, 1e-11), "mixed": (1e-4, 2e-6)}
 
 
 def _engine(w, precision, **kw):
@@ -23,12 +22,10 @@ def _engine(w, precision, **kw):
     return EnergyRepresentation(w.params, topo, bins, precision=precision, **kw), topo, bins
 
 
-def _check_uv(ug, uo, precision):
-    atol, rtol = TOL[precision]
-    huge = np.abs(uo) >= 1e10
-    assert np.all(ug[huge] >= 1e10)
-    err = np.abs(ug - uo)[~huge]
-    assert np.all(err <= atol + rtol * np.abs(uo[~huge])), f"max err {err.max():.3e}"
+def _check_uv(ug, uo, precision, edges=None, label=""):
+    helpers.check_energies(ug, uo, precision, label)
+    if edges is not None:
+        helpers.check_histograms(ug, uo, edges, precision, label)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -49,7 +46,7 @@ def test_empty_call(gpu_lib, oracle, precision):
     pl = w.placements(0, 8)
     tag = np.full(len(pl), topo["nummol"], np.int32)
     ro, rg = orc.placements(tag, pl), gpu.placements(tag, pl, want_uvengy=True)
-    _check_uv(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], precision)
+    _check_uv(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], precision, bins["uvcrd"], "after an empty call")
     gpu.close()
 
 
@@ -59,6 +56,7 @@ def test_ragged_batches(gpu_lib, oracle, precision):
     g16, topo, bins = _engine(w, precision, batch=16)
     g64, _, _ = _engine(w, precision, batch=64)
     orc = oracle.Oracle(w.params, topo, bins)
+    uo_all = []
     for f in range(2):
         pos, cell = w.frame(f)
         pl = w.placements(f, 53)
@@ -68,7 +66,8 @@ def test_ragged_batches(gpu_lib, oracle, precision):
         ro = orc.placements(tag, pl)
         r16 = g16.placements(tag, pl, want_uvengy=True)
         r64 = g64.placements(tag, pl, want_uvengy=True)
-        _check_uv(r16["uvengy"][:, 1:], ro["uvengy"][:, 1:], precision)
+        _check_uv(r16["uvengy"][:, 1:], ro["uvengy"][:, 1:], precision, bins["uvcrd"], "ragged batches")
+        uo_all.append(ro["uvengy"])
         # the batch size does not change a placement's energies: bit for bit on the mixed
         # path (per-placement arithmetic); the FP64 path's cuFFT plans differ per batch size
         if precision == "mixed":
@@ -76,11 +75,13 @@ def test_ragged_batches(gpu_lib, oracle, precision):
         else:
             np.testing.assert_allclose(r16["uvengy"], r64["uvengy"], rtol=1e-12, atol=1e-10)
     a16, a64, ao = g16.accum(), g64.accum(), orc.accum()
-    # wgtslf = 1: the weights follow the solute self energy, FP32-based on the mixed path
-    wtol = 1e-10 if precision == "fp64" else 5e-4
-    np.testing.assert_allclose(a16["engnorm"], ao["engnorm"], rtol=wtol)
-    np.testing.assert_allclose(a16["edens"].sum(), ao["edens"].sum(), rtol=wtol)
-    np.testing.assert_allclose(a16["ecorr"].sum(), ao["ecorr"].sum(), rtol=wtol)
+    # wgtslf = 1: the weights follow the solute self energy
+    if precision == "fp64":
+        np.testing.assert_allclose(a16["engnorm"], ao["engnorm"], rtol=1e-10)
+        np.testing.assert_allclose(a16["edens"], ao["edens"], rtol=1e-10, atol=0)
+        np.testing.assert_allclose(a16["ecorr"], ao["ecorr"], rtol=1e-10, atol=0)
+    else:
+        _check_weighted(a16, ao, np.concatenate(uo_all), bins["uvcrd"], w, label="ragged batches")
     # one batch of 64 against batches of 16: the same sums in placement order (ecorr's
     # float-float flush groups differ on the mixed path)
     for key in ("edens", "engnorm", "avslf", "minuv", "maxuv"):
@@ -111,11 +112,11 @@ def test_largest_solute(gpu_lib, oracle, precision):
     pl = w.placements(0, 6)
     tag = np.full(len(pl), topo["nummol"], np.int32)
     ro, rg = orc.placements(tag, pl), gpu.placements(tag, pl, want_uvengy=True)
-    _check_uv(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], precision)
+    _check_uv(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], precision, bins["uvcrd"], "256-site solute")
     # the self energy (all 256 sites' spectrum, summed over the site chunks): about
     # -1 kcal/mol, net of reciprocal and real-space parts that largely cancel
     np.testing.assert_allclose(rg["uvengy"][:, 0], ro["uvengy"][:, 0], rtol=0,
-                               atol=1e-9 if precision == "fp64" else 1e-3)
+                               atol=helpers.self_tol(precision, len(w.solute["charge"])))
     gpu.close()
 
 
@@ -151,10 +152,14 @@ def test_largest_uneven_system(gpu_lib, oracle, precision):
     pl = w.placements(0, 4)
     tag = np.full(len(pl), topo["nummol"], np.int32)
     ro, rg = orc.placements(tag, pl), gpu.placements(tag, pl, want_uvengy=True)
-    _check_uv(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], precision)
+    _check_uv(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], precision, bins["uvcrd"], "58,329 waters")
+    np.testing.assert_allclose(rg["uvengy"][:, 0], ro["uvengy"][:, 0], rtol=0,
+                               atol=helpers.self_tol(precision, len(w.solute["charge"])))
     ag, ao = gpu.accum(), orc.accum()
-    wtol = 1e-10 if precision == "fp64" else 5e-4  # wgtslf = 1: FP32-based weights when mixed
-    np.testing.assert_allclose(ag["engnorm"], ao["engnorm"], rtol=wtol)
-    np.testing.assert_allclose(ag["edens"].sum(), ao["edens"].sum(), rtol=wtol)
-    np.testing.assert_allclose(ag["ecorr"].sum(), ao["ecorr"].sum(), rtol=wtol)
+    if precision == "fp64":
+        np.testing.assert_allclose(ag["engnorm"], ao["engnorm"], rtol=1e-10)
+        np.testing.assert_allclose(ag["edens"], ao["edens"], rtol=1e-10, atol=0)
+        np.testing.assert_allclose(ag["ecorr"], ao["ecorr"], rtol=1e-10, atol=0)
+    else:
+        _check_weighted(ag, ao, ro["uvengy"], bins["uvcrd"], w, label="58,329 waters")
     gpu.close()

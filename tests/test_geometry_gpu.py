@@ -10,6 +10,8 @@
 import numpy as np
 import pytest
 
+from tests import helpers
+
 pytestmark = pytest.mark.gpu
 
 
@@ -50,11 +52,12 @@ def _run(oracle, params, species, pos, cell, nsolute, precision):
     tag = np.arange(topo["nummol"] - nsolute + 1, topo["nummol"] + 1, dtype=np.int32)
     ro = orc.placements(tag)
     rg = gpu.placements(tag, want_uvengy=True)
-    atol, rtol = (1e-9, 1e-11) if precision == "fp64" else (1e-4, 2e-6)
-    err = np.abs(rg["uvengy"] - ro["uvengy"])
-    assert np.all(err <= atol + rtol * np.abs(ro["uvengy"])), err.max()
+    helpers.check_energies(rg["uvengy"], ro["uvengy"], precision, "geometry")
+    rep = helpers.check_histograms(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], bins["uvcrd"], precision, "geometry")
     ag, ao = gpu.accum(), orc.accum()
     np.testing.assert_allclose(ag["edens"].sum(), ao["edens"].sum(), rtol=1e-12)
+    if rep["other_bin"] == 0:
+        np.testing.assert_array_equal(ag["edens"], ao["edens"])
     gpu.close()
     return ro
 
@@ -85,7 +88,6 @@ def test_solution_two_solute_molecules(gpu_lib, oracle, precision):
 @pytest.mark.parametrize("grid", [(30, 32, 36), (45, 48, 50)])  # the second: odd K1, generic kernels
 def test_noncubic_grid_self_energies(gpu_lib, oracle, precision, grid):
     from ermod_gb300.engproc import EnergyRepresentation
-    from tests import helpers
     w = helpers.small_refs(corrcal=0, wgtslf=0)
     w.params.update(ms1max=grid[0], ms2max=grid[1], ms3max=grid[2])
     topo, bins = helpers.build_inputs(w)
@@ -97,10 +99,7 @@ def test_noncubic_grid_self_energies(gpu_lib, oracle, precision, grid):
     pl = w.placements(0, 20)
     tag = np.full(len(pl), topo["nummol"], np.int32)
     ro, rg = orc.placements(tag, pl), gpu.placements(tag, pl, want_uvengy=True)
-    atol, rtol = (1e-9, 1e-11) if precision == "fp64" else (2e-4, 2e-6)
-    np.testing.assert_allclose(rg["uvengy"][:, 0], ro["uvengy"][:, 0], rtol=rtol, atol=atol)
-    uo, ug = ro["uvengy"][:, 1:], rg["uvengy"][:, 1:]
-    huge = np.abs(uo) >= 1e10
-    assert np.all(ug[huge] >= 1e10)
-    assert np.all(np.abs(ug - uo)[~huge] <= atol + rtol * np.abs(uo[~huge]))
+    np.testing.assert_allclose(rg["uvengy"][:, 0], ro["uvengy"][:, 0], rtol=0, atol=helpers.self_tol(precision, len(w.solute["charge"])))
+    helpers.check_energies(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], precision, f"grid {grid}")
+    helpers.check_histograms(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], bins["uvcrd"], precision, f"grid {grid}")
     gpu.close()

@@ -90,3 +90,47 @@ def test_two_rank_merge_equals_single_process(tmp_path, mode, oracle, gpu_lib):
                                ref["voffset"] + sign * T * np.log(ref["avslf"]), rtol=0, atol=1e-9)
     np.testing.assert_allclose(merged["minuv"], ref["minuv"])
     np.testing.assert_allclose(merged["maxuv"], ref["maxuv"])
+
+
+def _bench_rank(rank, world, port, out):
+    """One rank of bench.py's distributed branch: its own frames (bench.frames_of_rank)
+    and the exchange (bench.merge_ranks, the product's engstore merge), with the oracle
+    standing in for the per-rank GPU engine."""
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, root)
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    import torch.distributed as dist
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import bench
+    w = _work("refs")
+    acc = _run_frames(w, bench.frames_of_rank(rank, 2))
+    res = bench.merge_ranks(acc, w)
+    if rank == 0:
+        np.savez(out, **{k: v for k, v in res.items() if v is not None})
+    else:
+        assert res is None
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_bench_distributed_branch_merge(tmp_path, oracle, gpu_lib):
+    out = str(tmp_path / "bench_merged.npz")
+    port = _free_port()
+    ctx = mp.get_context("spawn")
+    procs = [ctx.Process(target=_bench_rank, args=(r, 2, port, out)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(300)
+        assert p.exitcode == 0
+    import bench
+    from ermod_gb300 import engstore
+    assert bench.frames_of_rank(0, 2) == [0, 1] and bench.frames_of_rank(1, 2) == [2, 3]
+    merged = dict(np.load(out))
+    w = _work("refs")
+    single = _run_frames(w, [0, 1, 2, 3])
+    ref = engstore.merge([single], w.params["slttype"], w.params["wgtslf"], w.params["temp"])
+    np.testing.assert_allclose(merged["edens"], ref["edens"], rtol=1e-9, atol=1e-14)
+    np.testing.assert_allclose(merged["ecorr"], ref["ecorr"], rtol=1e-9, atol=1e-14)
+    assert merged["engsmpl"] == ref["engsmpl"] == 4 * 12

@@ -81,7 +81,9 @@ def test_two_species_match_oracle(gpu_lib, oracle, precision, mode):
     species, frame, placements, params, topo, bins = _inputs(mode)
     gpu = EnergyRepresentation(params, topo, bins, precision=precision)
     orc = oracle.Oracle(params, topo, bins)
-    atol, rtol = (1e-9, 1e-11) if precision == "fp64" else (1e-4, 2e-6)
+    n1 = int(bins["uvmax"][0])
+    nw, nm = 420, 40  # columns of the waters, then of the cosolvent molecules
+    uo_all = []
     for f in range(2):
         pos, cell = frame(f)
         orc.frame(pos, cell)
@@ -94,22 +96,24 @@ def test_two_species_match_oracle(gpu_lib, oracle, precision, mode):
             tag = [topo["nummol"]]
             ro, rg = orc.placements(tag), gpu.placements(tag, want_uvengy=True, want_flceng=True)
         ug, uo = rg["uvengy"][:, 1:], ro["uvengy"][:, 1:]
-        huge = np.abs(uo) >= 1e10
-        assert np.all(ug[huge] >= 1e10)
-        assert np.all(np.abs(ug - uo)[~huge] <= atol + rtol * np.abs(uo[~huge]))
-        np.testing.assert_allclose(rg["flceng"], ro["flceng"], rtol=2e-6 if precision == "mixed" else 1e-11,
-                                   atol=1e-3 if precision == "mixed" else 1e-8)
+        helpers.check_energies(rg["uvengy"], ro["uvengy"], precision, f"two species {mode}")
+        for cols, edges in ((slice(0, nw), bins["uvcrd"][:n1]), (slice(nw, nw + nm), bins["uvcrd"][n1:])):
+            helpers.check_histograms(ug[:, cols], uo[:, cols], edges, precision, f"two species {mode}")
+        # flceng: per species sums of the molecules' energies
+        atol = helpers.ENERGY_TOL[precision][0] * nw
+        np.testing.assert_allclose(rg["flceng"], ro["flceng"], rtol=helpers.ENERGY_TOL[precision][1], atol=atol)
+        uo_all.append(ro["uvengy"])
     ag, ao = gpu.accum(), orc.accum()
-    # wgtslf = 1: the weights follow the solute self energy, FP32-based on the mixed path
-    wtol = 1e-10 if precision == "fp64" else 5e-4
-    np.testing.assert_allclose(ag["engnorm"], ao["engnorm"], rtol=wtol)
-    n1 = int(bins["uvmax"][0])
+    # wgtslf = 1: the weights follow the solute self energy (solution mode: exp(+(u0 - voffset)/kT))
+    rtol_w = helpers.weight_rtol(precision, 8, params["temp"])  # the 8-site solute
+    np.testing.assert_allclose(ag["engnorm"], ao["engnorm"], rtol=rtol_w)
     for blk in (slice(0, n1), slice(n1, None)):  # the species blocks of edens
-        np.testing.assert_allclose(ag["edens"][blk].sum(), ao["edens"][blk].sum(), rtol=wtol)
+        np.testing.assert_allclose(ag["edens"][blk].sum(), ao["edens"][blk].sum(), rtol=rtol_w)
     if precision == "fp64":
         np.testing.assert_allclose(ag["edens"], ao["edens"], rtol=1e-10, atol=1e-12 * ao["engnorm"])
     for key in ("minuv", "maxuv"):
-        np.testing.assert_allclose(ag[key], ao[key], rtol=2e-6, atol=1e-4)
+        np.testing.assert_allclose(ag[key], ao[key], rtol=helpers.ENERGY_TOL[precision][1],
+                                   atol=helpers.ENERGY_TOL[precision][0])
     if mode == "soln":
-        np.testing.assert_allclose(ag["slnuv"], ao["slnuv"], rtol=wtol, atol=1e-3)
+        np.testing.assert_allclose(ag["slnuv"], ao["slnuv"], rtol=rtol_w, atol=atol * ao["engnorm"])
     gpu.close()

@@ -117,7 +117,6 @@ def test_droplet_gpu_matches_oracle(gpu_lib, oracle, precision):
     w, topo, bins = _droplet_inputs()
     gpu = EnergyRepresentation(w.params, topo, bins, precision=precision)
     orc = oracle.Oracle(w.params, topo, bins)
-    atol, rtol = (1e-9, 1e-11) if precision == "fp64" else (1e-4, 2e-6)
     edges = np.asarray(bins["uvcrd"])
     for f in range(3):
         pos, cell = w.frame(f)
@@ -126,9 +125,8 @@ def test_droplet_gpu_matches_oracle(gpu_lib, oracle, precision):
         gpu.frame(pos, cell)
         rg = gpu.placements([topo["nummol"]], want_uvengy=True)
         ug, uo = rg["uvengy"][0], ro["uvengy"][0]
-        assert np.all(np.abs(ug - uo) <= atol + rtol * np.abs(uo)), np.abs(ug - uo).max()
-        near = helpers.near_edge(uo[1:], edges, max(1e-6, 10 * atol))
-        assert np.array_equal(helpers.histogram(ug[1:][~near], edges), helpers.histogram(uo[1:][~near], edges))
+        helpers.check_energies(ug, uo, precision, "droplet")
+        helpers.check_histograms(ug[1:], uo[1:], edges, precision, "droplet")
     ag, ao = gpu.accum(), orc.accum()
     np.testing.assert_allclose(ag["engnorm"], ao["engnorm"], rtol=1e-12)
     np.testing.assert_allclose(ag["edens"].sum(), ao["edens"].sum(), rtol=1e-12)
@@ -162,10 +160,7 @@ def test_droplet_insertion_and_reach_errors(gpu_lib, oracle):
     orc = oracle.Oracle(p, topo_r, bins_r)
     orc.frame(pos, cell)
     ro = orc.placements(tag, pl)
-    ug, uo = rg["uvengy"], ro["uvengy"]
-    huge = np.abs(uo) >= 1e10  # overlapping pairs: both beyond the last edge
-    assert np.all(ug[huge] >= 1e10)
-    assert np.all(np.abs(ug - uo)[~huge] <= 1e-4 + 2e-6 * np.abs(uo[~huge]))
+    helpers.check_energies(rg["uvengy"], ro["uvengy"], "mixed", "droplet insertions")
     far = pl.copy()
     far[0] += 1.0e4
     with pytest.raises(_lib.ErmodError) as ei:

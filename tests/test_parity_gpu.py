@@ -1,11 +1,10 @@
 """GPU path vs the FP64 oracle, through the C ABI (marked gpu).
 
-Tolerances (per molecule energy, kcal/mol):
-  FP64 path   |u_gpu - u_oracle| <= 1e-9 + 1e-11 |u|
-  mixed path  |u_gpu - u_oracle| <= 1e-4 + 2e-6 |u| (FP32 pair terms of overlapping
-              pairs reach 1e10 kcal/mol, where only the relative error is meaningful)
-Histograms: bit-exact counts except molecules whose oracle energy lies within the
-observed error (at least 1e-6) of a bin edge; those are counted and reported.
+Tolerances: ``tests/helpers.py`` states them (per-molecule energies, the bin-edge band of
+the mixed path, solute self energies) and derives the bin-by-bin bounds of the weighted
+accumulators from them.  Histograms are exact for every molecule outside the band; the
+molecules within 1e-6 and within the band of an edge and those binned elsewhere are
+counted and printed.
 """
 import numpy as np
 import pytest
@@ -13,8 +12,6 @@ import pytest
 from tests import helpers
 
 pytestmark = pytest.mark.gpu
-
-TOL = {"fp64": (1e-9, 1e-11), "mixed": (1e-4, 0.0)}
 
 
 def _engines(gpu_lib, oracle, w, topo, bins, precision, **kw):
@@ -24,32 +21,32 @@ def _engines(gpu_lib, oracle, w, topo, bins, precision, **kw):
     return gpu, orc
 
 
-def _check_energies(u_gpu, u_orc, precision):
-    """Energies agree within TOL; overlapping pairs beyond 1e10 kcal/mol (above ecdmax,
-    the last bin in both) only need to stay beyond it."""
-    atol, rtol = TOL[precision]
-    if precision == "mixed":
-        rtol = 2e-6  # FP32 relative precision of large (core-region) energies
-    huge = np.abs(u_orc) >= 1e10
-    assert np.all(u_gpu[huge] >= 1e10)
-    err = np.where(huge, 0.0, np.abs(u_gpu - u_orc))
-    bound = atol + rtol * np.abs(np.where(huge, 0.0, u_orc))
-    worst = int(np.argmax(err - bound))
-    assert np.all(err <= bound), f"{precision}: max err {err.max():.3e} at {worst} (u={u_orc.flat[worst]:.6f})"
-    soft = np.abs(u_orc) < 20.0
-    return float(err[soft].max()) if np.any(soft) else 0.0
+def _check_energies(u_gpu, u_orc, precision, label=""):
+    return helpers.check_energies(u_gpu, u_orc, precision, label)[1]
 
 
-def _hist_compare(u_gpu, u_orc, edges, tol):
-    """Per placement: histograms of GPU vs oracle energies agree off the bin edges."""
-    flips = 0
-    for ug, uo in zip(u_gpu, u_orc):
-        near = helpers.near_edge(uo, edges, tol)
-        hg = helpers.histogram(ug[~near], edges)
-        ho = helpers.histogram(uo[~near], edges)
-        assert np.array_equal(hg, ho)
-        flips += int(np.count_nonzero(helpers.histogram(ug[near], edges) != helpers.histogram(uo[near], edges)))
-    return flips
+def _placement_weights(u0, engnorm, temp, wgtslf):
+    """Each placement's engnmfc of one cell (the volume and charge factors are common to
+    all placements, so the weights are exp(-(u0 - voffset)/kT) scaled to sum to engnorm)."""
+    e = np.exp(-(u0 - u0[0]) / temp) if wgtslf else np.ones_like(u0)
+    return engnorm * e / e.sum()
+
+
+def _check_weighted(ag, ao, u_orc, edges, w, corr=True, label=""):
+    """edens and ecorr bin by bin: the weights' relative error from the self energies,
+    plus the weight of every near-edge molecule that may sit in a neighbouring bin."""
+    precision = "mixed"
+    ns = len(w.solute["charge"])
+    rtol_w = helpers.weight_rtol(precision, ns, w.params["temp"])
+    wts = _placement_weights(u_orc[:, 0], ao["engnorm"], w.params["temp"], w.params["wgtslf"])
+    b_ed, b_ec = helpers.weighted_bounds(u_orc[:, 1:], wts, edges, helpers.MIXED_BAND, rtol_w, corr=corr)
+    d_ed = np.abs(ag["edens"] - ao["edens"])
+    assert np.all(d_ed <= b_ed + 1e-12 * np.abs(ao["edens"])), f"{label}: edens bin {int(np.argmax(d_ed - b_ed))}"
+    if corr:
+        d_ec = np.abs(ag["ecorr"] - ao["ecorr"])
+        assert np.all(d_ec <= b_ec + 1e-12 * np.abs(ao["ecorr"])), f"{label}: ecorr entry {np.unravel_index(int(np.argmax(d_ec - b_ec)), d_ec.shape)}"
+    np.testing.assert_allclose(ag["engnorm"], ao["engnorm"], rtol=rtol_w)
+    np.testing.assert_allclose(ag["voffset"], ao["voffset"], atol=helpers.self_tol(precision, ns))
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -59,28 +56,30 @@ def test_soln_small_frames(gpu_lib, oracle, precision):
     topo, bins = helpers.build_inputs(w)
     gpu, orc = _engines(gpu_lib, oracle, w, topo, bins, precision)
     tag = [topo["nummol"]]
-    errs = []
+    ug_all, uo_all = [], []
     for f in range(3):
         pos, cell = w.frame(f)
         orc.frame(pos, cell)
         ro = orc.placements(tag)
         gpu.frame(pos, cell)
         rg = gpu.placements(tag, want_uvengy=True, want_flceng=True)
-        errs.append(_check_energies(rg["uvengy"], ro["uvengy"], precision))
-        np.testing.assert_allclose(rg["flceng"], ro["flceng"], atol=TOL[precision][0] * topo["nummol"], rtol=1e-9)
-    ag, ao = gpu.accum(), orc.accum()
+        _check_energies(rg["uvengy"], ro["uvengy"], precision, "soln_small")
+        np.testing.assert_allclose(rg["flceng"], ro["flceng"], atol=helpers.ENERGY_TOL[precision][0] * topo["nummol"],
+                                   rtol=1e-9)
+        ug_all.append(rg["uvengy"][:, 1:])
+        uo_all.append(ro["uvengy"][:, 1:])
     edges = bins["uvcrd"]
-    if precision == "fp64":
+    rep = helpers.check_histograms(np.concatenate(ug_all), np.concatenate(uo_all), edges, precision, "soln_small")
+    ag, ao = gpu.accum(), orc.accum()
+    if precision == "fp64" or rep["other_bin"] == 0:
         np.testing.assert_array_equal(ag["edens"], ao["edens"])
-    else:
-        np.testing.assert_allclose(ag["edens"].sum(), ao["edens"].sum(), rtol=1e-12)
     for k in ("engnorm", "engsmpl", "avslf"):
         np.testing.assert_allclose(ag[k], ao[k], rtol=1e-12)
-    np.testing.assert_allclose(ag["minuv"], ao["minuv"], atol=TOL[precision][0])
-    np.testing.assert_allclose(ag["maxuv"], ao["maxuv"], atol=TOL[precision][0])
+    np.testing.assert_allclose(ag["minuv"], ao["minuv"], atol=helpers.ENERGY_TOL[precision][0])
+    np.testing.assert_allclose(ag["maxuv"], ao["maxuv"], atol=helpers.ENERGY_TOL[precision][0])
     # slnuv = sum of flceng * engnmfc (engnmfc = V here): the per-molecule tolerance summed
     np.testing.assert_allclose(ag["slnuv"], ao["slnuv"], rtol=0,
-                               atol=3 * topo["nummol"] * TOL[precision][0] * ag["engnorm"] / 3)
+                               atol=topo["nummol"] * helpers.ENERGY_TOL[precision][0] * ag["engnorm"])
     gpu.close()
 
 
@@ -98,11 +97,10 @@ def test_refs_unit_weights_exact_counts(gpu_lib, oracle, precision):
     ro = orc.placements(tag, pl)
     gpu.frame(pos, cell)
     rg = gpu.placements(tag, pl, want_uvengy=True)
-    err = _check_energies(rg["uvengy"], ro["uvengy"], precision)
+    _check_energies(rg["uvengy"], ro["uvengy"], precision, "refs unit weights")
     edges = bins["uvcrd"]
     ug, uo = rg["uvengy"][:, 1:], ro["uvengy"][:, 1:]
-    tol = max(1e-6, 2 * err)
-    _hist_compare(ug, uo, edges, tol)
+    rep = helpers.check_histograms(ug, uo, edges, precision, "refs unit weights")
     ag, ao = gpu.accum(with_count=True), orc.accum()
     # device binning == host binning of the device's own energies
     hist_gpu = sum(helpers.histogram(u, edges) for u in ug)
@@ -113,18 +111,23 @@ def test_refs_unit_weights_exact_counts(gpu_lib, oracle, precision):
         counts += np.outer(h, h)
     np.testing.assert_array_equal(ag["ecorr_count"], counts)
     np.testing.assert_array_equal(ag["ecorr"], counts.astype(float))
-    if precision == "fp64":
+    if precision == "fp64" or rep["other_bin"] == 0:
         np.testing.assert_array_equal(ag["edens"], ao["edens"])
         np.testing.assert_array_equal(ag["ecorr"], ao["ecorr"])
+    else:  # unit weights: the bounds are the near-edge molecules' counts
+        _check_weighted(ag, ao, ro["uvengy"], edges, w, label="refs unit weights")
     gpu.close()
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_refs_weighted_accumulators(gpu_lib, oracle, precision):
-    """REFS defaults: wgtslf = 1, NPT; weights exp(-(u0 - voffset)/kT) V."""
+    """REFS defaults: wgtslf = 1, NPT; weights exp(-(u0 - voffset)/kT) V.  edens and ecorr
+    are compared bin by bin (mixed: within the bounds the energy band and the self-energy
+    tolerance give)."""
     w = helpers.small_refs()
     topo, bins = helpers.build_inputs(w)
     gpu, orc = _engines(gpu_lib, oracle, w, topo, bins, precision, batch=16)
+    uo_all = []
     for f in range(2):
         pos, cell = w.frame(f)
         pl = w.placements(f, 40)
@@ -133,20 +136,22 @@ def test_refs_weighted_accumulators(gpu_lib, oracle, precision):
         ro = orc.placements(tag, pl)
         gpu.frame(pos, cell)
         rg = gpu.placements(tag, pl, want_uvengy=True)
-        _check_energies(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], precision)
+        _check_energies(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], precision, "refs weighted")
+        helpers.check_histograms(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], bins["uvcrd"], precision, "refs weighted")
         # the solute self energy decides the weights
-        np.testing.assert_allclose(rg["uvengy"][:, 0], ro["uvengy"][:, 0], atol=1e-9 if precision == "fp64" else 2e-4)
+        np.testing.assert_allclose(rg["uvengy"][:, 0], ro["uvengy"][:, 0], rtol=0,
+                                   atol=helpers.self_tol(precision, len(w.solute["charge"])))
+        uo_all.append(ro["uvengy"])
     ag, ao = gpu.accum(), orc.accum()
-    rtol = 1e-10 if precision == "fp64" else 5e-4
-    np.testing.assert_allclose(ag["voffset"], ao["voffset"], atol=1e-9 if precision == "fp64" else 2e-4)
-    np.testing.assert_allclose(ag["engnorm"], ao["engnorm"], rtol=rtol)
     np.testing.assert_allclose(ag["avslf"], ao["avslf"], rtol=1e-12)
     assert ag["engsmpl"] == ao["engsmpl"] == 80
-    np.testing.assert_allclose(ag["edens"].sum(), ao["edens"].sum(), rtol=rtol)
-    np.testing.assert_allclose(ag["ecorr"].sum(), ao["ecorr"].sum(), rtol=rtol)
     if precision == "fp64":
+        np.testing.assert_allclose(ag["voffset"], ao["voffset"], atol=1e-9)
+        np.testing.assert_allclose(ag["engnorm"], ao["engnorm"], rtol=1e-10)
         np.testing.assert_allclose(ag["edens"], ao["edens"], rtol=1e-10, atol=0)
         np.testing.assert_allclose(ag["ecorr"], ao["ecorr"], rtol=1e-10, atol=0)
+    else:
+        _check_weighted(ag, ao, np.concatenate(uo_all), bins["uvcrd"], w, label="refs weighted")
     gpu.close()
 
 
@@ -272,8 +277,9 @@ def test_compile_time_grid_sizes(gpu_lib, oracle, K, order):
     ro = orc.placements(tag, pl)
     gpu.frame(pos, cell)
     rg = gpu.placements(tag, pl, want_uvengy=True)
-    _check_energies(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], "mixed")
-    np.testing.assert_allclose(rg["uvengy"][:, 0], ro["uvengy"][:, 0], rtol=1e-6, atol=1e-4)
+    _check_energies(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], "mixed", f"K={K} order {order}")
+    helpers.check_histograms(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], bins["uvcrd"], "mixed", f"K={K} order {order}")
+    np.testing.assert_allclose(rg["uvengy"][:, 0], ro["uvengy"][:, 0], rtol=0, atol=helpers.self_tol("mixed", len(w.solute["charge"])))
     gpu.close()
 
 

@@ -3,8 +3,9 @@
 The engine's ecorr for unit-weight REFS placements with per-placement solute weights
 is sum_p w_p h_p h_p^T, with h_p the histogram of placement p's energies.  The same
 histograms, built on the host from the engine's uvengy, go through the no-allocation
-entry point twice in a row (its fixed scratch is reused), and once split in two calls
-that accumulate into one matrix.  Sums run over placements in the same order as the
+entry point twice in a row (its fixed scratch is reused), once more with the device's
+free memory read before and after (a warmed call allocates nothing), and once split in
+two calls that accumulate into one matrix.  Sums run over placements in the same order as the
 engine's, so the tolerance is a few ulps.
 """
 import numpy as np
@@ -58,6 +59,18 @@ def test_ecorr_noalloc_matches_engine(gpu_lib):
         torch.cuda.synchronize(dev)
         np.testing.assert_allclose(ecorr.cpu().numpy(), ref_ecorr, rtol=1e-13, atol=0, err_msg=f"call {call}")
         np.testing.assert_array_equal(count.cpu().numpy(), ref_count)
+    # a warmed call allocates nothing: the device's free memory (cudaMemGetInfo) is the
+    # same before and after it
+    ecorr.zero_()
+    count.zero_()
+    torch.cuda.synchronize(dev)
+    free0, _ = torch.cuda.mem_get_info(dev)
+    st = f(d_hist.data_ptr(), d_w.data_ptr(), n, ermax, ecorr.data_ptr(), count.data_ptr(), stream)
+    assert st == _lib.OK
+    torch.cuda.synchronize(dev)
+    free1, _ = torch.cuda.mem_get_info(dev)
+    assert free1 == free0, f"free device memory changed by {free0 - free1} bytes"
+    np.testing.assert_array_equal(count.cpu().numpy(), ref_count)
     # two calls accumulating into one matrix, without the count mirror
     ecorr = torch.zeros((ermax, ermax), dtype=torch.float64, device=dev)
     h = n // 2
