@@ -62,6 +62,19 @@ def dist_env():
     return ws, rank, local
 
 
+def frames_of_rank(rank, nsteps):
+    """The frames rank `rank` processes (weak scaling: every rank its own nsteps frames,
+    the reference's plmode = 2 frame sharding)."""
+    return [rank * nsteps + i for i in range(nsteps)]
+
+
+def merge_ranks(acc, w):
+    """engstore's exchange over the ranks (engproc.F90:475-546): rank 0 receives the
+    merged, normalised distributions (ermod_engstore_merge); other ranks None."""
+    from ermod_gb300 import engstore
+    return engstore.merge_distributed(acc, w.params["slttype"], w.params["wgtslf"], w.params["temp"])
+
+
 class ClockSampler:
     """nvidia-smi samples (200 ms) of one GPU while the timed region runs, written as CSV to
     $ERMOD_CLOCK_LOG_DIR/clocks_<pid>.csv when that variable is set (else a temporary file)."""
@@ -143,9 +156,22 @@ def make_workload(args):
     return w
 
 
-def cpu_oracle_rate(w, topo, bins, nplace, frame_index=0):
-    """The FP64 oracle on nplace placements of one frame, all host cores (solution mode:
-    the frame's own solute, once)."""
+def workload_config(w, args, ws=1):
+    """The `config` object of both arms: the same workload named the same way."""
+    K = w.params["ms1max"]
+    soln = w.mode == "soln"
+    return {"workload": f"{w.name}: {w.nwater} waters, {w.box} A box, PME {K}^3 order {w.params['splodr']}, "
+                        f"{len(w.solute['charge'])}-site solute, "
+                        + ("solution mode" if soln else f"{w.ins_per_frame} insertions/frame")
+                        + (", ecorr on" if w.params.get("corrcal") else ""),
+            "batch": args.batch, "l2": "flushed between steps (256 MiB write)",
+            "parallelism": f"frames sharded over {ws} GPU(s)" if ws > 1 else "1 GPU"}
+
+
+def cpu_oracle_rate(w, topo, bins, nplace, frame_index=0, want_uvengy=False, placements=None):
+    """The FP64 oracle on nplace placements of one frame (the given ones, else the first
+    nplace of the frame's own draw), all host cores (solution mode: the frame's own
+    solute, once).  Returns (rate, seconds, uvengy or None)."""
     from oracle import oracle as O
     O.build()
     orc = O.Oracle(w.params, topo, bins)
@@ -153,29 +179,64 @@ def cpu_oracle_rate(w, topo, bins, nplace, frame_index=0):
     orc.frame(pos, cell)
     if w.mode == "soln":
         nplace = 1
-    pl = None if w.mode == "soln" else w.placements(frame_index, nplace)
+    if w.mode == "soln":
+        pl = None
+    elif placements is not None:
+        pl = np.ascontiguousarray(placements[:nplace])
+    else:
+        pl = w.placements(frame_index, w.ins_per_frame)[:nplace]
     tag = np.full(nplace, topo["nummol"], np.int32)
     t0 = time.perf_counter()
-    orc.placements(tag, pl, want_uvengy=False, nthreads=0)
+    r = orc.placements(tag, pl, want_uvengy=want_uvengy, nthreads=0)
     dt = time.perf_counter() - t0
     orc.close()
-    return nplace * w.nwater / dt, dt
+    return nplace * w.nwater / dt, dt, (r["uvengy"] if want_uvengy else None)
+
+
+# The mixed path's stated per-molecule error bound against the FP64 oracle (kcal/mol): the
+# band around each bin edge within which a molecule may take the neighbouring bin.
+MIXED_BAND = 3e-5
+
+
+def accuracy_report(u_gpu, u_orc, edges, band=MIXED_BAND):
+    """Per-molecule error of the GPU energies against the oracle's on the same placements,
+    molecules near a bin edge (within 1e-6 and within the stated band) and molecules that
+    the GPU bins elsewhere."""
+    ug, uo = u_gpu[:, 1:], u_orc[:, 1:]
+    err = np.abs(ug - uo)
+    soft = np.abs(uo) < 20.0
+    near6 = near = flips = 0
+    for a, b in zip(ug, uo):
+        idx = np.searchsorted(edges, b)
+        dlo = np.abs(b - edges[np.clip(idx - 1, 0, len(edges) - 1)])
+        dhi = np.abs(b - edges[np.clip(idx, 0, len(edges) - 1)])
+        d = np.minimum(dlo, dhi)
+        near6 += int(np.count_nonzero(d <= 1e-6))
+        near += int(np.count_nonzero(d <= band))
+        flips += int(np.count_nonzero(np.searchsorted(edges, a, side="left") != np.searchsorted(edges, b, side="left")))
+    return {"molecules": int(uo.size), "max_abs_err": float(err.max()),
+            "max_abs_err_soft": float(err[soft].max()) if soft.any() else 0.0,
+            "max_rel_err": float((err / np.maximum(np.abs(uo), 1e-300)).max()),
+            "self_energy_max_abs_err": float(np.abs(u_gpu[:, 0] - u_orc[:, 0]).max()),
+            "band": band, "near_edge_1e-6": near6, "near_edge_band": near, "other_bin": flips}
 
 
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    from ermod_gb300 import setconf
+    # the topology and bins from the oracle's own restatement of setconf/enginit, so that
+    # this arm loads nothing of the GPU library
+    from oracle import oracle as O
     w = make_workload(args)
-    topo = setconf.setparam_topology(w.species(), slttype=w.params["slttype"])
-    bins = setconf.enginit_bins(topo["numslv"], w.hist)
+    topo = O.setparam_topology(w.species(), slttype=w.params["slttype"])
+    bins = O.enginit_bins(topo["numslv"], w.hist)
     sample = 1 if w.mode == "soln" else max(1, args.cpu_sample // 4)  # solution mode: the frame's solute
     for i in range(args.warmup):
         cpu_oracle_rate(w, topo, bins, max(1, sample // 4), i)
     t_total, units = 0.0, 0
     for i in range(args.steps):
-        rate, dt = cpu_oracle_rate(w, topo, bins, sample, i)
+        rate, dt, _ = cpu_oracle_rate(w, topo, bins, sample, i)
         t_total += dt
         units += sample * w.nwater
     value = units / t_total
@@ -185,12 +246,11 @@ def run_reference(args):
         "unit": "molecule-energies/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * t_total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"{w.name}: {w.nwater} waters, {w.box} A box, PME {w.params['ms1max']}^3, "
-                               f"{len(w.solute['charge'])}-site solute, {w.ins_per_frame} insertions/frame",
-                   "sample": f"{sample} insertions of one frame per step"},
+        "config": workload_config(w, args, ws),
         "cpu_baseline": {"value": value, "unit": "molecule-energies/s", "cores": cores, "kind": "port",
-                         "sample": f"{sample} insertions x {args.steps} steps, FP64 oracle restating the "
-                                   f"Fortran reference (which cannot be built here), OpenMP over insertions"},
+                         "sample": f"{sample} insertions of one frame per step x {args.steps} steps, FP64 "
+                                   f"oracle restating the Fortran reference (which cannot be built here), "
+                                   f"OpenMP over insertions on all {cores} host cores"},
         "e2e": {"value": value, "unit": "molecule-energies/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -212,12 +272,12 @@ def run_ours(args):
     topo = setconf.setparam_topology(w.species(), slttype=w.params["slttype"])
     bins = setconf.enginit_bins(topo["numslv"], w.hist)
     nplace = w.ins_per_frame
-    nsite_u = len(w.solute["charge"])
     nsteps = args.warmup + args.steps
     # frames of this rank (weak scaling: every rank its own frames)
-    frames = [w.frame(rank * nsteps + i) for i in range(nsteps)]
+    fidx = frames_of_rank(rank, nsteps)
+    frames = [w.frame(i) for i in fidx]
     soln = w.mode == "soln"  # solution mode: the solute is the frame's own molecule
-    places = None if soln else [w.placements(rank * nsteps + i, nplace) for i in range(nsteps)]
+    places = None if soln else [w.placements(i, nplace) for i in fidx]
     tag_h = np.full(nplace, topo["nummol"], np.int32)
     cell = frames[0][1]
 
@@ -264,6 +324,8 @@ def run_ours(args):
     if ws > 1:
         torch.distributed.all_reduce(t_local, op=torch.distributed.ReduceOp.MAX)
     ms_max = float(t_local.item())
+    if ws > 1:  # the path's one exchange: engstore's merge of every rank's accumulators
+        merge_ranks(eng.accum(), w)
     units = nplace * w.nwater * args.steps * ws
     value = units / (ms_max / 1000.0)
 
@@ -330,12 +392,20 @@ def run_ours(args):
         plain = {"value": n * w.nwater / dt, "unit": "molecule-energies/s", "sample": f"{n} placements, frame 0",
                  "dtype": "f64"}
 
-    cpu = None
+    cpu = accuracy = None
     if rank == 0 and not args.no_cpu:
         ncpu = 1 if soln else args.cpu_sample
-        rate, dt = cpu_oracle_rate(w, topo, bins, ncpu, 0)
+        rate, dt, u_orc = cpu_oracle_rate(w, topo, bins, ncpu, fidx[0], want_uvengy=True,
+                                          placements=None if soln else places[0])
         cpu = {"value": rate, "unit": "molecule-energies/s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"{ncpu} placements of frame 0 ({dt:.2f} s), FP64 oracle, OpenMP"}
+        # the same placements on the mixed path, checked against the oracle's energies
+        eng3 = EnergyRepresentation(w.params, topo, bins, precision="mixed", device=local, batch=args.batch)
+        eng3.frame(frames[0][0], cell)
+        u_gpu = eng3.placements(tag_h[:ncpu], None if soln else places[0][:ncpu], want_uvengy=True)["uvengy"]
+        eng3.close()
+        accuracy = accuracy_report(u_gpu, u_orc, bins["uvcrd"])
+        accuracy["sample"] = f"{ncpu} placements of frame 0 against the FP64 oracle"
 
     if rank == 0:
         line = {
@@ -343,12 +413,8 @@ def run_ours(args):
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic",
-            "config": {"workload": f"{w.name}: {w.nwater} waters, {w.box} A box, PME {K}^3 order "
-                                   f"{w.params['splodr']}, {nsite_u}-site solute, "
-                                   + (f"solution mode" if soln else f"{nplace} insertions/frame")
-                                   + (", ecorr on" if w.params.get("corrcal") else ""), "batch": args.batch, "l2": "flushed between steps (256 MiB write)",
-                       "parallelism": f"frames sharded over {ws} GPU(s)" if ws > 1 else "1 GPU"},
-            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "plain_fp64_gpu": plain,
+            "config": workload_config(w, args, ws),
+            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "accuracy": accuracy, "plain_fp64_gpu": plain,
             "gpu_launches": int(launches), "clocks": clocks,
         }
         print(json.dumps(line))
