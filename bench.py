@@ -205,6 +205,7 @@ def accuracy_report(u_gpu, u_orc, edges, band=MIXED_BAND):
     ug, uo = u_gpu[:, 1:], u_orc[:, 1:]
     err = np.abs(ug - uo)
     soft = np.abs(uo) < 20.0
+    hard = np.abs(uo) >= 1e3
     near6 = near = flips = 0
     for a, b in zip(ug, uo):
         idx = np.searchsorted(edges, b)
@@ -214,9 +215,10 @@ def accuracy_report(u_gpu, u_orc, edges, band=MIXED_BAND):
         near6 += int(np.count_nonzero(d <= 1e-6))
         near += int(np.count_nonzero(d <= band))
         flips += int(np.count_nonzero(np.searchsorted(edges, a, side="left") != np.searchsorted(edges, b, side="left")))
-    return {"molecules": int(uo.size), "max_abs_err": float(err.max()),
+    return {"molecules": int(uo.size), "max_abs_err_below_1e3": float(err[~hard].max()) if (~hard).any() else 0.0,
             "max_abs_err_soft": float(err[soft].max()) if soft.any() else 0.0,
-            "max_rel_err": float((err / np.maximum(np.abs(uo), 1e-300)).max()),
+            "max_rel_err_above_1e3": float((err[hard] / np.abs(uo[hard])).max()) if hard.any() else 0.0,
+            "max_abs_energy": float(np.abs(uo).max()),
             "self_energy_max_abs_err": float(np.abs(u_gpu[:, 0] - u_orc[:, 0]).max()),
             "band": band, "near_edge_1e-6": near6, "near_edge_band": near, "other_bin": flips}
 
@@ -474,6 +476,22 @@ def run_uneven(args):
         ms = _timed(step, args.steps, args.warmup, stream)
     g.sync()
     units = sum(w.ins_per_frame * w.nwater for w in systems) * args.steps
+    cpu = accuracy = None
+    if not args.no_cpu:  # one system of the set (the median size) on the oracle, and the GPU on the same sample
+        k = int(np.argsort([w.nwater for w in systems])[len(systems) // 2])
+        w, topo = systems[k], tops[k]
+        bins = setconf.enginit_bins(topo["numslv"], w.hist)
+        n = max(8, args.cpu_sample // 4)
+        rate, dt, u_orc = cpu_oracle_rate(w, topo, bins, n, 1, want_uvengy=True, placements=places[k])
+        cpu = {"value": rate, "unit": "molecule-energies/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"system {k} ({w.nwater} waters, PME {w.params['ms1max']}^3): {n} placements ({dt:.2f} s), "
+                         f"FP64 oracle, OpenMP"}
+        eng = EnergyRepresentation(w.params, topo, bins, precision="mixed", batch=batches[k])
+        eng.frame(*frames[k])
+        u_gpu = eng.placements(np.full(n, topo["nummol"], np.int32), places[k][:n], want_uvengy=True)["uvengy"]
+        eng.close()
+        accuracy = accuracy_report(u_gpu, u_orc, bins["uvcrd"])
+        accuracy["sample"] = cpu["sample"]
     line = {"metric": "solute-solvent molecule energies/s", "value": units / (ms / 1e3),
             "unit": "molecule-energies/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -483,7 +501,7 @@ def run_uneven(args):
                        "systems": [{"waters": w.nwater, "K": w.params["ms1max"], "insertions": w.ins_per_frame,
                                     "solute_sites": len(w.solute["charge"]), "batch": b}
                                    for w, b in zip(systems, batches)]},
-            "clocks": clk.summary()}
+            "clocks": clk.summary(), "cpu_baseline": cpu, "accuracy": accuracy}
     print(json.dumps(line))
     g.close()
     for e in engines:
@@ -537,11 +555,31 @@ def run_adjoint(args):
         pos, cl = w.frame(0)
         t0 = time.perf_counter()
         orc.frame(pos, cl)
-        orc.placements([topo["nummol"]])
-        orc.adjoint(topo["nummol"])
+        u_orc = orc.placements([topo["nummol"]])["uvengy"]
+        du = orc.adjoint(topo["nummol"])
         dt = time.perf_counter() - t0
         line["cpu_baseline"] = {"value": w.nwater / dt, "unit": "molecule-energies/s", "cores": os.cpu_count(),
                                 "kind": "port", "sample": "1 frame: energies + analytic FP64 derivatives"}
+        # the same frame on the GPU: energies, and the bin-resolved derivatives against the
+        # oracle's per-molecule derivatives binned by the GPU's energies
+        eng = EnergyRepresentation(w.params, topo, bins, precision="mixed")
+        eng.adjoint_enable()
+        eng.frame(pos, cl)
+        u_gpu = eng.placements([topo["nummol"]], want_uvengy=True)["uvengy"]
+        grad, wt = eng.adjoint_get()
+        eng.close()
+        acc = accuracy_report(u_gpu, u_orc, bins["uvcrd"])
+        edges = np.asarray(bins["uvcrd"])
+        b = np.searchsorted(edges, u_gpu[0, 1:-1], side="left") - 1  # the solute itself is the last molecule
+        ref = np.zeros_like(grad)
+        mag = np.zeros_like(grad)
+        np.add.at(ref.T, b, du[:-1])
+        np.add.at(mag.T, b, np.abs(du[:-1]))
+        C = wt.sum() / max(len(b), 1)  # every molecule's weight: the volume factor
+        occ = mag > 0
+        acc["gradient_max_rel_err"] = float((np.abs(grad / C - ref)[occ] / mag[occ]).max())
+        acc["sample"] = "frame 0 against the FP64 oracle (energies and the oracle's analytic gradient)"
+        line["accuracy"] = acc
     print(json.dumps(line))
 
 

@@ -135,6 +135,28 @@ __host__ __device__ inline int ordered_key32(float f) {
   return k ^ ((k >> 31) & 0x7fffffff);
 }
 
+#ifdef __CUDACC__
+// float of an ordered 32-bit key (the inverse of ordered_key32)
+__device__ __forceinline__ float key32_to_float(int k) { return __int_as_float(k ^ ((k >> 31) & 0x7fffffff)); }
+
+// ordered 64-bit key of a float-float number (hi, lo): hi first, then lo; the order of
+// the keys is the order of the values hi + lo.  The mixed finish kernel keeps its
+// per-species minimum and maximum energies as such keys; the reduce kernel decodes them.
+__device__ __forceinline__ long long ff_key(float hi, float lo) {
+  return (long long)(((unsigned long long)(unsigned)ordered_key32(hi) << 32) |
+                     (unsigned long long)((unsigned)ordered_key32(lo) ^ 0x80000000u));
+}
+constexpr long long kFfKeyNone = 0x7fffffffffffffffll;        // min over no molecule
+constexpr long long kFfKeyNoneMax = (long long)0x8000000000000000ull;  // max over no molecule
+__device__ __forceinline__ double ff_key_to_double(long long k) {
+  if (k == kFfKeyNone) return HUGE_VAL;
+  if (k == kFfKeyNoneMax) return -HUGE_VAL;
+  const float hi = key32_to_float((int)(k >> 32));
+  const float lo = key32_to_float((int)((unsigned)k ^ 0x80000000u));
+  return (double)hi + (double)lo;
+}
+#endif
+
 struct FrameGeom {
   double L[3];       // cell lengths (cuboid cell)
   double invL[3];    // 1 / L as dtrtri computes it

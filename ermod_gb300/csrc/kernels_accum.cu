@@ -28,6 +28,7 @@ struct AccArgs {
   double screen;                // residual_ene(slt, slt) = -(pi Q Q / beta / beta / V) / 2
   double stat_weight_system;
   int bare;      // cltype 0: no reciprocal self energy, no residual, volcorrect without its factor
+  int ff_keys;   // the tile partials' min and max are ordered float-float keys (mixed path)
   double* scal;  // {engnorm, engsmpl, avslf, voffset, voffset_init, usreal, usreal_valid}
   double* edens;
   double* eself;
@@ -79,8 +80,14 @@ __global__ void __launch_bounds__(kAccThreads) reduce_kernel(AccArgs A) {
     const double s = block_sum_fixed(red, base, A.ntile, stride);
     double mn = INFINITY, mx = -INFINITY;
     for (int t = threadIdx.x; t < A.ntile; t += blockDim.x) {
-      mn = fmin(mn, base[(size_t)t * stride + 1]);
-      mx = fmax(mx, base[(size_t)t * stride + 2]);
+      const double* pt = base + (size_t)t * stride;
+      if (A.ff_keys) {
+        mn = fmin(mn, ff_key_to_double(reinterpret_cast<const long long*>(pt)[1]));
+        mx = fmax(mx, ff_key_to_double(reinterpret_cast<const long long*>(pt)[2]));
+      } else {
+        mn = fmin(mn, pt[1]);
+        mx = fmax(mx, pt[2]);
+      }
     }
     red[threadIdx.x] = mn;
     __syncthreads();
@@ -561,6 +568,7 @@ cudaError_t launch_accumulate(Engine& e, const BatchArgs& a, cudaStream_t s) {
   A.temp = e.P.temp;
   A.volume = e.geom.volume;
   A.bare = (e.P.cltype == 0) ? 1 : 0;
+  A.ff_keys = e.mixed ? 1 : 0;
   A.volfac = A.bare ? 0.0  // volcorrect multiplies by the volume only (engproc.F90:871-887)
                     : kPi * (e.total_charge_phys * e.total_charge_phys) / (e.P.screen * e.P.screen) / e.geom.volume / 2.0;
   A.screen = e.P.screen;

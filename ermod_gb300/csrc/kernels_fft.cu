@@ -526,8 +526,10 @@ __global__ void __launch_bounds__(kPmeAThreads, kPmeAMinBlocks) pme_a_kernel(Pme
     ff o{__shfl_down_sync(0xffffffffu, self.hi, off), __shfl_down_sync(0xffffffffu, self.lo, off)};
     self = ff_add2(self, o);
   }
-  __shared__ double wsum[kPmeAThreads / 32];
-  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = (double)self.hi + (double)self.lo;
+  // the warps' float-float sums, combined in FP32 by one thread: an FP64 instruction costs
+  // GB300 as much as 64 FP32 ones, so the CTA converts to FP64 once
+  __shared__ float2 wsum[kPmeAThreads / 32];
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = make_float2(self.hi, self.lo);
   // ---- inverse transform along k3 (columns k1, element stride Hp); the last pass
   // writes T1[b][z][k2][k1] ----
   float2* out = A.t1 + (size_t)b * K3 * A.K2 * H + (size_t)k2 * H;
@@ -541,9 +543,9 @@ __global__ void __launch_bounds__(kPmeAThreads, kPmeAMinBlocks) pme_a_kernel(Pme
     fft_cols_io(slab, Hp, 1, work, slab, A.p3, H, A.fH, Hp, 1, out, A.K2 * H, 1, tw3);
   }
   if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += wsum[w];
-    A.self_part[(size_t)b * A.K2 + k2] = t;
+    ff t{0.f, 0.f};
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = ff_add2(t, ff{wsum[w].x, wsum[w].y});
+    A.self_part[(size_t)b * A.K2 + k2] = ff_to_double(t);
   }
 }
 

@@ -285,18 +285,20 @@ __device__ __forceinline__ void hist_add(int* h, int bin) {
   if ((threadIdx.x & 31) == leader) atomicAdd(&h[bin], __popc(peers));
 }
 
-// FP32 pair terms larger than this (kcal/mol) are recomputed in FP64.  Below it an FP32
-// term is within a few units in the last place (6 for the sigma^12 of the LJ term), about
-// 5e-6 kcal/mol; above it the FP32 rounding, and the fixed-point quantisation of the
-// displacement (2.3e-8 A at L = 99.5 A), would grow with the term up to the 1e10 kcal/mol
-// of overlapping pairs.
-constexpr float kFp64Term = 8.0f;
+// FP32 pair terms larger than these (kcal/mol) are recomputed in FP64.  Below them an
+// FP32 term is within a few units in the last place (the LJ term's sigma^12 amplifies the
+// distance's rounding 6-fold; erfcf is within 4 ulp), 5e-6 kcal/mol at most; above them the
+// FP32 rounding, and the fixed-point quantisation of the displacement (2.3e-8 A at
+// L = 99.5 A), would grow with the term up to the 1e10 kcal/mol of overlapping pairs.
+constexpr float kFp64Lj = 8.0f;
+constexpr float kFp64Coulomb = 16.0f;
+constexpr int kPairLj = 1, kPairCoulomb = 2;  // the parts of a pair evaluated in FP64
 
-// one solute-solvent site pair in FP64, as the FP64 path computes it: minimum image of
-// the FP64 wrapped coordinates (realcal.F90:202-209), LJ with the switch form
+// parts of one solute-solvent site pair in FP64, as the FP64 path computes them: minimum
+// image of the FP64 wrapped coordinates (realcal.F90:202-209), LJ with the switch form
 // (realcal.F90:686-770) and the screened or bare Coulomb term (realcal.F90:771-782, 245)
 __device__ __forceinline__ double pair_fp64(const MolArgs& A, int idx, const double* __restrict__ ux, double qu,
-                                         int tu) {
+                                         int tu, int parts) {
   double dist = 0.0;
   for (int i = 0; i < 3; ++i) {
     const double h = 0.5 * A.g.L[i];
@@ -307,18 +309,20 @@ __device__ __forceinline__ double pair_fp64(const MolArgs& A, int idx, const dou
   const int tv = A.site_pos[idx].w;
   double e = 0.0;
   const double ljeps = A.ljene[tv + A.T * tu];
-  if (ljeps > 0) {
+  if ((parts & kPairLj) && ljeps > 0) {
     const double sg2 = A.ljlensq[tv + A.T * tu];
     if (dist <= A.k64.lw2)
       e += lj_low64(A.ljswitch, A.k64, ljeps, sg2, dist);
     else if (dist <= A.k64.up2)
       e += lj_switch64(A.ljswitch, A.k64, ljeps, sg2, dist);
   }
-  if (A.bare) {
-    if (dist < A.k64.ele2) e += qu * A.site_q[idx] / sqrt(dist);
-  } else if (dist <= A.k64.ele2) {
-    const double r = sqrt(dist);
-    e += qu * A.site_q[idx] * (1.0 - erf(A.screen * r)) / r;
+  if (parts & kPairCoulomb) {
+    if (A.bare) {
+      if (dist < A.k64.ele2) e += qu * A.site_q[idx] / sqrt(dist);
+    } else if (dist <= A.k64.ele2) {
+      const double r = sqrt(dist);
+      e += qu * A.site_q[idx] * (1.0 - erf(A.screen * r)) / r;
+    }
   }
   return e;
 }
@@ -334,20 +338,23 @@ __host__ __device__ __forceinline__ int finish_region_ints(int G, int ermax, int
   const int h = hist_global ? 0 : G * ermax;
   return h > kFinishScratchInts ? h : kFinishScratchInts;
 }
-// a recorded pair: placement j of the block (3 bits), solute site (8 bits), site of the
-// solvent molecule (13 bits)
-__device__ __forceinline__ int big_item(int j, int su, int s) { return (j << 21) | (su << 13) | s; }
+// a recorded pair: its FP64 parts (2 bits), placement j of the block (3 bits), solute site
+// (8 bits), site of the solvent molecule (13 bits)
+__device__ __forceinline__ int big_item(int parts, int j, int su, int s) {
+  return (parts << 24) | (j << 21) | (su << 13) | s;
+}
 
 // real-space LJ + screened Coulomb of one molecule against solute b (mixed path):
-// fixed-point displacements and FP32 pair terms, summed as a float-float number.  A pair
-// whose FP32 LJ or Coulomb term exceeds kFp64Term in magnitude (or is not finite) is left
-// out: the first pass (!kBig) records it in items[nbig] (up to kBigPerThread of them; nbig
-// counts them all) and sets bit j of fix; the second pass (kBig) sums exactly those pairs
-// in FP64.
-template <bool kBig>
+// fixed-point displacements and FP32 pair terms, summed as a float-float number.  An FP32
+// LJ or Coulomb term above kFp64Lj / kFp64Coulomb in magnitude (or not finite) is left out
+// of the sum and counted in nbig (in the thread's scan order); the count's values in
+// [win, win + kBigPerThread) are recorded with their parts in items[count - win], and bit j
+// of fix is set.  kSum: sum the FP32 terms (the first pass); else only record (the later
+// rounds of a thread with more pairs than one round takes).
+template <bool kSum>
 __device__ __forceinline__ ff real_mixed(const MolArgs& A, const BatchArgs& a, int b, int s0, int ns,
                                          const LjK& k32, float rcut, int4 p0, int4 u0, int j, int* items,
-                                         int& nbig, unsigned& fix) {
+                                         int win, int& nbig, unsigned& fix) {
   const size_t ub = (size_t)b * kMaxSoluteSites;
   const float fx = A.fxf[0], fy = A.fxf[1], fz = A.fxf[2];
   const float dx = (float)(int)((unsigned)p0.x - (unsigned)u0.x) * fx;
@@ -381,18 +388,17 @@ __device__ __forceinline__ ff real_mixed(const MolArgs& A, const BatchArgs& a, i
         const float r = sqrtf(r2);
         eco = qu * A.site_rec[s0 + s].w * erfcf(beta * r) / r;
       }
-      const bool small = fabsf(elj) <= kFp64Term && fabsf(eco) <= kFp64Term;  // false for NaN, inf
-      if (!kBig) {
-        if (small) {
-          real = ff_add(real, elj);
-          real = ff_add(real, eco);
-        } else {
-          if (nbig < kBigPerThread) items[nbig] = big_item(j, su, s);
-          ++nbig;
-          fix |= 1u << j;
-        }
-      } else if (!small) {
-        real = ff_add2(real, ff_from_double(pair_fp64(A, s0 + s, a.u_x + (ub + su) * 3, a.u_q[ub + su], up.w)));
+      // parts too large for FP32 (the comparisons are false for NaN and inf)
+      const int parts = (fabsf(elj) <= kFp64Lj ? 0 : kPairLj) | (fabsf(eco) <= kFp64Coulomb ? 0 : kPairCoulomb);
+      if (kSum) {
+        if (!(parts & kPairLj)) real = ff_add(real, elj);
+        if (!(parts & kPairCoulomb)) real = ff_add(real, eco);
+      }
+      if (parts) {
+        const int r = nbig - win;
+        if (r >= 0 && r < kBigPerThread) items[r] = big_item(parts, j, su, s);
+        ++nbig;
+        fix |= 1u << j;
       }
     }
   }
@@ -748,20 +754,6 @@ __global__ void __launch_bounds__(kGatherThreads) gather_tma_kernel(
   }
 }
 
-// float of an ordered 32-bit key (the inverse of ordered_key32)
-__device__ __forceinline__ float key32_to_float(int k) { return __int_as_float(k ^ ((k >> 31) & 0x7fffffff)); }
-
-// ordered 64-bit key of a float-float number (hi, lo): hi first, then lo; the order of
-// the keys is the order of the values hi + lo
-__device__ __forceinline__ long long ff_key(float hi, float lo) {
-  return (long long)(((unsigned long long)(unsigned)ordered_key32(hi) << 32) |
-                     (unsigned long long)((unsigned)ordered_key32(lo) ^ 0x80000000u));
-}
-__device__ __forceinline__ double ff_key_to_double(long long k) {
-  const float hi = key32_to_float((int)(k >> 32));
-  const float lo = key32_to_float((int)((unsigned)k ^ 0x80000000u));
-  return (double)hi + (double)lo;
-}
 
 // The number of a species' edges e below u = hi + lo, given pos, the number of edges
 // whose float keys rd(e) lie below key32(hi) (kk: the species' float keys, uvkey: its
@@ -769,8 +761,11 @@ __device__ __forceinline__ double ff_key_to_double(long long k) {
 // float step of hi; such an edge is compared exactly in FP64 (e - hi is exact there, and
 // lo is a float), so the bin is the one the FP64 value hi + lo takes against the FP64
 // edges (getiduv/binsearch, engproc.F90:927-1020).
-__device__ __forceinline__ int exact_count(const long long* __restrict__ uvkey, const int* kk, int n, int pos,
-                                           int khi, float hi, float lo) {
+// (The FP64 comparisons sit in a function of their own, called only for a total that near
+// an edge: inline, the compiler would issue them predicated for every molecule, and an
+// FP64 instruction costs GB300 about 64 times an FP32 one even when no lane executes it.)
+__device__ __noinline__ int exact_count_near(const long long* __restrict__ uvkey, const int* kk, int n, int pos,
+                                            int khi, float hi, float lo) {
   while (pos > 0 && kk[pos - 1] >= khi - 2) {  // counted, but maybe not below u
     if (key_to_double(__ldg(uvkey + pos - 1)) - (double)hi < (double)lo) break;
     --pos;
@@ -780,6 +775,45 @@ __device__ __forceinline__ int exact_count(const long long* __restrict__ uvkey, 
     ++pos;
   }
   return pos;
+}
+__device__ __forceinline__ int exact_count(const long long* __restrict__ uvkey, const int* kk, int n, int pos,
+                                           int khi, float hi, float lo) {
+  const bool near = (pos > 0 && kk[pos - 1] >= khi - 2) || (pos < n && kk[pos] <= khi + 2);
+  return near ? exact_count_near(uvkey, kk, n, pos, khi, hi, lo) : pos;
+}
+
+// the finish kernel's per-species partials of its block (see mol_finish_kernel)
+template <int G, bool kSum>
+__device__ __forceinline__ void species_partials(const MolArgs& A, const BatchArgs& a, const float (*su)[256],
+                                                 const float (*sul)[256], const unsigned char* sspec, int g0, int ng,
+                                                 int tile) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int pr = warp; pr < ng * A.numslv; pr += blockDim.x / 32) {
+    const int j = pr / A.numslv, sp = pr % A.numslv + 1;
+    long long mn = kFfKeyNone, mx = kFfKeyNoneMax;
+    double s = 0.0;
+    for (int t = lane; t < blockDim.x; t += 32) {
+      const float v = su[j][t];
+      if (sspec[t] == sp && v == v) {
+        const float lo = sul[j][t];
+        if (kSum) s += (double)v + (double)lo;
+        const long long key = ff_key(v, lo);
+        mn = min(mn, key);
+        mx = max(mx, key);
+      }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      if (kSum) s += __shfl_down_sync(0xffffffffu, s, off);
+      mn = min(mn, __shfl_down_sync(0xffffffffu, mn, off));
+      mx = max(mx, __shfl_down_sync(0xffffffffu, mx, off));
+    }
+    if (lane == 0) {
+      double* pt = a.part + (((size_t)(g0 + j) * A.ntile + tile) * A.numslv + (sp - 1)) * 3;
+      pt[0] = s;
+      reinterpret_cast<long long*>(pt)[1] = mn;  // kFfKeyNone: no molecule of the species
+      reinterpret_cast<long long*>(pt)[2] = mx;
+    }
+  }
 }
 
 // Mixed path, step 2 -- per molecule x G placements: float-float sums of the site terms
@@ -802,7 +836,7 @@ __global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const flo
   __shared__ int swarp[8];
   __shared__ float su[G][256];   // totals, hi part (NaN: no molecule)
   __shared__ float sul[G][256];  // totals, lo part
-  __shared__ double sres[G];     // residual factor x solute charge of the G placements
+  __shared__ float sres[G];      // residual factor x solute charge of the G placements
   __shared__ float srcut[G];     // bounding-sphere cutoff of the real-space sum
   __shared__ int skskip[G];      // slot of the solute molecule itself (not a solvent)
   __shared__ int4 supos[G];      // first solute site (fixed point)
@@ -816,20 +850,22 @@ __global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const flo
   for (int i = threadIdx.x; i < A.ermax; i += blockDim.x) skeys[i] = A.uvkey_f[i];
   if (threadIdx.x < ng) {
     const int b = g0 + threadIdx.x;
-    sres[threadIdx.x] = A.resid_fac * a.u_qmol[b];
+    sres[threadIdx.x] = (float)(A.resid_fac * a.u_qmol[b]);
     srcut[threadIdx.x] = A.rc_f + a.u_radius[b] + A.frame_scal[0];
     const int tg = a.tagslt[b] - 1;
     skskip[threadIdx.x] = (tg >= 0 && tg < A.nummol) ? A.mol_to_k[tg] : -2;
     supos[threadIdx.x] = a.u_pos[(size_t)b * kMaxSoluteSites];
   }
   int k = -1, s0 = 0, ns = 0, species = 0;
-  double qmol = 0.0;
+  // residual_ene's molecular charge: the term pi Q_u Q_v / (beta^2 V) is below 1e-2 kcal/mol
+  // for unit charges in these boxes, so its FP32 product is exact to 1e-9 kcal/mol
+  float qmol = 0.f;
   if (valid) {
     k = A.slot_mol[m];
     s0 = A.slot_site[m];
     ns = A.slot_site[m + 1] - s0;
     species = A.slot_species[m];
-    qmol = A.slot_qmol[m];
+    qmol = (float)A.slot_qmol[m];
   }
   const bool spec_ok = valid && species >= 1 && species <= A.numslv;
   sspec[threadIdx.x] = (unsigned char)(spec_ok ? species : 0);
@@ -842,109 +878,115 @@ __global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const flo
     sp_soft = A.spec[3 * (species - 1) + 2];
   }
   __syncthreads();  // sres staged
-  // ---- totals of the G placements, as float-float numbers, four placements at a time:
-  // the site terms of placements g0 + j4 .. g0 + j4 + 3 are 4 consecutive floats per site
-  // (one 16-byte load when g0, j4 and ldb are multiples of 4) ----
-  // the totals wait in this thread's entries of su (hi) and sul (lo) until the bin search
+  // ---- totals of the G placements, as float-float numbers.  First the site terms: the G
+  // placements' terms of a site are G consecutive floats (16-byte loads when G, g0 and ldb
+  // are multiples of 4).  The totals then wait in this thread's entries of su (hi) and sul
+  // (lo) until the bin search; the real-space pass adds to them placement by placement in a
+  // rolled loop (one copy of its code) ----
   unsigned actm = 0u;  // placements whose total is a solvent molecule's energy
   unsigned fix = 0u;   // placements with pairs left for the FP64 pass
-  int nbig = 0;       // such pairs of this thread (the first kBigPerThread recorded in sitem)
+  int nbig = 0;        // such pairs of this thread (the first kBigPerThread recorded in sitem)
   int* items = sitem + threadIdx.x * kBigPerThread;
-  const int4 p0 = valid ? A.site_pos[s0] : make_int4(0, 0, 0, 0);
+  {
+    ff rs[G];
 #pragma unroll
-  for (int j4 = 0; j4 < G; j4 += 4) {
-    ff rs[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) rs[i] = ff{0.f, 0.f};
+    for (int j = 0; j < G; ++j) rs[j] = ff{0.f, 0.f};
     if (valid) {
       for (int s = 0; s < (A.bare ? 0 : ns); ++s) {
-        const float* row = site_e + (size_t)(s0 + s) * ldb + g0 + j4;
-        if (j4 + 4 <= ng) {
-          const float4 v = __ldg(reinterpret_cast<const float4*>(row));
-          rs[0] = ff_add(rs[0], v.x);
-          rs[1] = ff_add(rs[1], v.y);
-          rs[2] = ff_add(rs[2], v.z);
-          rs[3] = ff_add(rs[3], v.w);
+        const float* row = site_e + (size_t)(s0 + s) * ldb + g0;
+        if (G % 4 == 0 && ng == G) {
+#pragma unroll
+          for (int j4 = 0; j4 < G; j4 += 4) {
+            const float4 v = __ldg(reinterpret_cast<const float4*>(row + j4));
+            rs[j4] = ff_add(rs[j4], v.x);
+            rs[j4 + 1] = ff_add(rs[j4 + 1], v.y);
+            rs[j4 + 2] = ff_add(rs[j4 + 2], v.z);
+            rs[j4 + 3] = ff_add(rs[j4 + 3], v.w);
+          }
         } else {
 #pragma unroll
-          for (int i = 0; i < 4; ++i)
-            if (j4 + i < ng) rs[i] = ff_add(rs[i], __ldg(row + i));
+          for (int j = 0; j < G; ++j)
+            if (j < ng) rs[j] = ff_add(rs[j], __ldg(row + j));
         }
       }
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int j = j4 + i;
-      ff t{0.f, 0.f};
-      if (j < ng && valid && k != skskip[j]) {
-        // get_uv_energy (engproc.F90:736-753): real + residual + recip
-        t = ff_add2(rs[i], real_mixed<false>(A, a, g0 + j, s0, ns, k32, srcut[j], p0, supos[j], j, items, nbig,
-                                             fix));
-        if (qmol != 0.0) t = ff_add2(t, ff_from_double(-sres[j] * qmol));  // residual_ene
-        actm |= 1u << j;
-      }
+    for (int j = 0; j < G; ++j) {
+      const bool on = j < ng && valid && k != skskip[j];
+      if (on) actm |= 1u << j;
+      // residual_ene (engproc.F90:859-869)
+      const ff t = on ? ff_add(rs[j], -sres[j] * qmol) : ff{0.f, 0.f};
       su[j][threadIdx.x] = t.hi;
       sul[j][threadIdx.x] = t.lo;
     }
   }
-  // ---- FP64 pass over the pairs left out above (overlapping pairs).  The block's
+  const int4 p0 = valid ? A.site_pos[s0] : make_int4(0, 0, 0, 0);
+#pragma unroll 1
+  for (int j = 0; j < G; ++j) {
+    if (!(actm & (1u << j))) continue;
+    // get_uv_energy (engproc.F90:736-753): real + residual + recip
+    const ff r = real_mixed<true>(A, a, g0 + j, s0, ns, k32, srcut[j], p0, supos[j], j, items, 0, nbig, fix);
+    if (r.hi != 0.f || r.lo != 0.f) {
+      const ff t = ff_add2(ff{su[j][threadIdx.x], sul[j][threadIdx.x]}, r);
+      su[j][threadIdx.x] = t.hi;
+      sul[j][threadIdx.x] = t.lo;
+    }
+  }
+  // ---- FP64 pass over the pair parts left out above (overlapping pairs).  The block's
   // recorded pairs are compacted (an exclusive scan over the threads) and evaluated one
   // per thread, so that every FP64 instruction of the pass runs on full warps; each owner
-  // then adds its pairs' values in the order it found them.  A thread with more pairs
-  // than it could record sums its own in FP64.  The totals wait in su/sul meanwhile. ----
+  // then adds its pairs' values in the order it found them.  A thread with more than
+  // kBigPerThread pairs takes further rounds, recording the next ones by a fresh scan. ----
   if (__syncthreads_or(fix != 0u)) {
     ss0[threadIdx.x] = s0;
-    const bool ovf = nbig > kBigPerThread;
-    const int cnt = ovf ? 0 : nbig;
-    // exclusive scan of cnt over the block
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    int incl = cnt;
-    for (int o = 1; o < 32; o <<= 1) {
-      const int v = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += v;
-    }
-    if (lane == 31) swarp[wid] = incl;
-    __syncthreads();
-    int off = incl - cnt, total = 0;
-    for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) {
-      if (w2 < wid) off += swarp[w2];
-      total += swarp[w2];
-    }
-    for (int i = 0; i < cnt; ++i) slist[off + i] = (unsigned short)(threadIdx.x * kBigPerThread + i);
-    __syncthreads();
-    for (int base = 0; base < total; base += blockDim.x) {
-      const int q = base + threadIdx.x;
-      double v = 0.0;
-      if (q < total) {
-        const int slot = slist[q];
-        const int t = slot / kBigPerThread, it = sitem[slot];
-        const int j = it >> 21, su_ = (it >> 13) & 0xff, sv = it & 0x1fff;
-        const size_t us = (size_t)(g0 + j) * kMaxSoluteSites + su_;
-        v = pair_fp64(A, ss0[t] + sv, a.u_x + us * 3, a.u_q[us], a.u_pos[us].w);
+    for (int win = 0;; win += kBigPerThread) {
+      if (win > 0) {  // later round: record pairs win .. win + kBigPerThread - 1 afresh
+        int n2 = 0;
+        unsigned f2 = 0u;
+        if (nbig > win)
+          for (int j = 0; j < G; ++j)
+            if (fix & (1u << j)) real_mixed<false>(A, a, g0 + j, s0, ns, k32, srcut[j], p0, supos[j], j, items, win, n2, f2);
       }
-      sbuf[threadIdx.x] = v;
-      __syncthreads();
-      for (int i = 0; i < cnt; ++i) {
-        const int qq = off + i - base;
-        if (qq < 0 || qq >= (int)blockDim.x) continue;
-        const int j = items[i] >> 21;
-        const ff t = ff_add2(ff{su[j][threadIdx.x], sul[j][threadIdx.x]}, ff_from_double(sbuf[qq]));
-        su[j][threadIdx.x] = t.hi;
-        sul[j][threadIdx.x] = t.lo;
+      const int cnt = min(max(nbig - win, 0), kBigPerThread);
+      // exclusive scan of cnt over the block
+      int incl = cnt;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
       }
+      if (lane == 31) swarp[wid] = incl;
       __syncthreads();
-    }
-    if (ovf) {
-      int nb2 = 0;
-      unsigned f2 = 0u;
-      for (int j = 0; j < G; ++j)
-        if (fix & (1u << j)) {
-          const ff t = ff_add2(ff{su[j][threadIdx.x], sul[j][threadIdx.x]},
-                               real_mixed<true>(A, a, g0 + j, s0, ns, k32, srcut[j], p0, supos[j], j, nullptr,
-                                                nb2, f2));
+      int off = incl - cnt, total = 0;
+      for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) {
+        if (w2 < wid) off += swarp[w2];
+        total += swarp[w2];
+      }
+      if (total == 0) break;  // block-uniform
+      for (int i = 0; i < cnt; ++i) slist[off + i] = (unsigned short)(threadIdx.x * kBigPerThread + i);
+      __syncthreads();
+      for (int base = 0; base < total; base += blockDim.x) {
+        const int q = base + threadIdx.x;
+        double v = 0.0;
+        if (q < total) {
+          const int slot = slist[q];
+          const int t = slot / kBigPerThread, it = sitem[slot];
+          const int j = (it >> 21) & 7, su_ = (it >> 13) & 0xff, sv = it & 0x1fff;
+          const size_t us = (size_t)(g0 + j) * kMaxSoluteSites + su_;
+          v = pair_fp64(A, ss0[t] + sv, a.u_x + us * 3, a.u_q[us], a.u_pos[us].w, it >> 24);
+        }
+        sbuf[threadIdx.x] = v;
+        __syncthreads();
+        for (int i = 0; i < cnt; ++i) {
+          const int qq = off + i - base;
+          if (qq < 0 || qq >= (int)blockDim.x) continue;
+          const int j = (items[i] >> 21) & 7;
+          const ff t = ff_add2(ff{su[j][threadIdx.x], sul[j][threadIdx.x]}, ff_from_double(sbuf[qq]));
           su[j][threadIdx.x] = t.hi;
           sul[j][threadIdx.x] = t.lo;
         }
+        __syncthreads();
+      }
     }
     __syncthreads();  // the scratch is free: the histograms may take the region
   }
@@ -1021,39 +1063,14 @@ __global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const flo
   }
   __syncthreads();
   // per-species {sum, min, max} of the block: one warp per (placement, species),
-  // fixed lane order and a fixed shuffle tree; min and max on ordered keys of the
-  // float-float totals
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // the species sums are flceng (engproc.F90:822-825): needed for slnuv (solution mode)
-  // and when the caller asks for flceng
-  const bool want_sum = A.soln || a.flceng_out != nullptr;
-  constexpr long long kKeyMax = 0x7fffffffffffffffll, kKeyMin = (long long)0x8000000000000000ull;
-  for (int pr = warp; pr < ng * A.numslv; pr += blockDim.x / 32) {
-    const int j = pr / A.numslv, sp = pr % A.numslv + 1;
-    long long mn = kKeyMax, mx = kKeyMin;
-    double s = 0.0;
-    for (int t = lane; t < blockDim.x; t += 32) {
-      const float v = su[j][t];
-      if (sspec[t] == sp && v == v) {
-        const float lo = sul[j][t];
-        if (want_sum) s += (double)v + (double)lo;
-        const long long key = ff_key(v, lo);
-        mn = min(mn, key);
-        mx = max(mx, key);
-      }
-    }
-    for (int off = 16; off > 0; off >>= 1) {
-      if (want_sum) s += __shfl_down_sync(0xffffffffu, s, off);
-      mn = min(mn, __shfl_down_sync(0xffffffffu, mn, off));
-      mx = max(mx, __shfl_down_sync(0xffffffffu, mx, off));
-    }
-    if (lane == 0) {
-      double* pt = a.part + (((size_t)(g0 + j) * A.ntile + tile) * A.numslv + (sp - 1)) * 3;
-      pt[0] = s;
-      pt[1] = (mn == kKeyMax) ? HUGE_VAL : ff_key_to_double(mn);
-      pt[2] = (mx == kKeyMin) ? -HUGE_VAL : ff_key_to_double(mx);
-    }
-  }
+  // fixed lane order and a fixed shuffle tree; min and max as ordered keys of the
+  // float-float totals (decoded by the reduce kernel), so that no FP64 instruction issues
+  // here unless the species sums are wanted -- they are flceng (engproc.F90:822-825),
+  // needed for slnuv (solution mode) and when the caller asks for flceng
+  if (A.soln || a.flceng_out != nullptr)
+    species_partials<G, true>(A, a, su, sul, sspec, g0, ng, tile);
+  else
+    species_partials<G, false>(A, a, su, sul, sspec, g0, ng, tile);
   if (A.hist_global) return;
   for (int j = 0; j < ng; ++j) {
     const int* h = smem_hist + j * A.ermax;

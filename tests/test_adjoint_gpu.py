@@ -126,3 +126,37 @@ def test_adjoint_matches_central_differences(gpu_lib, oracle):
             np.add.at(ref, b, fd[keep])
             np.add.at(mag, b, np.abs(fd[keep]))
         _check(g[p][None, :], ref[None, :], mag[None, :])
+
+
+def test_adjoint_full_size_against_oracle_gradient(gpu_lib, oracle):
+    """The adjoint workload at its own size: 8,000 waters in a 62 A box, a 16-site solute
+    (48 parameters), PME 64^3, two frames; the oracle's FP64 gradient binned by the GPU's
+    energies."""
+    w = synth.soln_adjoint(frames=2)
+    assert w.nwater == 8000 and len(w.solute["charge"]) == 16 and w.params["ms1max"] == 64
+    topo = setconf.setparam_topology(w.species(), slttype=1)
+    bins = setconf.enginit_bins(topo["numslv"])
+    frames = [0, 1]
+    g, wt, us = _run_gpu(w, topo, bins, frames)
+    orc = oracle.Oracle(w.params, topo, bins)
+    tag = topo["nummol"]
+    edges = bins["uvcrd"]
+    E, P = len(edges), 3 * 16
+    ref = np.zeros((P, E))
+    mag = np.zeros((P, E))
+    cnt = np.zeros(E)
+    for f, u in zip(frames, us):
+        pos, cell = w.frame(f)
+        orc.frame(pos, cell)
+        du = orc.adjoint(tag)
+        keep = np.ones(len(u), bool)
+        keep[-1] = False
+        b = _bins(u[keep], edges)
+        np.add.at(ref.T, b, du[keep])
+        np.add.at(mag.T, b, np.abs(du[keep]))
+        np.add.at(cnt, b, 1.0)
+    assert g.shape == (P, E)
+    # NPT: every molecule's weight is the same volume factor C
+    C = wt.sum() / cnt.sum()
+    np.testing.assert_allclose(wt, cnt * C, rtol=1e-12)
+    _check(g / C, ref, mag)
