@@ -194,8 +194,13 @@ def cpu_oracle_rate(w, topo, bins, nplace, frame_index=0, want_uvengy=False, pla
 
 
 # The mixed path's stated per-molecule error bound against the FP64 oracle (kcal/mol): the
-# band around each bin edge within which a molecule may take the neighbouring bin.
+# band around each bin edge within which a molecule may take the neighbouring bin; for a
+# solute of summed absolute charge above 3 e it grows as sqrt(sum|q| / 3 e).
 MIXED_BAND = 3e-5
+
+
+def mixed_band(solute):
+    return MIXED_BAND * max(1.0, float(np.sqrt(np.sum(np.abs(solute["charge"])) / 3.0)))
 
 
 def accuracy_report(u_gpu, u_orc, edges, band=MIXED_BAND):
@@ -406,7 +411,7 @@ def run_ours(args):
         eng3.frame(frames[0][0], cell)
         u_gpu = eng3.placements(tag_h[:ncpu], None if soln else places[0][:ncpu], want_uvengy=True)["uvengy"]
         eng3.close()
-        accuracy = accuracy_report(u_gpu, u_orc, bins["uvcrd"])
+        accuracy = accuracy_report(u_gpu, u_orc, bins["uvcrd"], mixed_band(w.solute))
         accuracy["sample"] = f"{ncpu} placements of frame 0 against the FP64 oracle"
 
     if rank == 0:
@@ -490,7 +495,7 @@ def run_uneven(args):
         eng.frame(*frames[k])
         u_gpu = eng.placements(np.full(n, topo["nummol"], np.int32), places[k][:n], want_uvengy=True)["uvengy"]
         eng.close()
-        accuracy = accuracy_report(u_gpu, u_orc, bins["uvcrd"])
+        accuracy = accuracy_report(u_gpu, u_orc, bins["uvcrd"], mixed_band(w.solute))
         accuracy["sample"] = cpu["sample"]
     line = {"metric": "solute-solvent molecule energies/s", "value": units / (ms / 1e3),
             "unit": "molecule-energies/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -568,7 +573,7 @@ def run_adjoint(args):
         u_gpu = eng.placements([topo["nummol"]], want_uvengy=True)["uvengy"]
         grad, wt = eng.adjoint_get()
         eng.close()
-        acc = accuracy_report(u_gpu, u_orc, bins["uvcrd"])
+        acc = accuracy_report(u_gpu, u_orc, bins["uvcrd"], mixed_band(w.solute))
         edges = np.asarray(bins["uvcrd"])
         b = np.searchsorted(edges, u_gpu[0, 1:-1], side="left") - 1  # the solute itself is the last molecule
         ref = np.zeros_like(grad)
@@ -576,8 +581,14 @@ def run_adjoint(args):
         np.add.at(ref.T, b, du[:-1])
         np.add.at(mag.T, b, np.abs(du[:-1]))
         C = wt.sum() / max(len(b), 1)  # every molecule's weight: the volume factor
-        occ = mag > 0
-        acc["gradient_max_rel_err"] = float((np.abs(grad / C - ref)[occ] / mag[occ]).max())
+        # error per (parameter, bin) relative to the bin's summed magnitude, on bins holding at
+        # least 1e-3 of the parameter's largest bin magnitude (elsewhere the derivatives of a
+        # few molecules nearly cancel and only an absolute bound means anything)
+        err = np.abs(grad / C - ref)
+        big = mag >= 1e-3 * mag.max(axis=1, keepdims=True)
+        acc["gradient_max_rel_err"] = float((err[big] / mag[big]).max())
+        small = ~big & (mag > 0)
+        acc["gradient_max_abs_err_small_bins"] = float(err[small].max()) if np.any(small) else 0.0
         acc["sample"] = "frame 0 against the FP64 oracle (energies and the oracle's analytic gradient)"
         line["accuracy"] = acc
     print(json.dumps(line))

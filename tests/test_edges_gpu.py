@@ -22,10 +22,11 @@ def _engine(w, precision, **kw):
     return EnergyRepresentation(w.params, topo, bins, precision=precision, **kw), topo, bins
 
 
-def _check_uv(ug, uo, precision, edges=None, label=""):
-    helpers.check_energies(ug, uo, precision, label)
+def _check_uv(ug, uo, precision, edges=None, label="", solute=None):
+    band = helpers.mixed_band(solute) if precision == "mixed" else None
+    helpers.check_energies(ug, uo, precision, label, band=band)
     if edges is not None:
-        helpers.check_histograms(ug, uo, edges, precision, label)
+        helpers.check_histograms(ug, uo, edges, precision, label, band=band)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -112,11 +113,11 @@ def test_largest_solute(gpu_lib, oracle, precision):
     pl = w.placements(0, 6)
     tag = np.full(len(pl), topo["nummol"], np.int32)
     ro, rg = orc.placements(tag, pl), gpu.placements(tag, pl, want_uvengy=True)
-    _check_uv(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], precision, bins["uvcrd"], "256-site solute")
+    _check_uv(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], precision, bins["uvcrd"], "256-site solute", w.solute)
     # the self energy (all 256 sites' spectrum, summed over the site chunks): about
     # -1 kcal/mol, net of reciprocal and real-space parts that largely cancel
     np.testing.assert_allclose(rg["uvengy"][:, 0], ro["uvengy"][:, 0], rtol=0,
-                               atol=helpers.self_tol(precision, len(w.solute["charge"])))
+                               atol=helpers.self_tol(precision, w.solute))
     gpu.close()
 
 
@@ -152,9 +153,9 @@ def test_largest_uneven_system(gpu_lib, oracle, precision):
     pl = w.placements(0, 4)
     tag = np.full(len(pl), topo["nummol"], np.int32)
     ro, rg = orc.placements(tag, pl), gpu.placements(tag, pl, want_uvengy=True)
-    _check_uv(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], precision, bins["uvcrd"], "58,329 waters")
+    _check_uv(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], precision, bins["uvcrd"], "58,329 waters", w.solute)
     np.testing.assert_allclose(rg["uvengy"][:, 0], ro["uvengy"][:, 0], rtol=0,
-                               atol=helpers.self_tol(precision, len(w.solute["charge"])))
+                               atol=helpers.self_tol(precision, w.solute))
     ag, ao = gpu.accum(), orc.accum()
     if precision == "fp64":
         np.testing.assert_allclose(ag["engnorm"], ao["engnorm"], rtol=1e-10)

@@ -99,7 +99,7 @@ def test_noncubic_grid_self_energies(gpu_lib, oracle, precision, grid):
     pl = w.placements(0, 20)
     tag = np.full(len(pl), topo["nummol"], np.int32)
     ro, rg = orc.placements(tag, pl), gpu.placements(tag, pl, want_uvengy=True)
-    np.testing.assert_allclose(rg["uvengy"][:, 0], ro["uvengy"][:, 0], rtol=0, atol=helpers.self_tol(precision, len(w.solute["charge"])))
+    np.testing.assert_allclose(rg["uvengy"][:, 0], ro["uvengy"][:, 0], rtol=0, atol=helpers.self_tol(precision, w.solute))
     helpers.check_energies(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], precision, f"grid {grid}")
     helpers.check_histograms(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], bins["uvcrd"], precision, f"grid {grid}")
     gpu.close()

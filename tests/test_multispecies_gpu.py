@@ -105,7 +105,7 @@ def test_two_species_match_oracle(gpu_lib, oracle, precision, mode):
         uo_all.append(ro["uvengy"])
     ag, ao = gpu.accum(), orc.accum()
     # wgtslf = 1: the weights follow the solute self energy (solution mode: exp(+(u0 - voffset)/kT))
-    rtol_w = helpers.weight_rtol(precision, 8, params["temp"])  # the 8-site solute
+    rtol_w = helpers.weight_rtol(precision, dict(charge=species[2]["charge"]), params["temp"])
     np.testing.assert_allclose(ag["engnorm"], ao["engnorm"], rtol=rtol_w)
     for blk in (slice(0, n1), slice(n1, None)):  # the species blocks of edens
         np.testing.assert_allclose(ag["edens"][blk].sum(), ao["edens"][blk].sum(), rtol=rtol_w)

@@ -36,17 +36,16 @@ def _check_weighted(ag, ao, u_orc, edges, w, corr=True, label=""):
     """edens and ecorr bin by bin: the weights' relative error from the self energies,
     plus the weight of every near-edge molecule that may sit in a neighbouring bin."""
     precision = "mixed"
-    ns = len(w.solute["charge"])
-    rtol_w = helpers.weight_rtol(precision, ns, w.params["temp"])
+    rtol_w = helpers.weight_rtol(precision, w.solute, w.params["temp"])
     wts = _placement_weights(u_orc[:, 0], ao["engnorm"], w.params["temp"], w.params["wgtslf"])
-    b_ed, b_ec = helpers.weighted_bounds(u_orc[:, 1:], wts, edges, helpers.MIXED_BAND, rtol_w, corr=corr)
+    b_ed, b_ec = helpers.weighted_bounds(u_orc[:, 1:], wts, edges, helpers.mixed_band(w.solute), rtol_w, corr=corr)
     d_ed = np.abs(ag["edens"] - ao["edens"])
     assert np.all(d_ed <= b_ed + 1e-12 * np.abs(ao["edens"])), f"{label}: edens bin {int(np.argmax(d_ed - b_ed))}"
     if corr:
         d_ec = np.abs(ag["ecorr"] - ao["ecorr"])
         assert np.all(d_ec <= b_ec + 1e-12 * np.abs(ao["ecorr"])), f"{label}: ecorr entry {np.unravel_index(int(np.argmax(d_ec - b_ec)), d_ec.shape)}"
     np.testing.assert_allclose(ag["engnorm"], ao["engnorm"], rtol=rtol_w)
-    np.testing.assert_allclose(ag["voffset"], ao["voffset"], atol=helpers.self_tol(precision, ns))
+    np.testing.assert_allclose(ag["voffset"], ao["voffset"], atol=helpers.self_tol(precision, w.solute))
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -140,7 +139,7 @@ def test_refs_weighted_accumulators(gpu_lib, oracle, precision):
         helpers.check_histograms(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], bins["uvcrd"], precision, "refs weighted")
         # the solute self energy decides the weights
         np.testing.assert_allclose(rg["uvengy"][:, 0], ro["uvengy"][:, 0], rtol=0,
-                                   atol=helpers.self_tol(precision, len(w.solute["charge"])))
+                                   atol=helpers.self_tol(precision, w.solute))
         uo_all.append(ro["uvengy"])
     ag, ao = gpu.accum(), orc.accum()
     np.testing.assert_allclose(ag["avslf"], ao["avslf"], rtol=1e-12)
@@ -279,7 +278,7 @@ def test_compile_time_grid_sizes(gpu_lib, oracle, K, order):
     rg = gpu.placements(tag, pl, want_uvengy=True)
     _check_energies(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], "mixed", f"K={K} order {order}")
     helpers.check_histograms(rg["uvengy"][:, 1:], ro["uvengy"][:, 1:], bins["uvcrd"], "mixed", f"K={K} order {order}")
-    np.testing.assert_allclose(rg["uvengy"][:, 0], ro["uvengy"][:, 0], rtol=0, atol=helpers.self_tol("mixed", len(w.solute["charge"])))
+    np.testing.assert_allclose(rg["uvengy"][:, 0], ro["uvengy"][:, 0], rtol=0, atol=helpers.self_tol("mixed", w.solute))
     gpu.close()
 
 

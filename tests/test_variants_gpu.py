@@ -67,10 +67,10 @@ def test_flexible_solute_with_weights(gpu_lib, oracle, precision):
         # the self energies differ between placements and match the oracle's
         assert np.ptp(ro["uvengy"][:, 0]) > 1e-3
         np.testing.assert_allclose(rg["uvengy"][:, 0], ro["uvengy"][:, 0], rtol=0,
-                                   atol=helpers.self_tol(precision, len(w.solute["charge"])))
+                                   atol=helpers.self_tol(precision, w.solute))
     ag, ao = gpu.accum(), orc.accum()
     # the weights' relative error from the self energies (u0 and voffset)
-    rtol = helpers.weight_rtol(precision, len(w.solute["charge"]), w.params["temp"])
+    rtol = helpers.weight_rtol(precision, w.solute, w.params["temp"])
     for key in ("engnorm", "avslf"):
         np.testing.assert_allclose(ag[key], ao[key], rtol=rtol)
     np.testing.assert_allclose(ag["edens"].sum(), ao["edens"].sum(), rtol=rtol)
@@ -92,7 +92,7 @@ def test_selfcal_and_frame_weight(gpu_lib, oracle, precision):
     ro = orc.placements(tag, pl)
     gpu.placements(tag, pl)
     ag, ao = gpu.accum(), orc.accum()
-    rtol = helpers.weight_rtol(precision, len(w.solute["charge"]), w.params["temp"])
+    rtol = helpers.weight_rtol(precision, w.solute, w.params["temp"])
     np.testing.assert_allclose(ag["engnorm"], ao["engnorm"], rtol=rtol)
     np.testing.assert_allclose(ag["avslf"], ao["avslf"], rtol=1e-12)
     np.testing.assert_allclose(ag["eself"].sum(), ao["eself"].sum(), rtol=rtol)
@@ -102,7 +102,7 @@ def test_selfcal_and_frame_weight(gpu_lib, oracle, precision):
     u0 = ro["uvengy"][:, 0]
     e = np.exp(-(u0 - u0[0]) / w.params["temp"])
     b_es, _ = helpers.weighted_bounds(u0[:, None], ao["engnorm"] * e / e.sum(), np.asarray(bins["escrd"]),
-                                      helpers.self_tol(precision, len(w.solute["charge"])), rtol)
+                                      helpers.self_tol(precision, w.solute), rtol)
     assert np.all(np.abs(ag["eself"] - ao["eself"]) <= b_es + 1e-12 * np.abs(ao["eself"]))
     gpu.close()
 
