@@ -13,7 +13,7 @@ LIB_PATH = os.path.join(HERE, "libermod_gb300.so")
 
 OK = 0
 E_ENG_MIN, E_ENG_SFT, E_ENG_BUG, E_ENG_CNS, E_RCP_CNS, E_RCP_FST = 101, 102, 103, 104, 105, 106
-E_INS_GEO, E_SET_PRS = 107, 108
+E_INS_GEO, E_SET_PRS, E_ENG_SLB = 107, 108, 109
 W_MBIN = 110
 E_PARAM, E_NONCUBOID, E_UNSUPPORTED = 120, 121, 122
 E_CUDA, E_CUFFT, E_NOMEM, E_DEVICE = 130, 131, 132, 133
@@ -23,7 +23,7 @@ ABI_VERSION = 2
 # halt_with_error identities (mpiproc.F90:203-264) of the status codes
 REFERENCE_CODE = {E_ENG_MIN: "eng_min", E_ENG_SFT: "eng_sft", E_ENG_BUG: "eng_bug", E_ENG_CNS: "eng_cns",
                   E_RCP_CNS: "rcp_cns", E_RCP_FST: "rcp_fst", E_INS_GEO: "ins_geo", E_SET_PRS: "set_prs",
-                  W_MBIN: "mbin"}
+                  E_ENG_SLB: "eng_slb", W_MBIN: "mbin"}
 
 
 class Params(C.Structure):
@@ -54,6 +54,7 @@ EXPORTS = [
     "ermod_graph_launch", "ermod_graph_sync", "ermod_graph_destroy", "ermod_write_engdist",
     "ermod_write_selfdist", "ermod_write_corr", "ermod_write_uvrange", "ermod_format_g",
     "ermod_generate_placements", "ermod_intermediate_enable", "ermod_intermediate_get",
+    "ermod_set_configuration_check", "ermod_set_aggregate", "ermod_set_reference_structure",
 ]
 
 _lib = None
@@ -114,6 +115,9 @@ def load(path: str = LIB_PATH):
     L.ermod_generate_placements.argtypes = [vp, C.c_int, C.c_int, dp, dp, C.POINTER(InsertParams), vp, vp]
     L.ermod_intermediate_enable.argtypes = [vp, dp]
     L.ermod_intermediate_get.argtypes = [vp, dp, dp, dp]
+    L.ermod_set_configuration_check.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double, C.c_double]
+    L.ermod_set_aggregate.argtypes = [vp, ip, dp]
+    L.ermod_set_reference_structure.argtypes = [vp, ip, dp, dp, C.c_int, dp, dp]
     _lib = L
     return L
 

@@ -21,7 +21,7 @@ LIB = os.path.join(HERE, "libermod_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["engine.cu", "kernels_frame.cu", "kernels_place.cu", "kernels_fft.cu", "kernels_mol.cu",
            "kernels_accum.cu", "kernels_insert.cu", "host_setup.cpp"]
-HEADERS = ["engine.cuh", "ermod_internal.cuh", "async_copy.cuh"]
+HEADERS = ["engine.cuh", "ermod_internal.cuh", "async_copy.cuh", "bestfit.cuh"]
 
 
 def nvcc() -> str:

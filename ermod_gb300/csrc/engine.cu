@@ -338,6 +338,7 @@ const char* ermod_status_string(int s) {
     case ERMOD_E_RCP_FST: return "rcp_fst: the solute must not be a solvent";
     case ERMOD_E_INS_GEO: return "ins_geo: the system geometry is incorrectly set";
     case ERMOD_E_SET_PRS: return "set_prs: the system parameters are incorrectly set";
+    case ERMOD_E_ENG_SLB: return "eng_slb: the slab configuration needs a periodic system";
     case ERMOD_W_MBIN: return "mbin: the maximum binning energy is too low for this species";
     case ERMOD_E_PARAM: return "invalid argument";
     case ERMOD_E_NONCUBOID: return "a non-cuboidal cell is not supported";
@@ -509,6 +510,7 @@ int ermod_create(const ermod_params* p_in, int device, ermod_ctx** out) {
 
 static void free_adjoint(Engine& e);
 static void free_intermediate(Engine& e);
+static void free_config_check(Engine& e);
 
 int ermod_destroy(ermod_ctx* c) {
   if (!c) return ERMOD_OK;
@@ -517,6 +519,7 @@ int ermod_destroy(ermod_ctx* c) {
   if (e.stream) cudaStreamSynchronize(e.stream);
   free_adjoint(e);
   free_intermediate(e);
+  free_config_check(e);
   dfree(e.d_ins);
   free_batch(e);
   free_frame(e);
@@ -577,6 +580,7 @@ int ermod_set_topology(ermod_ctx* c, int nummol, int numatm, const int* mbi, con
   cudaSetDevice(e.device);
   cudaStreamSynchronize(e.stream);
   free_adjoint(e);  // sized by the topology: enable it again afterwards
+  free_config_check(e);
   if (mbi[0] != 1 || mbi[nummol] - 1 != numatm) return fail_param("mol_begin_index must run from 1 to numatm+1");
   for (int i = 0; i < nummol; ++i) {
     if (mbi[i + 1] <= mbi[i]) return fail_param("every molecule needs at least one site");
@@ -936,6 +940,16 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
   // path, whose cuFFT plans are bound to it); every stream starts after what is
   // already queued on the caller's stream
   const bool dual = e.mixed;
+  // solution mode: the placements check_mol_configuration skips (engproc.F90:389-390)
+  const bool check = e.P.slttype == 1 && (e.cfg_pos != 0 || e.cfg_str != 0) && nplace > 0;
+  if (check) {
+    if (nplace > e.cap_skip) {
+      dfree(e.d_skip);
+      e.cap_skip = nplace;
+      ERMOD_CUDA(dalloc(&e.d_skip, (size_t)e.cap_skip));
+    }
+    ERMOD_CUDA(launch_config_check(e, nplace, d_tag));
+  }
   ERMOD_CUDA(cudaEventRecord(e.ev_done[0], e.stream));
   ERMOD_CUDA(cudaStreamWaitEvent(e.aux, e.ev_done[0], 0));
   ERMOD_CUDA(cudaStreamWaitEvent(e.prep, e.ev_done[0], 0));
@@ -973,6 +987,7 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
     a.stream = dual ? e.bs[slot] : e.stream;
     a.phases = 1;
     a.mol_bin = e.adj_on ? e.d_mol_bin + (size_t)slot * B * e.slvmax : nullptr;
+    a.skip = check ? e.d_skip + b0 : nullptr;
     if (e.mixed) {
       const size_t np = (size_t)e.phi_dims[0] * e.phi_dims[1] * e.phi_dims[2];
       a.spec = e.buf.spec + (size_t)slot * e.grid_cplx() * B;
@@ -1234,6 +1249,129 @@ static void free_intermediate(Engine& e) {
   dfree(e.d_edintm);
 }
 
+static void free_config_check(Engine& e) {
+  dfree(e.d_agg_mass);
+  dfree(e.d_site_mass);
+  dfree(e.d_ref_atoms);
+  dfree(e.d_ref_host);
+  dfree(e.d_ref_slt);
+  dfree(e.d_ref_fit);
+  dfree(e.d_skip);
+  e.cap_skip = 0;
+  e.ref_nh = e.ref_ns = 0;
+  e.cfg_pos = e.cfg_str = 0;
+}
+
+// hostspec's aggregate and the site masses (com_aggregate, insertion.F90:539-566)
+int ermod_set_aggregate(ermod_ctx* c, const int* host_mol, const double* sitemass) {
+  if (!c || !host_mol || !sitemass) return fail_param("null argument");
+  Engine& e = c->e;
+  if (!e.topo_ready) return fail_param("ermod_set_topology must come first");
+  cudaSetDevice(e.device);
+  ERMOD_CUDA(cudaStreamSynchronize(e.stream));
+  std::vector<double> hm((size_t)e.numatm, 0.0);
+  double tot = 0.0;
+  for (int i = 0; i < e.nummol; ++i)
+    if (host_mol[i])
+      for (int a = e.mbi0[i]; a < e.mbi0[i + 1]; ++a) {
+        hm[a] = sitemass[a];
+        tot += sitemass[a];
+      }
+  if (!(tot > 0.0)) return fail_param("bst_zrw: the host aggregate has no mass");
+  for (int i = 0; i < e.nummol; ++i) {  // center_of_mass of a solute (bestfit.F90:167-168)
+    if (e.sluvid[i] == 0) continue;
+    double m = 0.0;
+    for (int a = e.mbi0[i]; a < e.mbi0[i + 1]; ++a) m += sitemass[a];
+    if (m == 0.0) return fail_param("bst_zrw: a solute molecule has no mass");
+  }
+  if (!e.d_agg_mass) ERMOD_CUDA(dalloc(&e.d_agg_mass, (size_t)e.numatm));
+  if (!e.d_site_mass) ERMOD_CUDA(dalloc(&e.d_site_mass, (size_t)e.numatm));
+  ERMOD_CUDA(cudaMemcpy(e.d_agg_mass, hm.data(), sizeof(double) * e.numatm, cudaMemcpyHostToDevice));
+  ERMOD_CUDA(cudaMemcpy(e.d_site_mass, sitemass, sizeof(double) * e.numatm, cudaMemcpyHostToDevice));
+  return ERMOD_OK;
+}
+
+// load_refstructure (insertion.F90:619-700): refspec atoms and the reference solute
+int ermod_set_reference_structure(ermod_ctx* c, const int* ref_mol, const double* refhost_crd,
+                                  const double* refhost_weight, int refslt_natom, const double* refslt_crd,
+                                  const double* refslt_weight) {
+  if (!c || !ref_mol || !refslt_crd || !refslt_weight) return fail_param("null argument");
+  Engine& e = c->e;
+  if (!e.topo_ready) return fail_param("ermod_set_topology must come first");
+  if (refslt_natom <= 0 || refslt_natom > kMaxSoluteSites) return fail_param("refslt_natom out of range");
+  cudaSetDevice(e.device);
+  ERMOD_CUDA(cudaStreamSynchronize(e.stream));
+  std::vector<int> atoms;
+  for (int i = 0; i < e.nummol; ++i)
+    if (ref_mol[i])
+      for (int a = e.mbi0[i]; a < e.mbi0[i + 1]; ++a) atoms.push_back(a);
+  const int nh = (int)atoms.size();
+  if (nh > 0 && (!refhost_crd || !refhost_weight)) return fail_param("null reference host");
+  std::vector<double> host(4 * (size_t)std::max(nh, 1)), slt(4 * (size_t)refslt_natom);
+  double wh = 0.0, ws = 0.0;
+  for (int k = 0; k < nh; ++k) {
+    for (int i = 0; i < 3; ++i) host[4 * k + i] = refhost_crd[3 * k + i];
+    host[4 * k + 3] = refhost_weight[k];
+    wh += refhost_weight[k];
+  }
+  for (int k = 0; k < refslt_natom; ++k) {
+    for (int i = 0; i < 3; ++i) slt[4 * k + i] = refslt_crd[3 * k + i];
+    slt[4 * k + 3] = refslt_weight[k];
+    ws += refslt_weight[k];
+  }
+  if (nh > 0 && wh == 0.0) return fail_param("bst_zrw: the reference host has no weight");
+  if (ws == 0.0) return fail_param("bst_zrw: the reference solute has no weight");
+  dfree(e.d_ref_atoms);
+  dfree(e.d_ref_host);
+  dfree(e.d_ref_slt);
+  ERMOD_CUDA(dalloc(&e.d_ref_atoms, (size_t)std::max(nh, 1)));
+  ERMOD_CUDA(dalloc(&e.d_ref_host, host.size()));
+  ERMOD_CUDA(dalloc(&e.d_ref_slt, slt.size()));
+  if (nh > 0) ERMOD_CUDA(cudaMemcpy(e.d_ref_atoms, atoms.data(), sizeof(int) * nh, cudaMemcpyHostToDevice));
+  ERMOD_CUDA(cudaMemcpy(e.d_ref_host, host.data(), sizeof(double) * host.size(), cudaMemcpyHostToDevice));
+  ERMOD_CUDA(cudaMemcpy(e.d_ref_slt, slt.data(), sizeof(double) * slt.size(), cudaMemcpyHostToDevice));
+  e.ref_nh = nh;
+  e.ref_ns = refslt_natom;
+  return ERMOD_OK;
+}
+
+// check_mol_configuration (engproc.F90:1046-1100): solution mode
+int ermod_set_configuration_check(ermod_ctx* c, int insposition, double lwreg, double upreg, int insstructure,
+                                  double lwstr, double upstr) {
+  if (!c) return fail_param("null context");
+  Engine& e = c->e;
+  if (!e.topo_ready) return fail_param("ermod_set_topology must come first");
+  if (insposition < 0 || insposition > 6 || insstructure < 0 || insstructure > 1)
+    return fail_param("insposition 0..6, insstructure 0..1");
+  cudaSetDevice(e.device);
+  ERMOD_CUDA(cudaStreamSynchronize(e.stream));
+  const int pos = (insposition >= 2 && insposition <= 5) ? insposition : 0;  // 0, 1, 6 test nothing
+  if ((pos == 3 || pos == 4) && e.P.boxshp == 0) {
+    g_err = "eng_slb: a slab check needs a periodic system";
+    return ERMOD_E_ENG_SLB;
+  }
+  if (pos >= 2 && pos <= 4 && !e.d_agg_mass) return fail_param("ermod_set_aggregate must come first");
+  if (pos == 5 || insstructure == 1) {
+    if (e.ref_ns == 0) return fail_param("ermod_set_reference_structure must come first");
+    if (pos == 5 && e.ref_nh == 0) return fail_param("insposition 5 needs reference host atoms");
+    for (int i = 0; i < e.nummol; ++i)  // numsite(tagslt) /= refslt_natom stops the reference
+      if (e.sluvid[i] == 1 && e.mbi0[i + 1] - e.mbi0[i] != e.ref_ns)
+        return fail_param("eng_bug: a solute molecule and the reference solute differ in size");
+  }
+  e.cfg_pos = pos;
+  e.cfg_str = insstructure;
+  e.cfg_lw = lwreg;
+  e.cfg_up = upreg;
+  e.cfg_lwstr = lwstr;
+  e.cfg_upstr = upstr;
+  if ((pos || insstructure) && e.cap_skip < std::max(64, e.nummol)) {
+    dfree(e.d_skip);
+    e.cap_skip = std::max(64, e.nummol);
+    ERMOD_CUDA(dalloc(&e.d_skip, (size_t)e.cap_skip));
+  }
+  return ERMOD_OK;
+}
+
 int ermod_intermediate_enable(ermod_ctx* c, const double* refs_density) {
   if (!c || !refs_density) return fail_param("null argument");
   Engine& e = c->e;
@@ -1450,8 +1588,15 @@ int ermod_generate_placements(ermod_ctx* c, int nplace, int nsite, const double*
   if (!e.frame_ready) return fail_param("ermod_frame must come first (its cell is used)");
   if (nsite < 1 || nsite > kMaxSoluteSites) return fail_param("nsite must be 1..256");
   if (ip->insposition < 0 || ip->insposition > 6 || ip->insorient < 0 || ip->insorient > 1 || ip->insorigin < 0 ||
-      ip->insorigin > 1)
-    return fail_param("insposition 0..6, insorient 0..1, insorigin 0..1");
+      ip->insorigin > 3)
+    return fail_param("insposition 0..6, insorient 0..1, insorigin 0..3");
+  if (ip->insorigin == 2 && !e.d_agg_mass) return fail_param("insorigin 2 needs ermod_set_aggregate");
+  if (ip->insorigin == 3) {
+    if (e.ref_ns == 0 || e.ref_nh == 0) return fail_param("insorigin 3 needs ermod_set_reference_structure");
+    if (nsite != e.ref_ns) return fail_param("ins_bug: the solute and the reference solute differ in size");
+    // check_solute_configuration accepts only these with the reference structure
+    if (ip->insposition != 5 && ip->insposition != 6) return fail_param("ins_bug: insorigin 3 needs insposition 5 or 6");
+  }
   if ((ip->insposition == 2 || ip->insposition == 3 || ip->insposition == 4) && !(ip->upreg >= ip->lwreg))
     return fail_param("upreg < lwreg");
   if ((ip->insposition == 5 || ip->insposition == 6) && !(ip->upreg > 0.0)) return fail_param("upreg must be > 0");
@@ -1462,6 +1607,7 @@ int ermod_generate_placements(ermod_ctx* c, int nplace, int nsite, const double*
   if (nplace <= 0) return ERMOD_OK;
   cudaSetDevice(e.device);
   if (!e.d_ins) ERMOD_CUDA(dalloc(&e.d_ins, 4 * (size_t)kMaxSoluteSites));
+  if (ip->insorigin >= 2 && !e.d_ref_fit) ERMOD_CUDA(dalloc(&e.d_ref_fit, 6 * (size_t)kMaxSoluteSites + 8));
   ERMOD_CUDA(cudaMemcpyAsync(e.d_ins, bfcoord, sizeof(double) * 3 * nsite, cudaMemcpyHostToDevice, e.stream));
   ERMOD_CUDA(cudaMemcpyAsync(e.d_ins + 3 * kMaxSoluteSites, mass, sizeof(double) * nsite, cudaMemcpyHostToDevice,
                              e.stream));

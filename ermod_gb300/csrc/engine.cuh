@@ -169,6 +169,22 @@ struct Engine {
   float* d_ps_qf = nullptr;      // [Bmax][256]
   float2* d_ps_bvec = nullptr;   // [Bmax][256][3][Kmax]
   double* d_ps_self = nullptr;   // [Bmax][K2]
+  // host aggregate (hostspec) and reference structure (refspec + solute), both cleared by
+  // ermod_set_topology
+  double* d_agg_mass = nullptr;  // [numatm] site masses of the host aggregate (0 elsewhere)
+  double* d_site_mass = nullptr; // [numatm] site masses of every molecule
+  int ref_nh = 0, ref_ns = 0;    // reference host atoms and solute sites (ref_ns 0: none set)
+  int* d_ref_atoms = nullptr;    // [ref_nh] 0-based atoms of the refspec molecules, in order
+  double* d_ref_host = nullptr;  // [ref_nh][4] reference coordinates, weight
+  double* d_ref_slt = nullptr;   // [ref_ns][4] reference solute coordinates, weight
+  double* d_ref_fit = nullptr;   // generator: [256][3] starting structure, [256][3] fitted reference
+                                 // solute (insorigin 3), or [3] the aggregate centre (insorigin 2)
+  // solution-mode configuration check (check_mol_configuration): insposition 2-5 or 0
+  // (no position test), insstructure 1 or 0
+  int cfg_pos = 0, cfg_str = 0;
+  double cfg_lw = 0.0, cfg_up = 0.0, cfg_lwstr = 0.0, cfg_upstr = 0.0;
+  int* d_skip = nullptr;         // [cap_skip] 1: the placement is skipped
+  int cap_skip = 0;
   unsigned char* d_int_mask = nullptr;  // intermediate state: [ermax] zero-density bins
   double* d_edintm = nullptr;            // [ermax] edintm, [numslv] uvintm, [3] totals
   double* d_ins = nullptr;       // [4][256] solute reference coordinates and masses (placement generator)

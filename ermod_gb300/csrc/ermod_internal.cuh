@@ -221,6 +221,7 @@ struct BatchArgs {
   double* engnmfc;     // [nb] weights (0 for skipped placements)
   double* u0;          // [nb] solute self energies
   int* self_bin;       // [nb] eself bin (0-based) or -1
+  const int* skip;     // [nb] 1: the configuration check skips the placement (solution mode), or null
 };
 
 struct Engine;
@@ -233,6 +234,8 @@ cudaError_t launch_max_abs(Engine& e, const double* x_d, size_t n, double* host_
 cudaError_t launch_frame_sort(Engine& e);
 cudaError_t launch_frame_sites(Engine& e);
 cudaError_t launch_greenfunc(Engine& e);
+// solution mode: the placements check_mol_configuration would skip (e.d_skip[0..nplace))
+cudaError_t launch_config_check(Engine& e, int nplace, const int* d_tag);
 // placement preparation and PME
 cudaError_t launch_place_prep(Engine& e, const BatchArgs& a, const double* sol_xyz, int self_first_only,
                               cudaStream_t s);

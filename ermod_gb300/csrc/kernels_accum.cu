@@ -52,6 +52,16 @@ struct AccArgs {
 constexpr int kAccThreads = 256;
 constexpr int kMaxBatch = 512;
 
+// an error in this batch or an earlier one of the call; errors of later batches (already
+// running on the other stream) do not stop this batch's accumulation.  The answer cannot
+// change between the accumulation kernels of a batch: the earlier batches' kernels are
+// complete by then and the error key only decreases.
+__device__ __forceinline__ bool batch_failed(const AccArgs& A) {
+  const volatile unsigned long long* ek = &A.status->err_key;
+  const unsigned long long k = *ek;
+  return k != kNoError && (long long)(k >> 36) < (long long)A.a.b0 + A.a.nb;
+}
+
 // fixed-order block sum: thread t adds elements t, t+256, ... in order, then a fixed tree
 __device__ __forceinline__ double block_sum_fixed(double* red, const double* x, int n, int stride) {
   double s = 0.0;
@@ -113,7 +123,11 @@ __global__ void __launch_bounds__(kAccThreads) reduce_kernel(AccArgs A) {
       if (a.flceng_out) a.flceng_out[(size_t)(a.b0 + b) * A.numslv + sp] = s;
     }
   }
-  if (threadIdx.x == 0) {
+  if (threadIdx.x == 0 && a.skip && a.skip[b]) {  // rejected by check_mol_configuration
+    A.u0[b] = 0.0;
+    A.self_bin[b] = -1;
+    if (a.uvengy_out) a.uvengy_out[(size_t)(a.b0 + b) * (A.slvmax + 1)] = 0.0;
+  } else if (threadIdx.x == 0) {
     double usreal;
     if (A.rigid)
       usreal = (A.scal[6] != 0.0) ? A.scal[5] : a.u_usreal[0];
@@ -169,17 +183,22 @@ __global__ void __launch_bounds__(kAccThreads) accumulate_kernel(AccArgs A) {
   __shared__ int sbin[kMaxBatch];
   __shared__ double sterm[kMaxBatch];
   __shared__ double sred[2][kAccThreads];
+  __shared__ unsigned char srej[kMaxBatch];  // rejected by the configuration check
   __shared__ int skip;
   __shared__ double s_voffset;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) srej[b] = (a.skip && a.skip[b]) ? 1 : 0;
+  __syncthreads();
   if (threadIdx.x == 0) {
-    const volatile unsigned long long* ek = &A.status->err_key;
-    // an error in this batch or an earlier one of the call; errors of later batches
-    // (already running on the other stream) do not stop this batch's accumulation
-    const unsigned long long k = *ek;
-    skip = (k != kNoError && (long long)(k >> 36) < (long long)a.b0 + nb) ? 1 : 0;
+    skip = batch_failed(A) ? 1 : 0;
     if (!skip && A.wgtslf && A.scal[4] == 0.0) {
-      A.scal[3] = A.u0[0];  // voffset from the first placement ever processed
-      A.scal[4] = 1.0;
+      // voffset from the first placement ever accumulated (update_histogram,
+      // engproc.F90:779-783); rejected placements never reach it
+      int first = 0;
+      while (first < nb && srej[first]) ++first;
+      if (first < nb) {
+        A.scal[3] = A.u0[first];
+        A.scal[4] = 1.0;
+      }
     }
     if (!skip && A.rigid && A.scal[6] == 0.0) {
       A.scal[5] = a.u_usreal[0];
@@ -199,6 +218,14 @@ __global__ void __launch_bounds__(kAccThreads) accumulate_kernel(AccArgs A) {
   for (int b = threadIdx.x; b < nb; b += blockDim.x) {
     su0[b] = A.u0[b];
     sbin[b] = A.self_bin[b];
+    if (srej[b]) {  // the loop's skipcond (engproc.F90:389-390): no update_histogram
+      sw[b] = 0.0;
+      stw[b] = 0.0;
+      a.engnmfc[b] = 0.0;
+      A.ring_w[b] = 0.0;
+      A.ring_valid[b] = 0;
+      continue;
+    }
     double engnmfc;
     if (!A.wgtslf) {
       engnmfc = 1.0;
@@ -224,6 +251,7 @@ __global__ void __launch_bounds__(kAccThreads) accumulate_kernel(AccArgs A) {
     double engnorm = A.scal[0], engsmpl = A.scal[1], avslf = A.scal[2];
     double mn = A.minuv[0], mx = A.maxuv[0];
     for (int b = 0; b < nb; ++b) {
+      if (srej[b]) continue;
       engnorm = engnorm + sw[b];
       engsmpl = engsmpl + 1.0;
       avslf = avslf + stw[b];
@@ -261,7 +289,8 @@ __global__ void __launch_bounds__(kAccThreads) accumulate_kernel(AccArgs A) {
       A.maxuv[sp + 1] = fmax(A.maxuv[sp + 1], sred[1][0]);
       if (A.soln) {
         double sl = A.slnuv[sp];
-        for (int b = 0; b < nb; ++b) sl = sl + sterm[b];
+        for (int b = 0; b < nb; ++b)
+          if (!srej[b]) sl = sl + sterm[b];
         A.slnuv[sp] = sl;
       }
     }
@@ -297,6 +326,7 @@ __global__ void __launch_bounds__(kAccThreads) accumulate_kernel(AccArgs A) {
     if (threadIdx.x == 0) {
       double tot = A.iscal[0], in = A.iscal[1], nrm = A.iscal[2];
       for (int b = 0; b < nb; ++b) {
+        if (srej[b]) continue;
         tot = tot + sw[b];
         if (!sout[b]) {
           in = in + sw[b];
@@ -330,7 +360,7 @@ __global__ void __launch_bounds__(kAccThreads) accumulate_kernel(AccArgs A) {
 __global__ void __launch_bounds__(128) accumulate_bins_kernel(AccArgs A) {
   const BatchArgs& a = A.a;
   const int nb = a.nb;
-  if (nb <= 0 || A.ring_valid[0] == 0) return;  // the batch was not accumulated (an error)
+  if (nb <= 0 || batch_failed(A)) return;  // the batch was not accumulated (an error)
   __shared__ double sw[kMaxBatch];
   for (int b = threadIdx.x; b < nb; b += blockDim.x) sw[b] = a.engnmfc[b];
   __syncthreads();

@@ -15,6 +15,8 @@
 //           (Z = X + iY); writes the real plane phi[b][z][y][x] with coalesced stores.
 // Transforms are self-sorting Stockham passes (radices 2-16, composite radices done in
 // registers), unnormalised, sign +1, exactly the conventions of fft_iface.F90.
+#include <cooperative_groups.h>
+
 #include "engine.cuh"
 
 namespace ermod {
@@ -406,7 +408,7 @@ __device__ __forceinline__ void fft3_t(const float2* in, float2* mid, float2* mi
 
 constexpr int kSites = 32;  // solute sites staged per chunk
 constexpr int kR1 = 4, kR3 = 3;  // generation tile: kR3 k3 values x kR1 k1 values per thread
-static_assert(kR1 == 4, "pme_a reads a tile row's engfac values as one float4");
+// Hp = H rounded up to a multiple of kR1, so that the TX = Hp / kR1 tile columns cover k1 < Hp
 
 struct PmeArgs {
   const float2* bvec;   // [nb][S][3][Kmax]
@@ -435,11 +437,11 @@ __global__ void __launch_bounds__(kPmeAThreads, kPmeAMinBlocks) pme_a_kernel(Pme
   float2* slab = sm;                          // [K3][Hp]
   float2* work = sm + (size_t)K3 * Hp;        // [K3][Hp]; site staging during generation
   float2* tw3 = work + (size_t)K3 * Hp;       // [K3]
+  const int ns = A.u_nsite[b];
   for (int i = threadIdx.x; i < K3; i += blockDim.x) {
     const float2 t = A.twiddle[A.K1 + A.K2 + i];
     tw3[i] = make_float2(t.x, -t.y);
   }
-  const int ns = A.u_nsite[b];
   const float2* bv = A.bvec + (size_t)b * kMaxSoluteSites * 3 * A.Kmax;
   const int TX = Hp / kR1, TY = (K3 + kR3 - 1) / kR3;
   const bool even = (A.K1 % 2) == 0;
@@ -447,30 +449,61 @@ __global__ void __launch_bounds__(kPmeAThreads, kPmeAMinBlocks) pme_a_kernel(Pme
   // ---- generation: slab(k3, k1) = sum_s [q_s b2_s(k2) b3_s(k3)] b1_s(k1), then (last
   // chunk) the engfac multiply and the self energy sum 0.5 sum_k engfac |S|^2 ----
   float2* sd = work;                         // [chunk][K3]
-  // [chunk][kR1][TX]: b1(k1 = kR1 tx + i) at [i][tx], so that the lanes of a warp (consecutive
-  // tx) read consecutive words
+  // [chunk][Hp]: b1(k1); a tile thread tx takes k1 = tx + i TX (i < kR1), so that the lanes
+  // of a warp (consecutive tx) read and write consecutive words of every row
   float2* sb = work + (size_t)A.chunk * K3;
   for (int s0 = 0; s0 < ns; s0 += A.chunk) {
     const int nsc = min(A.chunk, ns - s0);
     const bool last = s0 + A.chunk >= ns;
     __syncthreads();
-    for (int t = threadIdx.x; t < nsc * K3; t += blockDim.x) {
-      const int sl = t / K3, k3 = t - sl * K3;
-      const size_t us = (size_t)(s0 + sl);
-      const float q = A.u_qf[(size_t)b * kMaxSoluteSites + us];
-      const float2 b2 = bv[(us * 3 + 1) * A.Kmax + k2];
-      const float2 b3 = bv[(us * 3 + 2) * A.Kmax + k3];
-      sd[sl * K3 + k3] = cmul(make_float2(q * b2.x, q * b2.y), b3);
-    }
-    for (int t = threadIdx.x; t < nsc * Hp; t += blockDim.x) {
-      const int sl = t / Hp, k1 = t - sl * Hp;
-      sb[sl * Hp + (k1 % kR1) * TX + k1 / kR1] =
-          (k1 < H) ? bv[((size_t)(s0 + sl) * 3 + 0) * A.Kmax + k1] : make_float2(0.f, 0.f);
+    // staging: each thread first issues the loads of its entries of both tables (and the
+    // first nsc threads those of q b2(k2) per site), then forms and stores them, so that
+    // one L2 round trip covers its share (issued one entry at a time, the round trips made
+    // the staging about a third of the CTA's time)
+    constexpr int kStage = 2;
+    const int nd = nsc * K3, n1 = nsc * Hp;
+    __shared__ float2 sqb2[kSites];  // q_s b2_s(k2)
+    // rounds counted from 0 in every thread, so that all of them meet the barrier below
+    // equally often
+    for (int r0 = 0; r0 < max(nd, n1); r0 += kStage * blockDim.x) {
+      const int base = r0 + (int)threadIdx.x;
+      float2 b3[kStage], b1[kStage];
+#pragma unroll
+      for (int i = 0; i < kStage; ++i) {
+        const int t = base + i * blockDim.x;
+        if (t < nd) {
+          const int sl = t / K3, k3 = t - sl * K3;
+          b3[i] = bv[((size_t)(s0 + sl) * 3 + 2) * A.Kmax + k3];
+        }
+        if (t < n1) {
+          const int sl = t / Hp, k1 = t - sl * Hp;
+          b1[i] = (k1 < H) ? bv[((size_t)(s0 + sl) * 3 + 0) * A.Kmax + k1] : make_float2(0.f, 0.f);
+        }
+      }
+      if (r0 == 0 && threadIdx.x < (unsigned)nsc) {
+        const size_t us = (size_t)(s0 + threadIdx.x);
+        const float q = A.u_qf[(size_t)b * kMaxSoluteSites + us];
+        const float2 b2 = bv[(us * 3 + 1) * A.Kmax + k2];
+        sqb2[threadIdx.x] = make_float2(q * b2.x, q * b2.y);
+      }
+      __syncthreads();  // sqb2 staged
+#pragma unroll
+      for (int i = 0; i < kStage; ++i) {
+        const int t = base + i * blockDim.x;
+        if (t < nd) {
+          const int sl = t / K3, k3 = t - sl * K3;
+          sd[sl * K3 + k3] = cmul(sqb2[sl], b3[i]);
+        }
+        if (t < n1) {
+          const int sl = t / Hp, k1 = t - sl * Hp;
+          sb[sl * Hp + k1] = b1[i];
+        }
+      }
     }
     __syncthreads();
     for (int mt = threadIdx.x; mt < TX * TY; mt += blockDim.x) {
       const int ty = KC ? mt / TX : fdiv(mt, A.fHp4), tx = mt - ty * TX;
-      const int k1a = tx * kR1, k3a = ty * kR3;
+      const int k3a = ty * kR3;
       float2 acc[kR3][kR1];
 #pragma unroll
       for (int j = 0; j < kR3; ++j)
@@ -495,29 +528,25 @@ __global__ void __launch_bounds__(kPmeAThreads, kPmeAMinBlocks) pme_a_kernel(Pme
       for (int j = 0; j < kR3; ++j) {
         const int k3 = k3a + j;
         if (k3 >= K3) continue;
-        float4* dst = reinterpret_cast<float4*>(slab + (size_t)k3 * Hp + k1a);
+        float2* dst = slab + (size_t)k3 * Hp + tx;  // element i at dst[i TX]
         if (s0 != 0) {
-          const float4 o0 = dst[0], o1 = dst[1];
-          acc[j][0] = cadd(acc[j][0], make_float2(o0.x, o0.y));
-          acc[j][1] = cadd(acc[j][1], make_float2(o0.z, o0.w));
-          acc[j][2] = cadd(acc[j][2], make_float2(o1.x, o1.y));
-          acc[j][3] = cadd(acc[j][3], make_float2(o1.z, o1.w));
+#pragma unroll
+          for (int i = 0; i < kR1; ++i) acc[j][i] = cadd(acc[j][i], dst[i * TX]);
         }
         if (last) {  // FP32 engfac rows are Hp points long, zeros beyond H
-          const float4 f4 = __ldg(reinterpret_cast<const float4*>(A.engfac + ((size_t)k3 * A.K2 + k2) * Hp + k1a));
-          const float fv[kR1] = {f4.x, f4.y, f4.z, f4.w};
+          const float* frow = A.engfac + ((size_t)k3 * A.K2 + k2) * Hp + tx;
 #pragma unroll
           for (int i = 0; i < kR1; ++i) {
-            const int k1 = k1a + i;
-            const float f = fv[i];
+            const int k1 = tx + i * TX;
+            const float f = __ldg(frow + i * TX);
             const float2 q = acc[j][i];
             const float wgt = (k1 == 0 || (even && k1 == H - 1)) ? 0.5f : 1.f;
             tile_self += wgt * f * (q.x * q.x + q.y * q.y);
             acc[j][i] = make_float2(f * q.x, f * q.y);
           }
         }
-        dst[0] = make_float4(acc[j][0].x, acc[j][0].y, acc[j][1].x, acc[j][1].y);
-        dst[1] = make_float4(acc[j][2].x, acc[j][2].y, acc[j][3].x, acc[j][3].y);
+#pragma unroll
+        for (int i = 0; i < kR1; ++i) dst[i * TX] = acc[j][i];
       }
       if (last) self = ff_add(self, tile_self);
     }
@@ -757,14 +786,22 @@ __device__ __forceinline__ float2* pme_b_planes(const PmeArgs& A, const float2* 
 
 // CTA per (z, placement): the k2 transform of the (k2, k1) plane, then the
 // complex-to-real transform along k1, two rows per complex transform; writes the real
-// plane phi[b][z][y][x] with coalesced row stores.
+// plane into the placement's lane of the interleaved potential grid.
+// Compile-time sizes (KC > 0): the four CTAs of an interleaved group (the same plane of
+// four placements) form a thread-block cluster.  Once their planes are done, each CTA
+// reads a quarter of the rows of all four planes through distributed shared memory and
+// writes them as whole float4 points (16-byte stores, full 32-byte sectors), instead of
+// every CTA storing 4 bytes at a 16-byte stride (a quarter-used sector per store).
 template <int KC>
 __global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(PmeArgs A) {
   extern __shared__ __align__(16) float2 sm[];  // 16-byte loads of row pairs
   // grid (4, K3, ceil(nb / 4)): the four placements that share an interleaved potential
-  // grid run side by side, so their 4-byte stores meet in L2
+  // grid run side by side
   const int z = blockIdx.y, b = 4 * blockIdx.z + blockIdx.x;
-  if (b >= A.nb) return;
+  const bool live = b < A.nb;  // the last group may hold fewer than four placements
+  if constexpr (KC == 0) {
+    if (!live) return;
+  }
   const int K1 = KC ? KC : A.K1, K2 = KC ? KC : A.K2, K3 = KC ? KC : A.K3;
   const int H = KC ? KC / 2 + 1 : A.H, K1p = KC ? (KC | 1) : A.K1p;
   const size_t plane = (size_t)K2 * H;
@@ -784,11 +821,13 @@ __global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(Pme
   const float2* in = A.t1 + ((size_t)b * K3 + z) * plane;
   // k2 transforms, row-pair packing and the complex-to-real row transforms; res holds
   // the real rows, pair p (rows 2p, 2p + 1 interleaved) K1p apart
-  float2* res;
-  if constexpr (KC > 0 && two_pass(KC) && KC % 4 == 0)
-    res = pme_b_planes_fused<KC>(in, s0, s1, tw1);
-  else
-    res = pme_b_planes<KC>(A, in, s0, s1, tw1, tw2);
+  float2* res = nullptr;
+  if (live) {
+    if constexpr (KC > 0 && two_pass(KC) && KC % 4 == 0)
+      res = pme_b_planes_fused<KC>(in, s0, s1, tw1);
+    else
+      res = pme_b_planes<KC>(A, in, s0, s1, tw1, tw2);
+  }
   // padded periodic layout: grid point (x, y, z) lives at (x+h, y+h, z+h), h = P-1, and
   // the last h points of every axis are repeated below 0, so any stencil halo of the
   // gather is one in-bounds box (rows XP floats, planes YP rows, ZP planes)
@@ -800,6 +839,19 @@ __global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(Pme
   const int ncopy = (z >= K3 - h) ? 2 : 1;
   const float* resf = reinterpret_cast<const float*>(res);  // row pair p: (y = 2p, 2p+1) interleaved
   if constexpr (KC > 0) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    __shared__ int sres_off;  // res within sm (float2 elements), -1 when the CTA has no placement
+    if (threadIdx.x == 0) sres_off = live ? (int)(res - sm) : -1;
+    cluster.sync();  // the four planes are complete and visible to the cluster
+    const float2* rb[4];
+    unsigned rlive = 0u;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int off = *cluster.map_shared_rank(&sres_off, k);
+      if (off >= 0) rlive |= 1u << k;
+      rb[k] = cluster.map_shared_rank(sm, k) + (off >= 0 ? off : 0);
+    }
     // the lane's padded columns xx = lane + 32 i and their source columns, set up once
     constexpr int NX = (KC + 7 + 31) / 32;  // h <= 7
     int sx[NX];
@@ -810,29 +862,34 @@ __global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(Pme
       sx[i] = (xx < h) ? xx - h + KC : xx - h;
       if (xx < KX) ok |= 1u << i;
     }
+    float4* grid4 = reinterpret_cast<float4*>(A.phi) + (size_t)blockIdx.z * A.ZP * A.YP * A.XP;
+    const int rank = blockIdx.x;  // == the cluster rank (cluster dims (4, 1, 1))
     for (int c = 0; c < ncopy; ++c) {
-      float* plane_out = out + (size_t)(c ? z - K3 + h : z + h) * A.YP * A.XP * 4 + 4 * lane;
-      // one warp per row pair: one 8-byte load gives rows y = 2p (.x) and 2p + 1 (.y);
-      // row y is stored at padded row y + h and, when y >= K2 - h, also at y + h - K2
-      for (int pp = warp; pp < npair; pp += nwarp) {
-        const float2* src = res + (size_t)pp * (KC | 1);
-        float2 v[NX];
+      float4* plane_out = grid4 + (size_t)(c ? z - K3 + h : z + h) * A.YP * A.XP + lane;
+      // one warp per row pair of this CTA's quarter (pairs rank, rank + 4, ...): one 8-byte
+      // load per placement gives rows y = 2p (.x) and 2p + 1 (.y); row y is stored at
+      // padded row y + h and, when y >= K2 - h, also at y + h - K2
+      for (int pp = rank + 4 * warp; pp < npair; pp += 4 * nwarp) {
+        const size_t prow = (size_t)pp * (KC | 1);
 #pragma unroll
-        for (int i = 0; i < NX; ++i) v[i] = (ok & (1u << i)) ? src[sx[i]] : make_float2(0.f, 0.f);
+        for (int i = 0; i < NX; ++i) {
+          if (!(ok & (1u << i))) continue;
+          float2 v[4];
 #pragma unroll
-        for (int e = 0; e < 2; ++e) {
-          const int y = 2 * pp + e;
-          if (y >= KC) break;
-          for (int rep = 0; rep < 2; ++rep) {
-            if (rep && y < KC - h) break;
-            float* dst = plane_out + (size_t)(rep ? y + h - KC : y + h) * A.XP * 4;
+          for (int k = 0; k < 4; ++k) v[k] = (rlive & (1u << k)) ? rb[k][prow + sx[i]] : make_float2(0.f, 0.f);
 #pragma unroll
-            for (int i = 0; i < NX; ++i)
-              if (ok & (1u << i)) dst[128 * i] = e ? v[i].y : v[i].x;
+          for (int e = 0; e < 2; ++e) {
+            const int y = 2 * pp + e;
+            if (y >= KC) break;
+            const float4 q = e ? make_float4(v[0].y, v[1].y, v[2].y, v[3].y)
+                               : make_float4(v[0].x, v[1].x, v[2].x, v[3].x);
+            plane_out[(size_t)(y + h) * A.XP + 32 * i] = q;
+            if (y >= KC - h) plane_out[(size_t)(y + h - KC) * A.XP + 32 * i] = q;
           }
         }
       }
     }
+    cluster.sync();  // no CTA leaves while another still reads its shared memory
   } else {
     for (int c = 0; c < ncopy; ++c) {
       float* plane_out = out + (size_t)(c ? z - K3 + h : z + h) * A.YP * A.XP * 4;
@@ -933,7 +990,23 @@ cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a) {
     e.phase_end_on(a.stream);
     e.phase_begin_on(PH_FFT, a.stream);
   }
-  kb<<<dim3(4, A.K3, (a.nb + 3) / 4), kPmeBThreads, sb, a.stream>>>(A);
+  if (slot) {  // compile-time sizes: the four CTAs of a group are one cluster
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(4, A.K3, (a.nb + 3) / 4);
+    cfg.blockDim = dim3(kPmeBThreads);
+    cfg.dynamicSmemBytes = sb;
+    cfg.stream = a.stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 4;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if ((err = cudaLaunchKernelEx(&cfg, kb, A)) != cudaSuccess) return err;
+  } else {
+    kb<<<dim3(4, A.K3, (a.nb + 3) / 4), kPmeBThreads, sb, a.stream>>>(A);
+  }
   e.count_launch();
   return cudaGetLastError();
 }

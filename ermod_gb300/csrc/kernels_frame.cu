@@ -15,8 +15,10 @@
 // All of these are HBM-streaming kernels over O(numatm) or O(K^3) elements.
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
+#include <cmath>
 #include <cstring>
 
+#include "bestfit.cuh"
 #include "engine.cuh"
 
 namespace ermod {
@@ -545,6 +547,219 @@ double host_spline_value(int order, double x) {
     for (int i = 0; i <= k; ++i) f = f + s.c[i] * ipow(x - (double)i, order - 1);
   }
   return f;
+}
+
+}  // namespace ermod
+
+namespace ermod {
+namespace {
+
+// ---- solution mode's configuration check (check_mol_configuration) ------------------
+
+struct CheckArgs {
+  const double* sitepos;    // (3, numatm) as the frame gave them
+  const double* agg_mass;   // [numatm] host-aggregate site masses, 0 elsewhere
+  const double* site_mass;  // [numatm]
+  const int* mbi0;
+  int numatm, nummol;
+  const int* tag;
+  int nplace;
+  int pos, str;  // insposition 2-5 or 0; insstructure 1 or 0
+  double lw, up, lwstr, upstr;
+  double inv3[3], len3;  // row 3 of the inverse cell, |cell axis 3|
+  int ref_nh, ref_ns;
+  const int* ref_atoms;    // [ref_nh]
+  const double* ref_host;  // [ref_nh][4]
+  const double* ref_slt;   // [ref_ns][4]
+  DevStatus* status;
+  int* skip;
+};
+
+// n sums over the block (fixed tree), returned to every thread
+template <int N>
+__device__ void block_sums(double (*red)[256], double (&v)[N]) {
+  for (int c = 0; c < N; ++c) red[c][threadIdx.x] = v[c];
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+      for (int c = 0; c < N; ++c) red[c][threadIdx.x] += red[c][threadIdx.x + st];
+    __syncthreads();
+  }
+  for (int c = 0; c < N; ++c) v[c] = red[c][0];
+  __syncthreads();
+}
+
+// rmsd_nofit (bestfit.F90:256-270) of a solute's sites (from atom a0) against points
+// ref[s][0..2] with weights w(s)
+template <class RefAt, class WAt>
+__device__ double rmsd_nofit_dev(int n, RefAt ref, const double* __restrict__ pos, int a0, WAt w) {
+  double W = 0.0, disp = 0.0;
+  for (int s = 0; s < n; ++s) {
+    W += w(s);
+    double d2 = 0.0;
+    for (int i = 0; i < 3; ++i) {
+      const double dx = pos[3 * (size_t)(a0 + s) + i] - ref(s, i);
+      d2 += dx * dx;
+    }
+    disp += w(s) * d2;
+  }
+  return sqrt(disp / W);
+}
+
+// One CTA for the placements of a call.  The frame-wide parts first: the host
+// aggregate's centre of mass (insposition 2-4; com_aggregate, insertion.F90:539-566), or
+// the reference solute carried into the frame by the best fit of the reference host onto
+// the frame's refspec atoms (insposition 5; engproc.F90:1099-1117).  Then a thread per
+// placement applies the position test and, for a placement that passes, the structure
+// test (insstructure 1: best-fit RMSD, engproc.F90:1127-1141); skip[p] = 1 where the
+// reference sets out_of_range.  FP64 throughout; the block sums run in a fixed order.
+__global__ void __launch_bounds__(256) config_check_kernel(CheckArgs A) {
+  __shared__ double red[9][256];
+  __shared__ double sfit[kMaxSoluteSites][3];  // the fitted reference solute (insposition 5)
+  const double* X = A.sitepos;
+  double ac[3] = {0.0, 0.0, 0.0};
+  if (A.pos >= 2 && A.pos <= 4) {
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int a = threadIdx.x; a < A.numatm; a += blockDim.x) {
+      const double w = A.agg_mass[a];
+      if (w != 0.0) {
+        v[0] += w;
+        for (int c = 0; c < 3; ++c) v[c + 1] += w * X[3 * (size_t)a + c];
+      }
+    }
+    block_sums<4>(red, v);
+    for (int c = 0; c < 3; ++c) ac[c] = v[c + 1] / v[0];
+  } else if (A.pos == 5) {
+    // fit_a_rotate_b(refhost_natom, hostcrd, refhost_crd, refhost_weight, refslt_natom,
+    // refslt_crd, refslt_bestfit): centres, then the centred sums of products
+    double v[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int k = threadIdx.x; k < A.ref_nh; k += blockDim.x) {
+      const double w = A.ref_host[4 * k + 3];
+      const int at = A.ref_atoms[k];
+      v[0] += w;
+      for (int c = 0; c < 3; ++c) {
+        v[1 + c] += w * X[3 * (size_t)at + c];
+        v[4 + c] += w * A.ref_host[4 * k + c];
+      }
+    }
+    block_sums<7>(red, v);
+    double cf[3], cr[3];  // centres: frame host (the fit's reference), reference host
+    for (int c = 0; c < 3; ++c) {
+      cf[c] = v[1 + c] / v[0];
+      cr[c] = v[4 + c] / v[0];
+    }
+    double S9[9];
+    for (int c = 0; c < 9; ++c) S9[c] = 0.0;
+    for (int k = threadIdx.x; k < A.ref_nh; k += blockDim.x) {
+      const double w = A.ref_host[4 * k + 3];
+      const int at = A.ref_atoms[k];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+          S9[3 * j + i] += (X[3 * (size_t)at + i] - cf[i]) * (A.ref_host[4 * k + j] - cr[j]) * w;
+    }
+    block_sums<9>(red, S9);
+    if (threadIdx.x == 0) {
+      double S[3][3], q[4];
+      for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i) S[j][i] = S9[3 * j + i];
+      bestfit::rotation_quaternion(S, q);
+      for (int s = 0; s < A.ref_ns; ++s) {
+        const double b[3] = {A.ref_slt[4 * s], A.ref_slt[4 * s + 1], A.ref_slt[4 * s + 2]};
+        double o[3];
+        bestfit::apply_fit(cf, cr, q, b, o);
+        for (int c = 0; c < 3; ++c) sfit[s][c] = o[c];
+      }
+    }
+    __syncthreads();
+  }
+  const int ns = A.ref_ns;
+  const double* RS = A.ref_slt;
+  auto wslt = [RS](int s) { return RS[4 * s + 3]; };
+  for (int p = threadIdx.x; p < A.nplace; p += blockDim.x) {
+    const int mol = A.tag[p] - 1;
+    int out = 1;  // a tag out of range is never accumulated (the placement call reports it)
+    if (mol >= 0 && mol < A.nummol) {
+      const int a0 = A.mbi0[mol], n = A.mbi0[mol + 1] - a0;
+      out = 0;
+      if (A.pos >= 2 && A.pos <= 4) {  // relative_com (engproc.F90:1151-1172)
+        double sm = 0.0, sc[3] = {0.0, 0.0, 0.0};
+        for (int a = a0; a < a0 + n; ++a) {
+          const double w = A.site_mass[a];
+          sm += w;
+          for (int c = 0; c < 3; ++c) sc[c] += w * X[3 * (size_t)a + c];
+        }
+        double dx[3];
+        for (int c = 0; c < 3; ++c) dx[c] = sc[c] / sm - ac[c];
+        double d;
+        if (A.pos == 2) {
+          d = sqrt(dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2]);
+        } else {
+          d = (A.inv3[0] * dx[0] + A.inv3[1] * dx[1] + A.inv3[2] * dx[2]) * A.len3;
+          if (A.pos == 4) d = fabs(d);
+        }
+        out = (A.lw > d || d > A.up) ? 1 : 0;
+      } else if (A.pos == 5 || A.str == 1) {
+        if (n != ns) {  // numsite(tagslt) /= refslt_natom: 'eng_bug'
+          atomicMin(&A.status->err_key, make_err_key(p, 0, ERMOD_E_ENG_BUG));
+          out = 1;
+        } else if (A.pos == 5) {
+          const double d = rmsd_nofit_dev(ns, [](int s, int c) { return sfit[s][c]; }, X, a0, wslt);
+          out = (A.lw > d || d > A.up) ? 1 : 0;
+        }
+      }
+      if (!out && A.str == 1 && n == ns) {  // rmsd_bestfit(refslt_crd, the solute)
+        double cref[3], cmol[3], q[4];
+        bestfit::fit_transform(
+            ns, [RS](int s, int c) { return RS[4 * s + c]; },
+            [X, a0](int s, int c) { return X[3 * (size_t)(a0 + s) + c]; }, wslt, cref, cmol, q);
+        double W = 0.0, disp = 0.0;
+        for (int s = 0; s < ns; ++s) {
+          const double b[3] = {X[3 * (size_t)(a0 + s)], X[3 * (size_t)(a0 + s) + 1], X[3 * (size_t)(a0 + s) + 2]};
+          double o[3];
+          bestfit::apply_fit(cref, cmol, q, b, o);
+          double d2 = 0.0;
+          for (int c = 0; c < 3; ++c) d2 += (o[c] - RS[4 * s + c]) * (o[c] - RS[4 * s + c]);
+          W += wslt(s);
+          disp += wslt(s) * d2;
+        }
+        const double d = sqrt(disp / W);
+        out = (A.lwstr > d || d > A.upstr) ? 1 : 0;
+      }
+    }
+    A.skip[p] = out;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_config_check(Engine& e, int nplace, const int* d_tag) {
+  CheckArgs A{};
+  A.sitepos = e.d_sitepos;
+  A.agg_mass = e.d_agg_mass;
+  A.site_mass = e.d_site_mass;
+  A.mbi0 = e.d_mbi0;
+  A.numatm = e.numatm;
+  A.nummol = e.nummol;
+  A.tag = d_tag;
+  A.nplace = nplace;
+  A.pos = e.cfg_pos;
+  A.str = e.cfg_str;
+  A.lw = e.cfg_lw;
+  A.up = e.cfg_up;
+  A.lwstr = e.cfg_lwstr;
+  A.upstr = e.cfg_upstr;
+  for (int c = 0; c < 3; ++c) A.inv3[c] = e.geom.invcl[2 + 3 * c];
+  A.len3 = std::sqrt(e.cell[6] * e.cell[6] + e.cell[7] * e.cell[7] + e.cell[8] * e.cell[8]);
+  A.ref_nh = e.ref_nh;
+  A.ref_ns = e.ref_ns;
+  A.ref_atoms = e.d_ref_atoms;
+  A.ref_host = e.d_ref_host;
+  A.ref_slt = e.d_ref_slt;
+  A.status = e.d_status;
+  A.skip = e.d_skip;
+  config_check_kernel<<<1, 256, 0, e.stream>>>(A);
+  e.count_launch();
+  return cudaGetLastError();
 }
 
 }  // namespace ermod

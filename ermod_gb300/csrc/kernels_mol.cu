@@ -450,7 +450,8 @@ __global__ void __launch_bounds__(256) mol_energy_kernel(MolArgs A) {
     if (b >= a.nb) break;  // uniform across the block
     const int tg = a.tagslt[b] - 1;
     const int kskip = (tg >= 0 && tg < A.nummol) ? A.mol_to_k[tg] : -2;
-    const bool active = valid && (k != kskip);
+    // a placement rejected by check_mol_configuration has no molecule (engproc.F90:690-691)
+    const bool active = valid && (k != kskip) && !(a.skip && a.skip[b]);
     double u = 0.0;
     if (active) {
       // ---- reciprocal part ----
@@ -839,6 +840,7 @@ __global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const flo
   __shared__ float sres[G];      // residual factor x solute charge of the G placements
   __shared__ float srcut[G];     // bounding-sphere cutoff of the real-space sum
   __shared__ int skskip[G];      // slot of the solute molecule itself (not a solvent)
+  __shared__ int srej[G];        // placement rejected by check_mol_configuration
   __shared__ int4 supos[G];      // first solute site (fixed point)
   __shared__ unsigned char sspec[256];
   const int tile = blockIdx.y;
@@ -854,6 +856,7 @@ __global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const flo
     srcut[threadIdx.x] = A.rc_f + a.u_radius[b] + A.frame_scal[0];
     const int tg = a.tagslt[b] - 1;
     skskip[threadIdx.x] = (tg >= 0 && tg < A.nummol) ? A.mol_to_k[tg] : -2;
+    srej[threadIdx.x] = (a.skip && a.skip[b]) ? 1 : 0;
     supos[threadIdx.x] = a.u_pos[(size_t)b * kMaxSoluteSites];
   }
   int k = -1, s0 = 0, ns = 0, species = 0;
@@ -912,7 +915,7 @@ __global__ void __launch_bounds__(256, 3) mol_finish_kernel(MolArgs A, const flo
     }
 #pragma unroll
     for (int j = 0; j < G; ++j) {
-      const bool on = j < ng && valid && k != skskip[j];
+      const bool on = j < ng && valid && k != skskip[j] && !srej[j];
       if (on) actm |= 1u << j;
       // residual_ene (engproc.F90:859-869)
       const ff t = on ? ff_add(rs[j], -sres[j] * qmol) : ff{0.f, 0.f};
@@ -1301,7 +1304,8 @@ __global__ void __launch_bounds__(256) adjoint_mol_kernel(MolArgs A, AdjArgs J) 
   const int species = A.slot_species[m];
   const int tg = a.tagslt[b] - 1;
   const int kskip = (tg >= 0 && tg < A.nummol) ? A.mol_to_k[tg] : -2;
-  bool take = (tg + 1 == J.adj_mol) && (k != kskip) && species >= 1 && species <= A.numslv;
+  bool take = (tg + 1 == J.adj_mol) && (k != kskip) && species >= 1 && species <= A.numslv &&
+              !(a.skip && a.skip[b]);
   if (J.first) {
     // the molecule's bin as the finish kernel found it (ermax: not binned)
     const int key = take ? J.mol_bin[m] : A.ermax;

@@ -83,6 +83,43 @@ class EnergyRepresentation:
         s = self.sizes()
         self.slvmax, self.ermax, self.esmax, self.numslv = s
 
+    def set_aggregate(self, host_mol, sitemass):
+        """The host aggregate (hostspec, com_aggregate insertion.F90:539-566): host_mol[i] != 0
+        for the 0-based molecules i that form it; sitemass holds one mass per site."""
+        hm = np.ascontiguousarray(host_mol, np.int32)
+        sm = np.ascontiguousarray(sitemass, np.float64)
+        if len(hm) != int(self.topo["nummol"]) or len(sm) != int(self.topo["numatm"]):
+            raise ValueError("host_mol needs one entry per molecule and sitemass one per site")
+        self._agg_keep = (hm, sm)
+        check(_lib.load().ermod_set_aggregate(self.ctx, _lib.ip(hm), _lib.dp(sm)), "ermod_set_aggregate")
+
+    def set_reference_structure(self, ref_mol, refhost_crd, refhost_weight, refslt_crd, refslt_weight):
+        """The reference structure (load_refstructure, insertion.F90:619-700): the refspec
+        molecules (ref_mol[i] != 0) whose atoms in order have reference coordinates
+        refhost_crd (n, 3) and weights refhost_weight (n), and the solute's refslt_crd (ns, 3)
+        and refslt_weight (ns)."""
+        rm = np.ascontiguousarray(ref_mol, np.int32)
+        hc = np.ascontiguousarray(refhost_crd, np.float64).reshape(-1, 3)
+        hw = np.ascontiguousarray(refhost_weight, np.float64)
+        sc = np.ascontiguousarray(refslt_crd, np.float64).reshape(-1, 3)
+        sw = np.ascontiguousarray(refslt_weight, np.float64)
+        if len(rm) != int(self.topo["nummol"]) or len(hc) != len(hw) or len(sc) != len(sw):
+            raise ValueError("ref_mol needs one entry per molecule; coordinates and weights must pair up")
+        self._ref_keep = (rm, hc, hw, sc, sw)
+        check(_lib.load().ermod_set_reference_structure(self.ctx, _lib.ip(rm), _lib.dp(hc), _lib.dp(hw), len(sc),
+                                                        _lib.dp(sc), _lib.dp(sw)), "ermod_set_reference_structure")
+
+    def set_configuration_check(self, insposition: int, lwreg: float = 0.0, upreg: float = 0.0,
+                                insstructure: int = 0, lwstr: float = 0.0, upstr: float = 0.0):
+        """check_mol_configuration (engproc.F90:1046-1100) for solution mode: a placement whose
+        solute fails the position test (insposition 2 sphere, 3 slab, 4 symmetric slab about
+        the host aggregate; 5 RMSD from the reference solute carried into the frame by the host
+        fit) or the structure test (insstructure 1: best-fit RMSD in [lwstr, upstr]) is
+        skipped; 0, 1 and 6 test no position."""
+        check(_lib.load().ermod_set_configuration_check(self.ctx, int(insposition), float(lwreg), float(upreg),
+                                                        int(insstructure), float(lwstr), float(upstr)),
+              "ermod_set_configuration_check")
+
     def sizes(self):
         a, b, c, d = C.c_int(), C.c_int(), C.c_int(), C.c_int()
         check(_lib.load().ermod_get_sizes(self.ctx, C.byref(a), C.byref(b), C.byref(c), C.byref(d)), "sizes")
@@ -135,8 +172,10 @@ class EnergyRepresentation:
                             insorigin: int = 0, lwreg: float = 0.0, upreg: float = 0.0, seed: int = 1,
                             offset: int = 0, weights: bool = False):
         """n placements of a solute with reference coordinates bfcoord (nsite, 3) and masses,
-        generated on the device in the cell of the last frame (insertion.F90 modes).
-        Returns torch tensors (placements (n, nsite, 3) float64, weights (n,) or None)."""
+        generated on the device in the cell of the last frame (insertion.F90 modes;
+        insorigin 2 needs set_aggregate, 3 set_reference_structure).  Returns torch tensors
+        (placements (n, nsite, 3) float64, weights (n,) or None); a placement the RMSD
+        acceptance of insorigin 3 cannot place raises ErmodError ('ins_geo')."""
         import torch
         bf = np.ascontiguousarray(bfcoord, np.float64)
         m = np.ascontiguousarray(mass, np.float64)
@@ -151,7 +190,7 @@ class EnergyRepresentation:
                                                     C.c_void_p(sol.data_ptr()),
                                                     C.c_void_p(sws.data_ptr()) if weights else None),
               "ermod_generate_placements")
-        self.sync_stream()
+        check(_lib.load().ermod_sync(self.ctx), "ermod_generate_placements")
         return sol, sws
 
     def sync_stream(self):

@@ -11,7 +11,7 @@ module ermod_gpu
   integer(c_int), parameter :: ERMOD_ABI_VERSION = 2
   integer(c_int), parameter :: ERMOD_OK = 0, ERMOD_E_ENG_MIN = 101, ERMOD_E_ENG_SFT = 102, &
        ERMOD_E_ENG_BUG = 103, ERMOD_E_ENG_CNS = 104, ERMOD_E_RCP_CNS = 105, ERMOD_E_RCP_FST = 106, &
-       ERMOD_E_INS_GEO = 107, ERMOD_E_SET_PRS = 108, ERMOD_W_MBIN = 110
+       ERMOD_E_INS_GEO = 107, ERMOD_E_SET_PRS = 108, ERMOD_E_ENG_SLB = 109, ERMOD_W_MBIN = 110
   integer(c_int), parameter :: ERMOD_PRECISION_FP64 = 0, ERMOD_PRECISION_MIXED = 1
 
   type, bind(C) :: ermod_params
@@ -52,6 +52,27 @@ module ermod_gpu
        integer(c_int), value :: numslv, esmax
        integer(c_int), intent(in) :: uvmax(*), uvsoft(*)
        real(c_double), intent(in) :: uvcrd(*), escrd(*)
+     end function
+     integer(c_int) function ermod_set_aggregate(ctx, host_mol, sitemass) bind(C, name="ermod_set_aggregate")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), intent(in) :: host_mol(*)
+       real(c_double), intent(in) :: sitemass(*)
+     end function
+     integer(c_int) function ermod_set_reference_structure(ctx, ref_mol, refhost_crd, refhost_weight, &
+          refslt_natom, refslt_crd, refslt_weight) bind(C, name="ermod_set_reference_structure")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), intent(in) :: ref_mol(*)
+       real(c_double), intent(in) :: refhost_crd(*), refhost_weight(*), refslt_crd(*), refslt_weight(*)
+       integer(c_int), value :: refslt_natom
+     end function
+     integer(c_int) function ermod_set_configuration_check(ctx, insposition, lwreg, upreg, insstructure, &
+          lwstr, upstr) bind(C, name="ermod_set_configuration_check")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: insposition, insstructure
+       real(c_double), value :: lwreg, upreg, lwstr, upstr
      end function
      integer(c_int) function ermod_frame(ctx, sitepos, cell, stat_weight_system) bind(C, name="ermod_frame")
        import :: c_int, c_ptr, c_double

@@ -44,6 +44,7 @@ typedef enum ermod_status {
   ERMOD_E_RCP_FST = 106,   /* 'rcp_fst': the solute is a solvent (recpcal.F90:469) */
   ERMOD_E_INS_GEO = 107,   /* 'ins_geo': random or slab insertion in a non-periodic system (insertion.F90:155,186) */
   ERMOD_E_SET_PRS = 108,   /* 'set_prs': a non-periodic system needs NVT and bare Coulomb (setconf.F90:368-372) */
+  ERMOD_E_ENG_SLB = 109,   /* 'eng_slb': slab configuration check in a non-periodic system (engproc.F90:1088) */
   ERMOD_W_MBIN = 110,      /* 'mbin' warning without force_calculation (engproc.F90:1010-1015) */
   ERMOD_E_PARAM = 120,     /* invalid argument or call order */
   ERMOD_E_NONCUBOID = 121, /* non-cuboid cell: the reference stops (realcal.F90:859-866) */
@@ -109,6 +110,43 @@ int ermod_set_topology(ermod_ctx* ctx, int nummol, int numatm, const int* mol_be
  * escrd(esmax). */
 int ermod_set_bins(ermod_ctx* ctx, int numslv, const int* uvmax, const int* uvsoft,
                    const double* uvcrd, int esmax, const double* escrd);
+
+/* The host aggregate (hostspec; com_aggregate, insertion.F90:539-566): the molecules i
+ * with host_mol[i] != 0 (0-based), and every site's mass sitemass[numatm] (engmain's
+ * sitemass; center_of_mass weights, bestfit.F90:158-172).  Used by the configuration
+ * check of insposition 2-4 and by device-generated placements with insorigin 2.  Call
+ * after ermod_set_topology (which clears it).  A host without mass returns ERMOD_E_PARAM
+ * ('bst_zrw' in the reference). */
+int ermod_set_aggregate(ermod_ctx* ctx, const int* host_mol, const double* sitemass);
+
+/* The reference structure (load_refstructure, insertion.F90:619-700): the refspec
+ * molecules i with ref_mol[i] != 0, whose atoms in order have the reference coordinates
+ * refhost_crd (3, n) and fitting weights refhost_weight (n), and the solute structure
+ * refslt_crd (3, refslt_natom) with weights refslt_weight.  The weights are the host's
+ * (read_refPDF_weight: 1 for heavy atoms, 0 for hydrogens and unlisted atoms).  Used by
+ * the configuration check of insposition 5 and insstructure 1 (solution mode) and by
+ * device-generated placements with insorigin 3 (reffit, insertion.F90:598-624).  Call
+ * after ermod_set_topology (which clears it). */
+int ermod_set_reference_structure(ermod_ctx* ctx, const int* ref_mol, const double* refhost_crd,
+                                  const double* refhost_weight, int refslt_natom, const double* refslt_crd,
+                                  const double* refslt_weight);
+
+/* Solution-mode configuration check (check_mol_configuration, engproc.F90:1046-1100).
+ * The reference skips a solution-mode placement whose solute fails it (get_uv_energy's
+ * out_of_range, the loop's skipcond, engproc.F90:389-390).  Position (insposition):
+ * 2 keeps a solute whose centre of mass lies at a distance in [lwreg, upreg] from that of
+ * the host aggregate, 3 one whose offset from it along cell axis 3 does, 4 one whose
+ * absolute offset does, 5 one whose RMSD from the reference solute structure, carried
+ * into the frame by the best fit of the reference host onto the frame's host atoms, does;
+ * 0, 1 and 6 test nothing (as in the reference).  Structure (insstructure 1): keeps a
+ * solute whose best-fit RMSD from the reference solute structure lies in [lwstr, upstr].
+ * A skipped placement adds nothing to any accumulator and leaves its uvengy and flceng
+ * rows zero.  Slab checks (3, 4) of a non-periodic system return ERMOD_E_ENG_SLB; 2-4
+ * need ermod_set_aggregate, 5 and insstructure 1 ermod_set_reference_structure with a
+ * solute structure as long as every solute molecule ('eng_bug' otherwise: ERMOD_E_PARAM).
+ * Call after ermod_set_topology (which switches the check off). */
+int ermod_set_configuration_check(ermod_ctx* ctx, int insposition, double lwreg, double upreg, int insstructure,
+                                  double lwstr, double upstr);
 
 /* engconst prologue: cell inverse (engproc.F90:898-919), Green function when the
  * cell changed (recpcal.F90:111-152), solvent splines (recpcal.F90:328-340,408-442)
@@ -276,7 +314,12 @@ int ermod_intermediate_enable(ermod_ctx* ctx, const double* refs_density);
 int ermod_intermediate_get(ermod_ctx* ctx, double* edintm, double* uvintm, double* totals);
 
 /* ---- placements generated on the device (instslt, insertion.F90:76-99) --------------
- * insorigin 0: solute COM to the origin (1: as given); insposition 0 random in the cell,
+ * insorigin 0: solute COM to the origin, 1 as given, 2 COM to the host aggregate's
+ * (ermod_set_aggregate), 3 the best fit onto the reference solute structure carried into
+ * the frame (reffit; ermod_set_reference_structure, insposition 5 or 6 only, as the
+ * reference demands, and then a placement whose RMSD from that structure lies outside
+ * [lwreg, upreg] is drawn again: check_solute_configuration, insertion.F90:569-595);
+ * insposition 0 random in the cell,
  * 1 as given, 2 spherical shell lwreg..upreg, 3 slab in z, 4 symmetric slab, 5 random
  * translation within upreg + 3 x solute size, 6 uniform/Gaussian mixture with its
  * weight (engmain.F90:320-326, insertion.F90:133-316); insorient 0: random rotation

@@ -288,6 +288,13 @@ struct orc_ctx {
   std::vector<char> zerodns_crd;          // (ermax)
   std::vector<double> edintm, uvintm;     // (ermax), (numslv)
   double soln_total = 0, soln_intm = 0, norm_intm = 0;
+  // check_mol_configuration (engproc.F90:1046-1100), solution mode
+  int cfg_pos = 0, cfg_str = 0;
+  double cfg_lw = 0.0, cfg_up = 0.0, cfg_lwstr = 0.0, cfg_upstr = 0.0;
+  std::vector<char> cfg_host;     // (nummol) molecule belongs to the host aggregate (hostspec)
+  std::vector<double> cfg_mass;   // (numatm) sitemass
+  std::vector<int> ref_atoms;     // refhost_specatm, 1-based atoms of the refspec molecules
+  std::vector<double> refhost_crd, refhost_weight, refslt_crd, refslt_weight;
   // last placement PME potential (for cross-checks)
   std::vector<double> last_cnv;
   double last_self = 0.0;
@@ -1389,6 +1396,239 @@ int orc_frame(orc_ctx* c, const double* sitepos, const double* cell, double stat
 
 int orc_slvmax(const orc_ctx* c) { return c ? c->slvmax : -1; }
 
+int orc_set_aggregate(orc_ctx* c, const int* host_mol, const double* sitemass) {
+  if (!c || c->nummol <= 0 || !host_mol || !sitemass) return ORC_E_PARAM;
+  c->cfg_host.assign(c->nummol, 0);
+  for (int i = 0; i < c->nummol; ++i) c->cfg_host[i] = host_mol[i] != 0;
+  c->cfg_mass.assign(sitemass, sitemass + c->numatm);
+  return ORC_OK;
+}
+
+int orc_set_reference_structure(orc_ctx* c, const int* ref_mol, const double* refhost_crd,
+                                const double* refhost_weight, int refslt_natom, const double* refslt_crd,
+                                const double* refslt_weight) {
+  if (!c || c->nummol <= 0 || !ref_mol || refslt_natom <= 0) return ORC_E_PARAM;
+  c->ref_atoms.clear();
+  for (int i = 0; i < c->nummol; ++i)  // load_refstructure, insertion.F90:630-646
+    if (ref_mol[i])
+      for (int a = c->mbi[i]; a < c->mbi[i + 1]; ++a) c->ref_atoms.push_back(a);
+  const size_t nh = c->ref_atoms.size();
+  c->refhost_crd.assign(refhost_crd, refhost_crd + 3 * nh);
+  c->refhost_weight.assign(refhost_weight, refhost_weight + nh);
+  c->refslt_crd.assign(refslt_crd, refslt_crd + 3 * (size_t)refslt_natom);
+  c->refslt_weight.assign(refslt_weight, refslt_weight + refslt_natom);
+  return ORC_OK;
+}
+
+int orc_set_configuration_check(orc_ctx* c, int insposition, double lwreg, double upreg, int insstructure,
+                                double lwstr, double upstr) {
+  if (!c || c->nummol <= 0) return ORC_E_PARAM;
+  c->cfg_pos = c->cfg_str = 0;
+  const int pos = (insposition >= 2 && insposition <= 5) ? insposition : 0;
+  if (c->p.boxshp == 0 && (pos == 3 || pos == 4)) return ORC_E_ENG_SLB;  // engproc.F90:1087
+  if (pos >= 2 && pos <= 4 && c->cfg_host.empty()) return ORC_E_PARAM;
+  if ((pos == 5 || insstructure == 1) && c->refslt_weight.empty()) return ORC_E_PARAM;
+  c->cfg_pos = pos;
+  c->cfg_str = insstructure == 1 ? 1 : 0;
+  c->cfg_lw = lwreg;
+  c->cfg_up = upreg;
+  c->cfg_lwstr = lwstr;
+  c->cfg_upstr = upstr;
+  return ORC_OK;
+}
+
+namespace {
+
+// --- bestfit.F90 ---------------------------------------------------------------------
+// center_of_mass (:158-172) of n points (3, n) with weights m
+int com_points(int n, const double* x, const double* m, double com[3]) {
+  double msum = 0.0;
+  for (int k = 0; k < n; ++k) msum += m[k];
+  if (msum == 0.0) return ORC_E_PARAM;  // bst_zrw
+  for (int i = 0; i < 3; ++i) {
+    double dot = 0.0;
+    for (int k = 0; k < n; ++k) dot += x[3 * k + i] * m[k];
+    com[i] = dot / msum;
+  }
+  return ORC_OK;
+}
+
+// The largest eigenpair of a symmetric 4 x 4 matrix, for find_rotation_quaternion's dsyev
+// call (:146-155).  LAPACK is not in the reference tree; its result is restated with the
+// cyclic Jacobi method (Golub & Van Loan, Matrix Computations, section 8.5) and checked
+// against numpy.linalg.eigh in the tests.
+void top_eigenvector4(double a[4][4], double vec[4]) {
+  double v[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}};
+  for (int sweep = 0; sweep < 50; ++sweep) {
+    double off = 0.0, diag = 0.0;
+    for (int i = 0; i < 4; ++i) {
+      diag += a[i][i] * a[i][i];
+      for (int j = i + 1; j < 4; ++j) off += 2.0 * a[i][j] * a[i][j];
+    }
+    if (off <= 1e-32 * (off + diag)) break;
+    for (int p = 0; p < 4; ++p)
+      for (int q = p + 1; q < 4; ++q) {
+        if (a[p][q] == 0.0) continue;
+        const double tau = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
+        const double t = std::copysign(1.0, tau) / (std::fabs(tau) + std::hypot(1.0, tau));
+        const double cs = 1.0 / std::hypot(1.0, t), sn = t * cs;
+        for (int k = 0; k < 4; ++k) {  // columns p, q
+          const double x = a[k][p], y = a[k][q];
+          a[k][p] = cs * x - sn * y;
+          a[k][q] = sn * x + cs * y;
+        }
+        for (int k = 0; k < 4; ++k) {  // rows p, q
+          const double x = a[p][k], y = a[q][k];
+          a[p][k] = cs * x - sn * y;
+          a[q][k] = sn * x + cs * y;
+        }
+        a[p][q] = a[q][p] = 0.0;
+        for (int k = 0; k < 4; ++k) {
+          const double x = v[k][p], y = v[k][q];
+          v[k][p] = cs * x - sn * y;
+          v[k][q] = sn * x + cs * y;
+        }
+      }
+  }
+  int top = 0;
+  for (int i = 1; i < 4; ++i)
+    if (a[i][i] > a[top][top]) top = i;
+  for (int i = 0; i < 4; ++i) vec[i] = v[i][top];
+}
+
+// quaternion product (:49-65) and rotate (:75-87)
+void qprod(const double a[4], const double b[4], double p[4]) {
+  p[0] = a[0] * b[0] - (a[1] * b[1] + a[2] * b[2] + a[3] * b[3]);
+  p[1] = (a[2] * b[3] - a[3] * b[2]) + a[0] * b[1] + b[0] * a[1];
+  p[2] = (a[3] * b[1] - a[1] * b[3]) + a[0] * b[2] + b[0] * a[2];
+  p[3] = (a[1] * b[2] - a[2] * b[1]) + a[0] * b[3] + b[0] * a[3];
+}
+void qrotate(const double x[3], const double r[4], double out[3]) {
+  const double q2[4] = {0.0, x[0], x[1], x[2]}, cj[4] = {r[0], -r[1], -r[2], -r[3]};
+  double t[4], res[4];
+  qprod(r, q2, t);
+  qprod(t, cj, res);
+  for (int i = 0; i < 3; ++i) out[i] = res[i + 1];
+}
+
+// fit_a_rotate_b (:215-242): fit a (3, na) onto refa with weights massa, apply to b (3, nb)
+int fit_a_rotate_b(int na, const double* refa, const double* a, const double* massa, int nb, const double* b,
+                   double* bout) {
+  double cref[3], ca[3];
+  int st = com_points(na, refa, massa, cref);
+  if (st == ORC_OK) st = com_points(na, a, massa, ca);
+  if (st != ORC_OK) return st;
+  double ip[3][3];  // inner_prod(j, i) = sum refPt(i, :) movedPt(j, :) masses(:)
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < na; ++k) s += (refa[3 * k + i] - cref[i]) * (a[3 * k + j] - ca[j]) * massa[k];
+      ip[j][i] = s;
+    }
+  double m[4][4];  // find_rotation_quaternion (:107-156), both triangles
+  m[0][0] = ip[0][0] + ip[1][1] + ip[2][2];
+  m[1][1] = ip[0][0] - ip[1][1] - ip[2][2];
+  m[2][2] = -ip[0][0] + ip[1][1] - ip[2][2];
+  m[3][3] = -ip[0][0] - ip[1][1] + ip[2][2];
+  m[0][1] = m[1][0] = ip[1][2] - ip[2][1];
+  m[0][2] = m[2][0] = ip[2][0] - ip[0][2];
+  m[0][3] = m[3][0] = ip[0][1] - ip[1][0];
+  m[1][2] = m[2][1] = ip[0][1] + ip[1][0];
+  m[2][3] = m[3][2] = ip[1][2] + ip[2][1];
+  m[1][3] = m[3][1] = ip[2][0] + ip[0][2];
+  double rot[4];
+  top_eigenvector4(m, rot);
+  for (int k = 0; k < nb; ++k) {
+    const double d[3] = {b[3 * k] - ca[0], b[3 * k + 1] - ca[1], b[3 * k + 2] - ca[2]};
+    double r[3];
+    qrotate(d, rot, r);
+    for (int i = 0; i < 3; ++i) bout[3 * k + i] = r[i] + cref[i];
+  }
+  return ORC_OK;
+}
+
+// rmsd_nofit (:256-270)
+double rmsd_nofit(int n, const double* A, const double* B, const double* m) {
+  double msum = 0.0, disp = 0.0;
+  for (int k = 0; k < n; ++k) msum += m[k];
+  for (int k = 0; k < n; ++k) {
+    double d2 = 0.0;
+    for (int i = 0; i < 3; ++i) d2 += (B[3 * k + i] - A[3 * k + i]) * (B[3 * k + i] - A[3 * k + i]);
+    disp += m[k] * d2;
+  }
+  return std::sqrt(disp / msum);
+}
+
+// center_of_mass (bestfit.F90:158-172) of the listed atoms (1-based), in their order
+int center_of_mass(const orc_ctx* c, const std::vector<int>& atoms, double com[3]) {
+  double msum = 0.0;
+  for (int a : atoms) msum += c->cfg_mass[a - 1];
+  if (msum == 0.0) return ORC_E_PARAM;  // bst_zrw
+  for (int i = 0; i < 3; ++i) {
+    double dot = 0.0;
+    for (int a : atoms) dot += c->pos(i + 1, a) * c->cfg_mass[a - 1];
+    com[i] = dot / msum;
+  }
+  return ORC_OK;
+}
+
+// check_mol_configuration for solute molecule tagslt (engproc.F90:1046-1100,
+// relative_com :1150-1172, com_aggregate insertion.F90:539-566).  refslt_bestfit is the
+// reference solute carried into the frame (insposition 5), computed once per call.
+int config_rejected(const orc_ctx* c, int tagslt, const std::vector<double>& refslt_bestfit, bool* out) {
+  *out = false;
+  const int b = c->mbi[tagslt - 1], n = c->numsite[tagslt - 1];
+  const double* sx = &c->sitepos[3 * (size_t)(b - 1)];
+  if (c->cfg_pos >= 2 && c->cfg_pos <= 4) {
+    std::vector<int> slt, agg;
+    for (int a = b; a < c->mbi[tagslt]; ++a) slt.push_back(a);
+    for (int i = 0; i < c->nummol; ++i)
+      if (c->cfg_host[i])
+        for (int a = c->mbi[i]; a < c->mbi[i + 1]; ++a) agg.push_back(a);
+    double scom[3], acom[3];
+    int st = center_of_mass(c, slt, scom);
+    if (st == ORC_OK) st = center_of_mass(c, agg, acom);
+    if (st != ORC_OK) return st;
+    const double dx[3] = {scom[0] - acom[0], scom[1] - acom[1], scom[2] - acom[2]};
+    double distance;
+    if (c->cfg_pos == 2) {
+      distance = std::sqrt(dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2]);
+    } else {
+      const double len3 = std::sqrt(c->cell[6] * c->cell[6] + c->cell[7] * c->cell[7] + c->cell[8] * c->cell[8]);
+      distance = (c->invcl[2] * dx[0] + c->invcl[5] * dx[1] + c->invcl[8] * dx[2]) * len3;
+      if (c->cfg_pos == 4) distance = std::fabs(distance);
+    }
+    if ((c->cfg_lw > distance) || (distance > c->cfg_up)) {
+      *out = true;
+      return ORC_OK;
+    }
+  } else if (c->cfg_pos == 5) {
+    if (n != (int)c->refslt_weight.size()) return ORC_E_ENG_BUG;
+    const double distance = rmsd_nofit(n, refslt_bestfit.data(), sx, c->refslt_weight.data());
+    if ((c->cfg_lw > distance) || (distance > c->cfg_up)) {
+      *out = true;
+      return ORC_OK;
+    }
+  }
+  if (c->cfg_str == 1) {  // INSSTR_RMSD: rmsd_bestfit(refslt_crd, the solute)
+    if (n != (int)c->refslt_weight.size()) return ORC_E_ENG_BUG;
+    std::vector<double> fitted(3 * (size_t)n);
+    const int st = fit_a_rotate_b(n, c->refslt_crd.data(), sx, c->refslt_weight.data(), n, sx, fitted.data());
+    if (st != ORC_OK) return st;
+    const double distance = rmsd_nofit(n, c->refslt_crd.data(), fitted.data(), c->refslt_weight.data());
+    if ((c->cfg_lwstr > distance) || (distance > c->cfg_upstr)) *out = true;
+  }
+  return ORC_OK;
+}
+
+}  // namespace
+
+int orc_fit_a_rotate_b(int na, const double* refa, const double* a, const double* massa, int nb, const double* b,
+                       double* bout) {
+  if (na <= 0 || nb < 0 || !refa || !a || !massa || (nb > 0 && (!b || !bout))) return ORC_E_PARAM;
+  return fit_a_rotate_b(na, refa, a, massa, nb, b, bout);
+}
+
 int orc_placements(orc_ctx* c, int nplace, const int* tagslt, const double* solute_sitepos,
                    const double* stat_weight_solute, double* uvengy_out, double* flceng_out, int nthreads) {
   if (!c || !c->frame_ready || nplace < 0 || !tagslt) return ORC_E_PARAM;
@@ -1400,6 +1640,28 @@ int orc_placements(orc_ctx* c, int nplace, const int* tagslt, const double* solu
   }
   const int ns0 = c->numsite[tagslt[0] - 1];
   std::vector<double> uv((size_t)nplace * S);
+  // the loop's skipcond (engproc.F90:389-390): rejected solution-mode placements compute
+  // and accumulate nothing
+  std::vector<char> rejected(nplace, 0);
+  if (c->p.slttype == 1 && (c->cfg_pos != 0 || c->cfg_str != 0)) {
+    std::vector<double> bestfit;  // refslt_bestfit: the reference host fitted onto the frame's
+    if (c->cfg_pos == 5) {
+      const int nh = (int)c->ref_atoms.size(), nsr = (int)c->refslt_weight.size();
+      std::vector<double> hostcrd(3 * (size_t)nh);
+      for (int k = 0; k < nh; ++k)
+        for (int i = 0; i < 3; ++i) hostcrd[3 * k + i] = c->pos(i + 1, c->ref_atoms[k]);
+      bestfit.resize(3 * (size_t)nsr);
+      const int st = fit_a_rotate_b(nh, hostcrd.data(), c->refhost_crd.data(), c->refhost_weight.data(), nsr,
+                                    c->refslt_crd.data(), bestfit.data());
+      if (st != ORC_OK) return st;
+    }
+    for (int q = 0; q < nplace; ++q) {
+      bool r = false;
+      const int st = config_rejected(c, tagslt[q], bestfit, &r);
+      if (st != ORC_OK) return st;
+      rejected[q] = r;
+    }
+  }
 #ifdef _OPENMP
   const int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
 #else
@@ -1430,6 +1692,7 @@ int orc_placements(orc_ctx* c, int nplace, const int* tagslt, const double* solu
         const int ns = c->numsite[tagslt[q] - 1];
         const double* sx = solute_sitepos ? solute_sitepos + (size_t)3 * ns0 * q : nullptr;
         (void)ns;
+        if (rejected[q]) continue;
         int st = get_uv_energy(c, tagslt[q], sx, &uv[(size_t)q * S], w, false, usreal, nullptr);
         if (st != ORC_OK) {
 #pragma omp critical
@@ -1451,6 +1714,7 @@ int orc_placements(orc_ctx* c, int nplace, const int* tagslt, const double* solu
 #endif
     for (int q = 0; q < nplace; ++q) {
       const double* sx = solute_sitepos ? solute_sitepos + (size_t)3 * ns0 * q : nullptr;
+      if (rejected[q]) continue;
       int st = get_uv_energy(c, tagslt[q], sx, &uv[(size_t)q * S], w, true, usreal, nullptr);
       if (st != ORC_OK) status = status ? status : st;
       c->last_cnv = w.cnv;
@@ -1459,6 +1723,11 @@ int orc_placements(orc_ctx* c, int nplace, const int* tagslt, const double* solu
   if (status != ORC_OK) return status;
   std::vector<double> fl(c->numslv);
   for (int q = 0; q < nplace; ++q) {
+    if (rejected[q]) {
+      if (uvengy_out) std::fill(uvengy_out + (size_t)q * S, uvengy_out + (size_t)(q + 1) * S, 0.0);
+      if (flceng_out) std::fill(flceng_out + (size_t)q * c->numslv, flceng_out + (size_t)(q + 1) * c->numslv, 0.0);
+      continue;
+    }
     const double sw = stat_weight_solute ? stat_weight_solute[q] : 1.0;
     const int st = update_histogram(c, tagslt[q], sw, &uv[(size_t)q * S], fl.data());
     if (uvengy_out) std::memcpy(uvengy_out + (size_t)q * S, &uv[(size_t)q * S], sizeof(double) * S);

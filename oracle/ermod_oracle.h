@@ -34,6 +34,7 @@ enum {
   ORC_E_RCP_CNS = 105, /* recpcal.F90:335,474 */
   ORC_E_RCP_FST = 106, /* solute listed as solvent (recpcal.F90:469) */
   ORC_E_SET_PRS = 108, /* non-periodic with NPT or a non-bare Coulomb (setconf.F90:368-372) */
+  ORC_E_ENG_SLB = 109, /* slab configuration check of a non-periodic system (engproc.F90:1087) */
   ORC_W_MBIN = 110,    /* last-bin warning without force_calculation (engproc.F90:1010-1015) */
   ORC_E_PARAM = 120,   /* invalid argument */
   ORC_E_NONCUBOID = 121 /* realcal.F90:859-866 */
@@ -96,6 +97,24 @@ int orc_placements(orc_ctx* c, int nplace, const int* tagslt, const double* solu
                    const double* stat_weight_solute, double* uvengy_out, double* flceng_out,
                    int nthreads);
 int orc_slvmax(const orc_ctx* c);
+/* The host aggregate (hostspec; host_mol[i] != 0 for 0-based molecules) and sitemass. */
+int orc_set_aggregate(orc_ctx* c, const int* host_mol, const double* sitemass);
+/* The reference structure (load_refstructure, insertion.F90:619-700): refspec molecules
+ * (ref_mol[i] != 0) with refhost_crd (3, n) and refhost_weight (n); the solute's
+ * refslt_crd (3, refslt_natom) and refslt_weight. */
+int orc_set_reference_structure(orc_ctx* c, const int* ref_mol, const double* refhost_crd,
+                                const double* refhost_weight, int refslt_natom, const double* refslt_crd,
+                                const double* refslt_weight);
+/* check_mol_configuration (engproc.F90:1046-1100), solution mode: insposition 2 (sphere),
+ * 3 (slab), 4 (symmetric slab) about the host aggregate, 5 (RMSD from the reference solute
+ * carried into the frame by the host fit); insstructure 1 (best-fit RMSD in [lwstr, upstr]).
+ * Rejected placements are skipped (engproc.F90:389-390), their uvengy/flceng rows zero. */
+int orc_set_configuration_check(orc_ctx* c, int insposition, double lwreg, double upreg, int insstructure,
+                                double lwstr, double upstr);
+/* bestfit.F90 fit_a_rotate_b (:215-242): a (3, na) fitted onto refa (weights massa), the same
+ * transform applied to b (3, nb) -> bout. */
+int orc_fit_a_rotate_b(int na, const double* refa, const double* a, const double* massa, int nb,
+                       const double* b, double* bout);
 /* raw accumulators, engclear (engproc.F90:276-288) */
 int orc_clear(orc_ctx* c);
 /* scalars = {engnorm, engsmpl, avslf, voffset, voffset_initialized}; any pointer may be NULL */

@@ -34,6 +34,7 @@ ENGCNV = 1.0 / 4.184                # kJ/mol -> kcal/mol
 OK = 0
 E_ENG_MIN, E_ENG_SFT, E_ENG_BUG, E_ENG_CNS, E_RCP_CNS, E_RCP_FST = 101, 102, 103, 104, 105, 106
 W_MBIN, E_PARAM, E_NONCUBOID = 110, 120, 121
+E_ENG_SLB = 109
 
 
 class OrcParams(C.Structure):
@@ -91,6 +92,11 @@ def lib():
         L.orc_adjoint.argtypes = [C.c_void_p, C.c_int, dp, C.c_int, dp]
         L.orc_intermediate_enable.argtypes = [C.c_void_p, dp]
         L.orc_intermediate_get.argtypes = [C.c_void_p, dp, dp, dp]
+        L.orc_set_configuration_check.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int,
+                                                  C.c_double, C.c_double]
+        L.orc_set_aggregate.argtypes = [C.c_void_p, ip, dp]
+        L.orc_set_reference_structure.argtypes = [C.c_void_p, ip, dp, dp, C.c_int, dp, dp]
+        L.orc_fit_a_rotate_b.argtypes = [C.c_int, dp, dp, dp, C.c_int, dp, dp]
         _lib = L
     return _lib
 
@@ -117,6 +123,18 @@ def _check(code, where):
 # ----------------------------------------------------------------------------------
 # routines with golden vectors / analytic checks
 # ----------------------------------------------------------------------------------
+def fit_a_rotate_b(refa, a, massa, b):
+    """bestfit.F90 fit_a_rotate_b: a (na, 3) fitted onto refa with weights massa; returns b
+    (nb, 3) under the same transform."""
+    refa = np.ascontiguousarray(refa, np.float64)
+    a = np.ascontiguousarray(a, np.float64)
+    m = np.ascontiguousarray(massa, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    out = np.zeros_like(b)
+    _check(lib().orc_fit_a_rotate_b(len(a), _dp(refa), _dp(a), _dp(m), len(b), _dp(b), _dp(out)), "fit_a_rotate_b")
+    return out
+
+
 def spline_value(order: int, x: float) -> float:
     """spline.F90:47-59 (M_order(x))."""
     return lib().orc_spline_value(order, x)
@@ -323,6 +341,29 @@ class Oracle:
         if raise_on_error:
             _check(st, "placements")
         return dict(status=st, uvengy=uv, flceng=fl)
+
+    def set_aggregate(self, host_mol, sitemass):
+        hm = np.ascontiguousarray(host_mol, np.int32)
+        sm = np.ascontiguousarray(sitemass, np.float64)
+        self._agg_keep = (hm, sm)
+        _check(lib().orc_set_aggregate(self.ctx, _ip(hm), _dp(sm)), "set_aggregate")
+
+    def set_reference_structure(self, ref_mol, refhost_crd, refhost_weight, refslt_crd, refslt_weight):
+        rm = np.ascontiguousarray(ref_mol, np.int32)
+        hc = np.ascontiguousarray(refhost_crd, np.float64).reshape(-1, 3)
+        hw = np.ascontiguousarray(refhost_weight, np.float64)
+        sc = np.ascontiguousarray(refslt_crd, np.float64).reshape(-1, 3)
+        sw = np.ascontiguousarray(refslt_weight, np.float64)
+        self._ref_keep = (rm, hc, hw, sc, sw)
+        _check(lib().orc_set_reference_structure(self.ctx, _ip(rm), _dp(hc), _dp(hw), len(sc), _dp(sc), _dp(sw)),
+               "set_reference_structure")
+
+    def set_configuration_check(self, insposition, lwreg=0.0, upreg=0.0, insstructure=0, lwstr=0.0, upstr=0.0):
+        """check_mol_configuration (engproc.F90:1046-1100), solution mode; see
+        orc_set_configuration_check."""
+        _check(lib().orc_set_configuration_check(self.ctx, int(insposition), float(lwreg), float(upreg),
+                                                 int(insstructure), float(lwstr), float(upstr)),
+               "set_configuration_check")
 
     def clear(self):
         _check(lib().orc_clear(self.ctx), "clear")

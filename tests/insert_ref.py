@@ -36,14 +36,51 @@ class Stream:
         return (a * 67108864.0 + b) * (1.0 / 9007199254740992.0)
 
 
-def place(bf, mass, cell, p, insposition=0, insorient=0, insorigin=0, lwreg=0.0, upreg=0.0, seed=1, offset=0):
+def horn_fit(refa, a, w, b):
+    """bestfit.F90 fit_a_rotate_b with numpy's LAPACK eigensolver: a (n, 3) fitted onto refa
+    (weights w), the transform applied to b (m, 3)."""
+    refa, a, b, w = (np.asarray(v, float) for v in (refa, a, b, w))
+    cr = (w[:, None] * refa).sum(0) / w.sum()
+    ca = (w[:, None] * a).sum(0) / w.sum()
+    S = np.einsum("k,ki,kj->ji", w, refa - cr, a - ca)  # S[j, i] = sum w ref_i a_j
+    M = np.array([
+        [S[0, 0] + S[1, 1] + S[2, 2], S[1, 2] - S[2, 1], S[2, 0] - S[0, 2], S[0, 1] - S[1, 0]],
+        [S[1, 2] - S[2, 1], S[0, 0] - S[1, 1] - S[2, 2], S[0, 1] + S[1, 0], S[2, 0] + S[0, 2]],
+        [S[2, 0] - S[0, 2], S[0, 1] + S[1, 0], -S[0, 0] + S[1, 1] - S[2, 2], S[1, 2] + S[2, 1]],
+        [S[0, 1] - S[1, 0], S[2, 0] + S[0, 2], S[1, 2] + S[2, 1], -S[0, 0] - S[1, 1] + S[2, 2]]])
+    q = np.linalg.eigh(M)[1][:, -1]
+    v = b - ca
+    u = q[1:]
+    t = 2.0 * np.cross(u, v)
+    return v + q[0] * t + np.cross(u, t) + cr
+
+
+def place(bf, mass, cell, p, insposition=0, insorient=0, insorigin=0, lwreg=0.0, upreg=0.0, seed=1, offset=0,
+          agg=None, start=None, refbest=None, refw=None):
+    """Placement p.  insorigin 2: agg is the aggregate centre; insorigin 3: start is bfcoord
+    fitted onto refbest, the reference solute in the frame, and a draw whose RMSD from it
+    (weights refw) lies outside [lwreg, upreg] is drawn again."""
     g = offset + p
     rng = Stream(seed, g)
-    x = np.array(bf, dtype=float)
+    w = 1.0
+    for draw in range(1 << 16):
+        x, w = _draw(rng, g + draw, bf if insorigin != 3 else start, mass, cell, insposition, insorient, insorigin,
+                     lwreg, upreg, agg, w)
+        if insorigin != 3:
+            break
+        rmsd = math.sqrt(float((refw * ((x - refbest) ** 2).sum(1)).sum() / refw.sum()))
+        if not (lwreg > rmsd or rmsd > upreg):
+            break
+    return x, w
+
+
+def _draw(rng, parity, x0, mass, cell, insposition, insorient, insorigin, lwreg, upreg, agg, w):
+    x = np.array(x0, dtype=float)
     com = lambda y: (mass[:, None] * y).sum(0) / mass.sum()
     if insorigin == 0:
         x = x - com(x)
-    w = 1.0
+    elif insorigin == 2:
+        x = x - com(x) + agg
     shift = np.zeros(3)
     if insposition == 0:
         r = np.array([rng.uniform() for _ in range(3)])
@@ -72,7 +109,7 @@ def place(bf, mass, cell, p, insposition=0, insorient=0, insorigin=0, lwreg=0.0,
         ls = np.linalg.norm(cell, axis=0) / 2.0 / upreg
         z0 = 8 * ls.prod()
         z1 = math.sqrt(math.pi) ** 3 * math.erf(ls[0]) * math.erf(ls[1]) * math.erf(ls[2])
-        if g % 2 == 0:
+        if parity % 2 == 0:
             sc = np.array([(2 * rng.uniform() - 1) * ls[i] for i in range(3)])
         else:
             sc = np.zeros(3)

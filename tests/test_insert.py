@@ -57,3 +57,60 @@ def test_device_placements_match_restatement(gpu_lib, mode):
     if mode["insposition"] in (0, 6):
         eng.placements(tag, sol)
     eng.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", [dict(insposition=2, lwreg=2.0, upreg=6.0, insorigin=2),
+                                  dict(insposition=4, lwreg=1.0, upreg=5.0, insorigin=2),
+                                  dict(insposition=5, lwreg=0.0, upreg=2.5, insorigin=3),
+                                  dict(insposition=6, lwreg=0.0, upreg=3.0, insorigin=3)])
+def test_device_placements_aggregate_and_reference(gpu_lib, mode):
+    """insorigin 2 (the solute's COM moved to the host aggregate's) and 3 (reffit: the solute
+    fitted onto the reference solute carried into the frame, and the RMSD acceptance of
+    check_solute_configuration, redrawing until it passes) against the restatement, whose
+    fits use numpy's LAPACK eigensolver."""
+    from ermod_gb300 import setconf, synth
+    from ermod_gb300.engproc import EnergyRepresentation
+    w = synth.refs_small()
+    w.nwater, w.lattice_n, w.box = 300, 7, 22.0
+    topo = setconf.setparam_topology(w.species(), slttype=2)
+    bins = setconf.enginit_bins(topo["numslv"])
+    eng = EnergyRepresentation(w.params, topo, bins, precision="mixed", batch=8)
+    pos, cell = w.frame(0)
+    eng.frame(pos, cell)
+    mbi = np.asarray(topo["mol_begin_index"])
+    mass_all = np.concatenate([np.tile(synth.WATER_MASS, w.nwater), w.solute["mass"]])
+    host = np.zeros(topo["nummol"], np.int32)
+    host[np.argsort(np.linalg.norm(pos[mbi[:-2] - 1] - w.box / 2, axis=1))[:12]] = 1
+    hidx = np.concatenate([np.arange(mbi[i] - 1, mbi[i + 1] - 1) for i in np.nonzero(host)[0]])
+    bf = w.solute["xyz"] + np.array([1.0, -2.0, 0.5])
+    mass = np.asarray(w.solute["mass"], float)
+    kw = {}
+    if mode["insorigin"] == 2:
+        eng.set_aggregate(host, mass_all)
+        kw["agg"] = (mass_all[hidx, None] * pos[hidx]).sum(0) / mass_all[hidx].sum()
+    else:
+        th = 0.4
+        R = np.array([[np.cos(th), 0.0, np.sin(th)], [0.0, 1.0, 0.0], [-np.sin(th), 0.0, np.cos(th)]])
+        hc = pos[hidx] @ R.T + np.array([-2.0, 1.0, 4.0])
+        hw = np.where(mass_all[hidx] > 0.95 * 4.0026, 1.0, 0.0)
+        sc = w.solute["xyz"] - w.solute["xyz"].mean(0) + np.array([0.5, 0.0, -0.5])
+        sw = np.where(mass > 0.95 * 4.0026, 1.0, 0.0)
+        eng.set_reference_structure(host, hc, hw, sc, sw)
+        best = insert_ref.horn_fit(pos[hidx], hc, hw, sc)
+        kw.update(start=insert_ref.horn_fit(best, bf, sw, bf), refbest=best, refw=sw)
+    n = 120
+    sol, sws = eng.generate_placements(n, bf, mass, seed=777, offset=5, weights=True, **mode)
+    sol, sws = sol.cpu().numpy(), sws.cpu().numpy()
+    for p in range(0, n, 5):
+        x, wt = insert_ref.place(bf, mass, cell, p, seed=777, offset=5, **mode, **kw)
+        np.testing.assert_allclose(sol[p], x, atol=1e-9, rtol=0)
+        np.testing.assert_allclose(sws[p], wt, rtol=1e-10)
+    com = (mass[None, :, None] * sol).sum(1) / mass.sum()
+    if mode["insorigin"] == 2 and mode["insposition"] == 2:
+        r = np.linalg.norm(com - kw["agg"], axis=1)
+        assert np.all((r >= 2.0 - 1e-9) & (r <= 6.0 + 1e-9))
+    if mode["insorigin"] == 3:  # every placement passed the acceptance
+        rmsd = np.sqrt((sw * ((sol - kw["refbest"]) ** 2).sum(2)).sum(1) / sw.sum())
+        assert np.all(rmsd <= mode["upreg"] + 1e-12)
+    eng.close()
