@@ -47,6 +47,8 @@ def parse_args():
     ap.add_argument("--workload", default="refs_large")
     ap.add_argument("--insertions", type=int, default=None, help="insertions per frame (default: workload's)")
     ap.add_argument("--batch", type=int, default=256, help="placements per PME launch")
+    ap.add_argument("--finish-group", type=int, default=0,
+                    help="placements per molecule-energy block, 4 or 8 (0: automatic)")
     ap.add_argument("--grid", type=int, default=None, help="PME grid points per axis (default: workload's)")
     ap.add_argument("--cpu-sample", type=int, default=96, help="placements timed on the CPU oracle")
     ap.add_argument("--plain-sample", type=int, default=48, help="placements timed on the plain FP64 GPU path")
@@ -288,7 +290,8 @@ def run_ours(args):
     tag_h = np.full(nplace, topo["nummol"], np.int32)
     cell = frames[0][1]
 
-    eng = EnergyRepresentation(w.params, topo, bins, precision="mixed", device=local, batch=args.batch)
+    eng = EnergyRepresentation(w.params, topo, bins, precision="mixed", device=local, batch=args.batch,
+                               finish_group=args.finish_group)
     stream = torch.cuda.Stream(device=dev)
     eng.set_stream(stream.cuda_stream)
     pos_d = [torch.from_numpy(f[0]).to(dev) for f in frames]
@@ -361,7 +364,8 @@ def run_ours(args):
     # ---- end to end through the host C ABI ----
     e2e = None
     if not args.no_e2e:
-        eng2 = EnergyRepresentation(w.params, topo, bins, precision="mixed", device=local, batch=args.batch)
+        eng2 = EnergyRepresentation(w.params, topo, bins, precision="mixed", device=local, batch=args.batch,
+                                   finish_group=args.finish_group)
         pinned_pl = [None] * nsteps if soln else [torch.from_numpy(np.ascontiguousarray(p)).pin_memory().numpy()
                                                   for p in places]
         pinned_pos = [torch.from_numpy(f[0]).pin_memory().numpy() for f in frames]
@@ -407,7 +411,8 @@ def run_ours(args):
         cpu = {"value": rate, "unit": "molecule-energies/s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"{ncpu} placements of frame 0 ({dt:.2f} s), FP64 oracle, OpenMP"}
         # the same placements on the mixed path, checked against the oracle's energies
-        eng3 = EnergyRepresentation(w.params, topo, bins, precision="mixed", device=local, batch=args.batch)
+        eng3 = EnergyRepresentation(w.params, topo, bins, precision="mixed", device=local, batch=args.batch,
+                                   finish_group=args.finish_group)
         eng3.frame(frames[0][0], cell)
         u_gpu = eng3.placements(tag_h[:ncpu], None if soln else places[0][:ncpu], want_uvengy=True)["uvengy"]
         eng3.close()
@@ -448,11 +453,12 @@ def _timed(fn, steps, warmup, stream):
 def run_uneven(args):
     """16 water systems of uneven size (2k-60k waters), each with its own solute, grid and
     insertion count, one step of all of them replayed as one CUDA graph launch; the batch
-    (placements per PME launch) of every system picked by the autotuner."""
+    (placements per PME launch) and the finish group (placements per molecule-energy block)
+    of every system picked by the autotuner."""
     import torch
     from ermod_gb300 import build, setconf, synth
     from ermod_gb300.engproc import EnergyRepresentation
-    from ermod_gb300.multisystem import SystemGraph, autotune_batch
+    from ermod_gb300.multisystem import SystemGraph, autotune_tiles
     build.build()
     torch.cuda.set_device(0)
     systems = synth.uneven()
@@ -462,15 +468,15 @@ def run_uneven(args):
         bins = setconf.enginit_bins(topo["numslv"], w.hist)
         f0, f1 = w.frame(0), w.frame(1)
         p0, p1 = w.placements(0), w.placements(1)
-        B = autotune_batch(w.params, topo, bins, f0, p0[:1024], topo["nummol"], candidates=(32, 64, 128, 256))
-        eng = EnergyRepresentation(w.params, topo, bins, precision="mixed", batch=B)
+        B, G, _ = autotune_tiles(w.params, topo, bins, f0, p0[:1024], topo["nummol"])
+        eng = EnergyRepresentation(w.params, topo, bins, precision="mixed", batch=B, finish_group=G)
         eng.frame(*f0)
         eng.placements(np.full(len(p0), topo["nummol"], np.int32), p0)
         engines.append(eng)
         tops.append(topo)
         frames.append(f1)
         places.append(p1)
-        batches.append(B)
+        batches.append((B, G))
     g = SystemGraph(engines, frames, places, [t["nummol"] for t in tops])
     stream = torch.cuda.Stream()
 
@@ -491,7 +497,8 @@ def run_uneven(args):
         cpu = {"value": rate, "unit": "molecule-energies/s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"system {k} ({w.nwater} waters, PME {w.params['ms1max']}^3): {n} placements ({dt:.2f} s), "
                          f"FP64 oracle, OpenMP"}
-        eng = EnergyRepresentation(w.params, topo, bins, precision="mixed", batch=batches[k])
+        eng = EnergyRepresentation(w.params, topo, bins, precision="mixed", batch=batches[k][0],
+                                   finish_group=batches[k][1])
         eng.frame(*frames[k])
         u_gpu = eng.placements(np.full(n, topo["nummol"], np.int32), places[k][:n], want_uvengy=True)["uvengy"]
         eng.close()
@@ -504,7 +511,7 @@ def run_uneven(args):
             "config": {"workload": "uneven: 16 systems, 2k-60k waters, own solutes (6-40 sites), grids and "
                                    "1k-20k insertions, one CUDA graph launch per step",
                        "systems": [{"waters": w.nwater, "K": w.params["ms1max"], "insertions": w.ins_per_frame,
-                                    "solute_sites": len(w.solute["charge"]), "batch": b}
+                                    "solute_sites": len(w.solute["charge"]), "batch": b[0], "finish_group": b[1]}
                                    for w, b in zip(systems, batches)]},
             "clocks": clk.summary(), "cpu_baseline": cpu, "accuracy": accuracy}
     print(json.dumps(line))

@@ -34,7 +34,7 @@ class Params(C.Structure):
         ("force_calculation", C.c_int32), ("precision", C.c_int32), ("batch", C.c_int32),
         ("count_mirror", C.c_int32),
         ("elecut", C.c_double), ("lwljcut", C.c_double), ("upljcut", C.c_double), ("screen", C.c_double),
-        ("temp", C.c_double), ("block_threshold", C.c_double), ("boxshp", C.c_int32), ("reserved_", C.c_int32),
+        ("temp", C.c_double), ("block_threshold", C.c_double), ("boxshp", C.c_int32), ("finish_group", C.c_int32),
     ]
 
 

@@ -408,7 +408,7 @@ __device__ __forceinline__ void fft3_t(const float2* in, float2* mid, float2* mi
 
 constexpr int kSites = 32;  // solute sites staged per chunk
 constexpr int kR1 = 4, kR3 = 3;  // generation tile: kR3 k3 values x kR1 k1 values per thread
-// Hp = H rounded up to a multiple of kR1, so that the TX = Hp / kR1 tile columns cover k1 < Hp
+static_assert(kR1 == 4, "pme_a reads a tile row's engfac values as one float4");
 
 struct PmeArgs {
   const float2* bvec;   // [nb][S][3][Kmax]
@@ -449,8 +449,8 @@ __global__ void __launch_bounds__(kPmeAThreads, kPmeAMinBlocks) pme_a_kernel(Pme
   // ---- generation: slab(k3, k1) = sum_s [q_s b2_s(k2) b3_s(k3)] b1_s(k1), then (last
   // chunk) the engfac multiply and the self energy sum 0.5 sum_k engfac |S|^2 ----
   float2* sd = work;                         // [chunk][K3]
-  // [chunk][Hp]: b1(k1); a tile thread tx takes k1 = tx + i TX (i < kR1), so that the lanes
-  // of a warp (consecutive tx) read and write consecutive words of every row
+  // [chunk][kR1][TX]: b1(k1 = kR1 tx + i) at [i][tx], so that the lanes of a warp (consecutive
+  // tx) read consecutive words
   float2* sb = work + (size_t)A.chunk * K3;
   for (int s0 = 0; s0 < ns; s0 += A.chunk) {
     const int nsc = min(A.chunk, ns - s0);
@@ -463,8 +463,6 @@ __global__ void __launch_bounds__(kPmeAThreads, kPmeAMinBlocks) pme_a_kernel(Pme
     constexpr int kStage = 2;
     const int nd = nsc * K3, n1 = nsc * Hp;
     __shared__ float2 sqb2[kSites];  // q_s b2_s(k2)
-    // rounds counted from 0 in every thread, so that all of them meet the barrier below
-    // equally often
     for (int r0 = 0; r0 < max(nd, n1); r0 += kStage * blockDim.x) {
       const int base = r0 + (int)threadIdx.x;
       float2 b3[kStage], b1[kStage];
@@ -486,7 +484,7 @@ __global__ void __launch_bounds__(kPmeAThreads, kPmeAMinBlocks) pme_a_kernel(Pme
         const float2 b2 = bv[(us * 3 + 1) * A.Kmax + k2];
         sqb2[threadIdx.x] = make_float2(q * b2.x, q * b2.y);
       }
-      __syncthreads();  // sqb2 staged
+      __syncthreads();  // sqb2 staged (the loop runs the same number of rounds in every thread)
 #pragma unroll
       for (int i = 0; i < kStage; ++i) {
         const int t = base + i * blockDim.x;
@@ -496,14 +494,14 @@ __global__ void __launch_bounds__(kPmeAThreads, kPmeAMinBlocks) pme_a_kernel(Pme
         }
         if (t < n1) {
           const int sl = t / Hp, k1 = t - sl * Hp;
-          sb[sl * Hp + k1] = b1[i];
+          sb[sl * Hp + (k1 % kR1) * TX + k1 / kR1] = b1[i];
         }
       }
     }
     __syncthreads();
     for (int mt = threadIdx.x; mt < TX * TY; mt += blockDim.x) {
       const int ty = KC ? mt / TX : fdiv(mt, A.fHp4), tx = mt - ty * TX;
-      const int k3a = ty * kR3;
+      const int k1a = tx * kR1, k3a = ty * kR3;
       float2 acc[kR3][kR1];
 #pragma unroll
       for (int j = 0; j < kR3; ++j)
@@ -528,25 +526,29 @@ __global__ void __launch_bounds__(kPmeAThreads, kPmeAMinBlocks) pme_a_kernel(Pme
       for (int j = 0; j < kR3; ++j) {
         const int k3 = k3a + j;
         if (k3 >= K3) continue;
-        float2* dst = slab + (size_t)k3 * Hp + tx;  // element i at dst[i TX]
+        float4* dst = reinterpret_cast<float4*>(slab + (size_t)k3 * Hp + k1a);
         if (s0 != 0) {
-#pragma unroll
-          for (int i = 0; i < kR1; ++i) acc[j][i] = cadd(acc[j][i], dst[i * TX]);
+          const float4 o0 = dst[0], o1 = dst[1];
+          acc[j][0] = cadd(acc[j][0], make_float2(o0.x, o0.y));
+          acc[j][1] = cadd(acc[j][1], make_float2(o0.z, o0.w));
+          acc[j][2] = cadd(acc[j][2], make_float2(o1.x, o1.y));
+          acc[j][3] = cadd(acc[j][3], make_float2(o1.z, o1.w));
         }
         if (last) {  // FP32 engfac rows are Hp points long, zeros beyond H
-          const float* frow = A.engfac + ((size_t)k3 * A.K2 + k2) * Hp + tx;
+          const float4 f4 = __ldg(reinterpret_cast<const float4*>(A.engfac + ((size_t)k3 * A.K2 + k2) * Hp + k1a));
+          const float fv[kR1] = {f4.x, f4.y, f4.z, f4.w};
 #pragma unroll
           for (int i = 0; i < kR1; ++i) {
-            const int k1 = tx + i * TX;
-            const float f = __ldg(frow + i * TX);
+            const int k1 = k1a + i;
+            const float f = fv[i];
             const float2 q = acc[j][i];
             const float wgt = (k1 == 0 || (even && k1 == H - 1)) ? 0.5f : 1.f;
             tile_self += wgt * f * (q.x * q.x + q.y * q.y);
             acc[j][i] = make_float2(f * q.x, f * q.y);
           }
         }
-#pragma unroll
-        for (int i = 0; i < kR1; ++i) dst[i * TX] = acc[j][i];
+        dst[0] = make_float4(acc[j][0].x, acc[j][0].y, acc[j][1].x, acc[j][1].y);
+        dst[1] = make_float4(acc[j][2].x, acc[j][2].y, acc[j][3].x, acc[j][3].y);
       }
       if (last) self = ff_add(self, tile_self);
     }

@@ -23,7 +23,7 @@ PARAM_KEYS = ("slttype", "estype", "ljswitch", "splodr", "ms1max", "ms2max", "ms
 
 class EnergyRepresentation:
     def __init__(self, params: dict, topo: dict, bins: dict, precision: str = "mixed", device: int = 0,
-                 batch: int = 0, count_mirror: bool = False):
+                 batch: int = 0, count_mirror: bool = False, finish_group: int = 0):
         L = _lib.load()
         p = _lib.Params()
         L.ermod_default_params(C.byref(p))
@@ -34,6 +34,7 @@ class EnergyRepresentation:
         p.precision = _lib.PRECISION_MIXED if precision == "mixed" else _lib.PRECISION_FP64
         p.batch = int(batch)
         p.count_mirror = 1 if count_mirror else 0
+        p.finish_group = int(finish_group)
         self.params = dict(params)
         self.precision = precision
         self.device = int(device)

@@ -5,9 +5,10 @@ CUDA graph (ermod_graph_create) and replays it with one launch per step; the sys
 run concurrently.  Inputs live in device buffers that the caller overwrites in place
 between launches (`set_frame`, `set_placements`).
 
-`autotune_batch` picks, per system, the number of placements per PME launch (the
-batch B: the tile of placements that the spectrum, transform and gather kernels work
-on together) by timing one step at each candidate with CUDA events.
+`autotune_tiles` picks, per system, the tile shape -- the number of placements per PME
+launch (the batch B: the tile of placements that the spectrum, transform and gather
+kernels work on together) and per molecule-energy block (the finish group G) -- by timing
+one step at each candidate with CUDA events.
 """
 from __future__ import annotations
 
@@ -81,29 +82,42 @@ class SystemGraph:
             pass
 
 
-def autotune_batch(params, topo, bins, frame, placements, tag, candidates=(32, 64, 128, 256), device=0):
-    """The batch size (placements per PME launch) with the highest placements/s on one
-    step of this system, timed with CUDA events after a warm-up step."""
+def autotune_tiles(params, topo, bins, frame, placements, tag, batches=(32, 64, 128, 256), groups=(4, 8),
+                   device=0):
+    """The tile shape of one system with the highest placements/s on one step, timed with
+    CUDA events after a warm-up step: the batch B (placements per PME launch: the tile of
+    placements the spectrum, transform and gather kernels work on together) and the finish
+    group G (placements per molecule-energy block: the real-space and binning tile).
+    Returns (B, G, {(B, G): placements/s})."""
     import torch
     from .engproc import EnergyRepresentation
-    best, best_rate = None, -1.0
     n = len(placements)
     tags = np.full(n, tag, np.int32)
-    for B in candidates:
+    rates = {}
+    for B in batches:
         if B > max(4, n):
             continue
-        eng = EnergyRepresentation(params, topo, bins, precision="mixed", device=device, batch=B)
-        eng.frame(frame[0], frame[1])
-        eng.placements(tags, placements)
-        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        t0.record()
-        eng.frame(frame[0], frame[1])
-        eng.placements(tags, placements)
-        t1.record()
-        torch.cuda.synchronize()
-        rate = n / (t0.elapsed_time(t1) / 1e3)
-        eng.close()
-        if rate > best_rate:
-            best, best_rate = B, rate
-    return best
+        for G in groups:
+            if B % G:
+                continue
+            eng = EnergyRepresentation(params, topo, bins, precision="mixed", device=device, batch=B,
+                                       finish_group=G)
+            eng.frame(frame[0], frame[1])
+            eng.placements(tags, placements)
+            t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            t0.record()
+            eng.frame(frame[0], frame[1])
+            eng.placements(tags, placements)
+            t1.record()
+            torch.cuda.synchronize()
+            rates[(B, G)] = n / (t0.elapsed_time(t1) / 1e3)
+            eng.close()
+    (B, G) = max(rates, key=rates.get)
+    return B, G, rates
+
+
+def autotune_batch(params, topo, bins, frame, placements, tag, candidates=(32, 64, 128, 256), device=0):
+    """The batch size alone (finish group automatic): autotune_tiles over batches."""
+    return autotune_tiles(params, topo, bins, frame, placements, tag, batches=candidates, groups=(8,),
+                          device=device)[0]

@@ -87,15 +87,16 @@ def random_solute(rng: np.random.Generator, nsite: int):
     return dict(xyz=xyz - xyz.mean(axis=0), charge=q, sig=sig, eps=eps, mass=mass)
 
 
+_RADICES = (16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2)
+
+
 def fft_friendly(n: int) -> int:
-    """Smallest 2^a 3^b 5^c >= n."""
-    m = max(int(n), 1)
+    """Smallest grid length >= n that the PME kernels transform best: even (the real rows
+    pair into complex ones) and a product of two radices of at most 16 (two shared-memory
+    passes per axis; 2^a 3^b 5^c lengths without such a split, like 125, take three)."""
+    m = max(int(n), 2)
     while True:
-        k = m
-        for p in (2, 3, 5):
-            while k % p == 0:
-                k //= p
-        if k == 1:
+        if m % 2 == 0 and any(m % r == 0 and m // r in _RADICES for r in _RADICES):
             return m
         m += 1
 

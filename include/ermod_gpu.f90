@@ -19,7 +19,7 @@ module ermod_gpu
      integer(c_int32_t) :: ms1max, ms2max, ms3max, wgtslf, corrcal, selfcal
      integer(c_int32_t) :: force_calculation, precision, batch, count_mirror
      real(c_double) :: elecut, lwljcut, upljcut, screen, temp, block_threshold
-     integer(c_int32_t) :: boxshp, reserved_
+     integer(c_int32_t) :: boxshp, finish_group
   end type ermod_params
 
   interface

@@ -81,7 +81,8 @@ typedef struct ermod_params {
   double temp;               /* kT in kcal/mol */
   double block_threshold;    /* accepted for interface parity; the GPU path needs no cell list */
   int32_t boxshp;            /* 1 periodic, 0 non-periodic (bare Coulomb, NVT; engmain.F90:306) */
-  int32_t reserved_;
+  int32_t finish_group;      /* mixed path: placements per molecule-energy block, 4 or 8 (0 = automatic;
+                                the batch must be a multiple of it); a tile shape for autotuners */
 } ermod_params;
 
 typedef struct ermod_ctx ermod_ctx;

@@ -137,11 +137,9 @@ def check_histograms(u_gpu, u_orc, edges, precision, label="", band=None):
     return rep
 
 
-def weighted_bounds(u_orc, weights, edges, band, rtol_w, corr=False):
-    """Bin-by-bin bounds on |edens_gpu - edens_orc| (and ecorr) of a weighted accumulation:
-    rtol_w of the oracle's value for the weights' relative error, plus, per placement, its
-    weight times the molecules within the band of either edge of the bin (each may sit in
-    the neighbouring bin on the GPU)."""
+def _counts_and_movers(u_orc, edges, band):
+    """Per placement: the oracle's histogram H and, bin by bin, the molecules M within the
+    band of one of the bin's edges (counted in the bin and in the neighbour across it)."""
     E = len(edges)
     H = np.stack([histogram(u, edges) for u in np.atleast_2d(u_orc)]).astype(float)
     M = np.zeros_like(H)
@@ -151,6 +149,20 @@ def weighted_bounds(u_orc, weights, edges, band, rtol_w, corr=False):
         dn = (b >= 1) & (np.abs(u - edges[np.clip(b, 0, E - 1)]) <= band)  # may move to b - 1
         for mask, tgt in ((up, b), (up, b + 1), (dn, b), (dn, b - 1)):
             np.add.at(M[p], tgt[mask], 1.0)
+    return H, M
+
+
+def weighted_bounds(u_orc, weights, edges, band, rtol_w, corr=False, blocks=None):
+    """Bin-by-bin bounds on |edens_gpu - edens_orc| (and ecorr) of a weighted accumulation:
+    rtol_w of the oracle's value for the weights' relative error, plus, per placement, its
+    weight times the molecules within the band of either edge of the bin (each may sit in
+    the neighbouring bin on the GPU).  Several solvent species: blocks = [(u_orc of the
+    species' molecules, the species' edges), ...] in bin-block order (u_orc, edges unused)."""
+    if blocks is None:
+        blocks = [(u_orc, edges)]
+    parts = [_counts_and_movers(u, e, band) for u, e in blocks]
+    H = np.concatenate([h for h, _ in parts], axis=1)
+    M = np.concatenate([m for _, m in parts], axis=1)
     w = np.asarray(weights, float)
     ed = (w[:, None] * H).sum(0)
     g = 1.0 + rtol_w  # a moved molecule carries the GPU's weight

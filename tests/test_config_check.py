@@ -249,18 +249,29 @@ def test_gpu_skip_matches_oracle(gpu_lib, oracle, precision, case):
     params, topo, bins, frames, check, tags, keep = _setup(wgtslf=1, **case)
     r_orc, a_orc = _run_oracle(oracle, params, topo, bins, frames, tags, check)
     gpu = _gpu(params, topo, bins, precision, check, batch=4)  # placements span batches
-    edges = bins["uvcrd"]
-    ug, uo, u0 = [], [], []
+    # two species: the waters (bin block 1) and the other solute molecules (block 2); each
+    # placement's own solute has no energy
+    n1 = int(bins["uvmax"][0])
+    e1, e2 = bins["uvcrd"][:n1], bins["uvcrd"][n1:]
+    nw = int(topo["nummol"]) - NSLT
+    first = int(topo["nummol"]) - NSLT + 1
+    ug1, uo1, ug2, uo2, u0 = [], [], [], [], []
     for (pos, cell), tg, k, ro in zip(frames, tags, keep, r_orc):
         gpu.frame(pos, cell)
         rg = gpu.placements(tg, want_uvengy=True, want_flceng=True)
         assert not np.any(rg["uvengy"][~k]) and not np.any(rg["flceng"][~k]), "rejected rows are zero"
         helpers.check_energies(rg["uvengy"][k], ro["uvengy"][k], precision, f"config check {insposition}")
-        ug.append(rg["uvengy"][k, 1:])
-        uo.append(ro["uvengy"][k, 1:])
-        u0.append(ro["uvengy"][k, 0])
-    ug, uo, u0 = np.concatenate(ug), np.concatenate(uo), np.concatenate(u0)
-    rep = helpers.check_histograms(ug, uo, edges, precision, f"config check {insposition}")
+        for p in np.nonzero(k)[0]:
+            others = np.delete(np.arange(1 + nw, 1 + nw + NSLT), tg[p] - first)
+            ug1.append(rg["uvengy"][p, 1:1 + nw])
+            uo1.append(ro["uvengy"][p, 1:1 + nw])
+            ug2.append(rg["uvengy"][p, others])
+            uo2.append(ro["uvengy"][p, others])
+            u0.append(ro["uvengy"][p, 0])
+    ug1, uo1, ug2, uo2, u0 = (np.array(x) for x in (ug1, uo1, ug2, uo2, u0))
+    rep = helpers.check_histograms(ug1, uo1, e1, precision, f"config check {insposition}")
+    rep2 = helpers.check_histograms(ug2, uo2, e2, precision, f"config check {insposition}, solutes")
+    rep["other_bin"] += rep2["other_bin"]
     ag = gpu.accum()
     gpu.close()
     assert ag["engsmpl"] == a_orc["engsmpl"] == len(u0)
@@ -277,7 +288,8 @@ def test_gpu_skip_matches_oracle(gpu_lib, oracle, precision, case):
     np.testing.assert_allclose(ag["engnorm"], a_orc["engnorm"], rtol=max(rtol_w, 1e-12))
     if precision == "fp64" or rep["other_bin"] == 0:
         np.testing.assert_allclose(ag["edens"], a_orc["edens"], rtol=max(rtol_w, 1e-12), atol=0)
-    b_ed, b_ec = helpers.weighted_bounds(uo, wts, edges, helpers.mixed_band(sol), rtol_w, corr=True)
+    b_ed, b_ec = helpers.weighted_bounds(None, wts, None, helpers.mixed_band(sol), rtol_w, corr=True,
+                                         blocks=[(uo1, e1), (uo2, e2)])
     assert np.all(np.abs(ag["edens"] - a_orc["edens"]) <= b_ed + 1e-12 * np.abs(a_orc["edens"]))
     assert np.all(np.abs(ag["ecorr"] - a_orc["ecorr"]) <= b_ec + 1e-12 * np.abs(a_orc["ecorr"]))
     for sp in range(1, len(ag["minuv"])):

@@ -75,3 +75,34 @@ def test_graph_of_systems_matches_ordinary_calls(gpu_lib):
     g.close()
     for eng in engines:
         eng.close()
+
+
+def test_tile_shapes_give_identical_results(gpu_lib):
+    """The autotuner's tile shapes change the work split, not the arithmetic: finish groups 4
+    and 8 and batches 8 and 16 give bit-identical energies and accumulators (ecorr: for
+    equal batches), and autotune_tiles returns one of its candidates with a rate for each."""
+    from ermod_gb300.engproc import EnergyRepresentation
+    from ermod_gb300.multisystem import autotune_tiles
+    w = _systems()[1]
+    topo = setconf.setparam_topology(w.species(), slttype=2)
+    bins = setconf.enginit_bins(topo["numslv"])
+    pos, cell = w.frame(0)
+    pl = w.placements(0, 24)
+    tag = np.full(len(pl), topo["nummol"], np.int32)
+    out = []
+    for B, G in ((8, 8), (8, 4), (16, 4), (16, 8)):
+        eng = EnergyRepresentation(w.params, topo, bins, precision="mixed", batch=B, finish_group=G)
+        eng.frame(pos, cell)
+        r = eng.placements(tag, pl, want_uvengy=True)
+        out.append((r["uvengy"], eng.accum()))
+        eng.close()
+    for u, a in out[1:]:
+        np.testing.assert_array_equal(u, out[0][0])
+        for key in ("edens", "engnorm", "minuv", "maxuv", "voffset"):
+            np.testing.assert_array_equal(a[key], out[0][1][key], err_msg=key)
+    # ecorr's float-float ring flushes follow the batch: equal for equal batches
+    np.testing.assert_array_equal(out[1][1]["ecorr"], out[0][1]["ecorr"])
+    np.testing.assert_array_equal(out[3][1]["ecorr"], out[2][1]["ecorr"])
+    B, G, rates = autotune_tiles(w.params, topo, bins, (pos, cell), pl, topo["nummol"], batches=(8, 16), groups=(4, 8))
+    assert (B, G) in rates and set(rates) == {(8, 4), (8, 8), (16, 4), (16, 8)}
+    assert all(v > 0 for v in rates.values())
