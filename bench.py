@@ -351,13 +351,20 @@ def run_ours(args):
     bytes_per_launch = per_pl[dom] * per_launch
     peak, peak_kind = load_peaks()
     achieved = bytes_per_launch / (avg_launch_ms / 1000.0) / 1e9
-    traffic = None
+    traffic = pipes = None
     if args.workload == "refs_large":
         traffic = roofline.MEASURED_TRAFFIC_REFS_LARGE[dom] * per_launch
+        # the issue / pipe use that bounds the kernel (the HBM fraction alone does not: it
+        # waits on barriers and instruction issue), and the fraction it reaches launched alone
+        pm = dict(roofline.MEASURED_PIPES_REFS_LARGE[dom])
+        alone_gbs = per_pl[dom] * 256 / (pm["standalone_us"] * 1e-6) / 1e9
+        pipes = dict(pm, frac_standalone=alone_gbs / peak, source=roofline.PIPES_SOURCE,
+                     note="ncu --set full of one 256-placement launch; frac_standalone = algorithmic "
+                          "bytes / that launch's duration / peak")
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
             "traffic_note": "ncu DRAM read+write per launch (one capture, scaled to the launch's placements)",
-            "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_ms,
+            "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_ms, "pipes": pipes,
             "phase_ms_per_step": {k: v / args.steps for k, v in phases.items()}}
     clocks = clk.summary()
 

@@ -410,6 +410,15 @@ constexpr int kSites = 32;  // solute sites staged per chunk
 constexpr int kR1 = 4, kR3 = 3;  // generation tile: kR3 k3 values x kR1 k1 values per thread
 static_assert(kR1 == 4, "pme_a reads a tile row's engfac values as one float4");
 
+// Large grids in pme_a: a work buffer as large as the slab would leave room for one CTA
+// per SM, so the k3 transform runs over two halves of the columns through a work buffer
+// of half the slab's columns (and the site staging takes smaller chunks to fit in it).
+constexpr int pme_a_hp(int KC) { return ((KC / 2 + 1 + kR1 - 1) / kR1) * kR1; }
+constexpr bool pme_a_halves(int KC) {  // cubic grids with compile-time sizes (KC > 0)
+  return KC > 0 && two_pass(KC) && sizeof(float2) * ((size_t)2 * KC * pme_a_hp(KC) + KC) > 110 * 1024;
+}
+constexpr int pme_a_work_cols(int KC) { return pme_a_halves(KC) ? (KC / 2 + 2) / 2 : pme_a_hp(KC); }
+
 struct PmeArgs {
   const float2* bvec;   // [nb][S][3][Kmax]
   const float* u_qf;    // [nb][S]
@@ -435,8 +444,8 @@ __global__ void __launch_bounds__(kPmeAThreads, kPmeAMinBlocks) pme_a_kernel(Pme
   const int K3 = KC ? KC : A.K3, H = KC ? KC / 2 + 1 : A.H;
   const int Hp = KC ? ((KC / 2 + 1 + kR1 - 1) / kR1) * kR1 : A.Hp;
   float2* slab = sm;                          // [K3][Hp]
-  float2* work = sm + (size_t)K3 * Hp;        // [K3][Hp]; site staging during generation
-  float2* tw3 = work + (size_t)K3 * Hp;       // [K3]
+  float2* work = sm + (size_t)K3 * Hp;        // [K3][Hp or half of it]; site staging during generation
+  float2* tw3 = work + (size_t)K3 * (KC ? pme_a_work_cols(KC) : Hp);  // [K3]
   const int ns = A.u_nsite[b];
   for (int i = threadIdx.x; i < K3; i += blockDim.x) {
     const float2 t = A.twiddle[A.K1 + A.K2 + i];
@@ -566,7 +575,11 @@ __global__ void __launch_bounds__(kPmeAThreads, kPmeAMinBlocks) pme_a_kernel(Pme
   float2* out = A.t1 + (size_t)b * K3 * A.K2 * H + (size_t)k2 * H;
   if constexpr (KC > 0) {
     constexpr int HC = KC / 2 + 1, HPC = ((HC + kR1 - 1) / kR1) * kR1;
-    if constexpr (two_pass(KC))
+    if constexpr (pme_a_halves(KC)) {  // columns [0, HA), then [HA, HC), through a half buffer
+      constexpr int HA = (HC + 1) / 2, HB = HC - HA;
+      fft2_t<KC, HA, HPC, 1, HA, 1, KC * HC, 1, kPmeAThreads>(slab, work, out, tw3);
+      fft2_t<KC, HB, HPC, 1, HB, 1, KC * HC, 1, kPmeAThreads>(slab + HA, work, out + HA, tw3);
+    } else if constexpr (two_pass(KC))
       fft2_t<KC, HC, HPC, 1, HPC, 1, KC * HC, 1, kPmeAThreads>(slab, work, out, tw3);
     else
       fft3_t<KC, HC, HPC, 1, HPC, 1, KC * HC, 1, kPmeAThreads>(slab, work, slab, out, tw3);
@@ -582,23 +595,24 @@ __global__ void __launch_bounds__(kPmeAThreads, kPmeAMinBlocks) pme_a_kernel(Pme
 
 // The two passes around the row-pair layout of pme_b_planes_fused.  pass_to_pairs: the
 // second k2 pass (radix R1 = K / R0, NS = R0, columns k1) storing element (k2, k1) at
-// [k2 / 2][k1][k2 % 2], pairs 2H apart.
-template <int KC>
+// [k2 / 2][k1][k2 % 2], pairs 2H apart.  NC columns starting at column c0 of the plane,
+// read from a buffer whose rows (fixed k2) are IS elements long.
+template <int KC, int NC = KC / 2 + 1, int IS = KC / 2 + 1>
 __device__ __forceinline__ void pass_to_pairs(const float2* __restrict__ A, float2* __restrict__ B,
-                                              const float2* __restrict__ tw) {
+                                              const float2* __restrict__ tw, int c0 = 0) {
   constexpr int HC = KC / 2 + 1, R0 = first_radix(KC), R = KC / R0, NR = KC / R, SP = 2 * HC;
   if constexpr (R0 % 2 == 0) {
     // a thread transforms the adjacent columns j, j + 1 (j even): their outputs e, e + 1
     // are the two rows of one pair, stored with one 16-byte, conflict-free store
-    for (int t = threadIdx.x; t < HC * (NR / 2); t += kPmeBThreads) {
-      const int jp = t / HC;
-      const int col = t - jp * HC;
+    for (int t = threadIdx.x; t < NC * (NR / 2); t += kPmeBThreads) {
+      const int jp = t / NC;
+      const int col = t - jp * NC;
       const int j = 2 * jp;
       float2 v0[R], v1[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        v0[r] = A[col + (j + r * NR) * HC];
-        v1[r] = A[col + (j + 1 + r * NR) * HC];
+        v0[r] = A[col + (j + r * NR) * IS];
+        v1[r] = A[col + (j + 1 + r * NR) * IS];
       }
 #pragma unroll
       for (int r = 1; r < R; ++r) {
@@ -610,16 +624,17 @@ __device__ __forceinline__ void pass_to_pairs(const float2* __restrict__ A, floa
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const int e = j + r * R0;  // even
-        *reinterpret_cast<float4*>(B + (e >> 1) * SP + 2 * col) = make_float4(v0[r].x, v0[r].y, v1[r].x, v1[r].y);
+        *reinterpret_cast<float4*>(B + (e >> 1) * SP + 2 * (c0 + col)) =
+            make_float4(v0[r].x, v0[r].y, v1[r].x, v1[r].y);
       }
     }
   } else {
-    for (int t = threadIdx.x; t < HC * NR; t += kPmeBThreads) {
-      const int j = t / HC;  // < NR = R0 = NS, so the pass's k is j
-      const int col = t - j * HC;
+    for (int t = threadIdx.x; t < NC * NR; t += kPmeBThreads) {
+      const int j = t / NC;  // < NR = R0 = NS, so the pass's k is j
+      const int col = t - j * NC;
       float2 v[R];
 #pragma unroll
-      for (int r = 0; r < R; ++r) v[r] = A[col + (j + r * NR) * HC];
+      for (int r = 0; r < R; ++r) v[r] = A[col + (j + r * NR) * IS];
       if (j > 0) {
 #pragma unroll
         for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[r * j]);
@@ -628,7 +643,7 @@ __device__ __forceinline__ void pass_to_pairs(const float2* __restrict__ A, floa
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const int e = j + r * R0;
-        B[(e >> 1) * SP + 2 * col + (e & 1)] = v[r];
+        B[(e >> 1) * SP + 2 * (c0 + col) + (e & 1)] = v[r];
       }
     }
   }
@@ -636,19 +651,20 @@ __device__ __forceinline__ void pass_to_pairs(const float2* __restrict__ A, floa
 
 // pass_from_pairs: the first row pass (radix R0, no twiddles, K / 2 row pairs) packing
 // Z_p[k] = X_{2p}[k] + i X_{2p+1}[k] while it loads, Hermitian-completed in k1 (the upper
-// half of k1 is the conjugate of the stored half); rows K | 1 apart in B
-template <int KC>
-__device__ __forceinline__ void pass_from_pairs(const float2* __restrict__ A, float2* __restrict__ B) {
-  constexpr int HC = KC / 2 + 1, R = first_radix(KC), NR = KC / R, NP = KC / 2, SP = 2 * HC, RS = KC | 1;
-  for (int t = threadIdx.x; t < NP * NR; t += kPmeBThreads) {
-    const int j = t / NP;
-    const int p = t - j * NP;
+// half of k1 is the conjugate of the stored half); rows K | 1 apart in B.  NPH pairs
+// starting at pair p0 of A, written from row 0 of B.
+template <int KC, int NPH = KC / 2>
+__device__ __forceinline__ void pass_from_pairs(const float2* __restrict__ A, float2* __restrict__ B, int p0 = 0) {
+  constexpr int HC = KC / 2 + 1, R = first_radix(KC), NR = KC / R, SP = 2 * HC, RS = KC | 1;
+  for (int t = threadIdx.x; t < NPH * NR; t += kPmeBThreads) {
+    const int j = t / NPH;
+    const int p = t - j * NPH;
     float2 v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int k = j + r * NR;
       const int kk = k < HC ? k : KC - k;
-      const float4 q = *reinterpret_cast<const float4*>(A + p * SP + 2 * kk);
+      const float4 q = *reinterpret_cast<const float4*>(A + (p0 + p) * SP + 2 * kk);
       float2 x0 = make_float2(q.x, q.y), x1 = make_float2(q.z, q.w);
       if (k >= HC) {
         x0.y = -x0.y;
@@ -683,6 +699,48 @@ __device__ __forceinline__ float2* pme_b_planes_fused(const float2* in, float2* 
   stockham_pass_t<R1, KC, R0, KC / 2, 1, RS, 1, RS, kPmeBThreads>(s0, s1, tw);
   __syncthreads();
   return s1;
+}
+
+// Large grids: two full plane buffers would leave room for one CTA per SM, so the plane
+// stays in one full buffer A and every transform runs in two halves through a buffer W of
+// half its size -- the k2 transforms over the left and then the right half of the columns
+// (first pass plane -> W, second W -> A in the pair layout), the row transforms over the
+// first and then the second half of the row pairs (first pass A -> W, second W -> A as
+// rows K | 1 apart: a half's rows end below the pairs the other half still reads).
+constexpr bool pme_b_halves(int KC) {  // cubic grids with compile-time sizes (KC > 0)
+  return KC > 0 && two_pass(KC) && KC % 4 == 0 &&
+         sizeof(float2) * (2 * (size_t)(KC / 2 + 1) * KC + KC) > 110 * 1024;
+}
+constexpr size_t pme_b_half_w(int KC) {  // W in float2: the wider half of either phase
+  return (size_t)KC * ((KC / 2 + 2) / 2) > (size_t)((KC / 2 + 1) / 2) * (KC | 1)
+             ? (size_t)KC * ((KC / 2 + 2) / 2)
+             : (size_t)((KC / 2 + 1) / 2) * (KC | 1);
+}
+
+template <int KC>
+__device__ __forceinline__ float2* pme_b_planes_halves(const float2* in, float2* A, float2* W,
+                                                       const float2* tw) {
+  constexpr int HC = KC / 2 + 1, R0 = first_radix(KC), R1 = KC / R0, RS = KC | 1, NP = KC / 2;
+  constexpr int HA = (HC + 1) / 2, HB = HC - HA;  // column halves
+  constexpr int PA = (NP + 1) / 2, PB = NP - PA;  // row-pair halves
+  __syncthreads();
+  stockham_pass_t<R0, KC, 1, HA, HC, 1, HA, 1, kPmeBThreads>(in, W, tw);
+  __syncthreads();
+  pass_to_pairs<KC, HA, HA>(W, A, tw, 0);
+  __syncthreads();
+  stockham_pass_t<R0, KC, 1, HB, HC, 1, HB, 1, kPmeBThreads>(in + HA, W, tw);
+  __syncthreads();
+  pass_to_pairs<KC, HB, HB>(W, A, tw, HA);
+  __syncthreads();
+  pass_from_pairs<KC, PA>(A, W, 0);
+  __syncthreads();
+  stockham_pass_t<R1, KC, R0, PA, 1, RS, 1, RS, kPmeBThreads>(W, A, tw);
+  __syncthreads();
+  pass_from_pairs<KC, PB>(A, W, PA);
+  __syncthreads();
+  stockham_pass_t<R1, KC, R0, PB, 1, RS, 1, RS, kPmeBThreads>(W, A + (size_t)PA * RS, tw);
+  __syncthreads();
+  return A;
 }
 
 // the plane's k2 transforms, a separate pass that packs row pairs (Hermitian-completed in
@@ -811,7 +869,7 @@ __global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(Pme
   const size_t bufsz = max(plane, (size_t)npair * K1p);
   float2* s0 = sm;
   float2* s1 = sm + bufsz;
-  float2* tw1 = s1 + bufsz;
+  float2* tw1 = s1 + (pme_b_halves(KC) ? pme_b_half_w(KC) : bufsz);
   float2* tw2 = KC ? tw1 : tw1 + K1;  // one table for a cubic grid (K1 = K2)
   for (int i = threadIdx.x; i < (KC ? K1 : K1 + K2); i += blockDim.x) {
     const float2 t = A.twiddle[i];
@@ -825,7 +883,9 @@ __global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(Pme
   // the real rows, pair p (rows 2p, 2p + 1 interleaved) K1p apart
   float2* res = nullptr;
   if (live) {
-    if constexpr (KC > 0 && two_pass(KC) && KC % 4 == 0)
+    if constexpr (pme_b_halves(KC))
+      res = pme_b_planes_halves<KC>(in, s0, s1, tw1);
+    else if constexpr (KC > 0 && two_pass(KC) && KC % 4 == 0)
       res = pme_b_planes_fused<KC>(in, s0, s1, tw1);
     else
       res = pme_b_planes<KC>(A, in, s0, s1, tw1, tw2);
@@ -908,13 +968,19 @@ __global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(Pme
   }
 }
 
-size_t pme_a_smem(int K3, int Hp) { return sizeof(float2) * ((size_t)2 * K3 * Hp + K3); }
+// sized: the compile-time cubic kernel of this K runs (its work buffer may be a half one)
+size_t pme_a_smem(int K3, int Hp, bool sized = false) {
+  const size_t wcols = sized ? (size_t)pme_a_work_cols(K3) : (size_t)Hp;
+  return sizeof(float2) * ((size_t)K3 * Hp + (size_t)K3 * wcols + K3);
+}
 // shared_tw: a cubic grid with compile-time sizes keeps one twiddle table for k1 and k2
 size_t pme_b_smem(int K1, int K2, int H, bool shared_tw) {
   const size_t plane = (size_t)K2 * H;
   const size_t npair = (K2 + 1) / 2;
   const size_t bufsz = std::max(plane, npair * (size_t)(K1 | 1));
-  return sizeof(float2) * (2 * bufsz + K1 + (shared_tw ? 0 : K2));
+  // the compile-time cubic kernels of large grids keep one full buffer and a half one
+  const size_t second = (shared_tw && pme_b_halves(K1)) ? pme_b_half_w(K1) : bufsz;
+  return sizeof(float2) * (bufsz + second + K1 + (shared_tw ? 0 : K2));
 }
 
 }  // namespace
@@ -943,7 +1009,6 @@ cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a) {
   A.H = e.H();
   A.Hp = ((A.H + kR1 - 1) / kR1) * kR1;
   A.Kmax = e.Kmax();
-  A.chunk = std::max(1, std::min(kSites, (A.K3 * A.Hp) / (A.K3 + A.Hp)));
   A.K1p = A.K1 | 1;
   A.halo = e.P_order - 1;
   A.XP = e.phi_dims[0];
@@ -981,7 +1046,11 @@ cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a) {
       kb = sized[i].b;
     }
   const int KC = slot ? A.K1 : 0;
-  const size_t sa = pme_a_smem(A.K3, A.Hp), sb = pme_b_smem(A.K1, A.K2, A.H, KC > 0);
+  // solute sites staged per generation chunk: both tables, chunk x (K3 + Hp), fit in pme_a's
+  // work buffer
+  const int wcols = KC ? pme_a_work_cols(KC) : A.Hp;
+  A.chunk = std::max(1, std::min(kSites, (A.K3 * wcols) / (A.K3 + A.Hp)));
+  const size_t sa = pme_a_smem(A.K3, A.Hp, KC > 0), sb = pme_b_smem(A.K1, A.K2, A.H, KC > 0);
   static SmemAttr attr_a[1 + nsized], attr_b[1 + nsized];  // per kernel
   if ((err = attr_a[slot].ensure(ka, sa)) != cudaSuccess) return err;
   if ((err = attr_b[slot].ensure(kb, sb)) != cudaSuccess) return err;

@@ -136,13 +136,15 @@ def test_solute_above_the_limit_is_refused(gpu_lib):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_largest_uneven_system(gpu_lib, oracle, precision):
-    """The largest system of the 16-system set: 58,329 waters in a 120 A box, PME 125^3
-    (three-pass transforms), a 15-site solute and an energy coordinate from -200 kcal/mol
-    (4,996 bins: global-memory counts in the finish kernel)."""
+    """The largest system of the 16-system set: 58,329 waters in a 120 A box, a 15-site
+    solute and an energy coordinate from -200 kcal/mol (4,996 bins: global-memory counts in
+    the finish kernel), with the grid set to 125^3 (three-pass transforms; the set itself
+    rounds the box to 128^3)."""
     from ermod_gb300 import setconf, synth
     from ermod_gb300.engproc import EnergyRepresentation
     w = max(synth.uneven(), key=lambda x: x.nwater)
-    assert w.nwater > 58000 and w.params["ms1max"] == 125
+    assert w.nwater > 58000 and w.params["ms1max"] == 128
+    w.params.update(ms1max=125, ms2max=125, ms3max=125)
     topo = setconf.setparam_topology(w.species(), slttype=w.params["slttype"])
     bins = setconf.enginit_bins(topo["numslv"], w.hist)
     gpu = EnergyRepresentation(w.params, topo, bins, precision=precision)
