@@ -130,7 +130,8 @@ struct Engine {
   bool flush_pend[2] = {false, false};  // a flush of that half may still be running
   int* d_ring_hist = nullptr;     // [ring_cap][ermax]
   double* d_ring_w = nullptr;     // [ring_cap]
-  int* d_ring_nz = nullptr;       // [ring_cap][ermax] packed (bin | count << 16)... see kernels
+  int* d_ring_nz = nullptr;       // ecorr flush scratch, [2][ring_cap][ermax]: the FP64 flush's occupied-bin
+                                  // lists (bins, counts); the mixed flush's active-bin flags and list
   int* d_ring_nnz = nullptr;      // [ring_cap] occupied bins per entry
   int* d_ring_valid = nullptr;    // [ring_cap] entry accumulated (no error in its batch)
   double* d_u0 = nullptr;         // [2][Bmax] solute self energies (two batch slots)

@@ -335,6 +335,10 @@ __device__ __forceinline__ void fft_cols_io(const float2* in, int ies, int ics, 
 // arithmetic (the ALU share of the transforms) folds into constants.
 constexpr int kPmeAThreads = 512, kPmeAMinBlocks = 2;  // pme_a
 constexpr int kPmeBThreads = 512, kPmeBMinBlocks = 2;  // pme_b
+// Small compile-time grids (K < 64) have too few transform columns and generation tiles
+// to keep 512 threads busy: their CTAs take 256 threads, four to an SM.
+constexpr int pme_threads(int KC) { return (KC > 0 && KC < 64) ? 256 : 512; }
+constexpr int pme_min_blocks(int KC) { return (KC > 0 && KC < 64) ? 4 : 2; }
 
 constexpr bool radix_ok(int r) {
   return r == 16 || r == 15 || r == 12 || r == 10 || r == 9 || r == 8 || r == 6 || r == 5 || r == 4 || r == 3 ||
@@ -437,7 +441,7 @@ struct PmeArgs {
 
 // KC > 0: a K^3 grid with K = KC and compile-time transforms; KC = 0: any grid
 template <int KC>
-__global__ void __launch_bounds__(kPmeAThreads, kPmeAMinBlocks) pme_a_kernel(PmeArgs A) {
+__global__ void __launch_bounds__(pme_threads(KC), pme_min_blocks(KC)) pme_a_kernel(PmeArgs A) {
   extern __shared__ float2 sm[];
   const int k2 = blockIdx.x, b = blockIdx.y;
   // compile-time sizes when specialised (the runtime values are then equal)
@@ -577,12 +581,12 @@ __global__ void __launch_bounds__(kPmeAThreads, kPmeAMinBlocks) pme_a_kernel(Pme
     constexpr int HC = KC / 2 + 1, HPC = ((HC + kR1 - 1) / kR1) * kR1;
     if constexpr (pme_a_halves(KC)) {  // columns [0, HA), then [HA, HC), through a half buffer
       constexpr int HA = (HC + 1) / 2, HB = HC - HA;
-      fft2_t<KC, HA, HPC, 1, HA, 1, KC * HC, 1, kPmeAThreads>(slab, work, out, tw3);
-      fft2_t<KC, HB, HPC, 1, HB, 1, KC * HC, 1, kPmeAThreads>(slab + HA, work, out + HA, tw3);
+      fft2_t<KC, HA, HPC, 1, HA, 1, KC * HC, 1, pme_threads(KC)>(slab, work, out, tw3);
+      fft2_t<KC, HB, HPC, 1, HB, 1, KC * HC, 1, pme_threads(KC)>(slab + HA, work, out + HA, tw3);
     } else if constexpr (two_pass(KC))
-      fft2_t<KC, HC, HPC, 1, HPC, 1, KC * HC, 1, kPmeAThreads>(slab, work, out, tw3);
+      fft2_t<KC, HC, HPC, 1, HPC, 1, KC * HC, 1, pme_threads(KC)>(slab, work, out, tw3);
     else
-      fft3_t<KC, HC, HPC, 1, HPC, 1, KC * HC, 1, kPmeAThreads>(slab, work, slab, out, tw3);
+      fft3_t<KC, HC, HPC, 1, HPC, 1, KC * HC, 1, pme_threads(KC)>(slab, work, slab, out, tw3);
   } else {
     fft_cols_io(slab, Hp, 1, work, slab, A.p3, H, A.fH, Hp, 1, out, A.K2 * H, 1, tw3);
   }
@@ -604,7 +608,7 @@ __device__ __forceinline__ void pass_to_pairs(const float2* __restrict__ A, floa
   if constexpr (R0 % 2 == 0) {
     // a thread transforms the adjacent columns j, j + 1 (j even): their outputs e, e + 1
     // are the two rows of one pair, stored with one 16-byte, conflict-free store
-    for (int t = threadIdx.x; t < NC * (NR / 2); t += kPmeBThreads) {
+    for (int t = threadIdx.x; t < NC * (NR / 2); t += pme_threads(KC)) {
       const int jp = t / NC;
       const int col = t - jp * NC;
       const int j = 2 * jp;
@@ -629,7 +633,7 @@ __device__ __forceinline__ void pass_to_pairs(const float2* __restrict__ A, floa
       }
     }
   } else {
-    for (int t = threadIdx.x; t < NC * NR; t += kPmeBThreads) {
+    for (int t = threadIdx.x; t < NC * NR; t += pme_threads(KC)) {
       const int j = t / NC;  // < NR = R0 = NS, so the pass's k is j
       const int col = t - j * NC;
       float2 v[R];
@@ -656,7 +660,7 @@ __device__ __forceinline__ void pass_to_pairs(const float2* __restrict__ A, floa
 template <int KC, int NPH = KC / 2>
 __device__ __forceinline__ void pass_from_pairs(const float2* __restrict__ A, float2* __restrict__ B, int p0 = 0) {
   constexpr int HC = KC / 2 + 1, R = first_radix(KC), NR = KC / R, SP = 2 * HC, RS = KC | 1;
-  for (int t = threadIdx.x; t < NPH * NR; t += kPmeBThreads) {
+  for (int t = threadIdx.x; t < NPH * NR; t += pme_threads(KC)) {
     const int j = t / NPH;
     const int p = t - j * NPH;
     float2 v[R];
@@ -690,13 +694,13 @@ template <int KC>
 __device__ __forceinline__ float2* pme_b_planes_fused(const float2* in, float2* s0, float2* s1, const float2* tw) {
   constexpr int HC = KC / 2 + 1, R0 = first_radix(KC), R1 = KC / R0, RS = KC | 1;
   __syncthreads();
-  stockham_pass_t<R0, KC, 1, HC, HC, 1, HC, 1, kPmeBThreads>(in, s0, tw);
+  stockham_pass_t<R0, KC, 1, HC, HC, 1, HC, 1, pme_threads(KC)>(in, s0, tw);
   __syncthreads();
   pass_to_pairs<KC>(s0, s1, tw);
   __syncthreads();
   pass_from_pairs<KC>(s1, s0);
   __syncthreads();
-  stockham_pass_t<R1, KC, R0, KC / 2, 1, RS, 1, RS, kPmeBThreads>(s0, s1, tw);
+  stockham_pass_t<R1, KC, R0, KC / 2, 1, RS, 1, RS, pme_threads(KC)>(s0, s1, tw);
   __syncthreads();
   return s1;
 }
@@ -724,21 +728,21 @@ __device__ __forceinline__ float2* pme_b_planes_halves(const float2* in, float2*
   constexpr int HA = (HC + 1) / 2, HB = HC - HA;  // column halves
   constexpr int PA = (NP + 1) / 2, PB = NP - PA;  // row-pair halves
   __syncthreads();
-  stockham_pass_t<R0, KC, 1, HA, HC, 1, HA, 1, kPmeBThreads>(in, W, tw);
+  stockham_pass_t<R0, KC, 1, HA, HC, 1, HA, 1, pme_threads(KC)>(in, W, tw);
   __syncthreads();
   pass_to_pairs<KC, HA, HA>(W, A, tw, 0);
   __syncthreads();
-  stockham_pass_t<R0, KC, 1, HB, HC, 1, HB, 1, kPmeBThreads>(in + HA, W, tw);
+  stockham_pass_t<R0, KC, 1, HB, HC, 1, HB, 1, pme_threads(KC)>(in + HA, W, tw);
   __syncthreads();
   pass_to_pairs<KC, HB, HB>(W, A, tw, HA);
   __syncthreads();
   pass_from_pairs<KC, PA>(A, W, 0);
   __syncthreads();
-  stockham_pass_t<R1, KC, R0, PA, 1, RS, 1, RS, kPmeBThreads>(W, A, tw);
+  stockham_pass_t<R1, KC, R0, PA, 1, RS, 1, RS, pme_threads(KC)>(W, A, tw);
   __syncthreads();
   pass_from_pairs<KC, PB>(A, W, PA);
   __syncthreads();
-  stockham_pass_t<R1, KC, R0, PB, 1, RS, 1, RS, kPmeBThreads>(W, A + (size_t)PA * RS, tw);
+  stockham_pass_t<R1, KC, R0, PB, 1, RS, 1, RS, pme_threads(KC)>(W, A + (size_t)PA * RS, tw);
   __syncthreads();
   return A;
 }
@@ -758,9 +762,9 @@ __device__ __forceinline__ float2* pme_b_planes(const PmeArgs& A, const float2* 
   if constexpr (KC > 0) {
     constexpr int HC = KC / 2 + 1;
     if constexpr (two_pass(KC))
-      fft2_t<KC, HC, HC, 1, HC, 1, HC, 1, kPmeBThreads>(in, s0, r, tw2);
+      fft2_t<KC, HC, HC, 1, HC, 1, HC, 1, pme_threads(KC)>(in, s0, r, tw2);
     else  // r is s0 for three passes (the runtime plan's count)
-      fft3_t<KC, HC, HC, 1, HC, 1, HC, 1, kPmeBThreads>(in, s0, s1, r, tw2);
+      fft3_t<KC, HC, HC, 1, HC, 1, HC, 1, pme_threads(KC)>(in, s0, s1, r, tw2);
   } else {
     fft_cols_io(in, H, 1, s0, s1, A.p2, H, A.fH, H, 1, r, H, 1, tw2);
   }
@@ -831,10 +835,10 @@ __device__ __forceinline__ float2* pme_b_planes(const PmeArgs& A, const float2* 
   if constexpr (KC > 0) {  // ping-pong between w and r: w -> r -> w (-> r)
     // (KC + 1) / 2 row pairs (the last one a single row when KC is odd), rows KC | 1 apart
     if constexpr (two_pass(KC)) {
-      fft2_t<KC, (KC + 1) / 2, 1, (KC | 1), 1, (KC | 1), 1, (KC | 1), kPmeBThreads>(w, r, w, tw1);
+      fft2_t<KC, (KC + 1) / 2, 1, (KC | 1), 1, (KC | 1), 1, (KC | 1), pme_threads(KC)>(w, r, w, tw1);
       res = w;
     } else {
-      fft3_t<KC, (KC + 1) / 2, 1, (KC | 1), 1, (KC | 1), 1, (KC | 1), kPmeBThreads>(w, r, w, r, tw1);
+      fft3_t<KC, (KC + 1) / 2, 1, (KC | 1), 1, (KC | 1), 1, (KC | 1), pme_threads(KC)>(w, r, w, r, tw1);
       res = r;
     }
     __syncthreads();
@@ -853,7 +857,7 @@ __device__ __forceinline__ float2* pme_b_planes(const PmeArgs& A, const float2* 
 // writes them as whole float4 points (16-byte stores, full 32-byte sectors), instead of
 // every CTA storing 4 bytes at a 16-byte stride (a quarter-used sector per store).
 template <int KC>
-__global__ void __launch_bounds__(kPmeBThreads, kPmeBMinBlocks) pme_b_kernel(PmeArgs A) {
+__global__ void __launch_bounds__(pme_threads(KC), pme_min_blocks(KC)) pme_b_kernel(PmeArgs A) {
   extern __shared__ __align__(16) float2 sm[];  // 16-byte loads of row pairs
   // grid (4, K3, ceil(nb / 4)): the four placements that share an interleaved potential
   // grid run side by side
@@ -1054,7 +1058,8 @@ cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a) {
   static SmemAttr attr_a[1 + nsized], attr_b[1 + nsized];  // per kernel
   if ((err = attr_a[slot].ensure(ka, sa)) != cudaSuccess) return err;
   if ((err = attr_b[slot].ensure(kb, sb)) != cudaSuccess) return err;
-  ka<<<dim3(A.K2, a.nb), kPmeAThreads, sa, a.stream>>>(A);
+  const int nthr = pme_threads(KC);
+  ka<<<dim3(A.K2, a.nb), nthr, sa, a.stream>>>(A);
   e.count_launch();
   if ((err = cudaGetLastError()) != cudaSuccess) return err;
   if (a.phases) {
@@ -1064,7 +1069,7 @@ cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a) {
   if (slot) {  // compile-time sizes: the four CTAs of a group are one cluster
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3(4, A.K3, (a.nb + 3) / 4);
-    cfg.blockDim = dim3(kPmeBThreads);
+    cfg.blockDim = dim3(nthr);
     cfg.dynamicSmemBytes = sb;
     cfg.stream = a.stream;
     cudaLaunchAttribute attr[1];
@@ -1076,7 +1081,7 @@ cudaError_t launch_pme_mixed(Engine& e, const BatchArgs& a) {
     cfg.numAttrs = 1;
     if ((err = cudaLaunchKernelEx(&cfg, kb, A)) != cudaSuccess) return err;
   } else {
-    kb<<<dim3(4, A.K3, (a.nb + 3) / 4), kPmeBThreads, sb, a.stream>>>(A);
+    kb<<<dim3(4, A.K3, (a.nb + 3) / 4), nthr, sb, a.stream>>>(A);
   }
   e.count_launch();
   return cudaGetLastError();
