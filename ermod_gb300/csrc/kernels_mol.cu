@@ -351,6 +351,8 @@ __device__ __forceinline__ int big_item(int parts, int j, int su, int s) {
 // [win, win + kBigPerThread) are recorded with their parts in items[count - win], and bit j
 // of fix is set.  kSum: sum the FP32 terms (the first pass); else only record (the later
 // rounds of a thread with more pairs than one round takes).
+constexpr int kMolSiteCache = 3;  // molecule sites held in registers by the real-space pass
+
 template <bool kSum>
 __device__ __forceinline__ ff real_mixed(const MolArgs& A, const BatchArgs& a, int b, int s0, int ns,
                                          const LjK& k32, float rcut, int4 p0, int4 u0, int j, int* items,
@@ -364,42 +366,63 @@ __device__ __forceinline__ ff real_mixed(const MolArgs& A, const BatchArgs& a, i
   if (dx * dx + dy * dy + dz * dz > rcut * rcut) return real;
   const int nu = a.u_nsite[b];
   const float beta = A.screen_f;
-  for (int su = 0; su < nu; ++su) {
-    const int4 up = a.u_pos[ub + su];
-    const float qu = a.u_qf[ub + su];
-    for (int s = 0; s < ns; ++s) {
-      const int4 vp = A.site_pos[s0 + s];
-      const float ex = (float)(int)((unsigned)vp.x - (unsigned)up.x) * fx;
-      const float ey = (float)(int)((unsigned)vp.y - (unsigned)up.y) * fy;
-      const float ez = (float)(int)((unsigned)vp.z - (unsigned)up.z) * fz;
-      const float r2 = ex * ex + ey * ey + ez * ez;
-      float elj = 0.f, eco = 0.f;
-      const float ljeps = A.ljene_f[vp.w + A.T * up.w];
-      if (ljeps > 0.f) {
-        const float sg2 = A.ljlensq_f[vp.w + A.T * up.w];
-        if (r2 <= k32.lw2)
-          elj = lj_low<float>(A.ljswitch, k32, ljeps, sg2, r2);
-        else if (r2 <= k32.up2)
-          elj = lj_switch<float>(A.ljswitch, k32, ljeps, sg2, r2);
+  // one pair (solute site su at up with charge qu, molecule site s at vp with charge qv)
+  auto pair = [&](int su, const int4& up, float qu, int s, const int4& vp, float qv) {
+    const float ex = (float)(int)((unsigned)vp.x - (unsigned)up.x) * fx;
+    const float ey = (float)(int)((unsigned)vp.y - (unsigned)up.y) * fy;
+    const float ez = (float)(int)((unsigned)vp.z - (unsigned)up.z) * fz;
+    const float r2 = ex * ex + ey * ey + ez * ez;
+    float elj = 0.f, eco = 0.f;
+    const float ljeps = A.ljene_f[vp.w + A.T * up.w];
+    if (ljeps > 0.f) {
+      const float sg2 = A.ljlensq_f[vp.w + A.T * up.w];
+      if (r2 <= k32.lw2)
+        elj = lj_low<float>(A.ljswitch, k32, ljeps, sg2, r2);
+      else if (r2 <= k32.up2)
+        elj = lj_switch<float>(A.ljswitch, k32, ljeps, sg2, r2);
+    }
+    if (A.bare) {
+      if (r2 < k32.ele2) eco = qu * qv / sqrtf(r2);  // realcal_bare
+    } else if (r2 <= k32.ele2) {
+      const float r = sqrtf(r2);
+      eco = qu * qv * erfcf(beta * r) / r;
+    }
+    // parts too large for FP32 (the comparisons are false for NaN and inf)
+    const int parts = (fabsf(elj) <= kFp64Lj ? 0 : kPairLj) | (fabsf(eco) <= kFp64Coulomb ? 0 : kPairCoulomb);
+    if (kSum) {
+      if (!(parts & kPairLj)) real = ff_add(real, elj);
+      if (!(parts & kPairCoulomb)) real = ff_add(real, eco);
+    }
+    if (parts) {
+      const int r = nbig - win;
+      if (r >= 0 && r < kBigPerThread) items[r] = big_item(parts, j, su, s);
+      ++nbig;
+      fix |= 1u << j;
+    }
+  };
+  if (ns <= kMolSiteCache) {
+    // small molecules (water): their sites' positions and charges held in registers for
+    // every solute site
+    int4 vpc[kMolSiteCache];
+    float qvc[kMolSiteCache];
+#pragma unroll
+    for (int s = 0; s < kMolSiteCache; ++s)
+      if (s < ns) {
+        vpc[s] = A.site_pos[s0 + s];
+        qvc[s] = A.site_rec[s0 + s].w;
       }
-      if (A.bare) {
-        if (r2 < k32.ele2) eco = qu * A.site_rec[s0 + s].w / sqrtf(r2);  // realcal_bare
-      } else if (r2 <= k32.ele2) {
-        const float r = sqrtf(r2);
-        eco = qu * A.site_rec[s0 + s].w * erfcf(beta * r) / r;
-      }
-      // parts too large for FP32 (the comparisons are false for NaN and inf)
-      const int parts = (fabsf(elj) <= kFp64Lj ? 0 : kPairLj) | (fabsf(eco) <= kFp64Coulomb ? 0 : kPairCoulomb);
-      if (kSum) {
-        if (!(parts & kPairLj)) real = ff_add(real, elj);
-        if (!(parts & kPairCoulomb)) real = ff_add(real, eco);
-      }
-      if (parts) {
-        const int r = nbig - win;
-        if (r >= 0 && r < kBigPerThread) items[r] = big_item(parts, j, su, s);
-        ++nbig;
-        fix |= 1u << j;
-      }
+    for (int su = 0; su < nu; ++su) {
+      const int4 up = a.u_pos[ub + su];
+      const float qu = a.u_qf[ub + su];
+#pragma unroll
+      for (int s = 0; s < kMolSiteCache; ++s)
+        if (s < ns) pair(su, up, qu, s, vpc[s], qvc[s]);
+    }
+  } else {
+    for (int su = 0; su < nu; ++su) {
+      const int4 up = a.u_pos[ub + su];
+      const float qu = a.u_qf[ub + su];
+      for (int s = 0; s < ns; ++s) pair(su, up, qu, s, A.site_pos[s0 + s], A.site_rec[s0 + s].w);
     }
   }
   return real;
