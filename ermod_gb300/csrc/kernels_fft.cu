@@ -333,8 +333,7 @@ __device__ __forceinline__ void fft_cols_io(const float2* in, int ies, int ics, 
 // The same two Stockham passes as fft_cols_io, with the transform length, radices,
 // column count, strides and thread count known to the compiler, so that the index
 // arithmetic (the ALU share of the transforms) folds into constants.
-constexpr int kPmeAThreads = 512, kPmeAMinBlocks = 2;  // pme_a
-constexpr int kPmeBThreads = 512, kPmeBMinBlocks = 2;  // pme_b
+constexpr int kPmeAThreads = 512;  // pme_a's largest CTA
 // Small compile-time grids (K < 64) have too few transform columns and generation tiles
 // to keep 512 threads busy: their CTAs take 256 threads, four to an SM.
 constexpr int pme_threads(int KC) { return (KC > 0 && KC < 64) ? 256 : 512; }
