@@ -14,7 +14,7 @@ LIB_PATH = os.path.join(HERE, "libermod_gb300.so")
 OK = 0
 E_ENG_MIN, E_ENG_SFT, E_ENG_BUG, E_ENG_CNS, E_RCP_CNS, E_RCP_FST = 101, 102, 103, 104, 105, 106
 E_INS_GEO, E_SET_PRS, E_ENG_SLB = 107, 108, 109
-W_MBIN = 110
+W_MBIN, E_INS_SIZ = 110, 111
 E_PARAM, E_NONCUBOID, E_UNSUPPORTED = 120, 121, 122
 E_CUDA, E_CUFFT, E_NOMEM, E_DEVICE = 130, 131, 132, 133
 PRECISION_FP64, PRECISION_MIXED = 0, 1
@@ -23,7 +23,7 @@ ABI_VERSION = 2
 # halt_with_error identities (mpiproc.F90:203-264) of the status codes
 REFERENCE_CODE = {E_ENG_MIN: "eng_min", E_ENG_SFT: "eng_sft", E_ENG_BUG: "eng_bug", E_ENG_CNS: "eng_cns",
                   E_RCP_CNS: "rcp_cns", E_RCP_FST: "rcp_fst", E_INS_GEO: "ins_geo", E_SET_PRS: "set_prs",
-                  E_ENG_SLB: "eng_slb", W_MBIN: "mbin"}
+                  E_ENG_SLB: "eng_slb", W_MBIN: "mbin", E_INS_SIZ: "ins_siz"}
 
 
 class Params(C.Structure):
@@ -55,6 +55,7 @@ EXPORTS = [
     "ermod_write_selfdist", "ermod_write_corr", "ermod_write_uvrange", "ermod_format_g",
     "ermod_generate_placements", "ermod_intermediate_enable", "ermod_intermediate_get",
     "ermod_set_configuration_check", "ermod_set_aggregate", "ermod_set_reference_structure",
+    "ermod_set_solute_library",
 ]
 
 _lib = None
@@ -118,6 +119,7 @@ def load(path: str = LIB_PATH):
     L.ermod_set_configuration_check.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double, C.c_double]
     L.ermod_set_aggregate.argtypes = [vp, ip, dp]
     L.ermod_set_reference_structure.argtypes = [vp, ip, dp, dp, C.c_int, dp, dp]
+    L.ermod_set_solute_library.argtypes = [vp, C.c_int, C.c_int, dp, C.c_int, dp, C.c_int, C.c_double, C.c_double]
     _lib = L
     return L
 

@@ -340,6 +340,7 @@ const char* ermod_status_string(int s) {
     case ERMOD_E_SET_PRS: return "set_prs: the system parameters are incorrectly set";
     case ERMOD_E_ENG_SLB: return "eng_slb: the slab configuration needs a periodic system";
     case ERMOD_W_MBIN: return "mbin: the maximum binning energy is too low for this species";
+    case ERMOD_E_INS_SIZ: return "ins_siz: the solute structures differ in size";
     case ERMOD_E_PARAM: return "invalid argument";
     case ERMOD_E_NONCUBOID: return "a non-cuboidal cell is not supported";
     case ERMOD_E_UNSUPPORTED: return "unsupported mode";
@@ -516,6 +517,7 @@ int ermod_create(const ermod_params* p_in, int device, ermod_ctx** out) {
 static void free_adjoint(Engine& e);
 static void free_intermediate(Engine& e);
 static void free_config_check(Engine& e);
+static void free_library(Engine& e);
 
 int ermod_destroy(ermod_ctx* c) {
   if (!c) return ERMOD_OK;
@@ -525,6 +527,7 @@ int ermod_destroy(ermod_ctx* c) {
   free_adjoint(e);
   free_intermediate(e);
   free_config_check(e);
+  free_library(e);
   dfree(e.d_ins);
   free_batch(e);
   free_frame(e);
@@ -1267,6 +1270,58 @@ static void free_config_check(Engine& e) {
   e.cfg_pos = e.cfg_str = 0;
 }
 
+static void free_library(Engine& e) {
+  dfree(e.d_lib);
+  dfree(e.d_lib_wt);
+  dfree(e.d_lib_acc);
+  e.lib_nconf = e.lib_ns = e.lib_nwt = e.lib_na = 0;
+}
+
+// getsolute (insertion.F90:384-495) for the device generator: the structure library, its
+// weights and the structures that pass insstructure's window, in file order
+int ermod_set_solute_library(ermod_ctx* c, int nconf, int nsite, const double* conf, int nweight,
+                             const double* weight, int insstructure, double lwstr, double upstr) {
+  if (!c) return fail_param("null argument");
+  Engine& e = c->e;
+  cudaSetDevice(e.device);
+  ERMOD_CUDA(cudaStreamSynchronize(e.stream));
+  if (nconf == 0) {
+    free_library(e);
+    return ERMOD_OK;
+  }
+  if (nconf < 0 || !conf) return fail_param("nconf must be >= 0 and conf not NULL");
+  if (nsite < 1 || nsite > kMaxSoluteSites) return fail_param("nsite must be 1..256");
+  if (nweight < 0 || (nweight > 0 && !weight)) return fail_param("nweight must be >= 0, weight not NULL");
+  if (insstructure != 0 && insstructure != 1) return fail_param("insstructure 0 or 1");
+  if (insstructure == 1) {
+    if (e.ref_ns == 0) return fail_param("insstructure 1 needs ermod_set_reference_structure");
+    if (nsite != e.ref_ns) {  // size(psite) /= size(refslt_crd) (insertion.F90:463-464)
+      g_err = "ins_siz: the library's structures and the reference solute differ in size";
+      return ERMOD_E_INS_SIZ;
+    }
+  }
+  free_library(e);
+  const int nwt = (weight && nweight > 0) ? nweight : 0;
+  ERMOD_CUDA(dalloc(&e.d_lib, 3 * (size_t)nsite * nconf));
+  ERMOD_CUDA(dalloc(&e.d_lib_wt, (size_t)std::max(nwt, 1)));
+  ERMOD_CUDA(dalloc(&e.d_lib_acc, (size_t)nconf + 1));
+  ERMOD_CUDA(cudaMemcpy(e.d_lib, conf, sizeof(double) * 3 * nsite * (size_t)nconf, cudaMemcpyHostToDevice));
+  if (nwt) ERMOD_CUDA(cudaMemcpy(e.d_lib_wt, weight, sizeof(double) * nwt, cudaMemcpyHostToDevice));
+  e.lib_nconf = nconf;
+  e.lib_ns = nsite;
+  e.lib_nwt = nwt;
+  ERMOD_CUDA(launch_library_filter(e, insstructure, lwstr, upstr));
+  int na = 0;
+  ERMOD_CUDA(cudaMemcpyAsync(&na, e.d_lib_acc + nconf, sizeof(int), cudaMemcpyDeviceToHost, e.stream));
+  ERMOD_CUDA(cudaStreamSynchronize(e.stream));
+  if (na <= 0) {
+    free_library(e);
+    return fail_param("no structure of the library lies in [lwstr, upstr] (getsolute would read forever)");
+  }
+  e.lib_na = na;
+  return ERMOD_OK;
+}
+
 // hostspec's aggregate and the site masses (com_aggregate, insertion.F90:539-566)
 int ermod_set_aggregate(ermod_ctx* c, const int* host_mol, const double* sitemass) {
   if (!c || !host_mol || !sitemass) return fail_param("null argument");
@@ -1588,10 +1643,16 @@ int ermod_ecorr_add_noalloc(const int* hist, const double* weight, int nplace, i
 
 int ermod_generate_placements(ermod_ctx* c, int nplace, int nsite, const double* bfcoord, const double* mass,
                               const ermod_insert_params* ip, double* sol_d, double* sws_d) {
-  if (!c || !bfcoord || !mass || !ip || (nplace > 0 && !sol_d)) return fail_param("null argument");
+  if (!c || !mass || !ip || (nplace > 0 && !sol_d)) return fail_param("null argument");
   Engine& e = c->e;
+  const bool lib = e.lib_nconf > 0;  // structures from the library (bfcoord unused)
+  if (!lib && !bfcoord) return fail_param("null bfcoord");
   if (!e.frame_ready) return fail_param("ermod_frame must come first (its cell is used)");
   if (nsite < 1 || nsite > kMaxSoluteSites) return fail_param("nsite must be 1..256");
+  if (lib && nsite != e.lib_ns) {  // size(psite) /= size(bfcoord) (insertion.F90:440)
+    g_err = "ins_siz: the library's structures and the solute differ in size";
+    return ERMOD_E_INS_SIZ;
+  }
   if (ip->insposition < 0 || ip->insposition > 6 || ip->insorient < 0 || ip->insorient > 1 || ip->insorigin < 0 ||
       ip->insorigin > 3)
     return fail_param("insposition 0..6, insorient 0..1, insorigin 0..3");
@@ -1613,7 +1674,10 @@ int ermod_generate_placements(ermod_ctx* c, int nplace, int nsite, const double*
   cudaSetDevice(e.device);
   if (!e.d_ins) ERMOD_CUDA(dalloc(&e.d_ins, 4 * (size_t)kMaxSoluteSites));
   if (ip->insorigin >= 2 && !e.d_ref_fit) ERMOD_CUDA(dalloc(&e.d_ref_fit, 6 * (size_t)kMaxSoluteSites + 8));
-  ERMOD_CUDA(cudaMemcpyAsync(e.d_ins, bfcoord, sizeof(double) * 3 * nsite, cudaMemcpyHostToDevice, e.stream));
+  if (lib)  // the origin kernel's rigid starting structure is unused; give it the first one
+    ERMOD_CUDA(cudaMemcpyAsync(e.d_ins, e.d_lib, sizeof(double) * 3 * nsite, cudaMemcpyDeviceToDevice, e.stream));
+  else
+    ERMOD_CUDA(cudaMemcpyAsync(e.d_ins, bfcoord, sizeof(double) * 3 * nsite, cudaMemcpyHostToDevice, e.stream));
   ERMOD_CUDA(cudaMemcpyAsync(e.d_ins + 3 * kMaxSoluteSites, mass, sizeof(double) * nsite, cudaMemcpyHostToDevice,
                              e.stream));
   ERMOD_CUDA(launch_insert(e, nplace, nsite, *ip, e.d_ins, e.d_ins + 3 * kMaxSoluteSites, sol_d, sws_d));

@@ -189,6 +189,12 @@ struct Engine {
   unsigned char* d_int_mask = nullptr;  // intermediate state: [ermax] zero-density bins
   double* d_edintm = nullptr;            // [ermax] edintm, [numslv] uvintm, [3] totals
   double* d_ins = nullptr;       // [4][256] solute reference coordinates and masses (placement generator)
+  // flexible solute (ermod_set_solute_library): SltConf's structures in file order, the
+  // structure weights and the accepted structures (lib_nconf 0: no library)
+  int lib_nconf = 0, lib_ns = 0, lib_nwt = 0, lib_na = 0;
+  double* d_lib = nullptr;       // [lib_nconf][lib_ns][3]
+  double* d_lib_wt = nullptr;    // [lib_nwt]
+  int* d_lib_acc = nullptr;      // [lib_nconf] accepted structures in file order, their count at [lib_nconf]
   bool tmap_ready = false;
 
   // ---- cuFFT -------------------------------------------------------------------------

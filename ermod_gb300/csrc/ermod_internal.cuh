@@ -252,6 +252,8 @@ size_t adjoint_cub_bytes(int n);
 // device placements (kernels_insert.cu)
 cudaError_t launch_insert(Engine& e, int nplace, int ns, const ermod_insert_params& ip, const double* bf_d,
                           const double* mass_d, double* out, double* weight);
+// getsolute's structure window over the library: accepted structures to e.d_lib_acc
+cudaError_t launch_library_filter(Engine& e, int insstructure, double lwstr, double upstr);
 // accumulation
 cudaError_t launch_accumulate(Engine& e, const BatchArgs& a, cudaStream_t s);
 cudaError_t launch_ecorr_flush(Engine& e, cudaStream_t s);

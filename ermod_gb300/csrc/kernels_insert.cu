@@ -22,6 +22,8 @@
 // check_solute_configuration, :569-595); as in the reference, the weight of insposition 6
 // takes the factor of every draw, rejected ones included, and the uniform / Gaussian
 // alternation advances per draw (draw d of placement g is uniform when g + d is even).
+// A flexible solute (getsolute, insertion.F90:384-495) takes placement g's structure and
+// initial weight from the structure library: the g-th accepted read of the wrapped file.
 #include "bestfit.cuh"
 #include "engine.cuh"
 
@@ -79,6 +81,12 @@ struct InsArgs {
   double* weight;      // [nplace] or null
   const double* fit;   // insorigin 2: [3] aggregate centre; 3: [ns][3] origin, [ns][3] fitted reference
   const double* rw;    // insorigin 3: [ns][4] reference solute (weights at [4 s + 3])
+  // flexible solute: structures [nconf][ns][3] (null: the rigid bf), weights [nwt] (nwt 0:
+  // 1), the na accepted structures in file order
+  const double* lib;
+  const double* lib_wt;
+  const int* lib_acc;
+  int lib_nconf, lib_nwt, lib_na;
   DevStatus* status;
 };
 
@@ -115,13 +123,36 @@ __global__ void __launch_bounds__(128) insert_kernel(InsArgs A) {
   rng.c2 = (uint32_t)g;
   rng.c3 = (uint32_t)(g >> 32);
   double* x = A.out + (size_t)p * A.ns * 3;
-  // set_solute_origin: bfcoord, or with insorigin 3 bfcoord fitted onto the reference
-  const double* x0 = (A.insorigin == 3) ? A.fit : sbf;
-  double c[3];
   double weight = 1.0;
+  const double* conf = sbf;  // bfcoord
+  if (A.lib) {
+    // getsolute: the g-th accepted read is read r = (g / na) nconf + acc[g mod na] of the
+    // wrapped structure file; the weight file, read once per structure read, wraps on its own
+    const unsigned long long na = (unsigned long long)A.lib_na;
+    const int f = A.lib_acc[g % na];
+    const unsigned long long r = (g / na) * (unsigned long long)A.lib_nconf + (unsigned long long)f;
+    conf = A.lib + (size_t)f * A.ns * 3;
+    if (A.lib_nwt > 0) weight = A.lib_wt[r % (unsigned long long)A.lib_nwt];
+  }
+  // set_solute_origin: bfcoord, or with insorigin 3 bfcoord fitted onto the reference
+  // solute in the frame (once per call for a rigid solute, per placement for a library's)
+  const bool refit = A.insorigin == 3 && A.lib;
+  double fc1[3], fc2[3], fq[4];
+  if (refit) {
+    const double* best = A.fit + 3 * (size_t)A.ns;
+    const double* rw = A.rw;
+    bestfit::fit_transform(
+        A.ns, [best](int s, int c) { return best[3 * s + c]; }, [conf](int s, int c) { return conf[3 * s + c]; },
+        [rw](int s) { return rw[4 * s + 3]; }, fc1, fc2, fq);
+  }
+  const double* x0 = (A.insorigin == 3) ? A.fit : conf;
+  double c[3];
   bool ok = true;  // every rejection loop accepted
   for (int draw = 0;; ++draw) {
-    for (int i = 0; i < 3 * A.ns; ++i) x[i] = x0[i];
+    if (refit)
+      for (int s = 0; s < A.ns; ++s) bestfit::apply_fit(fc1, fc2, fq, conf + 3 * s, x + 3 * s);
+    else
+      for (int i = 0; i < 3 * A.ns; ++i) x[i] = x0[i];
     if (A.insorigin == 0 || A.insorigin == 2) {  // set_solute_com(insml, 0 or the aggregate centre)
       com_of(x, sm, A.ns, c);
       for (int i = 0; i < 3; ++i) c[i] -= (A.insorigin == 2) ? A.fit[i] : 0.0;
@@ -344,7 +375,66 @@ __global__ void __launch_bounds__(256) insert_origin_kernel(const double* __rest
   for (int s = 0; s < ns; ++s) bestfit::apply_fit(c1, c2, q2, bf + 3 * s, fit + 3 * s);
 }
 
+// getsolute's structure rejection (insertion.F90:438-467) over the whole library, one CTA:
+// structure f passes when insstructure is 0, or when its best-fit RMSD from the reference
+// solute (rmsd_bestfit, bestfit.F90:245-252: f fitted onto refslt_crd with refslt_weight,
+// then rmsd_nofit) lies in [lw, up].  The passing structures are listed in file order in
+// acc[0 .. na), na at acc[nconf].  FP64.
+__global__ void __launch_bounds__(256) library_filter_kernel(const double* __restrict__ lib, int nconf, int ns,
+                                                             int str, double lw, double up,
+                                                             const double* __restrict__ rs, int* __restrict__ acc) {
+  __shared__ int wtot[8];
+  int base = 0;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int f0 = 0; f0 < nconf; f0 += blockDim.x) {  // the same number of rounds in every thread
+    const int f = f0 + (int)threadIdx.x;
+    int pass = 0;
+    if (f < nconf) {
+      if (str == 0) {
+        pass = 1;
+      } else {
+        const double* X = lib + (size_t)f * ns * 3;
+        double cref[3], cx[3], q[4];
+        bestfit::fit_transform(
+            ns, [rs](int s, int c) { return rs[4 * s + c]; }, [X](int s, int c) { return X[3 * s + c]; },
+            [rs](int s) { return rs[4 * s + 3]; }, cref, cx, q);
+        double W = 0.0, disp = 0.0;
+        for (int s = 0; s < ns; ++s) {
+          double o[3];
+          bestfit::apply_fit(cref, cx, q, X + 3 * s, o);
+          double d2 = 0.0;
+          for (int c = 0; c < 3; ++c) d2 += (o[c] - rs[4 * s + c]) * (o[c] - rs[4 * s + c]);
+          W += rs[4 * s + 3];
+          disp += rs[4 * s + 3] * d2;
+        }
+        const double d = sqrt(disp / W);
+        pass = (lw <= d && d <= up) ? 1 : 0;
+      }
+    }
+    // exclusive scan of pass over the block: the structure's place in the list
+    const unsigned bal = __ballot_sync(0xffffffffu, pass);
+    if (lane == 0) wtot[wid] = __popc(bal);
+    __syncthreads();
+    int off = base + __popc(bal & ((1u << lane) - 1u)), tot = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      if (w < wid) off += wtot[w];
+      tot += wtot[w];
+    }
+    if (pass) acc[off] = f;
+    base += tot;
+    __syncthreads();  // wtot free for the next round
+  }
+  if (threadIdx.x == 0) acc[nconf] = base;
+}
+
 }  // namespace
+
+cudaError_t launch_library_filter(Engine& e, int insstructure, double lwstr, double upstr) {
+  library_filter_kernel<<<1, 256, 0, e.stream>>>(e.d_lib, e.lib_nconf, e.lib_ns, insstructure, lwstr, upstr,
+                                                 e.d_ref_slt, e.d_lib_acc);
+  e.count_launch();
+  return cudaGetLastError();
+}
 
 cudaError_t launch_insert(Engine& e, int nplace, int ns, const ermod_insert_params& ip, const double* bf_d,
                           const double* mass_d, double* out, double* weight) {
@@ -365,6 +455,14 @@ cudaError_t launch_insert(Engine& e, int nplace, int ns, const ermod_insert_para
   A.out = out;
   A.weight = weight;
   A.status = e.d_status;
+  if (e.lib_nconf > 0) {
+    A.lib = e.d_lib;
+    A.lib_wt = e.d_lib_wt;
+    A.lib_acc = e.d_lib_acc;
+    A.lib_nconf = e.lib_nconf;
+    A.lib_nwt = e.lib_nwt;
+    A.lib_na = e.lib_na;
+  }
   if (ip.insorigin == 2 || ip.insorigin == 3) {
     insert_origin_kernel<<<1, 256, 0, e.stream>>>(e.d_sitepos, e.d_agg_mass, e.numatm, ip.insorigin, e.d_ref_atoms,
                                                   e.ref_nh, e.d_ref_host, e.d_ref_slt, ns, bf_d, e.d_ref_fit);

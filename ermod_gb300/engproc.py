@@ -110,6 +110,26 @@ class EnergyRepresentation:
         check(_lib.load().ermod_set_reference_structure(self.ctx, _lib.ip(rm), _lib.dp(hc), _lib.dp(hw), len(sc),
                                                         _lib.dp(sc), _lib.dp(sw)), "ermod_set_reference_structure")
 
+    def set_solute_library(self, conf, weight=None, insstructure: int = 0, lwstr: float = 0.0,
+                           upstr: float = 0.0):
+        """A flexible solute (slttype 3, getsolute in insertion.F90:384-495): SltConf's
+        structures conf (nconf, nsite, 3) in file order and SltWght's weights (or None); with
+        insstructure 1 only structures whose best-fit RMSD from the reference solute lies in
+        [lwstr, upstr] are used.  generate_placements then takes placement g's structure and
+        initial weight from the g-th accepted read of the wrapped files.  conf None removes
+        the library."""
+        if conf is None:
+            check(_lib.load().ermod_set_solute_library(self.ctx, 0, 0, None, 0, None, 0, 0.0, 0.0),
+                  "ermod_set_solute_library")
+            return
+        cf = np.ascontiguousarray(conf, np.float64)
+        if cf.ndim != 3 or cf.shape[2] != 3:
+            raise ValueError("conf must be (nconf, nsite, 3)")
+        wt = None if weight is None else np.ascontiguousarray(weight, np.float64)
+        check(_lib.load().ermod_set_solute_library(self.ctx, cf.shape[0], cf.shape[1], _lib.dp(cf),
+                                                   0 if wt is None else len(wt), _lib.dp(wt), int(insstructure),
+                                                   float(lwstr), float(upstr)), "ermod_set_solute_library")
+
     def set_configuration_check(self, insposition: int, lwreg: float = 0.0, upreg: float = 0.0,
                                 insstructure: int = 0, lwstr: float = 0.0, upstr: float = 0.0):
         """check_mol_configuration (engproc.F90:1046-1100) for solution mode: a placement whose
@@ -174,11 +194,12 @@ class EnergyRepresentation:
                             offset: int = 0, weights: bool = False):
         """n placements of a solute with reference coordinates bfcoord (nsite, 3) and masses,
         generated on the device in the cell of the last frame (insertion.F90 modes;
-        insorigin 2 needs set_aggregate, 3 set_reference_structure).  Returns torch tensors
+        insorigin 2 needs set_aggregate, 3 set_reference_structure; with a structure library
+        (set_solute_library) bfcoord is not used and may be None).  Returns torch tensors
         (placements (n, nsite, 3) float64, weights (n,) or None); a placement the RMSD
         acceptance of insorigin 3 cannot place raises ErmodError ('ins_geo')."""
         import torch
-        bf = np.ascontiguousarray(bfcoord, np.float64)
+        bf = None if bfcoord is None else np.ascontiguousarray(bfcoord, np.float64)
         m = np.ascontiguousarray(mass, np.float64)
         ns = len(m)
         dev = torch.device("cuda", self.device)

@@ -11,7 +11,8 @@ module ermod_gpu
   integer(c_int), parameter :: ERMOD_ABI_VERSION = 2
   integer(c_int), parameter :: ERMOD_OK = 0, ERMOD_E_ENG_MIN = 101, ERMOD_E_ENG_SFT = 102, &
        ERMOD_E_ENG_BUG = 103, ERMOD_E_ENG_CNS = 104, ERMOD_E_RCP_CNS = 105, ERMOD_E_RCP_FST = 106, &
-       ERMOD_E_INS_GEO = 107, ERMOD_E_SET_PRS = 108, ERMOD_E_ENG_SLB = 109, ERMOD_W_MBIN = 110
+       ERMOD_E_INS_GEO = 107, ERMOD_E_SET_PRS = 108, ERMOD_E_ENG_SLB = 109, ERMOD_W_MBIN = 110, &
+       ERMOD_E_INS_SIZ = 111
   integer(c_int), parameter :: ERMOD_PRECISION_FP64 = 0, ERMOD_PRECISION_MIXED = 1
 
   type, bind(C) :: ermod_params
@@ -66,6 +67,16 @@ module ermod_gpu
        integer(c_int), intent(in) :: ref_mol(*)
        real(c_double), intent(in) :: refhost_crd(*), refhost_weight(*), refslt_crd(*), refslt_weight(*)
        integer(c_int), value :: refslt_natom
+     end function
+     ! flexible solute (slttype 3): SltConf's structures conf(3, nsite, nconf), SltWght's
+     ! weights (nweight 0: none), getsolute's insstructure window
+     integer(c_int) function ermod_set_solute_library(ctx, nconf, nsite, conf, nweight, weight, &
+          insstructure, lwstr, upstr) bind(C, name="ermod_set_solute_library")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: nconf, nsite, nweight, insstructure
+       real(c_double), intent(in) :: conf(*), weight(*)
+       real(c_double), value :: lwstr, upstr
      end function
      integer(c_int) function ermod_set_configuration_check(ctx, insposition, lwreg, upreg, insstructure, &
           lwstr, upstr) bind(C, name="ermod_set_configuration_check")

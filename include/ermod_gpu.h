@@ -46,6 +46,7 @@ typedef enum ermod_status {
   ERMOD_E_SET_PRS = 108,   /* 'set_prs': a non-periodic system needs NVT and bare Coulomb (setconf.F90:368-372) */
   ERMOD_E_ENG_SLB = 109,   /* 'eng_slb': slab configuration check in a non-periodic system (engproc.F90:1088) */
   ERMOD_W_MBIN = 110,      /* 'mbin' warning without force_calculation (engproc.F90:1010-1015) */
+  ERMOD_E_INS_SIZ = 111,   /* 'ins_siz': solute structures of different sizes (insertion.F90:440,463-464) */
   ERMOD_E_PARAM = 120,     /* invalid argument or call order */
   ERMOD_E_NONCUBOID = 121, /* non-cuboid cell: the reference stops (realcal.F90:859-866) */
   ERMOD_E_UNSUPPORTED = 122, /* a mode the GPU path does not implement (cltype != PME) */
@@ -340,6 +341,26 @@ typedef struct ermod_insert_params {
  * ermod_placements_device. */
 int ermod_generate_placements(ermod_ctx* ctx, int nplace, int nsite, const double* bfcoord, const double* mass,
                               const ermod_insert_params* ip, double* sol_d, double* sws_d);
+
+/* ---- flexible solute (slttype 3: getsolute, insertion.F90:384-495) ------------------
+ * The structures of SltConf in file order, conf (3, nsite, nconf) host array, and the
+ * structure weights of SltWght's second column, weight[nweight] (nweight 0 or weight
+ * NULL: every structure weighs 1).  insstructure 0 takes every structure; 1 only those
+ * whose best-fit RMSD from the reference solute (rmsd_bestfit, bestfit.F90:245-252,
+ * against ermod_set_reference_structure's refslt) lies in [lwstr, upstr].  Both files
+ * wrap around on their own (setconf.F90:113-123 and insertion.F90:443-448), and a weight
+ * is read with every structure, a rejected one included.  After this call
+ * ermod_generate_placements ignores bfcoord (it may be NULL): placement g = offset + p
+ * starts from the g-th accepted read of the wrapped file, i.e. read r = (g / na) nconf +
+ * acc[g mod na] for the na accepted structures acc, with the initial weight
+ * weight[r mod nweight] (then multiplied by insposition 6's factor), as instslt's
+ * sequential reads give it; with insorigin 3 each placement fits its own structure onto
+ * the reference solute carried into the frame.  nconf 0 removes the library.
+ * ERMOD_E_INS_SIZ: nsite differs from the reference solute's (insstructure 1) or, later,
+ * from ermod_generate_placements' nsite; ERMOD_E_PARAM when no structure is accepted
+ * (the reference would read forever).  Synchronous. */
+int ermod_set_solute_library(ermod_ctx* ctx, int nconf, int nsite, const double* conf, int nweight,
+                             const double* weight, int insstructure, double lwstr, double upstr);
 
 /* ---- engstore's output files (engproc.F90:594-657), for slvfe ------------------------
  * Written from merged, normalised accumulators (ermod_engstore_merge) in the

@@ -56,13 +56,14 @@ def horn_fit(refa, a, w, b):
 
 
 def place(bf, mass, cell, p, insposition=0, insorient=0, insorigin=0, lwreg=0.0, upreg=0.0, seed=1, offset=0,
-          agg=None, start=None, refbest=None, refw=None):
+          agg=None, start=None, refbest=None, refw=None, w0=1.0):
     """Placement p.  insorigin 2: agg is the aggregate centre; insorigin 3: start is bfcoord
     fitted onto refbest, the reference solute in the frame, and a draw whose RMSD from it
-    (weights refw) lies outside [lwreg, upreg] is drawn again."""
+    (weights refw) lies outside [lwreg, upreg] is drawn again.  w0: the structure's weight
+    (a flexible solute's)."""
     g = offset + p
     rng = Stream(seed, g)
-    w = 1.0
+    w = w0
     for draw in range(1 << 16):
         x, w = _draw(rng, g + draw, bf if insorigin != 3 else start, mass, cell, insposition, insorient, insorigin,
                      lwreg, upreg, agg, w)
@@ -136,3 +137,42 @@ def _draw(rng, parity, x0, mass, cell, insposition, insorient, insorigin, lwreg,
         t = 2.0 * np.cross(u, v)
         x = v + q[0] * t + np.cross(u, t) + c
     return x, w
+
+
+def rmsd_bestfit(ref, x, w):
+    """bestfit.F90 rmsd_bestfit: x fitted onto ref (weights w), then rmsd_nofit."""
+    ref, x, w = (np.asarray(v, float) for v in (ref, x, w))
+    fitted = horn_fit(ref, x, w, x)
+    return math.sqrt(float((w * ((fitted - ref) ** 2).sum(1)).sum() / w.sum()))
+
+
+def library_accepted(conf, insstructure=0, lwstr=0.0, upstr=0.0, refslt=None, refw=None):
+    """getsolute's structure test (insertion.F90:457-470) for every structure of the library:
+    the accepted ones, in file order."""
+    if insstructure == 0:
+        return list(range(len(conf)))
+    return [f for f, x in enumerate(conf) if lwstr <= rmsd_bestfit(refslt, x, refw) <= upstr]
+
+
+def library_pick(g, nconf, acc, nwt):
+    """The g-th accepted read of the wrapped structure file: (structure, weight line) -- the
+    closed form the device uses."""
+    na = len(acc)
+    r = (g // na) * nconf + acc[g % na]
+    return acc[g % na], (r % nwt if nwt else None)
+
+
+def library_reads(n, nconf, accepted, nwt):
+    """getsolute's loop itself (insertion.F90:432-472), read by read: the structure file and the
+    weight file both wrap around, a weight is read with every structure (a rejected one too),
+    and a call returns at the first accepted structure.  The first n calls' (structure,
+    weight line)."""
+    out, r = [], 0
+    for _ in range(n):
+        while True:
+            f, wl = r % nconf, (r % nwt if nwt else None)
+            r += 1
+            if accepted[f]:
+                out.append((f, wl))
+                break
+    return out
