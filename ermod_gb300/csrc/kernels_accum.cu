@@ -503,7 +503,10 @@ __device__ __forceinline__ void ff_add_prod(float& hi, float& lo, float wh, floa
 // The rows and columns walked are the flush's active bins only (act[0 .. *nact): the bins
 // some placement of the ring occupies, in increasing order), so a coordinate of thousands
 // of bins costs what its occupied part costs; an inactive row or column has no
-// contribution, so the sums are those of the walk over every bin.
+// contribution, so the sums are those of the walk over every bin.  The matrix is
+// symmetric: only entries on or above the diagonal (column index >= row index in act) are
+// summed, and each is added at (row, column) and (column, row), so that both halves get
+// the same value from one sum.
 template <bool COUNT>
 __global__ void __launch_bounds__(256, 2) ecorr_ff_kernel(const int* __restrict__ hist, const int* __restrict__ valid,
                                                         const double* __restrict__ w, int nring, int ermax,
@@ -516,6 +519,7 @@ __global__ void __launch_bounds__(256, 2) ecorr_ff_kernel(const int* __restrict_
   const int nact = *nact_d;
   const int row0 = blockIdx.y * kEcRows;
   if (row0 >= nact) return;  // the grid covers every bin; the active ones come first
+  if ((int)(blockIdx.x * blockDim.x + blockDim.x) <= row0) return;  // all below the diagonal
   const int nrow = min(kEcRows, nact - row0);
   int rbin[kEcRows];
 #pragma unroll
@@ -542,7 +546,9 @@ __global__ void __launch_bounds__(256, 2) ecorr_ff_kernel(const int* __restrict_
     smask[p] = m;
   }
   __syncthreads();
-  if (j >= ermax) return;
+  if (j >= ermax || jj < row0) return;
+  // rows r <= jj - row0 of this column are on or above the diagonal
+  const unsigned rows_on = (jj - row0 >= kEcRows - 1) ? 0xffu : ((2u << (jj - row0)) - 1u);
   float hi[kEcRows], lo[kEcRows];
   long long cn[COUNT ? kEcRows : 1];
 #pragma unroll
@@ -565,7 +571,7 @@ __global__ void __launch_bounds__(256, 2) ecorr_ff_kernel(const int* __restrict_
       if (cj[u] == 0) continue;
       const int p = p0 + u;
       any = true;
-      const unsigned m = smask[p];
+      const unsigned m = smask[p] & rows_on;
       const float c = (float)cj[u];
       const float2* ap = sa + p * kEcRows;
 #pragma unroll
@@ -582,9 +588,16 @@ __global__ void __launch_bounds__(256, 2) ecorr_ff_kernel(const int* __restrict_
 #pragma unroll
   for (int r = 0; r < kEcRows; ++r) {
     if (r >= nrow) break;
-    const size_t at = (size_t)rbin[r] * ermax + j;
-    if (hi[r] != 0.f || lo[r] != 0.f) ecorr[at] = ecorr[at] + ((double)hi[r] + (double)lo[r]);
-    if (COUNT && cn[r] != 0) ecorr_n[at] += cn[r];
+    const size_t at = (size_t)rbin[r] * ermax + j, ta = (size_t)j * ermax + rbin[r];
+    if (hi[r] != 0.f || lo[r] != 0.f) {
+      const double v = (double)hi[r] + (double)lo[r];
+      ecorr[at] = ecorr[at] + v;
+      if (ta != at) ecorr[ta] = ecorr[ta] + v;
+    }
+    if (COUNT && cn[r] != 0) {
+      ecorr_n[at] += cn[r];
+      if (ta != at) ecorr_n[ta] += cn[r];
+    }
   }
 }
 
