@@ -7,7 +7,7 @@
 //           batch streams) -> reduce + accumulate (aux stream)
 //   [fp64]  place_prep -> spread64 -> D2Z -> influence64 -> Z2D -> mol_energy -> accumulate
 // and, when ecorr is on, a flush of the histogram ring every `ring_half` placements on
-// the aux stream while the next batches fill the ring's other half.
+// the flush stream while the next batches fill the ring's other half.
 // Status is reported once per call (host API) or per ermod_sync (device API).
 #include <cufft.h>
 
@@ -453,13 +453,14 @@ int ermod_create(const ermod_params* p_in, int device, ermod_ctx** out) {
     return fail_cuda(err, "cudaStreamCreate");
   }
   e.own_stream = true;
-  // the short kernels of the prep and aux streams (solute preparation, ordered
+  // the short kernels of the prep, aux and flush streams (solute preparation, ordered
   // accumulation, ecorr flush) take priority over the batch streams' pending blocks, so
   // the slots they free are not held up behind a whole PME launch
   int prio_lo = 0, prio_hi = 0;
   cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
   if ((err = cudaStreamCreateWithPriority(&e.aux, cudaStreamNonBlocking, prio_hi)) != cudaSuccess ||
       (err = cudaStreamCreateWithPriority(&e.prep, cudaStreamNonBlocking, prio_hi)) != cudaSuccess ||
+      (err = cudaStreamCreateWithPriority(&e.flush, cudaStreamNonBlocking, prio_hi)) != cudaSuccess ||
       (err = cudaStreamCreateWithFlags(&e.bs[0], cudaStreamNonBlocking)) != cudaSuccess ||
       (err = cudaStreamCreateWithFlags(&e.bs[1], cudaStreamNonBlocking)) != cudaSuccess) {
     ermod_destroy(c);
@@ -472,7 +473,7 @@ int ermod_create(const ermod_params* p_in, int device, ermod_ctx** out) {
   }
   cudaEventCreateWithFlags(&e.ev_flush[0], cudaEventDisableTiming);
   cudaEventCreateWithFlags(&e.ev_flush[1], cudaEventDisableTiming);
-  for (int s = 0; s < 4; ++s) cudaEventCreateWithFlags(&e.ev_join[s], cudaEventDisableTiming);
+  for (int s = 0; s < 5; ++s) cudaEventCreateWithFlags(&e.ev_join[s], cudaEventDisableTiming);
   if ((err = dalloc(&e.d_status, 1)) != cudaSuccess || (err = cudaMallocHost(&e.h_status, sizeof(DevStatus))) != cudaSuccess) {
     ermod_destroy(c);
     return fail_cuda(err, "status allocation");
@@ -547,6 +548,7 @@ int ermod_destroy(ermod_ctx* c) {
   if (e.own_stream && e.stream) cudaStreamDestroy(e.stream);
   if (e.aux) cudaStreamSynchronize(e.aux);
   if (e.prep) cudaStreamSynchronize(e.prep);
+  if (e.flush) cudaStreamSynchronize(e.flush);
   for (int s = 0; s < 2; ++s)
     if (e.bs[s]) cudaStreamSynchronize(e.bs[s]);
   for (int s = 0; s < 2; ++s) {
@@ -558,9 +560,10 @@ int ermod_destroy(ermod_ctx* c) {
     if (e.ev_flush[s]) cudaEventDestroy(e.ev_flush[s]);
   if (e.aux) cudaStreamDestroy(e.aux);
   if (e.prep) cudaStreamDestroy(e.prep);
+  if (e.flush) cudaStreamDestroy(e.flush);
   for (int s = 0; s < 2; ++s)
     if (e.bs[s]) cudaStreamDestroy(e.bs[s]);
-  for (int s = 0; s < 4; ++s)
+  for (int s = 0; s < 5; ++s)
     if (e.ev_join[s]) cudaEventDestroy(e.ev_join[s]);
   delete c;
   return ERMOD_OK;
@@ -934,8 +937,8 @@ int ermod_frame_device(ermod_ctx* c, const double* sitepos_d, const double* cell
 
 // the placement loop on device-resident inputs.  Batch i runs its kernels on the main
 // stream with the buffers of slot i%2.  Its solute preparation runs on the prep stream
-// during batch i-1; its ordered accumulation (and, every ring_half placements, the ecorr
-// flush) runs on the aux stream during batch i+1.
+// during batch i-1; its ordered accumulation runs on the aux stream during batch i+1 and,
+// every ring_half placements, the ecorr flush on the flush stream after it.
 static int run_placements(Engine& e, int nplace, const int* d_tag, const double* d_sol, const double* d_sws,
                           double* d_uv, double* d_fl, int ns_solute) {
   int st = ensure_batch(e);
@@ -1063,13 +1066,16 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
       ERMOD_CUDA(launch_adjoint(e, a, e.aux));
       e.phase_end_on(e.aux);
     }
+    ERMOD_CUDA(cudaEventRecord(e.ev_acc[slot], e.aux));
     if (e.P.corrcal) {
       e.ring_fill += nb;
       if (e.ring_fill + B > e.ring_half) {  // flush this half; the next batches fill the other
-        e.phase_begin_on(PH_ECORR, e.aux);
-        ERMOD_CUDA(launch_ecorr_flush(e, e.aux));
-        e.phase_end_on(e.aux);
-        ERMOD_CUDA(cudaEventRecord(e.ev_flush[half], e.aux));
+        // after the half's accumulations (the aux stream runs them in order)
+        ERMOD_CUDA(cudaStreamWaitEvent(e.flush, e.ev_acc[slot], 0));
+        e.phase_begin_on(PH_ECORR, e.flush);
+        ERMOD_CUDA(launch_ecorr_flush(e, e.flush));
+        e.phase_end_on(e.flush);
+        ERMOD_CUDA(cudaEventRecord(e.ev_flush[half], e.flush));
         e.flush_pend[half] = true;
         e.ring_off = e.ring_half - e.ring_off;
         e.ring_fill = 0;
@@ -1077,20 +1083,20 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
     } else {
       e.ring_off = e.ring_half - e.ring_off;  // two histogram slots, ordered by ev_acc
     }
-    ERMOD_CUDA(cudaEventRecord(e.ev_acc[slot], e.aux));
   }
   if (e.P.corrcal && e.ring_fill > 0) {
-    e.phase_begin_on(PH_ECORR, e.aux);
-    ERMOD_CUDA(launch_ecorr_flush(e, e.aux));
-    e.phase_end_on(e.aux);
+    ERMOD_CUDA(cudaStreamWaitEvent(e.flush, e.ev_acc[(nbatch - 1) & 1], 0));
+    e.phase_begin_on(PH_ECORR, e.flush);
+    ERMOD_CUDA(launch_ecorr_flush(e, e.flush));
+    e.phase_end_on(e.flush);
   }
   // the join below orders every flush before the next call's work
   e.ring_fill = 0;
   e.ring_off = 0;
   e.flush_pend[0] = e.flush_pend[1] = false;
   // join every stream back into the caller's stream, then snapshot the status
-  cudaStream_t others[4] = {e.aux, e.prep, e.bs[0], e.bs[1]};
-  for (int k = 0; k < (dual ? 4 : 2); ++k) {
+  cudaStream_t others[5] = {e.aux, e.prep, e.flush, e.bs[0], e.bs[1]};
+  for (int k = 0; k < (dual ? 5 : 3); ++k) {
     ERMOD_CUDA(cudaEventRecord(e.ev_join[k], others[k]));
     ERMOD_CUDA(cudaStreamWaitEvent(e.stream, e.ev_join[k], 0));
   }

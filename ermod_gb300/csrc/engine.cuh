@@ -31,8 +31,8 @@ struct Engine {
   std::vector<cudaEvent_t> ev_pool;
   struct Pending { cudaEvent_t a, b; int phase; };
   std::vector<Pending> pending;
-  int cur_phase[5] = {-1, -1, -1, -1, -1};  // per stream: caller's, aux, prep, batch 0/1
-  cudaEvent_t cur_ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  int cur_phase[6] = {-1, -1, -1, -1, -1, -1};  // per stream: caller's, aux, prep, batch 0/1, flush
+  cudaEvent_t cur_ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 
   // ---- topology ----------------------------------------------------------------
   int nummol = 0, numatm = 0, ljtype_max = 0, slvmax = 0, nsite_phys = 0, max_mol_sites = 0;
@@ -213,11 +213,14 @@ struct Engine {
   // third stream: the solute preparation of batch i+1 overlaps batch i's kernels
   cudaStream_t aux = nullptr;
   cudaStream_t prep = nullptr;
+  // stream of the ecorr flushes (high priority, like aux): a flush only has to end before
+  // its ring half is filled again, so the batch slots are freed without waiting for it
+  cudaStream_t flush = nullptr;
   cudaEvent_t ev_prep[2] = {nullptr, nullptr};  // preparation of the slot finished
   // mixed path: batches alternate between two streams (their PME grids and site terms
   // are double-buffered), so one batch's kernels fill the other's partial waves
   cudaStream_t bs[2] = {nullptr, nullptr};
-  cudaEvent_t ev_join[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev_join[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t ev_done[2] = {nullptr, nullptr};  // batch kernels finished (slot)
   cudaEvent_t ev_acc[2] = {nullptr, nullptr};   // accumulation of the slot finished
   cudaEvent_t ev_flush[2] = {nullptr, nullptr};  // ecorr flush of ring half 0 / 1 finished
@@ -227,7 +230,8 @@ struct Engine {
   void phase_begin_on(int ph, cudaStream_t s);
   void phase_end_on(cudaStream_t s);
   int stream_index(cudaStream_t s) const {
-    return s == aux ? 1 : (s == prep ? 2 : (s == bs[0] && s ? 3 : (s == bs[1] && s ? 4 : 0)));
+    return s == aux ? 1
+                    : (s == prep ? 2 : (s == bs[0] && s ? 3 : (s == bs[1] && s ? 4 : (s == flush && s ? 5 : 0))));
   }
   void count_launch(int n = 1) { launches += n; }
 };
