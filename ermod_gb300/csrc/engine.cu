@@ -1095,9 +1095,13 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
   e.ring_off = 0;
   e.flush_pend[0] = e.flush_pend[1] = false;
   // join every stream back into the caller's stream, then snapshot the status
-  cudaStream_t others[5] = {e.aux, e.prep, e.flush, e.bs[0], e.bs[1]};
-  for (int k = 0; k < (dual ? 5 : 3); ++k) {
-    ERMOD_CUDA(cudaEventRecord(e.ev_join[k], others[k]));
+  // (the flush stream only when ecorr is on: otherwise no work of this call reaches it,
+  // and under graph capture it would be a stream outside the capture)
+  cudaStream_t others[5] = {e.aux, e.prep, e.bs[0], e.bs[1], e.flush};
+  const int nj = (dual ? 4 : 2);
+  for (int k = 0; k < nj + (e.P.corrcal ? 1 : 0); ++k) {
+    const cudaStream_t sk = (k < nj) ? others[k] : e.flush;
+    ERMOD_CUDA(cudaEventRecord(e.ev_join[k], sk));
     ERMOD_CUDA(cudaStreamWaitEvent(e.stream, e.ev_join[k], 0));
   }
   ERMOD_CUDA(cudaMemcpyAsync(e.h_status, e.d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, e.stream));

@@ -60,6 +60,16 @@ class SystemGraph:
     def set_placements(self, i: int, solute_sitepos):
         self._pl[i].copy_(self._pl[i].new_tensor(np.ascontiguousarray(solute_sitepos, np.float64)))
 
+    def frame_buffer(self, i: int):
+        """System i's coordinate buffer on the device (the graph's input), for callers that
+        write the next frame into it themselves."""
+        return self._pos[i]
+
+    def launch_ordered(self, stream_handle: int):
+        """One step, asynchronous on stream_handle, ordered after what the caller queued on
+        that stream (its input copies included); no host wait."""
+        check(_lib.load().ermod_graph_launch(self.g, C.c_void_p(stream_handle or None)), "ermod_graph_launch")
+
     def launch(self, stream_handle: int = 0):
         """One step of every system, asynchronous on stream_handle (the input copies on
         torch's current stream are waited for first)."""

@@ -106,3 +106,46 @@ def test_tile_shapes_give_identical_results(gpu_lib):
     B, G, rates = autotune_tiles(w.params, topo, bins, (pos, cell), pl, topo["nummol"], batches=(8, 16), groups=(4, 8))
     assert (B, G) in rates and set(rates) == {(8, 4), (8, 8), (16, 4), (16, 8)}
     assert all(v > 0 for v in rates.values())
+
+
+@pytest.mark.parametrize("adjoint", [False, True])
+def test_graph_of_a_solution_mode_system(gpu_lib, adjoint):
+    """A solution-mode system (ecorr off, the in-frame solute; the benchmark's form of a
+    launch-bound step) captured alone: frame 1 as a graph launch after an ordinary frame 0
+    gives the accumulators (and the adjoint sums) of two ordinary frames, bit for bit."""
+    from ermod_gb300.engproc import EnergyRepresentation
+    from ermod_gb300.multisystem import SystemGraph
+    w = synth.soln_small(frames=3)
+    topo = setconf.setparam_topology(w.species(), slttype=1)
+    bins = setconf.enginit_bins(topo["numslv"], w.hist)
+    tag = [topo["nummol"]]
+
+    def make():
+        eng = EnergyRepresentation(w.params, topo, bins, precision="mixed")
+        if adjoint:
+            eng.adjoint_enable()
+        eng.frame(*w.frame(0))
+        eng.placements(tag)
+        return eng
+
+    ref = make()
+    ref.frame(*w.frame(1))
+    ref.placements(tag)
+    a_ref = ref.accum()
+    g_ref = ref.adjoint_get() if adjoint else None
+    ref.close()
+    eng = make()
+    g = SystemGraph([eng], [w.frame(1)], [None], tag)
+    g.launch()
+    g.sync()
+    a = eng.accum()
+    for k in ("edens", "eself", "slnuv", "minuv", "maxuv"):
+        np.testing.assert_array_equal(a[k], a_ref[k], err_msg=k)
+    for k in ("engnorm", "engsmpl", "avslf"):
+        assert a[k] == a_ref[k], k
+    if adjoint:
+        gr, wt = eng.adjoint_get()
+        np.testing.assert_array_equal(gr, g_ref[0])
+        np.testing.assert_array_equal(wt, g_ref[1])
+    g.close()
+    eng.close()
