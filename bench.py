@@ -423,8 +423,8 @@ def run_ours(args):
         dt = time.perf_counter() - t0
         eng2.close()
         h2d = frames[0][0].nbytes + (0 if soln else places[0].nbytes) + tag_h.nbytes
-        ermax = len(bins["uvcrd"])
-        d2h = (ermax * ermax + ermax + 2 * (topo["numslv"] + 1) + topo["numslv"] + 5) * 8
+        # the accumulators read back every step (ecorr only when it is on), from the arrays
+        d2h = sum(v.nbytes for v in acc.values() if isinstance(v, np.ndarray)) + 5 * 8
         e2e = {"value": nplace * w.nwater * args.steps / dt * ws, "unit": "molecule-energies/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
         del acc
