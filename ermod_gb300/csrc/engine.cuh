@@ -125,7 +125,7 @@ struct Engine {
   BatchArgs buf{};                // device buffers sized for Bmax (pointers only)
   // histogram ring for ecorr (corrcal) / per-batch histograms
   // histogram ring of the ecorr flush: two halves of ring_half entries; batches fill the
-  // half at ring_off while the aux stream flushes the other one
+  // half at ring_off while the flush stream flushes the other one
   int ring_cap = 0, ring_fill = 0, ring_half = 0, ring_off = 0;
   bool flush_pend[2] = {false, false};  // a flush of that half may still be running
   int* d_ring_hist = nullptr;     // [ring_cap][ermax]

@@ -96,7 +96,10 @@ void ermod_default_params(ermod_params* p);
 int ermod_create(const ermod_params* p, int device, ermod_ctx** out);
 int ermod_destroy(ermod_ctx* ctx);
 
-/* Optional: run all work of this context on an existing cudaStream_t. */
+/* Optional: order all work of this context on an existing cudaStream_t.  A placement call
+ * forks from it onto the context's own streams (solute preparation, two batch streams,
+ * the ordered accumulation and, with ecorr on, the flush) and joins them back into it
+ * before it returns, so the caller sees one stream. */
 int ermod_set_stream(ermod_ctx* ctx, void* cuda_stream);
 
 /* Topology (engmain.F90:252-277).  mol_begin_index has nummol+1 entries (1-based),
