@@ -253,25 +253,26 @@ static int ensure_batch(Engine& e) {
   BatchArgs& b = e.buf;
   const size_t nr = e.grid_real(), nc = e.grid_cplx();
   e.ntile = (e.slvmax + e.tile - 1) / e.tile;
-  // solute data: two batch slots (the preparation of batch i+1 runs during batch i)
-  ERMOD_CUDA(dalloc(&b.u_nsite, 2 * B));
-  ERMOD_CUDA(dalloc(&b.u_x, (size_t)2 * B * S * 3));
-  ERMOD_CUDA(dalloc(&b.u_pos, (size_t)2 * B * S));
-  ERMOD_CUDA(dalloc(&b.u_q, (size_t)2 * B * S));
-  ERMOD_CUDA(dalloc(&b.u_qf, (size_t)2 * B * S));
-  ERMOD_CUDA(dalloc(&b.u_grid, (size_t)2 * B * S));
-  ERMOD_CUDA(dalloc(&b.u_w, (size_t)2 * B * S * 3 * kMaxSplineOrder));
-  ERMOD_CUDA(dalloc(&b.u_qmol, 2 * B));
-  ERMOD_CUDA(dalloc(&b.u_usreal, 2 * B));
-  ERMOD_CUDA(dalloc(&b.u_radius, 2 * B));
-  ERMOD_CUDA(dalloc(&b.engnmfc, 2 * B));
-  ERMOD_CUDA(dalloc(&e.d_u0, 2 * B));
-  ERMOD_CUDA(dalloc(&e.d_self_bin, 2 * B));
+  // solute data: kBatchSlots batch slots (the preparation of batch i+1 runs during batch i)
+  const size_t NS = kBatchSlots;
+  ERMOD_CUDA(dalloc(&b.u_nsite, NS * B));
+  ERMOD_CUDA(dalloc(&b.u_x, NS * B * S * 3));
+  ERMOD_CUDA(dalloc(&b.u_pos, NS * B * S));
+  ERMOD_CUDA(dalloc(&b.u_q, NS * B * S));
+  ERMOD_CUDA(dalloc(&b.u_qf, NS * B * S));
+  ERMOD_CUDA(dalloc(&b.u_grid, NS * B * S));
+  ERMOD_CUDA(dalloc(&b.u_w, NS * B * S * 3 * kMaxSplineOrder));
+  ERMOD_CUDA(dalloc(&b.u_qmol, NS * B));
+  ERMOD_CUDA(dalloc(&b.u_usreal, NS * B));
+  ERMOD_CUDA(dalloc(&b.u_radius, NS * B));
+  ERMOD_CUDA(dalloc(&b.engnmfc, NS * B));
+  ERMOD_CUDA(dalloc(&e.d_u0, NS * B));
+  ERMOD_CUDA(dalloc(&e.d_self_bin, NS * B));
   if (e.mixed) {
-    ERMOD_CUDA(dalloc(&b.u_bvec, (size_t)2 * B * S * 3 * e.Kmax()));
+    ERMOD_CUDA(dalloc(&b.u_bvec, NS * B * S * 3 * e.Kmax()));
     // PME intermediate, padded potential grids and site terms: one set per batch slot
-    ERMOD_CUDA(dalloc(&e.d_site_e, (size_t)2 * e.nsite_phys * B));
-    ERMOD_CUDA(dalloc(&b.spec, 2 * nc * B));
+    ERMOD_CUDA(dalloc(&e.d_site_e, NS * e.nsite_phys * B));
+    ERMOD_CUDA(dalloc(&b.spec, NS * nc * B));
     const int h = e.P_order - 1;
     e.phi_dims[0] = ((e.geom.K[0] + h + 3) / 4) * 4;
     e.phi_dims[1] = e.geom.K[1] + h;
@@ -282,19 +283,19 @@ static int ensure_batch(Engine& e) {
     e.gbox[1] = kBrickY + h;
     e.gbox[2] = kBrickZ + h;
     const size_t np = (size_t)e.phi_dims[0] * e.phi_dims[1] * e.phi_dims[2];
-    ERMOD_CUDA(dalloc(&b.phi, 2 * np * B));
-    ERMOD_CUDA(cudaMemset(b.phi, 0, sizeof(float) * 2 * np * B));
-    for (int s = 0; s < 2; ++s) {
+    ERMOD_CUDA(dalloc(&b.phi, NS * np * B));
+    ERMOD_CUDA(cudaMemset(b.phi, 0, sizeof(float) * NS * np * B));
+    for (int s = 0; s < kBatchSlots; ++s) {
       const int st = make_phi_tmap(e, b.phi + (size_t)s * np * B, &e.phi_tmap[s]);
       if (st) return st;
     }
-    ERMOD_CUDA(dalloc(&b.self_part, (size_t)2 * B * spectrum_partials(e)));
+    ERMOD_CUDA(dalloc(&b.self_part, NS * B * spectrum_partials(e)));
   } else {
     ERMOD_CUDA(dalloc(&b.spec64, nc * B));
     ERMOD_CUDA(dalloc(&b.phi64, nr * B));
-    ERMOD_CUDA(dalloc(&b.self_part, (size_t)2 * B * influence64_blocks()));
+    ERMOD_CUDA(dalloc(&b.self_part, NS * B * influence64_blocks()));
   }
-  ERMOD_CUDA(dalloc(&b.part, (size_t)2 * B * e.ntile * e.numslv * 3));
+  ERMOD_CUDA(dalloc(&b.part, NS * B * e.ntile * e.numslv * 3));
   e.ring_half = e.P.corrcal ? std::max(2 * B, (512 / B) * B) : B;
   e.ring_cap = 2 * e.ring_half;
   e.ring_fill = 0;
@@ -466,7 +467,7 @@ int ermod_create(const ermod_params* p_in, int device, ermod_ctx** out) {
     ermod_destroy(c);
     return fail_cuda(err, "cudaStreamCreate");
   }
-  for (int s = 0; s < 2; ++s) {
+  for (int s = 0; s < kBatchSlots; ++s) {
     cudaEventCreateWithFlags(&e.ev_done[s], cudaEventDisableTiming);
     cudaEventCreateWithFlags(&e.ev_acc[s], cudaEventDisableTiming);
     cudaEventCreateWithFlags(&e.ev_prep[s], cudaEventDisableTiming);
@@ -551,7 +552,7 @@ int ermod_destroy(ermod_ctx* c) {
   if (e.flush) cudaStreamSynchronize(e.flush);
   for (int s = 0; s < 2; ++s)
     if (e.bs[s]) cudaStreamSynchronize(e.bs[s]);
-  for (int s = 0; s < 2; ++s) {
+  for (int s = 0; s < kBatchSlots; ++s) {
     if (e.ev_done[s]) cudaEventDestroy(e.ev_done[s]);
     if (e.ev_acc[s]) cudaEventDestroy(e.ev_acc[s]);
     if (e.ev_prep[s]) cudaEventDestroy(e.ev_prep[s]);
@@ -935,8 +936,8 @@ int ermod_frame_device(ermod_ctx* c, const double* sitepos_d, const double* cell
   return frame_launch(e);
 }
 
-// the placement loop on device-resident inputs.  Batch i runs its kernels on the main
-// stream with the buffers of slot i%2.  Its solute preparation runs on the prep stream
+// the placement loop on device-resident inputs.  Batch i runs its kernels on batch stream
+// i%2 with the buffers of slot i%kBatchSlots.  Its solute preparation runs on the prep stream
 // during batch i-1; its ordered accumulation runs on the aux stream during batch i+1 and,
 // every ring_half placements, the ecorr flush on the flush stream after it.
 static int run_placements(Engine& e, int nplace, const int* d_tag, const double* d_sol, const double* d_sws,
@@ -969,7 +970,7 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
     ERMOD_CUDA(cudaStreamWaitEvent(e.bs[1], e.ev_done[0], 0));
   }
   auto batch_args = [&](int ib) {
-    const int b0 = ib * B, slot = ib & 1;
+    const int b0 = ib * B, slot = ib % kBatchSlots;
     BatchArgs a = e.buf;
     a.nb = std::min(B, nplace - b0);
     a.b0 = b0;
@@ -995,7 +996,7 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
     a.u0 = e.d_u0 + (size_t)slot * B;
     a.self_bin = e.d_self_bin + (size_t)slot * B;
     a.slot = slot;
-    a.stream = dual ? e.bs[slot] : e.stream;
+    a.stream = dual ? e.bs[ib & 1] : e.stream;  // streams alternate; slots take turns
     a.phases = 1;
     a.mol_bin = e.adj_on ? e.d_mol_bin + (size_t)slot * B * e.slvmax : nullptr;
     a.skip = check ? e.d_skip + b0 : nullptr;
@@ -1008,9 +1009,9 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
     return a;
   };
   auto issue_prep = [&](int ib) -> int {
-    const int slot = ib & 1;
+    const int slot = ib % kBatchSlots;
     const BatchArgs a = batch_args(ib);
-    if (ib >= 2) ERMOD_CUDA(cudaStreamWaitEvent(e.prep, e.ev_acc[slot], 0));  // slot free again
+    if (ib >= kBatchSlots) ERMOD_CUDA(cudaStreamWaitEvent(e.prep, e.ev_acc[slot], 0));  // slot free again
     const double* sol = d_sol ? d_sol + (size_t)a.b0 * ns_solute * 3 : nullptr;
     e.phase_begin_on(PH_PREP, e.prep);
     ERMOD_CUDA(launch_place_prep(e, a, sol, e.P.slttype == 2 ? 2 : 1, e.prep));
@@ -1020,13 +1021,13 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
   };
   if (nbatch > 0 && (st = issue_prep(0)) != ERMOD_OK) return st;
   for (int ibatch = 0; ibatch < nbatch; ++ibatch) {
-    const int slot = ibatch & 1;
+    const int slot = ibatch % kBatchSlots;
     if (ibatch + 1 < nbatch && (st = issue_prep(ibatch + 1)) != ERMOD_OK) return st;
     BatchArgs a = batch_args(ibatch);
     const int nb = a.nb;
     a.hist = e.d_ring_hist + (size_t)(e.ring_off + e.ring_fill) * e.ermax;
     cudaStream_t bst = a.stream;
-    if (ibatch >= 2) ERMOD_CUDA(cudaStreamWaitEvent(bst, e.ev_acc[slot], 0));  // slot free again
+    if (ibatch >= kBatchSlots) ERMOD_CUDA(cudaStreamWaitEvent(bst, e.ev_acc[slot], 0));  // slot free again
     ERMOD_CUDA(cudaStreamWaitEvent(bst, e.ev_prep[slot], 0));
     const int half = e.ring_off ? 1 : 0;
     if (e.flush_pend[half]) {  // the first batch in this half waits for its previous flush
@@ -1085,7 +1086,7 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
     }
   }
   if (e.P.corrcal && e.ring_fill > 0) {
-    ERMOD_CUDA(cudaStreamWaitEvent(e.flush, e.ev_acc[(nbatch - 1) & 1], 0));
+    ERMOD_CUDA(cudaStreamWaitEvent(e.flush, e.ev_acc[(nbatch - 1) % kBatchSlots], 0));
     e.phase_begin_on(PH_ECORR, e.flush);
     ERMOD_CUDA(launch_ecorr_flush(e, e.flush));
     e.phase_end_on(e.flush);
@@ -1526,7 +1527,7 @@ int ermod_adjoint_enable(ermod_ctx* c, int solute_mol, int cmbrule) {
   ERMOD_CUDA(dalloc(&e.d_adj_seg, 2 * (size_t)e.ermax));
   e.adj_cub_bytes = adjoint_cub_bytes(e.slvmax);
   ERMOD_CUDA(cudaMalloc(&e.d_adj_cub, std::max<size_t>(e.adj_cub_bytes, 16)));
-  ERMOD_CUDA(dalloc(&e.d_mol_bin, 2 * (size_t)B * e.slvmax));
+  ERMOD_CUDA(dalloc(&e.d_mol_bin, (size_t)kBatchSlots * B * e.slvmax));
   ERMOD_CUDA(dalloc(&e.d_ps_nsite, (size_t)B));
   ERMOD_CUDA(dalloc(&e.d_ps_qf, (size_t)B * kMaxSoluteSites));
   ERMOD_CUDA(dalloc(&e.d_ps_bvec, (size_t)B * kMaxSoluteSites * 3 * e.Kmax()));

@@ -148,7 +148,7 @@ struct Engine {
   // ---- mixed path potential grids: padded periodic layout + TMA descriptor ----------
   int phi_dims[3] = {0, 0, 0};   // XP (multiple of 4), YP, ZP
   int gbox[3] = {0, 0, 0};       // gather box: x (multiple of 4), y, z
-  CUtensorMap phi_tmap[2];  // per slot (the type carries its alignment)
+  CUtensorMap phi_tmap[kBatchSlots];  // per slot (the type carries its alignment)
 
   // adjoint mode (mixed path): bin-resolved derivatives of the solvent molecules'
   // energies with respect to the per-site charge, LJ epsilon and LJ sigma of a solute
@@ -164,7 +164,7 @@ struct Engine {
   int* d_adj_seg = nullptr;      // [2][ermax] segment begin / end in the sorted order
   void* d_adj_cub = nullptr;
   size_t adj_cub_bytes = 0;
-  int* d_mol_bin = nullptr;      // [2][Bmax][slvmax] per-molecule bins (slot order)
+  int* d_mol_bin = nullptr;      // [kBatchSlots][Bmax][slvmax] per-molecule bins (slot order)
   // unit-charge single-site "placements" whose potentials give d u / d q_s
   int* d_ps_nsite = nullptr;     // [Bmax]
   float* d_ps_qf = nullptr;      // [Bmax][256]
@@ -216,13 +216,14 @@ struct Engine {
   // stream of the ecorr flushes (high priority, like aux): a flush only has to end before
   // its ring half is filled again, so the batch slots are freed without waiting for it
   cudaStream_t flush = nullptr;
-  cudaEvent_t ev_prep[2] = {nullptr, nullptr};  // preparation of the slot finished
+  cudaEvent_t ev_prep[kBatchSlots] = {};  // preparation of the slot finished
   // mixed path: batches alternate between two streams (their PME grids and site terms
-  // are double-buffered), so one batch's kernels fill the other's partial waves
+  // in kBatchSlots sets taken in turn), so one batch's kernels fill the other's partial
+  // waves
   cudaStream_t bs[2] = {nullptr, nullptr};
   cudaEvent_t ev_join[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-  cudaEvent_t ev_done[2] = {nullptr, nullptr};  // batch kernels finished (slot)
-  cudaEvent_t ev_acc[2] = {nullptr, nullptr};   // accumulation of the slot finished
+  cudaEvent_t ev_done[kBatchSlots] = {};  // batch kernels finished (slot)
+  cudaEvent_t ev_acc[kBatchSlots] = {};   // accumulation of the slot finished
   cudaEvent_t ev_flush[2] = {nullptr, nullptr};  // ecorr flush of ring half 0 / 1 finished
 
   void phase_begin(int ph) { phase_begin_on(ph, stream); }

@@ -27,6 +27,10 @@ namespace ermod {
 
 constexpr int kMaxSoluteSites = 256;  // sites of one solute molecule
 constexpr int kMaxSplineOrder = 8;
+// batch slots: the buffers of a batch (solute data, PME grids, site terms) in flight at
+// once; batches alternate between two streams and take the slots in turn, so a batch
+// reuses the buffers of the batch three before it, whose accumulation is long done
+constexpr int kBatchSlots = 3;
 constexpr int kMaxSpecies = 16;
 constexpr int kGridBits = 10;         // packed grid coordinates: K <= 1024 per axis
 constexpr double kPi = 3.1415926535897932;
@@ -187,7 +191,7 @@ struct BatchArgs {
   int b0;             // index of the batch's first placement within the call
   int G;              // placements per mol_energy block
   int n_u_max;        // max solute sites in the batch
-  int slot;           // batch parity: selects the double-buffered PME grids
+  int slot;           // batch slot (batch index mod kBatchSlots): selects the PME grids' set
   cudaStream_t stream;  // stream of the batch's PME, gather and finish kernels
   float* site_e;      // [nsite_phys][Bmax] reciprocal site terms of this slot (mixed)
   int phases;         // 1: the launchers split the caller's timing phase (gather/finish...)
