@@ -167,63 +167,68 @@ struct SiteArgs {
 // one thread per slot (molecule): its sites
 __global__ void frame_sites_kernel(SiteArgs A) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= A.slvmax) return;
-  const int k = A.slot_mol[m];
-  const int a0 = A.mol_atom0[k];
-  const int ns = A.mol_nsite[k];
-  const int s0 = A.slot_site[m];
-  const FrameGeom& g = A.g;
-  const int P = A.sc.order;
   double rmax = 0.0;
-  double w0[3] = {A.wrapped[3 * (size_t)a0], A.wrapped[3 * (size_t)a0 + 1], A.wrapped[3 * (size_t)a0 + 2]};
-  for (int s = 0; s < ns; ++s) {
-    const int a = a0 + s;
-    const int idx = s0 + s;
-    double w[3] = {A.wrapped[3 * (size_t)a], A.wrapped[3 * (size_t)a + 1], A.wrapped[3 * (size_t)a + 2]};
-    // radius about the first site (minimum image)
-    double r2 = 0.0;
-    for (int i = 0; i < 3; ++i) {
-      const double h = 0.5 * g.L[i];
-      const double d = h - fabs(h - fabs(w[i] - w0[i]));
-      r2 += d * d;
-    }
-    rmax = fmax(rmax, sqrt(r2));
-    // calc_spline_molecule (recpcal.F90:408-442) on the raw coordinates
-    const double xst[3] = {A.pos[3 * (size_t)a], A.pos[3 * (size_t)a + 1], A.pos[3 * (size_t)a + 2]};
-    int rci[3];
-    double tfrac[3];
-    for (int kk = 0; kk < 3; ++kk) {
-      double factor = g.invcl[kk + 0] * xst[0] + g.invcl[kk + 3] * xst[1] + g.invcl[kk + 6] * xst[2];
-      factor = factor - floor(factor);
-      const double f2 = factor * (double)g.K[kk];
-      rci[kk] = (int)f2;
-      tfrac[kk] = f2 - (double)rci[kk];
-      if (!A.mixed) {
-        for (int spi = 0; spi < P; ++spi)
-          A.site_w[((size_t)idx * 3 + kk) * P + spi] = spline_value(A.sc, f2 - (double)(rci[kk] - spi));
-      }
-    }
-    A.site_grid[idx] = rci[0] | (rci[1] << kGridBits) | (rci[2] << (2 * kGridBits));
-    const double q = A.charge[a];
-    // FP64 wrapped coordinates and charge: the FP64 path's pair terms, and the mixed
-    // path's FP64 terms of close pairs
-    A.site_x[3 * (size_t)idx + 0] = w[0];
-    A.site_x[3 * (size_t)idx + 1] = w[1];
-    A.site_x[3 * (size_t)idx + 2] = w[2];
-    A.site_q[idx] = q;
-    if (A.mixed) {
-      unsigned int X[3];
+  if (m < A.slvmax) {  // (no early return: the warp's maximum below takes every lane)
+    const int k = A.slot_mol[m];
+    const int a0 = A.mol_atom0[k];
+    const int ns = A.mol_nsite[k];
+    const int s0 = A.slot_site[m];
+    const FrameGeom& g = A.g;
+    const int P = A.sc.order;
+    double w0[3] = {A.wrapped[3 * (size_t)a0], A.wrapped[3 * (size_t)a0 + 1], A.wrapped[3 * (size_t)a0 + 2]};
+    for (int s = 0; s < ns; ++s) {
+      const int a = a0 + s;
+      const int idx = s0 + s;
+      double w[3] = {A.wrapped[3 * (size_t)a], A.wrapped[3 * (size_t)a + 1], A.wrapped[3 * (size_t)a + 2]};
+      // radius about the first site (minimum image)
+      double r2 = 0.0;
       for (int i = 0; i < 3; ++i) {
-        const double u = w[i] * g.invL[i] * 4294967296.0;
-        X[i] = (unsigned int)(unsigned long long)llrint(u);
+        const double h = 0.5 * g.L[i];
+        const double d = h - fabs(h - fabs(w[i] - w0[i]));
+        r2 += d * d;
       }
-      A.site_pos[idx] = make_int4((int)X[0], (int)X[1], (int)X[2], A.ljtype[a]);
-      A.site_rec[idx] = make_float4((float)tfrac[0], (float)tfrac[1], (float)tfrac[2], (float)q);
-    } else {
-      A.site_pos[idx] = make_int4(0, 0, 0, A.ljtype[a]);
+      rmax = fmax(rmax, sqrt(r2));
+      // calc_spline_molecule (recpcal.F90:408-442) on the raw coordinates
+      const double xst[3] = {A.pos[3 * (size_t)a], A.pos[3 * (size_t)a + 1], A.pos[3 * (size_t)a + 2]};
+      int rci[3];
+      double tfrac[3];
+      for (int kk = 0; kk < 3; ++kk) {
+        double factor = g.invcl[kk + 0] * xst[0] + g.invcl[kk + 3] * xst[1] + g.invcl[kk + 6] * xst[2];
+        factor = factor - floor(factor);
+        const double f2 = factor * (double)g.K[kk];
+        rci[kk] = (int)f2;
+        tfrac[kk] = f2 - (double)rci[kk];
+        if (!A.mixed) {
+          for (int spi = 0; spi < P; ++spi)
+            A.site_w[((size_t)idx * 3 + kk) * P + spi] = spline_value(A.sc, f2 - (double)(rci[kk] - spi));
+        }
+      }
+      A.site_grid[idx] = rci[0] | (rci[1] << kGridBits) | (rci[2] << (2 * kGridBits));
+      const double q = A.charge[a];
+      // FP64 wrapped coordinates and charge: the FP64 path's pair terms, and the mixed
+      // path's FP64 terms of close pairs
+      A.site_x[3 * (size_t)idx + 0] = w[0];
+      A.site_x[3 * (size_t)idx + 1] = w[1];
+      A.site_x[3 * (size_t)idx + 2] = w[2];
+      A.site_q[idx] = q;
+      if (A.mixed) {
+        unsigned int X[3];
+        for (int i = 0; i < 3; ++i) {
+          const double u = w[i] * g.invL[i] * 4294967296.0;
+          X[i] = (unsigned int)(unsigned long long)llrint(u);
+        }
+        A.site_pos[idx] = make_int4((int)X[0], (int)X[1], (int)X[2], A.ljtype[a]);
+        A.site_rec[idx] = make_float4((float)tfrac[0], (float)tfrac[1], (float)tfrac[2], (float)q);
+      } else {
+        A.site_pos[idx] = make_int4(0, 0, 0, A.ljtype[a]);
+      }
     }
   }
-  atomicMax((int*)&A.frame_scal[0], __float_as_int((float)rmax * 1.0001f + 1e-4f));
+  // the largest molecule radius: a warp maximum first, then one atomic per warp on this
+  // one address instead of one per molecule
+  float r = (m < A.slvmax) ? (float)rmax * 1.0001f + 1e-4f : 0.f;
+  for (int off = 16; off > 0; off >>= 1) r = fmaxf(r, __shfl_xor_sync(0xffffffffu, r, off));
+  if ((threadIdx.x & 31) == 0) atomicMax((int*)&A.frame_scal[0], __float_as_int(r));
 }
 
 // brick of every site: the kBrickX x kBrickY x kBrickZ block of PME grid points holding its
