@@ -448,6 +448,9 @@ int ermod_create(const ermod_params* p_in, int device, ermod_ctx** out) {
   // than eight on the 33,000-water workload (fewer registers, more blocks in flight)
   e.G = e.mixed ? 4 : 1;
   if (e.mixed && e.P.finish_group == 8 && e.Bmax % 8 == 0) e.G = 8;
+  int nsm = 0;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) == cudaSuccess && nsm > 0)
+    e.num_sm = nsm;
   cudaError_t err = cudaStreamCreateWithFlags(&e.stream, cudaStreamNonBlocking);
   if (err != cudaSuccess) {
     delete c;

@@ -19,6 +19,7 @@ extern const char* const kPhaseNames[PH_COUNT];
 struct Engine {
   ermod_params P{};
   int device = 0;
+  int num_sm = 152;  // the device's SM count (launch shapes of the small kernels)
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   bool mixed = true;

@@ -497,7 +497,11 @@ cudaError_t launch_frame_sites(Engine& e) {
   A.site_w = e.d_site_w;
   A.site_q = e.d_site_q;
   A.frame_scal = e.d_frame_scal;
-  frame_sites_kernel<<<nblk(e.slvmax, 128), 128, 0, e.stream>>>(A);
+  // a thread per molecule, its FP64 arithmetic on GB300's narrow FP64 pipe: small systems
+  // take warp-sized blocks, so that their molecules spread over many SMs instead of a few
+  const int sm2 = 2 * e.num_sm;  // two blocks per SM
+  const int nthr = std::min(128, std::max(32, 32 * ((e.slvmax + sm2 * 32 - 1) / (sm2 * 32))));
+  frame_sites_kernel<<<nblk(e.slvmax, nthr), nthr, 0, e.stream>>>(A);
   e.count_launch();
   return cudaGetLastError();
 }
