@@ -6,7 +6,6 @@ import re
 import subprocess
 
 import numpy as np
-import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 

@@ -9,7 +9,6 @@ import numpy as np
 import pytest
 
 from ermod_gb300 import setconf, synth
-from tests import helpers
 
 
 def _system(ljswitch, cmbrule=0):
