@@ -464,12 +464,15 @@ int ermod_create(const ermod_params* p_in, int device, ermod_ctx** out) {
   cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
   if ((err = cudaStreamCreateWithPriority(&e.aux, cudaStreamNonBlocking, prio_hi)) != cudaSuccess ||
       (err = cudaStreamCreateWithPriority(&e.prep, cudaStreamNonBlocking, prio_hi)) != cudaSuccess ||
-      (err = cudaStreamCreateWithPriority(&e.flush, cudaStreamNonBlocking, prio_hi)) != cudaSuccess ||
-      (err = cudaStreamCreateWithFlags(&e.bs[0], cudaStreamNonBlocking)) != cudaSuccess ||
-      (err = cudaStreamCreateWithFlags(&e.bs[1], cudaStreamNonBlocking)) != cudaSuccess) {
+      (err = cudaStreamCreateWithPriority(&e.flush, cudaStreamNonBlocking, prio_hi)) != cudaSuccess) {
     ermod_destroy(c);
     return fail_cuda(err, "cudaStreamCreate");
   }
+  for (int k = 0; k < kBatchStreams; ++k)
+    if ((err = cudaStreamCreateWithFlags(&e.bs[k], cudaStreamNonBlocking)) != cudaSuccess) {
+      ermod_destroy(c);
+      return fail_cuda(err, "cudaStreamCreate");
+    }
   for (int s = 0; s < kBatchSlots; ++s) {
     cudaEventCreateWithFlags(&e.ev_done[s], cudaEventDisableTiming);
     cudaEventCreateWithFlags(&e.ev_acc[s], cudaEventDisableTiming);
@@ -477,7 +480,7 @@ int ermod_create(const ermod_params* p_in, int device, ermod_ctx** out) {
   }
   cudaEventCreateWithFlags(&e.ev_flush[0], cudaEventDisableTiming);
   cudaEventCreateWithFlags(&e.ev_flush[1], cudaEventDisableTiming);
-  for (int s = 0; s < 5; ++s) cudaEventCreateWithFlags(&e.ev_join[s], cudaEventDisableTiming);
+  for (int s = 0; s < 3 + kBatchStreams; ++s) cudaEventCreateWithFlags(&e.ev_join[s], cudaEventDisableTiming);
   if ((err = dalloc(&e.d_status, 1)) != cudaSuccess || (err = cudaMallocHost(&e.h_status, sizeof(DevStatus))) != cudaSuccess) {
     ermod_destroy(c);
     return fail_cuda(err, "status allocation");
@@ -553,7 +556,7 @@ int ermod_destroy(ermod_ctx* c) {
   if (e.aux) cudaStreamSynchronize(e.aux);
   if (e.prep) cudaStreamSynchronize(e.prep);
   if (e.flush) cudaStreamSynchronize(e.flush);
-  for (int s = 0; s < 2; ++s)
+  for (int s = 0; s < kBatchStreams; ++s)
     if (e.bs[s]) cudaStreamSynchronize(e.bs[s]);
   for (int s = 0; s < kBatchSlots; ++s) {
     if (e.ev_done[s]) cudaEventDestroy(e.ev_done[s]);
@@ -565,9 +568,9 @@ int ermod_destroy(ermod_ctx* c) {
   if (e.aux) cudaStreamDestroy(e.aux);
   if (e.prep) cudaStreamDestroy(e.prep);
   if (e.flush) cudaStreamDestroy(e.flush);
-  for (int s = 0; s < 2; ++s)
+  for (int s = 0; s < kBatchStreams; ++s)
     if (e.bs[s]) cudaStreamDestroy(e.bs[s]);
-  for (int s = 0; s < 5; ++s)
+  for (int s = 0; s < 3 + kBatchStreams; ++s)
     if (e.ev_join[s]) cudaEventDestroy(e.ev_join[s]);
   delete c;
   return ERMOD_OK;
@@ -969,8 +972,7 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
   ERMOD_CUDA(cudaStreamWaitEvent(e.aux, e.ev_done[0], 0));
   ERMOD_CUDA(cudaStreamWaitEvent(e.prep, e.ev_done[0], 0));
   if (dual) {
-    ERMOD_CUDA(cudaStreamWaitEvent(e.bs[0], e.ev_done[0], 0));
-    ERMOD_CUDA(cudaStreamWaitEvent(e.bs[1], e.ev_done[0], 0));
+    for (int k = 0; k < kBatchStreams; ++k) ERMOD_CUDA(cudaStreamWaitEvent(e.bs[k], e.ev_done[0], 0));
   }
   auto batch_args = [&](int ib) {
     const int b0 = ib * B, slot = ib % kBatchSlots;
@@ -999,7 +1001,7 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
     a.u0 = e.d_u0 + (size_t)slot * B;
     a.self_bin = e.d_self_bin + (size_t)slot * B;
     a.slot = slot;
-    a.stream = dual ? e.bs[ib & 1] : e.stream;  // streams alternate; slots take turns
+    a.stream = dual ? e.bs[ib % kBatchStreams] : e.stream;  // streams and slots taken in turn
     a.phases = 1;
     a.mol_bin = e.adj_on ? e.d_mol_bin + (size_t)slot * B * e.slvmax : nullptr;
     a.skip = check ? e.d_skip + b0 : nullptr;
@@ -1101,8 +1103,9 @@ static int run_placements(Engine& e, int nplace, const int* d_tag, const double*
   // join every stream back into the caller's stream, then snapshot the status
   // (the flush stream only when ecorr is on: otherwise no work of this call reaches it,
   // and under graph capture it would be a stream outside the capture)
-  cudaStream_t others[5] = {e.aux, e.prep, e.bs[0], e.bs[1], e.flush};
-  const int nj = (dual ? 4 : 2);
+  cudaStream_t others[2 + kBatchStreams] = {e.aux, e.prep};
+  for (int k = 0; k < kBatchStreams; ++k) others[2 + k] = e.bs[k];
+  const int nj = (dual ? 2 + kBatchStreams : 2);
   for (int k = 0; k < nj + (e.P.corrcal ? 1 : 0); ++k) {
     const cudaStream_t sk = (k < nj) ? others[k] : e.flush;
     ERMOD_CUDA(cudaEventRecord(e.ev_join[k], sk));

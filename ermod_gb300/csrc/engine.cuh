@@ -32,8 +32,10 @@ struct Engine {
   std::vector<cudaEvent_t> ev_pool;
   struct Pending { cudaEvent_t a, b; int phase; };
   std::vector<Pending> pending;
-  int cur_phase[6] = {-1, -1, -1, -1, -1, -1};  // per stream: caller's, aux, prep, batch 0/1, flush
-  cudaEvent_t cur_ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  // per stream: caller's, aux, prep, flush, the batch streams
+  static_assert(4 + kBatchStreams <= 8, "phase slots per stream");
+  int cur_phase[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
+  cudaEvent_t cur_ev[8] = {};
 
   // ---- topology ----------------------------------------------------------------
   int nummol = 0, numatm = 0, ljtype_max = 0, slvmax = 0, nsite_phys = 0, max_mol_sites = 0;
@@ -221,8 +223,8 @@ struct Engine {
   // mixed path: batches alternate between two streams (their PME grids and site terms
   // in kBatchSlots sets taken in turn), so one batch's kernels fill the other's partial
   // waves
-  cudaStream_t bs[2] = {nullptr, nullptr};
-  cudaEvent_t ev_join[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  cudaStream_t bs[kBatchStreams] = {};
+  cudaEvent_t ev_join[3 + kBatchStreams] = {};
   cudaEvent_t ev_done[kBatchSlots] = {};  // batch kernels finished (slot)
   cudaEvent_t ev_acc[kBatchSlots] = {};   // accumulation of the slot finished
   cudaEvent_t ev_flush[2] = {nullptr, nullptr};  // ecorr flush of ring half 0 / 1 finished
@@ -232,8 +234,13 @@ struct Engine {
   void phase_begin_on(int ph, cudaStream_t s);
   void phase_end_on(cudaStream_t s);
   int stream_index(cudaStream_t s) const {
-    return s == aux ? 1
-                    : (s == prep ? 2 : (s == bs[0] && s ? 3 : (s == bs[1] && s ? 4 : (s == flush && s ? 5 : 0))));
+    if (!s) return 0;
+    if (s == aux) return 1;
+    if (s == prep) return 2;
+    if (s == flush) return 3;
+    for (int k = 0; k < kBatchStreams; ++k)
+      if (s == bs[k]) return 4 + k;
+    return 0;
   }
   void count_launch(int n = 1) { launches += n; }
 };

@@ -31,6 +31,10 @@ constexpr int kMaxSplineOrder = 8;
 // once; batches alternate between two streams and take the slots in turn, so a batch
 // reuses the buffers of the batch three before it, whose accumulation is long done
 constexpr int kBatchSlots = 3;
+// batch streams: batches take them in turn (batch i: stream i mod 2).  A third one was
+// measured: +0.5% on the 96^3 workload and -2.4% at 48^3, with each kernel's in-pipeline
+// launch time half as long again (it shares the SMs with two other batches)
+constexpr int kBatchStreams = 2;
 constexpr int kMaxSpecies = 16;
 constexpr int kGridBits = 10;         // packed grid coordinates: K <= 1024 per axis
 constexpr double kPi = 3.1415926535897932;
