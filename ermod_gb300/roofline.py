@@ -22,8 +22,8 @@ from __future__ import annotations
 # intermediate does not stay in L2, so these are close to the launch's full traffic;
 # a launch of B placements moves about B times these bytes.
 MEASURED_TRAFFIC_REFS_LARGE = {
-    "spectrum": (8.5e6 + 866.0e6) / 256,  # pme_a: writes the half spectrum after the k3 transform
-    "fft_c2r": (944.0e6 + 956.7e6) / 256,  # pme_b: reads it, writes the padded potential grid
+    "spectrum": (8.3e6 + 865.7e6) / 256,  # pme_a: writes the half spectrum after the k3 transform
+    "fft_c2r": (944.1e6 + 956.7e6) / 256,  # pme_b: reads it, writes the padded potential grid
     "gather": (1022.9e6 + 96.5e6) / 256,  # gather_tma: reads the grid (halo boxes) and site data
 }
 
@@ -31,10 +31,10 @@ MEASURED_TRAFFIC_REFS_LARGE = {
 # peak as ncu reports it) and its duration launched alone (us, one 256-placement launch,
 # serialised and cold, so slower than inside the pipelined step).
 MEASURED_PIPES_REFS_LARGE = {
-    "spectrum": {"kernel": "pme_a_kernel<96>", "issue_active_pct": 65.0, "fma_pipe_pct": 41.5,
-                 "alu_pipe_pct": 22.1, "fp64_pipe_pct": 0.5, "dram_pct": 15.0, "standalone_us": 736.3},
-    "fft_c2r": {"kernel": "pme_b_kernel<96>", "issue_active_pct": 45.5, "fma_pipe_pct": 21.8,
-                "alu_pipe_pct": 26.0, "fp64_pipe_pct": 0.0, "dram_pct": 34.3, "standalone_us": 698.0},
+    "spectrum": {"kernel": "pme_a_kernel<96>", "issue_active_pct": 62.7, "fma_pipe_pct": 40.8,
+                 "alu_pipe_pct": 21.1, "fp64_pipe_pct": 0.5, "dram_pct": 15.3, "standalone_us": 720.9},
+    "fft_c2r": {"kernel": "pme_b_kernel<96>", "issue_active_pct": 44.9, "fma_pipe_pct": 22.1,
+                "alu_pipe_pct": 25.5, "fp64_pipe_pct": 0.0, "dram_pct": 34.8, "standalone_us": 688.9},
     "gather": {"kernel": "gather_tma_kernel<4>", "issue_active_pct": 28.2, "fma_pipe_pct": 18.3,
                "alu_pipe_pct": 4.7, "fp64_pipe_pct": 0.0, "dram_pct": 32.2, "standalone_us": 438.8},
 }
