@@ -413,20 +413,21 @@ static_assert(kR1 == 4, "pme_a reads a tile row's engfac values as one float4");
 // per SM, so the k3 transform runs over two halves of the columns through a work buffer
 // of half the slab's columns (and the site staging takes smaller chunks to fit in it).
 constexpr int pme_a_hp(int KC) { return ((KC / 2 + 1 + kR1 - 1) / kR1) * kR1; }
-// CTA size of the compile-time PME kernels.  Small grids (K < 64) have too few transform
-// columns and generation tiles to keep 512 threads busy: their CTAs take 256 threads, four
-// to an SM.  From 64 up a CTA takes one thread per generation tile (kR3 x kR1 points),
-// rounded up to whole warps and capped at 512, and as many CTAs per SM as its registers
-// allow at 64 per thread: at 96^3, 416 threads for the 13 x 32 tiles (measured +0.8% on the
-// 33,000-water workload against 512, every transform pass but the last in one round).
+// CTA size of the compile-time PME kernels: one thread per generation tile (kR3 x kR1
+// points), rounded up to whole warps and capped at 512, and as many CTAs per SM as its
+// registers allow at 64 per thread.  Small grids have few transform columns and tiles, so
+// their CTAs are small and many share an SM; at 96^3, 416 threads for the 13 x 32 tiles
+// (measured +0.8% on the 33,000-water workload against 512, every transform pass but the
+// last in one round).
 constexpr int pme_tiles(int KC) { return (pme_a_hp(KC) / kR1) * ((KC + kR3 - 1) / kR3); }
 constexpr int pme_threads(int KC) {
-  return KC == 0 ? 512 : KC < 64 ? 256 : (((pme_tiles(KC) + 31) / 32) * 32 > 512 ? 512 : ((pme_tiles(KC) + 31) / 32) * 32);
+  return KC == 0 ? 512 : (((pme_tiles(KC) + 31) / 32) * 32 > 512 ? 512 : ((pme_tiles(KC) + 31) / 32) * 32);
 }
 constexpr int pme_min_blocks(int KC) {
-  return (KC > 0 && KC < 64) ? 4 : pme_threads(KC) <= 256 ? 4 : pme_threads(KC) <= 320 ? 3 : 2;
+  return 65536 / (pme_threads(KC) * 64) > 16 ? 16 : 65536 / (pme_threads(KC) * 64);
 }
-static_assert(pme_threads(96) == 416 && pme_threads(80) == 320 && pme_threads(128) == 512, "CTA sizes");
+static_assert(pme_threads(96) == 416 && pme_threads(80) == 320 && pme_threads(128) == 512 && pme_threads(32) == 64,
+              "CTA sizes");
 
 constexpr bool pme_a_halves(int KC) {  // cubic grids with compile-time sizes (KC > 0)
   return KC > 0 && two_pass(KC) && sizeof(float2) * ((size_t)2 * KC * pme_a_hp(KC) + KC) > 110 * 1024;
